@@ -1,0 +1,389 @@
+"""GB300-native coupled DEM-SPH step - Python binding of the C ABI.
+
+The product is ``libdemsph_gb300.so`` (CUDA kernels for sm_103a plus the host
+API, include/demsph_gb300.h).  This module is a thin ctypes layer over it so
+Python code (tests, benchmarks, notebooks) can build a scene with the
+reference's setup calls and drive the step:
+
+    import dem_sphsource_gb300 as ds
+    b = ds.Builder()
+    b.setDomain(...); b.addFluid(...); ...          # the reference's dataBase calls
+    eng = ds.Engine(b.scene())                       # DeviceData::copy + buildDeviceData
+    eng.initialize()                                 # neighborSearch(0,1), bonds, normals
+    eng.update(dt, first_step=1, n_steps=100, gap=1) # 100 x solverBase::update()
+    pos, vel, acc, drho = eng.download_fluids()
+
+There is no CPU fallback: if the library is missing or no sm_103a GPU is
+present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdemsph_gb300.so")
+
+DEMSPH_OK = 0
+DEMSPH_ERR_CAPACITY = 5
+FIX_WALL_LOOP = 1
+FIX_CLUMP_ROTATION = 2
+
+_D = C.c_double
+_I = C.c_int
+_P = C.c_void_p
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int)
+
+
+class Scene(C.Structure):
+    """ctypes mirror of ``demsph_scene`` (include/demsph_gb300.h)."""
+
+    _fields_ = [
+        ("domain_origin", _D * 3), ("domain_size", _D * 3), ("gravity", _D * 3), ("time_step", _D),
+        ("fluid_integrate_gap", _I), ("maximum_time", _D), ("num_frames", _I),
+        ("n_fluid", _I), ("fluid_position", _DP), ("fluid_velocity", _DP), ("fluid_acceleration", _DP),
+        ("fluid_smoothing_length", _DP), ("fluid_rho0", _DP), ("fluid_drho", _DP), ("fluid_sound_speed", _DP),
+        ("fluid_nu", _DP),
+        ("n_solid", _I), ("solid_position", _DP), ("solid_velocity", _DP), ("solid_acceleration", _DP),
+        ("solid_normal", _DP), ("solid_torque", _DP), ("solid_angular_velocity", _DP),
+        ("solid_effective_radius", _DP), ("solid_radius", _DP), ("solid_inverse_mass", _DP),
+        ("solid_material", _IP), ("solid_cluster", _IP), ("solid_clump", _IP), ("solid_is_dummy", _IP),
+        ("n_clump", _I), ("clump_centroid", _DP), ("clump_velocity", _DP), ("clump_acceleration", _DP),
+        ("clump_angular_velocity", _DP), ("clump_torque", _DP), ("clump_orientation", _DP),
+        ("clump_inverse_inertia", _DP), ("clump_inverse_mass", _DP), ("clump_pebble_start", _IP),
+        ("clump_pebble_end", _IP),
+        ("n_wall", _I), ("wall_point", _DP), ("wall_normal", _DP), ("wall_material", _IP),
+        ("n_material", _I), ("hertzian", _DP), ("linear", _DP), ("bonded", _DP),
+    ]
+
+
+class Options(C.Structure):
+    """ctypes mirror of ``demsph_options``."""
+
+    _fields_ = [("device", _I), ("fluid_neighbors_max", _I), ("fluid_solids_max", _I),
+                ("solid_contacts_per_particle", _I), ("fixes", _I), ("debug", _I)]
+
+
+class Counts(C.Structure):
+    _fields_ = [("fluid_pairs", C.c_longlong), ("fluid_solid_pairs", C.c_longlong), ("solid_pairs", C.c_longlong),
+                ("bonds", C.c_longlong), ("bonds_intact", C.c_longlong), ("grid_cells", _I), ("grid_size", _I * 3),
+                ("cell_size", _D * 3)]
+
+
+class DemSphError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+_lib = None
+
+
+def library_available():
+    return os.path.exists(LIB_PATH)
+
+
+def load_library():
+    """Loads libdemsph_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build() "
+                           "(dem-sphsource_gb300/build.py); there is no CPU fallback")
+    lib = C.CDLL(LIB_PATH)
+    lib.demsph_status_string.restype = C.c_char_p
+    lib.demsph_last_error.restype = C.c_char_p
+    lib.demsph_last_error.argtypes = [_P]
+    lib.demsph_version.restype = C.c_char_p
+    lib.demsph_builder_new.restype = _P
+    lib.demsph_builder_last_error.restype = C.c_char_p
+    lib.demsph_builder_last_error.argtypes = [_P]
+    for name in dir(lib):
+        pass
+    _lib = lib
+    return lib
+
+
+def _ptr(a, t=_DP):
+    return a.ctypes.data_as(t)
+
+
+def _v3(v):
+    return (_D * 3)(*map(float, v))
+
+
+class Builder:
+    """The reference's setup API (class dataBase, core/dataBase.h:33-219) over
+    the C ABI scene builder.  Method names and arguments are the reference's."""
+
+    def __init__(self, n_material=10):
+        self.lib = load_library()
+        self.h = self.lib.demsph_builder_new(_I(n_material))
+        if not self.h:
+            raise DemSphError(1, "demsph_builder_new failed")
+        self._keep = []
+
+    def __del__(self):
+        try:
+            self.lib.demsph_builder_free(_P(self.h))
+        except Exception:
+            pass
+
+    def _chk(self, rc, what):
+        if rc != DEMSPH_OK:
+            msg = self.lib.demsph_builder_last_error(_P(self.h)).decode()
+            raise DemSphError(rc, f"{what}: {msg}")
+
+    def setDomain(self, o, s):
+        self._chk(self.lib.demsph_builder_set_domain(_P(self.h), _v3(o), _v3(s)), "setDomain")
+
+    def setGravity(self, g):
+        self._chk(self.lib.demsph_builder_set_gravity(_P(self.h), _v3(g)), "setGravity")
+
+    def setSimulationParameterTimeStep(self, dt):
+        self._chk(self.lib.demsph_builder_set_time_step(_P(self.h), _D(dt)), "setSimulationParameterTimeStep")
+
+    def setSimulationParameterMaximumTime(self, t):
+        self._chk(self.lib.demsph_builder_set_maximum_time(_P(self.h), _D(t)), "setSimulationParameterMaximumTime")
+
+    def setSimulationParameterNumFrames(self, n):
+        self._chk(self.lib.demsph_builder_set_num_frames(_P(self.h), _I(n)), "setSimulationParameterNumFrames")
+
+    def setFluidIntegrateGap(self, g):
+        self._chk(self.lib.demsph_builder_set_fluid_integrate_gap(_P(self.h), _I(g)), "setFluidIntegrateGap")
+
+    def setHertzianContactModel(self, mi, mj, *v):
+        self._chk(self.lib.demsph_builder_set_hertzian(_P(self.h), _I(mi), _I(mj), *map(_D, v)),
+                  "setHertzianContactModel")
+
+    def setLinearContactModel(self, mi, mj, *v):
+        self._chk(self.lib.demsph_builder_set_linear(_P(self.h), _I(mi), _I(mj), *map(_D, v)),
+                  "setLinearContactModel")
+
+    def setBondedContactModel(self, mi, mj, *v):
+        self._chk(self.lib.demsph_builder_set_bonded(_P(self.h), _I(mi), _I(mj), *map(_D, v)),
+                  "setBondedContactModel")
+
+    def addFluid(self, p, v, sl, rho, c, nu):
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+        self._chk(self.lib.demsph_builder_add_fluid(_P(self.h), _I(len(p)), _ptr(p), _v3(v), _D(sl), _D(rho), _D(c),
+                                                    _D(nu)), "addFluid")
+
+    def addDummyParticleWall(self, p, spacing):
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+        self._chk(self.lib.demsph_builder_add_dummy_wall(_P(self.h), _I(len(p)), _ptr(p), _D(spacing)),
+                  "addDummyParticleWall")
+
+    def addSolid(self, p, v, r, rho, mat):
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+        self._chk(self.lib.demsph_builder_add_solid(_P(self.h), _I(len(p)), _ptr(p), _v3(v), _D(r), _D(rho),
+                                                    _I(mat)), "addSolid")
+
+    def addInfiniteWall(self, p, n, mat):
+        self._chk(self.lib.demsph_builder_add_infinite_wall(_P(self.h), _v3(p), _v3(n), _I(mat)), "addInfiniteWall")
+
+    def addCylinderWall(self, p, axis, w, r, mat):
+        self._chk(self.lib.demsph_builder_add_cylinder_wall(_P(self.h), _v3(p), _v3(axis), _v3(w), _D(r), _I(mat)),
+                  "addCylinderWall")
+
+    def addCluster(self, p, r, rho, v, mat):
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        self._chk(self.lib.demsph_builder_add_cluster(_P(self.h), _I(len(p)), _ptr(p), _ptr(r), _ptr(rho), _v3(v),
+                                                      _I(mat)), "addCluster")
+
+    def addClump(self, p, r, c, v, w, mass, I6, mat):
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        I6 = (_D * 6)(*map(float, I6))
+        self._chk(self.lib.demsph_builder_add_clump(_P(self.h), _I(len(p)), _ptr(p), _ptr(r), _v3(c), _v3(v), _v3(w),
+                                                    _D(mass), I6, _I(mat)), "addClump")
+
+    def scene(self):
+        """The C view of the builder's arrays (valid while the builder lives and is unchanged)."""
+        s = Scene()
+        self._chk(self.lib.demsph_builder_scene(_P(self.h), C.byref(s)), "scene")
+        s._builder = self  # keep the arrays alive
+        return s
+
+
+def build_scene(recipe, n_material=10):
+    """Replays a scenes.Recipe on a new Builder; returns (builder, scene)."""
+    b = Builder(n_material)
+    recipe.apply(b)
+    return b, b.scene()
+
+
+class Engine:
+    """One scene on one GPU (the C ABI engine)."""
+
+    def __init__(self, scene, device=0, fluid_neighbors_max=0, fluid_solids_max=0, solid_contacts_per_particle=0,
+                 fixes=0, debug=0):
+        self.lib = load_library()
+        self.scene = scene
+        opts = Options(device, fluid_neighbors_max, fluid_solids_max, solid_contacts_per_particle, fixes, debug)
+        h = _P()
+        rc = self.lib.demsph_create(C.byref(scene), C.byref(opts), C.byref(h))
+        self.h = h
+        if rc != DEMSPH_OK:
+            msg = self.lib.demsph_last_error(h).decode() if h else ""
+            if h:
+                self.lib.demsph_destroy(h)
+                self.h = None
+            raise DemSphError(rc, f"demsph_create: {msg}")
+        self.nf, self.ns, self.nc = scene.n_fluid, scene.n_solid, scene.n_clump
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.demsph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc, what):
+        if rc != DEMSPH_OK:
+            msg = self.lib.demsph_last_error(self.h).decode()
+            raise DemSphError(rc, f"{what}: {msg}")
+
+    # ---- life cycle and the five stages ----
+    def initialize(self):
+        self._chk(self.lib.demsph_initialize(self.h), "demsph_initialize")
+
+    def neighbor_search(self, i_step, gap):
+        self._chk(self.lib.demsph_neighbor_search(self.h, _I(i_step), _I(gap)), "demsph_neighbor_search")
+
+    def solid_integrate_before_contact(self, dt):
+        self._chk(self.lib.demsph_solid_integrate_before_contact(self.h, _D(dt)), "before_contact")
+
+    def fluid_integrate(self, dt, i_step, gap):
+        self._chk(self.lib.demsph_fluid_integrate(self.h, _D(dt), _I(i_step), _I(gap)), "fluid_integrate")
+
+    def solid_contact_after_fluid_integrate(self, dt):
+        self._chk(self.lib.demsph_solid_contact_after_fluid_integrate(self.h, _D(dt)), "contact")
+
+    def solid_integrate_after_contact(self, dt):
+        self._chk(self.lib.demsph_solid_integrate_after_contact(self.h, _D(dt)), "after_contact")
+
+    def step(self, dt, i_step, gap):
+        """One solverBase::update() through the five stage calls."""
+        self.neighbor_search(i_step, gap)
+        self.solid_integrate_before_contact(dt)
+        self.fluid_integrate(dt, i_step, gap)
+        self.solid_contact_after_fluid_integrate(dt)
+        self.solid_integrate_after_contact(dt)
+
+    def update(self, dt, first_step, n_steps, gap, use_graph=True):
+        self._chk(self.lib.demsph_update(self.h, _D(dt), _I(first_step), _I(n_steps), _I(gap), _I(1 if use_graph else 0)),
+                  "demsph_update")
+
+    def synchronize(self):
+        self._chk(self.lib.demsph_synchronize(self.h), "demsph_synchronize")
+
+    # ---- state ----
+    def download_fluids(self):
+        n = self.nf
+        pos, vel, acc, drho = (np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n))
+        self._chk(self.lib.demsph_download_fluids(self.h, _ptr(pos), _ptr(vel), _ptr(acc), _ptr(drho)),
+                  "download_fluids")
+        return pos, vel, acc, drho
+
+    def download_solids(self):
+        n = self.ns
+        out = [np.zeros((n, 3)) for _ in range(6)]
+        self._chk(self.lib.demsph_download_solids(self.h, *[_ptr(a) for a in out]), "download_solids")
+        return dict(zip(("pos", "vel", "acc", "normal", "torque", "angvel"), out))
+
+    def download_clumps(self):
+        n = self.nc
+        out = [np.zeros((n, 3)) for _ in range(5)] + [np.zeros((n, 4))]
+        self._chk(self.lib.demsph_download_clumps(self.h, *[_ptr(a) for a in out]), "download_clumps")
+        return dict(zip(("centroid", "vel", "acc", "angvel", "torque", "orientation"), out))
+
+    def upload_fluids(self, pos=None, vel=None, drho=None):
+        a = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (pos, vel, drho)]
+        self._chk(self.lib.demsph_upload_fluids(self.h, *[None if x is None else _ptr(x) for x in a]), "upload_fluids")
+
+    def upload_solids(self, pos=None, vel=None, angvel=None):
+        a = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (pos, vel, angvel)]
+        self._chk(self.lib.demsph_upload_solids(self.h, *[None if x is None else _ptr(x) for x in a]), "upload_solids")
+
+    def set_gravity(self, g):
+        self._chk(self.lib.demsph_set_gravity(self.h, _v3(g)), "set_gravity")
+
+    def set_clump_velocity(self, c, v):
+        self._chk(self.lib.demsph_set_clump_velocity(self.h, _I(c), _v3(v)), "set_clump_velocity")
+
+    def add_external_force(self, i, f):
+        self._chk(self.lib.demsph_add_external_force(self.h, _I(i), _v3(f)), "add_external_force")
+
+    def add_global_damping(self, i, cd):
+        self._chk(self.lib.demsph_add_global_damping(self.h, _I(i), _D(cd)), "add_global_damping")
+
+    # ---- artefacts in the reference's index space ----
+    def counts(self):
+        c = Counts()
+        self._chk(self.lib.demsph_get_counts(self.h, C.byref(c)), "get_counts")
+        return c
+
+    def cell_hash(self, which):
+        n = self.nf if which == 0 else self.ns
+        ng = self.counts().grid_cells
+        value, index = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        start, end = np.zeros(ng, np.int32), np.zeros(ng, np.int32)
+        self._chk(self.lib.demsph_export_cell_hash(self.h, _I(which), _ptr(value, _IP), _ptr(index, _IP),
+                                                   _ptr(start, _IP), _ptr(end, _IP)), "export_cell_hash")
+        return {"value": value, "index": index, "start": start, "end": end}
+
+    def fluid_pairs(self):
+        prefix = np.zeros(self.nf, np.int32)
+        self._chk(self.lib.demsph_export_fluid_pairs(self.h, _ptr(prefix, _IP), None, None, C.c_longlong(0)), "ff")
+        m = int(prefix[-1]) if self.nf else 0
+        a, b = np.zeros(m, np.int32), np.zeros(m, np.int32)
+        self._chk(self.lib.demsph_export_fluid_pairs(self.h, _ptr(prefix, _IP), _ptr(a, _IP), _ptr(b, _IP),
+                                                     C.c_longlong(m)), "ff")
+        return {"prefix": prefix, "pointed": a, "pointing": b}
+
+    def fluid_solid_pairs(self):
+        prefix = np.zeros(self.nf, np.int32)
+        self._chk(self.lib.demsph_export_fluid_solid_pairs(self.h, _ptr(prefix, _IP), None, None, None,
+                                                           C.c_longlong(0)), "fs")
+        m = int(prefix[-1]) if self.nf else 0
+        a, b, f = np.zeros(m, np.int32), np.zeros(m, np.int32), np.zeros((m, 3))
+        self._chk(self.lib.demsph_export_fluid_solid_pairs(self.h, _ptr(prefix, _IP), _ptr(a, _IP), _ptr(b, _IP),
+                                                           _ptr(f), C.c_longlong(m)), "fs")
+        return {"prefix": prefix, "pointed": a, "pointing": b, "force": f}
+
+    def solid_pairs(self):
+        prefix = np.zeros(self.ns, np.int32)
+        self._chk(self.lib.demsph_export_solid_pairs(self.h, _ptr(prefix, _IP), *([None] * 7), C.c_longlong(0)), "ss")
+        m = int(prefix[-1]) if self.ns else 0
+        a, b = np.zeros(m, np.int32), np.zeros(m, np.int32)
+        F, T, S, R, Q = (np.zeros((m, 3)) for _ in range(5))
+        self._chk(self.lib.demsph_export_solid_pairs(self.h, _ptr(prefix, _IP), _ptr(a, _IP), _ptr(b, _IP), _ptr(F),
+                                                     _ptr(T), _ptr(S), _ptr(R), _ptr(Q), C.c_longlong(m)), "ss")
+        return {"prefix": prefix, "pointed": a, "pointing": b, "force": F, "torque": T, "sliding": S, "rolling": R,
+                "torsion": Q}
+
+    def bonds(self):
+        m = self.counts().bonds
+        a, b, on = np.zeros(m, np.int32), np.zeros(m, np.int32), np.zeros(m, np.int32)
+        fn, tt = np.zeros(m), np.zeros(m)
+        fs, tb, n, p = (np.zeros((m, 3)) for _ in range(4))
+        self._chk(self.lib.demsph_export_bonds(self.h, _ptr(a, _IP), _ptr(b, _IP), _ptr(on, _IP), _ptr(fn), _ptr(tt),
+                                               _ptr(fs), _ptr(tb), _ptr(n), _ptr(p), C.c_longlong(m)), "bonds")
+        return {"pointed": a, "pointing": b, "isBonded": on, "normalForce": fn, "torsionTorque": tt,
+                "shearForce": fs, "bendingTorque": tb, "contactNormal": n, "contactPoint": p}
+
+    def sumw0(self):
+        out = np.zeros(self.nf)
+        self._chk(self.lib.demsph_export_fluid_sumw0(self.h, _ptr(out)), "sumw0")
+        return out

@@ -1,0 +1,754 @@
+// Engine life cycle, step schedule, CUDA-graph batching and overflow
+// recovery - the step half of the C ABI in include/demsph_gb300.h.
+//
+// Step schedule (solverBase::update, core/solverBase.cpp:47-67):
+//   neighborSearch -> solidIntegrateBeforeContact -> fluidIntegrate ->
+//   calSolidContactAfterFluidIntegrate -> [driver hook] -> solidIntegrateAfterContact
+// with the reference's cadences: fluid lists and the fluid step every `gap`
+// DEM steps, Shepard re-initialisation at i % (5 gap) == 0 and at i == 1, the
+// coupling force every DEM step.
+//
+// Buffers keep fixed roles inside a step (fluid state in set [0] between
+// steps; set [1] holds the mid-step copy), except the solid contact list,
+// whose two parities alternate every build (the previous list is the spring
+// history).  A CUDA graph therefore captures one period of steps - a multiple
+// of 2 and of 5 gap - and is replayed; steps that do not fill a whole period
+// run uncaptured.
+//
+// Overflow: list kernels record an overflow in a status word and every later
+// kernel returns at once, so a failed step leaves the state as it was after
+// the previous step (re-hashing and re-ordering are idempotent).  The host
+// grows the list and re-runs from the first incomplete step.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine_impl.cuh"
+
+namespace demsph {
+
+void freeOne(demsph_engine* e, void*& p)
+{
+    if (!p) return;
+    auto it = std::find(e->owned.begin(), e->owned.end(), p);
+    if (it != e->owned.end()) e->owned.erase(it);
+    cudaFree(p);
+    p = nullptr;
+}
+
+void dropGraph(demsph_engine* e)
+{
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+    e->graphPeriod = 0;
+}
+
+double* scratchDoubles(demsph_engine* e, size_t n)
+{
+    if (n > e->dscratchN) {
+        void* p = e->dscratch;
+        freeOne(e, p);
+        e->dscratch = dalloc<double>(n, e->owned, false);
+        e->dscratchN = n;
+    }
+    return e->dscratch;
+}
+
+// Cell and double-float offset of an absolute FP64 position.  The cell is the
+// reference's hashing cell int((p - min) / cs) (core/neighborSearch.h:44-49),
+// which is the floor inside the domain; outside it the floor is kept (the
+// stencil centre applies the truncation).
+void splitPosition(const DeviceState& d, double3 p, int4& c, float4& h, float4& l)
+{
+    const double q[3] = {p.x, p.y, p.z};
+    int ci[3];
+    float hi[3], lo[3];
+    for (int a = 0; a < 3; ++a) {
+        const double u = (q[a] - d.minB[a]) / d.cs[a];
+        const int k = u >= 0 ? (int)u : (int)std::floor(u);
+        const double o = q[a] - (d.minB[a] + (double)k * d.cs[a]);
+        ci[a] = k;
+        const dfl s = df_from_double(o);
+        hi[a] = s.hi;
+        lo[a] = s.lo;
+    }
+    c = make_int4(ci[0], ci[1], ci[2], 0);
+    h.x = hi[0]; h.y = hi[1]; h.z = hi[2];
+    l.x = lo[0]; l.y = lo[1]; l.z = lo[2];
+}
+
+int readStatus(demsph_engine* e, int* stepsDone)
+{
+    int st[2] = {0, 0};
+    CK(cudaMemcpyAsync(&st[0], e->d.status, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaMemcpyAsync(&st[1], e->d.stepsDone, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    if (stepsDone) *stepsDone = st[1];
+    return st[0];
+}
+
+}  // namespace demsph
+
+using namespace demsph;
+
+namespace {
+
+inline double3 v3(const double* p, int i)
+{
+    return p ? make_double3(p[3 * i], p[3 * i + 1], p[3 * i + 2]) : make_double3(0, 0, 0);
+}
+
+int checkDevice(demsph_engine* e, int dev)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return fail(e, DEMSPH_ERR_NO_DEVICE, "no CUDA device");
+    if (dev < 0 || dev >= n) return fail(e, DEMSPH_ERR_ARGUMENT, "device index out of range");
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return fail(e, DEMSPH_ERR_NO_DEVICE, "cannot query device");
+    if (p.major * 10 + p.minor != 103)
+        return fail(e, DEMSPH_ERR_NO_DEVICE, "this library is built for sm_103a (GB300); the device is sm_" +
+                                                 std::to_string(p.major * 10 + p.minor));
+    return DEMSPH_OK;
+}
+
+void allocFluidLists(demsph_engine* e)
+{
+    DeviceState& d = e->d;
+    d.ff = dalloc<unsigned>((size_t)d.kff * d.nf, e->owned, false);
+    d.fs = dalloc<int>((size_t)d.kfs * d.nf, e->owned, false);
+    if (e->debug & 1) d.fsPairForce = dalloc<float4>((size_t)d.kfs * d.nf, e->owned);
+}
+
+void allocContactLists(demsph_engine* e)
+{
+    DeviceState& d = e->d;
+    const size_t c = (size_t)d.ssCap;
+    d.spa = dalloc<int>(c, e->owned);
+    d.srpartner = dalloc<int>(c, e->owned);
+    d.pF = dalloc<float4>(c, e->owned);
+    d.pT = dalloc<float4>(c, e->owned);
+    d.pTA = dalloc<float4>(c, e->owned);
+    d.pTB = dalloc<float4>(c, e->owned);
+    for (int p = 0; p < 2; ++p) {
+        d.spb[p] = dalloc<int>(c, e->owned);
+        for (int k = 0; k < 3; ++k) d.spring[p][k] = dalloc<float4>(c, e->owned);
+    }
+}
+
+// ---- the five stages ----
+void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
+{
+    DeviceState& d = e->d;
+    const cudaStream_t s = e->stream;
+    const bool fluidStep = d.nf > 0 && (iStep % gap == 0);
+    if (fluidStep) launchFluidHashReorder(d, s);
+    launchSolidHashSort(d, s);
+    if (fluidStep) {
+        launchFluidLists(d, s);
+        launchCouplingLists(d, s);
+    }
+    e->par ^= 1;
+    launchSolidContactList(d, e->par, s);
+}
+
+void stageBefore(demsph_engine* e, double dt) { launchSolidIntegrate(e->d, dt, true, e->stream); }
+
+void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
+{
+    DeviceState& d = e->d;
+    const cudaStream_t s = e->stream;
+    const double dtf = dt * (double)gap;
+    const bool fluidStep = iStep % gap == 0;
+    if (d.nf > 0 && (iStep % (5 * gap) == 0 || iStep == 1)) launchDensityReinit(d, iStep, s);
+    if (fluidStep) launchContinuityPass(d, 0, dtf, s);
+    launchCoupling(d, fluidStep ? 1 : 0, s);
+    if (d.fsPairForce) launchCouplingPairForces(d, fluidStep ? 1 : 0, d.fsPairForce, s);
+    if (fluidStep) {
+        launchMomentumPass(d, dtf, s);
+        launchContinuityPass(d, 1, dtf, s);
+    }
+}
+
+void stageContact(demsph_engine* e, double dt)
+{
+    DeviceState& d = e->d;
+    launchPairContacts(d, e->par, (float)dt, e->stream);
+    launchBonds(d, e->par, (float)dt, e->stream);
+    launchGatherWalls(d, e->par, (float)dt, e->stream);
+    launchClumpForce(d, e->stream);
+}
+
+void stageAfter(demsph_engine* e, double dt) { launchSolidIntegrate(e->d, dt, false, e->stream); }
+
+void fullStep(demsph_engine* e, double dt, int iStep, int gap)
+{
+    stageNeighborSearch(e, iStep, gap);
+    stageBefore(e, dt);
+    stageFluid(e, dt, iStep, gap);
+    stageContact(e, dt);
+    stageAfter(e, dt);
+    launchStepDone(e->d, e->stream);
+}
+
+// Grows whatever overflowed and clears the status.  e->par must be the parity
+// of the last successful solid list build (the history the retry reads).
+void grow(demsph_engine* e, int status)
+{
+    DeviceState& d = e->d;
+    CK(cudaStreamSynchronize(e->stream));
+    if (status & (ST_FF_OVERFLOW | ST_FS_OVERFLOW)) {
+        void* p = d.ff;
+        freeOne(e, p);
+        p = d.fs;
+        freeOne(e, p);
+        if (d.fsPairForce) {
+            p = d.fsPairForce;
+            freeOne(e, p);
+            d.fsPairForce = nullptr;
+        }
+        if (status & ST_FF_OVERFLOW) d.kff *= 2;
+        if (status & ST_FS_OVERFLOW) d.kfs *= 2;
+        allocFluidLists(e);
+    }
+    if (status & ST_SS_OVERFLOW) {
+        const int keep = e->par, failed = e->par ^ 1;
+        int need[2] = {0, 0};
+        CK(cudaMemcpy(&need[0], d.sfbase[failed] + d.ns, sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&need[1], d.srbase + d.ns, sizeof(int), cudaMemcpyDeviceToHost));
+        // keep the spring history (the last successful list) across the reallocation
+        const int old = d.ssCap;
+        std::vector<int> pb(old);
+        std::vector<float4> sp[3];
+        CK(cudaMemcpy(pb.data(), d.spb[keep], sizeof(int) * old, cudaMemcpyDeviceToHost));
+        for (int k = 0; k < 3; ++k) {
+            sp[k].resize(old);
+            CK(cudaMemcpy(sp[k].data(), d.spring[keep][k], sizeof(float4) * old, cudaMemcpyDeviceToHost));
+        }
+        void* ptrs[] = {d.spa, d.srpartner, d.pF, d.pT, d.pTA, d.pTB, d.spb[0], d.spb[1], d.spring[0][0],
+                        d.spring[0][1], d.spring[0][2], d.spring[1][0], d.spring[1][1], d.spring[1][2]};
+        for (void* p : ptrs) freeOne(e, p);
+        d.ssCap = (int)std::min<long long>(2000000000LL, (long long)(std::max(need[0], need[1]) * 1.5) + 1024);
+        allocContactLists(e);
+        CK(cudaMemcpy(d.spb[keep], pb.data(), sizeof(int) * old, cudaMemcpyHostToDevice));
+        for (int k = 0; k < 3; ++k)
+            CK(cudaMemcpy(d.spring[keep][k], sp[k].data(), sizeof(float4) * old, cudaMemcpyHostToDevice));
+    }
+    if (status & ST_COUPLE_OVERFLOW) {
+        int need = 0;
+        CK(cudaMemcpy(&need, d.coupStart + d.ns, sizeof(int), cudaMemcpyDeviceToHost));
+        void* p = d.coupList;
+        freeOne(e, p);
+        d.coupCap = (int)std::min<long long>(2000000000LL, (long long)(need * 1.5) + 1024);
+        d.coupList = dalloc<int>(d.coupCap, e->owned);
+    }
+    CK(cudaMemset(d.status, 0, sizeof(int)));
+    dropGraph(e);
+}
+
+constexpr int ALL_OVERFLOWS = ST_FF_OVERFLOW | ST_FS_OVERFLOW | ST_SS_OVERFLOW | ST_COUPLE_OVERFLOW;
+
+// Neighbour search of the staged API: synchronises once, grows and retries.
+int neighborSearchChecked(demsph_engine* e, int iStep, int gap)
+{
+    for (int attempt = 0; attempt < 16; ++attempt) {
+        const int parBefore = e->par;
+        stageNeighborSearch(e, iStep, gap);
+        const int st = readStatus(e);
+        if (st == 0) return DEMSPH_OK;
+        e->par = parBefore;
+        if (st & ~ALL_OVERFLOWS) return fail(e, DEMSPH_ERR_STATE, "unexpected device status " + std::to_string(st));
+        grow(e, st);
+    }
+    return fail(e, DEMSPH_ERR_CAPACITY, "list overflow persists after growing");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* demsph_status_string(int s)
+{
+    switch (s) {
+    case DEMSPH_OK: return "ok";
+    case DEMSPH_ERR_ARGUMENT: return "invalid argument";
+    case DEMSPH_ERR_STATE: return "call out of order";
+    case DEMSPH_ERR_CUDA: return "CUDA error";
+    case DEMSPH_ERR_NO_DEVICE: return "no usable CUDA device";
+    case DEMSPH_ERR_CAPACITY: return "list capacity exceeded";
+    case DEMSPH_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case DEMSPH_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+    }
+}
+
+const char* demsph_last_error(const demsph_engine* e) { return e ? e->err.c_str() : ""; }
+const char* demsph_version(void) { return "demsph_gb300 0.1 (sm_103a)"; }
+
+int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engine** out)
+{
+    if (!sc || !out) return DEMSPH_ERR_ARGUMENT;
+    *out = nullptr;
+    if (sc->n_fluid < 0 || sc->n_solid < 0 || sc->n_clump < 0 || sc->n_wall < 0 || sc->n_material < 1)
+        return DEMSPH_ERR_ARGUMENT;
+    demsph_options o{};
+    if (opt) o = *opt;
+    demsph_engine* e = new demsph_engine();
+    e->debug = o.debug;
+    int rc = checkDevice(e, o.device);
+    if (rc != DEMSPH_OK) {
+        *out = e;  // keep the message readable
+        return rc;
+    }
+    try {
+        e->device = o.device;
+        CK(cudaSetDevice(o.device));
+        CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+        DeviceState& d = e->d;
+        d.fixes = o.fixes;
+        d.nf = sc->n_fluid;
+        d.ns = sc->n_solid;
+        d.nc = sc->n_clump;
+        d.nw = sc->n_wall;
+        d.kff = o.fluid_neighbors_max > 0 ? o.fluid_neighbors_max : 160;
+        d.kfs = o.fluid_solids_max > 0 ? o.fluid_solids_max : 96;
+        const int perParticle = o.solid_contacts_per_particle > 0 ? o.solid_contacts_per_particle : 16;
+
+        // ---- grid: dataBase::setSpatialGrids (core/dataBase.cpp:415-432) ----
+        double mf = 0, ms = 0;
+        for (int i = 0; i < d.nf; ++i) mf = std::max(mf, sc->fluid_smoothing_length[i]);
+        for (int i = 0; i < d.ns; ++i) ms = std::max(ms, sc->solid_effective_radius[i]);
+        e->hmax = mf;
+        const double cell = 2 * std::max(mf, ms);
+        int g[3];
+        for (int a = 0; a < 3; ++a) {
+            const double L = sc->domain_size[a];
+            g[a] = L > cell ? int(L / cell) : 1;
+            d.minB[a] = sc->domain_origin[a];
+            d.cs[a] = L / double(g[a]);
+        }
+        const long long ncell = (long long)g[0] * g[1] * g[2] + 1;
+        if (ncell > 1500000000LL) throw CudaError{cudaErrorMemoryAllocation, "grid has too many cells"};
+        d.grid.gx = g[0];
+        d.grid.gy = g[1];
+        d.grid.gz = g[2];
+        d.grid.num = (int)ncell;
+        d.grid.csx = df_from_double(d.cs[0]);
+        d.grid.csy = df_from_double(d.cs[1]);
+        d.grid.csz = df_from_double(d.cs[2]);
+        d.grid.cs = make_float3((float)d.cs[0], (float)d.cs[1], (float)d.cs[2]);
+        for (int a = 0; a < 3; ++a) d.g64[a] = sc->gravity[a];
+        d.g = make_float3((float)sc->gravity[0], (float)sc->gravity[1], (float)sc->gravity[2]);
+
+        // ---- contact tables ----
+        const int nslot = sc->n_material * (sc->n_material + 1) / 2;
+        e->hzF.assign(sc->hertzian, sc->hertzian + 8 * nslot);
+        e->lnF.assign(sc->linear, sc->linear + 11 * nslot);
+        e->bdF.assign(sc->bonded, sc->bonded + 6 * nslot);
+        e->dampF.resize(nslot);
+        for (int k = 0; k < nslot; ++k) {
+            const double lr = std::log(sc->hertzian[8 * k + 2]);
+            e->dampF[k] = (float)(-lr / std::sqrt(lr * lr + 3.1415926535897931 * 3.1415926535897931));
+        }
+        float* tab = dalloc<float>(26 * nslot, e->owned);
+        CK(cudaMemcpy(tab, e->hzF.data(), sizeof(float) * 8 * nslot, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(tab + 8 * nslot, e->lnF.data(), sizeof(float) * 11 * nslot, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(tab + 19 * nslot, e->bdF.data(), sizeof(float) * 6 * nslot, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(tab + 25 * nslot, e->dampF.data(), sizeof(float) * nslot, cudaMemcpyHostToDevice));
+        d.tab.nMat = sc->n_material;
+        d.tab.hz = tab;
+        d.tab.ln = tab + 8 * nslot;
+        d.tab.bd = tab + 19 * nslot;
+        d.tab.damp = tab + 25 * nslot;
+
+        d.status = dalloc<int>(1, e->owned);
+        d.stepsDone = dalloc<int>(1, e->owned);
+        size_t wk = std::max({scanWorkspaceInts(d.grid.num), scanWorkspaceInts(std::max(1, d.ns)),
+                              scanWorkspaceInts(std::max(1, d.nf))});
+        d.scanWork = dalloc<int>(wk, e->owned);
+
+        // ---- fluid ----
+        const int nf = d.nf;
+        {
+            std::vector<int4> cell(nf);
+            std::vector<float4> ph(nf), pl(nf), vh(nf), vl(nf), acc(nf), par(nf);
+            std::vector<float> drho(nf);
+            std::vector<int> id(nf);
+            for (int i = 0; i < nf; ++i) {
+                splitPosition(d, v3(sc->fluid_position, i), cell[i], ph[i], pl[i]);
+                const dfl h = df_from_double(sc->fluid_smoothing_length[i]);
+                ph[i].w = h.hi;
+                pl[i].w = h.lo;
+                const double3 v = v3(sc->fluid_velocity, i);
+                const dfl vx = df_from_double(v.x), vy = df_from_double(v.y), vz = df_from_double(v.z);
+                vh[i] = make_float4(vx.hi, vy.hi, vz.hi, 0.f);
+                vl[i] = make_float4(vx.lo, vy.lo, vz.lo, 0.f);
+                const double3 a = v3(sc->fluid_acceleration, i);
+                acc[i] = make_float4((float)a.x, (float)a.y, (float)a.z, 0.f);
+                const double rho0 = sc->fluid_rho0[i];
+                const double m = std::pow(sc->fluid_smoothing_length[i] / 1.3, 3) * rho0;
+                par[i] = make_float4((float)rho0, (float)sc->fluid_sound_speed[i], (float)sc->fluid_nu[i], (float)m);
+                drho[i] = sc->fluid_drho ? (float)sc->fluid_drho[i] : 0.f;
+                id[i] = i;
+            }
+            d.fcell = dalloc<int4>(nf, e->owned);
+            for (int b = 0; b < 2; ++b) {
+                d.fph[b] = dalloc<float4>(nf, e->owned);
+                d.fpl[b] = dalloc<float4>(nf, e->owned);
+                d.fvh[b] = dalloc<float4>(nf, e->owned);
+                d.fvl[b] = dalloc<float4>(nf, e->owned);
+                d.fdrho[b] = dalloc<float>(nf, e->owned);
+            }
+            d.facc = dalloc<float4>(nf, e->owned);
+            d.fpar = dalloc<float4>(nf, e->owned);
+            d.fsumW0 = dalloc<float>(nf, e->owned);
+            d.fid = dalloc<int>(nf, e->owned);
+            d.fslot = dalloc<int>(nf, e->owned);
+            d.tcell = dalloc<int4>(nf, e->owned);
+            d.tacc = dalloc<float4>(nf, e->owned);
+            d.tpar = dalloc<float4>(nf, e->owned);
+            d.tsumW0 = dalloc<float>(nf, e->owned);
+            d.tid = dalloc<int>(nf, e->owned);
+            d.fkey = dalloc<int>(nf, e->owned);
+            d.fslotInCell = dalloc<int>(nf, e->owned);
+            d.fsortTmp = dalloc<int>(nf, e->owned);
+            d.fcellCount = dalloc<int>(d.grid.num, e->owned);
+            d.fcellStart = dalloc<int>((size_t)d.grid.num + 1, e->owned);
+            d.ffc = dalloc<int>(nf, e->owned);
+            d.fsc = dalloc<int>(nf, e->owned);
+            allocFluidLists(e);
+            if (nf > 0) {
+                CK(cudaMemcpy(d.fcell, cell.data(), sizeof(int4) * nf, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.fph[0], ph.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.fpl[0], pl.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.fvh[0], vh.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.fvl[0], vl.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.fdrho[0], drho.data(), sizeof(float) * nf, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.facc, acc.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.fpar, par.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.fid, id.data(), sizeof(int) * nf, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.fslot, id.data(), sizeof(int) * nf, cudaMemcpyHostToDevice));
+            }
+        }
+
+        // ---- solids ----
+        const int ns = d.ns;
+        {
+            std::vector<int4> cell(ns), flags(ns);
+            std::vector<float4> ph(ns), pl(ns), vh(ns), vl(ns), wh(ns), wl(ns), acc(ns), tq(ns), nrm(ns), rad(ns);
+            for (int i = 0; i < ns; ++i) {
+                splitPosition(d, v3(sc->solid_position, i), cell[i], ph[i], pl[i]);
+                const double im = sc->solid_inverse_mass[i];
+                ph[i].w = (float)im;
+                pl[i].w = 0.f;
+                auto put = [&](const double* src, float4& hi, float4& lo) {
+                    const double3 v = v3(src, i);
+                    const dfl x = df_from_double(v.x), y = df_from_double(v.y), z = df_from_double(v.z);
+                    hi = make_float4(x.hi, y.hi, z.hi, 0.f);
+                    lo = make_float4(x.lo, y.lo, z.lo, 0.f);
+                };
+                put(sc->solid_velocity, vh[i], vl[i]);
+                put(sc->solid_angular_velocity, wh[i], wl[i]);
+                const double3 a = v3(sc->solid_acceleration, i), t = v3(sc->solid_torque, i), n = v3(sc->solid_normal, i);
+                acc[i] = make_float4((float)a.x, (float)a.y, (float)a.z, 0.f);
+                tq[i] = make_float4((float)t.x, (float)t.y, (float)t.z, 0.f);
+                nrm[i] = make_float4((float)n.x, (float)n.y, (float)n.z, 0.f);
+                const dfl r = df_from_double(sc->solid_radius[i]), ef = df_from_double(sc->solid_effective_radius[i]);
+                rad[i] = make_float4(r.hi, r.lo, ef.hi, ef.lo);
+                int bits = 0;
+                if (sc->solid_is_dummy[i] == 1) bits |= F_DUMMY;
+                if (im < 1.e-10) bits |= F_FIXED;
+                if (im > 1.e-10) bits |= F_MASSIVE;
+                if (im > 0.) bits |= F_HASMASS;
+                if (im > 0.) e->nMassive++;
+                flags[i] = make_int4(sc->solid_material[i], sc->solid_cluster[i], sc->solid_clump[i], bits);
+            }
+            d.scell = dalloc<int4>(ns, e->owned);
+            d.sph = dalloc<float4>(ns, e->owned);
+            d.spl = dalloc<float4>(ns, e->owned);
+            d.svh = dalloc<float4>(ns, e->owned);
+            d.svl = dalloc<float4>(ns, e->owned);
+            d.swh = dalloc<float4>(ns, e->owned);
+            d.swl = dalloc<float4>(ns, e->owned);
+            d.sacc = dalloc<float4>(ns, e->owned);
+            d.storque = dalloc<float4>(ns, e->owned);
+            d.snormal = dalloc<float4>(ns, e->owned);
+            d.sfcoup = dalloc<float4>(ns, e->owned);
+            d.srad = dalloc<float4>(ns, e->owned);
+            d.sflags = dalloc<int4>(ns, e->owned);
+            d.skey = dalloc<int>(ns, e->owned);
+            d.sslotInCell = dalloc<int>(ns, e->owned);
+            d.ssorted = dalloc<int>(ns, e->owned);
+            d.ssortTmp = dalloc<int>(ns, e->owned);
+            d.scellCount = dalloc<int>(d.grid.num, e->owned);
+            d.scellStart = dalloc<int>((size_t)d.grid.num + 1, e->owned);
+            d.sfcnt = dalloc<int>(ns, e->owned);
+            d.srcnt = dalloc<int>(ns, e->owned);
+            d.sfbase[0] = dalloc<int>((size_t)ns + 1, e->owned);
+            d.sfbase[1] = dalloc<int>((size_t)ns + 1, e->owned);
+            d.srbase = dalloc<int>((size_t)ns + 1, e->owned);
+            d.ssCap = std::max(1024, perParticle * ns);
+            allocContactLists(e);
+            d.coupCount = dalloc<int>(ns, e->owned);
+            d.coupStart = dalloc<int>((size_t)ns + 1, e->owned);
+            d.coupCap = std::max(1024, std::min(64 * e->nMassive + 1024, std::max(1, d.kfs * nf)));
+            d.coupList = dalloc<int>(d.coupCap, e->owned);
+            if (ns > 0) {
+                CK(cudaMemcpy(d.scell, cell.data(), sizeof(int4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.sph, ph.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.spl, pl.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.svh, vh.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.svl, vl.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.swh, wh.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.swl, wl.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.sacc, acc.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.storque, tq.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.snormal, nrm.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.srad, rad.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.sflags, flags.data(), sizeof(int4) * ns, cudaMemcpyHostToDevice));
+            }
+        }
+
+        // ---- walls ----
+        {
+            const int nw = d.nw;
+            std::vector<float4> nh(nw), nl(nw);
+            std::vector<float2> P(nw);
+            std::vector<int> mat(nw);
+            for (int k = 0; k < nw; ++k) {
+                const double3 p = v3(sc->wall_point, k), n = v3(sc->wall_normal, k);
+                const dfl x = df_from_double(n.x), y = df_from_double(n.y), z = df_from_double(n.z);
+                nh[k] = make_float4(x.hi, y.hi, z.hi, 0.f);
+                nl[k] = make_float4(x.lo, y.lo, z.lo, 0.f);
+                const dfl pp = df_from_double((p.x - d.minB[0]) * n.x + (p.y - d.minB[1]) * n.y + (p.z - d.minB[2]) * n.z);
+                P[k] = make_float2(pp.hi, pp.lo);
+                mat[k] = sc->wall_material[k];
+            }
+            d.wnh = dalloc<float4>(nw, e->owned);
+            d.wnl = dalloc<float4>(nw, e->owned);
+            d.wP = dalloc<float2>(nw, e->owned);
+            d.wmat = dalloc<int>(nw, e->owned);
+            for (int k = 0; k < 3; ++k) d.wspring[k] = dalloc<float4>((size_t)ns * nw, e->owned);
+            if (nw > 0) {
+                CK(cudaMemcpy(d.wnh, nh.data(), sizeof(float4) * nw, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.wnl, nl.data(), sizeof(float4) * nw, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.wP, P.data(), sizeof(float2) * nw, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.wmat, mat.data(), sizeof(int) * nw, cudaMemcpyHostToDevice));
+            }
+        }
+
+        // ---- clumps ----
+        {
+            const int nc = d.nc;
+            d.cpos = dalloc<double3>(nc, e->owned);
+            d.cvel = dalloc<double3>(nc, e->owned);
+            d.cacc = dalloc<double3>(nc, e->owned);
+            d.cw = dalloc<double3>(nc, e->owned);
+            d.ctorque = dalloc<double3>(nc, e->owned);
+            d.cq = dalloc<double4>(nc, e->owned);
+            d.cinvI = dalloc<double>(6 * (size_t)nc, e->owned);
+            d.cinvm = dalloc<double>(nc, e->owned);
+            d.cstart = dalloc<int>(nc, e->owned);
+            d.cend = dalloc<int>(nc, e->owned);
+            if (nc > 0) {
+                CK(cudaMemcpy(d.cpos, sc->clump_centroid, sizeof(double3) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cvel, sc->clump_velocity, sizeof(double3) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cacc, sc->clump_acceleration, sizeof(double3) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cw, sc->clump_angular_velocity, sizeof(double3) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.ctorque, sc->clump_torque, sizeof(double3) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cq, sc->clump_orientation, sizeof(double4) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cinvI, sc->clump_inverse_inertia, sizeof(double) * 6 * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cinvm, sc->clump_inverse_mass, sizeof(double) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cstart, sc->clump_pebble_start, sizeof(int) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cend, sc->clump_pebble_end, sizeof(int) * nc, cudaMemcpyHostToDevice));
+            }
+        }
+        CK(cudaDeviceSynchronize());
+    } catch (const CudaError& c) {
+        rc = cudaFail(e, c);
+        *out = e;
+        return rc;
+    }
+    *out = e;
+    return DEMSPH_OK;
+}
+
+
+int demsph_destroy(demsph_engine* e)
+{
+    if (!e) return DEMSPH_ERR_ARGUMENT;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    delete e;
+    return DEMSPH_OK;
+}
+
+int demsph_initialize(demsph_engine* e)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    const int rc = neighborSearchChecked(e, 0, 1);
+    if (rc != DEMSPH_OK) return rc;
+    // bonds between touching spheres of one cluster
+    int np = 0;
+    if (d.ns > 0) CK(cudaMemcpy(&np, d.sfbase[e->par] + d.ns, sizeof(int), cudaMemcpyDeviceToHost));
+    np = std::min(np, d.ssCap);
+    if (np > 0) {
+        std::vector<void*> tmp;
+        int* flag = dalloc<int>((size_t)np + 1, tmp);
+        int* pos = dalloc<int>((size_t)np + 1, tmp);
+        int* work = dalloc<int>(scanWorkspaceInts(np), tmp);
+        const int nb = launchBondFlags(d, e->par, np, flag, pos, work, e->stream);
+        if (nb > 0) {
+            d.nb = nb;
+            d.bab = dalloc<int2>(nb, e->owned);
+            d.bon = dalloc<int>(nb, e->owned);
+            d.bFnTt = dalloc<float4>(nb, e->owned);
+            d.bFsH = dalloc<float4>(nb, e->owned);
+            d.bFsL = dalloc<float4>(nb, e->owned);
+            d.bTbH = dalloc<float4>(nb, e->owned);
+            d.bTbL = dalloc<float4>(nb, e->owned);
+            d.bN = dalloc<float4>(nb, e->owned);
+            d.bLever = dalloc<float4>(nb, e->owned);
+            launchBondWrite(d, e->par, np, flag, pos, e->stream);
+        }
+        CK(cudaStreamSynchronize(e->stream));
+        for (void* p : tmp) cudaFree(p);
+    }
+    // normals of walls and clump pebbles (setSolidNormal), kernel length = largest fluid h
+    const dfl h = df_from_double(e->hmax);
+    launchSolidNormals(d, h.hi, h.lo, e->stream);
+    CK(cudaStreamSynchronize(e->stream));
+    CK(cudaGetLastError());
+    e->initialized = true;
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+#define REQUIRE_INIT(e) \
+    if (!(e)->initialized) return fail((e), DEMSPH_ERR_STATE, "demsph_initialize has not been called")
+
+int demsph_neighbor_search(demsph_engine* e, int i_step, int gap)
+{
+    if (gap < 1) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    REQUIRE_INIT(e);
+    return neighborSearchChecked(e, i_step, gap);
+    ENGINE_END(e)
+}
+
+int demsph_solid_integrate_before_contact(demsph_engine* e, double dt)
+{
+    ENGINE_GUARD(e)
+    REQUIRE_INIT(e);
+    stageBefore(e, dt);
+    CK(cudaGetLastError());
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_fluid_integrate(demsph_engine* e, double dt, int i_step, int gap)
+{
+    if (gap < 1) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    REQUIRE_INIT(e);
+    stageFluid(e, dt, i_step, gap);
+    CK(cudaGetLastError());
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_solid_contact_after_fluid_integrate(demsph_engine* e, double dt)
+{
+    ENGINE_GUARD(e)
+    REQUIRE_INIT(e);
+    stageContact(e, dt);
+    CK(cudaGetLastError());
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_solid_integrate_after_contact(demsph_engine* e, double dt)
+{
+    ENGINE_GUARD(e)
+    REQUIRE_INIT(e);
+    stageAfter(e, dt);
+    CK(cudaGetLastError());
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_synchronize(demsph_engine* e)
+{
+    ENGINE_GUARD(e)
+    CK(cudaStreamSynchronize(e->stream));
+    CK(cudaGetLastError());
+    const int st = readStatus(e);
+    if (st) return fail(e, DEMSPH_ERR_CAPACITY, "a list overflowed (status " + std::to_string(st) + ")");
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+// n_steps update() bodies without the driver hook.  With use_graph, steps run
+// uncaptured until i_step is a multiple of the period (and > 1: step 1 stores
+// the Shepard reference), whole periods replay one captured graph, the rest
+// runs uncaptured.  One synchronisation at the end; on a list overflow the
+// engine grows the list and resumes from the first incomplete step.
+int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph)
+{
+    if (gap < 1 || n_steps < 0) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    REQUIRE_INIT(e);
+    DeviceState& d = e->d;
+    const int period = 10 * gap;  // multiple of 2 (contact-list parity) and of 5 gap (re-initialisation)
+    const int end = first_step + n_steps;
+    int step = first_step;
+    for (int attempt = 0; step < end; ++attempt) {
+        if (attempt > 32) return fail(e, DEMSPH_ERR_CAPACITY, "list overflow persists after growing");
+        CK(cudaMemsetAsync(d.stepsDone, 0, sizeof(int), e->stream));
+        const int startPar = e->par;
+        int s = step;
+        auto graphable = [&](int k) { return use_graph && k > 1 && k % period == 0 && end - k >= period; };
+        while (s < end && !graphable(s)) fullStep(e, dt, s++, gap);
+        if (s < end && graphable(s)) {
+            if (!e->graph || e->graphPeriod != period || e->graphGap != gap || e->graphDt != dt ||
+                e->graphParity != e->par) {
+                dropGraph(e);
+                const int parity = e->par;
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+                for (int k = 0; k < period; ++k) fullStep(e, dt, s + k, gap);
+                CK(cudaStreamEndCapture(e->stream, &g));
+                const cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
+                cudaGraphDestroy(g);
+                CK(ie);
+                e->graphPeriod = period;
+                e->graphGap = gap;
+                e->graphDt = dt;
+                e->graphParity = parity;
+                e->par = parity;  // a period flips the parity an even number of times
+            }
+            while (end - s >= period) {
+                CK(cudaGraphLaunch(e->graph, e->stream));
+                s += period;
+            }
+            while (s < end) fullStep(e, dt, s++, gap);
+        }
+        int done = 0;
+        const int st = readStatus(e, &done);
+        if (st == 0) {
+            step = s;
+            continue;
+        }
+        if (st & ~ALL_OVERFLOWS) return fail(e, DEMSPH_ERR_STATE, "unexpected device status " + std::to_string(st));
+        step += done;                        // steps before the failed one completed
+        e->par = startPar ^ (done & 1);      // every step builds one contact list
+        grow(e, st);
+    }
+    CK(cudaGetLastError());
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+}  // extern "C"

@@ -1,0 +1,567 @@
+// State transfer, run-time setters and artefact export - the I/O half of the
+// C ABI in include/demsph_gb300.h.
+//
+// Downloads return the reference's host layout (FP64, original particle
+// order): positions are rebuilt as cell origin + double-float offset in FP64
+// on the device, then copied.  Exports rebuild the reference's artefacts
+// (objectHash, half pair lists in CSR order, springs, bonds) from the
+// engine's own structures, in the reference's order (core/neighborSearch.cu).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "engine_impl.cuh"
+
+using namespace demsph;
+
+namespace {
+
+__device__ __forceinline__ double cellOrigin(const DeviceState& d, int a, int c) { return d.minB[a] + (double)c * d.cs[a]; }
+
+__global__ void kFluidOut(DeviceState d, double* out)  // 10 doubles per original index
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.nf) return;
+    const int id = d.fid[s];
+    const int4 c = d.fcell[s];
+    const float4 h = d.fph[0][s], l = d.fpl[0][s];
+    const float4 vh = d.fvh[0][s], vl = d.fvl[0][s];
+    const float4 a = d.facc[s];
+    double* o = out + 10 * (size_t)id;
+    o[0] = cellOrigin(d, 0, c.x) + ((double)h.x + (double)l.x);
+    o[1] = cellOrigin(d, 1, c.y) + ((double)h.y + (double)l.y);
+    o[2] = cellOrigin(d, 2, c.z) + ((double)h.z + (double)l.z);
+    o[3] = (double)vh.x + (double)vl.x;
+    o[4] = (double)vh.y + (double)vl.y;
+    o[5] = (double)vh.z + (double)vl.z;
+    o[6] = a.x;
+    o[7] = a.y;
+    o[8] = a.z;
+    o[9] = d.fdrho[0][s];
+}
+
+__global__ void kSolidOut(DeviceState d, double* out)  // 18 doubles per solid
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.ns) return;
+    const int4 c = d.scell[i];
+    const float4 h = d.sph[i], l = d.spl[i];
+    const float4 vh = d.svh[i], vl = d.svl[i], wh = d.swh[i], wl = d.swl[i];
+    const float4 a = d.sacc[i], n = d.snormal[i], t = d.storque[i];
+    double* o = out + 18 * (size_t)i;
+    o[0] = cellOrigin(d, 0, c.x) + ((double)h.x + (double)l.x);
+    o[1] = cellOrigin(d, 1, c.y) + ((double)h.y + (double)l.y);
+    o[2] = cellOrigin(d, 2, c.z) + ((double)h.z + (double)l.z);
+    o[3] = (double)vh.x + vl.x; o[4] = (double)vh.y + vl.y; o[5] = (double)vh.z + vl.z;
+    o[6] = a.x; o[7] = a.y; o[8] = a.z;
+    o[9] = n.x; o[10] = n.y; o[11] = n.z;
+    o[12] = t.x; o[13] = t.y; o[14] = t.z;
+    o[15] = (double)wh.x + wl.x; o[16] = (double)wh.y + wl.y; o[17] = (double)wh.z + wl.z;
+}
+
+// Writes the state given in original order (FP64) into the engine; NaN in the
+// first component of an entry leaves that entry untouched.
+__global__ void kFluidIn(DeviceState d, const double* pos, const double* vel, const double* drho)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.nf) return;
+    const int id = d.fid[s];
+    if (pos) {
+        int4 c = d.fcell[s];
+        float4 h = d.fph[0][s], l = d.fpl[0][s];
+        const double p[3] = {pos[3 * id], pos[3 * id + 1], pos[3 * id + 2]};
+        float hh[3], ll[3];
+        const int cc[3] = {c.x, c.y, c.z};
+        for (int a = 0; a < 3; ++a) {
+            const dfl o = df_from_double(p[a] - cellOrigin(d, a, cc[a]));
+            hh[a] = o.hi;
+            ll[a] = o.lo;
+        }
+        h.x = hh[0]; h.y = hh[1]; h.z = hh[2];
+        l.x = ll[0]; l.y = ll[1]; l.z = ll[2];
+        d.fph[0][s] = h;
+        d.fpl[0][s] = l;
+    }
+    if (vel) {
+        const dfl x = df_from_double(vel[3 * id]), y = df_from_double(vel[3 * id + 1]), z = df_from_double(vel[3 * id + 2]);
+        d.fvh[0][s] = make_float4(x.hi, y.hi, z.hi, 0.f);
+        d.fvl[0][s] = make_float4(x.lo, y.lo, z.lo, 0.f);
+    }
+    if (drho) d.fdrho[0][s] = (float)drho[id];
+}
+
+__global__ void kSolidIn(DeviceState d, const double* pos, const double* vel, const double* w)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.ns) return;
+    if (pos) {
+        const int4 c = d.scell[i];
+        float4 h = d.sph[i], l = d.spl[i];
+        const dfl x = df_from_double(pos[3 * i] - cellOrigin(d, 0, c.x));
+        const dfl y = df_from_double(pos[3 * i + 1] - cellOrigin(d, 1, c.y));
+        const dfl z = df_from_double(pos[3 * i + 2] - cellOrigin(d, 2, c.z));
+        d.sph[i] = make_float4(x.hi, y.hi, z.hi, h.w);
+        d.spl[i] = make_float4(x.lo, y.lo, z.lo, l.w);
+    }
+    if (vel) {
+        const dfl x = df_from_double(vel[3 * i]), y = df_from_double(vel[3 * i + 1]), z = df_from_double(vel[3 * i + 2]);
+        d.svh[i] = make_float4(x.hi, y.hi, z.hi, 0.f);
+        d.svl[i] = make_float4(x.lo, y.lo, z.lo, 0.f);
+    }
+    if (w) {
+        const dfl x = df_from_double(w[3 * i]), y = df_from_double(w[3 * i + 1]), z = df_from_double(w[3 * i + 2]);
+        d.swh[i] = make_float4(x.hi, y.hi, z.hi, 0.f);
+        d.swl[i] = make_float4(x.lo, y.lo, z.lo, 0.f);
+    }
+}
+
+__global__ void kSetClumpVelocity(DeviceState d, int c, double vx, double vy, double vz)
+{
+    d.cvel[c] = make_double3(vx, vy, vz);
+}
+
+// addExternalForce (core/dataBase.cpp:179-195): a += F * invM.
+__global__ void kAddForce(DeviceState d, int i, float fx, float fy, float fz)
+{
+    const float im = d.sph[i].w;
+    float4 a = d.sacc[i];
+    a.x += fx * im;
+    a.y += fy * im;
+    a.z += fz * im;
+    d.sacc[i] = a;
+}
+
+// addGlobalDamping (core/dataBase.cpp:197-224): F += -C |F| v/|v|, T += -C |T| w/|w|.
+__global__ void kAddDamping(DeviceState d, int i, float cd)
+{
+    const float im = d.sph[i].w;
+    if (!(im >= 1.e-10f)) return;
+    float3 F = xyz(d.sacc[i]) / im;
+    float3 T = xyz(d.storque[i]);
+    const float3 v = xyz(d.svh[i]), w = xyz(d.swh[i]);
+    if (len3(v) > 1.e-10f) F = F + unit3(v) * (-cd * len3(F));
+    if (len3(w) > 1.e-10f) T = T + unit3(w) * (-cd * len3(T));
+    d.sacc[i] = f4(F * im);
+    d.storque[i] = f4(T);
+}
+
+template <class T>
+void d2h(std::vector<T>& v, const T* src, size_t n)
+{
+    v.resize(n);
+    if (n) CK(cudaMemcpy(v.data(), src, sizeof(T) * n, cudaMemcpyDeviceToHost));
+}
+
+}  // namespace
+
+extern "C" {
+
+int demsph_download_fluids(demsph_engine* e, double* pos, double* vel, double* acc, double* drho)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    if (d.nf == 0) return DEMSPH_OK;
+    double* buf = scratchDoubles(e, 10 * (size_t)d.nf);
+    kFluidOut<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, buf);
+    std::vector<double> h(10 * (size_t)d.nf);
+    CK(cudaMemcpyAsync(h.data(), buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    for (int i = 0; i < d.nf; ++i) {
+        const double* o = &h[10 * (size_t)i];
+        if (pos) std::memcpy(pos + 3 * (size_t)i, o, 3 * sizeof(double));
+        if (vel) std::memcpy(vel + 3 * (size_t)i, o + 3, 3 * sizeof(double));
+        if (acc) std::memcpy(acc + 3 * (size_t)i, o + 6, 3 * sizeof(double));
+        if (drho) drho[i] = o[9];
+    }
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_download_solids(demsph_engine* e, double* pos, double* vel, double* acc, double* normal, double* torque,
+                           double* angvel)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    if (d.ns == 0) return DEMSPH_OK;
+    double* buf = scratchDoubles(e, 18 * (size_t)d.ns);
+    kSolidOut<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, buf);
+    std::vector<double> h(18 * (size_t)d.ns);
+    CK(cudaMemcpyAsync(h.data(), buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    double* outs[6] = {pos, vel, acc, normal, torque, angvel};
+    for (int i = 0; i < d.ns; ++i)
+        for (int k = 0; k < 6; ++k)
+            if (outs[k]) std::memcpy(outs[k] + 3 * (size_t)i, &h[18 * (size_t)i + 3 * k], 3 * sizeof(double));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_download_clumps(demsph_engine* e, double* centroid, double* vel, double* acc, double* angvel,
+                           double* torque, double* orientation)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    CK(cudaStreamSynchronize(e->stream));
+    const size_t n = d.nc;
+    if (n == 0) return DEMSPH_OK;
+    if (centroid) CK(cudaMemcpy(centroid, d.cpos, sizeof(double3) * n, cudaMemcpyDeviceToHost));
+    if (vel) CK(cudaMemcpy(vel, d.cvel, sizeof(double3) * n, cudaMemcpyDeviceToHost));
+    if (acc) CK(cudaMemcpy(acc, d.cacc, sizeof(double3) * n, cudaMemcpyDeviceToHost));
+    if (angvel) CK(cudaMemcpy(angvel, d.cw, sizeof(double3) * n, cudaMemcpyDeviceToHost));
+    if (torque) CK(cudaMemcpy(torque, d.ctorque, sizeof(double3) * n, cudaMemcpyDeviceToHost));
+    if (orientation) CK(cudaMemcpy(orientation, d.cq, sizeof(double4) * n, cudaMemcpyDeviceToHost));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_upload_fluids(demsph_engine* e, const double* pos, const double* vel, const double* drho)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    if (d.nf == 0) return DEMSPH_OK;
+    double* buf = scratchDoubles(e, 7 * (size_t)d.nf);
+    double* dp = pos ? buf : nullptr;
+    double* dv = vel ? buf + 3 * (size_t)d.nf : nullptr;
+    double* dr = drho ? buf + 6 * (size_t)d.nf : nullptr;
+    if (dp) CK(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, e->stream));
+    if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, e->stream));
+    if (dr) CK(cudaMemcpyAsync(dr, drho, sizeof(double) * d.nf, cudaMemcpyHostToDevice, e->stream));
+    kFluidIn<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, dp, dv, dr);
+    CK(cudaStreamSynchronize(e->stream));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel, const double* angvel)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    if (d.ns == 0) return DEMSPH_OK;
+    double* buf = scratchDoubles(e, 9 * (size_t)d.ns);
+    double* dp = pos ? buf : nullptr;
+    double* dv = vel ? buf + 3 * (size_t)d.ns : nullptr;
+    double* dw = angvel ? buf + 6 * (size_t)d.ns : nullptr;
+    if (dp) CK(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
+    if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
+    if (dw) CK(cudaMemcpyAsync(dw, angvel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
+    kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw);
+    CK(cudaStreamSynchronize(e->stream));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_set_gravity(demsph_engine* e, const double g[3])
+{
+    if (!g) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    for (int a = 0; a < 3; ++a) e->d.g64[a] = g[a];
+    e->d.g = make_float3((float)g[0], (float)g[1], (float)g[2]);
+    dropGraph(e);  // gravity is a kernel argument baked into captured graphs
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_set_contact_models(demsph_engine* e, const demsph_scene* t)
+{
+    if (!t || !t->hertzian || !t->linear || !t->bonded || t->n_material != e->d.tab.nMat) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    const int nslot = t->n_material * (t->n_material + 1) / 2;
+    std::vector<float> all(26 * (size_t)nslot);
+    for (int k = 0; k < 8 * nslot; ++k) all[k] = (float)t->hertzian[k];
+    for (int k = 0; k < 11 * nslot; ++k) all[8 * nslot + k] = (float)t->linear[k];
+    for (int k = 0; k < 6 * nslot; ++k) all[19 * nslot + k] = (float)t->bonded[k];
+    for (int k = 0; k < nslot; ++k) {
+        const double lr = std::log(t->hertzian[8 * k + 2]);
+        all[25 * nslot + k] = (float)(-lr / std::sqrt(lr * lr + 3.1415926535897931 * 3.1415926535897931));
+    }
+    CK(cudaMemcpyAsync(const_cast<float*>(e->d.tab.hz), all.data(), sizeof(float) * all.size(), cudaMemcpyHostToDevice,
+                       e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_set_clump_velocity(demsph_engine* e, int c, const double v[3])
+{
+    if (!v) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    if (c < 0 || c >= e->d.nc) return DEMSPH_OK;  // the reference ignores out-of-range clumps (dataBase.h:171)
+    kSetClumpVelocity<<<1, 1, 0, e->stream>>>(e->d, c, v[0], v[1], v[2]);
+    CK(cudaStreamSynchronize(e->stream));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_add_external_force(demsph_engine* e, int i, const double f[3])
+{
+    if (!f) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    if (i < 0 || i >= e->d.ns) return fail(e, DEMSPH_ERR_ARGUMENT, "solid index out of range");
+    kAddForce<<<1, 1, 0, e->stream>>>(e->d, i, (float)f[0], (float)f[1], (float)f[2]);
+    CK(cudaStreamSynchronize(e->stream));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_add_global_damping(demsph_engine* e, int i, double cd)
+{
+    ENGINE_GUARD(e)
+    if (i < 0 || i >= e->d.ns) return fail(e, DEMSPH_ERR_ARGUMENT, "solid index out of range");
+    kAddDamping<<<1, 1, 0, e->stream>>>(e->d, i, (float)cd);
+    CK(cudaStreamSynchronize(e->stream));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_get_counts(demsph_engine* e, demsph_counts* out)
+{
+    if (!out) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    CK(cudaStreamSynchronize(e->stream));
+    *out = demsph_counts{};
+    std::vector<int> ffc, fsc;
+    d2h(ffc, d.ffc, d.nf);
+    d2h(fsc, d.fsc, d.nf);
+    long long ff = 0, fs = 0;
+    for (int i = 0; i < d.nf; ++i) {
+        ff += std::min(ffc[i], d.kff);
+        fs += std::min(fsc[i], d.kfs);
+    }
+    out->fluid_pairs = ff / 2;
+    out->fluid_solid_pairs = fs;
+    int np = 0;
+    if (d.ns > 0) CK(cudaMemcpy(&np, d.sfbase[e->par] + d.ns, sizeof(int), cudaMemcpyDeviceToHost));
+    out->solid_pairs = np;
+    out->bonds = d.nb;
+    std::vector<int> on;
+    d2h(on, d.bon, d.nb);
+    for (int b = 0; b < d.nb; ++b) out->bonds_intact += on[b] != 0;
+    out->grid_cells = d.grid.num;
+    out->grid_size[0] = d.grid.gx;
+    out->grid_size[1] = d.grid.gy;
+    out->grid_size[2] = d.grid.gz;
+    for (int a = 0; a < 3; ++a) out->cell_size[a] = d.cs[a];
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+// objectHash + cell spans (core/neighborSearch.cu:71-113).  For fluids these
+// are the structures of the last fluid list rebuild.
+int demsph_export_cell_hash(demsph_engine* e, int which, int* value, int* index, int* start, int* end)
+{
+    if (which != 0 && which != 1) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    CK(cudaStreamSynchronize(e->stream));
+    const int n = which == 0 ? d.nf : d.ns;
+    std::vector<int> cs;
+    d2h(cs, which == 0 ? d.fcellStart : d.scellStart, (size_t)d.grid.num + 1);
+    if (which == 0) {
+        std::vector<int4> cell;
+        std::vector<int> id;
+        d2h(cell, d.fcell, n);
+        d2h(id, d.fid, n);
+        for (int s = 0; s < n; ++s) {
+            if (value) value[s] = cell[s].w;
+            if (index) index[s] = id[s];
+        }
+    } else {
+        std::vector<int> sorted, key;
+        d2h(sorted, d.ssorted, n);
+        d2h(key, d.skey, n);
+        for (int p = 0; p < n; ++p) {
+            if (value) value[p] = key[sorted[p]];
+            if (index) index[p] = sorted[p];
+        }
+    }
+    for (int k = 0; k < d.grid.num; ++k) {
+        const bool empty = cs[k] == cs[k + 1];
+        if (start) start[k] = empty ? -1 : cs[k];
+        if (end) end[k] = empty ? -1 : cs[k + 1];
+    }
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+// fluid2Fluid half list (core/neighborSearch.cu:115-220): for each fluid i in
+// original order, its partners j > i in walk order.  Returns the pair count
+// through prefix[n-1]; pairs beyond capacity are not written.
+int demsph_export_fluid_pairs(demsph_engine* e, int* prefix, int* pointed, int* pointing, long long cap)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    CK(cudaStreamSynchronize(e->stream));
+    const int n = d.nf;
+    std::vector<unsigned> ff;
+    std::vector<int> ffc, id, slot;
+    d2h(ff, d.ff, (size_t)d.kff * n);
+    d2h(ffc, d.ffc, n);
+    d2h(id, d.fid, n);
+    slot.resize(n);
+    for (int s = 0; s < n; ++s) slot[id[s]] = s;
+    long long w = 0;
+    for (int i = 0; i < n; ++i) {
+        const int s = slot[i];
+        const int m = std::min(ffc[s], d.kff);
+        for (int k = 0; k < m; ++k) {
+            const int j = id[ff[(size_t)k * n + s] >> 5];
+            if (j <= i) continue;
+            if (w < cap) {
+                if (pointed) pointed[w] = i;
+                if (pointing) pointing[w] = j;
+            }
+            ++w;
+        }
+        if (prefix) prefix[i] = (int)w;
+    }
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+// fluid2Solid list (core/neighborSearch.cu:115-220) with the coupling force of
+// each pair (core/integrate.cu:282-330) as of the last step (debug bit 0) or
+// zeros otherwise.
+int demsph_export_fluid_solid_pairs(demsph_engine* e, int* prefix, int* pointed, int* pointing, double* force,
+                                    long long cap)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    CK(cudaStreamSynchronize(e->stream));
+    const int n = d.nf;
+    std::vector<int> fs, fsc, id, slot;
+    std::vector<float4> pf;
+    d2h(fs, d.fs, (size_t)d.kfs * n);
+    d2h(fsc, d.fsc, n);
+    d2h(id, d.fid, n);
+    if (d.fsPairForce) d2h(pf, d.fsPairForce, (size_t)d.kfs * n);
+    slot.resize(n);
+    for (int s = 0; s < n; ++s) slot[id[s]] = s;
+    long long w = 0;
+    for (int i = 0; i < n; ++i) {
+        const int s = slot[i];
+        const int m = std::min(fsc[s], d.kfs);
+        for (int k = 0; k < m; ++k) {
+            if (w < cap) {
+                if (pointed) pointed[w] = i;
+                if (pointing) pointing[w] = fs[(size_t)k * n + s];
+                if (force) {
+                    const float4 f = pf.empty() ? make_float4(0, 0, 0, 0) : pf[(size_t)k * n + s];
+                    force[3 * w] = f.x;
+                    force[3 * w + 1] = f.y;
+                    force[3 * w + 2] = f.z;
+                }
+            }
+            ++w;
+        }
+        if (prefix) prefix[i] = (int)w;
+    }
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+// solid2Solid list (core/neighborSearch.cu:222-312) with the contact forces,
+// torques and springs of the last contact phase (core/integrate.cu:423-512).
+int demsph_export_solid_pairs(demsph_engine* e, int* prefix, int* pointed, int* pointing, double* force,
+                              double* torque, double* sliding, double* rolling, double* torsion, long long cap)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    CK(cudaStreamSynchronize(e->stream));
+    const int ns = d.ns;
+    const int par = e->par;
+    std::vector<int> fb, pa, pb;
+    d2h(fb, d.sfbase[par], (size_t)ns + 1);
+    const int np = ns > 0 ? std::min(fb[ns], d.ssCap) : 0;
+    d2h(pa, d.spa, np);
+    d2h(pb, d.spb[par], np);
+    std::vector<float4> F, T, S0, S1, S2;
+    if (force) d2h(F, d.pF, np);
+    if (torque) d2h(T, d.pT, np);
+    if (sliding) d2h(S0, d.spring[par][0], np);
+    if (rolling) d2h(S1, d.spring[par][1], np);
+    if (torsion) d2h(S2, d.spring[par][2], np);
+    auto put = [&](double* out, const std::vector<float4>& v, int k) {
+        if (!out) return;
+        out[3 * (size_t)k] = v[k].x;
+        out[3 * (size_t)k + 1] = v[k].y;
+        out[3 * (size_t)k + 2] = v[k].z;
+    };
+    for (int k = 0; k < np && k < cap; ++k) {
+        if (pointed) pointed[k] = pa[k];
+        if (pointing) pointing[k] = pb[k];
+        put(force, F, k);
+        put(torque, T, k);
+        put(sliding, S0, k);
+        put(rolling, S1, k);
+        put(torsion, S2, k);
+    }
+    if (prefix)
+        for (int i = 0; i < ns; ++i) prefix[i] = fb[i + 1];
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+// interactionBonded (core/deviceStructs.h:714-789).  The contact point is the
+// bond's stored lever added to the current position of its first sphere.
+int demsph_export_bonds(demsph_engine* e, int* pointed, int* pointing, int* isb, double* fn, double* tt, double* fs,
+                        double* tb, double* normal, double* point, long long cap)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    CK(cudaStreamSynchronize(e->stream));
+    const int nb = d.nb;
+    std::vector<int2> ab;
+    std::vector<int> on;
+    std::vector<float4> FnTt, FsH, FsL, TbH, TbL, N, L;
+    d2h(ab, d.bab, nb);
+    d2h(on, d.bon, nb);
+    d2h(FnTt, d.bFnTt, nb);
+    d2h(FsH, d.bFsH, nb);
+    d2h(FsL, d.bFsL, nb);
+    d2h(TbH, d.bTbH, nb);
+    d2h(TbL, d.bTbL, nb);
+    d2h(N, d.bN, nb);
+    d2h(L, d.bLever, nb);
+    std::vector<double> pos;
+    if (point && d.ns > 0) {
+        pos.resize(3 * (size_t)d.ns);
+        const int rc = demsph_download_solids(e, pos.data(), nullptr, nullptr, nullptr, nullptr, nullptr);
+        if (rc != DEMSPH_OK) return rc;
+    }
+    for (int b = 0; b < nb && b < cap; ++b) {
+        if (pointed) pointed[b] = ab[b].x;
+        if (pointing) pointing[b] = ab[b].y;
+        if (isb) isb[b] = on[b];
+        if (fn) fn[b] = (double)FnTt[b].x + FnTt[b].y;
+        if (tt) tt[b] = (double)FnTt[b].z + FnTt[b].w;
+        for (int a = 0; a < 3; ++a) {
+            const float* sh = &FsH[b].x; const float* sl = &FsL[b].x;
+            const float* th = &TbH[b].x; const float* tl = &TbL[b].x;
+            if (fs) fs[3 * b + a] = (double)sh[a] + sl[a];
+            if (tb) tb[3 * b + a] = (double)th[a] + tl[a];
+            if (normal) normal[3 * b + a] = (&N[b].x)[a];
+            if (point) point[3 * b + a] = pos[3 * (size_t)ab[b].x + a] + (&L[b].x)[a];
+        }
+    }
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_export_fluid_sumw0(demsph_engine* e, double* out)
+{
+    if (!out) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    CK(cudaStreamSynchronize(e->stream));
+    std::vector<float> w;
+    std::vector<int> id;
+    d2h(w, d.fsumW0, d.nf);
+    d2h(id, d.fid, d.nf);
+    for (int s = 0; s < d.nf; ++s) out[id[s]] = w[s];
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+// Hashed grid: cell keys, counting sort by cell, cell spans.
+//
+// The reference hashes every particle each step (calculatePointHash,
+// core/neighborSearch.cu:19-36), sorts (key, index) pairs with thrust (a
+// stable radix sort) and finds cellStart/cellEnd (:38-113).  Here:
+//   1. one pass renormalises each position into its cell, computes the key and
+//      takes a slot in its cell with an atomic counter;
+//   2. an exclusive scan of the counts gives every cell's start;
+//   3. each particle is scattered to start + slot;
+//   4. within a cell the atomic slots are arbitrary, so each particle's final
+//      place is start + (number of particles of the same cell with a smaller
+//      original index) - the same (key, index) order as the reference's stable
+//      sort, deterministically.
+// Fluids are then physically reordered (gathered) into that order; solids keep
+// their original order and use the sorted index.
+#include "kernels.cuh"
+
+namespace demsph {
+
+namespace {
+
+constexpr int T = 256;
+
+__global__ void kFluidHash(DeviceState d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nf || *d.status) return;
+    int4 c = d.fcell[i];
+    float4 h = d.fph[0][i];
+    float4 l = d.fpl[0][i];
+    renormAxis(c.x, h.x, l.x, d.grid.csx);
+    renormAxis(c.y, h.y, l.y, d.grid.csy);
+    renormAxis(c.z, h.z, l.z, d.grid.csz);
+    const int key = cellKey(c.x, c.y, c.z, d.grid);
+    c.w = key;
+    // copy the whole particle into the gather sources
+    d.tcell[i] = c;
+    d.fph[1][i] = h;
+    d.fpl[1][i] = l;
+    d.fvh[1][i] = d.fvh[0][i];
+    d.fvl[1][i] = d.fvl[0][i];
+    d.fdrho[1][i] = d.fdrho[0][i];
+    d.tacc[i] = d.facc[i];
+    d.tpar[i] = d.fpar[i];
+    d.tsumW0[i] = d.fsumW0[i];
+    d.tid[i] = d.fid[i];
+    d.fkey[i] = key;
+    d.fslotInCell[i] = atomicAdd(&d.fcellCount[key], 1);
+}
+
+__global__ void kScatter(int n, const int* __restrict__ key, const int* __restrict__ slotInCell,
+                         const int* __restrict__ cellStart, int* __restrict__ out, const int* status)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || *status) return;
+    out[cellStart[key[i]] + slotInCell[i]] = i;
+}
+
+// Final slot of the element at sorted position p: its cell start plus the
+// number of elements of the same cell with a smaller original index.
+__device__ __forceinline__ int stableRank(int p, const int* __restrict__ sorted, const int* __restrict__ key,
+                                          const int* __restrict__ cellStart, const int* __restrict__ ident, int& e)
+{
+    e = sorted[p];
+    const int k = key[e];
+    const int s = cellStart[k], t = cellStart[k + 1];
+    const int me = ident ? ident[e] : e;
+    int rank = 0;
+    for (int q = s; q < t; ++q) {
+        const int o = sorted[q];
+        rank += (ident ? ident[o] : o) < me;
+    }
+    return s + rank;
+}
+
+__global__ void kFluidGather(DeviceState d)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.nf || *d.status) return;
+    int e;
+    const int q = stableRank(p, d.fsortTmp, d.fkey, d.fcellStart, d.tid, e);
+    d.fcell[q] = d.tcell[e];
+    d.fph[0][q] = d.fph[1][e];
+    d.fpl[0][q] = d.fpl[1][e];
+    d.fvh[0][q] = d.fvh[1][e];
+    d.fvl[0][q] = d.fvl[1][e];
+    d.fdrho[0][q] = d.fdrho[1][e];
+    d.facc[q] = d.tacc[e];
+    d.fpar[q] = d.tpar[e];
+    d.fsumW0[q] = d.tsumW0[e];
+    const int id = d.tid[e];
+    d.fid[q] = id;
+    d.fslot[id] = q;
+}
+
+__global__ void kSolidHash(DeviceState d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.ns || *d.status) return;
+    int4 c = d.scell[i];
+    float4 h = d.sph[i];
+    float4 l = d.spl[i];
+    renormAxis(c.x, h.x, l.x, d.grid.csx);
+    renormAxis(c.y, h.y, l.y, d.grid.csy);
+    renormAxis(c.z, h.z, l.z, d.grid.csz);
+    const int key = cellKey(c.x, c.y, c.z, d.grid);
+    c.w = key;
+    d.scell[i] = c;
+    d.sph[i] = h;
+    d.spl[i] = l;
+    d.skey[i] = key;
+    d.sslotInCell[i] = atomicAdd(&d.scellCount[key], 1);
+}
+
+__global__ void kSolidRank(DeviceState d)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.ns || *d.status) return;
+    int e;
+    const int q = stableRank(p, d.ssortTmp, d.skey, d.scellStart, nullptr, e);
+    d.ssorted[q] = e;
+}
+
+}  // namespace
+
+void launchFluidHashReorder(const DeviceState& d, cudaStream_t s)
+{
+    if (d.nf <= 0) return;
+    cudaMemsetAsync(d.fcellCount, 0, sizeof(int) * d.grid.num, s);
+    kFluidHash<<<blocksFor(d.nf, T), T, 0, s>>>(d);
+    scanExclusive(d.fcellCount, d.fcellStart, d.grid.num, d.scanWork, s);
+    kScatter<<<blocksFor(d.nf, T), T, 0, s>>>(d.nf, d.fkey, d.fslotInCell, d.fcellStart, d.fsortTmp, d.status);
+    kFluidGather<<<blocksFor(d.nf, T), T, 0, s>>>(d);
+}
+
+void launchSolidHashSort(const DeviceState& d, cudaStream_t s)
+{
+    if (d.ns <= 0) return;
+    cudaMemsetAsync(d.scellCount, 0, sizeof(int) * d.grid.num, s);
+    kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d);
+    scanExclusive(d.scellCount, d.scellStart, d.grid.num, d.scanWork, s);
+    kScatter<<<blocksFor(d.ns, T), T, 0, s>>>(d.ns, d.skey, d.sslotInCell, d.scellStart, d.ssortTmp, d.status);
+    kSolidRank<<<blocksFor(d.ns, T), T, 0, s>>>(d);
+}
+
+}  // namespace demsph

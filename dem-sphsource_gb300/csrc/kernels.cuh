@@ -1,0 +1,164 @@
+// All device buffers of one scene, as a plain struct of pointers, and the
+// launch functions of the step.  engine.cu owns the allocations; the kernel
+// files (grid.cu, lists.cu, sph.cu, dem.cu) only read this struct.
+#pragma once
+#include <cuda_runtime.h>
+#include "engine.cuh"
+#include "../../include/demsph_gb300.h"
+
+namespace demsph {
+
+struct DeviceState {
+    GridDev grid;
+    double minB[3], cs[3];   // FP64 grid, for import and export
+    float3 g;                // gravity
+    double g64[3];
+    Tables tab;
+    int fixes;
+    int* status;             // StatusBits, sticky until the host clears it
+    int* stepsDone;          // steps completed since the last reset
+    int* scanWork;
+
+    // ---- fluid (slots in cell order) ----
+    int nf, kff, kfs;
+    int4* fcell;
+    float4* fph[2];
+    float4* fpl[2];
+    float4* fvh[2];
+    float4* fvl[2];
+    float* fdrho[2];
+    float4* facc;
+    float4* fpar;
+    float* fsumW0;
+    int* fid;                // slot -> original index
+    int* fslot;              // original index -> slot
+    // reorder temporaries
+    int4* tcell;
+    float4* tacc;
+    float4* tpar;
+    float* tsumW0;
+    int* tid;
+    int* fkey;
+    int* fslotInCell;
+    int* fsortTmp;
+    int* fcellCount;         // grid.num
+    int* fcellStart;         // grid.num + 1
+    // lists (column-major, stride nf)
+    unsigned* ff;
+    int* ffc;
+    int* fs;
+    int* fsc;
+    // fluid partners of each solid (for the coupling force), CSR over solids
+    int coupCap;
+    int* coupCount;          // ns
+    int* coupStart;          // ns + 1
+    int* coupList;           // coupCap fluid slots
+
+    // ---- solids (original order) ----
+    int ns;
+    int4* scell;
+    float4* sph;             // offset hi, w = inverse mass
+    float4* spl;
+    float4* svh;
+    float4* svl;
+    float4* swh;
+    float4* swl;
+    float4* sacc;
+    float4* storque;
+    float4* snormal;
+    float4* sfcoup;
+    float4* srad;            // r hi, r lo, eff hi, eff lo
+    int4* sflags;            // material, cluster, clump, dummy
+    int* skey;
+    int* sslotInCell;
+    int* ssorted;            // solid indices in (cell, index) order
+    int* ssortTmp;
+    int* scellCount;
+    int* scellStart;
+    // contact list, forward CSR over solids (pairs (A, B), A < B), two parities
+    int ssCap;
+    int* sfcnt;              // ns
+    int* srcnt;              // ns
+    int* sfbase[2];          // ns + 1
+    int* srbase;             // ns + 1
+    int* spa;                // pair -> A
+    int* spb[2];             // pair -> B
+    int* srpartner;          // reverse entries: partner A' < B for each B
+    float4* spring[2][3];    // sliding, rolling, torsion springs per pair
+    float4* pF;              // pair force (on A)
+    float4* pT;              // pair contact torque (rolling + torsion + bond), as the reference stores it
+    float4* pTA;             // pair torque on A incl. lever arm
+    float4* pTB;             // pair torque on B incl. lever arm (to subtract)
+
+    // ---- infinite walls ----
+    int nw;
+    float4* wnh;             // normal hi
+    float4* wnl;             // normal lo
+    float2* wP;              // (p - min) . n, double-float
+    int* wmat;
+    float4* wspring[3];      // ns * nw
+
+    // ---- bonds ----
+    int nb;
+    int2* bab;
+    int* bon;
+    float4* bFnTt;           // normal force hi lo, torsion torque hi lo
+    float4* bFsH;
+    float4* bFsL;
+    float4* bTbH;
+    float4* bTbL;
+    float4* bN;              // contact normal
+    float4* bLever;          // contact point - position of A
+    float4* fsPairForce;     // optional: per fluid-solid pair coupling force of the last step (column-major)
+
+    // ---- clumps (FP64) ----
+    int nc;
+    double3* cpos;
+    double3* cvel;
+    double3* cacc;
+    double3* cw;
+    double3* ctorque;
+    double4* cq;
+    double* cinvI;           // 6 per clump
+    double* cinvm;
+    int* cstart;
+    int* cend;
+};
+
+// scan.cu
+size_t scanWorkspaceInts(int n);
+void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s);
+
+// grid.cu
+void launchFluidHashReorder(const DeviceState& d, cudaStream_t s);
+void launchSolidHashSort(const DeviceState& d, cudaStream_t s);
+
+// lists.cu
+void launchFluidLists(const DeviceState& d, cudaStream_t s);
+void launchCouplingLists(const DeviceState& d, cudaStream_t s);
+void launchSolidContactList(const DeviceState& d, int parity, cudaStream_t s);
+int launchBondFlags(const DeviceState& d, int parity, int np, int* flag, int* pos, int* work, cudaStream_t s);
+void launchBondWrite(const DeviceState& d, int parity, int np, const int* flag, const int* pos, cudaStream_t s);
+void launchSolidNormals(const DeviceState& d, float h, float hlo, cudaStream_t s);
+
+// sph.cu
+void launchDensityReinit(const DeviceState& d, int iStep, cudaStream_t s);
+// which = 0: first half step (densities 0 -> 1, positions drift 0 -> 1);
+// which = 1: second half step (densities 1 -> 0, velocities 1 -> 0).
+void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStream_t s);
+// momentum + kick (dt_f) + drift (dt_f / 2): reads buffers [1], writes velocity [1], position [0].
+void launchMomentumPass(const DeviceState& d, double dtf, cudaStream_t s);
+void launchCoupling(const DeviceState& d, int src, cudaStream_t s);
+void launchCouplingPairForces(const DeviceState& d, int src, float4* out, cudaStream_t s);
+
+// dem.cu
+void launchPairContacts(const DeviceState& d, int parity, float dt, cudaStream_t s);
+void launchBonds(const DeviceState& d, int parity, float dt, cudaStream_t s);
+void launchGatherWalls(const DeviceState& d, int parity, float dt, cudaStream_t s);
+void launchClumpForce(const DeviceState& d, cudaStream_t s);
+void launchSolidIntegrate(const DeviceState& d, double dt, bool beforeContact, cudaStream_t s);
+void launchStepDone(const DeviceState& d, cudaStream_t s);
+
+inline int blocksFor(long long n, int threads) { return (int)((n + threads - 1) / threads > 0 ? (n + threads - 1) / threads : 1); }
+
+}  // namespace demsph

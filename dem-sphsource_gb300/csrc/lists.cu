@@ -1,0 +1,369 @@
+// Neighbour and contact lists.
+//
+// Reference: setFluidInteractionsKernel (core/neighborSearch.cu:115-220) and
+// setSolid2SolidInteractionsKernel (:222-312) walk the 27 cells around each
+// particle in (z, y, x) order and, within a cell, in (index) order, and keep
+// HALF lists (i < j) in CSR form, evaluated from both sides later through
+// reverse spans.  Pair membership is decided once per rebuild, on the
+// positions of that moment, with FP64 distances.
+//
+// Here the same walk, the same order and the same membership test (a FP32
+// distance with a 1e-5 margin, and a double-float distance inside the margin,
+// so decisions agree with the FP64 reference), but:
+//   * fluid lists are FULL lists (both directions) per fluid slot, column-major
+//     ([k * n + i]) so a warp reads one coalesced 128-byte line per entry, and
+//     each entry carries the cell delta of the pair so the SPH loops never
+//     load the partner's cell;
+//   * solid contacts are a forward CSR (A < B, by original index - the
+//     reference's list exactly) plus a per-particle reverse CSR of the lower
+//     partners, both filled in walk order; spring history is remapped by
+//     looking the pair (A, B) up in A's previous forward segment, which holds
+//     the same springs the reference finds through B's reverse span.
+#include "kernels.cuh"
+
+namespace demsph {
+
+namespace {
+
+constexpr int T = 128;
+
+enum FlagBits { F_DUMMY = 1, F_FIXED = 2, F_MASSIVE = 4, F_HASMASS = 8 };  // see engine.cu
+
+__device__ __forceinline__ unsigned deltaCode(int dx, int dy, int dz)
+{
+    if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) return 27u;
+    return (unsigned)((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
+}
+
+__device__ __forceinline__ dfl dfMax(dfl a, dfl b) { return (a.hi > b.hi || (a.hi == b.hi && a.lo >= b.lo)) ? a : b; }
+
+// |x_a - x_b| <= cut (cut in double-float): FP32 decision outside a 1e-5
+// relative band, double-float inside it.
+__device__ __forceinline__ bool withinCut(int4 ca, float4 ha, float4 la, int4 cb, float4 hb, const float4* lbPtr,
+                                          int jb, dfl cut, const GridDev& g)
+{
+    const float3 r = relF(ca, ha, cb, hb, g);
+    const float d2 = dot3(r, r);
+    const float c2 = cut.hi * cut.hi;
+    if (d2 > c2 * (1.f + 1.e-5f)) return false;
+    if (d2 < c2 * (1.f - 1.e-5f)) return true;
+    const float4 lb = lbPtr[jb];
+    const dfl dist = dfNorm(relDF(ca, ha, la, cb, hb, lb, g));
+    return df_ge0(df_sub(cut, dist));
+}
+
+// Stencil walk shared by all list builders: calls f(hash, regular, hx, hy, hz)
+// for the 27 cells around the (truncated) cell of a point, in the reference's
+// order, skipping hashes outside [0, num).  "regular" means the hash is an
+// in-domain cell whose coordinates are (hx, hy, hz); otherwise (aliased rows,
+// overflow bucket) members carry their own cells.
+template <class F>
+__device__ __forceinline__ void forStencil(int4 c, float4 h, float4 l, const GridDev& g, F&& f)
+{
+    const int sx = truncAxis(c.x, h.x, l.x), sy = truncAxis(c.y, h.y, l.y), sz = truncAxis(c.z, h.z, l.z);
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int hx = sx + dx, hy = sy + dy, hz = sz + dz;
+                const int hash = hz * g.gy * g.gx + hy * g.gx + hx;
+                if (hash < 0 || hash >= g.num) continue;
+                f(hash, inDomain(hx, hy, hz, g), hx, hy, hz);
+            }
+}
+
+// ---- fluid lists (full) ----
+__global__ void __launch_bounds__(T) kFluidLists(DeviceState d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nf || *d.status) return;
+    const int4 ci = d.fcell[i];
+    const float4 hi = d.fph[0][i];
+    const float4 li = d.fpl[0][i];
+    const dfl hI = df_make(hi.w, li.w);
+    const dfl cutS = df_add(hI, hI);  // fluid-solid: 2 h_i
+    const int n = d.nf;
+    int nff = 0, nfs = 0;
+    forStencil(ci, hi, li, d.grid, [&](int hash, bool regular, int hx, int hy, int hz) {
+        const int4 cellHere = make_int4(hx, hy, hz, hash);
+        for (int j = d.fcellStart[hash], je = d.fcellStart[hash + 1]; j < je; ++j) {
+            if (j == i) continue;
+            const int4 cj = regular ? cellHere : d.fcell[j];
+            const float4 hj = d.fph[0][j];
+            const dfl hJ = df_make(hj.w, d.fpl[0][j].w);
+            const dfl rad = dfMax(hI, hJ);
+            if (!withinCut(ci, hi, li, cj, hj, d.fpl[0], j, df_add(rad, rad), d.grid)) continue;
+            if (nff < d.kff) d.ff[(size_t)nff * n + i] = ((unsigned)j << 5) | deltaCode(cj.x - ci.x, cj.y - ci.y, cj.z - ci.z);
+            ++nff;
+        }
+        for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
+            const int a = d.ssorted[p];
+            const int4 ca = regular ? cellHere : d.scell[a];
+            if (!withinCut(ci, hi, li, ca, d.sph[a], d.spl, a, cutS, d.grid)) continue;
+            if (nfs < d.kfs) d.fs[(size_t)nfs * n + i] = a;
+            ++nfs;
+        }
+    });
+    d.ffc[i] = nff;
+    d.fsc[i] = nfs;
+    if (nff > d.kff) atomicOr(d.status, ST_FF_OVERFLOW);
+    if (nfs > d.kfs) atomicOr(d.status, ST_FS_OVERFLOW);
+}
+
+// ---- fluid partners of each massive solid (coupling force) ----
+__global__ void kCoupCount(DeviceState d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nf || *d.status) return;
+    const int m = min(d.fsc[i], d.kfs);
+    for (int k = 0; k < m; ++k) {
+        const int a = d.fs[(size_t)k * d.nf + i];
+        if (d.sflags[a].w & F_HASMASS) atomicAdd(&d.coupCount[a], 1);
+    }
+}
+__global__ void kCoupFill(DeviceState d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nf || *d.status) return;
+    if (d.coupStart[d.ns] > d.coupCap) {
+        if (i == 0) atomicOr(d.status, ST_COUPLE_OVERFLOW);
+        return;
+    }
+    const int m = min(d.fsc[i], d.kfs);
+    for (int k = 0; k < m; ++k) {
+        const int a = d.fs[(size_t)k * d.nf + i];
+        if (d.sflags[a].w & F_HASMASS) d.coupList[d.coupStart[a] + atomicAdd(&d.coupCount[a], 1)] = i;
+    }
+}
+// atomics leave each solid's fluid partners in arbitrary order: sort them
+__global__ void kCoupSort(DeviceState d)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= d.ns || *d.status) return;
+    const int s = d.coupStart[a], e = d.coupStart[a + 1];
+    for (int p = s + 1; p < e; ++p) {
+        const int v = d.coupList[p];
+        int q = p - 1;
+        while (q >= s && d.coupList[q] > v) {
+            d.coupList[q + 1] = d.coupList[q];
+            --q;
+        }
+        d.coupList[q + 1] = v;
+    }
+}
+
+// ---- solid contact list ----
+// Filters of core/neighborSearch.cu:246-263 for candidate b of particle a.
+__device__ __forceinline__ bool solidPairCandidate(const DeviceState& d, int a, int4 fa, int b)
+{
+    if (b == a) return false;
+    const int4 fb = d.sflags[b];
+    if (fb.w & F_DUMMY) return false;
+    if (fa.z >= 0 && fa.z == fb.z) return false;           // same clump
+    if ((fa.w & F_FIXED) && (fb.w & F_FIXED)) return false;  // both fixed
+    return true;
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(T) kSolidList(DeviceState d, int par)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= d.ns || *d.status) return;
+    const int4 fa = d.sflags[a];
+    if (fa.w & F_DUMMY) {
+        if (!FILL) d.sfcnt[a] = d.srcnt[a] = 0;
+        return;
+    }
+    const int4 ca = d.scell[a];
+    const float4 ha = d.sph[a], la = d.spl[a];
+    const float4 ra = d.srad[a];
+    const dfl effA = df_make(ra.z, ra.w);
+    int nf = 0, nr = 0;
+    int fbase = 0, rbase = 0, pbase = 0, pend = 0;
+    const int prev = par ^ 1;
+    bool room = true;
+    if (FILL) {
+        fbase = d.sfbase[par][a];
+        rbase = d.srbase[a];
+        pbase = d.sfbase[prev][a];
+        pend = d.sfbase[prev][a + 1];
+        room = d.sfbase[par][d.ns] <= d.ssCap && d.srbase[d.ns] <= d.ssCap;
+        if (!room) {
+            if (a == 0) atomicOr(d.status, ST_SS_OVERFLOW);
+            return;
+        }
+    }
+    forStencil(ca, ha, la, d.grid, [&](int hash, bool regular, int hx, int hy, int hz) {
+        const int4 cellHere = make_int4(hx, hy, hz, hash);
+        for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
+            const int b = d.ssorted[p];
+            if (!solidPairCandidate(d, a, fa, b)) continue;
+            const int4 cb = regular ? cellHere : d.scell[b];
+            const float4 rb = d.srad[b];
+            const dfl cut = df_add(effA, df_make(rb.z, rb.w));
+            if (!withinCut(ca, ha, la, cb, d.sph[b], d.spl, b, cut, d.grid)) continue;
+            if (b > a) {
+                if (FILL) {
+                    const int slot = fbase + nf;
+                    d.spa[slot] = a;
+                    d.spb[par][slot] = b;
+                    float4 s0 = make_float4(0, 0, 0, 0), s1 = s0, s2 = s0;
+                    for (int q = pbase; q < pend; ++q)
+                        if (d.spb[prev][q] == b) {
+                            s0 = d.spring[prev][0][q];
+                            s1 = d.spring[prev][1][q];
+                            s2 = d.spring[prev][2][q];
+                            break;
+                        }
+                    d.spring[par][0][slot] = s0;
+                    d.spring[par][1][slot] = s1;
+                    d.spring[par][2][slot] = s2;
+                }
+                ++nf;
+            } else {
+                if (FILL) d.srpartner[rbase + nr] = b;
+                ++nr;
+            }
+        }
+    });
+    if (!FILL) {
+        d.sfcnt[a] = nf;
+        d.srcnt[a] = nr;
+    }
+}
+
+// ---- bonds at initialisation (addBondData, core/dataBase.cpp:270-308) ----
+__global__ void kBondFlags(DeviceState d, int par, int* flag)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int np = d.sfbase[par][d.ns];
+    if (k >= np || k >= d.ssCap) return;
+    const int a = d.spa[k], b = d.spb[par][k];
+    const float4 ra = d.srad[a], rb = d.srad[b];
+    const dfl dist = dfNorm(relDF(d.scell[a], d.sph[a], d.spl[a], d.scell[b], d.sph[b], d.spl[b], d.grid));
+    // skip when r_a + r_b + 1e-10 <= |x_a - x_b|
+    const dfl gap = df_sub(df_add_f(df_add(df_make(ra.x, ra.y), df_make(rb.x, rb.y)), 1.e-10f), dist);
+    int ok = 0;
+    if (df_ge0(gap) && !(gap.hi == 0.f && gap.lo == 0.f)) {
+        const int4 fa = d.sflags[a], fb = d.sflags[b];
+        const int slot = tableSlot(d.tab, fa.x, fb.x);
+        if (slot >= 0 && d.tab.bd[6 * slot + 1] > 1.e-10f && fa.y >= 0 && fa.y == fb.y) ok = 1;
+    }
+    flag[k] = ok;
+}
+__global__ void kBondWrite(DeviceState d, int par, const int* flag, const int* pos)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int np = d.sfbase[par][d.ns];
+    if (k >= np || k >= d.ssCap || !flag[k]) return;
+    const int b = pos[k];
+    const int i = d.spa[k], j = d.spb[par][k];
+    const DF3 r = relDF(d.scell[i], d.sph[i], d.spl[i], d.scell[j], d.sph[j], d.spl[j], d.grid);
+    const dfl dist = dfNorm(r);
+    const float dd = dist.hi;
+    const float3 n = toF3(r) / dd;
+    const float4 ri = d.srad[i], rj = d.srad[j];
+    const float delta = df_sub(df_add(df_make(ri.x, ri.y), df_make(rj.x, rj.y)), dist).hi;
+    // contact point - x_i = -(d + r_i - r_j) / 2 * n
+    const float lever = -0.5f * (dd + ri.x - rj.x);
+    (void)delta;
+    d.bab[b] = make_int2(i, j);
+    d.bon[b] = 1;
+    d.bFnTt[b] = make_float4(0, 0, 0, 0);
+    d.bFsH[b] = d.bFsL[b] = d.bTbH[b] = d.bTbL[b] = make_float4(0, 0, 0, 0);
+    d.bN[b] = f4(n);
+    d.bLever[b] = f4(n * lever);
+}
+
+// ---- solid normals at initialisation (setSolidNormal, core/dataBase.cpp:348-413) ----
+__global__ void kSolidNormals(DeviceState d, float h, float hlo)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= d.ns) return;
+    const int4 ca = d.scell[a];
+    const float4 ha = d.sph[a], la = d.spl[a];
+    const int4 fa = d.sflags[a];
+    const dfl twoH = df_make(2.f * h, 2.f * hlo);
+    const float sigmaG = 5.f * 21.f / (16.f * 3.14159265358979f) / (h * h * h * h * h);
+    const float vFixed = (h / 1.3f) * (h / 1.3f) * (h / 1.3f);
+    KahanF3 th;
+    forStencil(ca, ha, la, d.grid, [&](int hash, bool regular, int hx, int hy, int hz) {
+        const int4 cellHere = make_int4(hx, hy, hz, hash);
+        for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
+            const int b = d.ssorted[p];
+            const int4 cb = regular ? cellHere : d.scell[b];
+            const float4 hb = d.sph[b];
+            // kept when |r_ab| <= 2h
+            if (!withinCut(ca, ha, la, cb, hb, d.spl, b, twoH, d.grid)) continue;
+            const int4 fb = d.sflags[b];
+            float vol;
+            if (!(fa.w & F_MASSIVE) && !(fb.w & F_MASSIVE)) vol = vFixed;                  // both inverse mass <= 1e-10
+            else if (fa.z >= 0 && fa.z == fb.z) vol = 8.f * d.srad[b].x * d.srad[b].x * d.srad[b].x;  // same clump
+            else continue;
+            const float3 r = relF(ca, ha, cb, hb, d.grid);
+            const float rr = len3(r);
+            if (rr < 1.e-10f || rr >= 2.f * h) continue;
+            const float t = 1.f - 0.5f * rr / h;
+            // grad W = -5 sigma t^3 / h^2 r ;  Theta += -V grad W
+            th.add(r * (vol * sigmaG * t * t * t));
+        }
+    });
+    const float3 s = th.sum();
+    const float l = len3(s);
+    d.snormal[a] = l > 1.e-10f ? f4(s / l) : make_float4(0, 0, 0, 0);
+}
+
+}  // namespace
+
+void launchFluidLists(const DeviceState& d, cudaStream_t s)
+{
+    if (d.nf <= 0) return;
+    kFluidLists<<<blocksFor(d.nf, T), T, 0, s>>>(d);
+}
+
+void launchCouplingLists(const DeviceState& d, cudaStream_t s)
+{
+    if (d.nf <= 0 || d.ns <= 0) return;
+    cudaMemsetAsync(d.coupCount, 0, sizeof(int) * d.ns, s);
+    kCoupCount<<<blocksFor(d.nf, 256), 256, 0, s>>>(d);
+    scanExclusive(d.coupCount, d.coupStart, d.ns, d.scanWork, s);
+    cudaMemsetAsync(d.coupCount, 0, sizeof(int) * d.ns, s);
+    kCoupFill<<<blocksFor(d.nf, 256), 256, 0, s>>>(d);
+    kCoupSort<<<blocksFor(d.ns, 256), 256, 0, s>>>(d);
+}
+
+void launchSolidContactList(const DeviceState& d, int par, cudaStream_t s)
+{
+    if (d.ns <= 0) return;
+    kSolidList<false><<<blocksFor(d.ns, T), T, 0, s>>>(d, par);
+    scanExclusive(d.sfcnt, d.sfbase[par], d.ns, d.scanWork, s);
+    scanExclusive(d.srcnt, d.srbase, d.ns, d.scanWork, s);
+    kSolidList<true><<<blocksFor(d.ns, T), T, 0, s>>>(d, par);
+}
+
+// Bond creation from the contact list (addBondData at initialisation,
+// core/dataBase.cpp:270-308), in two launches: flags + exclusive scan give each
+// new bond its index in list order; returns the bond count (synchronises).
+int launchBondFlags(const DeviceState& d, int par, int np, int* flag, int* pos, int* work, cudaStream_t s)
+{
+    if (np <= 0) return 0;
+    kBondFlags<<<blocksFor(np, 256), 256, 0, s>>>(d, par, flag);
+    scanExclusive(flag, pos, np, work, s);
+    int nb = 0;
+    cudaMemcpyAsync(&nb, pos + np, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    return nb;
+}
+
+void launchBondWrite(const DeviceState& d, int par, int np, const int* flag, const int* pos, cudaStream_t s)
+{
+    if (np <= 0 || d.nb <= 0) return;
+    kBondWrite<<<blocksFor(np, 256), 256, 0, s>>>(d, par, flag, pos);
+}
+
+void launchSolidNormals(const DeviceState& d, float h, float hlo, cudaStream_t s)
+{
+    if (d.ns <= 0 || !(h > 0.f)) return;
+    kSolidNormals<<<blocksFor(d.ns, T), T, 0, s>>>(d, h, hlo);
+}
+
+}  // namespace demsph

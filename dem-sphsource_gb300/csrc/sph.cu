@@ -1,0 +1,372 @@
+// WCSPH pair loops: Riemann continuity, Riemann momentum, Shepard density
+// re-initialisation and the SPH->DEM coupling force.
+//
+// Physics restated from core/integrate.cu:3-330 (reference) with the Wendland
+// C2 kernel of core/SPHKernelDEMContactModel.h:5-32.  Algebraic forms used
+// here (equal to the reference's expressions, with fewer operations and no
+// cancellation of the Riemann averages):
+//   grad W(r, h)   = -G r,  G = 5 sigma t^3 / h^2,  t = 1 - |r| / (2h),
+//                    sigma = 21 / (16 pi h^3)        (zero for |r| >= 2h)
+//   continuity, fluid partner j (integrate.cu:75-103):
+//     dRho/dt += -2 rho_i V_j G / (rho_i + rho_j)
+//                * [rho_j (v_i - v_j).r + (P_i - P_j) |r| / c_ij]
+//   continuity, solid partner a (integrate.cu:139-158), with the mirrored
+//   velocity 2 v_a - v_i and the hydrostatic wall pressure P_a:
+//     dRho/dt += -2 rho_i V_a G / (rho_i + rho_a)
+//                * [2 rho_a (v_i - v_a).r + (P_i - P_a) |r| / c_i]
+//   momentum, fluid partner (integrate.cu:185-213):
+//     dv/dt += 2 V_i V_j G / m_i [P* r - gamma_ij (v_i - v_j)]
+//   momentum, solid partner (integrate.cu:251-277) and the per-pair coupling
+//   force (integrate.cu:282-329, = m_i times the same term):
+//     dv/dt += 2 V_i V_a G / m_i [P* r - 2 gamma_i (v_i - v_a)]
+// Sums are Kahan-compensated FP32; positions and velocities are integrated
+// in double-float.  The continuity pass reads every partner's density as of
+// the pass start (dRho is double-buffered).
+#include "kernels.cuh"
+
+namespace demsph {
+
+namespace {
+
+constexpr int T = 128;
+constexpr float KG = 5.f * 21.f / (16.f * 3.14159265358979323846f);  // G = KG t^3 / h^5
+constexpr float SIG = 21.f / (16.f * 3.14159265358979323846f);       // sigma h^3
+
+// Relative position of fluid partner entry e of slot i.
+__device__ __forceinline__ float3 fluidRel(const DeviceState& d, int ps, int i, int4 ci, float4 pi, unsigned e,
+                                           int j, float4 pj)
+{
+    const unsigned code = e & 31u;
+    if (code < 27u) {
+        const int dx = (int)(code % 3u) - 1, dy = (int)((code / 3u) % 3u) - 1, dz = (int)(code / 9u) - 1;
+        return make_float3((pi.x - pj.x) - (float)dx * d.grid.cs.x, (pi.y - pj.y) - (float)dy * d.grid.cs.y,
+                           (pi.z - pj.z) - (float)dz * d.grid.cs.z);
+    }
+    return relF(ci, pi, d.fcell[j], pj, d.grid);
+}
+
+struct SolidPartner {
+    float3 r;      // x_i - x_a
+    float3 v;      // v_a
+    float Pa, rhoa, Va, G, rr;
+    bool inside;
+};
+
+// Wall/solid partner quantities shared by continuity, momentum and coupling.
+__device__ __forceinline__ SolidPartner solidPartner(const DeviceState& d, int4 ci, float4 pi, float hi, float Pi,
+                                                     float rhoi, float rho0i, float ci2, int a)
+{
+    SolidPartner s;
+    const float4 pa = d.sph[a];
+    s.r = relF(ci, pi, d.scell[a], pa, d.grid);
+    const float ra = d.srad[a].x;
+    const float h = 0.5f * (hi + 2.6f * ra);
+    const float r2 = dot3(s.r, s.r);
+    s.inside = r2 < 4.f * h * h;
+    if (!s.inside) return s;
+    s.rr = sqrtf(r2);
+    const float t = 1.f - 0.5f * s.rr / h;
+    const float h2 = h * h;
+    s.G = KG * t * t * t / (h2 * h2 * h);
+    s.v = xyz(d.svh[a]);
+    const float3 na = xyz(d.snormal[a]);
+    const float3 aa = xyz(d.sacc[a]);
+    s.Pa = Pi + rhoi * fmaxf(0.f, dot3(d.g - aa, na)) * dot3(s.r, na);
+    s.rhoa = s.Pa / ci2 + rho0i;
+    s.Va = 8.f * ra * ra * ra;
+    return s;
+}
+
+struct Self {
+    int4 c;
+    float4 p;
+    float3 v;
+    float h, rho0, cs, nu, m, rho, P, V, gam;
+};
+
+__device__ __forceinline__ Self loadSelf(const DeviceState& d, int i, int ps, int vs, int ds)
+{
+    Self o;
+    o.c = d.fcell[i];
+    o.p = d.fph[ps][i];
+    o.v = xyz(d.fvh[vs][i]);
+    const float dr = d.fdrho[ds][i];
+    const float4 par = d.fpar[i];
+    o.h = o.p.w;
+    o.rho0 = par.x;
+    o.cs = par.y;
+    o.nu = par.z;
+    o.m = par.w;
+    o.rho = o.rho0 + dr;
+    o.P = dr * o.cs * o.cs;
+    o.V = o.m / o.rho;
+    o.gam = o.nu * o.rho;
+    return o;
+}
+
+// Position/velocity update in double-float: x += v dt.
+__device__ __forceinline__ void dfAxpy(float4& xh, float4& xl, float4 vh, float4 vl, dfl dt)
+{
+    dfl x = df_add(df_make(xh.x, xl.x), df_mul(df_make(vh.x, vl.x), dt));
+    dfl y = df_add(df_make(xh.y, xl.y), df_mul(df_make(vh.y, vl.y), dt));
+    dfl z = df_add(df_make(xh.z, xl.z), df_mul(df_make(vh.z, vl.z), dt));
+    xh.x = x.hi; xl.x = x.lo;
+    xh.y = y.hi; xl.y = y.lo;
+    xh.z = z.hi; xl.z = z.lo;
+}
+
+// ---- continuity (+ optional drift) ----
+struct ContinuityArgs {
+    int ps, vs, ds, dd;  // position / velocity / density source, density destination
+    int driftTo;         // -1: no drift; else position buffer receiving x + v * drift
+    int velCopyTo;       // -1: none; else velocity buffer receiving a copy of this particle's velocity
+    float dt;
+    dfl drift;
+};
+
+__global__ void __launch_bounds__(T) kContinuity(DeviceState d, ContinuityArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nf || *d.status) return;
+    const Self o = loadSelf(d, i, a.ps, a.vs, a.ds);
+    const int n = d.nf;
+    KahanF acc;
+    const int nff = min(d.ffc[i], d.kff);
+    for (int k = 0; k < nff; ++k) {
+        const unsigned e = d.ff[(size_t)k * n + i];
+        const int j = (int)(e >> 5);
+        const float4 pj = d.fph[a.ps][j];
+        const float3 r = fluidRel(d, a.ps, i, o.c, o.p, e, j, pj);
+        const float h = 0.5f * (o.h + pj.w);
+        const float r2 = dot3(r, r);
+        if (r2 >= 4.f * h * h) continue;
+        const float4 par = d.fpar[j];
+        const float drj = d.fdrho[a.ds][j];
+        const float rhoj = par.x + drj;
+        const float Pj = drj * par.y * par.y;
+        const float Vj = par.w / rhoj;
+        const float rr = sqrtf(r2);
+        const float t = 1.f - 0.5f * rr / h;
+        const float h2 = h * h;
+        const float G = KG * t * t * t / (h2 * h2 * h);
+        const float c = 0.5f * (o.cs + par.y);
+        const float3 vij = o.v - xyz(d.fvh[a.vs][j]);
+        acc.add(-2.f * o.rho * Vj * G / (o.rho + rhoj) * (rhoj * dot3(vij, r) + (o.P - Pj) * rr / c));
+    }
+    const int nfs = min(d.fsc[i], d.kfs);
+    const float ci2 = o.cs * o.cs;
+    for (int k = 0; k < nfs; ++k) {
+        const int sa = d.fs[(size_t)k * n + i];
+        const SolidPartner s = solidPartner(d, o.c, o.p, o.h, o.P, o.rho, o.rho0, ci2, sa);
+        if (!s.inside) continue;
+        acc.add(-2.f * o.rho * s.Va * s.G / (o.rho + s.rhoa) *
+                (2.f * s.rhoa * dot3(o.v - s.v, s.r) + (o.P - s.Pa) * s.rr / o.cs));
+    }
+    d.fdrho[a.dd][i] = d.fdrho[a.ds][i] + a.dt * acc.value();
+    if (a.driftTo >= 0) {
+        float4 xh = d.fph[a.ps][i], xl = d.fpl[a.ps][i];
+        dfAxpy(xh, xl, d.fvh[a.vs][i], d.fvl[a.vs][i], a.drift);
+        d.fph[a.driftTo][i] = xh;
+        d.fpl[a.driftTo][i] = xl;
+    }
+    if (a.velCopyTo >= 0) {
+        d.fvh[a.velCopyTo][i] = d.fvh[a.vs][i];
+        d.fvl[a.velCopyTo][i] = d.fvl[a.vs][i];
+    }
+}
+
+// ---- momentum + kick (dt_f) + drift (dt_f / 2) ----
+// Reads position [1], velocity [0], density [1]; writes acc, velocity [1] and
+// position [0] (the buffers no other thread reads in this pass).
+__global__ void __launch_bounds__(T) kMomentum(DeviceState d, dfl dtf, dfl halfDtf)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nf || *d.status) return;
+    const Self o = loadSelf(d, i, 1, 0, 1);
+    const int n = d.nf;
+    KahanF3 acc;
+    const int nff = min(d.ffc[i], d.kff);
+    for (int k = 0; k < nff; ++k) {
+        const unsigned e = d.ff[(size_t)k * n + i];
+        const int j = (int)(e >> 5);
+        const float4 pj = d.fph[1][j];
+        const float3 r = fluidRel(d, 1, i, o.c, o.p, e, j, pj);
+        const float h = 0.5f * (o.h + pj.w);
+        const float r2 = dot3(r, r);
+        if (r2 >= 4.f * h * h) continue;
+        const float4 par = d.fpar[j];
+        const float drj = d.fdrho[1][j];
+        const float rhoj = par.x + drj;
+        const float Pj = drj * par.y * par.y;
+        const float Vj = par.w / rhoj;
+        const float gj = par.z * rhoj;
+        const float rr = sqrtf(r2);
+        const float t = 1.f - 0.5f * rr / h;
+        const float h2 = h * h;
+        const float G = KG * t * t * t / (h2 * h2 * h);
+        const float c = 0.5f * (o.cs + par.y);
+        const float3 vij = o.v - xyz(d.fvh[0][j]);
+        const float dU = -dot3(vij, r) / rr;  // U_L - U_R
+        const float beta = fminf(3.f * fmaxf(dU, 0.f), c);
+        const float Ps = (o.rho * Pj + rhoj * o.P + o.rho * rhoj * beta * dU) / (o.rho + rhoj);
+        const float gbar = 2.f * o.gam * gj / (o.gam + gj);
+        const float w = 2.f * o.V * Vj * G / o.m;
+        acc.add((r * Ps - vij * gbar) * w);
+    }
+    const int nfs = min(d.fsc[i], d.kfs);
+    const float ci2 = o.cs * o.cs;
+    for (int k = 0; k < nfs; ++k) {
+        const int sa = d.fs[(size_t)k * n + i];
+        const SolidPartner s = solidPartner(d, o.c, o.p, o.h, o.P, o.rho, o.rho0, ci2, sa);
+        if (!s.inside) continue;
+        const float3 via = o.v - s.v;
+        const float dU = -2.f * dot3(via, xyz(d.snormal[sa]));
+        const float beta = fminf(3.f * fmaxf(dU, 0.f), o.cs);
+        const float Ps = (o.rho * s.Pa + s.rhoa * o.P + o.rho * s.rhoa * beta * dU) / (o.rho + s.rhoa);
+        const float w = 2.f * o.V * s.Va * s.G / o.m;
+        acc.add((s.r * Ps - via * (2.f * o.gam)) * w);
+    }
+    const float3 acl = acc.sum() + d.g;
+    d.facc[i] = f4(acl);
+    // kick: v += a dt_f
+    const float4 vh0 = d.fvh[0][i], vl0 = d.fvl[0][i];
+    const dfl vx = df_add(df_make(vh0.x, vl0.x), df_mul_f(dtf, acl.x));
+    const dfl vy = df_add(df_make(vh0.y, vl0.y), df_mul_f(dtf, acl.y));
+    const dfl vz = df_add(df_make(vh0.z, vl0.z), df_mul_f(dtf, acl.z));
+    const float4 vh = make_float4(vx.hi, vy.hi, vz.hi, 0.f), vl = make_float4(vx.lo, vy.lo, vz.lo, 0.f);
+    d.fvh[1][i] = vh;
+    d.fvl[1][i] = vl;
+    // drift: x += v dt_f / 2
+    float4 xh = d.fph[1][i], xl = d.fpl[1][i];
+    dfAxpy(xh, xl, vh, vl, halfDtf);
+    d.fph[0][i] = xh;
+    d.fpl[0][i] = xl;
+}
+
+// ---- Shepard density re-initialisation (integrate.cu:3-53) ----
+__global__ void __launch_bounds__(T) kDensityReinit(DeviceState d, int storeReference)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nf || *d.status) return;
+    const int4 ci = d.fcell[i];
+    const float4 pi = d.fph[0][i];
+    const float hi = pi.w;
+    const int n = d.nf;
+    const float hi3 = hi * hi * hi;
+    const float sig = SIG / hi3;
+    KahanF sum;
+    sum.add(sig);  // W(0, h_i)
+    const int nff = min(d.ffc[i], d.kff);
+    for (int k = 0; k < nff; ++k) {
+        const unsigned e = d.ff[(size_t)k * n + i];
+        const int j = (int)(e >> 5);
+        const float3 r = fluidRel(d, 0, i, ci, pi, e, j, d.fph[0][j]);
+        const float q = len3(r) / hi;
+        if (q >= 2.f) continue;
+        const float t = 1.f - 0.5f * q;
+        sum.add(sig * t * t * t * t * (1.f + 2.f * q));
+    }
+    const float V0i = hi3 / (1.3f * 1.3f * 1.3f);
+    const int nfs = min(d.fsc[i], d.kfs);
+    for (int k = 0; k < nfs; ++k) {
+        const int a = d.fs[(size_t)k * n + i];
+        const float3 r = relF(ci, pi, d.scell[a], d.sph[a], d.grid);
+        const float q = len3(r) / hi;
+        if (q >= 2.f) continue;
+        const float t = 1.f - 0.5f * q;
+        const float ra = d.srad[a].x;
+        sum.add(sig * t * t * t * t * (1.f + 2.f * q) * (8.f * ra * ra * ra) / V0i);
+    }
+    if (storeReference) {
+        d.fsumW0[i] = sum.value();
+    } else {
+        const float rho0 = d.fpar[i].x;
+        const float rhoStar = rho0 + d.fdrho[0][i];
+        const float rho1 = fmaxf(rhoStar, rho0 * sum.value() / d.fsumW0[i]);
+        d.fdrho[0][i] = rho1 - rho0;
+    }
+}
+
+// ---- coupling force, per massive solid: sum over its fluid partners of
+// m_i x (solid term of momentum) (integrate.cu:282-330, gathered per solid
+// as calSolidForceTorque does through fluidSolidRange, :847-854) ----
+__device__ __forceinline__ float3 couplingPairForce(const DeviceState& d, int src, int i, int a, bool& inside)
+{
+    const Self o = loadSelf(d, i, src, 0, src);
+    const SolidPartner s = solidPartner(d, o.c, o.p, o.h, o.P, o.rho, o.rho0, o.cs * o.cs, a);
+    inside = s.inside;
+    if (!s.inside) return make_float3(0.f, 0.f, 0.f);
+    const float3 via = o.v - s.v;
+    const float dU = -2.f * dot3(via, xyz(d.snormal[a]));
+    const float beta = fminf(3.f * fmaxf(dU, 0.f), o.cs);
+    const float Ps = (o.rho * s.Pa + s.rhoa * o.P + o.rho * s.rhoa * beta * dU) / (o.rho + s.rhoa);
+    return (s.r * Ps - via * (2.f * o.gam)) * (2.f * o.V * s.Va * s.G);
+}
+
+__global__ void kCoupling(DeviceState d, int src)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= d.ns || *d.status) return;
+    KahanF3 f;
+    for (int p = d.coupStart[a], e = d.coupStart[a + 1]; p < e; ++p) {
+        bool inside;
+        const float3 fi = couplingPairForce(d, src, d.coupList[p], a, inside);
+        if (inside) f.add(fi);
+    }
+    d.sfcoup[a] = f4(f.sum());
+}
+
+// Per-pair coupling force in the fluid's list order (for export only).
+__global__ void kCouplingPairs(DeviceState d, int src, float4* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nf) return;
+    const int m = min(d.fsc[i], d.kfs);
+    for (int k = 0; k < m; ++k) {
+        bool inside;
+        const float3 f = couplingPairForce(d, src, i, d.fs[(size_t)k * d.nf + i], inside);
+        out[(size_t)k * d.nf + i] = f4(f);
+    }
+}
+
+}  // namespace
+
+void launchDensityReinit(const DeviceState& d, int iStep, cudaStream_t s)
+{
+    if (d.nf <= 0) return;
+    kDensityReinit<<<blocksFor(d.nf, T), T, 0, s>>>(d, iStep == 1 ? 1 : 0);
+}
+
+void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStream_t s)
+{
+    if (d.nf <= 0) return;
+    ContinuityArgs a;
+    a.dt = (float)(0.5 * dtf);
+    a.drift = df_from_double(0.5 * dtf);
+    if (which == 0) {  // first half step: densities 0 -> 1, drift positions 0 -> 1
+        a.ps = 0; a.vs = 0; a.ds = 0; a.dd = 1; a.driftTo = 1; a.velCopyTo = -1;
+    } else {           // second half step: densities 1 -> 0, velocity 1 -> 0
+        a.ps = 0; a.vs = 1; a.ds = 1; a.dd = 0; a.driftTo = -1; a.velCopyTo = 0;
+    }
+    kContinuity<<<blocksFor(d.nf, T), T, 0, s>>>(d, a);
+}
+
+void launchMomentumPass(const DeviceState& d, double dtf, cudaStream_t s)
+{
+    if (d.nf <= 0) return;
+    kMomentum<<<blocksFor(d.nf, T), T, 0, s>>>(d, df_from_double(dtf), df_from_double(0.5 * dtf));
+}
+
+void launchCoupling(const DeviceState& d, int src, cudaStream_t s)
+{
+    if (d.nf <= 0 || d.ns <= 0) return;
+    kCoupling<<<blocksFor(d.ns, 128), 128, 0, s>>>(d, src);
+}
+
+void launchCouplingPairForces(const DeviceState& d, int src, float4* out, cudaStream_t s)
+{
+    if (d.nf <= 0 || d.ns <= 0) return;
+    kCouplingPairs<<<blocksFor(d.nf, 128), 128, 0, s>>>(d, src, out);
+}
+
+}  // namespace demsph

@@ -1,0 +1,276 @@
+/*
+ * demsph_gb300.h - C ABI of the GB300-native coupled DEM-SPH step.
+ *
+ * The reference (kaiqideng/DEM-SPHSource) has no plugin or FFI interface: its
+ * engine boundary is five C++ host functions that take the device data by
+ * reference,
+ *     neighborSearch                       core/neighborSearch.h:28
+ *     solidIntegrateBeforeContact          core/integrate.h:43
+ *     fluidIntegrate                       core/integrate.h:19
+ *     calSolidContactAfterFluidIntegrate   core/integrate.h:41
+ *     solidIntegrateAfterContact           core/integrate.h:45
+ * plus the DeviceData life cycle (copy / uploadState / release,
+ * core/deviceStructs.h) driven by class dataBase (core/dataBase.cpp:192-260,
+ * 434-449).  This header replaces exactly that boundary with plain C: an
+ * opaque engine handle, host pointers and sizes, and a status code on every
+ * call.  Nothing here aborts; device memory is owned by the engine.
+ *
+ * Conventions
+ *   - double3 data is passed as 3 interleaved doubles per element (the memory
+ *     layout of std::vector<double3>), quaternions as 4 and symmetric
+ *     matrices as 6 (xx, yy, zz, xy, xz, yz) - the reference's host layouts.
+ *   - Indices are the reference's: fluid and solid particles numbered in the
+ *     order they were added (core/hostStructs.h).
+ *   - Output pointers may be NULL to skip a field.
+ *   - Calls on one engine are not thread-safe; different engines are
+ *     independent.  Work is issued on the engine's own CUDA stream; download
+ *     and export calls synchronise that stream.
+ *
+ * The scene builder (demsph_builder_*) is the host-side mirror of the
+ * reference's setup API (class dataBase, core/dataBase.h:33-219): the same
+ * calls, argument meanings and validation, producing the arrays the engine
+ * (and the FP64 oracle) take.
+ */
+#ifndef DEMSPH_GB300_H
+#define DEMSPH_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define DEMSPH_API __attribute__((visibility("default")))
+#else
+#define DEMSPH_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum demsph_status {
+    DEMSPH_OK = 0,
+    DEMSPH_ERR_ARGUMENT = 1,      /* bad pointer, index, size or parameter */
+    DEMSPH_ERR_STATE = 2,         /* call out of order (e.g. a step before initialize) */
+    DEMSPH_ERR_CUDA = 3,          /* a CUDA runtime call failed; see demsph_last_error */
+    DEMSPH_ERR_NO_DEVICE = 4,     /* no usable CUDA device / wrong architecture */
+    DEMSPH_ERR_CAPACITY = 5,      /* a neighbour or contact list overflowed; the engine grew it, re-run the step */
+    DEMSPH_ERR_OUT_OF_MEMORY = 6,
+    DEMSPH_ERR_TIMEOUT = 7        /* a bounded device-side wait gave up */
+} demsph_status;
+
+/* Reference behaviours that can be switched off (all kept by default). */
+enum {
+    /* integrate.cu:540 returns from the wall loop at the first wall a particle
+       does not touch, skipping later walls; the fix continues the loop. */
+    DEMSPH_FIX_WALL_LOOP = 1,
+    /* integrate.cu:919 reads clump orientations that are never integrated;
+       the fix integrates the quaternion (FP64) each half step. */
+    DEMSPH_FIX_CLUMP_ROTATION = 2
+};
+
+/* Everything class dataBase holds after the setup calls (HostData,
+   core/hostStructs.h:387-398) plus the solver parameters, as host arrays. */
+typedef struct demsph_scene {
+    /* spatial grid and gravity (dataBase members, core/dataBase.h:243-246) */
+    double domain_origin[3];
+    double domain_size[3];
+    double gravity[3];
+    double time_step;
+    int fluid_integrate_gap;
+    double maximum_time;
+    int num_frames;
+
+    /* fluid particles (HostFluid, core/hostStructs.h:48-75) */
+    int n_fluid;
+    const double* fluid_position;        /* 3n */
+    const double* fluid_velocity;        /* 3n */
+    const double* fluid_acceleration;    /* 3n */
+    const double* fluid_smoothing_length;/* n: points.effectiveRadii */
+    const double* fluid_rho0;            /* n */
+    const double* fluid_drho;            /* n */
+    const double* fluid_sound_speed;     /* n */
+    const double* fluid_nu;              /* n: kinematic viscosity */
+
+    /* solid particles (HostSolid, core/hostStructs.h:77-117) */
+    int n_solid;
+    const double* solid_position;        /* 3n */
+    const double* solid_velocity;        /* 3n */
+    const double* solid_acceleration;    /* 3n */
+    const double* solid_normal;          /* 3n */
+    const double* solid_torque;          /* 3n */
+    const double* solid_angular_velocity;/* 3n */
+    const double* solid_effective_radius;/* n: points.effectiveRadii */
+    const double* solid_radius;          /* n */
+    const double* solid_inverse_mass;    /* n */
+    const int* solid_material;           /* n */
+    const int* solid_cluster;            /* n, -1 = none */
+    const int* solid_clump;              /* n, -1 = none */
+    const int* solid_is_dummy;           /* n, 1 = dummy wall particle */
+
+    /* clumps (HostClump, core/hostStructs.h:119-152) */
+    int n_clump;
+    const double* clump_centroid;        /* 3n */
+    const double* clump_velocity;        /* 3n */
+    const double* clump_acceleration;    /* 3n */
+    const double* clump_angular_velocity;/* 3n */
+    const double* clump_torque;          /* 3n */
+    const double* clump_orientation;     /* 4n: q0 q1 q2 q3 */
+    const double* clump_inverse_inertia; /* 6n */
+    const double* clump_inverse_mass;    /* n */
+    const int* clump_pebble_start;       /* n */
+    const int* clump_pebble_end;         /* n */
+
+    /* infinite walls (HostInfiniteWall, core/hostStructs.h:154-174) */
+    int n_wall;
+    const double* wall_point;            /* 3n */
+    const double* wall_normal;           /* 3n */
+    const int* wall_material;            /* n */
+
+    /* contact models per material pair (HostSolidContactModel,
+       core/hostStructs.h:291-385); n_material*(n_material+1)/2 pair slots,
+       slot index = getCombinedIndex (core/hostStructs.h:369-384) */
+    int n_material;
+    const double* hertzian;  /* 8 per slot: E G res k_r_k_s k_t_k_s mu_s mu_r mu_t */
+    const double* linear;    /* 11 per slot: k_n k_s k_r k_t d_n d_s d_r d_t mu_s mu_r mu_t */
+    const double* bonded;    /* 6 per slot: gamma E k_n_k_s sigma_s C mu */
+} demsph_scene;
+
+typedef struct demsph_options {
+    int device;                  /* CUDA device ordinal (gpuPara.deviceIndex) */
+    int fluid_neighbors_max;     /* fluid partners kept per fluid particle; 0 = 160 */
+    int fluid_solids_max;        /* solid partners kept per fluid particle; 0 = 96 */
+    int solid_contacts_per_particle; /* contact list capacity / solid count; 0 = 16 */
+    int fixes;                   /* DEMSPH_FIX_* bits; 0 = reference behaviour */
+    int debug;                   /* bit 0: keep each step's per-pair coupling forces for export */
+} demsph_options;
+
+typedef struct demsph_counts {
+    long long fluid_pairs;       /* fluid2Fluid.num: half list, i < j */
+    long long fluid_solid_pairs; /* fluid2Solid.num */
+    long long solid_pairs;       /* solid2Solid.num */
+    long long bonds;             /* solidBond2Solid.num */
+    long long bonds_intact;      /* bonds with isBonded == 1 */
+    int grid_cells;              /* spatialGrid.num (cells + overflow bucket) */
+    int grid_size[3];
+    double cell_size[3];
+} demsph_counts;
+
+typedef struct demsph_engine demsph_engine;
+typedef struct demsph_builder demsph_builder;
+
+/* ---- status ---- */
+DEMSPH_API const char* demsph_status_string(int status);
+/* Last error message recorded on this engine ("" if none); valid until the next call. */
+DEMSPH_API const char* demsph_last_error(const demsph_engine* e);
+/* Library version string. */
+DEMSPH_API const char* demsph_version(void);
+
+/* ---- scene builder: the reference's setup API (core/dataBase.h:33-219) ---- */
+/* HostSolidContactModel(n_material) as in solverBase::initialize (core/solverBase.cpp:16). */
+DEMSPH_API demsph_builder* demsph_builder_new(int n_material);
+DEMSPH_API void demsph_builder_free(demsph_builder* b);
+DEMSPH_API const char* demsph_builder_last_error(const demsph_builder* b);
+DEMSPH_API int demsph_builder_set_domain(demsph_builder* b, const double origin[3], const double size[3]); /* dataBase.h:93 */
+DEMSPH_API int demsph_builder_set_gravity(demsph_builder* b, const double g[3]);                         /* dataBase.h:105 */
+DEMSPH_API int demsph_builder_set_time_step(demsph_builder* b, double dt);                               /* dataBase.h:68 */
+DEMSPH_API int demsph_builder_set_maximum_time(demsph_builder* b, double t);                             /* dataBase.h:38 */
+DEMSPH_API int demsph_builder_set_num_frames(demsph_builder* b, int n);                                  /* dataBase.h:53 */
+DEMSPH_API int demsph_builder_set_fluid_integrate_gap(demsph_builder* b, int gap);                       /* dataBase.h:83 */
+DEMSPH_API int demsph_builder_set_hertzian(demsph_builder* b, int mi, int mj, double E, double G, double res,
+                                double k_r_k_s, double k_t_k_s, double mu_s, double mu_r,
+                                double mu_t);                                                 /* dataBase.h:111 */
+DEMSPH_API int demsph_builder_set_linear(demsph_builder* b, int mi, int mj, double k_n, double k_s, double k_r,
+                              double k_t, double d_n, double d_s, double d_r, double d_t, double mu_s,
+                              double mu_r, double mu_t);                                      /* dataBase.h:130 */
+DEMSPH_API int demsph_builder_set_bonded(demsph_builder* b, int mi, int mj, double E, double k_n_k_s, double gamma,
+                              double sigma_s, double C, double mu);                           /* dataBase.h:152 */
+DEMSPH_API int demsph_builder_add_fluid(demsph_builder* b, int n, const double* xyz, const double velocity[3],
+                             double smoothing_length, double density, double sound_speed,
+                             double kinematic_viscosity);                                     /* dataBase.cpp:3 */
+DEMSPH_API int demsph_builder_add_dummy_wall(demsph_builder* b, int n, const double* xyz, double spacing); /* dataBase.cpp:19 */
+DEMSPH_API int demsph_builder_add_solid(demsph_builder* b, int n, const double* xyz, const double velocity[3],
+                             double radius, double density, int material);                    /* dataBase.cpp:33 */
+DEMSPH_API int demsph_builder_add_infinite_wall(demsph_builder* b, const double point[3], const double normal[3],
+                                     int material);                                           /* dataBase.cpp:55 */
+DEMSPH_API int demsph_builder_add_cylinder_wall(demsph_builder* b, const double point[3], const double axis[3],
+                                     const double angular_velocity[3], double radius, int material); /* dataBase.cpp:69 */
+DEMSPH_API int demsph_builder_add_cluster(demsph_builder* b, int n, const double* xyz, const double* radius,
+                               const double* density, const double velocity[3], int material); /* dataBase.cpp:84 */
+DEMSPH_API int demsph_builder_add_clump(demsph_builder* b, int n, const double* xyz, const double* radius,
+                             const double centroid[3], const double velocity[3],
+                             const double angular_velocity[3], double mass, const double inertia6[6],
+                             int material);                                                   /* dataBase.cpp:120 */
+/* Points *out at the builder's arrays (valid until the builder changes or is freed). */
+DEMSPH_API int demsph_builder_scene(const demsph_builder* b, demsph_scene* out);
+
+/* ---- engine life cycle ---- */
+/* DeviceData::copy of every part + dataBase::setSpatialGrids/buildDeviceData
+   (core/dataBase.cpp:415-449).  opts may be NULL (defaults). */
+DEMSPH_API int demsph_create(const demsph_scene* scene, const demsph_options* opts, demsph_engine** out);
+/* DeviceData::release (core/deviceStructs.h:1033-1048). */
+DEMSPH_API int demsph_destroy(demsph_engine* e);
+/* Device part of solverBase::initialize (core/solverBase.cpp:29-31):
+   neighborSearch(dev, 0, 1), addBondData (core/dataBase.cpp:270-346) and
+   setSolidNormal (core/dataBase.cpp:348-413), all on the GPU. */
+DEMSPH_API int demsph_initialize(demsph_engine* e);
+
+/* ---- the five step functions (one call each per solverBase::update) ---- */
+DEMSPH_API int demsph_neighbor_search(demsph_engine* e, int i_step, int gap);               /* neighborSearch.cu:314-382 */
+DEMSPH_API int demsph_solid_integrate_before_contact(demsph_engine* e, double dt);          /* integrate.cu:964-980 */
+DEMSPH_API int demsph_fluid_integrate(demsph_engine* e, double dt, int i_step, int gap);    /* integrate.cu:385-421 */
+DEMSPH_API int demsph_solid_contact_after_fluid_integrate(demsph_engine* e, double dt);     /* integrate.cu:940-962 */
+DEMSPH_API int demsph_solid_integrate_after_contact(demsph_engine* e, double dt);           /* integrate.cu:982-998 */
+/* n_steps consecutive solverBase::update() bodies (core/solverBase.cpp:47-58)
+   for i_step = first_step .. first_step+n_steps-1, without the driver hook;
+   replayed as a CUDA graph when use_graph != 0. */
+DEMSPH_API int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph);
+/* Waits for queued work; returns the first deferred error (e.g. capacity). */
+DEMSPH_API int demsph_synchronize(demsph_engine* e);
+
+/* ---- state transfer (fluid/solid/clump uploadState, core/deviceStructs.h) ---- */
+DEMSPH_API int demsph_download_fluids(demsph_engine* e, double* position, double* velocity, double* acceleration,
+                           double* drho);
+DEMSPH_API int demsph_download_solids(demsph_engine* e, double* position, double* velocity, double* acceleration,
+                           double* normal, double* torque, double* angular_velocity);
+DEMSPH_API int demsph_download_clumps(demsph_engine* e, double* centroid, double* velocity, double* acceleration,
+                           double* angular_velocity, double* torque, double* orientation);
+/* Overwrite the dynamic state (inverse of the downloads); NULL skips a field. */
+DEMSPH_API int demsph_upload_fluids(demsph_engine* e, const double* position, const double* velocity, const double* drho);
+DEMSPH_API int demsph_upload_solids(demsph_engine* e, const double* position, const double* velocity,
+                         const double* angular_velocity);
+
+/* ---- run-time setters of class dataBase ---- */
+DEMSPH_API int demsph_set_gravity(demsph_engine* e, const double g[3]);                              /* dataBase.h:105-109 */
+DEMSPH_API int demsph_set_contact_models(demsph_engine* e, const demsph_scene* tables);              /* dataBase.h:111-167 */
+DEMSPH_API int demsph_set_clump_velocity(demsph_engine* e, int clump, const double v[3]);            /* dataBase.h:169-182 */
+DEMSPH_API int demsph_add_external_force(demsph_engine* e, int solid, const double force[3]);        /* dataBase.cpp:179-195 */
+DEMSPH_API int demsph_add_global_damping(demsph_engine* e, int solid, double c_d);                   /* dataBase.cpp:197-224 */
+
+/* ---- artefacts in the reference's index space and order (for parity) ---- */
+DEMSPH_API int demsph_get_counts(demsph_engine* e, demsph_counts* out);
+/* objectHash after buildHashSpans (core/neighborSearch.cu:71-113): per particle
+   the cell key (hash.value, sorted) and the sorted particle index (hash.index),
+   and cellStart/cellEnd per cell (-1 = empty).  which: 0 fluid, 1 solid. */
+DEMSPH_API int demsph_export_cell_hash(demsph_engine* e, int which, int* hash_value, int* hash_index, int* cell_start,
+                            int* cell_end);
+/* fluid2Fluid half list (core/neighborSearch.cu:115-220): prefix = inclusive
+   prefix sum per fluid particle; pairs in the reference's order. */
+DEMSPH_API int demsph_export_fluid_pairs(demsph_engine* e, int* prefix, int* pointed, int* pointing, long long capacity);
+/* fluid2Solid list and the per-pair coupling force (core/integrate.cu:282-330). */
+DEMSPH_API int demsph_export_fluid_solid_pairs(demsph_engine* e, int* prefix, int* pointed, int* pointing, double* force,
+                                    long long capacity);
+/* solid2Solid half list with forces, torques and springs
+   (core/neighborSearch.cu:222-312, core/integrate.cu:423-512). */
+DEMSPH_API int demsph_export_solid_pairs(demsph_engine* e, int* prefix, int* pointed, int* pointing, double* force,
+                              double* torque, double* sliding, double* rolling, double* torsion,
+                              long long capacity);
+/* interactionBonded (core/deviceStructs.h:714-789). */
+DEMSPH_API int demsph_export_bonds(demsph_engine* e, int* pointed, int* pointing, int* is_bonded, double* normal_force,
+                        double* torsion_torque, double* shear_force, double* bending_torque,
+                        double* contact_normal, double* contact_point, long long capacity);
+/* Shepard reference sums sumW0 (core/integrate.cu:44-47). */
+DEMSPH_API int demsph_export_fluid_sumw0(demsph_engine* e, double* sumw0);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DEMSPH_GB300_H */
