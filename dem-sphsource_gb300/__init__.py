@@ -192,14 +192,20 @@ class Builder:
 
     def addCluster(self, p, r, rho, v, mat):
         p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
-        r = np.ascontiguousarray(r, dtype=np.float64)
-        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        r = np.ascontiguousarray(r, dtype=np.float64).ravel()
+        rho = np.ascontiguousarray(rho, dtype=np.float64).ravel()
+        if len(r) != len(p) or len(rho) != len(p):  # the C call takes one count for all three arrays
+            raise DemSphError(1, "addCluster: Error: the size of position, velocity, and radius vectors must be "
+                                 "the same when adding a cluster.")
         self._chk(self.lib.demsph_builder_add_cluster(_P(self.h), _I(len(p)), _ptr(p), _ptr(r), _ptr(rho), _v3(v),
                                                       _I(mat)), "addCluster")
 
     def addClump(self, p, r, c, v, w, mass, I6, mat):
         p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
-        r = np.ascontiguousarray(r, dtype=np.float64)
+        r = np.ascontiguousarray(r, dtype=np.float64).ravel()
+        if len(r) != len(p):
+            raise DemSphError(1, "addClump: Error: the size of position and radius vectors must be the same when "
+                                 "adding a clump.")
         I6 = (_D * 6)(*map(float, I6))
         self._chk(self.lib.demsph_builder_add_clump(_P(self.h), _I(len(p)), _ptr(p), _ptr(r), _v3(c), _v3(v), _v3(w),
                                                     _D(mass), I6, _I(mat)), "addClump")

@@ -60,10 +60,12 @@ __device__ __forceinline__ float3 torsionSpring(float3 prev, float3 vel, float3 
     return s;
 }
 
-// Linear / Hertz-Mindlin dispatch (integrate.cu:463-505).
-__device__ __forceinline__ void contactLaw(const Tables& tab, int slot, float3& F, float3& T, float3& es, float3& er,
-                                           float3& et, float3 vc, float3 wr, float3 n, float delta, float m, float R,
-                                           float dt)
+// Linear / Hertz-Mindlin dispatch (integrate.cu:463-505).  Also returns the
+// tangential (sliding) part Ft of F: a lever arm along n turns F into the
+// torque s (n x Ft) exactly, without the FP32 residue of n x (Fn n).
+__device__ __forceinline__ void contactLaw(const Tables& tab, int slot, float3& F, float3& Ft, float3& T, float3& es,
+                                           float3& er, float3& et, float3 vc, float3 wr, float3 n, float delta, float m,
+                                           float R, float dt)
 {
     if (!(delta > 0.f)) {
         es = er = et = make_float3(0.f, 0.f, 0.f);
@@ -106,17 +108,19 @@ __device__ __forceinline__ void contactLaw(const Tables& tab, int slot, float3& 
     const float Dm = 2.f * R;
     const float3 vt = n * (Dm * dot3(wr, n));
     et = torsionSpring(et, vt, n, aN, mut, kt, ct, dt);
-    const float3 Ft = et * (-kt) - vt * ct;
+    const float3 Fto = et * (-kt) - vt * ct;
     F = Fn + Fs;
-    T = Tr + Ft * Dm;
+    Ft = Fs;
+    T = Tr + Fto * Dm;
 }
 
 struct PairGeom {
     float3 n;        // unit vector from B to A
     float delta;     // overlap r_A + r_B - |x_A - x_B|
     float dist;
-    float3 leverA;   // contact point - x_A
-    float3 leverB;   // contact point - x_B
+    float sA, sB;    // contact point - x_A = sA n, contact point - x_B = sB n
+    float3 leverA;
+    float3 leverB;
 };
 __device__ __forceinline__ PairGeom pairGeometry(const DeviceState& d, int a, int b)
 {
@@ -128,14 +132,29 @@ __device__ __forceinline__ PairGeom pairGeometry(const DeviceState& d, int a, in
     g.delta = del.hi + del.lo;
     g.dist = dist.hi + dist.lo;
     g.n = g.dist > 0.f ? toF3(r) / g.dist : make_float3(0.f, 0.f, 0.f);
-    g.leverA = g.n * (-0.5f * (g.dist + ra.x - rb.x));
-    g.leverB = g.n * (0.5f * (g.dist + rb.x - ra.x));
+    g.sA = -0.5f * (g.dist + ra.x - rb.x);
+    g.sB = 0.5f * (g.dist + rb.x - ra.x);
+    g.leverA = g.n * g.sA;
+    g.leverB = g.n * g.sB;
     return g;
 }
 
-__device__ __forceinline__ float3 velAt(const DeviceState& d, int i, float3 lever)
+// (v_a - v_b) from the double-float velocities: grains moving together have
+// nearly equal velocities, whose float parts alone would cancel.
+__device__ __forceinline__ float3 velDiff(const DeviceState& d, int a, int b)
 {
-    return xyz(d.svh[i]) + cross3(xyz(d.swh[i]), lever);
+    const float4 ha = d.svh[a], la = d.svl[a], hb = d.svh[b], lb = d.svl[b];
+    return make_float3((ha.x - hb.x) + (la.x - lb.x), (ha.y - hb.y) + (la.y - lb.y), (ha.z - hb.z) + (la.z - lb.z));
+}
+__device__ __forceinline__ float3 spinDiff(const DeviceState& d, int a, int b)
+{
+    const float4 ha = d.swh[a], la = d.swl[a], hb = d.swh[b], lb = d.swl[b];
+    return make_float3((ha.x - hb.x) + (la.x - lb.x), (ha.y - hb.y) + (la.y - lb.y), (ha.z - hb.z) + (la.z - lb.z));
+}
+// velocity of b's contact point relative to a's: v_a + w_a x lever_a - (v_b + w_b x lever_b)
+__device__ __forceinline__ float3 contactVel(const DeviceState& d, int a, int b, float3 leverA, float3 leverB)
+{
+    return velDiff(d, a, b) + cross3(xyz(d.swh[a]), leverA) - cross3(xyz(d.swh[b]), leverB);
 }
 
 __global__ void __launch_bounds__(T) kPairContacts(DeviceState d, int par, float dt)
@@ -148,19 +167,20 @@ __global__ void __launch_bounds__(T) kPairContacts(DeviceState d, int par, float
         const float4 ra = d.srad[a], rb = d.srad[b];
         const float R = ra.x * rb.x / (ra.x + rb.x);
         const float m = 1.f / (d.sph[a].w + d.sph[b].w);
-        const float3 vc = velAt(d, a, g.leverA) - velAt(d, b, g.leverB);
-        const float3 wr = xyz(d.swh[a]) - xyz(d.swh[b]);
+        const float3 vc = contactVel(d, a, b, g.leverA, g.leverB);
+        const float3 wr = spinDiff(d, a, b);
         float3 es = xyz(d.spring[par][0][k]), er = xyz(d.spring[par][1][k]), et = xyz(d.spring[par][2][k]);
-        float3 F = make_float3(0.f, 0.f, 0.f), Tq = F;
+        float3 F = make_float3(0.f, 0.f, 0.f), Ft = F, Tq = F;
         const int slot = tableSlot(d.tab, d.sflags[a].x, d.sflags[b].x);
-        contactLaw(d.tab, slot, F, Tq, es, er, et, vc, wr, g.n, g.delta, m, R, dt);
+        contactLaw(d.tab, slot, F, Ft, Tq, es, er, et, vc, wr, g.n, g.delta, m, R, dt);
         d.spring[par][0][k] = f4(es);
         d.spring[par][1][k] = f4(er);
         d.spring[par][2][k] = f4(et);
         d.pF[k] = f4(F);
         d.pT[k] = f4(Tq);
-        d.pTA[k] = f4(Tq + cross3(g.leverA, F));
-        d.pTB[k] = f4(Tq + cross3(g.leverB, F));
+        const float3 nxF = cross3(g.n, Ft);
+        d.pTA[k] = f4(Tq + nxF * g.sA);
+        d.pTB[k] = f4(Tq + nxF * g.sB);
     }
 }
 
@@ -213,7 +233,7 @@ __global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
     const float3 n = g.n;
     const float3 n0 = xyz(d.bN[b]);
     const float3 wi = xyz(d.swh[i]), wj = xyz(d.swh[j]);
-    const float3 vc = velAt(d, i, g.leverA) - velAt(d, j, g.leverB);
+    const float3 vc = contactVel(d, i, j, g.leverA, g.leverB);
     const float4 ri = d.srad[i], rj = d.srad[j];
     const int ms = tableSlot(d.tab, d.sflags[i].x, d.sflags[j].x);
     const float* B = d.tab.bd + 6 * ms;  // gamma E knks sigma C mu
@@ -237,7 +257,7 @@ __global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
     const float3 dtg = vc * dt - dn;
     dfl Fn = df_add_f(df_make(FnTt.x, FnTt.y), -dot3(dn * (kn * Ab), n));
     addDF3(FsH, FsL, dtg * (-ks * Ab));
-    const float3 wr = wi - wj;
+    const float3 wr = spinDiff(d, i, j);
     const float3 dn2 = n * (dot3(wr, n) * dt);
     const float3 dt2 = wr * dt - dn2;
     dfl Tt = df_add_f(df_make(FnTt.z, FnTt.w), -dot3(dn2 * (ks * Jb), n));
@@ -260,10 +280,11 @@ __global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
     // add onto the pair's force and torque (integrate.cu:802-803)
     const float3 F = n * fn + Fs;
     const float3 Tq = n * tt + Tb;
+    const float3 nxF = cross3(n, Fs);  // the lever is along n: n x (fn n) = 0
     d.pF[slot] = f4(xyz(d.pF[slot]) + F);
     d.pT[slot] = f4(xyz(d.pT[slot]) + Tq);
-    d.pTA[slot] = f4(xyz(d.pTA[slot]) + Tq + cross3(g.leverA, F));
-    d.pTB[slot] = f4(xyz(d.pTB[slot]) + Tq + cross3(g.leverB, F));
+    d.pTA[slot] = f4(xyz(d.pTA[slot]) + Tq + nxF * g.sA);
+    d.pTB[slot] = f4(xyz(d.pTB[slot]) + Tq + nxF * g.sB);
 }
 
 // Wall overlap r - ((x - p) . n) in double-float.
@@ -326,14 +347,14 @@ __global__ void __launch_bounds__(T) kGatherWalls(DeviceState d, int par, float 
             const float3 lever = n * (-(rad.x - delta));
             const float3 vc = v + cross3(w, lever);
             float3 es = xyz(d.wspring[0][h]), er = xyz(d.wspring[1][h]), et = xyz(d.wspring[2][h]);
-            float3 Fw = make_float3(0.f, 0.f, 0.f), Tw = Fw;
+            float3 Fw = make_float3(0.f, 0.f, 0.f), Fwt = Fw, Tw = Fw;
             const int slot = tableSlot(d.tab, fa.x, d.wmat[k]);
-            contactLaw(d.tab, slot, Fw, Tw, es, er, et, vc, w, n, delta, 1.f / im, rad.x, dt);
+            contactLaw(d.tab, slot, Fw, Fwt, Tw, es, er, et, vc, w, n, delta, 1.f / im, rad.x, dt);
             d.wspring[0][h] = f4(es);
             d.wspring[1][h] = f4(er);
             d.wspring[2][h] = f4(et);
             acc = acc + Fw * im;
-            tq = tq + Tw + cross3(lever, Fw);
+            tq = tq + Tw + cross3(n, Fwt) * (-(rad.x - delta));
         }
     }
     d.sacc[a] = f4(acc);

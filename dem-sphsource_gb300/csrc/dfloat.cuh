@@ -84,6 +84,13 @@ __device__ __forceinline__ dfl df_mul_f(dfl a, float b)
     p.lo = __fmaf_rn(a.lo, b, p.lo);
     return df_fast_two_sum(p.hi, p.lo);
 }
+// a / b: float quotient plus one correction from the double-float remainder.
+__device__ __forceinline__ dfl df_div(dfl a, dfl b)
+{
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const dfl r = df_sub(a, df_mul_f(b, q1));
+    return df_fast_two_sum(q1, __fdiv_rn(r.hi, b.hi));
+}
 // sqrt by one Newton correction of the float root: x + (a - x^2) / (2x).
 __device__ __forceinline__ dfl df_sqrt(dfl a)
 {

@@ -294,6 +294,16 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
         return DEMSPH_ERR_ARGUMENT;
     demsph_options o{};
     if (opt) o = *opt;
+    // Material ids index the contact tables (getCombinedIndex, core/hostStructs.h:369-384);
+    // the reference reads outside the table for ids >= n_material, so reject them here.
+    for (int i = 0; i < sc->n_solid; ++i)
+        if (sc->solid_material[i] < 0 || sc->solid_material[i] >= sc->n_material) return DEMSPH_ERR_ARGUMENT;
+    for (int k = 0; k < sc->n_wall; ++k)
+        if (sc->wall_material[k] < 0 || sc->wall_material[k] >= sc->n_material) return DEMSPH_ERR_ARGUMENT;
+    for (int c = 0; c < sc->n_clump; ++c)
+        if (sc->clump_pebble_start[c] < 0 || sc->clump_pebble_end[c] > sc->n_solid ||
+            sc->clump_pebble_start[c] > sc->clump_pebble_end[c])
+            return DEMSPH_ERR_ARGUMENT;
     demsph_engine* e = new demsph_engine();
     e->debug = o.debug;
     int rc = checkDevice(e, o.device);
@@ -402,13 +412,13 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             }
             d.facc = dalloc<float4>(nf, e->owned);
             d.fpar = dalloc<float4>(nf, e->owned);
-            d.fsumW0 = dalloc<float>(nf, e->owned);
+            d.fsumW0 = dalloc<float2>(nf, e->owned);
             d.fid = dalloc<int>(nf, e->owned);
             d.fslot = dalloc<int>(nf, e->owned);
             d.tcell = dalloc<int4>(nf, e->owned);
             d.tacc = dalloc<float4>(nf, e->owned);
             d.tpar = dalloc<float4>(nf, e->owned);
-            d.tsumW0 = dalloc<float>(nf, e->owned);
+            d.tsumW0 = dalloc<float2>(nf, e->owned);
             d.tid = dalloc<int>(nf, e->owned);
             d.fkey = dalloc<int>(nf, e->owned);
             d.fslotInCell = dalloc<int>(nf, e->owned);
@@ -617,8 +627,7 @@ int demsph_initialize(demsph_engine* e)
         for (void* p : tmp) cudaFree(p);
     }
     // normals of walls and clump pebbles (setSolidNormal), kernel length = largest fluid h
-    const dfl h = df_from_double(e->hmax);
-    launchSolidNormals(d, h.hi, h.lo, e->stream);
+    launchSolidNormals(d, e->hmax, e->stream);
     CK(cudaStreamSynchronize(e->stream));
     CK(cudaGetLastError());
     e->initialized = true;

@@ -60,8 +60,7 @@ __global__ void kSolidOut(DeviceState d, double* out)  // 18 doubles per solid
     o[15] = (double)wh.x + wl.x; o[16] = (double)wh.y + wl.y; o[17] = (double)wh.z + wl.z;
 }
 
-// Writes the state given in original order (FP64) into the engine; NaN in the
-// first component of an entry leaves that entry untouched.
+// Writes the state given in original order (FP64) into the engine.
 __global__ void kFluidIn(DeviceState d, const double* pos, const double* vel, const double* drho)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -555,11 +554,18 @@ int demsph_export_fluid_sumw0(demsph_engine* e, double* out)
     ENGINE_GUARD(e)
     DeviceState& d = e->d;
     CK(cudaStreamSynchronize(e->stream));
-    std::vector<float> w;
+    // sumW0 = sigma(h) * S0 with sigma = 21 / (16 pi h^3) (core/SPHKernelDEMContactModel.h:5-13)
+    std::vector<float2> w;
+    std::vector<float4> ph, pl;
     std::vector<int> id;
     d2h(w, d.fsumW0, d.nf);
+    d2h(ph, d.fph[0], d.nf);
+    d2h(pl, d.fpl[0], d.nf);
     d2h(id, d.fid, d.nf);
-    for (int s = 0; s < d.nf; ++s) out[id[s]] = w[s];
+    for (int s = 0; s < d.nf; ++s) {
+        const double h = (double)ph[s].w + (double)pl[s].w;
+        out[id[s]] = 21.0 / (16.0 * 3.1415926535897931 * h * h * h) * ((double)w[s].x + (double)w[s].y);
+    }
     return DEMSPH_OK;
     ENGINE_END(e)
 }

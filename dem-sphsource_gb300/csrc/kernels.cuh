@@ -29,14 +29,14 @@ struct DeviceState {
     float* fdrho[2];
     float4* facc;
     float4* fpar;
-    float* fsumW0;
+    float2* fsumW0;          // Shepard reference sum / sigma(h), double-float
     int* fid;                // slot -> original index
     int* fslot;              // original index -> slot
     // reorder temporaries
     int4* tcell;
     float4* tacc;
     float4* tpar;
-    float* tsumW0;
+    float2* tsumW0;
     int* tid;
     int* fkey;
     int* fslotInCell;
@@ -139,7 +139,7 @@ void launchCouplingLists(const DeviceState& d, cudaStream_t s);
 void launchSolidContactList(const DeviceState& d, int parity, cudaStream_t s);
 int launchBondFlags(const DeviceState& d, int parity, int np, int* flag, int* pos, int* work, cudaStream_t s);
 void launchBondWrite(const DeviceState& d, int parity, int np, const int* flag, const int* pos, cudaStream_t s);
-void launchSolidNormals(const DeviceState& d, float h, float hlo, cudaStream_t s);
+void launchSolidNormals(const DeviceState& d, double h, cudaStream_t s);
 
 // sph.cu
 void launchDensityReinit(const DeviceState& d, int iStep, cudaStream_t s);
@@ -158,6 +158,16 @@ void launchGatherWalls(const DeviceState& d, int parity, float dt, cudaStream_t 
 void launchClumpForce(const DeviceState& d, cudaStream_t s);
 void launchSolidIntegrate(const DeviceState& d, double dt, bool beforeContact, cudaStream_t s);
 void launchStepDone(const DeviceState& d, cudaStream_t s);
+
+// Absolute FP64 position of solid i (cell origin + double-float offset).
+__device__ __forceinline__ double3 solidAbsPos(const DeviceState& d, int i)
+{
+    const int4 c = d.scell[i];
+    const float4 h = d.sph[i], l = d.spl[i];
+    return make_double3(d.minB[0] + c.x * d.cs[0] + ((double)h.x + (double)l.x),
+                        d.minB[1] + c.y * d.cs[1] + ((double)h.y + (double)l.y),
+                        d.minB[2] + c.z * d.cs[2] + ((double)h.z + (double)l.z));
+}
 
 inline int blocksFor(long long n, int threads) { return (int)((n + threads - 1) / threads > 0 ? (n + threads - 1) / threads : 1); }
 

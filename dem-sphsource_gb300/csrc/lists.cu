@@ -275,41 +275,46 @@ __global__ void kBondWrite(DeviceState d, int par, const int* flag, const int* p
 }
 
 // ---- solid normals at initialisation (setSolidNormal, core/dataBase.cpp:348-413) ----
-__global__ void kSolidNormals(DeviceState d, float h, float hlo)
+// FP64, once per scene: inside a three-layer wall the kernel-gradient sum of
+// the middle layer cancels exactly, and the reference's absolute 1e-10
+// threshold then sees an FP64 residue (~1e-15: zero normal) where FP32 would
+// leave ~1e-6 (a spurious unit normal).
+__global__ void kSolidNormals(DeviceState d, double h)
 {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= d.ns) return;
     const int4 ca = d.scell[a];
     const float4 ha = d.sph[a], la = d.spl[a];
     const int4 fa = d.sflags[a];
-    const dfl twoH = df_make(2.f * h, 2.f * hlo);
-    const float sigmaG = 5.f * 21.f / (16.f * 3.14159265358979f) / (h * h * h * h * h);
-    const float vFixed = (h / 1.3f) * (h / 1.3f) * (h / 1.3f);
-    KahanF3 th;
-    forStencil(ca, ha, la, d.grid, [&](int hash, bool regular, int hx, int hy, int hz) {
-        const int4 cellHere = make_int4(hx, hy, hz, hash);
+    const double3 pa = solidAbsPos(d, a);
+    const double PI = 3.1415926535897931;
+    const double sigma = 21.0 / (16.0 * PI * h * h * h);
+    const double vFixed = pow(h / 1.3, 3);
+    double tx = 0, ty = 0, tz = 0;
+    forStencil(ca, ha, la, d.grid, [&](int hash, bool, int, int, int) {
         for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
             const int b = d.ssorted[p];
-            const int4 cb = regular ? cellHere : d.scell[b];
-            const float4 hb = d.sph[b];
-            // kept when |r_ab| <= 2h
-            if (!withinCut(ca, ha, la, cb, hb, d.spl, b, twoH, d.grid)) continue;
+            const double3 pb = solidAbsPos(d, b);
+            const double rx = pa.x - pb.x, ry = pa.y - pb.y, rz = pa.z - pb.z;
+            const double rr = sqrt(rx * rx + ry * ry + rz * rz);
+            if (rr > 2 * h) continue;
             const int4 fb = d.sflags[b];
-            float vol;
-            if (!(fa.w & F_MASSIVE) && !(fb.w & F_MASSIVE)) vol = vFixed;                  // both inverse mass <= 1e-10
-            else if (fa.z >= 0 && fa.z == fb.z) vol = 8.f * d.srad[b].x * d.srad[b].x * d.srad[b].x;  // same clump
+            double vol;
+            if (!(fa.w & F_MASSIVE) && !(fb.w & F_MASSIVE)) vol = vFixed;  // both inverse mass <= 1e-10
+            else if (fa.z >= 0 && fa.z == fb.z) vol = pow(2.0 * (double)d.srad[b].x + 2.0 * (double)d.srad[b].y, 3.0);
             else continue;
-            const float3 r = relF(ca, ha, cb, hb, d.grid);
-            const float rr = len3(r);
-            if (rr < 1.e-10f || rr >= 2.f * h) continue;
-            const float t = 1.f - 0.5f * rr / h;
-            // grad W = -5 sigma t^3 / h^2 r ;  Theta += -V grad W
-            th.add(r * (vol * sigmaG * t * t * t));
+            if (rr < 1.e-10 || rr >= 2.0 * h) continue;  // gradient of W is zero
+            const double q = rr / h, t = 1.0 - 0.5 * q;
+            const double dWdq = -2.0 * pow(t, 3) * (1.0 + 2.0 * q) + 2.0 * pow(t, 4);
+            const double f = sigma * dWdq / h / rr;
+            tx -= vol * f * rx;
+            ty -= vol * f * ry;
+            tz -= vol * f * rz;
         }
     });
-    const float3 s = th.sum();
-    const float l = len3(s);
-    d.snormal[a] = l > 1.e-10f ? f4(s / l) : make_float4(0, 0, 0, 0);
+    const double l = sqrt(tx * tx + ty * ty + tz * tz);
+    d.snormal[a] = l > 1.e-10 ? make_float4((float)(tx / l), (float)(ty / l), (float)(tz / l), 0.f)
+                              : make_float4(0, 0, 0, 0);
 }
 
 }  // namespace
@@ -360,10 +365,10 @@ void launchBondWrite(const DeviceState& d, int par, int np, const int* flag, con
     kBondWrite<<<blocksFor(np, 256), 256, 0, s>>>(d, par, flag, pos);
 }
 
-void launchSolidNormals(const DeviceState& d, float h, float hlo, cudaStream_t s)
+void launchSolidNormals(const DeviceState& d, double h, cudaStream_t s)
 {
-    if (d.ns <= 0 || !(h > 0.f)) return;
-    kSolidNormals<<<blocksFor(d.ns, T), T, 0, s>>>(d, h, hlo);
+    if (d.ns <= 0 || !(h > 0.0)) return;
+    kSolidNormals<<<blocksFor(d.ns, T), T, 0, s>>>(d, h);
 }
 
 }  // namespace demsph

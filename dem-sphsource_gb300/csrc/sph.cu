@@ -244,46 +244,64 @@ __global__ void __launch_bounds__(T) kMomentum(DeviceState d, dfl dtf, dfl halfD
 }
 
 // ---- Shepard density re-initialisation (integrate.cu:3-53) ----
+// sumW = sigma(h_i) S with S = 1 + sum_j f(q_j) + sum_a f(q_a) V0_a / V0_i,
+// f(q) = (1 - q/2)^4 (1 + 2q).  The update rho0 S / S0 - rho0 is a difference
+// of two nearly equal sums (1e-3 apart), so S is carried in double-float from
+// double-float distances, and S - S0 is formed before dividing.
+__device__ __forceinline__ dfl shepardTerm(dfl r, dfl invh)
+{
+    const dfl q = df_mul(r, invh);
+    const dfl t = df_add_f(df_mul_f(q, -0.5f), 1.0f);
+    const dfl t2 = df_mul(t, t);
+    return df_mul(df_mul(t2, t2), df_add_f(df_mul_f(q, 2.0f), 1.0f));
+}
+
 __global__ void __launch_bounds__(T) kDensityReinit(DeviceState d, int storeReference)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.nf || *d.status) return;
     const int4 ci = d.fcell[i];
-    const float4 pi = d.fph[0][i];
-    const float hi = pi.w;
+    const float4 pi = d.fph[0][i], li = d.fpl[0][i];
+    const dfl h = df_make(pi.w, li.w);
+    const dfl invh = df_div(df_make(1.f), h);
+    const dfl twoH = df_add(h, h);
     const int n = d.nf;
-    const float hi3 = hi * hi * hi;
-    const float sig = SIG / hi3;
-    KahanF sum;
-    sum.add(sig);  // W(0, h_i)
+    dfl S = df_make(1.f);
     const int nff = min(d.ffc[i], d.kff);
     for (int k = 0; k < nff; ++k) {
         const unsigned e = d.ff[(size_t)k * n + i];
         const int j = (int)(e >> 5);
-        const float3 r = fluidRel(d, 0, i, ci, pi, e, j, d.fph[0][j]);
-        const float q = len3(r) / hi;
-        if (q >= 2.f) continue;
-        const float t = 1.f - 0.5f * q;
-        sum.add(sig * t * t * t * t * (1.f + 2.f * q));
+        const unsigned code = e & 31u;
+        int4 cj;
+        if (code < 27u)
+            cj = make_int4(ci.x + (int)(code % 3u) - 1, ci.y + (int)((code / 3u) % 3u) - 1, ci.z + (int)(code / 9u) - 1, 0);
+        else
+            cj = d.fcell[j];
+        const dfl r = dfNorm(relDF(ci, pi, li, cj, d.fph[0][j], d.fpl[0][j], d.grid));
+        if (df_ge0(df_sub(r, twoH))) continue;  // q >= 2
+        S = df_add(S, shepardTerm(r, invh));
     }
-    const float V0i = hi3 / (1.3f * 1.3f * 1.3f);
+    // V0_a / V0_i = (2 r_a / (h_i / 1.3))^3 = (2.6 r_a / h_i)^3
+    const dfl k26 = df_from_double(2.6);
     const int nfs = min(d.fsc[i], d.kfs);
     for (int k = 0; k < nfs; ++k) {
         const int a = d.fs[(size_t)k * n + i];
-        const float3 r = relF(ci, pi, d.scell[a], d.sph[a], d.grid);
-        const float q = len3(r) / hi;
-        if (q >= 2.f) continue;
-        const float t = 1.f - 0.5f * q;
-        const float ra = d.srad[a].x;
-        sum.add(sig * t * t * t * t * (1.f + 2.f * q) * (8.f * ra * ra * ra) / V0i);
+        const dfl r = dfNorm(relDF(ci, pi, li, d.scell[a], d.sph[a], d.spl[a], d.grid));
+        if (df_ge0(df_sub(r, twoH))) continue;
+        const float4 ra = d.srad[a];
+        const dfl x = df_mul(df_mul(k26, df_make(ra.x, ra.y)), invh);
+        const dfl vr = df_mul(df_mul(x, x), x);
+        S = df_add(S, df_mul(shepardTerm(r, invh), vr));
     }
     if (storeReference) {
-        d.fsumW0[i] = sum.value();
+        d.fsumW0[i] = make_float2(S.hi, S.lo);
     } else {
+        const float2 s0 = d.fsumW0[i];
+        const dfl diff = df_sub(S, df_make(s0.x, s0.y));
         const float rho0 = d.fpar[i].x;
-        const float rhoStar = rho0 + d.fdrho[0][i];
-        const float rho1 = fmaxf(rhoStar, rho0 * sum.value() / d.fsumW0[i]);
-        d.fdrho[0][i] = rho1 - rho0;
+        // max(rho*, rho0 S / S0) - rho0 = max(dRho, rho0 (S - S0) / S0)
+        const float cand = rho0 * ((diff.hi + diff.lo) / s0.x);
+        d.fdrho[0][i] = fmaxf(d.fdrho[0][i], cand);
     }
 }
 

@@ -1,0 +1,156 @@
+"""GPU engine against the FP64 oracle on the same scenes, through the C ABI.
+
+Integer artefacts must be identical; floating-point results must agree within
+the tolerances stated in tests/parity.py.  The oracle itself is pinned to the
+reference's own kernels (tests/test_oracle_golden.py).
+"""
+import numpy as np
+import pytest
+
+from parity import (DRHO_TOL, DRIFT_TOL, FORCE_TOL, POS_TOL, compare_integer_artefacts, engine_artefacts,
+                    oracle_for, pair_floors, rel_pair_error, state_errors)
+
+pytestmark = pytest.mark.gpu
+
+SCENES = ("tiny_dam_break", "tiny_granular", "tiny_coupled")
+
+
+def _setup(ds, scenes, name, **opts):
+    recipe = getattr(scenes, name)()
+    b, sc = ds.build_scene(recipe)
+    eng = ds.Engine(sc, **opts)
+    orc = oracle_for(sc, fixes=opts.get("fixes", 0))
+    return recipe, b, sc, eng, orc
+
+
+def _spacing(recipe):
+    return recipe.meta.get("dx", 2.0e-3)
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_initialize_artefacts_identical(ds, scenes, name):
+    recipe, b, sc, eng, orc = _setup(ds, scenes, name)
+    eng.initialize()
+    orc.initialize()
+    bad, art = compare_integer_artefacts(eng, orc)
+    assert bad == [], f"integer artefacts differ after initialize: {bad}"
+    if eng.ns:
+        s = eng.download_solids()
+        assert np.max(np.abs(s["normal"] - orc.get("solid.normal"))) < 1e-5
+        if len(art["bond.pointed"]):
+            assert np.allclose(art["bond.contactNormal"], orc.get("bond.contactNormal"), atol=1e-6)
+            assert np.allclose(art["bond.contactPoint"], orc.get("bond.contactPoint"), atol=1e-9)
+
+
+def _check_step(eng, orc, sc, dx, step, dt, tol_force, tol_pos):
+    err = state_errors(eng, orc, dx, step, dt)
+    for k, v in err.items():
+        tol = {"fluid.pos": tol_pos, "solid.pos": tol_pos, "fluid.dRho": DRHO_TOL, "solid.normal": 1e-5}.get(k, tol_force)
+        assert v <= tol, f"step {step}: {k} error {v:.3e} > {tol:.1e}"
+    art = engine_artefacts(eng)
+    fl = pair_floors(sc, dt, step)
+    if eng.ns and len(art["ss.pointed"]):
+        assert rel_pair_error(art["ss.force"], orc.get("ss.force"), fl["force"]) <= tol_force
+        assert rel_pair_error(art["ss.torque"], orc.get("ss.torque"), fl["torque"]) <= tol_force
+        assert rel_pair_error(art["ss.sliding"], orc.get("ss.sliding"), fl["spring"]) <= tol_force
+    if eng.ns and len(art["bond.pointed"]):
+        assert rel_pair_error(art["bond.normalForce"], orc.get("bond.normalForce"), fl["force"]) <= tol_force
+        assert rel_pair_error(art["bond.shearForce"], orc.get("bond.shearForce"), fl["force"]) <= tol_force
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_one_step_within_force_tolerance(ds, scenes, name):
+    """One update() from the same initial state: every force, torque, spring,
+    density and state within the per-step tolerance, integer artefacts equal."""
+    recipe, b, sc, eng, orc = _setup(ds, scenes, name)
+    eng.initialize()
+    orc.initialize()
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    eng.step(dt, 1, gap)
+    orc.update(dt, 1, 1, gap)
+    bad, _ = compare_integer_artefacts(eng, orc, skip_fluid_hash=(1 % gap != 0))
+    assert bad == [], f"integer artefacts differ: {bad}"
+    _check_step(eng, orc, sc, _spacing(recipe), 1, dt, FORCE_TOL, POS_TOL)
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_ten_steps_artefacts_equal_drift_bounded(ds, scenes, name):
+    """Ten update() calls through the five stage calls: integer artefacts equal
+    after every step; floating-point drift within DRIFT_TOL."""
+    recipe, b, sc, eng, orc = _setup(ds, scenes, name)
+    eng.initialize()
+    orc.initialize()
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for step in range(1, 11):
+        eng.step(dt, step, gap)
+        orc.update(dt, step, 1, gap)
+        bad, _ = compare_integer_artefacts(eng, orc, skip_fluid_hash=(step % gap != 0))
+        assert bad == [], f"step {step}: integer artefacts differ: {bad}"
+        _check_step(eng, orc, sc, _spacing(recipe), step, dt, DRIFT_TOL, 1e-8)
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_graph_batch_equals_staged_calls(ds, scenes, name):
+    """demsph_update (CUDA graph over whole periods) gives the same bits as the
+    five stage calls per step."""
+    recipe, b, sc, e1, _ = _setup(ds, scenes, name)
+    e2 = ds.Engine(sc)
+    e1.initialize()
+    e2.initialize()
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    n = 10 * gap * 2 + 3
+    for s in range(1, n + 1):
+        e1.step(dt, s, gap)
+    e2.update(dt, 1, n, gap, use_graph=True)
+    if e1.nf:
+        for a, c in zip(e1.download_fluids(), e2.download_fluids()):
+            assert np.array_equal(a, c)
+    if e1.ns:
+        s1, s2 = e1.download_solids(), e2.download_solids()
+        for k in s1:
+            assert np.array_equal(s1[k], s2[k]), k
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_deterministic(ds, scenes, name):
+    recipe, b, sc, e1, _ = _setup(ds, scenes, name)
+    e2 = ds.Engine(sc)
+    for e in (e1, e2):
+        e.initialize()
+        e.update(sc.time_step, 1, 12, sc.fluid_integrate_gap, use_graph=False)
+    if e1.nf:
+        assert all(np.array_equal(a, c) for a, c in zip(e1.download_fluids(), e2.download_fluids()))
+    if e1.ns:
+        s1, s2 = e1.download_solids(), e2.download_solids()
+        assert all(np.array_equal(s1[k], s2[k]) for k in s1)
+
+
+def test_list_overflow_grows_and_matches(ds, scenes):
+    """With lists far too small the engine grows them and re-runs; the result is
+    the same as with ample lists."""
+    recipe = scenes.tiny_coupled()
+    b, sc = ds.build_scene(recipe)
+    small = ds.Engine(sc, fluid_neighbors_max=4, fluid_solids_max=2, solid_contacts_per_particle=1)
+    big = ds.Engine(sc)
+    for e in (small, big):
+        e.initialize()
+        e.update(sc.time_step, 1, 30, sc.fluid_integrate_gap, use_graph=True)
+    for a, c in zip(small.download_fluids(), big.download_fluids()):
+        assert np.array_equal(a, c)
+    s1, s2 = small.download_solids(), big.download_solids()
+    assert all(np.array_equal(s1[k], s2[k]) for k in s1)
+
+
+def test_drift_bounded_over_run(ds, scenes):
+    """Forty steps of the coupled scene: the engine stays within bounded
+    distance of the FP64 oracle (no systematic FP32 drift)."""
+    recipe, b, sc, eng, orc = _setup(ds, scenes, "tiny_coupled")
+    eng.initialize()
+    orc.initialize()
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    eng.update(dt, 1, 40, gap)
+    orc.update(dt, 1, 40, gap)
+    err = state_errors(eng, orc, recipe.meta["dx"], 40, dt)
+    assert err["fluid.pos"] < 1e-7, err
+    assert err["solid.pos"] < 1e-7, err
+    assert err["fluid.dRho"] < 1e-5, err
