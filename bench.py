@@ -1,0 +1,431 @@
+#!/usr/bin/env python3
+"""Benchmark: particle-updates/s of the coupled DEM-SPH step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config 0|1|2]
+
+One step is one solverBase::update() of the scene (core/solverBase.cpp:47-67):
+neighbour search, the two solid half-step integrations, the fluid step (every
+`gap` steps) and the contact phase.  particle-updates/s counts every mobile
+particle once per step it is advanced: N_fluid for each fluid step plus the
+solids with non-zero inverse mass for every step (dummy wall particles are
+not counted).
+
+Workloads (synthetic, seeded, generated by dem-sphsource_gb300/scenes.py):
+  0  48k-fluid WCSPH dam break (dx 0.01 m, 3-layer dummy walls)
+  1  Hertz-Mindlin settle: 200k lognormal spheres + 5k four-pebble clumps (default)
+  2  coupled dam break: 1.0M fluid (dx 0.004 m) against 64 bonded 8^3 cubes
+
+`value` is measured with the scene resident in HBM: K steps replayed as CUDA
+graphs on the engine's stream, bracketed by CUDA events.  `e2e` is the same
+metric through the C ABI with host buffers: every step uploads the dynamic
+state from pinned host memory, runs the step and downloads it again.
+`roofline` times each stage with CUDA events (an uncaptured pass) and relates
+the dominant stage's algorithmic bytes to the measured HBM copy bandwidth.
+`cpu_baseline` is the FP64 oracle (a CPU restatement of the reference's step;
+the reference has no CPU solver) on all host cores, on a bounded sample.
+
+--impl reference times that CPU implementation alone on the same workload
+(the reference's own code is CUDA and is not available on the GPU machine).
+Under torchrun (N > 1) every rank runs an independent replica of the scene on
+its own GPU (the step has no inter-GPU exchange); `value` is the sum over ranks
+divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def _package():
+    name = "dem_sphsource_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    d = os.path.join(ROOT, "dem-sphsource_gb300")
+    spec = importlib.util.spec_from_file_location(name, os.path.join(d, "__init__.py"),
+                                                  submodule_search_locations=[d])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+WORKLOADS = {
+    0: ("dam_break_48k", "WCSPH dam break: tank 1.6x0.4x0.6 m, column 0.4x0.4x0.3 m, dx 0.01 m, 3-layer walls"),
+    1: ("granular_settle_200k_5k", "Hertz-Mindlin settle: 200k lognormal spheres (median 1 mm, sigma 0.2) + 5k "
+                                   "4-pebble clumps, floor + 4 walls"),
+    2: ("coupled_dam_break_1M_64cubes", "1.0M fluid (dx 0.004 m) dam break onto 64 bonded 8^3 sphere cubes"),
+}
+
+
+def make_recipe(config):
+    import dem_sphsource_gb300.scenes as scenes
+    if config == 0:
+        return scenes.dam_break()
+    if config == 1:
+        return scenes.granular_settle()
+    if config == 2:
+        return scenes.coupled_dam_break()
+    raise ValueError(config)
+
+
+def mobile_counts(scene):
+    import numpy as np
+    nf = scene.n_fluid
+    ns = scene.n_solid
+    if ns:
+        im = np.ctypeslib.as_array(scene.solid_inverse_mass, shape=(ns,))
+        dummy = np.ctypeslib.as_array(scene.solid_is_dummy, shape=(ns,))
+        n_mobile = int(((im > 0) & (dummy == 0)).sum())
+        n_dummy = int((dummy == 1).sum())
+    else:
+        n_mobile = n_dummy = 0
+    return nf, n_mobile, n_dummy
+
+
+def updates_for(first, n, gap, nf, n_mobile):
+    fluid_steps = sum(1 for s in range(first, first + n) if s % gap == 0)
+    return nf * fluid_steps + n_mobile * n
+
+
+# ---- clocks during the timed region -------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- algorithmic bytes per stage (compulsory traffic) -------------------------
+def stage_bytes(stage, c):
+    """Bytes one launch of `stage` must move at least, from the scene counts `c`."""
+    P, Ns, Nf, Nb = c["solid_pairs"], c["n_solid_active"], c["n_fluid"], c["bonds"]
+    kff = c.get("fluid_partners", 0.0)
+    kfs = c.get("fluid_solid_partners", 0.0)
+    table = {
+        # per pair: ids 8 + springs in 48 + springs out 48 + F T TA TB 64; per active solid 9 float4 reads
+        "pair_contacts": 168 * P + 144 * Ns,
+        # per active solid: cell ph pl rad flags 80 + counts 8 + bases 12; per pair: A B 8 + springs 48 in + 48 out + history ids 4 + reverse 4
+        "solid_contact_list": 100 * Ns + 112 * P,
+        # per pair: F + TA forward, F + TB reverse (64) + partner id and search (8); per solid: bases 12 + flags 16 + ph 16 + acc torque out 32
+        "gather_walls": 72 * P + 76 * Ns,
+        # per solid: cell ph pl r/w 96 + key slot 8 + scatter 12 + rank 12 + sorted 4
+        "solid_hash_sort": 132 * c["n_solid"],
+        # per solid: ph pl vh vl wh wl acc torque flags rad (10 float4 read, 6 written)
+        "integrate_before": 256 * c["n_solid"],
+        "integrate_after": 256 * c["n_solid"],
+        # per fluid particle: list entries 4/partner + own 112 + one neighbour copy 52 + out 4..64
+        "continuity": (4 * (kff + kfs) + 200) * Nf,
+        "momentum": (4 * (kff + kfs) + 260) * Nf,
+        "density_reinit": (4 * (kff + kfs) + 120) * Nf,
+        "fluid_lists": (4 * (kff + kfs) + 64) * Nf,
+        "fluid_hash_reorder": 496 * Nf,
+        "coupling_lists": 8 * kfs * Nf,
+        "coupling_force": 64 * c.get("coupling_pairs", 0) + 96 * Ns,
+        "bonds": 160 * Nb,
+        "clump_force": 64 * c.get("n_pebbles", 0),
+    }
+    return table.get(stage)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def load_traffic(stage):
+    """Measured DRAM bytes per unit for a stage, from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(stage)
+    except (OSError, ValueError):
+        return None
+
+
+# ---- CPU baseline: the FP64 oracle ------------------------------------------------------------
+def cpu_baseline(scene, gap, dt, budget_s, nf, n_mobile):
+    from oracle import oracle as orc_mod
+    threads = os.cpu_count() or 1
+    orc_mod.set_threads(threads)
+    orc = orc_mod.OracleSolver(scene)
+    orc.initialize()
+    # one timed step to size the sample
+    t0 = time.perf_counter()
+    orc.update(dt, 1, 1, gap)
+    t1 = time.perf_counter() - t0
+    n = max(1, min(1000, int(budget_s / max(t1, 1e-6))))
+    if gap > 1:
+        n = max(n, gap)  # cover at least one fluid step
+    t0 = time.perf_counter()
+    orc.update(dt, 2, n, gap)
+    el = time.perf_counter() - t0
+    ups = updates_for(2, n, gap, nf, n_mobile) / el
+    return {"value": ups, "unit": "particle-updates/s", "cores": threads, "kind": "port",
+            "sample": f"{n} consecutive steps (2..{n + 1}) of the full workload after one warm-up step; "
+                      f"FP64 oracle, OpenMP over particles"}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--config", type=int, choices=(0, 1, 2), default=1)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--profile-steps", type=int, default=40)
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline stepping")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    workload, desc = WORKLOADS[args.config]
+
+    ds = _package()
+    recipe = make_recipe(args.config)
+    builder, scene = ds.build_scene(recipe)
+    dt, gap = scene.time_step, scene.fluid_integrate_gap
+    nf, n_mobile, n_dummy = mobile_counts(scene)
+    base_config = {"workload": workload, "description": desc, "n_fluid": nf, "n_solid_mobile": n_mobile,
+                   "n_dummy_wall": n_dummy, "n_clump": scene.n_clump, "dt": dt, "fluid_integrate_gap": gap,
+                   "l2": "working set larger than L2 (129 MB) for configs 1 and 2; config 0 is L2-resident",
+                   "parallelism": f"replicas x{args.gpus}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(scene, gap, dt, args.cpu_budget, nf, n_mobile)
+        step_ms = None
+        upd_per_step = updates_for(1, 10 * gap, gap, nf, n_mobile) / (10 * gap)
+        if cb["value"] > 0:
+            step_ms = 1000.0 * upd_per_step / cb["value"]
+        print(json.dumps({
+            "metric": "particle-updates/s", "value": cb["value"], "unit": "particle-updates/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic", "config": base_config,
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "particle-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference's step exists only as CUDA kernels; its CPU restatement (the FP64 oracle) is "
+                    "timed on the host cores"}))
+        return
+
+    import numpy as np
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    device = local if world > 1 else 0
+    torch.cuda.set_device(device)
+
+    eng = ds.Engine(scene, device=device)
+    eng.initialize()
+    step = 1
+    eng.update(dt, step, args.warmup, gap, use_graph=True)
+    step += args.warmup
+    eng.synchronize()
+
+    stream = torch.cuda.ExternalStream(eng.stream_ptr(), device=device)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = eng.kernel_launches()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(device) as clocks:
+        ev0.record(stream)
+        eng.update(dt, step, args.steps, gap, use_graph=True)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    launches = eng.kernel_launches() - launches0
+    ms = ev0.elapsed_time(ev1)
+    updates = updates_for(step, args.steps, gap, nf, n_mobile)
+    step += args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        u = torch.tensor([float(updates)], device="cuda")
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        updates = float(u.item())
+    value = updates / (ms / 1000.0)
+
+    # ---- stage timing pass (uncaptured, CUDA events per stage) for the roofline and latency ----
+    eng.set_profiling(True)
+    eng.profile_report()
+    per_step = []
+    for k in range(args.profile_steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.update(dt, step, 1, gap, use_graph=False)
+        e1.record(stream)
+        e1.synchronize()
+        per_step.append(e0.elapsed_time(e1))
+        step += 1
+    stages = eng.profile_report()
+    eng.set_profiling(False)
+    c = eng.counts()
+    counts = {"solid_pairs": c.solid_pairs, "n_solid": scene.n_solid, "n_solid_active": n_mobile,
+              "n_fluid": nf, "bonds": c.bonds,
+              "fluid_partners": 2.0 * c.fluid_pairs / max(nf, 1), "fluid_solid_partners": c.fluid_solid_pairs / max(nf, 1),
+              "n_pebbles": n_mobile if scene.n_clump else 0}
+    dom = max(stages.items(), key=lambda kv: kv[1][1]) if stages else None
+    peak, peak_kind = load_peaks()
+    roofline = None
+    if dom:
+        name, (n_launch, tot_ms) = dom
+        avg_ms = tot_ms / max(n_launch, 1)
+        alg = stage_bytes(name, counts)
+        achieved = alg / (avg_ms / 1000.0) / 1e9 if alg else None
+        tr = load_traffic(name)
+        traffic = None
+        if tr and tr.get("bytes_per_unit") is not None:
+            traffic = tr["bytes_per_unit"] * counts.get(tr.get("unit_count", "solid_pairs"), 0)
+        total_ms = sum(v[1] for v in stages.values())
+        roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                    "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
+                    "fallback 6.8 TB/s", "avg_launch_ms": avg_ms, "algorithmic_bytes_per_launch": alg,
+                    "stage_share": {k: round(v[1] / total_ms, 4) for k, v in sorted(stages.items(),
+                                                                                     key=lambda kv: -kv[1][1])}}
+
+    # ---- end to end through the C ABI with host buffers ----
+    ne = max(1, args.e2e_steps)
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    bi = bo = 0
+    if scene.n_solid:
+        sp, sv, sw = pin((scene.n_solid, 3)), pin((scene.n_solid, 3)), pin((scene.n_solid, 3))
+        eng.download_solids(out={"pos": sp, "vel": sv, "angvel": sw})
+        bi += 3 * sp.nbytes
+        bo += 3 * sp.nbytes
+    if nf:
+        fp, fv, fd = pin((nf, 3)), pin((nf, 3)), pin((nf,))
+        eng.download_fluids(out=(fp, fv, None, fd))
+        bi += fp.nbytes + fv.nbytes + fd.nbytes
+        bo += fp.nbytes + fv.nbytes + fd.nbytes
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(ne):
+        if scene.n_solid:
+            eng.upload_solids(sp, sv, sw)
+        if nf:
+            eng.upload_fluids(fp, fv, fd)
+        eng.update(dt, step, 1, gap, use_graph=False)
+        step += 1
+        if scene.n_solid:
+            eng.download_solids(out={"pos": sp, "vel": sv, "angvel": sw})
+        if nf:
+            eng.download_fluids(out=(fp, fv, None, fd))
+    e2e_s = time.perf_counter() - t0
+    e2e_updates = updates_for(step - ne, ne, gap, nf, n_mobile)
+    e2e_val = e2e_updates / e2e_s
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_val = e2e_updates * world / float(t.item())
+
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(scene, gap, dt, args.cpu_budget, nf, n_mobile)
+
+    if rank == 0:
+        per_step.sort()
+        cfg = dict(base_config)
+        cfg.update({"solid_pairs": c.solid_pairs, "fluid_pairs_half": c.fluid_pairs,
+                    "fluid_solid_pairs": c.fluid_solid_pairs, "bonds": c.bonds,
+                    "timing": "CUDA events on the engine stream; K steps replayed as CUDA graphs",
+                    "precision": "FP32 arithmetic with Kahan sums; double-float positions, velocities, overlaps "
+                                 "and bond accumulators; FP64 clump rigid bodies"})
+        out = {
+            "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic", "config": cfg, "impl": "ours",
+            "p50_step_ms": per_step[len(per_step) // 2] if per_step else None,
+            "p99_step_ms": per_step[min(len(per_step) - 1, int(math.ceil(0.99 * len(per_step))) - 1)]
+            if per_step else None,
+            "roofline": roofline, "cpu_baseline": cb,
+            "e2e": {"value": e2e_val, "unit": "particle-updates/s", "h2d_bytes_per_step": bi,
+                    "d2h_bytes_per_step": bo, "steps": ne,
+                    "path": "demsph_upload_* + demsph_update(1 step) + demsph_download_* per step, pinned host "
+                            "buffers, FP64 reference layout"},
+            "gpu_launches": launches, "clocks": clocks.summary(),
+        }
+        print(json.dumps(out))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -102,8 +102,10 @@ def load_library():
     lib.demsph_builder_new.restype = _P
     lib.demsph_builder_last_error.restype = C.c_char_p
     lib.demsph_builder_last_error.argtypes = [_P]
-    for name in dir(lib):
-        pass
+    lib.demsph_stream.restype = _P
+    lib.demsph_stream.argtypes = [_P]
+    lib.demsph_kernel_launches.restype = C.c_longlong
+    lib.demsph_kernel_launches.argtypes = [_P]
     _lib = lib
     return lib
 
@@ -294,19 +296,46 @@ class Engine:
     def synchronize(self):
         self._chk(self.lib.demsph_synchronize(self.h), "demsph_synchronize")
 
+    # ---- timing ----
+    def stream_ptr(self):
+        """Address of the engine's cudaStream_t (for CUDA events around its work)."""
+        return int(self.lib.demsph_stream(self.h) or 0)
+
+    def kernel_launches(self):
+        return int(self.lib.demsph_kernel_launches(self.h))
+
+    def set_profiling(self, on):
+        self._chk(self.lib.demsph_set_profiling(self.h, _I(1 if on else 0)), "set_profiling")
+
+    def profile_report(self):
+        """{stage: (launches, total_ms)} since the last report."""
+        buf = C.create_string_buffer(1 << 16)
+        self._chk(self.lib.demsph_profile_report(self.h, buf, _I(len(buf))), "profile_report")
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms = line.split()
+            out[name] = (int(n), float(ms))
+        return out
+
     # ---- state ----
-    def download_fluids(self):
+    def download_fluids(self, out=None):
+        """(pos, vel, acc, dRho) in original order; ``out`` may supply the four arrays."""
         n = self.nf
-        pos, vel, acc, drho = (np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n))
-        self._chk(self.lib.demsph_download_fluids(self.h, _ptr(pos), _ptr(vel), _ptr(acc), _ptr(drho)),
+        pos, vel, acc, drho = out if out is not None else (np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3)),
+                                                           np.zeros(n))
+        self._chk(self.lib.demsph_download_fluids(self.h, *[None if a is None else _ptr(a) for a in (pos, vel, acc,
+                                                                                                    drho)]),
                   "download_fluids")
         return pos, vel, acc, drho
 
-    def download_solids(self):
+    def download_solids(self, out=None):
+        """dict of pos, vel, acc, normal, torque, angvel; ``out`` may supply (some of) the six arrays."""
         n = self.ns
-        out = [np.zeros((n, 3)) for _ in range(6)]
-        self._chk(self.lib.demsph_download_solids(self.h, *[_ptr(a) for a in out]), "download_solids")
-        return dict(zip(("pos", "vel", "acc", "normal", "torque", "angvel"), out))
+        keys = ("pos", "vel", "acc", "normal", "torque", "angvel")
+        arrs = [out.get(k) for k in keys] if out is not None else [np.zeros((n, 3)) for _ in range(6)]
+        self._chk(self.lib.demsph_download_solids(self.h, *[None if a is None else _ptr(a) for a in arrs]),
+                  "download_solids")
+        return dict(zip(keys, arrs))
 
     def download_clumps(self):
         n = self.nc

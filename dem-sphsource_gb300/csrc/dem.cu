@@ -533,30 +533,30 @@ void launchPairContacts(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.ns <= 0) return;
     const int blocks = blocksFor(d.ssCap < 1 ? 1 : d.ssCap, T);
-    kPairContacts<<<blocks < 152 * 16 ? blocks : 152 * 16, T, 0, s>>>(d, par, dt);
+    ++t_kernelLaunches, kPairContacts<<<blocks < 152 * 16 ? blocks : 152 * 16, T, 0, s>>>(d, par, dt);
 }
 void launchBonds(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.nb <= 0) return;
-    kBonds<<<blocksFor(d.nb, T), T, 0, s>>>(d, par, dt);
+    ++t_kernelLaunches, kBonds<<<blocksFor(d.nb, T), T, 0, s>>>(d, par, dt);
 }
 void launchGatherWalls(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.ns <= 0) return;
-    kGatherWalls<<<blocksFor(d.ns, T), T, 0, s>>>(d, par, dt, d.nf > 0 ? 1 : 0);
+    ++t_kernelLaunches, kGatherWalls<<<blocksFor(d.ns, T), T, 0, s>>>(d, par, dt, d.nf > 0 ? 1 : 0);
 }
 void launchClumpForce(const DeviceState& d, cudaStream_t s)
 {
     if (d.nc <= 0) return;
-    kClumpForce<<<blocksFor(d.nc, 64), 64, 0, s>>>(d);
+    ++t_kernelLaunches, kClumpForce<<<blocksFor(d.nc, 64), 64, 0, s>>>(d);
 }
 void launchSolidIntegrate(const DeviceState& d, double dt, bool before, cudaStream_t s)
 {
     const double half = 0.5 * dt;
     const dfl h = df_from_double(half);
-    if (d.ns > 0) kSolidIntegrate<<<blocksFor(d.ns, 256), 256, 0, s>>>(d, h, before ? 1 : 0);
-    if (d.nc > 0) kClumpIntegrate<<<blocksFor(d.nc, 64), 64, 0, s>>>(d, half, h, before ? 1 : 0);
+    if (d.ns > 0) ++t_kernelLaunches, kSolidIntegrate<<<blocksFor(d.ns, 256), 256, 0, s>>>(d, h, before ? 1 : 0);
+    if (d.nc > 0) ++t_kernelLaunches, kClumpIntegrate<<<blocksFor(d.nc, 64), 64, 0, s>>>(d, half, h, before ? 1 : 0);
 }
-void launchStepDone(const DeviceState& d, cudaStream_t s) { kStepDone<<<1, 1, 0, s>>>(d.status, d.stepsDone); }
+void launchStepDone(const DeviceState& d, cudaStream_t s) { ++t_kernelLaunches, kStepDone<<<1, 1, 0, s>>>(d.status, d.stepsDone); }
 
 }  // namespace demsph

@@ -137,23 +137,59 @@ void allocContactLists(demsph_engine* e)
     }
 }
 
+// ---- stage timing ----
+struct StageTimer {
+    demsph_engine* e;
+    const char* tag;
+    cudaEvent_t a = nullptr, b = nullptr;
+    StageTimer(demsph_engine* eng, const char* t) : e(eng), tag(t)
+    {
+        if (!e->profiling) return;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        CK(cudaEventRecord(a, e->stream));
+    }
+    ~StageTimer()
+    {
+        if (!a) return;
+        cudaEventRecord(b, e->stream);
+        e->timed.push_back({tag, a, b});
+    }
+};
+#define TIMED(tag) StageTimer _stage_timer(e, tag)
+
 // ---- the five stages ----
 void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
 {
     DeviceState& d = e->d;
     const cudaStream_t s = e->stream;
     const bool fluidStep = d.nf > 0 && (iStep % gap == 0);
-    if (fluidStep) launchFluidHashReorder(d, s);
-    launchSolidHashSort(d, s);
     if (fluidStep) {
-        launchFluidLists(d, s);
+        TIMED("fluid_hash_reorder");
+        launchFluidHashReorder(d, s);
+    }
+    {
+        TIMED("solid_hash_sort");
+        launchSolidHashSort(d, s);
+    }
+    if (fluidStep) {
+        {
+            TIMED("fluid_lists");
+            launchFluidLists(d, s);
+        }
+        TIMED("coupling_lists");
         launchCouplingLists(d, s);
     }
     e->par ^= 1;
+    TIMED("solid_contact_list");
     launchSolidContactList(d, e->par, s);
 }
 
-void stageBefore(demsph_engine* e, double dt) { launchSolidIntegrate(e->d, dt, true, e->stream); }
+void stageBefore(demsph_engine* e, double dt)
+{
+    TIMED("integrate_before");
+    launchSolidIntegrate(e->d, dt, true, e->stream);
+}
 
 void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
 {
@@ -161,12 +197,25 @@ void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
     const cudaStream_t s = e->stream;
     const double dtf = dt * (double)gap;
     const bool fluidStep = iStep % gap == 0;
-    if (d.nf > 0 && (iStep % (5 * gap) == 0 || iStep == 1)) launchDensityReinit(d, iStep, s);
-    if (fluidStep) launchContinuityPass(d, 0, dtf, s);
-    launchCoupling(d, fluidStep ? 1 : 0, s);
+    if (d.nf > 0 && (iStep % (5 * gap) == 0 || iStep == 1)) {
+        TIMED("density_reinit");
+        launchDensityReinit(d, iStep, s);
+    }
+    if (fluidStep) {
+        TIMED("continuity");
+        launchContinuityPass(d, 0, dtf, s);
+    }
+    {
+        TIMED("coupling_force");
+        launchCoupling(d, fluidStep ? 1 : 0, s);
+    }
     if (d.fsPairForce) launchCouplingPairForces(d, fluidStep ? 1 : 0, d.fsPairForce, s);
     if (fluidStep) {
-        launchMomentumPass(d, dtf, s);
+        {
+            TIMED("momentum");
+            launchMomentumPass(d, dtf, s);
+        }
+        TIMED("continuity");
         launchContinuityPass(d, 1, dtf, s);
     }
 }
@@ -174,13 +223,29 @@ void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
 void stageContact(demsph_engine* e, double dt)
 {
     DeviceState& d = e->d;
-    launchPairContacts(d, e->par, (float)dt, e->stream);
-    launchBonds(d, e->par, (float)dt, e->stream);
-    launchGatherWalls(d, e->par, (float)dt, e->stream);
-    launchClumpForce(d, e->stream);
+    {
+        TIMED("pair_contacts");
+        launchPairContacts(d, e->par, (float)dt, e->stream);
+    }
+    if (d.nb > 0) {
+        TIMED("bonds");
+        launchBonds(d, e->par, (float)dt, e->stream);
+    }
+    {
+        TIMED("gather_walls");
+        launchGatherWalls(d, e->par, (float)dt, e->stream);
+    }
+    if (d.nc > 0) {
+        TIMED("clump_force");
+        launchClumpForce(d, e->stream);
+    }
 }
 
-void stageAfter(demsph_engine* e, double dt) { launchSolidIntegrate(e->d, dt, false, e->stream); }
+void stageAfter(demsph_engine* e, double dt)
+{
+    TIMED("integrate_after");
+    launchSolidIntegrate(e->d, dt, false, e->stream);
+}
 
 void fullStep(demsph_engine* e, double dt, int iStep, int gap)
 {
@@ -306,6 +371,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             return DEMSPH_ERR_ARGUMENT;
     demsph_engine* e = new demsph_engine();
     e->debug = o.debug;
+    e->launchBase = t_kernelLaunches;
     int rc = checkDevice(e, o.device);
     if (rc != DEMSPH_OK) {
         *out = e;  // keep the message readable
@@ -718,7 +784,8 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
         CK(cudaMemsetAsync(d.stepsDone, 0, sizeof(int), e->stream));
         const int startPar = e->par;
         int s = step;
-        auto graphable = [&](int k) { return use_graph && k > 1 && k % period == 0 && end - k >= period; };
+        const bool graphs = use_graph && !e->profiling;
+        auto graphable = [&](int k) { return graphs && k > 1 && k % period == 0 && end - k >= period; };
         while (s < end && !graphable(s)) fullStep(e, dt, s++, gap);
         if (s < end && graphable(s)) {
             if (!e->graph || e->graphPeriod != period || e->graphGap != gap || e->graphDt != dt ||
@@ -726,9 +793,12 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
                 dropGraph(e);
                 const int parity = e->par;
                 cudaGraph_t g;
+                const long long before = t_kernelLaunches;
                 CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
                 for (int k = 0; k < period; ++k) fullStep(e, dt, s + k, gap);
                 CK(cudaStreamEndCapture(e->stream, &g));
+                e->graphKernels = t_kernelLaunches - before;
+                e->capturedLaunches += e->graphKernels;
                 const cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
                 cudaGraphDestroy(g);
                 CK(ie);
@@ -740,6 +810,7 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
             }
             while (end - s >= period) {
                 CK(cudaGraphLaunch(e->graph, e->stream));
+                e->replayedKernels += e->graphKernels;
                 s += period;
             }
             while (s < end) fullStep(e, dt, s++, gap);
@@ -756,6 +827,53 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
         grow(e, st);
     }
     CK(cudaGetLastError());
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+void* demsph_stream(demsph_engine* e) { return e ? (void*)e->stream : nullptr; }
+
+long long demsph_kernel_launches(demsph_engine* e)
+{
+    if (!e) return -1;
+    return (t_kernelLaunches - e->launchBase) - e->capturedLaunches + e->replayedKernels;
+}
+
+int demsph_set_profiling(demsph_engine* e, int enable)
+{
+    if (!e) return DEMSPH_ERR_ARGUMENT;
+    e->profiling = enable != 0;
+    return DEMSPH_OK;
+}
+
+int demsph_profile_report(demsph_engine* e, char* buf, int cap)
+{
+    if (!e || !buf || cap <= 0) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    CK(cudaStreamSynchronize(e->stream));
+    std::vector<std::string> order;
+    std::vector<std::pair<int, double>> acc;
+    for (auto& t : e->timed) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, t.a, t.b));
+        size_t k = 0;
+        while (k < order.size() && order[k] != t.tag) ++k;
+        if (k == order.size()) {
+            order.push_back(t.tag);
+            acc.push_back({0, 0.0});
+        }
+        acc[k].first += 1;
+        acc[k].second += ms;
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    e->timed.clear();
+    std::string out;
+    for (size_t k = 0; k < order.size(); ++k)
+        out += order[k] + " " + std::to_string(acc[k].first) + " " + std::to_string(acc[k].second) + "\n";
+    const size_t n = std::min(out.size(), (size_t)cap - 1);
+    std::memcpy(buf, out.data(), n);
+    buf[n] = 0;
     return DEMSPH_OK;
     ENGINE_END(e)
 }

@@ -53,12 +53,28 @@ struct demsph_engine {
     double graphDt = 0;
     // contact tables as uploaded (FP32)
     std::vector<float> hzF, lnF, bdF, dampF;
+    // kernel launch accounting (demsph_kernel_launches)
+    long long launchBase = 0;        // t_kernelLaunches when the engine was created
+    long long capturedLaunches = 0;  // launch calls recorded into graphs (not executed then)
+    long long replayedKernels = 0;   // kernels executed by graph replays
+    long long graphKernels = 0;      // kernels in the current graph
+    // stage timing (demsph_set_profiling)
+    bool profiling = false;
+    struct Timed {
+        const char* tag;
+        cudaEvent_t a, b;
+    };
+    std::vector<Timed> timed;
     // scratch for downloads (device, grown on demand)
     double* dscratch = nullptr;
     size_t dscratchN = 0;
 
     ~demsph_engine()
     {
+        for (auto& t : timed) {
+            cudaEventDestroy(t.a);
+            cudaEventDestroy(t.b);
+        }
         if (graph) cudaGraphExecDestroy(graph);
         for (void* p : owned) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);

@@ -19,45 +19,56 @@ namespace {
 
 __device__ __forceinline__ double cellOrigin(const DeviceState& d, int a, int c) { return d.minB[a] + (double)c * d.cs[a]; }
 
-__global__ void kFluidOut(DeviceState d, double* out)  // 10 doubles per original index
+// Planar FP64 output in original order: pos[3n] vel[3n] acc[3n] drho[n].
+__global__ void kFluidOut(DeviceState d, double* out)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.nf) return;
+    const size_t n = d.nf;
     const int id = d.fid[s];
     const int4 c = d.fcell[s];
     const float4 h = d.fph[0][s], l = d.fpl[0][s];
     const float4 vh = d.fvh[0][s], vl = d.fvl[0][s];
     const float4 a = d.facc[s];
-    double* o = out + 10 * (size_t)id;
-    o[0] = cellOrigin(d, 0, c.x) + ((double)h.x + (double)l.x);
-    o[1] = cellOrigin(d, 1, c.y) + ((double)h.y + (double)l.y);
-    o[2] = cellOrigin(d, 2, c.z) + ((double)h.z + (double)l.z);
-    o[3] = (double)vh.x + (double)vl.x;
-    o[4] = (double)vh.y + (double)vl.y;
-    o[5] = (double)vh.z + (double)vl.z;
-    o[6] = a.x;
-    o[7] = a.y;
-    o[8] = a.z;
-    o[9] = d.fdrho[0][s];
+    double* p = out + 3 * (size_t)id;
+    double* v = out + 3 * n + 3 * (size_t)id;
+    double* ac = out + 6 * n + 3 * (size_t)id;
+    p[0] = cellOrigin(d, 0, c.x) + ((double)h.x + (double)l.x);
+    p[1] = cellOrigin(d, 1, c.y) + ((double)h.y + (double)l.y);
+    p[2] = cellOrigin(d, 2, c.z) + ((double)h.z + (double)l.z);
+    v[0] = (double)vh.x + (double)vl.x;
+    v[1] = (double)vh.y + (double)vl.y;
+    v[2] = (double)vh.z + (double)vl.z;
+    ac[0] = a.x;
+    ac[1] = a.y;
+    ac[2] = a.z;
+    out[9 * n + id] = d.fdrho[0][s];
 }
 
-__global__ void kSolidOut(DeviceState d, double* out)  // 18 doubles per solid
+// Planar FP64 output: pos vel acc normal torque angvel, 3n each.
+__global__ void kSolidOut(DeviceState d, double* out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.ns) return;
+    const size_t n3 = 3 * (size_t)d.ns;
     const int4 c = d.scell[i];
     const float4 h = d.sph[i], l = d.spl[i];
     const float4 vh = d.svh[i], vl = d.svl[i], wh = d.swh[i], wl = d.swl[i];
-    const float4 a = d.sacc[i], n = d.snormal[i], t = d.storque[i];
-    double* o = out + 18 * (size_t)i;
+    const float4 a = d.sacc[i], nr = d.snormal[i], t = d.storque[i];
+    double* o = out + 3 * (size_t)i;
     o[0] = cellOrigin(d, 0, c.x) + ((double)h.x + (double)l.x);
     o[1] = cellOrigin(d, 1, c.y) + ((double)h.y + (double)l.y);
     o[2] = cellOrigin(d, 2, c.z) + ((double)h.z + (double)l.z);
-    o[3] = (double)vh.x + vl.x; o[4] = (double)vh.y + vl.y; o[5] = (double)vh.z + vl.z;
-    o[6] = a.x; o[7] = a.y; o[8] = a.z;
-    o[9] = n.x; o[10] = n.y; o[11] = n.z;
-    o[12] = t.x; o[13] = t.y; o[14] = t.z;
-    o[15] = (double)wh.x + wl.x; o[16] = (double)wh.y + wl.y; o[17] = (double)wh.z + wl.z;
+    o += n3;
+    o[0] = (double)vh.x + vl.x; o[1] = (double)vh.y + vl.y; o[2] = (double)vh.z + vl.z;
+    o += n3;
+    o[0] = a.x; o[1] = a.y; o[2] = a.z;
+    o += n3;
+    o[0] = nr.x; o[1] = nr.y; o[2] = nr.z;
+    o += n3;
+    o[0] = t.x; o[1] = t.y; o[2] = t.z;
+    o += n3;
+    o[0] = (double)wh.x + wl.x; o[1] = (double)wh.y + wl.y; o[2] = (double)wh.z + wl.z;
 }
 
 // Writes the state given in original order (FP64) into the engine.
@@ -161,18 +172,14 @@ int demsph_download_fluids(demsph_engine* e, double* pos, double* vel, double* a
     ENGINE_GUARD(e)
     DeviceState& d = e->d;
     if (d.nf == 0) return DEMSPH_OK;
-    double* buf = scratchDoubles(e, 10 * (size_t)d.nf);
-    kFluidOut<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, buf);
-    std::vector<double> h(10 * (size_t)d.nf);
-    CK(cudaMemcpyAsync(h.data(), buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, e->stream));
+    const size_t n = d.nf;
+    double* buf = scratchDoubles(e, 10 * n);
+    ++t_kernelLaunches, kFluidOut<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, buf);
+    double* outs[3] = {pos, vel, acc};
+    for (int k = 0; k < 3; ++k)
+        if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + 3 * n * k, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (drho) CK(cudaMemcpyAsync(drho, buf + 9 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
-    for (int i = 0; i < d.nf; ++i) {
-        const double* o = &h[10 * (size_t)i];
-        if (pos) std::memcpy(pos + 3 * (size_t)i, o, 3 * sizeof(double));
-        if (vel) std::memcpy(vel + 3 * (size_t)i, o + 3, 3 * sizeof(double));
-        if (acc) std::memcpy(acc + 3 * (size_t)i, o + 6, 3 * sizeof(double));
-        if (drho) drho[i] = o[9];
-    }
     return DEMSPH_OK;
     ENGINE_END(e)
 }
@@ -183,15 +190,13 @@ int demsph_download_solids(demsph_engine* e, double* pos, double* vel, double* a
     ENGINE_GUARD(e)
     DeviceState& d = e->d;
     if (d.ns == 0) return DEMSPH_OK;
-    double* buf = scratchDoubles(e, 18 * (size_t)d.ns);
-    kSolidOut<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, buf);
-    std::vector<double> h(18 * (size_t)d.ns);
-    CK(cudaMemcpyAsync(h.data(), buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, e->stream));
-    CK(cudaStreamSynchronize(e->stream));
+    const size_t n3 = 3 * (size_t)d.ns;
+    double* buf = scratchDoubles(e, 6 * n3);
+    ++t_kernelLaunches, kSolidOut<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, buf);
     double* outs[6] = {pos, vel, acc, normal, torque, angvel};
-    for (int i = 0; i < d.ns; ++i)
-        for (int k = 0; k < 6; ++k)
-            if (outs[k]) std::memcpy(outs[k] + 3 * (size_t)i, &h[18 * (size_t)i + 3 * k], 3 * sizeof(double));
+    for (int k = 0; k < 6; ++k)
+        if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + n3 * k, sizeof(double) * n3, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)
 }
@@ -226,7 +231,7 @@ int demsph_upload_fluids(demsph_engine* e, const double* pos, const double* vel,
     if (dp) CK(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, e->stream));
     if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, e->stream));
     if (dr) CK(cudaMemcpyAsync(dr, drho, sizeof(double) * d.nf, cudaMemcpyHostToDevice, e->stream));
-    kFluidIn<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, dp, dv, dr);
+    ++t_kernelLaunches, kFluidIn<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, dp, dv, dr);
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)
@@ -244,7 +249,7 @@ int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel,
     if (dp) CK(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     if (dw) CK(cudaMemcpyAsync(dw, angvel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
-    kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw);
+    ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw);
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)
@@ -286,7 +291,7 @@ int demsph_set_clump_velocity(demsph_engine* e, int c, const double v[3])
     if (!v) return DEMSPH_ERR_ARGUMENT;
     ENGINE_GUARD(e)
     if (c < 0 || c >= e->d.nc) return DEMSPH_OK;  // the reference ignores out-of-range clumps (dataBase.h:171)
-    kSetClumpVelocity<<<1, 1, 0, e->stream>>>(e->d, c, v[0], v[1], v[2]);
+    ++t_kernelLaunches, kSetClumpVelocity<<<1, 1, 0, e->stream>>>(e->d, c, v[0], v[1], v[2]);
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)
@@ -297,7 +302,7 @@ int demsph_add_external_force(demsph_engine* e, int i, const double f[3])
     if (!f) return DEMSPH_ERR_ARGUMENT;
     ENGINE_GUARD(e)
     if (i < 0 || i >= e->d.ns) return fail(e, DEMSPH_ERR_ARGUMENT, "solid index out of range");
-    kAddForce<<<1, 1, 0, e->stream>>>(e->d, i, (float)f[0], (float)f[1], (float)f[2]);
+    ++t_kernelLaunches, kAddForce<<<1, 1, 0, e->stream>>>(e->d, i, (float)f[0], (float)f[1], (float)f[2]);
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)
@@ -307,7 +312,7 @@ int demsph_add_global_damping(demsph_engine* e, int i, double cd)
 {
     ENGINE_GUARD(e)
     if (i < 0 || i >= e->d.ns) return fail(e, DEMSPH_ERR_ARGUMENT, "solid index out of range");
-    kAddDamping<<<1, 1, 0, e->stream>>>(e->d, i, (float)cd);
+    ++t_kernelLaunches, kAddDamping<<<1, 1, 0, e->stream>>>(e->d, i, (float)cd);
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)

@@ -127,20 +127,20 @@ void launchFluidHashReorder(const DeviceState& d, cudaStream_t s)
 {
     if (d.nf <= 0) return;
     cudaMemsetAsync(d.fcellCount, 0, sizeof(int) * d.grid.num, s);
-    kFluidHash<<<blocksFor(d.nf, T), T, 0, s>>>(d);
+    ++t_kernelLaunches, kFluidHash<<<blocksFor(d.nf, T), T, 0, s>>>(d);
     scanExclusive(d.fcellCount, d.fcellStart, d.grid.num, d.scanWork, s);
-    kScatter<<<blocksFor(d.nf, T), T, 0, s>>>(d.nf, d.fkey, d.fslotInCell, d.fcellStart, d.fsortTmp, d.status);
-    kFluidGather<<<blocksFor(d.nf, T), T, 0, s>>>(d);
+    ++t_kernelLaunches, kScatter<<<blocksFor(d.nf, T), T, 0, s>>>(d.nf, d.fkey, d.fslotInCell, d.fcellStart, d.fsortTmp, d.status);
+    ++t_kernelLaunches, kFluidGather<<<blocksFor(d.nf, T), T, 0, s>>>(d);
 }
 
 void launchSolidHashSort(const DeviceState& d, cudaStream_t s)
 {
     if (d.ns <= 0) return;
     cudaMemsetAsync(d.scellCount, 0, sizeof(int) * d.grid.num, s);
-    kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d);
+    ++t_kernelLaunches, kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d);
     scanExclusive(d.scellCount, d.scellStart, d.grid.num, d.scanWork, s);
-    kScatter<<<blocksFor(d.ns, T), T, 0, s>>>(d.ns, d.skey, d.sslotInCell, d.scellStart, d.ssortTmp, d.status);
-    kSolidRank<<<blocksFor(d.ns, T), T, 0, s>>>(d);
+    ++t_kernelLaunches, kScatter<<<blocksFor(d.ns, T), T, 0, s>>>(d.ns, d.skey, d.sslotInCell, d.scellStart, d.ssortTmp, d.status);
+    ++t_kernelLaunches, kSolidRank<<<blocksFor(d.ns, T), T, 0, s>>>(d);
 }
 
 }  // namespace demsph

@@ -8,6 +8,10 @@
 
 namespace demsph {
 
+// Kernel launches issued by this thread (every launch site increments it);
+// the engine turns deltas of it into the launch count of a run.
+inline thread_local long long t_kernelLaunches = 0;
+
 struct DeviceState {
     GridDev grid;
     double minB[3], cs[3];   // FP64 grid, for import and export

@@ -322,27 +322,27 @@ __global__ void kSolidNormals(DeviceState d, double h)
 void launchFluidLists(const DeviceState& d, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    kFluidLists<<<blocksFor(d.nf, T), T, 0, s>>>(d);
+    ++t_kernelLaunches, kFluidLists<<<blocksFor(d.nf, T), T, 0, s>>>(d);
 }
 
 void launchCouplingLists(const DeviceState& d, cudaStream_t s)
 {
     if (d.nf <= 0 || d.ns <= 0) return;
     cudaMemsetAsync(d.coupCount, 0, sizeof(int) * d.ns, s);
-    kCoupCount<<<blocksFor(d.nf, 256), 256, 0, s>>>(d);
+    ++t_kernelLaunches, kCoupCount<<<blocksFor(d.nf, 256), 256, 0, s>>>(d);
     scanExclusive(d.coupCount, d.coupStart, d.ns, d.scanWork, s);
     cudaMemsetAsync(d.coupCount, 0, sizeof(int) * d.ns, s);
-    kCoupFill<<<blocksFor(d.nf, 256), 256, 0, s>>>(d);
-    kCoupSort<<<blocksFor(d.ns, 256), 256, 0, s>>>(d);
+    ++t_kernelLaunches, kCoupFill<<<blocksFor(d.nf, 256), 256, 0, s>>>(d);
+    ++t_kernelLaunches, kCoupSort<<<blocksFor(d.ns, 256), 256, 0, s>>>(d);
 }
 
 void launchSolidContactList(const DeviceState& d, int par, cudaStream_t s)
 {
     if (d.ns <= 0) return;
-    kSolidList<false><<<blocksFor(d.ns, T), T, 0, s>>>(d, par);
+    ++t_kernelLaunches, kSolidList<false><<<blocksFor(d.ns, T), T, 0, s>>>(d, par);
     scanExclusive(d.sfcnt, d.sfbase[par], d.ns, d.scanWork, s);
     scanExclusive(d.srcnt, d.srbase, d.ns, d.scanWork, s);
-    kSolidList<true><<<blocksFor(d.ns, T), T, 0, s>>>(d, par);
+    ++t_kernelLaunches, kSolidList<true><<<blocksFor(d.ns, T), T, 0, s>>>(d, par);
 }
 
 // Bond creation from the contact list (addBondData at initialisation,
@@ -351,7 +351,7 @@ void launchSolidContactList(const DeviceState& d, int par, cudaStream_t s)
 int launchBondFlags(const DeviceState& d, int par, int np, int* flag, int* pos, int* work, cudaStream_t s)
 {
     if (np <= 0) return 0;
-    kBondFlags<<<blocksFor(np, 256), 256, 0, s>>>(d, par, flag);
+    ++t_kernelLaunches, kBondFlags<<<blocksFor(np, 256), 256, 0, s>>>(d, par, flag);
     scanExclusive(flag, pos, np, work, s);
     int nb = 0;
     cudaMemcpyAsync(&nb, pos + np, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -362,13 +362,13 @@ int launchBondFlags(const DeviceState& d, int par, int np, int* flag, int* pos, 
 void launchBondWrite(const DeviceState& d, int par, int np, const int* flag, const int* pos, cudaStream_t s)
 {
     if (np <= 0 || d.nb <= 0) return;
-    kBondWrite<<<blocksFor(np, 256), 256, 0, s>>>(d, par, flag, pos);
+    ++t_kernelLaunches, kBondWrite<<<blocksFor(np, 256), 256, 0, s>>>(d, par, flag, pos);
 }
 
 void launchSolidNormals(const DeviceState& d, double h, cudaStream_t s)
 {
     if (d.ns <= 0 || !(h > 0.0)) return;
-    kSolidNormals<<<blocksFor(d.ns, T), T, 0, s>>>(d, h);
+    ++t_kernelLaunches, kSolidNormals<<<blocksFor(d.ns, T), T, 0, s>>>(d, h);
 }
 
 }  // namespace demsph

@@ -99,14 +99,14 @@ void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s)
     }
     const int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (tiles == 1) {
-        kTileScan<<<1, SCAN_THREADS, 0, s>>>(in, n, out, nullptr);
+        ++t_kernelLaunches, kTileScan<<<1, SCAN_THREADS, 0, s>>>(in, n, out, nullptr);
         return;
     }
     int* sums = work;
     int* offs = work + tiles;  // tiles + 1 entries
-    kTileSums<<<tiles, SCAN_THREADS, 0, s>>>(in, n, sums);
+    ++t_kernelLaunches, kTileSums<<<tiles, SCAN_THREADS, 0, s>>>(in, n, sums);
     scanExclusive(sums, offs, tiles, offs + tiles + 1, s);
-    kTileScan<<<tiles, SCAN_THREADS, 0, s>>>(in, n, out, offs);
+    ++t_kernelLaunches, kTileScan<<<tiles, SCAN_THREADS, 0, s>>>(in, n, out, offs);
 }
 
 }  // namespace demsph

@@ -352,7 +352,7 @@ __global__ void kCouplingPairs(DeviceState d, int src, float4* out)
 void launchDensityReinit(const DeviceState& d, int iStep, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    kDensityReinit<<<blocksFor(d.nf, T), T, 0, s>>>(d, iStep == 1 ? 1 : 0);
+    ++t_kernelLaunches, kDensityReinit<<<blocksFor(d.nf, T), T, 0, s>>>(d, iStep == 1 ? 1 : 0);
 }
 
 void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStream_t s)
@@ -366,25 +366,25 @@ void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStrea
     } else {           // second half step: densities 1 -> 0, velocity 1 -> 0
         a.ps = 0; a.vs = 1; a.ds = 1; a.dd = 0; a.driftTo = -1; a.velCopyTo = 0;
     }
-    kContinuity<<<blocksFor(d.nf, T), T, 0, s>>>(d, a);
+    ++t_kernelLaunches, kContinuity<<<blocksFor(d.nf, T), T, 0, s>>>(d, a);
 }
 
 void launchMomentumPass(const DeviceState& d, double dtf, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    kMomentum<<<blocksFor(d.nf, T), T, 0, s>>>(d, df_from_double(dtf), df_from_double(0.5 * dtf));
+    ++t_kernelLaunches, kMomentum<<<blocksFor(d.nf, T), T, 0, s>>>(d, df_from_double(dtf), df_from_double(0.5 * dtf));
 }
 
 void launchCoupling(const DeviceState& d, int src, cudaStream_t s)
 {
     if (d.nf <= 0 || d.ns <= 0) return;
-    kCoupling<<<blocksFor(d.ns, 128), 128, 0, s>>>(d, src);
+    ++t_kernelLaunches, kCoupling<<<blocksFor(d.ns, 128), 128, 0, s>>>(d, src);
 }
 
 void launchCouplingPairForces(const DeviceState& d, int src, float4* out, cudaStream_t s)
 {
     if (d.nf <= 0 || d.ns <= 0) return;
-    kCouplingPairs<<<blocksFor(d.nf, 128), 128, 0, s>>>(d, src, out);
+    ++t_kernelLaunches, kCouplingPairs<<<blocksFor(d.nf, 128), 128, 0, s>>>(d, src, out);
 }
 
 }  // namespace demsph

@@ -223,6 +223,18 @@ DEMSPH_API int demsph_solid_integrate_after_contact(demsph_engine* e, double dt)
    for i_step = first_step .. first_step+n_steps-1, without the driver hook;
    replayed as a CUDA graph when use_graph != 0. */
 DEMSPH_API int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph);
+/* The CUDA stream (cudaStream_t) the engine issues all its work on, for
+   callers that time or order work around it. */
+DEMSPH_API void* demsph_stream(demsph_engine* e);
+/* Kernels this engine has executed so far (graph replays counted by their
+   kernels), as issued from the calling thread. */
+DEMSPH_API long long demsph_kernel_launches(demsph_engine* e);
+/* Per-stage timing with CUDA events on the engine's stream (enable != 0).
+   While enabled, demsph_update runs uncaptured so every launch is timed. */
+DEMSPH_API int demsph_set_profiling(demsph_engine* e, int enable);
+/* Writes "name launches total_ms\n" lines for the stages timed since the last
+   report into buf (NUL-terminated, truncated to cap) and resets the tally. */
+DEMSPH_API int demsph_profile_report(demsph_engine* e, char* buf, int cap);
 /* Waits for queued work; returns the first deferred error (e.g. capacity). */
 DEMSPH_API int demsph_synchronize(demsph_engine* e);
 
