@@ -282,6 +282,26 @@ DEMSPH_API int demsph_export_bonds(demsph_engine* e, int* pointed, int* pointing
 /* Shepard reference sums sumW0 (core/integrate.cu:44-47). */
 DEMSPH_API int demsph_export_fluid_sumw0(demsph_engine* e, double* sumw0);
 
+/* ---- cell sort without allocation ----
+   No counterpart in the reference.  Sorts n particle cell keys (device
+   array, each in [0, num_cells)) into the reference's stable (key, index)
+   order: sorted_index[n] (the objectHash.index of core/neighborSearch.cu) and
+   cell_start / cell_end[num_cells] (-1 for empty cells), all device arrays.
+   For callers that cannot allocate device memory when they call it (their
+   allocator already holds the GPU's memory, they run inside a legacy-mode
+   stream capture, or they must avoid cudaMalloc's synchronisation): the
+   scratch is one fixed array of device memory in this library, about 8 MB,
+   that every GPU loading the library keeps until exit.  Limits: n and
+   num_cells at most 524288 each; larger sizes return DEMSPH_ERR_ARGUMENT, as
+   do keys outside [0, num_cells).  The first call on each device looks up the
+   array's address on that device; make that first call before any stream
+   capture.  All calls share the array: calls that overlap on the GPU (other
+   streams, other threads) race and must be serialised by the caller.  The
+   call waits for its stream to finish.  stream is a cudaStream_t (NULL = the
+   default stream). */
+DEMSPH_API int demsph_cell_sort_noalloc(const int* keys, int n, int num_cells, int* sorted_index, int* cell_start,
+                                        int* cell_end, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
