@@ -154,7 +154,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-# ---- algorithmic bytes per stage (compulsory traffic; see DESIGN.md) -------------------------
+# ---- algorithmic bytes per stage (compulsory traffic) -------------------------
 def stage_bytes(stage, c):
     """Bytes one launch of `stage` must move at least, from the scene counts `c`."""
     P, Ns, Nf, Nb = c["solid_pairs"], c["n_solid_active"], c["n_fluid"], c["bonds"]

@@ -1,6 +1,6 @@
 // FP64 host oracle of the coupled DEM-SPH step.
 //
-// TEST INFRASTRUCTURE - the checker, never the product.  Only tests/,
+// TEST INFRASTRUCTURE - the oracle, never the product.  Only tests/,
 // __graft_entry__.smoke() and bench.py's CPU-baseline leg load this library.
 //
 // A CPU restatement, in FP64 and in plain loops (OpenMP over particles), of

@@ -1,6 +1,6 @@
 """ctypes driver for oracle/liboracle_demsph.so - the FP64 CPU oracle.
 
-TEST INFRASTRUCTURE: the checker for the GPU engine's parity tests, the CPU
+TEST INFRASTRUCTURE: the reference side of the GPU engine's parity tests, the CPU
 baseline leg of bench.py, and nothing else.  The product never loads it.
 
 The oracle takes the same ``demsph_scene`` the engine takes (built by the

@@ -16,7 +16,7 @@ Tolerances (stated once, used by every test):
   S = max(1e-3 max|f64|, floor); the floor is the physical scale of the
   quantity (weight m g of the lightest grain for forces, m g r for torques,
   1e-6 r for springs, g dt n / r for spins), so that a field that is still
-  ~0 everywhere is not judged by its rounding noise;
+  ~0 everywhere is not measured by its rounding noise;
 * velocities: |v - v64| <= FORCE_TOL * max(|v64|, g dt n) after n steps.
 
 These bounds hold for ONE step from the same state (the per-step force
