@@ -64,7 +64,7 @@ class Options(C.Structure):
     """ctypes mirror of ``demsph_options``."""
 
     _fields_ = [("device", _I), ("fluid_neighbors_max", _I), ("fluid_solids_max", _I),
-                ("solid_contacts_per_particle", _I), ("fixes", _I), ("debug", _I)]
+                ("solid_contacts_per_particle", _I), ("fixes", _I), ("debug", _I), ("solid_verlet_skin", _D)]
 
 
 class Counts(C.Structure):
@@ -231,10 +231,13 @@ class Engine:
     """One scene on one GPU (the C ABI engine)."""
 
     def __init__(self, scene, device=0, fluid_neighbors_max=0, fluid_solids_max=0, solid_contacts_per_particle=0,
-                 fixes=0, debug=0):
+                 fixes=0, debug=0, solid_verlet_skin=0.0):
+        """``solid_verlet_skin``: margin (m) of the solid contact candidates
+        (0 = 0.2 x the smallest solid radius, < 0 = the 27-cell walk every step)."""
         self.lib = load_library()
         self.scene = scene
-        opts = Options(device, fluid_neighbors_max, fluid_solids_max, solid_contacts_per_particle, fixes, debug)
+        opts = Options(device, fluid_neighbors_max, fluid_solids_max, solid_contacts_per_particle, fixes, debug,
+                       float(solid_verlet_skin))
         h = _P()
         rc = self.lib.demsph_create(C.byref(scene), C.byref(opts), C.byref(h))
         self.h = h

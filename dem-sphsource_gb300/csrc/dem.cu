@@ -157,21 +157,30 @@ __device__ __forceinline__ float3 contactVel(const DeviceState& d, int a, int b,
     return velDiff(d, a, b) + cross3(xyz(d.swh[a]), leverA) - cross3(xyz(d.swh[b]), leverB);
 }
 
+// Contact forces of every forward slot (calSolidContactForceTorque,
+// core/integrate.cu:423-512), one thread per row.
 __global__ void __launch_bounds__(T) kPairContacts(DeviceState d, int par, float dt)
 {
-    if (*d.status) return;
-    const int np = min(d.sfbase[par][d.ns], d.ssCap);
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np; k += gridDim.x * blockDim.x) {
-        const int a = d.spa[k], b = d.spb[par][k];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= d.nrow || *d.status) return;
+    const int a = d.rowSolid[r];
+    const int n = min(d.fcnt[par][r], d.scap);
+    if (n == 0) return;
+    const float4 ra = d.srad[a];
+    const float ima = d.sph[a].w;
+    const int mata = d.sflags[a].x;
+    for (int q = 0; q < n; ++q) {
+        const size_t k = (size_t)q * d.nrow + r;
+        const int b = d.fwd[par][k];
         const PairGeom g = pairGeometry(d, a, b);
-        const float4 ra = d.srad[a], rb = d.srad[b];
+        const float4 rb = d.srad[b];
         const float R = ra.x * rb.x / (ra.x + rb.x);
-        const float m = 1.f / (d.sph[a].w + d.sph[b].w);
+        const float m = 1.f / (ima + d.sph[b].w);
         const float3 vc = contactVel(d, a, b, g.leverA, g.leverB);
         const float3 wr = spinDiff(d, a, b);
         float3 es = xyz(d.spring[par][0][k]), er = xyz(d.spring[par][1][k]), et = xyz(d.spring[par][2][k]);
         float3 F = make_float3(0.f, 0.f, 0.f), Ft = F, Tq = F;
-        const int slot = tableSlot(d.tab, d.sflags[a].x, d.sflags[b].x);
+        const int slot = tableSlot(d.tab, mata, d.sflags[b].x);
         contactLaw(d.tab, slot, F, Ft, Tq, es, er, et, vc, wr, g.n, g.delta, m, R, dt);
         d.spring[par][0][k] = f4(es);
         d.spring[par][1][k] = f4(er);
@@ -182,6 +191,20 @@ __global__ void __launch_bounds__(T) kPairContacts(DeviceState d, int par, float
         d.pTA[k] = f4(Tq + nxF * g.sA);
         d.pTB[k] = f4(Tq + nxF * g.sB);
     }
+}
+
+// Slot (index into the per-slot arrays) of the forward contact (a, b), b > a,
+// or -1 when the pair is not in a's row.
+__device__ __forceinline__ long long forwardSlot(const DeviceState& d, int par, int a, int b)
+{
+    const int r = d.srow[a];
+    if (r < 0) return -1;
+    const int n = min(d.fcnt[par][r], d.scap);
+    for (int q = 0; q < n; ++q) {
+        const size_t k = (size_t)q * d.nrow + r;
+        if (d.fwd[par][k] == b) return (long long)k;
+    }
+    return -1;
 }
 
 // Adds the small rotation (R(theta) - I) v to a double-float vector.
@@ -219,12 +242,7 @@ __global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
     }
     const int2 ab = d.bab[b];
     const int i = ab.x, j = ab.y;
-    int slot = -1;
-    for (int q = d.sfbase[par][i], e = d.sfbase[par][i + 1]; q < e; ++q)
-        if (d.spb[par][q] == j) {
-            slot = q;
-            break;
-        }
+    const long long slot = forwardSlot(d, par, i, j);
     if (slot < 0) {  // the pair left the contact list: the bond breaks
         d.bon[b] = 0;
         return;
@@ -310,18 +328,24 @@ __global__ void __launch_bounds__(T) kGatherWalls(DeviceState d, int par, float 
     if (a >= d.ns || *d.status) return;
     const int4 fa = d.sflags[a];
     KahanF3 F, Tq;
-    for (int q = d.sfbase[par][a], e = d.sfbase[par][a + 1]; q < e; ++q) {
-        F.add(xyz(d.pF[q]));
-        Tq.add(xyz(d.pTA[q]));
-    }
-    for (int r = d.srbase[a], e = d.srbase[a + 1]; r < e; ++r) {
-        const int b = d.srpartner[r];
-        for (int q = d.sfbase[par][b], qe = d.sfbase[par][b + 1]; q < qe; ++q)
-            if (d.spb[par][q] == a) {
-                F.add(-xyz(d.pF[q]));
-                Tq.add(-xyz(d.pTB[q]));
-                break;
+    const int row = d.srow[a];
+    if (row >= 0) {
+        // forward slots (+), then the reverse partners' slots of this pair (-)
+        const int n = min(d.fcnt[par][row], d.scap);
+        for (int q = 0; q < n; ++q) {
+            const size_t k = (size_t)q * d.nrow + row;
+            F.add(xyz(d.pF[k]));
+            Tq.add(xyz(d.pTA[k]));
+        }
+        const int m = min(d.rcnt[row], d.scap);
+        for (int q = 0; q < m; ++q) {
+            const int b = d.rev[(size_t)q * d.nrow + row];
+            const long long k = forwardSlot(d, par, b, a);
+            if (k >= 0) {
+                F.add(-xyz(d.pF[k]));
+                Tq.add(-xyz(d.pTB[k]));
             }
+        }
     }
     if (withCoupling) F.add(-xyz(d.sfcoup[a]));
     const float4 ph = d.sph[a];
@@ -378,13 +402,22 @@ __device__ __forceinline__ double3 absPos(const DeviceState& d, int i)
                         d.minB[2] + c.z * d.cs[2] + ((double)h.z + (double)l.z));
 }
 
+__device__ __forceinline__ double warpSumD(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// calClumpForceTorque (integrate.cu:860-881): one warp per clump, its lanes
+// over the pebbles, FP64 sums reduced in a fixed tree (deterministic).
 __global__ void kClumpForce(DeviceState d)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= d.nc || *d.status) return;
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (c >= d.nc || *d.status) return;  // uniform over the warp
     double3 F = make_double3(0, 0, 0), Tq = F;
     const double3 cp = d.cpos[c];
-    for (int i = d.cstart[c]; i < d.cend[c]; ++i) {
+    for (int i = d.cstart[c] + lane; i < d.cend[c]; i += 32) {
         double3 fi = make_double3(0, 0, 0);
         if (d.sflags[i].w & F_MASSIVE) fi = dscale(toD3(d.sacc[i]), 1.0 / (double)d.sph[i].w);
         F = dadd(F, fi);
@@ -392,11 +425,15 @@ __global__ void kClumpForce(DeviceState d)
         d.sacc[i] = make_float4(0, 0, 0, 0);
         d.storque[i] = make_float4(0, 0, 0, 0);
     }
-    const double im = d.cinvm[c];
-    double3 a = dscale(F, im);
-    if (im > 0.) a = dadd(a, make_double3(d.g64[0], d.g64[1], d.g64[2]));
-    d.cacc[c] = a;
-    d.ctorque[c] = Tq;
+    F = make_double3(warpSumD(F.x), warpSumD(F.y), warpSumD(F.z));
+    Tq = make_double3(warpSumD(Tq.x), warpSumD(Tq.y), warpSumD(Tq.z));
+    if (lane == 0) {
+        const double im = d.cinvm[c];
+        double3 a = dscale(F, im);
+        if (im > 0.) a = dadd(a, make_double3(d.g64[0], d.g64[1], d.g64[2]));
+        d.cacc[c] = a;
+        d.ctorque[c] = Tq;
+    }
 }
 
 // double-float x += v dt for one particle's position (solid arrays).
@@ -435,6 +472,22 @@ __device__ __forceinline__ void kickSolid(const DeviceState& d, int i, dfl dt, i
     d.swl[i] = make_float4(x.lo, y.lo, z.lo, wl.w);
 }
 
+// After the last drift of a step: once a solid that can touch others has
+// moved half the candidate margin since the candidates were built, the next
+// step rebuilds them.
+__device__ __forceinline__ void checkDisplacement(const DeviceState& d, int i)
+{
+    const int r = d.srow[i];
+    if (r < 0) return;
+    const int4 c = d.scell[i];
+    const float4 h = d.sph[i];
+    const float4 p0 = d.vref[r];
+    const float dx = (float)c.x * d.grid.cs.x + h.x - p0.x, dy = (float)c.y * d.grid.cs.y + h.y - p0.y,
+                dz = (float)c.z * d.grid.cs.z + h.z - p0.z;
+    const float half = 0.5f * d.skin;
+    if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)d.rebuild = 1;
+}
+
 __global__ void kSolidIntegrate(DeviceState d, dfl half, int before)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -447,6 +500,7 @@ __global__ void kSolidIntegrate(DeviceState d, dfl half, int before)
     } else {
         driftSolid(d, i, half);
         kickSolid(d, i, half, f);
+        checkDisplacement(d, i);
     }
 }
 
@@ -469,56 +523,81 @@ __device__ __forceinline__ double3 rotInvInertiaTimes(double4 q, const double* I
                         R20 * wx + R21 * wy + R22 * wz);
 }
 
-// clumpVelocityAngularVelocityIntegrate (integrate.cu:908-929) of clump c.
-__device__ void clumpKick(const DeviceState& d, int c, double dt)
+// clumpVelocityAngularVelocityIntegrate (integrate.cu:908-929): the clump's
+// new velocity v and spin w (from w0) after a kick of dt.
+__device__ __forceinline__ void clumpKickState(const DeviceState& d, int c, double dt, double3& a, double3& v,
+                                               double3& w0, double3& w)
 {
-    const double3 a = d.cacc[c];
-    const double3 w0 = d.cw[c];
-    d.cvel[c] = dadd(d.cvel[c], dscale(a, dt));
-    if (d.cinvm[c] > 0.) d.cw[c] = dadd(w0, dscale(rotInvInertiaTimes(d.cq[c], d.cinvI + 6 * c, d.ctorque[c]), dt));
-    const double3 w = d.cw[c];
-    const double3 vc = d.cvel[c];
-    const double3 cp = d.cpos[c];
-    const float3 rotn = make_float3((float)(0.5 * (w0.x + w.x) * dt), (float)(0.5 * (w0.y + w.y) * dt),
-                                    (float)(0.5 * (w0.z + w.z) * dt));
-    for (int i = d.cstart[c]; i < d.cend[c]; ++i) {
-        const double3 r = dsub(absPos(d, i), cp);
-        const double3 ai = dadd(dadd(a, dcross(a, r)), dcross(w, dcross(w, r)));
-        const double3 vi = dadd(vc, dcross(w, r));
-        d.sacc[i] = make_float4((float)ai.x, (float)ai.y, (float)ai.z, 0.f);
-        const dfl vx = df_from_double(vi.x), vy = df_from_double(vi.y), vz = df_from_double(vi.z);
-        d.svh[i] = make_float4(vx.hi, vy.hi, vz.hi, 0.f);
-        d.svl[i] = make_float4(vx.lo, vy.lo, vz.lo, 0.f);
-        const dfl wx = df_from_double(w.x), wy = df_from_double(w.y), wz = df_from_double(w.z);
-        d.swh[i] = make_float4(wx.hi, wy.hi, wz.hi, 0.f);
-        d.swl[i] = make_float4(wx.lo, wy.lo, wz.lo, 0.f);
-        d.snormal[i] = f4(rotateF(xyz(d.snormal[i]), rotn));
-    }
-    if (d.fixes & DEMSPH_FIX_CLUMP_ROTATION) {  // first-order quaternion update, renormalised
-        const double3 v = dscale(dadd(w0, w), 0.5 * dt);
-        double4 q = d.cq[c];
-        double4 n = make_double4(q.x + 0.5 * (-q.y * v.x - q.z * v.y - q.w * v.z),
-                                 q.y + 0.5 * (q.x * v.x + q.w * v.y - q.z * v.z),
-                                 q.z + 0.5 * (-q.w * v.x + q.x * v.y + q.y * v.z),
-                                 q.w + 0.5 * (q.z * v.x - q.y * v.y + q.x * v.z));
-        const double l = sqrt(n.x * n.x + n.y * n.y + n.z * n.z + n.w * n.w);
-        if (l > 0) n = make_double4(n.x / l, n.y / l, n.z / l, n.w / l);
-        d.cq[c] = n;
-    }
+    a = d.cacc[c];
+    w0 = d.cw[c];
+    v = dadd(d.cvel[c], dscale(a, dt));
+    w = w0;
+    if (d.cinvm[c] > 0.) w = dadd(w0, dscale(rotInvInertiaTimes(d.cq[c], d.cinvI + 6 * c, d.ctorque[c]), dt));
 }
 
+// The rigid-body motion handed to pebble i (clump centroid cp): acceleration,
+// velocity, spin and the normal turned by the mean spin.
+__device__ __forceinline__ void pebbleKick(const DeviceState& d, int i, double3 a, double3 v, double3 w, double3 cp,
+                                           float3 rotn)
+{
+    const double3 r = dsub(absPos(d, i), cp);
+    const double3 ai = dadd(dadd(a, dcross(a, r)), dcross(w, dcross(w, r)));
+    const double3 vi = dadd(v, dcross(w, r));
+    d.sacc[i] = make_float4((float)ai.x, (float)ai.y, (float)ai.z, 0.f);
+    const dfl vx = df_from_double(vi.x), vy = df_from_double(vi.y), vz = df_from_double(vi.z);
+    d.svh[i] = make_float4(vx.hi, vy.hi, vz.hi, 0.f);
+    d.svl[i] = make_float4(vx.lo, vy.lo, vz.lo, 0.f);
+    const dfl wx = df_from_double(w.x), wy = df_from_double(w.y), wz = df_from_double(w.z);
+    d.swh[i] = make_float4(wx.hi, wy.hi, wz.hi, 0.f);
+    d.swl[i] = make_float4(wx.lo, wy.lo, wz.lo, 0.f);
+    d.snormal[i] = f4(rotateF(xyz(d.snormal[i]), rotn));
+}
+
+// First-order quaternion update with the mean spin, renormalised (only with
+// DEMSPH_FIX_CLUMP_ROTATION; the reference never turns a clump's orientation).
+__device__ __forceinline__ void clumpRotate(const DeviceState& d, int c, double3 w0, double3 w, double dt)
+{
+    const double3 v = dscale(dadd(w0, w), 0.5 * dt);
+    const double4 q = d.cq[c];
+    double4 n = make_double4(q.x + 0.5 * (-q.y * v.x - q.z * v.y - q.w * v.z),
+                             q.y + 0.5 * (q.x * v.x + q.w * v.y - q.z * v.z),
+                             q.z + 0.5 * (-q.w * v.x + q.x * v.y + q.y * v.z),
+                             q.w + 0.5 * (q.z * v.x - q.y * v.y + q.x * v.z));
+    const double l = sqrt(n.x * n.x + n.y * n.y + n.z * n.z + n.w * n.w);
+    if (l > 0) n = make_double4(n.x / l, n.y / l, n.z / l, n.w / l);
+    d.cq[c] = n;
+}
+
+// Half-step clump integration (clumpVelocityAngularVelocityIntegrate and
+// clumpPositionIntegrate, integrate.cu:908-938, in the order of
+// integrate.cu:964-1027), one warp per clump: every lane computes the clump's
+// new state (the same FP64 operations, so the same bits), lane 0 stores it,
+// the lanes move the pebbles.
+//   before contact: kick, pebbles from the kicked state, centroid and pebble drift;
+//   after contact:  pebble and centroid drift, kick, pebbles from the kicked state.
 __global__ void kClumpIntegrate(DeviceState d, double half, dfl halfDF, int before)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= d.nc || *d.status) return;
-    if (before) {
-        clumpKick(d, c, half);
-        d.cpos[c] = dadd(d.cpos[c], dscale(d.cvel[c], half));
-        for (int i = d.cstart[c]; i < d.cend[c]; ++i) driftSolid(d, i, halfDF);
-    } else {
-        for (int i = d.cstart[c]; i < d.cend[c]; ++i) driftSolid(d, i, halfDF);
-        d.cpos[c] = dadd(d.cpos[c], dscale(d.cvel[c], half));
-        clumpKick(d, c, half);
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (c >= d.nc || *d.status) return;  // uniform over the warp
+    const int s = d.cstart[c], e = d.cend[c];
+    if (!before)
+        for (int i = s + lane; i < e; i += 32) driftSolid(d, i, halfDF);
+    const double3 cp = before ? d.cpos[c] : dadd(d.cpos[c], dscale(d.cvel[c], half));
+    double3 a, v, w0, w;
+    clumpKickState(d, c, half, a, v, w0, w);
+    const float3 rotn = make_float3((float)(0.5 * (w0.x + w.x) * half), (float)(0.5 * (w0.y + w.y) * half),
+                                    (float)(0.5 * (w0.z + w.z) * half));
+    __syncwarp();  // every lane has read the old state
+    if (lane == 0) {
+        d.cvel[c] = v;
+        d.cw[c] = w;
+        d.cpos[c] = before ? dadd(cp, dscale(v, half)) : cp;
+        if (d.fixes & DEMSPH_FIX_CLUMP_ROTATION) clumpRotate(d, c, w0, w, half);
+    }
+    for (int i = s + lane; i < e; i += 32) {
+        pebbleKick(d, i, a, v, w, cp, rotn);
+        if (before) driftSolid(d, i, halfDF);
+        else checkDisplacement(d, i);
     }
 }
 
@@ -531,9 +610,8 @@ __global__ void kStepDone(int* status, int* steps)
 
 void launchPairContacts(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
-    if (d.ns <= 0) return;
-    const int blocks = blocksFor(d.ssCap < 1 ? 1 : d.ssCap, T);
-    ++t_kernelLaunches, kPairContacts<<<blocks < 152 * 16 ? blocks : 152 * 16, T, 0, s>>>(d, par, dt);
+    if (d.nrow <= 0) return;
+    ++t_kernelLaunches, kPairContacts<<<blocksFor(d.nrow, T), T, 0, s>>>(d, par, dt);
 }
 void launchBonds(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
@@ -548,15 +626,18 @@ void launchGatherWalls(const DeviceState& d, int par, float dt, cudaStream_t s)
 void launchClumpForce(const DeviceState& d, cudaStream_t s)
 {
     if (d.nc <= 0) return;
-    ++t_kernelLaunches, kClumpForce<<<blocksFor(d.nc, 64), 64, 0, s>>>(d);
+    ++t_kernelLaunches, kClumpForce<<<blocksFor(d.nc, 8), 256, 0, s>>>(d);
 }
 void launchSolidIntegrate(const DeviceState& d, double dt, bool before, cudaStream_t s)
 {
     const double half = 0.5 * dt;
     const dfl h = df_from_double(half);
     if (d.ns > 0) ++t_kernelLaunches, kSolidIntegrate<<<blocksFor(d.ns, 256), 256, 0, s>>>(d, h, before ? 1 : 0);
-    if (d.nc > 0) ++t_kernelLaunches, kClumpIntegrate<<<blocksFor(d.nc, 64), 64, 0, s>>>(d, half, h, before ? 1 : 0);
+    if (d.nc > 0) ++t_kernelLaunches, kClumpIntegrate<<<blocksFor(d.nc, 8), 256, 0, s>>>(d, half, h, before ? 1 : 0);
 }
-void launchStepDone(const DeviceState& d, cudaStream_t s) { ++t_kernelLaunches, kStepDone<<<1, 1, 0, s>>>(d.status, d.stepsDone); }
+void launchStepDone(const DeviceState& d, cudaStream_t s)
+{
+    ++t_kernelLaunches, kStepDone<<<1, 1, 0, s>>>(d.status, d.stepsDone);
+}
 
 }  // namespace demsph

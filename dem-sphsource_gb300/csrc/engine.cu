@@ -121,18 +121,18 @@ void allocFluidLists(demsph_engine* e)
     if (e->debug & 1) d.fsPairForce = dalloc<float4>((size_t)d.kfs * d.nf, e->owned);
 }
 
+// Per-slot arrays of the contact rows (scap slots per row).
 void allocContactLists(demsph_engine* e)
 {
     DeviceState& d = e->d;
-    const size_t c = (size_t)d.ssCap;
-    d.spa = dalloc<int>(c, e->owned);
-    d.srpartner = dalloc<int>(c, e->owned);
+    const size_t c = (size_t)d.scap * std::max(1, d.nrow);
+    d.rev = dalloc<int>(c, e->owned);
     d.pF = dalloc<float4>(c, e->owned);
     d.pT = dalloc<float4>(c, e->owned);
     d.pTA = dalloc<float4>(c, e->owned);
     d.pTB = dalloc<float4>(c, e->owned);
     for (int p = 0; p < 2; ++p) {
-        d.spb[p] = dalloc<int>(c, e->owned);
+        d.fwd[p] = dalloc<int>(c, e->owned);
         for (int k = 0; k < 3; ++k) d.spring[p][k] = dalloc<float4>(c, e->owned);
     }
 }
@@ -170,7 +170,7 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
     }
     {
         TIMED("solid_hash_sort");
-        launchSolidHashSort(d, s);
+        launchSolidHashSort(d, fluidStep || e->forceWalk, s);
     }
     if (fluidStep) {
         {
@@ -182,7 +182,8 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
     }
     e->par ^= 1;
     TIMED("solid_contact_list");
-    launchSolidContactList(d, e->par, s);
+    e->walkOrder[e->par] = e->forceWalk;
+    launchSolidContactList(d, e->par, e->forceWalk, s);
 }
 
 void stageBefore(demsph_engine* e, double dt)
@@ -277,28 +278,38 @@ void grow(demsph_engine* e, int status)
         if (status & ST_FS_OVERFLOW) d.kfs *= 2;
         allocFluidLists(e);
     }
-    if (status & ST_SS_OVERFLOW) {
-        const int keep = e->par, failed = e->par ^ 1;
+    if (status & (ST_SS_OVERFLOW | ST_VERLET_OVERFLOW)) {
         int need[2] = {0, 0};
-        CK(cudaMemcpy(&need[0], d.sfbase[failed] + d.ns, sizeof(int), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(&need[1], d.srbase + d.ns, sizeof(int), cudaMemcpyDeviceToHost));
-        // keep the spring history (the last successful list) across the reallocation
-        const int old = d.ssCap;
-        std::vector<int> pb(old);
-        std::vector<float4> sp[3];
-        CK(cudaMemcpy(pb.data(), d.spb[keep], sizeof(int) * old, cudaMemcpyDeviceToHost));
-        for (int k = 0; k < 3; ++k) {
-            sp[k].resize(old);
-            CK(cudaMemcpy(sp[k].data(), d.spring[keep][k], sizeof(float4) * old, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(need, d.need, sizeof(int) * 2, cudaMemcpyDeviceToHost));
+        CK(cudaMemset(d.need, 0, sizeof(int) * 2));
+        const size_t nr = (size_t)std::max(1, d.nrow);
+        if (status & ST_SS_OVERFLOW) {
+            // keep the spring history (the last successful list): slot k of row r
+            // is element k * nrow + r, so the old slots are a prefix of the new
+            const int keep = e->par;
+            const size_t old = (size_t)d.scap * nr;
+            int* keepFwd = d.fwd[keep];
+            float4* keepSpring[3] = {d.spring[keep][0], d.spring[keep][1], d.spring[keep][2]};
+            d.fwd[keep] = nullptr;
+            for (int k = 0; k < 3; ++k) d.spring[keep][k] = nullptr;
+            void* ptrs[] = {d.rev, d.pF, d.pT, d.pTA, d.pTB, d.fwd[keep ^ 1], d.spring[keep ^ 1][0],
+                            d.spring[keep ^ 1][1], d.spring[keep ^ 1][2]};
+            for (void* p : ptrs) freeOne(e, p);
+            d.scap = std::max(d.scap * 2, need[0] + need[0] / 2 + 1);
+            allocContactLists(e);
+            CK(cudaMemcpy(d.fwd[keep], keepFwd, sizeof(int) * old, cudaMemcpyDeviceToDevice));
+            for (int k = 0; k < 3; ++k)
+                CK(cudaMemcpy(d.spring[keep][k], keepSpring[k], sizeof(float4) * old, cudaMemcpyDeviceToDevice));
+            void* olds[] = {keepFwd, keepSpring[0], keepSpring[1], keepSpring[2]};
+            for (void* p : olds) freeOne(e, p);
         }
-        void* ptrs[] = {d.spa, d.srpartner, d.pF, d.pT, d.pTA, d.pTB, d.spb[0], d.spb[1], d.spring[0][0],
-                        d.spring[0][1], d.spring[0][2], d.spring[1][0], d.spring[1][1], d.spring[1][2]};
-        for (void* p : ptrs) freeOne(e, p);
-        d.ssCap = (int)std::min<long long>(2000000000LL, (long long)(std::max(need[0], need[1]) * 1.5) + 1024);
-        allocContactLists(e);
-        CK(cudaMemcpy(d.spb[keep], pb.data(), sizeof(int) * old, cudaMemcpyHostToDevice));
-        for (int k = 0; k < 3; ++k)
-            CK(cudaMemcpy(d.spring[keep][k], sp[k].data(), sizeof(float4) * old, cudaMemcpyHostToDevice));
+        if (status & ST_VERLET_OVERFLOW) {
+            void* p = d.vcand;
+            freeOne(e, p);
+            d.vcap = std::max(d.vcap * 2, need[1] + need[1] / 2 + 1);
+            d.vcand = dalloc<int>((size_t)d.vcap * nr, e->owned, false);
+            CK(cudaMemset(d.rebuild, 0xff, sizeof(int)));  // rebuild on the retry
+        }
     }
     if (status & ST_COUPLE_OVERFLOW) {
         int need = 0;
@@ -308,11 +319,16 @@ void grow(demsph_engine* e, int status)
         d.coupCap = (int)std::min<long long>(2000000000LL, (long long)(need * 1.5) + 1024);
         d.coupList = dalloc<int>(d.coupCap, e->owned);
     }
+    if (status & ST_MODE_CHANGE) {
+        // the abandoned step may have counted some solids into cells
+        CK(cudaMemset(d.scellCount, 0, sizeof(int) * d.grid.num));
+    }
     CK(cudaMemset(d.status, 0, sizeof(int)));
     dropGraph(e);
 }
 
-constexpr int ALL_OVERFLOWS = ST_FF_OVERFLOW | ST_FS_OVERFLOW | ST_SS_OVERFLOW | ST_COUPLE_OVERFLOW;
+constexpr int ALL_OVERFLOWS =
+    ST_FF_OVERFLOW | ST_FS_OVERFLOW | ST_SS_OVERFLOW | ST_COUPLE_OVERFLOW | ST_VERLET_OVERFLOW | ST_MODE_CHANGE;
 
 // Neighbour search of the staged API: synchronises once, grows and retries.
 int neighborSearchChecked(demsph_engine* e, int iStep, int gap)
@@ -559,13 +575,43 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.ssortTmp = dalloc<int>(ns, e->owned);
             d.scellCount = dalloc<int>(d.grid.num, e->owned);
             d.scellStart = dalloc<int>((size_t)d.grid.num + 1, e->owned);
-            d.sfcnt = dalloc<int>(ns, e->owned);
-            d.srcnt = dalloc<int>(ns, e->owned);
-            d.sfbase[0] = dalloc<int>((size_t)ns + 1, e->owned);
-            d.sfbase[1] = dalloc<int>((size_t)ns + 1, e->owned);
-            d.srbase = dalloc<int>((size_t)ns + 1, e->owned);
-            d.ssCap = std::max(1024, perParticle * ns);
+            // contact rows: every solid but the dummy wall particles, in index order
+            std::vector<int> srow(ns, -1), rowSolid;
+            double rmin = 0, effMax = 0;
+            for (int i = 0; i < ns; ++i) {
+                if (flags[i].w & F_DUMMY) continue;
+                srow[i] = (int)rowSolid.size();
+                rowSolid.push_back(i);
+                rmin = rowSolid.size() == 1 ? sc->solid_radius[i] : std::min(rmin, sc->solid_radius[i]);
+                effMax = std::max(effMax, sc->solid_effective_radius[i]);
+            }
+            d.nrow = (int)rowSolid.size();
+            d.srow = dalloc<int>(ns, e->owned);
+            d.rowSolid = dalloc<int>(d.nrow, e->owned);
+            d.scentre = dalloc<int4>(d.nrow, e->owned);
+            if (ns > 0) CK(cudaMemcpy(d.srow, srow.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
+            if (d.nrow > 0)
+                CK(cudaMemcpy(d.rowSolid, rowSolid.data(), sizeof(int) * d.nrow, cudaMemcpyHostToDevice));
+            const size_t nr = (size_t)std::max(1, d.nrow);
+            d.scap = perParticle;
+            d.fcnt[0] = dalloc<int>(nr, e->owned);
+            d.fcnt[1] = dalloc<int>(nr, e->owned);
+            d.rcnt = dalloc<int>(nr, e->owned);
             allocContactLists(e);
+            // Verlet candidates
+            d.skin = (float)(o.solid_verlet_skin > 0 ? o.solid_verlet_skin : 0.2 * rmin);
+            d.vmaxEff = (float)effMax;
+            d.vcap = 2 * perParticle;
+            d.vcand = dalloc<int>((size_t)d.vcap * nr, e->owned, false);
+            d.vcnt = dalloc<int>(nr, e->owned);
+            d.vref = dalloc<float4>(nr, e->owned);
+            d.rebuild = dalloc<int>(1, e->owned);
+            d.slowMode = dalloc<int>(1, e->owned);
+            d.need = dalloc<int>(2, e->owned);
+            const int one = 1;
+            const bool walkOnly = o.solid_verlet_skin < 0 || d.grid.gx < 3 || d.grid.gy < 3 || d.grid.gz < 3;
+            CK(cudaMemcpy(d.rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
+            if (walkOnly) CK(cudaMemcpy(d.slowMode, &one, sizeof(int), cudaMemcpyHostToDevice));
             d.coupCount = dalloc<int>(ns, e->owned);
             d.coupStart = dalloc<int>((size_t)ns + 1, e->owned);
             d.coupCap = std::max(1024, std::min(64 * e->nMassive + 1024, std::max(1, d.kfs * nf)));
@@ -664,18 +710,21 @@ int demsph_initialize(demsph_engine* e)
 {
     ENGINE_GUARD(e)
     DeviceState& d = e->d;
+    // the initial list comes from the reference's walk, in its order, so bonds
+    // are numbered as addBondData numbers them
+    e->forceWalk = true;
     const int rc = neighborSearchChecked(e, 0, 1);
+    e->forceWalk = false;
     if (rc != DEMSPH_OK) return rc;
     // bonds between touching spheres of one cluster
-    int np = 0;
-    if (d.ns > 0) CK(cudaMemcpy(&np, d.sfbase[e->par] + d.ns, sizeof(int), cudaMemcpyDeviceToHost));
-    np = std::min(np, d.ssCap);
-    if (np > 0) {
+    const long long nslots = (long long)d.nrow * d.scap;
+    if (nslots > 0) {
+        if (nslots > 2000000000LL) return fail(e, DEMSPH_ERR_CAPACITY, "contact rows too large for bond creation");
         std::vector<void*> tmp;
-        int* flag = dalloc<int>((size_t)np + 1, tmp);
-        int* pos = dalloc<int>((size_t)np + 1, tmp);
-        int* work = dalloc<int>(scanWorkspaceInts(np), tmp);
-        const int nb = launchBondFlags(d, e->par, np, flag, pos, work, e->stream);
+        int* flag = dalloc<int>((size_t)nslots + 1, tmp);
+        int* pos = dalloc<int>((size_t)nslots + 1, tmp);
+        int* work = dalloc<int>(scanWorkspaceInts((int)nslots), tmp);
+        const int nb = launchBondFlags(d, e->par, flag, pos, work, e->stream);
         if (nb > 0) {
             d.nb = nb;
             d.bab = dalloc<int2>(nb, e->owned);
@@ -687,7 +736,7 @@ int demsph_initialize(demsph_engine* e)
             d.bTbL = dalloc<float4>(nb, e->owned);
             d.bN = dalloc<float4>(nb, e->owned);
             d.bLever = dalloc<float4>(nb, e->owned);
-            launchBondWrite(d, e->par, np, flag, pos, e->stream);
+            launchBondWrite(d, e->par, flag, pos, e->stream);
         }
         CK(cudaStreamSynchronize(e->stream));
         for (void* p : tmp) cudaFree(p);

@@ -20,8 +20,10 @@ namespace demsph {
 enum StatusBits : int {
     ST_FF_OVERFLOW = 1,      // a fluid particle has more fluid partners than the list holds
     ST_FS_OVERFLOW = 2,      // ... more solid partners
-    ST_SS_OVERFLOW = 4,      // solid contact list (forward or reverse) over capacity
+    ST_SS_OVERFLOW = 4,      // a solid has more contacts (forward or reverse) than its row holds
     ST_COUPLE_OVERFLOW = 8,  // fluid-solid coupling reverse list over capacity
+    ST_VERLET_OVERFLOW = 16, // a solid has more contact candidates than its row holds
+    ST_MODE_CHANGE = 32,     // a solid left the domain: lists switch to the 27-cell walk; redo the step
 };
 
 struct GridDev {

@@ -43,6 +43,8 @@ struct demsph_engine {
     std::vector<void*> owned;     // every cudaMalloc'd buffer
     std::string err;
     int par = 1;                  // parity of the last successful solid list build
+    bool forceWalk = false;       // next contact list from the reference's 27-cell walk
+    bool walkOrder[2] = {true, true};  // list of each parity is in the reference's walk order
     bool initialized = false;
     int debug = 0;
     double hmax = 0;              // largest fluid smoothing length

@@ -250,6 +250,7 @@ int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel,
     if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     if (dw) CK(cudaMemcpyAsync(dw, angvel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw);
+    if (dp) CK(cudaMemsetAsync(d.rebuild, 0xff, sizeof(int), e->stream));  // candidates from the new positions
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)
@@ -335,8 +336,10 @@ int demsph_get_counts(demsph_engine* e, demsph_counts* out)
     }
     out->fluid_pairs = ff / 2;
     out->fluid_solid_pairs = fs;
-    int np = 0;
-    if (d.ns > 0) CK(cudaMemcpy(&np, d.sfbase[e->par] + d.ns, sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<int> fc;
+    d2h(fc, d.fcnt[e->par], d.nrow);
+    long long np = 0;
+    for (int r = 0; r < d.nrow; ++r) np += std::min(fc[r], d.scap);
     out->solid_pairs = np;
     out->bonds = d.nb;
     std::vector<int> on;
@@ -361,8 +364,8 @@ int demsph_export_cell_hash(demsph_engine* e, int which, int* value, int* index,
     CK(cudaStreamSynchronize(e->stream));
     const int n = which == 0 ? d.nf : d.ns;
     std::vector<int> cs;
-    d2h(cs, which == 0 ? d.fcellStart : d.scellStart, (size_t)d.grid.num + 1);
     if (which == 0) {
+        d2h(cs, d.fcellStart, (size_t)d.grid.num + 1);
         std::vector<int4> cell;
         std::vector<int> id;
         d2h(cell, d.fcell, n);
@@ -372,12 +375,18 @@ int demsph_export_cell_hash(demsph_engine* e, int which, int* value, int* index,
             if (index) index[s] = id[s];
         }
     } else {
-        std::vector<int> sorted, key;
-        d2h(sorted, d.ssorted, n);
+        // the solids' keys are computed every step, their device-side sort only
+        // when a list needs it: the (key, index) order is restored here
+        std::vector<int> key, order(n);
         d2h(key, d.skey, n);
+        for (int i = 0; i < n; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
+        cs.assign((size_t)d.grid.num + 1, 0);
+        for (int i = 0; i < n; ++i) cs[key[i] + 1]++;
+        for (int k = 0; k < d.grid.num; ++k) cs[k + 1] += cs[k];
         for (int p = 0; p < n; ++p) {
-            if (value) value[p] = key[sorted[p]];
-            if (index) index[p] = sorted[p];
+            if (value) value[p] = key[order[p]];
+            if (index) index[p] = order[p];
         }
     }
     for (int k = 0; k < d.grid.num; ++k) {
@@ -473,36 +482,91 @@ int demsph_export_solid_pairs(demsph_engine* e, int* prefix, int* pointed, int* 
     ENGINE_GUARD(e)
     DeviceState& d = e->d;
     CK(cudaStreamSynchronize(e->stream));
-    const int ns = d.ns;
+    const int ns = d.ns, nr = d.nrow, C = d.scap;
     const int par = e->par;
-    std::vector<int> fb, pa, pb;
-    d2h(fb, d.sfbase[par], (size_t)ns + 1);
-    const int np = ns > 0 ? std::min(fb[ns], d.ssCap) : 0;
-    d2h(pa, d.spa, np);
-    d2h(pb, d.spb[par], np);
-    std::vector<float4> F, T, S0, S1, S2;
-    if (force) d2h(F, d.pF, np);
-    if (torque) d2h(T, d.pT, np);
-    if (sliding) d2h(S0, d.spring[par][0], np);
-    if (rolling) d2h(S1, d.spring[par][1], np);
-    if (torsion) d2h(S2, d.spring[par][2], np);
-    auto put = [&](double* out, const std::vector<float4>& v, int k) {
-        if (!out) return;
-        out[3 * (size_t)k] = v[k].x;
-        out[3 * (size_t)k + 1] = v[k].y;
-        out[3 * (size_t)k + 2] = v[k].z;
-    };
-    for (int k = 0; k < np && k < cap; ++k) {
-        if (pointed) pointed[k] = pa[k];
-        if (pointing) pointing[k] = pb[k];
-        put(force, F, k);
-        put(torque, T, k);
-        put(sliding, S0, k);
-        put(rolling, S1, k);
-        put(torsion, S2, k);
+    std::vector<int> fc, fw, rs, key;
+    std::vector<int4> centre;
+    d2h(fc, d.fcnt[par], nr);
+    d2h(fw, d.fwd[par], (size_t)C * nr);
+    d2h(rs, d.rowSolid, nr);
+    const bool walkOrder = e->walkOrder[par];
+    if (!walkOrder) {
+        d2h(key, d.skey, ns);
+        d2h(centre, d.scentre, nr);
     }
-    if (prefix)
-        for (int i = 0; i < ns; ++i) prefix[i] = fb[i + 1];
+    std::vector<float4> F, T, S0, S1, S2;
+    const size_t all = (size_t)C * nr;
+    if (force) d2h(F, d.pF, all);
+    if (torque) d2h(T, d.pT, all);
+    if (sliding) d2h(S0, d.spring[par][0], all);
+    if (rolling) d2h(S1, d.spring[par][1], all);
+    if (torsion) d2h(S2, d.spring[par][2], all);
+    auto put = [&](double* out, const std::vector<float4>& v, long long w, size_t k) {
+        if (!out) return;
+        out[3 * w] = v[k].x;
+        out[3 * w + 1] = v[k].y;
+        out[3 * w + 2] = v[k].z;
+    };
+    // Rows ascend with the solid index, as the reference's CSR does.  A list
+    // kept in index order is put back in the reference's walk order: the
+    // partners of A by the position, in A's 27-cell walk ((z, y, x) loops
+    // around its centre cell, core/neighborSearch.cu:236-245), of the first
+    // visited cell whose key is the partner's key - the k-th copy of a partner
+    // listed twice (a key visited twice) at the k-th such cell - then by index
+    // (the stable (cell, index) sort).
+    const int gx = d.grid.gx, gy = d.grid.gy, num = d.grid.num;
+    std::vector<std::pair<long long, size_t>> order;
+    std::vector<int> walk;
+    long long w = 0;
+    int row = 0;
+    for (int i = 0; i < ns; ++i) {
+        if (row < nr && rs[row] == i) {
+            const int n = std::min(fc[row], C);
+            order.clear();
+            if (!walkOrder) {
+                walk.clear();
+                const int4 c = centre[row];
+                for (int dz = -1; dz <= 1; ++dz)
+                    for (int dy = -1; dy <= 1; ++dy)
+                        for (int dx = -1; dx <= 1; ++dx) {
+                            const long long h = (long long)(c.z + dz) * gy * gx + (long long)(c.y + dy) * gx + (c.x + dx);
+                            walk.push_back(h >= 0 && h < num ? (int)h : -1);
+                        }
+            }
+            for (int q = 0; q < n; ++q) {
+                const size_t k = (size_t)q * nr + row;
+                const int b = fw[k];
+                long long rank = q;
+                if (!walkOrder) {
+                    int copy = 0;  // earlier copies of b in this (index-ordered) row
+                    for (int p = q - 1; p >= 0 && fw[(size_t)p * nr + row] == b; --p) ++copy;
+                    int t = 27;
+                    for (int u = 0; u < 27; ++u)
+                        if (walk[u] == key[b] && copy-- == 0) {
+                            t = u;
+                            break;
+                        }
+                    rank = (long long)t * ns + b;
+                }
+                order.push_back({rank, k});
+            }
+            std::sort(order.begin(), order.end());
+            for (const auto& o : order) {
+                if (w < cap) {
+                    if (pointed) pointed[w] = i;
+                    if (pointing) pointing[w] = fw[o.second];
+                    put(force, F, w, o.second);
+                    put(torque, T, w, o.second);
+                    put(sliding, S0, w, o.second);
+                    put(rolling, S1, w, o.second);
+                    put(torsion, S2, w, o.second);
+                }
+                ++w;
+            }
+            ++row;
+        }
+        if (prefix) prefix[i] = (int)w;
+    }
     return DEMSPH_OK;
     ENGINE_END(e)
 }

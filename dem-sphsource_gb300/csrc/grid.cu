@@ -12,7 +12,8 @@
 //      original index) - the same (key, index) order as the reference's stable
 //      sort, deterministically.
 // Fluids are then physically reordered (gathered) into that order; solids keep
-// their original order and use the sorted index.
+// their original order and use the sorted index.  The solid hash also checks
+// how far each solid has moved since its contact candidates were built.
 #include "kernels.cuh"
 
 namespace demsph {
@@ -49,10 +50,10 @@ __global__ void kFluidHash(DeviceState d)
 }
 
 __global__ void kScatter(int n, const int* __restrict__ key, const int* __restrict__ slotInCell,
-                         const int* __restrict__ cellStart, int* __restrict__ out, const int* status)
+                         const int* __restrict__ cellStart, int* __restrict__ out, const int* status, RunIf when)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || *status) return;
+    if (i >= n || *status || !when.active()) return;
     out[cellStart[key[i]] + slotInCell[i]] = i;
 }
 
@@ -93,7 +94,9 @@ __global__ void kFluidGather(DeviceState d)
     d.fslot[id] = q;
 }
 
-__global__ void kSolidHash(DeviceState d)
+// Cell keys of the solids every step (they are exported in the reference's
+// objectHash); the atomic slots only when the sort follows.
+__global__ void kSolidHash(DeviceState d, RunIf sortNow)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.ns || *d.status) return;
@@ -109,16 +112,26 @@ __global__ void kSolidHash(DeviceState d)
     d.sph[i] = h;
     d.spl[i] = l;
     d.skey[i] = key;
-    d.sslotInCell[i] = atomicAdd(&d.scellCount[key], 1);
+    if (sortNow.active()) d.sslotInCell[i] = atomicAdd(&d.scellCount[key], 1);
+    const int row = d.srow[i];
+    if (row >= 0) d.scentre[row] = make_int4(truncAxis(c.x, h.x, l.x), truncAxis(c.y, h.y, l.y), truncAxis(c.z, h.z, l.z), 0);
+    if (key == d.grid.num - 1 && row >= 0 && !*d.slowMode) {
+        // a solid that can touch others left the domain: from now on the lists
+        // come from the reference's walk, which finds it through the overflow
+        // cell; this step is redone in that mode
+        *(volatile int*)d.slowMode = 1;
+        atomicOr(d.status, ST_MODE_CHANGE);
+    }
 }
 
-__global__ void kSolidRank(DeviceState d)
+__global__ void kSolidRank(DeviceState d, RunIf when)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.ns || *d.status) return;
+    if (p >= d.ns || *d.status || !when.active()) return;
     int e;
     const int q = stableRank(p, d.ssortTmp, d.skey, d.scellStart, nullptr, e);
     d.ssorted[q] = e;
+    d.scellCount[d.skey[e]] = 0;  // the counts are consumed: clear them for the next sort
 }
 
 }  // namespace
@@ -129,18 +142,23 @@ void launchFluidHashReorder(const DeviceState& d, cudaStream_t s)
     cudaMemsetAsync(d.fcellCount, 0, sizeof(int) * d.grid.num, s);
     ++t_kernelLaunches, kFluidHash<<<blocksFor(d.nf, T), T, 0, s>>>(d);
     scanExclusive(d.fcellCount, d.fcellStart, d.grid.num, d.scanWork, s);
-    ++t_kernelLaunches, kScatter<<<blocksFor(d.nf, T), T, 0, s>>>(d.nf, d.fkey, d.fslotInCell, d.fcellStart, d.fsortTmp, d.status);
+    ++t_kernelLaunches, kScatter<<<blocksFor(d.nf, T), T, 0, s>>>(d.nf, d.fkey, d.fslotInCell, d.fcellStart, d.fsortTmp, d.status, RunIf{});
     ++t_kernelLaunches, kFluidGather<<<blocksFor(d.nf, T), T, 0, s>>>(d);
 }
 
-void launchSolidHashSort(const DeviceState& d, cudaStream_t s)
+void launchSolidHashSort(const DeviceState& d, bool force, cudaStream_t s)
 {
     if (d.ns <= 0) return;
-    cudaMemsetAsync(d.scellCount, 0, sizeof(int) * d.grid.num, s);
-    ++t_kernelLaunches, kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d);
-    scanExclusive(d.scellCount, d.scellStart, d.grid.num, d.scanWork, s);
-    ++t_kernelLaunches, kScatter<<<blocksFor(d.ns, T), T, 0, s>>>(d.ns, d.skey, d.sslotInCell, d.scellStart, d.ssortTmp, d.status);
-    ++t_kernelLaunches, kSolidRank<<<blocksFor(d.ns, T), T, 0, s>>>(d);
+    // scellCount is zero here: cleared at creation, by kSolidRank after every
+    // sort, and by the host after a step abandoned in kSolidHash
+    RunIf when;
+    when.always = force ? 1 : 0;
+    when.a = d.rebuild;
+    when.b = d.slowMode;
+    ++t_kernelLaunches, kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d, when);
+    scanExclusive(d.scellCount, d.scellStart, d.grid.num, d.scanWork, s, when);
+    ++t_kernelLaunches, kScatter<<<blocksFor(d.ns, T), T, 0, s>>>(d.ns, d.skey, d.sslotInCell, d.scellStart, d.ssortTmp, d.status, when);
+    ++t_kernelLaunches, kSolidRank<<<blocksFor(d.ns, T), T, 0, s>>>(d, when);
 }
 
 }  // namespace demsph

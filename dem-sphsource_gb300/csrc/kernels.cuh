@@ -79,20 +79,36 @@ struct DeviceState {
     int* ssortTmp;
     int* scellCount;
     int* scellStart;
-    // contact list, forward CSR over solids (pairs (A, B), A < B), two parities
-    int ssCap;
-    int* sfcnt;              // ns
-    int* srcnt;              // ns
-    int* sfbase[2];          // ns + 1
-    int* srbase;             // ns + 1
-    int* spa;                // pair -> A
-    int* spb[2];             // pair -> B
-    int* srpartner;          // reverse entries: partner A' < B for each B
-    float4* spring[2][3];    // sliding, rolling, torsion springs per pair
+    // ---- contact lists: fixed slots per non-dummy solid ("row") ----
+    // Slot k of row r is element [k * nrow + r] (a warp of consecutive rows
+    // reads one line per slot).  Forward contacts (A, B) with B > A live in A's
+    // row; two parities alternate between steps so each step's springs are
+    // remapped from the previous list.  Reverse entries list the partners
+    // A < B of row B.
+    int nrow;                // solids that can be in contact (not dummy wall particles)
+    int* srow;               // solid -> row, -1 for dummy particles
+    int* rowSolid;           // row -> solid
+    int4* scentre;           // per row: centre cell of the reference's 27-cell walk at the last hash (exports)
+    int scap;                // slots per row
+    int* fwd[2];             // partner id B of each forward slot
+    int* fcnt[2];            // forward slots used per row
+    int* rev;                // partner id A of each reverse slot
+    int* rcnt;
+    float4* spring[2][3];    // sliding, rolling, torsion springs per forward slot
     float4* pF;              // pair force (on A)
     float4* pT;              // pair contact torque (rolling + torsion + bond), as the reference stores it
     float4* pTA;             // pair torque on A incl. lever arm
     float4* pTB;             // pair torque on B incl. lever arm (to subtract)
+    // Verlet candidates: partners within cut + skin at the last rebuild, by id
+    int vcap;
+    int* vcand;              // [k * nrow + r]
+    int* vcnt;
+    float4* vref;            // position (relative to the grid origin) at the last rebuild
+    float skin;              // candidate margin; a rebuild follows once a solid moved skin / 2
+    float vmaxEff;           // largest effective radius of a non-dummy solid
+    int* rebuild;            // 1: candidates are stale; set by the hash, cleared by a completed step
+    int* slowMode;           // 1: lists come from the 27-cell walk every step (grid too small, or a solid left the domain)
+    int* need;               // [0] most contacts of a row, [1] most candidates of a row (for growing)
 
     // ---- infinite walls ----
     int nw;
@@ -129,20 +145,33 @@ struct DeviceState {
     int* cend;
 };
 
+// Device-side launch condition: a kernel given one does its work when
+// `always` is set or either flag is non-zero, and otherwise returns at once
+// (work a CUDA graph holds on every step but needs only on some).
+struct RunIf {
+    int always = 1;
+    const int* a = nullptr;
+    const int* b = nullptr;
+    __device__ __forceinline__ bool active() const { return always || (a && *a) || (b && *b); }
+};
+
 // scan.cu
 size_t scanWorkspaceInts(int n);
-void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s);
+void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s, RunIf when = RunIf{});
 
 // grid.cu
 void launchFluidHashReorder(const DeviceState& d, cudaStream_t s);
-void launchSolidHashSort(const DeviceState& d, cudaStream_t s);
+// Solid cell keys every step; the sort by cell only when `force`, when the
+// contact candidates are stale or when lists come from the 27-cell walk.
+void launchSolidHashSort(const DeviceState& d, bool force, cudaStream_t s);
 
 // lists.cu
 void launchFluidLists(const DeviceState& d, cudaStream_t s);
 void launchCouplingLists(const DeviceState& d, cudaStream_t s);
-void launchSolidContactList(const DeviceState& d, int parity, cudaStream_t s);
-int launchBondFlags(const DeviceState& d, int parity, int np, int* flag, int* pos, int* work, cudaStream_t s);
-void launchBondWrite(const DeviceState& d, int parity, int np, const int* flag, const int* pos, cudaStream_t s);
+// forceWalk: build from the reference's 27-cell walk (list in the reference's order)
+void launchSolidContactList(const DeviceState& d, int parity, bool forceWalk, cudaStream_t s);
+int launchBondFlags(const DeviceState& d, int parity, int* flag, int* pos, int* work, cudaStream_t s);
+void launchBondWrite(const DeviceState& d, int parity, const int* flag, const int* pos, cudaStream_t s);
 void launchSolidNormals(const DeviceState& d, double h, cudaStream_t s);
 
 // sph.cu

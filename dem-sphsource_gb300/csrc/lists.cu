@@ -151,7 +151,7 @@ __global__ void kCoupSort(DeviceState d)
     }
 }
 
-// ---- solid contact list ----
+// ---- solid contact lists ----
 // Filters of core/neighborSearch.cu:246-263 for candidate b of particle a.
 __device__ __forceinline__ bool solidPairCandidate(const DeviceState& d, int a, int4 fa, int b)
 {
@@ -163,110 +163,203 @@ __device__ __forceinline__ bool solidPairCandidate(const DeviceState& d, int a, 
     return true;
 }
 
-template <bool FILL>
-__global__ void __launch_bounds__(T) kSolidList(DeviceState d, int par)
+// The reference's contact test |x_a - x_b| <= eff_a + eff_b
+// (core/neighborSearch.cu:264-270), always evaluated with the lower index
+// first, so that the rows of both solids reach the same decision bit for bit.
+__device__ __forceinline__ bool solidsTouch(const DeviceState& d, int a, int b)
 {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= d.ns || *d.status) return;
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    const float4 rl = d.srad[lo], rh = d.srad[hi];
+    const dfl cut = df_add(df_make(rl.z, rl.w), df_make(rh.z, rh.w));
+    return withinCut(d.scell[lo], d.sph[lo], d.spl[lo], d.scell[hi], d.sph[hi], d.spl, hi, cut, d.grid);
+}
+
+// Insertion sort of the n slots [k * nrow + r] of one row (n is small).
+__device__ __forceinline__ void sortSlots(int* v, int r, int nrow, int n)
+{
+    const size_t nr = (size_t)nrow;
+    for (int k = 1; k < n; ++k) {
+        const int x = v[(size_t)k * nr + r];
+        int q = k - 1;
+        while (q >= 0 && v[(size_t)q * nr + r] > x) {
+            v[(size_t)(q + 1) * nr + r] = v[(size_t)q * nr + r];
+            --q;
+        }
+        v[(size_t)(q + 1) * nr + r] = x;
+    }
+}
+
+__device__ __forceinline__ float3 gridPos(int4 c, float4 h, const GridDev& g)
+{
+    return make_float3((float)c.x * g.cs.x + h.x, (float)c.y * g.cs.y + h.y, (float)c.z * g.cs.z + h.z);
+}
+
+// Verlet candidates of one row: every solid passing the reference's filters
+// within eff_a + eff_b + skin, found in the cells that box overlaps.  Runs only
+// on steps where the hash found a solid displaced by more than skin / 2 since
+// the last rebuild (so every pair within eff_a + eff_b now was within
+// eff_a + eff_b + skin then).  All non-dummy solids are inside the domain
+// here (otherwise the lists come from the 27-cell walk), so the cells are
+// plain (x, y, z) cells.
+__global__ void __launch_bounds__(T) kVerletBuild(DeviceState d)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= d.nrow || *d.status || !*d.rebuild || *d.slowMode) return;
+    const int a = d.rowSolid[r];
     const int4 fa = d.sflags[a];
-    if (fa.w & F_DUMMY) {
-        if (!FILL) d.sfcnt[a] = d.srcnt[a] = 0;
+    const int4 ca = d.scell[a];
+    const float4 ha = d.sph[a];
+    const float effA = d.srad[a].z;
+    const float reach = effA + d.vmaxEff + d.skin;
+    const GridDev& g = d.grid;
+    const int x0 = max(0, ca.x + (int)floorf((ha.x - reach) / g.cs.x)), x1 = min(g.gx - 1, ca.x + (int)floorf((ha.x + reach) / g.cs.x));
+    const int y0 = max(0, ca.y + (int)floorf((ha.y - reach) / g.cs.y)), y1 = min(g.gy - 1, ca.y + (int)floorf((ha.y + reach) / g.cs.y));
+    const int z0 = max(0, ca.z + (int)floorf((ha.z - reach) / g.cs.z)), z1 = min(g.gz - 1, ca.z + (int)floorf((ha.z + reach) / g.cs.z));
+    int n = 0;
+    for (int z = z0; z <= z1; ++z)
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) {
+                const int hash = (z * g.gy + y) * g.gx + x;
+                for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
+                    const int b = d.ssorted[p];
+                    if (!solidPairCandidate(d, a, fa, b)) continue;
+                    const float3 rr = relF(ca, ha, make_int4(x, y, z, hash), d.sph[b], g);
+                    const float c = (effA + d.srad[b].z + d.skin) * 1.0001f;
+                    if (dot3(rr, rr) > c * c) continue;
+                    if (n < d.vcap) d.vcand[(size_t)n * d.nrow + r] = b;
+                    ++n;
+                }
+            }
+    // by index: the contact list filtered from them is then in index order
+    sortSlots(d.vcand, r, d.nrow, min(n, d.vcap));
+    d.vcnt[r] = n;
+    d.vref[r] = f4(gridPos(ca, ha, g));
+    if (n > d.vcap) {
+        atomicOr(d.status, ST_VERLET_OVERFLOW);
+        atomicMax(&d.need[1], n);
+    }
+}
+
+// One row's contacts of this step (setSolid2SolidInteractionsKernel,
+// core/neighborSearch.cu:222-312): the partners that pass the reference's
+// test, either from the Verlet candidates or - for grids under 3 cells on an
+// axis, or once a solid has left the domain - from the reference's own 27-cell
+// walk.  Forward partners (B > A) and reverse partners (B < A) are kept in
+// index order, whichever way they were found, so the forces - and their sums
+// per solid - do not depend on the candidate margin; the reference's pair
+// order (walk order) matters only to exports, which restore it.  Each forward
+// pair then takes the springs of the same pair in the previous list (the exact
+// history remap of the reference).  At initialisation (forceWalk) the list
+// stays in walk order: bonds are numbered in it.
+__global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int forceWalk)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= d.nrow || *d.status) return;
+    // the candidates (if this step rebuilt them) are fresh from here on; the
+    // last drift of the step raises the flag again if a solid moves too far
+    if (r == 0 && !forceWalk) *(volatile int*)d.rebuild = 0;
+    const int a = d.rowSolid[r];
+    const int4 fa = d.sflags[a];
+    const int prev = par ^ 1;
+    const int C = d.scap;
+    const size_t nr = (size_t)d.nrow;
+    int nf = 0, nb = 0;
+    auto emit = [&](int b) {
+        if (b > a) {
+            if (nf < C) d.fwd[par][(size_t)nf * nr + r] = b;
+            ++nf;
+        } else {
+            if (nb < C) d.rev[(size_t)nb * nr + r] = b;
+            ++nb;
+        }
+    };
+    const bool walk = forceWalk || *d.slowMode;
+    if (walk) {
+        const int4 ca = d.scell[a];
+        const float4 ha = d.sph[a], la = d.spl[a];
+        forStencil(ca, ha, la, d.grid, [&](int hash, bool, int, int, int) {
+            for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
+                const int b = d.ssorted[p];
+                if (solidPairCandidate(d, a, fa, b) && solidsTouch(d, a, b)) emit(b);
+            }
+        });
+    } else {
+        const int n = min(d.vcnt[r], d.vcap);
+        for (int k = 0; k < n; ++k) {
+            const int b = d.vcand[(size_t)k * nr + r];
+            if (solidsTouch(d, a, b)) emit(b);
+        }
+    }
+    d.fcnt[par][r] = nf;
+    d.rcnt[r] = nb;
+    if (nf > C || nb > C) {
+        atomicOr(d.status, ST_SS_OVERFLOW);
+        atomicMax(&d.need[0], max(nf, nb));
         return;
     }
-    const int4 ca = d.scell[a];
-    const float4 ha = d.sph[a], la = d.spl[a];
-    const float4 ra = d.srad[a];
-    const dfl effA = df_make(ra.z, ra.w);
-    int nf = 0, nr = 0;
-    int fbase = 0, rbase = 0, pbase = 0, pend = 0;
-    const int prev = par ^ 1;
-    bool room = true;
-    if (FILL) {
-        fbase = d.sfbase[par][a];
-        rbase = d.srbase[a];
-        pbase = d.sfbase[prev][a];
-        pend = d.sfbase[prev][a + 1];
-        room = d.sfbase[par][d.ns] <= d.ssCap && d.srbase[d.ns] <= d.ssCap;
-        if (!room) {
-            if (a == 0) atomicOr(d.status, ST_SS_OVERFLOW);
-            return;
-        }
+    if (walk && !forceWalk) {
+        sortSlots(d.fwd[par], r, d.nrow, nf);
+        sortSlots(d.rev, r, d.nrow, nb);
     }
-    forStencil(ca, ha, la, d.grid, [&](int hash, bool regular, int hx, int hy, int hz) {
-        const int4 cellHere = make_int4(hx, hy, hz, hash);
-        for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
-            const int b = d.ssorted[p];
-            if (!solidPairCandidate(d, a, fa, b)) continue;
-            const int4 cb = regular ? cellHere : d.scell[b];
-            const float4 rb = d.srad[b];
-            const dfl cut = df_add(effA, df_make(rb.z, rb.w));
-            if (!withinCut(ca, ha, la, cb, d.sph[b], d.spl, b, cut, d.grid)) continue;
-            if (b > a) {
-                if (FILL) {
-                    const int slot = fbase + nf;
-                    d.spa[slot] = a;
-                    d.spb[par][slot] = b;
-                    float4 s0 = make_float4(0, 0, 0, 0), s1 = s0, s2 = s0;
-                    for (int q = pbase; q < pend; ++q)
-                        if (d.spb[prev][q] == b) {
-                            s0 = d.spring[prev][0][q];
-                            s1 = d.spring[prev][1][q];
-                            s2 = d.spring[prev][2][q];
-                            break;
-                        }
-                    d.spring[par][0][slot] = s0;
-                    d.spring[par][1][slot] = s1;
-                    d.spring[par][2][slot] = s2;
-                }
-                ++nf;
-            } else {
-                if (FILL) d.srpartner[rbase + nr] = b;
-                ++nr;
+    const int prevCnt = min(d.fcnt[prev][r], C);
+    for (int q = 0; q < nf; ++q) {
+        const size_t slot = (size_t)q * nr + r;
+        const int b = d.fwd[par][slot];
+        float4 s0 = make_float4(0, 0, 0, 0), s1 = s0, s2 = s0;
+        for (int k = 0; k < prevCnt; ++k) {
+            const size_t ps = (size_t)k * nr + r;
+            if (d.fwd[prev][ps] == b) {
+                s0 = d.spring[prev][0][ps];
+                s1 = d.spring[prev][1][ps];
+                s2 = d.spring[prev][2][ps];
+                break;
             }
         }
-    });
-    if (!FILL) {
-        d.sfcnt[a] = nf;
-        d.srcnt[a] = nr;
+        d.spring[par][0][slot] = s0;
+        d.spring[par][1][slot] = s1;
+        d.spring[par][2][slot] = s2;
     }
 }
 
 // ---- bonds at initialisation (addBondData, core/dataBase.cpp:270-308) ----
+// Flags over (row, slot) in row-major order: rows ascend with the solid index
+// and the initial list is in walk order, so the exclusive scan numbers the new
+// bonds in the reference's list order.
 __global__ void kBondFlags(DeviceState d, int par, int* flag)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int np = d.sfbase[par][d.ns];
-    if (k >= np || k >= d.ssCap) return;
-    const int a = d.spa[k], b = d.spb[par][k];
-    const float4 ra = d.srad[a], rb = d.srad[b];
-    const dfl dist = dfNorm(relDF(d.scell[a], d.sph[a], d.spl[a], d.scell[b], d.sph[b], d.spl[b], d.grid));
-    // skip when r_a + r_b + 1e-10 <= |x_a - x_b|
-    const dfl gap = df_sub(df_add_f(df_add(df_make(ra.x, ra.y), df_make(rb.x, rb.y)), 1.e-10f), dist);
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)d.nrow * d.scap) return;
+    const int r = (int)(i / d.scap), k = (int)(i % d.scap);
     int ok = 0;
-    if (df_ge0(gap) && !(gap.hi == 0.f && gap.lo == 0.f)) {
-        const int4 fa = d.sflags[a], fb = d.sflags[b];
-        const int slot = tableSlot(d.tab, fa.x, fb.x);
-        if (slot >= 0 && d.tab.bd[6 * slot + 1] > 1.e-10f && fa.y >= 0 && fa.y == fb.y) ok = 1;
+    if (k < min(d.fcnt[par][r], d.scap)) {
+        const int a = d.rowSolid[r], b = d.fwd[par][(size_t)k * d.nrow + r];
+        const float4 ra = d.srad[a], rb = d.srad[b];
+        const dfl dist = dfNorm(relDF(d.scell[a], d.sph[a], d.spl[a], d.scell[b], d.sph[b], d.spl[b], d.grid));
+        // skip when r_a + r_b + 1e-10 <= |x_a - x_b|
+        const dfl gap = df_sub(df_add_f(df_add(df_make(ra.x, ra.y), df_make(rb.x, rb.y)), 1.e-10f), dist);
+        if (df_ge0(gap) && !(gap.hi == 0.f && gap.lo == 0.f)) {
+            const int4 fa = d.sflags[a], fb = d.sflags[b];
+            const int slot = tableSlot(d.tab, fa.x, fb.x);
+            if (slot >= 0 && d.tab.bd[6 * slot + 1] > 1.e-10f && fa.y >= 0 && fa.y == fb.y) ok = 1;
+        }
     }
-    flag[k] = ok;
+    flag[i] = ok;
 }
 __global__ void kBondWrite(DeviceState d, int par, const int* flag, const int* pos)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int np = d.sfbase[par][d.ns];
-    if (k >= np || k >= d.ssCap || !flag[k]) return;
-    const int b = pos[k];
-    const int i = d.spa[k], j = d.spb[par][k];
-    const DF3 r = relDF(d.scell[i], d.sph[i], d.spl[i], d.scell[j], d.sph[j], d.spl[j], d.grid);
-    const dfl dist = dfNorm(r);
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)d.nrow * d.scap || !flag[i]) return;
+    const int r = (int)(i / d.scap), k = (int)(i % d.scap);
+    const int b = pos[i];
+    const int ii = d.rowSolid[r], j = d.fwd[par][(size_t)k * d.nrow + r];
+    const DF3 rr = relDF(d.scell[ii], d.sph[ii], d.spl[ii], d.scell[j], d.sph[j], d.spl[j], d.grid);
+    const dfl dist = dfNorm(rr);
     const float dd = dist.hi;
-    const float3 n = toF3(r) / dd;
-    const float4 ri = d.srad[i], rj = d.srad[j];
-    const float delta = df_sub(df_add(df_make(ri.x, ri.y), df_make(rj.x, rj.y)), dist).hi;
+    const float3 n = toF3(rr) / dd;
+    const float4 ri = d.srad[ii], rj = d.srad[j];
     // contact point - x_i = -(d + r_i - r_j) / 2 * n
     const float lever = -0.5f * (dd + ri.x - rj.x);
-    (void)delta;
-    d.bab[b] = make_int2(i, j);
+    d.bab[b] = make_int2(ii, j);
     d.bon[b] = 1;
     d.bFnTt[b] = make_float4(0, 0, 0, 0);
     d.bFsH[b] = d.bFsL[b] = d.bTbH[b] = d.bTbL[b] = make_float4(0, 0, 0, 0);
@@ -336,33 +429,34 @@ void launchCouplingLists(const DeviceState& d, cudaStream_t s)
     ++t_kernelLaunches, kCoupSort<<<blocksFor(d.ns, 256), 256, 0, s>>>(d);
 }
 
-void launchSolidContactList(const DeviceState& d, int par, cudaStream_t s)
+void launchSolidContactList(const DeviceState& d, int par, bool forceWalk, cudaStream_t s)
 {
-    if (d.ns <= 0) return;
-    ++t_kernelLaunches, kSolidList<false><<<blocksFor(d.ns, T), T, 0, s>>>(d, par);
-    scanExclusive(d.sfcnt, d.sfbase[par], d.ns, d.scanWork, s);
-    scanExclusive(d.srcnt, d.srbase, d.ns, d.scanWork, s);
-    ++t_kernelLaunches, kSolidList<true><<<blocksFor(d.ns, T), T, 0, s>>>(d, par);
+    if (d.nrow <= 0) return;
+    if (!forceWalk) ++t_kernelLaunches, kVerletBuild<<<blocksFor(d.nrow, T), T, 0, s>>>(d);
+    ++t_kernelLaunches, kContactDetect<<<blocksFor(d.nrow, T), T, 0, s>>>(d, par, forceWalk ? 1 : 0);
 }
 
 // Bond creation from the contact list (addBondData at initialisation,
 // core/dataBase.cpp:270-308), in two launches: flags + exclusive scan give each
 // new bond its index in list order; returns the bond count (synchronises).
-int launchBondFlags(const DeviceState& d, int par, int np, int* flag, int* pos, int* work, cudaStream_t s)
+// flag and pos hold nrow * scap + 1 ints.
+int launchBondFlags(const DeviceState& d, int par, int* flag, int* pos, int* work, cudaStream_t s)
 {
-    if (np <= 0) return 0;
-    ++t_kernelLaunches, kBondFlags<<<blocksFor(np, 256), 256, 0, s>>>(d, par, flag);
-    scanExclusive(flag, pos, np, work, s);
+    const long long n = (long long)d.nrow * d.scap;
+    if (n <= 0) return 0;
+    ++t_kernelLaunches, kBondFlags<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, par, flag);
+    scanExclusive(flag, pos, (int)n, work, s);
     int nb = 0;
-    cudaMemcpyAsync(&nb, pos + np, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&nb, pos + n, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     return nb;
 }
 
-void launchBondWrite(const DeviceState& d, int par, int np, const int* flag, const int* pos, cudaStream_t s)
+void launchBondWrite(const DeviceState& d, int par, const int* flag, const int* pos, cudaStream_t s)
 {
-    if (np <= 0 || d.nb <= 0) return;
-    ++t_kernelLaunches, kBondWrite<<<blocksFor(np, 256), 256, 0, s>>>(d, par, flag, pos);
+    const long long n = (long long)d.nrow * d.scap;
+    if (n <= 0 || d.nb <= 0) return;
+    ++t_kernelLaunches, kBondWrite<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, par, flag, pos);
 }
 
 void launchSolidNormals(const DeviceState& d, double h, cudaStream_t s)

@@ -44,8 +44,10 @@ __device__ __forceinline__ int blockExclusiveScan(int v, int& total)
     return warpOffset + x - v;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) kTileSums(const int* __restrict__ in, int n, int* __restrict__ sums)
+__global__ void __launch_bounds__(SCAN_THREADS) kTileSums(const int* __restrict__ in, int n, int* __restrict__ sums,
+                                                          RunIf when)
 {
+    if (!when.active()) return;
     const long long base = (long long)blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     int s = 0;
 #pragma unroll
@@ -58,8 +60,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) kTileSums(const int* __restrict_
 
 // Scans in[0..n) into out[0..n] (out[n] = total), adding offsets[blockIdx].
 __global__ void __launch_bounds__(SCAN_THREADS) kTileScan(const int* __restrict__ in, int n, int* __restrict__ out,
-                                                          const int* __restrict__ offsets)
+                                                          const int* __restrict__ offsets, RunIf when)
 {
+    if (!when.active()) return;
     const long long base = (long long)blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     int v[SCAN_ITEMS];
     int s = 0;
@@ -91,7 +94,7 @@ size_t scanWorkspaceInts(int n)
     return w + 1;
 }
 
-void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s)
+void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s, RunIf when)
 {
     if (n <= 0) {
         cudaMemsetAsync(out, 0, sizeof(int), s);
@@ -99,14 +102,14 @@ void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s)
     }
     const int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (tiles == 1) {
-        ++t_kernelLaunches, kTileScan<<<1, SCAN_THREADS, 0, s>>>(in, n, out, nullptr);
+        ++t_kernelLaunches, kTileScan<<<1, SCAN_THREADS, 0, s>>>(in, n, out, nullptr, when);
         return;
     }
     int* sums = work;
     int* offs = work + tiles;  // tiles + 1 entries
-    ++t_kernelLaunches, kTileSums<<<tiles, SCAN_THREADS, 0, s>>>(in, n, sums);
-    scanExclusive(sums, offs, tiles, offs + tiles + 1, s);
-    ++t_kernelLaunches, kTileScan<<<tiles, SCAN_THREADS, 0, s>>>(in, n, out, offs);
+    ++t_kernelLaunches, kTileSums<<<tiles, SCAN_THREADS, 0, s>>>(in, n, sums, when);
+    scanExclusive(sums, offs, tiles, offs + tiles + 1, s, when);
+    ++t_kernelLaunches, kTileScan<<<tiles, SCAN_THREADS, 0, s>>>(in, n, out, offs, when);
 }
 
 }  // namespace demsph

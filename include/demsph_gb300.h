@@ -141,6 +141,9 @@ typedef struct demsph_options {
     int solid_contacts_per_particle; /* contact list capacity / solid count; 0 = 16 */
     int fixes;                   /* DEMSPH_FIX_* bits; 0 = reference behaviour */
     int debug;                   /* bit 0: keep each step's per-pair coupling forces for export */
+    double solid_verlet_skin;    /* margin (m) of the solid contact candidates, rebuilt once a solid has
+                                    moved half of it; 0 = 0.2 x the smallest solid radius; < 0 = no
+                                    candidates: the reference's 27-cell walk every step */
 } demsph_options;
 
 typedef struct demsph_counts {

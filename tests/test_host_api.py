@@ -83,9 +83,9 @@ def test_point_generators_match_the_reference(tmp_path):
 def read_vtu(path):
     text = open(path).read()
     arrays = {}
-    for m in re.finditer(r'<DataArray[^>]*?(?:Name="([^"]+)")?[^>]*>([^<]*)</DataArray>', text):
-        name = m.group(1) or "Points"
-        arrays[name] = np.array(m.group(2).split(), dtype=float)
+    for m in re.finditer(r'<DataArray([^>]*)>([^<]*)</DataArray>', text):
+        name = re.search(r'Name="([^"]+)"', m.group(1))
+        arrays[name.group(1) if name else "Points"] = np.array(m.group(2).split(), dtype=float)
     return arrays
 
 
