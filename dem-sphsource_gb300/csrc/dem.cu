@@ -402,32 +402,38 @@ __device__ __forceinline__ double3 absPos(const DeviceState& d, int i)
                         d.minB[2] + c.z * d.cs[2] + ((double)h.z + (double)l.z));
 }
 
-__device__ __forceinline__ double warpSumD(double v)
+// Sum over the `width` lanes of a group (width a power of two <= 32), in a
+// fixed tree: every lane gets the same bits.
+__device__ __forceinline__ double groupSumD(double v, int width)
 {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int o = width >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, width);
     return v;
 }
 
-// calClumpForceTorque (integrate.cu:860-881): one warp per clump, its lanes
-// over the pebbles, FP64 sums reduced in a fixed tree (deterministic).
-__global__ void kClumpForce(DeviceState d)
+// calClumpForceTorque (integrate.cu:860-881): a group of `width` lanes per
+// clump over its pebbles, FP64 sums reduced in a fixed tree (deterministic).
+__global__ void kClumpForce(DeviceState d, int width)
 {
-    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (c >= d.nc || *d.status) return;  // uniform over the warp
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = t / width, lane = t % width;
+    // whole warps only: the shuffles below take every lane of the warp
+    if ((t & ~31) >= d.nc * width || *d.status) return;
+    const bool live = c < d.nc;
     double3 F = make_double3(0, 0, 0), Tq = F;
-    const double3 cp = d.cpos[c];
-    for (int i = d.cstart[c] + lane; i < d.cend[c]; i += 32) {
-        double3 fi = make_double3(0, 0, 0);
-        if (d.sflags[i].w & F_MASSIVE) fi = dscale(toD3(d.sacc[i]), 1.0 / (double)d.sph[i].w);
-        F = dadd(F, fi);
-        Tq = dadd(Tq, dadd(toD3(d.storque[i]), dcross(dsub(absPos(d, i), cp), fi)));
-        d.sacc[i] = make_float4(0, 0, 0, 0);
-        d.storque[i] = make_float4(0, 0, 0, 0);
+    if (live) {
+        const double3 cp = d.cpos[c];
+        for (int i = d.cstart[c] + lane; i < d.cend[c]; i += width) {
+            double3 fi = make_double3(0, 0, 0);
+            if (d.sflags[i].w & F_MASSIVE) fi = dscale(toD3(d.sacc[i]), 1.0 / (double)d.sph[i].w);
+            F = dadd(F, fi);
+            Tq = dadd(Tq, dadd(toD3(d.storque[i]), dcross(dsub(absPos(d, i), cp), fi)));
+            d.sacc[i] = make_float4(0, 0, 0, 0);
+            d.storque[i] = make_float4(0, 0, 0, 0);
+        }
     }
-    F = make_double3(warpSumD(F.x), warpSumD(F.y), warpSumD(F.z));
-    Tq = make_double3(warpSumD(Tq.x), warpSumD(Tq.y), warpSumD(Tq.z));
-    if (lane == 0) {
+    F = make_double3(groupSumD(F.x, width), groupSumD(F.y, width), groupSumD(F.z, width));
+    Tq = make_double3(groupSumD(Tq.x, width), groupSumD(Tq.y, width), groupSumD(Tq.z, width));
+    if (live && lane == 0) {
         const double im = d.cinvm[c];
         double3 a = dscale(F, im);
         if (im > 0.) a = dadd(a, make_double3(d.g64[0], d.g64[1], d.g64[2]));
@@ -568,33 +574,47 @@ __device__ __forceinline__ void clumpRotate(const DeviceState& d, int c, double3
     d.cq[c] = n;
 }
 
+__device__ __forceinline__ double3 shflD3(double3 v, int src, int width)
+{
+    return make_double3(__shfl_sync(0xffffffffu, v.x, src, width), __shfl_sync(0xffffffffu, v.y, src, width),
+                        __shfl_sync(0xffffffffu, v.z, src, width));
+}
+
 // Half-step clump integration (clumpVelocityAngularVelocityIntegrate and
 // clumpPositionIntegrate, integrate.cu:908-938, in the order of
-// integrate.cu:964-1027), one warp per clump: every lane computes the clump's
-// new state (the same FP64 operations, so the same bits), lane 0 stores it,
-// the lanes move the pebbles.
+// integrate.cu:964-1027), a group of `width` lanes per clump: the group's
+// first lane computes the clump's new state in FP64 and hands it to the
+// others, the lanes move the pebbles.
 //   before contact: kick, pebbles from the kicked state, centroid and pebble drift;
 //   after contact:  pebble and centroid drift, kick, pebbles from the kicked state.
-__global__ void kClumpIntegrate(DeviceState d, double half, dfl halfDF, int before)
+__global__ void kClumpIntegrate(DeviceState d, double half, dfl halfDF, int before, int width)
 {
-    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (c >= d.nc || *d.status) return;  // uniform over the warp
-    const int s = d.cstart[c], e = d.cend[c];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = t / width, lane = t % width;
+    // whole warps only: the shuffles below take every lane of the warp
+    if ((t & ~31) >= d.nc * width || *d.status) return;
+    const bool live = c < d.nc;
+    const int s = live ? d.cstart[c] : 0, e = live ? d.cend[c] : 0;
     if (!before)
-        for (int i = s + lane; i < e; i += 32) driftSolid(d, i, halfDF);
-    const double3 cp = before ? d.cpos[c] : dadd(d.cpos[c], dscale(d.cvel[c], half));
-    double3 a, v, w0, w;
-    clumpKickState(d, c, half, a, v, w0, w);
-    const float3 rotn = make_float3((float)(0.5 * (w0.x + w.x) * half), (float)(0.5 * (w0.y + w.y) * half),
-                                    (float)(0.5 * (w0.z + w.z) * half));
-    __syncwarp();  // every lane has read the old state
-    if (lane == 0) {
+        for (int i = s + lane; i < e; i += width) driftSolid(d, i, halfDF);
+    double3 a = make_double3(0, 0, 0), v = a, w0 = a, w = a, cp = a;
+    if (live && lane == 0) {
+        cp = before ? d.cpos[c] : dadd(d.cpos[c], dscale(d.cvel[c], half));
+        clumpKickState(d, c, half, a, v, w0, w);
         d.cvel[c] = v;
         d.cw[c] = w;
         d.cpos[c] = before ? dadd(cp, dscale(v, half)) : cp;
         if (d.fixes & DEMSPH_FIX_CLUMP_ROTATION) clumpRotate(d, c, w0, w, half);
     }
-    for (int i = s + lane; i < e; i += 32) {
+    const int src = 0;  // lane 0 of the group
+    a = shflD3(a, src, width);
+    v = shflD3(v, src, width);
+    w0 = shflD3(w0, src, width);
+    w = shflD3(w, src, width);
+    cp = shflD3(cp, src, width);
+    const float3 rotn = make_float3((float)(0.5 * (w0.x + w.x) * half), (float)(0.5 * (w0.y + w.y) * half),
+                                    (float)(0.5 * (w0.z + w.z) * half));
+    for (int i = s + lane; i < e; i += width) {
         pebbleKick(d, i, a, v, w, cp, rotn);
         if (before) driftSolid(d, i, halfDF);
         else checkDisplacement(d, i);
@@ -626,14 +646,19 @@ void launchGatherWalls(const DeviceState& d, int par, float dt, cudaStream_t s)
 void launchClumpForce(const DeviceState& d, cudaStream_t s)
 {
     if (d.nc <= 0) return;
-    ++t_kernelLaunches, kClumpForce<<<blocksFor(d.nc, 8), 256, 0, s>>>(d);
+    const int w = d.clumpLanes;
+    ++t_kernelLaunches, kClumpForce<<<blocksFor((long long)d.nc * w, 256), 256, 0, s>>>(d, w);
 }
 void launchSolidIntegrate(const DeviceState& d, double dt, bool before, cudaStream_t s)
 {
     const double half = 0.5 * dt;
     const dfl h = df_from_double(half);
     if (d.ns > 0) ++t_kernelLaunches, kSolidIntegrate<<<blocksFor(d.ns, 256), 256, 0, s>>>(d, h, before ? 1 : 0);
-    if (d.nc > 0) ++t_kernelLaunches, kClumpIntegrate<<<blocksFor(d.nc, 8), 256, 0, s>>>(d, half, h, before ? 1 : 0);
+    if (d.nc > 0) {
+        const int w = d.clumpLanes;
+        ++t_kernelLaunches,
+            kClumpIntegrate<<<blocksFor((long long)d.nc * w, 256), 256, 0, s>>>(d, half, h, before ? 1 : 0, w);
+    }
 }
 void launchStepDone(const DeviceState& d, cudaStream_t s)
 {

@@ -673,6 +673,10 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.cinvm = dalloc<double>(nc, e->owned);
             d.cstart = dalloc<int>(nc, e->owned);
             d.cend = dalloc<int>(nc, e->owned);
+            int most = 1;
+            for (int c = 0; c < nc; ++c) most = std::max(most, sc->clump_pebble_end[c] - sc->clump_pebble_start[c]);
+            d.clumpLanes = 1;
+            while (d.clumpLanes < most && d.clumpLanes < 32) d.clumpLanes *= 2;
             if (nc > 0) {
                 CK(cudaMemcpy(d.cpos, sc->clump_centroid, sizeof(double3) * nc, cudaMemcpyHostToDevice));
                 CK(cudaMemcpy(d.cvel, sc->clump_velocity, sizeof(double3) * nc, cudaMemcpyHostToDevice));

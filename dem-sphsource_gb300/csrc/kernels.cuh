@@ -143,6 +143,7 @@ struct DeviceState {
     double* cinvm;
     int* cstart;
     int* cend;
+    int clumpLanes;          // lanes per clump in the clump kernels: a power of two <= 32 covering most pebbles
 };
 
 // Device-side launch condition: a kernel given one does its work when
