@@ -161,14 +161,15 @@ def stage_bytes(stage, c):
     kff = c.get("fluid_partners", 0.0)
     kfs = c.get("fluid_solid_partners", 0.0)
     table = {
-        # per pair: ids 8 + springs in 48 + springs out 48 + F T TA TB 64; per active solid 9 float4 reads
-        "pair_contacts": 168 * P + 144 * Ns,
-        # per active solid: cell ph pl rad flags 80 + counts 8 + bases 12; per pair: A B 8 + springs 48 in + 48 out + history ids 4 + reverse 4
+        # per pair, from both sides: partner id 4 + springs in 48 + springs out 48 + F T 32;
+        # per active solid: cell ph pl vh vl wh wl rad flags 144 + counts 8 + acc torque out 32
+        "solid_forces": 132 * P + 184 * Ns,
+        # per active solid: cell ph pl rad flags 80 + list and candidate counts 12 + walk
+        # centre 8; per pair: partner ids 8 + previous springs 48 in + springs 48 out + history id 8
         "solid_contact_list": 100 * Ns + 112 * P,
-        # per pair: F + TA forward, F + TB reverse (64) + partner id and search (8); per solid: bases 12 + flags 16 + ph 16 + acc torque out 32
-        "gather_walls": 72 * P + 76 * Ns,
-        # per solid: cell ph pl r/w 96 + key slot 8 + scatter 12 + rank 12 + sorted 4
-        "solid_hash_sort": 132 * c["n_solid"],
+        # per solid and step: cell ph pl read and written 96 + key 4 + walk centre 16 (the sort
+        # by cell runs only when lists need it)
+        "solid_hash_sort": 116 * c["n_solid"],
         # per solid: ph pl vh vl wh wl acc torque flags rad (10 float4 read, 6 written)
         "integrate_before": 256 * c["n_solid"],
         "integrate_after": 256 * c["n_solid"],

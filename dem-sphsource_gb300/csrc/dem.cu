@@ -157,40 +157,32 @@ __device__ __forceinline__ float3 contactVel(const DeviceState& d, int a, int b,
     return velDiff(d, a, b) + cross3(xyz(d.swh[a]), leverA) - cross3(xyz(d.swh[b]), leverB);
 }
 
-// Contact forces of every forward slot (calSolidContactForceTorque,
-// core/integrate.cu:423-512), one thread per row.
-__global__ void __launch_bounds__(T) kPairContacts(DeviceState d, int par, float dt)
+// One contact (calSolidContactForceTorque, core/integrate.cu:423-512) of the
+// pair (A, B), A < B, with the springs es, er, et (updated in place): the
+// force on A, the contact torque as the reference stores it, and the torques
+// on A and B with their lever arms.
+struct PairForce {
+    float3 F, T, TA, TB;
+};
+__device__ __forceinline__ PairForce pairForce(const DeviceState& d, int a, int b, float3& es, float3& er,
+                                               float3& et, float dt)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= d.nrow || *d.status) return;
-    const int a = d.rowSolid[r];
-    const int n = min(d.fcnt[par][r], d.scap);
-    if (n == 0) return;
-    const float4 ra = d.srad[a];
-    const float ima = d.sph[a].w;
-    const int mata = d.sflags[a].x;
-    for (int q = 0; q < n; ++q) {
-        const size_t k = (size_t)q * d.nrow + r;
-        const int b = d.fwd[par][k];
-        const PairGeom g = pairGeometry(d, a, b);
-        const float4 rb = d.srad[b];
-        const float R = ra.x * rb.x / (ra.x + rb.x);
-        const float m = 1.f / (ima + d.sph[b].w);
-        const float3 vc = contactVel(d, a, b, g.leverA, g.leverB);
-        const float3 wr = spinDiff(d, a, b);
-        float3 es = xyz(d.spring[par][0][k]), er = xyz(d.spring[par][1][k]), et = xyz(d.spring[par][2][k]);
-        float3 F = make_float3(0.f, 0.f, 0.f), Ft = F, Tq = F;
-        const int slot = tableSlot(d.tab, mata, d.sflags[b].x);
-        contactLaw(d.tab, slot, F, Ft, Tq, es, er, et, vc, wr, g.n, g.delta, m, R, dt);
-        d.spring[par][0][k] = f4(es);
-        d.spring[par][1][k] = f4(er);
-        d.spring[par][2][k] = f4(et);
-        d.pF[k] = f4(F);
-        d.pT[k] = f4(Tq);
-        const float3 nxF = cross3(g.n, Ft);
-        d.pTA[k] = f4(Tq + nxF * g.sA);
-        d.pTB[k] = f4(Tq + nxF * g.sB);
-    }
+    const PairGeom g = pairGeometry(d, a, b);
+    const float4 ra = d.srad[a], rb = d.srad[b];
+    const float R = ra.x * rb.x / (ra.x + rb.x);
+    const float m = 1.f / (d.sph[a].w + d.sph[b].w);
+    const float3 vc = contactVel(d, a, b, g.leverA, g.leverB);
+    const float3 wr = spinDiff(d, a, b);
+    float3 F = make_float3(0.f, 0.f, 0.f), Ft = F, Tq = F;
+    const int slot = tableSlot(d.tab, d.sflags[a].x, d.sflags[b].x);
+    contactLaw(d.tab, slot, F, Ft, Tq, es, er, et, vc, wr, g.n, g.delta, m, R, dt);
+    const float3 nxF = cross3(g.n, Ft);
+    PairForce p;
+    p.F = F;
+    p.T = Tq;
+    p.TA = Tq + nxF * g.sA;
+    p.TB = Tq + nxF * g.sB;
+    return p;
 }
 
 // Slot (index into the per-slot arrays) of the forward contact (a, b), b > a,
@@ -238,6 +230,7 @@ __global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
         d.bFnTt[b] = make_float4(0, 0, 0, 0);
         d.bFsH[b] = d.bFsL[b] = d.bTbH[b] = d.bTbL[b] = make_float4(0, 0, 0, 0);
         d.bN[b] = make_float4(0, 0, 0, 0);
+        d.bF[b] = d.bTA[b] = d.bTB[b] = make_float4(0, 0, 0, 0);
         return;
     }
     const int2 ab = d.bab[b];
@@ -245,6 +238,7 @@ __global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
     const long long slot = forwardSlot(d, par, i, j);
     if (slot < 0) {  // the pair left the contact list: the bond breaks
         d.bon[b] = 0;
+        d.bF[b] = d.bTA[b] = d.bTB[b] = make_float4(0, 0, 0, 0);
         return;
     }
     const PairGeom g = pairGeometry(d, i, j);
@@ -295,14 +289,14 @@ __global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
     d.bTbL[b] = TbL;
     d.bN[b] = f4(n);
     d.bLever[b] = f4(g.leverA);
-    // add onto the pair's force and torque (integrate.cu:802-803)
+    // the bond's share of the pair's force and torque (integrate.cu:802-803),
+    // added per solid by kSolidForces
     const float3 F = n * fn + Fs;
     const float3 Tq = n * tt + Tb;
     const float3 nxF = cross3(n, Fs);  // the lever is along n: n x (fn n) = 0
-    d.pF[slot] = f4(xyz(d.pF[slot]) + F);
-    d.pT[slot] = f4(xyz(d.pT[slot]) + Tq);
-    d.pTA[slot] = f4(xyz(d.pTA[slot]) + Tq + nxF * g.sA);
-    d.pTB[slot] = f4(xyz(d.pTB[slot]) + Tq + nxF * g.sB);
+    d.bF[b] = f4(F);
+    d.bTA[b] = f4(Tq + nxF * g.sA);
+    d.bTB[b] = f4(Tq + nxF * g.sB);
 }
 
 // Wall overlap r - ((x - p) . n) in double-float.
@@ -322,29 +316,61 @@ __device__ __forceinline__ float wallOverlap(const DeviceState& d, int4 c, float
     return del.hi + del.lo;
 }
 
-__global__ void __launch_bounds__(T) kGatherWalls(DeviceState d, int par, float dt, int withCoupling)
+// Force and torque on every solid that can touch others (calSolidForceTorque,
+// core/integrate.cu:806-858, with the contact forces of :423-512, the bonds of
+// :717-804 and the walls of :514-610), one thread per row: each contact is
+// evaluated by both of its solids (pairForce, the same bits on both sides) -
+// the forward side also advances the springs - so no per-pair forces are
+// gathered.  Sums are Kahan-compensated, in index order.
+__global__ void __launch_bounds__(T) kSolidForces(DeviceState d, int par, float dt, int withCoupling)
 {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= d.ns || *d.status) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= d.nrow || *d.status) return;
+    const int a = d.rowSolid[row];
     const int4 fa = d.sflags[a];
+    const size_t nr = (size_t)d.nrow;
     KahanF3 F, Tq;
-    const int row = d.srow[a];
-    if (row >= 0) {
-        // forward slots (+), then the reverse partners' slots of this pair (-)
-        const int n = min(d.fcnt[par][row], d.scap);
-        for (int q = 0; q < n; ++q) {
-            const size_t k = (size_t)q * d.nrow + row;
-            F.add(xyz(d.pF[k]));
-            Tq.add(xyz(d.pTA[k]));
+    // forward contacts (a, b), then reverse ones (b, a), through ONE inlined
+    // copy of pairForce: a pair's two solids run the same instructions on the
+    // same inputs and get the same bits
+    const int n = min(d.fcnt[par][row], d.scap);
+    const int total = n + min(d.rcnt[row], d.scap);
+    for (int q = 0; q < total; ++q) {
+        const bool fwdSide = q < n;
+        int A = a, B;
+        long long k;
+        if (fwdSide) {
+            k = (long long)q * nr + row;
+            B = d.fwd[par][k];
+        } else {
+            A = d.rev[(size_t)(q - n) * nr + row];
+            B = a;
+            k = forwardSlot(d, par, A, a);
+            if (k < 0) continue;
         }
-        const int m = min(d.rcnt[row], d.scap);
-        for (int q = 0; q < m; ++q) {
-            const int b = d.rev[(size_t)q * d.nrow + row];
-            const long long k = forwardSlot(d, par, b, a);
-            if (k >= 0) {
-                F.add(-xyz(d.pF[k]));
-                Tq.add(-xyz(d.pTB[k]));
-            }
+        float3 es = xyz(d.springIn[0][k]), er = xyz(d.springIn[1][k]), et = xyz(d.springIn[2][k]);
+        const PairForce p = pairForce(d, A, B, es, er, et, dt);
+        if (fwdSide) {
+            d.springOut[0][k] = f4(es);
+            d.springOut[1][k] = f4(er);
+            d.springOut[2][k] = f4(et);
+            d.pF[k] = f4(p.F);
+            d.pT[k] = f4(p.T);
+            F.add(p.F);
+            Tq.add(p.TA);
+        } else {
+            F.add(-p.F);
+            Tq.add(-p.TB);
+        }
+    }
+    for (int q = d.bondStart[a], qe = d.bondStart[a + 1]; q < qe; ++q) {
+        const int bi = d.bondList[q];
+        if (d.bab[bi].x == a) {
+            F.add(xyz(d.bF[bi]));
+            Tq.add(xyz(d.bTA[bi]));
+        } else {
+            F.add(-xyz(d.bF[bi]));
+            Tq.add(-xyz(d.bTB[bi]));
         }
     }
     if (withCoupling) F.add(-xyz(d.sfcoup[a]));
@@ -385,33 +411,32 @@ __global__ void __launch_bounds__(T) kGatherWalls(DeviceState d, int par, float 
     d.storque[a] = f4(tq);
 }
 
-__device__ __forceinline__ double3 dadd(double3 a, double3 b) { return make_double3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ double3 dsub(double3 a, double3 b) { return make_double3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ double3 dscale(double3 a, double s) { return make_double3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ double3 dcross(double3 a, double3 b)
-{
-    return make_double3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ double3 toD3(float4 v) { return make_double3(v.x, v.y, v.z); }
-__device__ __forceinline__ double3 absPos(const DeviceState& d, int i)
+// x_i - centroid of pebble i as double-float per axis, then float.
+__device__ __forceinline__ float3 pebbleLever(const DeviceState& d, int i, float4 cH, float4 cL)
 {
     const int4 c = d.scell[i];
     const float4 h = d.sph[i], l = d.spl[i];
-    return make_double3(d.minB[0] + c.x * d.cs[0] + ((double)h.x + (double)l.x),
-                        d.minB[1] + c.y * d.cs[1] + ((double)h.y + (double)l.y),
-                        d.minB[2] + c.z * d.cs[2] + ((double)h.z + (double)l.z));
+    const dfl x = df_sub(df_add(df_mul_f(d.grid.csx, (float)c.x), df_make(h.x, l.x)), df_make(cH.x, cL.x));
+    const dfl y = df_sub(df_add(df_mul_f(d.grid.csy, (float)c.y), df_make(h.y, l.y)), df_make(cH.y, cL.y));
+    const dfl z = df_sub(df_add(df_mul_f(d.grid.csz, (float)c.z), df_make(h.z, l.z)), df_make(cH.z, cL.z));
+    return make_float3(x.hi + x.lo, y.hi + y.lo, z.hi + z.lo);
 }
 
-// Sum over the `width` lanes of a group (width a power of two <= 32), in a
-// fixed tree: every lane gets the same bits.
-__device__ __forceinline__ double groupSumD(double v, int width)
+// Double-float sum over the `width` lanes of a group (width a power of two
+// <= 32), in a fixed tree: every lane gets the same bits.
+__device__ __forceinline__ dfl groupSumDF(dfl v, int width)
 {
-    for (int o = width >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, width);
+    for (int o = width >> 1; o > 0; o >>= 1) {
+        const dfl u = df_make(__shfl_xor_sync(0xffffffffu, v.hi, o, width), __shfl_xor_sync(0xffffffffu, v.lo, o, width));
+        // the same operand order on both lanes of a pair: lower lane first
+        v = (threadIdx.x & o) ? df_add(u, v) : df_add(v, u);
+    }
     return v;
 }
 
 // calClumpForceTorque (integrate.cu:860-881): a group of `width` lanes per
-// clump over its pebbles, FP64 sums reduced in a fixed tree (deterministic).
+// clump over its pebbles; the pebbles' forces (a m) and torques about the
+// centroid are summed in double-float, reduced in a fixed tree.
 __global__ void kClumpForce(DeviceState d, int width)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -419,26 +444,35 @@ __global__ void kClumpForce(DeviceState d, int width)
     // whole warps only: the shuffles below take every lane of the warp
     if ((t & ~31) >= d.nc * width || *d.status) return;
     const bool live = c < d.nc;
-    double3 F = make_double3(0, 0, 0), Tq = F;
+    dfl Fx = df_make(0.f, 0.f), Fy = Fx, Fz = Fx, Tx = Fx, Ty = Fx, Tz = Fx;
     if (live) {
-        const double3 cp = d.cpos[c];
+        const float4 cH = d.cpH[c], cL = d.cpL[c];
         for (int i = d.cstart[c] + lane; i < d.cend[c]; i += width) {
-            double3 fi = make_double3(0, 0, 0);
-            if (d.sflags[i].w & F_MASSIVE) fi = dscale(toD3(d.sacc[i]), 1.0 / (double)d.sph[i].w);
-            F = dadd(F, fi);
-            Tq = dadd(Tq, dadd(toD3(d.storque[i]), dcross(dsub(absPos(d, i), cp), fi)));
+            float3 fi = make_float3(0.f, 0.f, 0.f);
+            if (d.sflags[i].w & F_MASSIVE) fi = xyz(d.sacc[i]) / d.sph[i].w;
+            const float3 ti = xyz(d.storque[i]) + cross3(pebbleLever(d, i, cH, cL), fi);
+            Fx = df_add_f(Fx, fi.x);
+            Fy = df_add_f(Fy, fi.y);
+            Fz = df_add_f(Fz, fi.z);
+            Tx = df_add_f(Tx, ti.x);
+            Ty = df_add_f(Ty, ti.y);
+            Tz = df_add_f(Tz, ti.z);
             d.sacc[i] = make_float4(0, 0, 0, 0);
             d.storque[i] = make_float4(0, 0, 0, 0);
         }
     }
-    F = make_double3(groupSumD(F.x, width), groupSumD(F.y, width), groupSumD(F.z, width));
-    Tq = make_double3(groupSumD(Tq.x, width), groupSumD(Tq.y, width), groupSumD(Tq.z, width));
+    Fx = groupSumDF(Fx, width);
+    Fy = groupSumDF(Fy, width);
+    Fz = groupSumDF(Fz, width);
+    Tx = groupSumDF(Tx, width);
+    Ty = groupSumDF(Ty, width);
+    Tz = groupSumDF(Tz, width);
     if (live && lane == 0) {
-        const double im = d.cinvm[c];
-        double3 a = dscale(F, im);
-        if (im > 0.) a = dadd(a, make_double3(d.g64[0], d.g64[1], d.g64[2]));
-        d.cacc[c] = a;
-        d.ctorque[c] = Tq;
+        const float im = d.cinvm[c];
+        float3 a = make_float3(Fx.hi + Fx.lo, Fy.hi + Fy.lo, Fz.hi + Fz.lo) * im;
+        if (im > 0.f) a = a + d.g;
+        d.cacc[c] = f4(a);
+        d.ctorque[c] = make_float4(Tx.hi + Tx.lo, Ty.hi + Ty.lo, Tz.hi + Tz.lo, 0.f);
     }
 }
 
@@ -510,84 +544,92 @@ __global__ void kSolidIntegrate(DeviceState d, dfl half, int before)
     }
 }
 
-__device__ __forceinline__ double3 rotInvInertiaTimes(double4 q, const double* I, double3 t)
+// Symmetric 3x3 (xx yy zz xy xz yz) times a vector.
+__device__ __forceinline__ float3 symTimes(const float* I, float3 t)
 {
-    // R(q) invI R(q)^T t  (core/myMat.h:102-127 applied to a vector)
-    const double q0 = q.x, q1 = q.y, q2 = q.z, q3 = q.w;
-    const double R00 = 1 - 2 * q2 * q2 - 2 * q3 * q3, R01 = 2 * q1 * q2 - 2 * q0 * q3, R02 = 2 * q1 * q3 + 2 * q0 * q2;
-    const double R10 = 2 * q1 * q2 + 2 * q0 * q3, R11 = 1 - 2 * q1 * q1 - 2 * q3 * q3, R12 = 2 * q2 * q3 - 2 * q0 * q1;
-    const double R20 = 2 * q1 * q3 - 2 * q0 * q2, R21 = 2 * q2 * q3 + 2 * q0 * q1, R22 = 1 - 2 * q1 * q1 - 2 * q2 * q2;
-    // body frame: u = R^T t
-    const double ux = R00 * t.x + R10 * t.y + R20 * t.z;
-    const double uy = R01 * t.x + R11 * t.y + R21 * t.z;
-    const double uz = R02 * t.x + R12 * t.y + R22 * t.z;
-    // I = (xx, yy, zz, xy, xz, yz)
-    const double wx = I[0] * ux + I[3] * uy + I[4] * uz;
-    const double wy = I[3] * ux + I[1] * uy + I[5] * uz;
-    const double wz = I[4] * ux + I[5] * uy + I[2] * uz;
-    return make_double3(R00 * wx + R01 * wy + R02 * wz, R10 * wx + R11 * wy + R12 * wz,
-                        R20 * wx + R21 * wy + R22 * wz);
+    return make_float3(I[0] * t.x + I[3] * t.y + I[4] * t.z, I[3] * t.x + I[1] * t.y + I[5] * t.z,
+                       I[4] * t.x + I[5] * t.y + I[2] * t.z);
 }
 
-// clumpVelocityAngularVelocityIntegrate (integrate.cu:908-929): the clump's
-// new velocity v and spin w (from w0) after a kick of dt.
-__device__ __forceinline__ void clumpKickState(const DeviceState& d, int c, double dt, double3& a, double3& v,
-                                               double3& w0, double3& w)
+__device__ __forceinline__ void addDF(float4& h, float4& l, float3 dv)
 {
-    a = d.cacc[c];
-    w0 = d.cw[c];
-    v = dadd(d.cvel[c], dscale(a, dt));
-    w = w0;
-    if (d.cinvm[c] > 0.) w = dadd(w0, dscale(rotInvInertiaTimes(d.cq[c], d.cinvI + 6 * c, d.ctorque[c]), dt));
+    const dfl x = df_add_f(df_make(h.x, l.x), dv.x), y = df_add_f(df_make(h.y, l.y), dv.y),
+              z = df_add_f(df_make(h.z, l.z), dv.z);
+    h = make_float4(x.hi, y.hi, z.hi, 0.f);
+    l = make_float4(x.lo, y.lo, z.lo, 0.f);
 }
 
-// The rigid-body motion handed to pebble i (clump centroid cp): acceleration,
-// velocity, spin and the normal turned by the mean spin.
-__device__ __forceinline__ void pebbleKick(const DeviceState& d, int i, double3 a, double3 v, double3 w, double3 cp,
-                                           float3 rotn)
+// x += v dt in double-float (x, v as hi/lo float4 pairs).
+__device__ __forceinline__ void axpyDF(float4& xh, float4& xl, float4 vh, float4 vl, dfl dt)
 {
-    const double3 r = dsub(absPos(d, i), cp);
-    const double3 ai = dadd(dadd(a, dcross(a, r)), dcross(w, dcross(w, r)));
-    const double3 vi = dadd(v, dcross(w, r));
-    d.sacc[i] = make_float4((float)ai.x, (float)ai.y, (float)ai.z, 0.f);
-    const dfl vx = df_from_double(vi.x), vy = df_from_double(vi.y), vz = df_from_double(vi.z);
-    d.svh[i] = make_float4(vx.hi, vy.hi, vz.hi, 0.f);
-    d.svl[i] = make_float4(vx.lo, vy.lo, vz.lo, 0.f);
-    const dfl wx = df_from_double(w.x), wy = df_from_double(w.y), wz = df_from_double(w.z);
-    d.swh[i] = make_float4(wx.hi, wy.hi, wz.hi, 0.f);
-    d.swl[i] = make_float4(wx.lo, wy.lo, wz.lo, 0.f);
-    d.snormal[i] = f4(rotateF(xyz(d.snormal[i]), rotn));
+    const dfl x = df_add(df_make(xh.x, xl.x), df_mul(df_make(vh.x, vl.x), dt));
+    const dfl y = df_add(df_make(xh.y, xl.y), df_mul(df_make(vh.y, vl.y), dt));
+    const dfl z = df_add(df_make(xh.z, xl.z), df_mul(df_make(vh.z, vl.z), dt));
+    xh = make_float4(x.hi, y.hi, z.hi, 0.f);
+    xl = make_float4(x.lo, y.lo, z.lo, 0.f);
 }
 
-// First-order quaternion update with the mean spin, renormalised (only with
+// First-order quaternion update with the mean spin, renormalised, and the
+// world-frame inverse inertia from the new orientation (only with
 // DEMSPH_FIX_CLUMP_ROTATION; the reference never turns a clump's orientation).
-__device__ __forceinline__ void clumpRotate(const DeviceState& d, int c, double3 w0, double3 w, double dt)
+__device__ void clumpRotate(const DeviceState& d, int c, float3 w0, float3 w, float dt)
 {
-    const double3 v = dscale(dadd(w0, w), 0.5 * dt);
+    const double vx = 0.5 * ((double)w0.x + w.x) * dt, vy = 0.5 * ((double)w0.y + w.y) * dt,
+                 vz = 0.5 * ((double)w0.z + w.z) * dt;
     const double4 q = d.cq[c];
-    double4 n = make_double4(q.x + 0.5 * (-q.y * v.x - q.z * v.y - q.w * v.z),
-                             q.y + 0.5 * (q.x * v.x + q.w * v.y - q.z * v.z),
-                             q.z + 0.5 * (-q.w * v.x + q.x * v.y + q.y * v.z),
-                             q.w + 0.5 * (q.z * v.x - q.y * v.y + q.x * v.z));
+    double4 n = make_double4(q.x + 0.5 * (-q.y * vx - q.z * vy - q.w * vz), q.y + 0.5 * (q.x * vx + q.w * vy - q.z * vz),
+                             q.z + 0.5 * (-q.w * vx + q.x * vy + q.y * vz), q.w + 0.5 * (q.z * vx - q.y * vy + q.x * vz));
     const double l = sqrt(n.x * n.x + n.y * n.y + n.z * n.z + n.w * n.w);
     if (l > 0) n = make_double4(n.x / l, n.y / l, n.z / l, n.w / l);
     d.cq[c] = n;
+    // R invI R^T (core/myMat.h:102-127)
+    const double q0 = n.x, q1 = n.y, q2 = n.z, q3 = n.w;
+    const double R[3][3] = {{1 - 2 * q2 * q2 - 2 * q3 * q3, 2 * q1 * q2 - 2 * q0 * q3, 2 * q1 * q3 + 2 * q0 * q2},
+                            {2 * q1 * q2 + 2 * q0 * q3, 1 - 2 * q1 * q1 - 2 * q3 * q3, 2 * q2 * q3 - 2 * q0 * q1},
+                            {2 * q1 * q3 - 2 * q0 * q2, 2 * q2 * q3 + 2 * q0 * q1, 1 - 2 * q1 * q1 - 2 * q2 * q2}};
+    const double* I = d.cinvI + 6 * c;
+    const double B[3][3] = {{I[0], I[3], I[4]}, {I[3], I[1], I[5]}, {I[4], I[5], I[2]}};
+    double W[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double s = 0;
+            for (int k = 0; k < 3; ++k)
+                for (int m = 0; m < 3; ++m) s += R[i][k] * B[k][m] * R[j][m];
+            W[i][j] = s;
+        }
+    float* o = d.cIw + 6 * c;
+    o[0] = (float)W[0][0];
+    o[1] = (float)W[1][1];
+    o[2] = (float)W[2][2];
+    o[3] = (float)W[0][1];
+    o[4] = (float)W[0][2];
+    o[5] = (float)W[1][2];
 }
 
-__device__ __forceinline__ double3 shflD3(double3 v, int src, int width)
+// The rigid-body motion handed to pebble i (clumpVelocityAngularVelocityIntegrate,
+// integrate.cu:908-929): acceleration a + a x r + w x (w x r) (the reference's
+// form), velocity v + w x r, spin w, and the normal turned by the mean spin.
+__device__ __forceinline__ void pebbleKick(const DeviceState& d, int i, float3 a, float4 vH, float4 vL, float4 wH,
+                                           float4 wL, float4 cH, float4 cL, float3 rotn)
 {
-    return make_double3(__shfl_sync(0xffffffffu, v.x, src, width), __shfl_sync(0xffffffffu, v.y, src, width),
-                        __shfl_sync(0xffffffffu, v.z, src, width));
+    const float3 r = pebbleLever(d, i, cH, cL);
+    const float3 w = xyz(wH);
+    d.sacc[i] = f4(a + cross3(a, r) + cross3(w, cross3(w, r)));
+    addDF(vH, vL, cross3(w, r));
+    d.svh[i] = vH;
+    d.svl[i] = vL;
+    d.swh[i] = wH;
+    d.swl[i] = wL;
+    d.snormal[i] = f4(rotateF(xyz(d.snormal[i]), rotn));
 }
 
 // Half-step clump integration (clumpVelocityAngularVelocityIntegrate and
 // clumpPositionIntegrate, integrate.cu:908-938, in the order of
 // integrate.cu:964-1027), a group of `width` lanes per clump: the group's
-// first lane computes the clump's new state in FP64 and hands it to the
-// others, the lanes move the pebbles.
+// first lane advances the clump's state, the lanes then move the pebbles.
 //   before contact: kick, pebbles from the kicked state, centroid and pebble drift;
 //   after contact:  pebble and centroid drift, kick, pebbles from the kicked state.
-__global__ void kClumpIntegrate(DeviceState d, double half, dfl halfDF, int before, int width)
+__global__ void kClumpIntegrate(DeviceState d, dfl halfDF, int before, int width)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = t / width, lane = t % width;
@@ -597,25 +639,39 @@ __global__ void kClumpIntegrate(DeviceState d, double half, dfl halfDF, int befo
     const int s = live ? d.cstart[c] : 0, e = live ? d.cend[c] : 0;
     if (!before)
         for (int i = s + lane; i < e; i += width) driftSolid(d, i, halfDF);
-    double3 a = make_double3(0, 0, 0), v = a, w0 = a, w = a, cp = a;
+    float4 v[6];  // centroid hi lo, velocity hi lo, spin hi lo
+    float3 a = make_float3(0.f, 0.f, 0.f), w0 = a;
     if (live && lane == 0) {
-        cp = before ? d.cpos[c] : dadd(d.cpos[c], dscale(d.cvel[c], half));
-        clumpKickState(d, c, half, a, v, w0, w);
-        d.cvel[c] = v;
-        d.cw[c] = w;
-        d.cpos[c] = before ? dadd(cp, dscale(v, half)) : cp;
-        if (d.fixes & DEMSPH_FIX_CLUMP_ROTATION) clumpRotate(d, c, w0, w, half);
+        float4 cH = d.cpH[c], cL = d.cpL[c], vH = d.cvH[c], vL = d.cvL[c], wH = d.cwH[c], wL = d.cwL[c];
+        if (!before) axpyDF(cH, cL, vH, vL, halfDF);
+        a = xyz(d.cacc[c]);
+        w0 = xyz(wH);
+        const float hdt = halfDF.hi;
+        addDF(vH, vL, a * hdt);
+        if (d.cinvm[c] > 0.f) addDF(wH, wL, symTimes(d.cIw + 6 * c, xyz(d.ctorque[c])) * hdt);
+        v[0] = cH; v[1] = cL; v[2] = vH; v[3] = vL; v[4] = wH; v[5] = wL;
+        d.cvH[c] = vH;
+        d.cvL[c] = vL;
+        d.cwH[c] = wH;
+        d.cwL[c] = wL;
+        if (before) axpyDF(cH, cL, vH, vL, halfDF);
+        d.cpH[c] = cH;
+        d.cpL[c] = cL;
+        if (d.fixes & DEMSPH_FIX_CLUMP_ROTATION) clumpRotate(d, c, w0, xyz(wH), hdt);
     }
-    const int src = 0;  // lane 0 of the group
-    a = shflD3(a, src, width);
-    v = shflD3(v, src, width);
-    w0 = shflD3(w0, src, width);
-    w = shflD3(w, src, width);
-    cp = shflD3(cp, src, width);
-    const float3 rotn = make_float3((float)(0.5 * (w0.x + w.x) * half), (float)(0.5 * (w0.y + w.y) * half),
-                                    (float)(0.5 * (w0.z + w.z) * half));
+    // hand the state (centroid before this half step's drift when before
+    // contact, after it when after contact) to the group
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        v[k] = make_float4(__shfl_sync(0xffffffffu, v[k].x, 0, width), __shfl_sync(0xffffffffu, v[k].y, 0, width),
+                           __shfl_sync(0xffffffffu, v[k].z, 0, width), 0.f);
+    a = make_float3(__shfl_sync(0xffffffffu, a.x, 0, width), __shfl_sync(0xffffffffu, a.y, 0, width),
+                    __shfl_sync(0xffffffffu, a.z, 0, width));
+    w0 = make_float3(__shfl_sync(0xffffffffu, w0.x, 0, width), __shfl_sync(0xffffffffu, w0.y, 0, width),
+                     __shfl_sync(0xffffffffu, w0.z, 0, width));
+    const float3 rotn = (w0 + xyz(v[4])) * (0.5f * halfDF.hi);
     for (int i = s + lane; i < e; i += width) {
-        pebbleKick(d, i, a, v, w, cp, rotn);
+        pebbleKick(d, i, a, v[2], v[3], v[4], v[5], v[0], v[1], rotn);
         if (before) driftSolid(d, i, halfDF);
         else checkDisplacement(d, i);
     }
@@ -628,20 +684,15 @@ __global__ void kStepDone(int* status, int* steps)
 
 }  // namespace
 
-void launchPairContacts(const DeviceState& d, int par, float dt, cudaStream_t s)
-{
-    if (d.nrow <= 0) return;
-    ++t_kernelLaunches, kPairContacts<<<blocksFor(d.nrow, T), T, 0, s>>>(d, par, dt);
-}
 void launchBonds(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.nb <= 0) return;
     ++t_kernelLaunches, kBonds<<<blocksFor(d.nb, T), T, 0, s>>>(d, par, dt);
 }
-void launchGatherWalls(const DeviceState& d, int par, float dt, cudaStream_t s)
+void launchSolidForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
-    if (d.ns <= 0) return;
-    ++t_kernelLaunches, kGatherWalls<<<blocksFor(d.ns, T), T, 0, s>>>(d, par, dt, d.nf > 0 ? 1 : 0);
+    if (d.nrow <= 0) return;
+    ++t_kernelLaunches, kSolidForces<<<blocksFor(d.nrow, T), T, 0, s>>>(d, par, dt, d.nf > 0 ? 1 : 0);
 }
 void launchClumpForce(const DeviceState& d, cudaStream_t s)
 {
@@ -656,8 +707,7 @@ void launchSolidIntegrate(const DeviceState& d, double dt, bool before, cudaStre
     if (d.ns > 0) ++t_kernelLaunches, kSolidIntegrate<<<blocksFor(d.ns, 256), 256, 0, s>>>(d, h, before ? 1 : 0);
     if (d.nc > 0) {
         const int w = d.clumpLanes;
-        ++t_kernelLaunches,
-            kClumpIntegrate<<<blocksFor((long long)d.nc * w, 256), 256, 0, s>>>(d, half, h, before ? 1 : 0, w);
+        ++t_kernelLaunches, kClumpIntegrate<<<blocksFor((long long)d.nc * w, 256), 256, 0, s>>>(d, h, before ? 1 : 0, w);
     }
 }
 void launchStepDone(const DeviceState& d, cudaStream_t s)

@@ -129,11 +129,10 @@ void allocContactLists(demsph_engine* e)
     d.rev = dalloc<int>(c, e->owned);
     d.pF = dalloc<float4>(c, e->owned);
     d.pT = dalloc<float4>(c, e->owned);
-    d.pTA = dalloc<float4>(c, e->owned);
-    d.pTB = dalloc<float4>(c, e->owned);
-    for (int p = 0; p < 2; ++p) {
-        d.fwd[p] = dalloc<int>(c, e->owned);
-        for (int k = 0; k < 3; ++k) d.spring[p][k] = dalloc<float4>(c, e->owned);
+    for (int p = 0; p < 2; ++p) d.fwd[p] = dalloc<int>(c, e->owned);
+    for (int k = 0; k < 3; ++k) {
+        d.springIn[k] = dalloc<float4>(c, e->owned);
+        d.springOut[k] = dalloc<float4>(c, e->owned);
     }
 }
 
@@ -224,17 +223,13 @@ void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
 void stageContact(demsph_engine* e, double dt)
 {
     DeviceState& d = e->d;
-    {
-        TIMED("pair_contacts");
-        launchPairContacts(d, e->par, (float)dt, e->stream);
-    }
     if (d.nb > 0) {
         TIMED("bonds");
         launchBonds(d, e->par, (float)dt, e->stream);
     }
     {
-        TIMED("gather_walls");
-        launchGatherWalls(d, e->par, (float)dt, e->stream);
+        TIMED("solid_forces");
+        launchSolidForces(d, e->par, (float)dt, e->stream);
     }
     if (d.nc > 0) {
         TIMED("clump_force");
@@ -284,22 +279,22 @@ void grow(demsph_engine* e, int status)
         CK(cudaMemset(d.need, 0, sizeof(int) * 2));
         const size_t nr = (size_t)std::max(1, d.nrow);
         if (status & ST_SS_OVERFLOW) {
-            // keep the spring history (the last successful list): slot k of row r
-            // is element k * nrow + r, so the old slots are a prefix of the new
+            // keep the spring history (the last successful list and the springs
+            // its contact phase left): slot k of row r is element k * nrow + r,
+            // so the old slots are a prefix of the new
             const int keep = e->par;
             const size_t old = (size_t)d.scap * nr;
             int* keepFwd = d.fwd[keep];
-            float4* keepSpring[3] = {d.spring[keep][0], d.spring[keep][1], d.spring[keep][2]};
+            float4* keepSpring[3] = {d.springOut[0], d.springOut[1], d.springOut[2]};
             d.fwd[keep] = nullptr;
-            for (int k = 0; k < 3; ++k) d.spring[keep][k] = nullptr;
-            void* ptrs[] = {d.rev, d.pF, d.pT, d.pTA, d.pTB, d.fwd[keep ^ 1], d.spring[keep ^ 1][0],
-                            d.spring[keep ^ 1][1], d.spring[keep ^ 1][2]};
+            for (int k = 0; k < 3; ++k) d.springOut[k] = nullptr;
+            void* ptrs[] = {d.rev, d.pF, d.pT, d.fwd[keep ^ 1], d.springIn[0], d.springIn[1], d.springIn[2]};
             for (void* p : ptrs) freeOne(e, p);
             d.scap = std::max(d.scap * 2, need[0] + need[0] / 2 + 1);
             allocContactLists(e);
             CK(cudaMemcpy(d.fwd[keep], keepFwd, sizeof(int) * old, cudaMemcpyDeviceToDevice));
             for (int k = 0; k < 3; ++k)
-                CK(cudaMemcpy(d.spring[keep][k], keepSpring[k], sizeof(float4) * old, cudaMemcpyDeviceToDevice));
+                CK(cudaMemcpy(d.springOut[k], keepSpring[k], sizeof(float4) * old, cudaMemcpyDeviceToDevice));
             void* olds[] = {keepFwd, keepSpring[0], keepSpring[1], keepSpring[2]};
             for (void* p : olds) freeOne(e, p);
         }
@@ -663,14 +658,18 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
         // ---- clumps ----
         {
             const int nc = d.nc;
-            d.cpos = dalloc<double3>(nc, e->owned);
-            d.cvel = dalloc<double3>(nc, e->owned);
-            d.cacc = dalloc<double3>(nc, e->owned);
-            d.cw = dalloc<double3>(nc, e->owned);
-            d.ctorque = dalloc<double3>(nc, e->owned);
+            d.cpH = dalloc<float4>(nc, e->owned);
+            d.cpL = dalloc<float4>(nc, e->owned);
+            d.cvH = dalloc<float4>(nc, e->owned);
+            d.cvL = dalloc<float4>(nc, e->owned);
+            d.cwH = dalloc<float4>(nc, e->owned);
+            d.cwL = dalloc<float4>(nc, e->owned);
+            d.cacc = dalloc<float4>(nc, e->owned);
+            d.ctorque = dalloc<float4>(nc, e->owned);
+            d.cIw = dalloc<float>(6 * (size_t)nc, e->owned);
+            d.cinvm = dalloc<float>(nc, e->owned);
             d.cq = dalloc<double4>(nc, e->owned);
             d.cinvI = dalloc<double>(6 * (size_t)nc, e->owned);
-            d.cinvm = dalloc<double>(nc, e->owned);
             d.cstart = dalloc<int>(nc, e->owned);
             d.cend = dalloc<int>(nc, e->owned);
             int most = 1;
@@ -678,14 +677,53 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.clumpLanes = 1;
             while (d.clumpLanes < most && d.clumpLanes < 32) d.clumpLanes *= 2;
             if (nc > 0) {
-                CK(cudaMemcpy(d.cpos, sc->clump_centroid, sizeof(double3) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cvel, sc->clump_velocity, sizeof(double3) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cacc, sc->clump_acceleration, sizeof(double3) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cw, sc->clump_angular_velocity, sizeof(double3) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.ctorque, sc->clump_torque, sizeof(double3) * nc, cudaMemcpyHostToDevice));
+                std::vector<float4> pH(nc), pL(nc), vH(nc), vL(nc), wH(nc), wL(nc), acc(nc), tq(nc);
+                std::vector<float> Iw(6 * (size_t)nc), im(nc);
+                auto split = [](double3 v, float4& h, float4& l) {
+                    const dfl x = df_from_double(v.x), y = df_from_double(v.y), z = df_from_double(v.z);
+                    h = make_float4(x.hi, y.hi, z.hi, 0.f);
+                    l = make_float4(x.lo, y.lo, z.lo, 0.f);
+                };
+                for (int c = 0; c < nc; ++c) {
+                    const double3 p = v3(sc->clump_centroid, c);
+                    split(make_double3(p.x - d.minB[0], p.y - d.minB[1], p.z - d.minB[2]), pH[c], pL[c]);
+                    split(v3(sc->clump_velocity, c), vH[c], vL[c]);
+                    split(v3(sc->clump_angular_velocity, c), wH[c], wL[c]);
+                    const double3 a = v3(sc->clump_acceleration, c), t = v3(sc->clump_torque, c);
+                    acc[c] = make_float4((float)a.x, (float)a.y, (float)a.z, 0.f);
+                    tq[c] = make_float4((float)t.x, (float)t.y, (float)t.z, 0.f);
+                    im[c] = (float)sc->clump_inverse_mass[c];
+                    // world-frame inverse inertia R invI R^T (core/myMat.h:102-127)
+                    const double* q = sc->clump_orientation + 4 * c;
+                    const double q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+                    const double R[3][3] = {{1 - 2 * q2 * q2 - 2 * q3 * q3, 2 * q1 * q2 - 2 * q0 * q3, 2 * q1 * q3 + 2 * q0 * q2},
+                                            {2 * q1 * q2 + 2 * q0 * q3, 1 - 2 * q1 * q1 - 2 * q3 * q3, 2 * q2 * q3 - 2 * q0 * q1},
+                                            {2 * q1 * q3 - 2 * q0 * q2, 2 * q2 * q3 + 2 * q0 * q1, 1 - 2 * q1 * q1 - 2 * q2 * q2}};
+                    const double* I = sc->clump_inverse_inertia + 6 * c;
+                    const double B[3][3] = {{I[0], I[3], I[4]}, {I[3], I[1], I[5]}, {I[4], I[5], I[2]}};
+                    double W[3][3];
+                    for (int i = 0; i < 3; ++i)
+                        for (int j = 0; j < 3; ++j) {
+                            double sum = 0;
+                            for (int k = 0; k < 3; ++k)
+                                for (int m = 0; m < 3; ++m) sum += R[i][k] * B[k][m] * R[j][m];
+                            W[i][j] = sum;
+                        }
+                    const double w6[6] = {W[0][0], W[1][1], W[2][2], W[0][1], W[0][2], W[1][2]};
+                    for (int k = 0; k < 6; ++k) Iw[6 * c + k] = (float)w6[k];
+                }
+                CK(cudaMemcpy(d.cpH, pH.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cpL, pL.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cvH, vH.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cvL, vL.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cwH, wH.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cwL, wL.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cacc, acc.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.ctorque, tq.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cIw, Iw.data(), sizeof(float) * 6 * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(d.cinvm, im.data(), sizeof(float) * nc, cudaMemcpyHostToDevice));
                 CK(cudaMemcpy(d.cq, sc->clump_orientation, sizeof(double4) * nc, cudaMemcpyHostToDevice));
                 CK(cudaMemcpy(d.cinvI, sc->clump_inverse_inertia, sizeof(double) * 6 * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cinvm, sc->clump_inverse_mass, sizeof(double) * nc, cudaMemcpyHostToDevice));
                 CK(cudaMemcpy(d.cstart, sc->clump_pebble_start, sizeof(int) * nc, cudaMemcpyHostToDevice));
                 CK(cudaMemcpy(d.cend, sc->clump_pebble_end, sizeof(int) * nc, cudaMemcpyHostToDevice));
             }
@@ -740,10 +778,36 @@ int demsph_initialize(demsph_engine* e)
             d.bTbL = dalloc<float4>(nb, e->owned);
             d.bN = dalloc<float4>(nb, e->owned);
             d.bLever = dalloc<float4>(nb, e->owned);
+            d.bF = dalloc<float4>(nb, e->owned);
+            d.bTA = dalloc<float4>(nb, e->owned);
+            d.bTB = dalloc<float4>(nb, e->owned);
             launchBondWrite(d, e->par, flag, pos, e->stream);
         }
         CK(cudaStreamSynchronize(e->stream));
         for (void* p : tmp) cudaFree(p);
+    }
+    // bonds of each solid, in bond order (the per-solid force sums)
+    {
+        std::vector<int2> ab;
+        if (d.nb > 0) {
+            ab.resize(d.nb);
+            CK(cudaMemcpy(ab.data(), d.bab, sizeof(int2) * d.nb, cudaMemcpyDeviceToHost));
+        }
+        std::vector<int> start((size_t)d.ns + 1, 0), list(2 * (size_t)d.nb);
+        for (const int2& p : ab) {
+            start[p.x + 1]++;
+            start[p.y + 1]++;
+        }
+        for (int i = 0; i < d.ns; ++i) start[i + 1] += start[i];
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int b = 0; b < d.nb; ++b) {
+            list[fill[ab[b].x]++] = b;
+            list[fill[ab[b].y]++] = b;
+        }
+        d.bondStart = dalloc<int>((size_t)d.ns + 1, e->owned);
+        d.bondList = dalloc<int>(list.size(), e->owned);
+        if (d.ns > 0) CK(cudaMemcpy(d.bondStart, start.data(), sizeof(int) * (d.ns + 1), cudaMemcpyHostToDevice));
+        if (!list.empty()) CK(cudaMemcpy(d.bondList, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
     }
     // normals of walls and clump pebbles (setSolidNormal), kernel length = largest fluid h
     launchSolidNormals(d, e->hmax, e->stream);

@@ -128,7 +128,42 @@ __global__ void kSolidIn(DeviceState d, const double* pos, const double* vel, co
 
 __global__ void kSetClumpVelocity(DeviceState d, int c, double vx, double vy, double vz)
 {
-    d.cvel[c] = make_double3(vx, vy, vz);
+    const dfl x = df_from_double(vx), y = df_from_double(vy), z = df_from_double(vz);
+    d.cvH[c] = make_float4(x.hi, y.hi, z.hi, 0.f);
+    d.cvL[c] = make_float4(x.lo, y.lo, z.lo, 0.f);
+}
+
+// Clump state as planar FP64: centroid, velocity, acceleration, spin, torque
+// (3n each) and orientation (4n).
+__global__ void kClumpOut(DeviceState d, double* out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nc) return;
+    const size_t n3 = 3 * (size_t)d.nc;
+    const float4 pH = d.cpH[c], pL = d.cpL[c], vH = d.cvH[c], vL = d.cvL[c], wH = d.cwH[c], wL = d.cwL[c];
+    const float4 a = d.cacc[c], t = d.ctorque[c];
+    double* o = out + 3 * (size_t)c;
+    o[0] = d.minB[0] + ((double)pH.x + pL.x);
+    o[1] = d.minB[1] + ((double)pH.y + pL.y);
+    o[2] = d.minB[2] + ((double)pH.z + pL.z);
+    o[n3 + 0] = (double)vH.x + vL.x;
+    o[n3 + 1] = (double)vH.y + vL.y;
+    o[n3 + 2] = (double)vH.z + vL.z;
+    o[2 * n3 + 0] = a.x;
+    o[2 * n3 + 1] = a.y;
+    o[2 * n3 + 2] = a.z;
+    o[3 * n3 + 0] = (double)wH.x + wL.x;
+    o[3 * n3 + 1] = (double)wH.y + wL.y;
+    o[3 * n3 + 2] = (double)wH.z + wL.z;
+    o[4 * n3 + 0] = t.x;
+    o[4 * n3 + 1] = t.y;
+    o[4 * n3 + 2] = t.z;
+    const double4 q = d.cq[c];
+    double* oq = out + 5 * n3 + 4 * (size_t)c;
+    oq[0] = q.x;
+    oq[1] = q.y;
+    oq[2] = q.z;
+    oq[3] = q.w;
 }
 
 // addExternalForce (core/dataBase.cpp:179-195): a += F * invM.
@@ -209,12 +244,13 @@ int demsph_download_clumps(demsph_engine* e, double* centroid, double* vel, doub
     CK(cudaStreamSynchronize(e->stream));
     const size_t n = d.nc;
     if (n == 0) return DEMSPH_OK;
-    if (centroid) CK(cudaMemcpy(centroid, d.cpos, sizeof(double3) * n, cudaMemcpyDeviceToHost));
-    if (vel) CK(cudaMemcpy(vel, d.cvel, sizeof(double3) * n, cudaMemcpyDeviceToHost));
-    if (acc) CK(cudaMemcpy(acc, d.cacc, sizeof(double3) * n, cudaMemcpyDeviceToHost));
-    if (angvel) CK(cudaMemcpy(angvel, d.cw, sizeof(double3) * n, cudaMemcpyDeviceToHost));
-    if (torque) CK(cudaMemcpy(torque, d.ctorque, sizeof(double3) * n, cudaMemcpyDeviceToHost));
-    if (orientation) CK(cudaMemcpy(orientation, d.cq, sizeof(double4) * n, cudaMemcpyDeviceToHost));
+    double* buf = scratchDoubles(e, 19 * n);
+    ++t_kernelLaunches, kClumpOut<<<blocksFor((long long)n, 128), 128, 0, e->stream>>>(d, buf);
+    double* outs[5] = {centroid, vel, acc, angvel, torque};
+    for (int k = 0; k < 5; ++k)
+        if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + 3 * n * k, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (orientation) CK(cudaMemcpyAsync(orientation, buf + 15 * n, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)
 }
@@ -498,9 +534,44 @@ int demsph_export_solid_pairs(demsph_engine* e, int* prefix, int* pointed, int* 
     const size_t all = (size_t)C * nr;
     if (force) d2h(F, d.pF, all);
     if (torque) d2h(T, d.pT, all);
-    if (sliding) d2h(S0, d.spring[par][0], all);
-    if (rolling) d2h(S1, d.spring[par][1], all);
-    if (torsion) d2h(S2, d.spring[par][2], all);
+    if (sliding) d2h(S0, d.springOut[0], all);
+    if (rolling) d2h(S1, d.springOut[1], all);
+    if (torsion) d2h(S2, d.springOut[2], all);
+    // the reference adds each bond's force and torque onto its pair's
+    // (integrate.cu:802-803); the engine keeps them per bond
+    if ((force || torque) && d.nb > 0) {
+        std::vector<int2> ab;
+        std::vector<float4> FnTt, FsH, FsL, TbH, TbL, N;
+        d2h(ab, d.bab, d.nb);
+        d2h(FnTt, d.bFnTt, d.nb);
+        d2h(FsH, d.bFsH, d.nb);
+        d2h(FsL, d.bFsL, d.nb);
+        d2h(TbH, d.bTbH, d.nb);
+        d2h(TbL, d.bTbL, d.nb);
+        d2h(N, d.bN, d.nb);
+        std::vector<int> rowOf(ns, -1);
+        for (int r = 0; r < nr; ++r) rowOf[rs[r]] = r;
+        for (int b = 0; b < d.nb; ++b) {
+            const int r = rowOf[ab[b].x];
+            if (r < 0) continue;
+            for (int q = 0; q < std::min(fc[r], C); ++q) {
+                const size_t k = (size_t)q * nr + r;
+                if (fw[k] != ab[b].y) continue;
+                const float fn = FnTt[b].x + FnTt[b].y, tt = FnTt[b].z + FnTt[b].w;
+                if (force) {
+                    F[k].x += N[b].x * fn + (FsH[b].x + FsL[b].x);
+                    F[k].y += N[b].y * fn + (FsH[b].y + FsL[b].y);
+                    F[k].z += N[b].z * fn + (FsH[b].z + FsL[b].z);
+                }
+                if (torque) {
+                    T[k].x += N[b].x * tt + (TbH[b].x + TbL[b].x);
+                    T[k].y += N[b].y * tt + (TbH[b].y + TbL[b].y);
+                    T[k].z += N[b].z * tt + (TbH[b].z + TbL[b].z);
+                }
+                break;
+            }
+        }
+    }
     auto put = [&](double* out, const std::vector<float4>& v, long long w, size_t k) {
         if (!out) return;
         out[3 * w] = v[k].x;

@@ -94,11 +94,12 @@ struct DeviceState {
     int* fcnt[2];            // forward slots used per row
     int* rev;                // partner id A of each reverse slot
     int* rcnt;
-    float4* spring[2][3];    // sliding, rolling, torsion springs per forward slot
-    float4* pF;              // pair force (on A)
-    float4* pT;              // pair contact torque (rolling + torsion + bond), as the reference stores it
-    float4* pTA;             // pair torque on A incl. lever arm
-    float4* pTB;             // pair torque on B incl. lever arm (to subtract)
+    // sliding, rolling, torsion springs per forward slot: as remapped from the
+    // previous list (In) and after this step's contact forces (Out)
+    float4* springIn[3];
+    float4* springOut[3];
+    float4* pF;              // pair contact force on A, as the reference stores it (exports)
+    float4* pT;              // pair contact torque (rolling + torsion), as the reference stores it (exports)
     // Verlet candidates: partners within cut + skin at the last rebuild, by id
     int vcap;
     int* vcand;              // [k * nrow + r]
@@ -129,18 +130,31 @@ struct DeviceState {
     float4* bTbL;
     float4* bN;              // contact normal
     float4* bLever;          // contact point - position of A
+    float4* bF;              // this step's bond force on i
+    float4* bTA;             // ... torque on i (with lever arm)
+    float4* bTB;             // ... torque on j (with lever arm, to subtract)
+    int* bondStart;          // bonds of each solid: bondList[bondStart[s] .. bondStart[s + 1])
+    int* bondList;
     float4* fsPairForce;     // optional: per fluid-solid pair coupling force of the last step (column-major)
 
-    // ---- clumps (FP64) ----
+    // ---- clumps ----
+    // Centroid (relative to the grid minimum), velocity and spin in
+    // double-float; forces in FP32.  GB300's FP64 pipe is two orders of
+    // magnitude slower than FP32, so FP64 is left to the orientation and the
+    // body-frame inertia, which the step only reads through cIw.
     int nc;
-    double3* cpos;
-    double3* cvel;
-    double3* cacc;
-    double3* cw;
-    double3* ctorque;
-    double4* cq;
-    double* cinvI;           // 6 per clump
-    double* cinvm;
+    float4* cpH;
+    float4* cpL;
+    float4* cvH;
+    float4* cvL;
+    float4* cwH;
+    float4* cwL;
+    float4* cacc;
+    float4* ctorque;
+    float* cIw;              // world-frame inverse inertia R invI R^T, 6 per clump (xx yy zz xy xz yz)
+    float* cinvm;
+    double4* cq;             // orientation (q0 q1 q2 q3)
+    double* cinvI;           // body-frame inverse inertia, 6 per clump (xx yy zz xy xz yz)
     int* cstart;
     int* cend;
     int clumpLanes;          // lanes per clump in the clump kernels: a power of two <= 32 covering most pebbles
@@ -186,9 +200,9 @@ void launchCoupling(const DeviceState& d, int src, cudaStream_t s);
 void launchCouplingPairForces(const DeviceState& d, int src, float4* out, cudaStream_t s);
 
 // dem.cu
-void launchPairContacts(const DeviceState& d, int parity, float dt, cudaStream_t s);
 void launchBonds(const DeviceState& d, int parity, float dt, cudaStream_t s);
-void launchGatherWalls(const DeviceState& d, int parity, float dt, cudaStream_t s);
+// Contact, bond, wall, coupling and gravity forces of every solid.
+void launchSolidForces(const DeviceState& d, int parity, float dt, cudaStream_t s);
 void launchClumpForce(const DeviceState& d, cudaStream_t s);
 void launchSolidIntegrate(const DeviceState& d, double dt, bool beforeContact, cudaStream_t s);
 void launchStepDone(const DeviceState& d, cudaStream_t s);

@@ -249,7 +249,8 @@ __global__ void __launch_bounds__(T) kVerletBuild(DeviceState d)
 // per solid - do not depend on the candidate margin; the reference's pair
 // order (walk order) matters only to exports, which restore it.  Each forward
 // pair then takes the springs of the same pair in the previous list (the exact
-// history remap of the reference).  At initialisation (forceWalk) the list
+// history remap of the reference, from the springs the last contact phase
+// left in the previous list's slots).  At initialisation (forceWalk) the list
 // stays in walk order: bonds are numbered in it.
 __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int forceWalk)
 {
@@ -309,15 +310,15 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
         for (int k = 0; k < prevCnt; ++k) {
             const size_t ps = (size_t)k * nr + r;
             if (d.fwd[prev][ps] == b) {
-                s0 = d.spring[prev][0][ps];
-                s1 = d.spring[prev][1][ps];
-                s2 = d.spring[prev][2][ps];
+                s0 = d.springOut[0][ps];
+                s1 = d.springOut[1][ps];
+                s2 = d.springOut[2][ps];
                 break;
             }
         }
-        d.spring[par][0][slot] = s0;
-        d.spring[par][1][slot] = s1;
-        d.spring[par][2][slot] = s2;
+        d.springIn[0][slot] = s0;
+        d.springIn[1][slot] = s1;
+        d.springIn[2][slot] = s2;
     }
 }
 
