@@ -230,13 +230,157 @@ def cpu_baseline(scene, gap, dt, budget_s, nf, n_mobile):
                       f"FP64 oracle, OpenMP over particles"}
 
 
+# ---- many scenes: batched (config 3) and served (config 4) -----------------------------------
+def scene_updates(scene, steps):
+    nf, n_mobile, _ = mobile_counts(scene)
+    return updates_for(1, steps, scene.fluid_integrate_gap, nf, n_mobile)
+
+
+def run_many(args, world, rank, local):
+    """Config 3: the batched mix through the scene server, against the same
+    scenes run one at a time.  Config 4: a Poisson stream of requests served
+    for --duration seconds.  Under torchrun every rank runs its own server on
+    its own GPU over its share of the scenes (no exchange between ranks)."""
+    ds = _package()
+    import dem_sphsource_gb300.scenes as sc
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    device = local if world > 1 else 0
+    torch.cuda.set_device(device)
+    # warm-up: one small scene (module load, pool, graph instantiation)
+    _, wsc = ds.build_scene(sc.tiny_coupled())
+    warm = ds.Server(device=device, workers=1)
+    warm.wait(warm.submit(wsc, 10), 600.0)
+    warm.close()
+
+    def reduce(v, op):
+        if not dist:
+            return v
+        t = torch.tensor([float(v)], device="cuda")
+        dist.all_reduce(t, op=op)
+        return float(t.item())
+
+    budget = 150 << 30
+    if args.config == 3:
+        steps = args.steps if args.steps != 2000 else 1000
+        recipes = sc.batch_mix(n_scenes=args.scenes, steps=steps)[rank::world]
+        built = [ds.build_scene(r) for r in recipes]
+        total = sum(scene_updates(s, steps) for _, s in built)
+        srv = ds.Server(device=device, workers=args.workers, hbm_budget_bytes=budget)
+        if dist:
+            dist.barrier()
+        with ClockSampler(device) as clocks:
+            t0 = time.perf_counter()
+            for _, s in built:
+                srv.submit(s, steps)
+            srv.wait(-1, -1.0)
+            wall = time.perf_counter() - t0
+        st = srv.stats()
+        launches = None
+        srv.close()
+        wall = reduce(wall, dist.ReduceOp.MAX if dist else None)
+        total = reduce(total, dist.ReduceOp.SUM if dist else None)
+        # plain: a spaced sample of the same scenes, one at a time, same engine path
+        k = max(1, len(built) // max(1, args.plain_scenes))
+        sample = built[::k][:args.plain_scenes]
+        plain = ds.Server(device=device, workers=1, hbm_budget_bytes=budget)
+        p_upd = sum(scene_updates(s, steps) for _, s in sample)
+        t1 = time.perf_counter()
+        for _, s in sample:
+            plain.wait(plain.submit(s, steps), -1.0)
+        p_wall = time.perf_counter() - t1
+        pst = plain.stats()
+        plain.close()
+        if rank != 0:
+            return
+        value = total / wall
+        print(json.dumps({
+            "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": world,
+            "steps": steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": f"batched_mix_{args.scenes}",
+                       "description": f"{args.scenes} independent scenes, 60% SPH dam breaks and 40% coupled dam "
+                                      "breaks, fluid counts log-uniform in [2k, 60k], column heights uniform in "
+                                      f"[0.2, 0.5] m, {steps} steps each, through the scene server",
+                       "workers": args.workers, "hbm_budget_bytes": budget,
+                       "timing": "host wall clock from the first submission to the last completion (engine "
+                                 "creation and initialisation included)"},
+            "impl": "ours", "batched": {"value": value, "wall_s": wall, "p50_step_ms": st["p50_step_ms"],
+                                        "p99_step_ms": st["p99_step_ms"], "peak_bytes": st["peak_bytes"],
+                                        "scenes": st["completed"], "worker_create_s": st["create_s"],
+                                        "worker_step_s": st["step_s"], "worker_download_s": st["download_s"]},
+            "plain": {"value": p_upd / p_wall, "wall_s": p_wall, "scenes": len(sample),
+                      "p50_step_ms": pst["p50_step_ms"], "p99_step_ms": pst["p99_step_ms"],
+                      "sample": f"every {k}-th scene of the mix, one at a time"},
+            "batched_over_plain": value / (p_upd / p_wall), "clocks": clocks.summary(),
+            "e2e": {"value": value, "unit": "particle-updates/s", "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": None, "path": "scene arrays copied in at submission, final state "
+                                                        "copied out at completion"},
+        }))
+        return
+
+    # config 4: serving
+    arrivals = sc.serving_stream(duration=args.duration)[rank::world]
+    srv = ds.Server(device=device, workers=args.workers, hbm_budget_bytes=budget)
+    if dist:
+        dist.barrier()
+    lag = []
+    submitted = 0
+    with ClockSampler(device) as clocks:
+        t0 = time.perf_counter()
+        for (ta, kind, n, steps, seed) in arrivals:
+            now = time.perf_counter() - t0
+            if ta > now:
+                time.sleep(ta - now)
+            _, s = ds.build_scene(sc.make_request(kind, n, steps, seed))
+            srv.submit(s, steps)
+            submitted += 1
+            lag.append(time.perf_counter() - t0 - ta)
+        window = time.perf_counter() - t0
+        st = srv.stats()
+    srv.close()  # requests still queued or running are dropped
+    upd = reduce(st["particle_updates"], dist.ReduceOp.SUM if dist else None)
+    window = reduce(window, dist.ReduceOp.MAX if dist else None)
+    if rank != 0:
+        return
+    lag.sort()
+    print(json.dumps({
+        "metric": "particle-updates/s", "value": upd / window, "unit": "particle-updates/s", "n_gpus": world,
+        "steps": None, "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": "serving_stream",
+                   "description": f"Poisson arrivals at 20/s for {args.duration:g} s (the workload names 300 s); "
+                                  "SPH, DEM and coupled scenes in equal shares, sizes log-uniform in [5k, 500k], "
+                                  "steps uniform in [200, 5000]; 150 GiB admission budget",
+                   "workers": args.workers},
+        "impl": "ours",
+        "serving": {"submitted": submitted, "admitted": st["admitted"], "completed": st["completed"],
+                    "p50_step_ms": st["p50_step_ms"], "p99_step_ms": st["p99_step_ms"],
+                    "peak_bytes": st["peak_bytes"], "window_s": window,
+                    "submit_lag_p99_s": lag[int(0.99 * (len(lag) - 1))] if lag else None},
+        "clocks": clocks.summary(),
+        "e2e": {"value": upd / window, "unit": "particle-updates/s", "h2d_bytes_per_step": None,
+                "d2h_bytes_per_step": None},
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--config", type=int, choices=(0, 1, 2), default=1)
+    ap.add_argument("--config", type=int, choices=(0, 1, 2, 3, 4), default=1)
+    ap.add_argument("--scenes", type=int, default=256, help="batched workload: number of scenes")
+    ap.add_argument("--plain-scenes", type=int, default=32,
+                    help="batched workload: scenes (evenly spaced in the list) also run one at a time")
+    ap.add_argument("--duration", type=float, default=60.0, help="serving workload: seconds of arrivals")
+    ap.add_argument("--workers", type=int, default=32, help="batched/serving: server worker threads")
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--profile-steps", type=int, default=40)
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline stepping")
@@ -246,6 +390,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.config in (3, 4):
+        return run_many(args, world, rank, local)
     workload, desc = WORKLOADS[args.config]
 
     ds = _package()
@@ -404,8 +550,8 @@ def main():
         cfg.update({"solid_pairs": c.solid_pairs, "fluid_pairs_half": c.fluid_pairs,
                     "fluid_solid_pairs": c.fluid_solid_pairs, "bonds": c.bonds,
                     "timing": "CUDA events on the engine stream; K steps replayed as CUDA graphs",
-                    "precision": "FP32 arithmetic with Kahan sums; double-float positions, velocities, overlaps "
-                                 "and bond accumulators; FP64 clump rigid bodies"})
+                    "precision": "FP32 arithmetic with Kahan sums; double-float positions, velocities, overlaps, "
+                                 "bond accumulators and clump states; FP64 clump orientation"})
         out = {
             "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,

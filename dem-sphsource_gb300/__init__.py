@@ -73,6 +73,24 @@ class Counts(C.Structure):
                 ("cell_size", _D * 3)]
 
 
+class ServerConfig(C.Structure):
+    """ctypes mirror of ``demsph_server_config``."""
+
+    _fields_ = [("device", _I), ("workers", _I), ("chunk_steps", _I), ("hbm_budget_bytes", C.c_longlong)]
+
+
+class ServerSummary(C.Structure):
+    _fields_ = [(k, C.c_longlong) for k in ("submitted", "admitted", "completed", "failed", "pending", "steps",
+                                             "particle_updates", "chunks", "bytes_in_use", "peak_bytes")] + \
+               [(k, _D) for k in ("busy_s", "updates_per_s", "p50_step_ms", "p99_step_ms", "create_s", "step_s",
+                                  "download_s")]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", _I), ("steps_done", _I), ("reserved_bytes", C.c_longlong), ("queued_s", _D),
+                ("run_s", _D)]
+
+
 class DemSphError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"{message} (status {status})")
@@ -106,6 +124,10 @@ def load_library():
     lib.demsph_stream.argtypes = [_P]
     lib.demsph_kernel_launches.restype = C.c_longlong
     lib.demsph_kernel_launches.argtypes = [_P]
+    lib.demsph_device_bytes.restype = C.c_longlong
+    lib.demsph_device_bytes.argtypes = [_P]
+    lib.demsph_estimate_bytes.restype = C.c_longlong
+    lib.demsph_estimate_bytes.argtypes = [_P, _P]
     _lib = lib
     return lib
 
@@ -425,3 +447,87 @@ class Engine:
         out = np.zeros(self.nf)
         self._chk(self.lib.demsph_export_fluid_sumw0(self.h, _ptr(out)), "sumw0")
         return out
+
+
+def estimate_bytes(scene, **opts):
+    """Device memory demsph_create will allocate for the scene (an estimate)."""
+    lib = load_library()
+    o = Options(0, opts.get("fluid_neighbors_max", 0), opts.get("fluid_solids_max", 0),
+                opts.get("solid_contacts_per_particle", 0), opts.get("fixes", 0), opts.get("debug", 0),
+                float(opts.get("solid_verlet_skin", 0.0)))
+    return int(lib.demsph_estimate_bytes(C.byref(scene), C.byref(o)))
+
+
+class Server:
+    """Many scenes on one GPU (demsph_server_*): submit, wait, fetch."""
+
+    STATES = ("pending", "running", "done", "failed")
+
+    def __init__(self, device=0, workers=0, chunk_steps=0, hbm_budget_bytes=0):
+        self.lib = load_library()
+        cfg = ServerConfig(device, workers, chunk_steps, int(hbm_budget_bytes))
+        h = _P()
+        rc = self.lib.demsph_server_create(C.byref(cfg), C.byref(h))
+        if rc != DEMSPH_OK:
+            raise DemSphError(rc, "demsph_server_create")
+        self.h = h
+        self._sizes = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.demsph_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, scene, n_steps, **opts):
+        o = Options(0, opts.get("fluid_neighbors_max", 0), opts.get("fluid_solids_max", 0),
+                    opts.get("solid_contacts_per_particle", 0), opts.get("fixes", 0), opts.get("debug", 0),
+                    float(opts.get("solid_verlet_skin", 0.0)))
+        rid = C.c_longlong()
+        rc = self.lib.demsph_server_submit(self.h, C.byref(scene), C.byref(o), _I(n_steps), C.byref(rid))
+        if rc != DEMSPH_OK:
+            raise DemSphError(rc, "demsph_server_submit")
+        self._sizes[rid.value] = (scene.n_fluid, scene.n_solid)
+        return rid.value
+
+    def wait(self, request_id=-1, timeout=-1.0):
+        rc = self.lib.demsph_server_wait(self.h, C.c_longlong(request_id), _D(timeout))
+        if rc != DEMSPH_OK:
+            raise DemSphError(rc, f"request {request_id}")
+
+    def fetch(self, request_id):
+        nf, ns = self._sizes[request_id]
+        out = {"fluid_pos": np.zeros((nf, 3)), "fluid_vel": np.zeros((nf, 3)), "fluid_drho": np.zeros(nf),
+               "solid_pos": np.zeros((ns, 3)), "solid_vel": np.zeros((ns, 3)), "solid_angvel": np.zeros((ns, 3))}
+        rc = self.lib.demsph_server_fetch(self.h, C.c_longlong(request_id),
+                                          *[_ptr(out[k]) for k in ("fluid_pos", "fluid_vel", "fluid_drho",
+                                                                    "solid_pos", "solid_vel", "solid_angvel")])
+        if rc != DEMSPH_OK:
+            raise DemSphError(rc, f"fetch {request_id}")
+        return out
+
+    def release(self, request_id):
+        rc = self.lib.demsph_server_release(self.h, C.c_longlong(request_id))
+        if rc != DEMSPH_OK:
+            raise DemSphError(rc, f"release {request_id}")
+        self._sizes.pop(request_id, None)
+
+    def info(self, request_id):
+        i = RequestInfo()
+        rc = self.lib.demsph_server_request_info(self.h, C.c_longlong(request_id), C.byref(i))
+        if rc != DEMSPH_OK:
+            raise DemSphError(rc, f"info {request_id}")
+        return {"state": self.STATES[i.state], "steps_done": i.steps_done, "reserved_bytes": i.reserved_bytes,
+                "queued_s": i.queued_s, "run_s": i.run_s}
+
+    def stats(self):
+        st = ServerSummary()
+        rc = self.lib.demsph_server_stats(self.h, C.byref(st))
+        if rc != DEMSPH_OK:
+            raise DemSphError(rc, "stats")
+        return {k: getattr(st, k) for k, _ in ServerSummary._fields_}

@@ -25,6 +25,8 @@
 #include <string>
 #include <vector>
 
+#include <mutex>
+
 #include "engine_impl.cuh"
 
 namespace demsph {
@@ -32,17 +34,16 @@ namespace demsph {
 void freeOne(demsph_engine* e, void*& p)
 {
     if (!p) return;
-    auto it = std::find(e->owned.begin(), e->owned.end(), p);
+    auto it = std::find_if(e->owned.begin(), e->owned.end(), [&](const Allocation& a) { return a.p == p; });
     if (it != e->owned.end()) e->owned.erase(it);
-    cudaFree(p);
+    cudaFreeAsync(p, e->stream);
     p = nullptr;
 }
 
 void dropGraph(demsph_engine* e)
 {
-    if (e->graph) cudaGraphExecDestroy(e->graph);
-    e->graph = nullptr;
-    e->graphPeriod = 0;
+    for (const auto& g : e->graphs) cudaGraphExecDestroy(g.exec);
+    e->graphs.clear();
 }
 
 double* scratchDoubles(demsph_engine* e, size_t n)
@@ -50,7 +51,7 @@ double* scratchDoubles(demsph_engine* e, size_t n)
     if (n > e->dscratchN) {
         void* p = e->dscratch;
         freeOne(e, p);
-        e->dscratch = dalloc<double>(n, e->owned, false);
+        e->dscratch = dalloc<double>(n, e->owned, e->stream, false);
         e->dscratchN = n;
     }
     return e->dscratch;
@@ -100,6 +101,23 @@ inline double3 v3(const double* p, int i)
     return p ? make_double3(p[3 * i], p[3 * i + 1], p[3 * i + 2]) : make_double3(0, 0, 0);
 }
 
+// Freed engine memory stays in the device's stream-ordered pool for the next
+// engine instead of going back to the driver at every synchronisation (a
+// setting of this process's pool only).
+void keepPoolMemory(int dev)
+{
+    static std::mutex m;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lock(m);
+    if (std::find(done.begin(), done.end(), dev) != done.end()) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    done.push_back(dev);
+}
+
 int checkDevice(demsph_engine* e, int dev)
 {
     int n = 0;
@@ -116,9 +134,9 @@ int checkDevice(demsph_engine* e, int dev)
 void allocFluidLists(demsph_engine* e)
 {
     DeviceState& d = e->d;
-    d.ff = dalloc<unsigned>((size_t)d.kff * d.nf, e->owned, false);
-    d.fs = dalloc<int>((size_t)d.kfs * d.nf, e->owned, false);
-    if (e->debug & 1) d.fsPairForce = dalloc<float4>((size_t)d.kfs * d.nf, e->owned);
+    d.ff = dalloc<unsigned>((size_t)d.kff * d.nf, e->owned, e->stream, false);
+    d.fs = dalloc<int>((size_t)d.kfs * d.nf, e->owned, e->stream, false);
+    if (e->debug & 1) d.fsPairForce = dalloc<float4>((size_t)d.kfs * d.nf, e->owned, e->stream);
 }
 
 // Per-slot arrays of the contact rows (scap slots per row).
@@ -126,13 +144,13 @@ void allocContactLists(demsph_engine* e)
 {
     DeviceState& d = e->d;
     const size_t c = (size_t)d.scap * std::max(1, d.nrow);
-    d.rev = dalloc<int>(c, e->owned);
-    d.pF = dalloc<float4>(c, e->owned);
-    d.pT = dalloc<float4>(c, e->owned);
-    for (int p = 0; p < 2; ++p) d.fwd[p] = dalloc<int>(c, e->owned);
+    d.rev = dalloc<int>(c, e->owned, e->stream);
+    d.pF = dalloc<float4>(c, e->owned, e->stream);
+    d.pT = dalloc<float4>(c, e->owned, e->stream);
+    for (int p = 0; p < 2; ++p) d.fwd[p] = dalloc<int>(c, e->owned, e->stream);
     for (int k = 0; k < 3; ++k) {
-        d.springIn[k] = dalloc<float4>(c, e->owned);
-        d.springOut[k] = dalloc<float4>(c, e->owned);
+        d.springIn[k] = dalloc<float4>(c, e->owned, e->stream);
+        d.springOut[k] = dalloc<float4>(c, e->owned, e->stream);
     }
 }
 
@@ -275,8 +293,9 @@ void grow(demsph_engine* e, int status)
     }
     if (status & (ST_SS_OVERFLOW | ST_VERLET_OVERFLOW)) {
         int need[2] = {0, 0};
-        CK(cudaMemcpy(need, d.need, sizeof(int) * 2, cudaMemcpyDeviceToHost));
-        CK(cudaMemset(d.need, 0, sizeof(int) * 2));
+        CK(cudaMemcpyAsync(need, d.need, sizeof(int) * 2, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        CK(cudaMemsetAsync(d.need, 0, sizeof(int) * 2, e->stream));
         const size_t nr = (size_t)std::max(1, d.nrow);
         if (status & ST_SS_OVERFLOW) {
             // keep the spring history (the last successful list and the springs
@@ -292,9 +311,9 @@ void grow(demsph_engine* e, int status)
             for (void* p : ptrs) freeOne(e, p);
             d.scap = std::max(d.scap * 2, need[0] + need[0] / 2 + 1);
             allocContactLists(e);
-            CK(cudaMemcpy(d.fwd[keep], keepFwd, sizeof(int) * old, cudaMemcpyDeviceToDevice));
+            CK(cudaMemcpyAsync(d.fwd[keep], keepFwd, sizeof(int) * old, cudaMemcpyDeviceToDevice, e->stream));
             for (int k = 0; k < 3; ++k)
-                CK(cudaMemcpy(d.springOut[k], keepSpring[k], sizeof(float4) * old, cudaMemcpyDeviceToDevice));
+                CK(cudaMemcpyAsync(d.springOut[k], keepSpring[k], sizeof(float4) * old, cudaMemcpyDeviceToDevice, e->stream));
             void* olds[] = {keepFwd, keepSpring[0], keepSpring[1], keepSpring[2]};
             for (void* p : olds) freeOne(e, p);
         }
@@ -302,23 +321,24 @@ void grow(demsph_engine* e, int status)
             void* p = d.vcand;
             freeOne(e, p);
             d.vcap = std::max(d.vcap * 2, need[1] + need[1] / 2 + 1);
-            d.vcand = dalloc<int>((size_t)d.vcap * nr, e->owned, false);
-            CK(cudaMemset(d.rebuild, 0xff, sizeof(int)));  // rebuild on the retry
+            d.vcand = dalloc<int>((size_t)d.vcap * nr, e->owned, e->stream, false);
+            CK(cudaMemsetAsync(d.rebuild, 0xff, sizeof(int), e->stream));  // rebuild on the retry
         }
     }
     if (status & ST_COUPLE_OVERFLOW) {
         int need = 0;
-        CK(cudaMemcpy(&need, d.coupStart + d.ns, sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpyAsync(&need, d.coupStart + d.ns, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
         void* p = d.coupList;
         freeOne(e, p);
         d.coupCap = (int)std::min<long long>(2000000000LL, (long long)(need * 1.5) + 1024);
-        d.coupList = dalloc<int>(d.coupCap, e->owned);
+        d.coupList = dalloc<int>(d.coupCap, e->owned, e->stream);
     }
     if (status & ST_MODE_CHANGE) {
         // the abandoned step may have counted some solids into cells
-        CK(cudaMemset(d.scellCount, 0, sizeof(int) * d.grid.num));
+        CK(cudaMemsetAsync(d.scellCount, 0, sizeof(int) * d.grid.num, e->stream));
     }
-    CK(cudaMemset(d.status, 0, sizeof(int)));
+    CK(cudaMemsetAsync(d.status, 0, sizeof(int), e->stream));
     dropGraph(e);
 }
 
@@ -382,7 +402,6 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             return DEMSPH_ERR_ARGUMENT;
     demsph_engine* e = new demsph_engine();
     e->debug = o.debug;
-    e->launchBase = t_kernelLaunches;
     int rc = checkDevice(e, o.device);
     if (rc != DEMSPH_OK) {
         *out = e;  // keep the message readable
@@ -391,6 +410,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
     try {
         e->device = o.device;
         CK(cudaSetDevice(o.device));
+        keepPoolMemory(o.device);
         CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
         DeviceState& d = e->d;
         d.fixes = o.fixes;
@@ -438,22 +458,22 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             const double lr = std::log(sc->hertzian[8 * k + 2]);
             e->dampF[k] = (float)(-lr / std::sqrt(lr * lr + 3.1415926535897931 * 3.1415926535897931));
         }
-        float* tab = dalloc<float>(26 * nslot, e->owned);
-        CK(cudaMemcpy(tab, e->hzF.data(), sizeof(float) * 8 * nslot, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(tab + 8 * nslot, e->lnF.data(), sizeof(float) * 11 * nslot, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(tab + 19 * nslot, e->bdF.data(), sizeof(float) * 6 * nslot, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(tab + 25 * nslot, e->dampF.data(), sizeof(float) * nslot, cudaMemcpyHostToDevice));
+        float* tab = dalloc<float>(26 * nslot, e->owned, e->stream);
+        CK(cudaMemcpyAsync(tab, e->hzF.data(), sizeof(float) * 8 * nslot, cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemcpyAsync(tab + 8 * nslot, e->lnF.data(), sizeof(float) * 11 * nslot, cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemcpyAsync(tab + 19 * nslot, e->bdF.data(), sizeof(float) * 6 * nslot, cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemcpyAsync(tab + 25 * nslot, e->dampF.data(), sizeof(float) * nslot, cudaMemcpyHostToDevice, e->stream));
         d.tab.nMat = sc->n_material;
         d.tab.hz = tab;
         d.tab.ln = tab + 8 * nslot;
         d.tab.bd = tab + 19 * nslot;
         d.tab.damp = tab + 25 * nslot;
 
-        d.status = dalloc<int>(1, e->owned);
-        d.stepsDone = dalloc<int>(1, e->owned);
+        d.status = dalloc<int>(1, e->owned, e->stream);
+        d.stepsDone = dalloc<int>(1, e->owned, e->stream);
         size_t wk = std::max({scanWorkspaceInts(d.grid.num), scanWorkspaceInts(std::max(1, d.ns)),
                               scanWorkspaceInts(std::max(1, d.nf))});
-        d.scanWork = dalloc<int>(wk, e->owned);
+        d.scanWork = dalloc<int>(wk, e->owned, e->stream);
 
         // ---- fluid ----
         const int nf = d.nf;
@@ -479,43 +499,43 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 drho[i] = sc->fluid_drho ? (float)sc->fluid_drho[i] : 0.f;
                 id[i] = i;
             }
-            d.fcell = dalloc<int4>(nf, e->owned);
+            d.fcell = dalloc<int4>(nf, e->owned, e->stream);
             for (int b = 0; b < 2; ++b) {
-                d.fph[b] = dalloc<float4>(nf, e->owned);
-                d.fpl[b] = dalloc<float4>(nf, e->owned);
-                d.fvh[b] = dalloc<float4>(nf, e->owned);
-                d.fvl[b] = dalloc<float4>(nf, e->owned);
-                d.fdrho[b] = dalloc<float>(nf, e->owned);
+                d.fph[b] = dalloc<float4>(nf, e->owned, e->stream);
+                d.fpl[b] = dalloc<float4>(nf, e->owned, e->stream);
+                d.fvh[b] = dalloc<float4>(nf, e->owned, e->stream);
+                d.fvl[b] = dalloc<float4>(nf, e->owned, e->stream);
+                d.fdrho[b] = dalloc<float>(nf, e->owned, e->stream);
             }
-            d.facc = dalloc<float4>(nf, e->owned);
-            d.fpar = dalloc<float4>(nf, e->owned);
-            d.fsumW0 = dalloc<float2>(nf, e->owned);
-            d.fid = dalloc<int>(nf, e->owned);
-            d.fslot = dalloc<int>(nf, e->owned);
-            d.tcell = dalloc<int4>(nf, e->owned);
-            d.tacc = dalloc<float4>(nf, e->owned);
-            d.tpar = dalloc<float4>(nf, e->owned);
-            d.tsumW0 = dalloc<float2>(nf, e->owned);
-            d.tid = dalloc<int>(nf, e->owned);
-            d.fkey = dalloc<int>(nf, e->owned);
-            d.fslotInCell = dalloc<int>(nf, e->owned);
-            d.fsortTmp = dalloc<int>(nf, e->owned);
-            d.fcellCount = dalloc<int>(d.grid.num, e->owned);
-            d.fcellStart = dalloc<int>((size_t)d.grid.num + 1, e->owned);
-            d.ffc = dalloc<int>(nf, e->owned);
-            d.fsc = dalloc<int>(nf, e->owned);
+            d.facc = dalloc<float4>(nf, e->owned, e->stream);
+            d.fpar = dalloc<float4>(nf, e->owned, e->stream);
+            d.fsumW0 = dalloc<float2>(nf, e->owned, e->stream);
+            d.fid = dalloc<int>(nf, e->owned, e->stream);
+            d.fslot = dalloc<int>(nf, e->owned, e->stream);
+            d.tcell = dalloc<int4>(nf, e->owned, e->stream);
+            d.tacc = dalloc<float4>(nf, e->owned, e->stream);
+            d.tpar = dalloc<float4>(nf, e->owned, e->stream);
+            d.tsumW0 = dalloc<float2>(nf, e->owned, e->stream);
+            d.tid = dalloc<int>(nf, e->owned, e->stream);
+            d.fkey = dalloc<int>(nf, e->owned, e->stream);
+            d.fslotInCell = dalloc<int>(nf, e->owned, e->stream);
+            d.fsortTmp = dalloc<int>(nf, e->owned, e->stream);
+            d.fcellCount = dalloc<int>(d.grid.num, e->owned, e->stream);
+            d.fcellStart = dalloc<int>((size_t)d.grid.num + 1, e->owned, e->stream);
+            d.ffc = dalloc<int>(nf, e->owned, e->stream);
+            d.fsc = dalloc<int>(nf, e->owned, e->stream);
             allocFluidLists(e);
             if (nf > 0) {
-                CK(cudaMemcpy(d.fcell, cell.data(), sizeof(int4) * nf, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.fph[0], ph.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.fpl[0], pl.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.fvh[0], vh.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.fvl[0], vl.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.fdrho[0], drho.data(), sizeof(float) * nf, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.facc, acc.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.fpar, par.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.fid, id.data(), sizeof(int) * nf, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.fslot, id.data(), sizeof(int) * nf, cudaMemcpyHostToDevice));
+                CK(cudaMemcpyAsync(d.fcell, cell.data(), sizeof(int4) * nf, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.fph[0], ph.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.fpl[0], pl.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.fvh[0], vh.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.fvl[0], vl.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.fdrho[0], drho.data(), sizeof(float) * nf, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.facc, acc.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.fpar, par.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.fid, id.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.fslot, id.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, e->stream));
             }
         }
 
@@ -551,25 +571,25 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 if (im > 0.) e->nMassive++;
                 flags[i] = make_int4(sc->solid_material[i], sc->solid_cluster[i], sc->solid_clump[i], bits);
             }
-            d.scell = dalloc<int4>(ns, e->owned);
-            d.sph = dalloc<float4>(ns, e->owned);
-            d.spl = dalloc<float4>(ns, e->owned);
-            d.svh = dalloc<float4>(ns, e->owned);
-            d.svl = dalloc<float4>(ns, e->owned);
-            d.swh = dalloc<float4>(ns, e->owned);
-            d.swl = dalloc<float4>(ns, e->owned);
-            d.sacc = dalloc<float4>(ns, e->owned);
-            d.storque = dalloc<float4>(ns, e->owned);
-            d.snormal = dalloc<float4>(ns, e->owned);
-            d.sfcoup = dalloc<float4>(ns, e->owned);
-            d.srad = dalloc<float4>(ns, e->owned);
-            d.sflags = dalloc<int4>(ns, e->owned);
-            d.skey = dalloc<int>(ns, e->owned);
-            d.sslotInCell = dalloc<int>(ns, e->owned);
-            d.ssorted = dalloc<int>(ns, e->owned);
-            d.ssortTmp = dalloc<int>(ns, e->owned);
-            d.scellCount = dalloc<int>(d.grid.num, e->owned);
-            d.scellStart = dalloc<int>((size_t)d.grid.num + 1, e->owned);
+            d.scell = dalloc<int4>(ns, e->owned, e->stream);
+            d.sph = dalloc<float4>(ns, e->owned, e->stream);
+            d.spl = dalloc<float4>(ns, e->owned, e->stream);
+            d.svh = dalloc<float4>(ns, e->owned, e->stream);
+            d.svl = dalloc<float4>(ns, e->owned, e->stream);
+            d.swh = dalloc<float4>(ns, e->owned, e->stream);
+            d.swl = dalloc<float4>(ns, e->owned, e->stream);
+            d.sacc = dalloc<float4>(ns, e->owned, e->stream);
+            d.storque = dalloc<float4>(ns, e->owned, e->stream);
+            d.snormal = dalloc<float4>(ns, e->owned, e->stream);
+            d.sfcoup = dalloc<float4>(ns, e->owned, e->stream);
+            d.srad = dalloc<float4>(ns, e->owned, e->stream);
+            d.sflags = dalloc<int4>(ns, e->owned, e->stream);
+            d.skey = dalloc<int>(ns, e->owned, e->stream);
+            d.sslotInCell = dalloc<int>(ns, e->owned, e->stream);
+            d.ssorted = dalloc<int>(ns, e->owned, e->stream);
+            d.ssortTmp = dalloc<int>(ns, e->owned, e->stream);
+            d.scellCount = dalloc<int>(d.grid.num, e->owned, e->stream);
+            d.scellStart = dalloc<int>((size_t)d.grid.num + 1, e->owned, e->stream);
             // contact rows: every solid but the dummy wall particles, in index order
             std::vector<int> srow(ns, -1), rowSolid;
             double rmin = 0, effMax = 0;
@@ -581,49 +601,49 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 effMax = std::max(effMax, sc->solid_effective_radius[i]);
             }
             d.nrow = (int)rowSolid.size();
-            d.srow = dalloc<int>(ns, e->owned);
-            d.rowSolid = dalloc<int>(d.nrow, e->owned);
-            d.scentre = dalloc<int4>(d.nrow, e->owned);
-            if (ns > 0) CK(cudaMemcpy(d.srow, srow.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
+            d.srow = dalloc<int>(ns, e->owned, e->stream);
+            d.rowSolid = dalloc<int>(d.nrow, e->owned, e->stream);
+            d.scentre = dalloc<int4>(d.nrow, e->owned, e->stream);
+            if (ns > 0) CK(cudaMemcpyAsync(d.srow, srow.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, e->stream));
             if (d.nrow > 0)
-                CK(cudaMemcpy(d.rowSolid, rowSolid.data(), sizeof(int) * d.nrow, cudaMemcpyHostToDevice));
+                CK(cudaMemcpyAsync(d.rowSolid, rowSolid.data(), sizeof(int) * d.nrow, cudaMemcpyHostToDevice, e->stream));
             const size_t nr = (size_t)std::max(1, d.nrow);
             d.scap = perParticle;
-            d.fcnt[0] = dalloc<int>(nr, e->owned);
-            d.fcnt[1] = dalloc<int>(nr, e->owned);
-            d.rcnt = dalloc<int>(nr, e->owned);
+            d.fcnt[0] = dalloc<int>(nr, e->owned, e->stream);
+            d.fcnt[1] = dalloc<int>(nr, e->owned, e->stream);
+            d.rcnt = dalloc<int>(nr, e->owned, e->stream);
             allocContactLists(e);
             // Verlet candidates
             d.skin = (float)(o.solid_verlet_skin > 0 ? o.solid_verlet_skin : 0.2 * rmin);
             d.vmaxEff = (float)effMax;
             d.vcap = 2 * perParticle;
-            d.vcand = dalloc<int>((size_t)d.vcap * nr, e->owned, false);
-            d.vcnt = dalloc<int>(nr, e->owned);
-            d.vref = dalloc<float4>(nr, e->owned);
-            d.rebuild = dalloc<int>(1, e->owned);
-            d.slowMode = dalloc<int>(1, e->owned);
-            d.need = dalloc<int>(2, e->owned);
+            d.vcand = dalloc<int>((size_t)d.vcap * nr, e->owned, e->stream, false);
+            d.vcnt = dalloc<int>(nr, e->owned, e->stream);
+            d.vref = dalloc<float4>(nr, e->owned, e->stream);
+            d.rebuild = dalloc<int>(1, e->owned, e->stream);
+            d.slowMode = dalloc<int>(1, e->owned, e->stream);
+            d.need = dalloc<int>(2, e->owned, e->stream);
             const int one = 1;
             const bool walkOnly = o.solid_verlet_skin < 0 || d.grid.gx < 3 || d.grid.gy < 3 || d.grid.gz < 3;
-            CK(cudaMemcpy(d.rebuild, &one, sizeof(int), cudaMemcpyHostToDevice));
-            if (walkOnly) CK(cudaMemcpy(d.slowMode, &one, sizeof(int), cudaMemcpyHostToDevice));
-            d.coupCount = dalloc<int>(ns, e->owned);
-            d.coupStart = dalloc<int>((size_t)ns + 1, e->owned);
+            CK(cudaMemcpyAsync(d.rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+            if (walkOnly) CK(cudaMemcpyAsync(d.slowMode, &one, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+            d.coupCount = dalloc<int>(ns, e->owned, e->stream);
+            d.coupStart = dalloc<int>((size_t)ns + 1, e->owned, e->stream);
             d.coupCap = std::max(1024, std::min(64 * e->nMassive + 1024, std::max(1, d.kfs * nf)));
-            d.coupList = dalloc<int>(d.coupCap, e->owned);
+            d.coupList = dalloc<int>(d.coupCap, e->owned, e->stream);
             if (ns > 0) {
-                CK(cudaMemcpy(d.scell, cell.data(), sizeof(int4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.sph, ph.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.spl, pl.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.svh, vh.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.svl, vl.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.swh, wh.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.swl, wl.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.sacc, acc.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.storque, tq.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.snormal, nrm.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.srad, rad.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.sflags, flags.data(), sizeof(int4) * ns, cudaMemcpyHostToDevice));
+                CK(cudaMemcpyAsync(d.scell, cell.data(), sizeof(int4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.sph, ph.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.spl, pl.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.svh, vh.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.svl, vl.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.swh, wh.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.swl, wl.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.sacc, acc.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.storque, tq.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.snormal, nrm.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.srad, rad.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.sflags, flags.data(), sizeof(int4) * ns, cudaMemcpyHostToDevice, e->stream));
             }
         }
 
@@ -642,36 +662,36 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 P[k] = make_float2(pp.hi, pp.lo);
                 mat[k] = sc->wall_material[k];
             }
-            d.wnh = dalloc<float4>(nw, e->owned);
-            d.wnl = dalloc<float4>(nw, e->owned);
-            d.wP = dalloc<float2>(nw, e->owned);
-            d.wmat = dalloc<int>(nw, e->owned);
-            for (int k = 0; k < 3; ++k) d.wspring[k] = dalloc<float4>((size_t)ns * nw, e->owned);
+            d.wnh = dalloc<float4>(nw, e->owned, e->stream);
+            d.wnl = dalloc<float4>(nw, e->owned, e->stream);
+            d.wP = dalloc<float2>(nw, e->owned, e->stream);
+            d.wmat = dalloc<int>(nw, e->owned, e->stream);
+            for (int k = 0; k < 3; ++k) d.wspring[k] = dalloc<float4>((size_t)ns * nw, e->owned, e->stream);
             if (nw > 0) {
-                CK(cudaMemcpy(d.wnh, nh.data(), sizeof(float4) * nw, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.wnl, nl.data(), sizeof(float4) * nw, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.wP, P.data(), sizeof(float2) * nw, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.wmat, mat.data(), sizeof(int) * nw, cudaMemcpyHostToDevice));
+                CK(cudaMemcpyAsync(d.wnh, nh.data(), sizeof(float4) * nw, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.wnl, nl.data(), sizeof(float4) * nw, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.wP, P.data(), sizeof(float2) * nw, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.wmat, mat.data(), sizeof(int) * nw, cudaMemcpyHostToDevice, e->stream));
             }
         }
 
         // ---- clumps ----
         {
             const int nc = d.nc;
-            d.cpH = dalloc<float4>(nc, e->owned);
-            d.cpL = dalloc<float4>(nc, e->owned);
-            d.cvH = dalloc<float4>(nc, e->owned);
-            d.cvL = dalloc<float4>(nc, e->owned);
-            d.cwH = dalloc<float4>(nc, e->owned);
-            d.cwL = dalloc<float4>(nc, e->owned);
-            d.cacc = dalloc<float4>(nc, e->owned);
-            d.ctorque = dalloc<float4>(nc, e->owned);
-            d.cIw = dalloc<float>(6 * (size_t)nc, e->owned);
-            d.cinvm = dalloc<float>(nc, e->owned);
-            d.cq = dalloc<double4>(nc, e->owned);
-            d.cinvI = dalloc<double>(6 * (size_t)nc, e->owned);
-            d.cstart = dalloc<int>(nc, e->owned);
-            d.cend = dalloc<int>(nc, e->owned);
+            d.cpH = dalloc<float4>(nc, e->owned, e->stream);
+            d.cpL = dalloc<float4>(nc, e->owned, e->stream);
+            d.cvH = dalloc<float4>(nc, e->owned, e->stream);
+            d.cvL = dalloc<float4>(nc, e->owned, e->stream);
+            d.cwH = dalloc<float4>(nc, e->owned, e->stream);
+            d.cwL = dalloc<float4>(nc, e->owned, e->stream);
+            d.cacc = dalloc<float4>(nc, e->owned, e->stream);
+            d.ctorque = dalloc<float4>(nc, e->owned, e->stream);
+            d.cIw = dalloc<float>(6 * (size_t)nc, e->owned, e->stream);
+            d.cinvm = dalloc<float>(nc, e->owned, e->stream);
+            d.cq = dalloc<double4>(nc, e->owned, e->stream);
+            d.cinvI = dalloc<double>(6 * (size_t)nc, e->owned, e->stream);
+            d.cstart = dalloc<int>(nc, e->owned, e->stream);
+            d.cend = dalloc<int>(nc, e->owned, e->stream);
             int most = 1;
             for (int c = 0; c < nc; ++c) most = std::max(most, sc->clump_pebble_end[c] - sc->clump_pebble_start[c]);
             d.clumpLanes = 1;
@@ -712,23 +732,23 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                     const double w6[6] = {W[0][0], W[1][1], W[2][2], W[0][1], W[0][2], W[1][2]};
                     for (int k = 0; k < 6; ++k) Iw[6 * c + k] = (float)w6[k];
                 }
-                CK(cudaMemcpy(d.cpH, pH.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cpL, pL.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cvH, vH.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cvL, vL.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cwH, wH.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cwL, wL.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cacc, acc.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.ctorque, tq.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cIw, Iw.data(), sizeof(float) * 6 * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cinvm, im.data(), sizeof(float) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cq, sc->clump_orientation, sizeof(double4) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cinvI, sc->clump_inverse_inertia, sizeof(double) * 6 * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cstart, sc->clump_pebble_start, sizeof(int) * nc, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(d.cend, sc->clump_pebble_end, sizeof(int) * nc, cudaMemcpyHostToDevice));
+                CK(cudaMemcpyAsync(d.cpH, pH.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cpL, pL.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cvH, vH.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cvL, vL.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cwH, wH.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cwL, wL.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cacc, acc.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.ctorque, tq.data(), sizeof(float4) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cIw, Iw.data(), sizeof(float) * 6 * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cinvm, im.data(), sizeof(float) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cq, sc->clump_orientation, sizeof(double4) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cinvI, sc->clump_inverse_inertia, sizeof(double) * 6 * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cstart, sc->clump_pebble_start, sizeof(int) * nc, cudaMemcpyHostToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.cend, sc->clump_pebble_end, sizeof(int) * nc, cudaMemcpyHostToDevice, e->stream));
             }
         }
-        CK(cudaDeviceSynchronize());
+        CK(cudaStreamSynchronize(e->stream));
     } catch (const CudaError& c) {
         rc = cudaFail(e, c);
         *out = e;
@@ -762,36 +782,37 @@ int demsph_initialize(demsph_engine* e)
     const long long nslots = (long long)d.nrow * d.scap;
     if (nslots > 0) {
         if (nslots > 2000000000LL) return fail(e, DEMSPH_ERR_CAPACITY, "contact rows too large for bond creation");
-        std::vector<void*> tmp;
-        int* flag = dalloc<int>((size_t)nslots + 1, tmp);
-        int* pos = dalloc<int>((size_t)nslots + 1, tmp);
-        int* work = dalloc<int>(scanWorkspaceInts((int)nslots), tmp);
+        std::vector<Allocation> tmp;
+        int* flag = dalloc<int>((size_t)nslots + 1, tmp, e->stream);
+        int* pos = dalloc<int>((size_t)nslots + 1, tmp, e->stream);
+        int* work = dalloc<int>(scanWorkspaceInts((int)nslots), tmp, e->stream);
         const int nb = launchBondFlags(d, e->par, flag, pos, work, e->stream);
         if (nb > 0) {
             d.nb = nb;
-            d.bab = dalloc<int2>(nb, e->owned);
-            d.bon = dalloc<int>(nb, e->owned);
-            d.bFnTt = dalloc<float4>(nb, e->owned);
-            d.bFsH = dalloc<float4>(nb, e->owned);
-            d.bFsL = dalloc<float4>(nb, e->owned);
-            d.bTbH = dalloc<float4>(nb, e->owned);
-            d.bTbL = dalloc<float4>(nb, e->owned);
-            d.bN = dalloc<float4>(nb, e->owned);
-            d.bLever = dalloc<float4>(nb, e->owned);
-            d.bF = dalloc<float4>(nb, e->owned);
-            d.bTA = dalloc<float4>(nb, e->owned);
-            d.bTB = dalloc<float4>(nb, e->owned);
+            d.bab = dalloc<int2>(nb, e->owned, e->stream);
+            d.bon = dalloc<int>(nb, e->owned, e->stream);
+            d.bFnTt = dalloc<float4>(nb, e->owned, e->stream);
+            d.bFsH = dalloc<float4>(nb, e->owned, e->stream);
+            d.bFsL = dalloc<float4>(nb, e->owned, e->stream);
+            d.bTbH = dalloc<float4>(nb, e->owned, e->stream);
+            d.bTbL = dalloc<float4>(nb, e->owned, e->stream);
+            d.bN = dalloc<float4>(nb, e->owned, e->stream);
+            d.bLever = dalloc<float4>(nb, e->owned, e->stream);
+            d.bF = dalloc<float4>(nb, e->owned, e->stream);
+            d.bTA = dalloc<float4>(nb, e->owned, e->stream);
+            d.bTB = dalloc<float4>(nb, e->owned, e->stream);
             launchBondWrite(d, e->par, flag, pos, e->stream);
         }
         CK(cudaStreamSynchronize(e->stream));
-        for (void* p : tmp) cudaFree(p);
+        for (const auto& a : tmp) cudaFreeAsync(a.p, e->stream);
     }
     // bonds of each solid, in bond order (the per-solid force sums)
     {
         std::vector<int2> ab;
         if (d.nb > 0) {
             ab.resize(d.nb);
-            CK(cudaMemcpy(ab.data(), d.bab, sizeof(int2) * d.nb, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpyAsync(ab.data(), d.bab, sizeof(int2) * d.nb, cudaMemcpyDeviceToHost, e->stream));
+            CK(cudaStreamSynchronize(e->stream));
         }
         std::vector<int> start((size_t)d.ns + 1, 0), list(2 * (size_t)d.nb);
         for (const int2& p : ab) {
@@ -804,10 +825,10 @@ int demsph_initialize(demsph_engine* e)
             list[fill[ab[b].x]++] = b;
             list[fill[ab[b].y]++] = b;
         }
-        d.bondStart = dalloc<int>((size_t)d.ns + 1, e->owned);
-        d.bondList = dalloc<int>(list.size(), e->owned);
-        if (d.ns > 0) CK(cudaMemcpy(d.bondStart, start.data(), sizeof(int) * (d.ns + 1), cudaMemcpyHostToDevice));
-        if (!list.empty()) CK(cudaMemcpy(d.bondList, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
+        d.bondStart = dalloc<int>((size_t)d.ns + 1, e->owned, e->stream);
+        d.bondList = dalloc<int>(list.size(), e->owned, e->stream);
+        if (d.ns > 0) CK(cudaMemcpyAsync(d.bondStart, start.data(), sizeof(int) * (d.ns + 1), cudaMemcpyHostToDevice, e->stream));
+        if (!list.empty()) CK(cudaMemcpyAsync(d.bondList, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, e->stream));
     }
     // normals of walls and clump pebbles (setSolidNormal), kernel length = largest fluid h
     launchSolidNormals(d, e->hmax, e->stream);
@@ -887,50 +908,76 @@ int demsph_synchronize(demsph_engine* e)
 // the Shepard reference), whole periods replay one captured graph, the rest
 // runs uncaptured.  One synchronisation at the end; on a list overflow the
 // engine grows the list and resumes from the first incomplete step.
+// Kind of step i: bit 0 a fluid step (every gap steps), bit 1 a Shepard
+// re-initialisation (every 5 gap steps).  Steps of one kind launch the same
+// kernels with the same arguments, apart from the contact-list parity.
+static int stepKind(const DeviceState& d, int i, int gap)
+{
+    if (d.nf <= 0) return 0;
+    return (i % gap == 0 ? 1 : 0) | (i % (5 * gap) == 0 ? 2 : 0);
+}
+
+// The graph of `length` steps of `kind` starting from the current parity,
+// captured on first use.
+static const demsph_engine::CachedGraph& graphFor(demsph_engine* e, int kind, int length, double dt, int step, int gap)
+{
+    for (const auto& g : e->graphs)
+        if (g.kind == kind && g.parity == e->par && g.length == length) return g;
+    const int parity = e->par;
+    cudaGraph_t g;
+    const long long before = t_kernelLaunches;
+    CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < length; ++k) fullStep(e, dt, step + k, gap);
+    CK(cudaStreamEndCapture(e->stream, &g));
+    e->par = parity;  // nothing ran: the parity is where it was
+    demsph_engine::CachedGraph c{kind, parity, length, nullptr, t_kernelLaunches - before};
+    e->capturedLaunches += c.kernels;
+    const cudaError_t ie = cudaGraphInstantiate(&c.exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(ie);
+    e->graphs.push_back(c);
+    return e->graphs.back();
+}
+
 int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph)
 {
     if (gap < 1 || n_steps < 0) return DEMSPH_ERR_ARGUMENT;
     ENGINE_GUARD(e)
     REQUIRE_INIT(e);
     DeviceState& d = e->d;
-    const int period = 10 * gap;  // multiple of 2 (contact-list parity) and of 5 gap (re-initialisation)
     const int end = first_step + n_steps;
     int step = first_step;
     for (int attempt = 0; step < end; ++attempt) {
         if (attempt > 32) return fail(e, DEMSPH_ERR_CAPACITY, "list overflow persists after growing");
         CK(cudaMemsetAsync(d.stepsDone, 0, sizeof(int), e->stream));
         const int startPar = e->par;
-        int s = step;
         const bool graphs = use_graph && !e->profiling;
-        auto graphable = [&](int k) { return graphs && k > 1 && k % period == 0 && end - k >= period; };
-        while (s < end && !graphable(s)) fullStep(e, dt, s++, gap);
-        if (s < end && graphable(s)) {
-            if (!e->graph || e->graphPeriod != period || e->graphGap != gap || e->graphDt != dt ||
-                e->graphParity != e->par) {
-                dropGraph(e);
-                const int parity = e->par;
-                cudaGraph_t g;
-                const long long before = t_kernelLaunches;
-                CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-                for (int k = 0; k < period; ++k) fullStep(e, dt, s + k, gap);
-                CK(cudaStreamEndCapture(e->stream, &g));
-                e->graphKernels = t_kernelLaunches - before;
-                e->capturedLaunches += e->graphKernels;
-                const cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
-                cudaGraphDestroy(g);
-                CK(ie);
-                e->graphPeriod = period;
-                e->graphGap = gap;
-                e->graphDt = dt;
-                e->graphParity = parity;
-                e->par = parity;  // a period flips the parity an even number of times
+        if (graphs && (e->graphDt != dt || e->graphGap != gap)) {
+            dropGraph(e);
+            e->graphDt = dt;
+            e->graphGap = gap;
+        }
+        int s = step;
+        while (s < end) {
+            const int kind = stepKind(d, s, gap);
+            if (!graphs || s == 1) {  // step 1 stores the Shepard reference sums: run it as it is
+                fullStep(e, dt, s++, gap);
+                continue;
             }
-            while (end - s >= period) {
-                CK(cudaGraphLaunch(e->graph, e->stream));
-                e->replayedKernels += e->graphKernels;
-                s += period;
+            // a run of plain DEM steps replays 10- and 2-step graphs (parity
+            // unchanged), an odd last step or a fluid step a 1-step graph
+            int run = 1;
+            if (kind == 0)
+                while (s + run < end && stepKind(d, s + run, gap) == 0) ++run;
+            while (run > 0) {
+                const int len = kind != 0 ? 1 : (run >= 10 ? 10 : (run >= 2 ? 2 : 1));
+                const auto& g = graphFor(e, kind, len, dt, s, gap);
+                CK(cudaGraphLaunch(g.exec, e->stream));
+                e->replayedKernels += g.kernels;
+                e->par ^= (len & 1);
+                s += len;
+                run -= len;
             }
-            while (s < end) fullStep(e, dt, s++, gap);
         }
         int done = 0;
         const int st = readStatus(e, &done);
@@ -950,10 +997,43 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
 
 void* demsph_stream(demsph_engine* e) { return e ? (void*)e->stream : nullptr; }
 
+long long demsph_device_bytes(const demsph_engine* e)
+{
+    if (!e) return -1;
+    long long b = 0;
+    for (const auto& a : e->owned) b += (long long)a.bytes;
+    return b;
+}
+
+long long demsph_estimate_bytes(const demsph_scene* sc, const demsph_options* opt)
+{
+    if (!sc || sc->n_fluid < 0 || sc->n_solid < 0) return -1;
+    demsph_options o{};
+    if (opt) o = *opt;
+    const long long kff = o.fluid_neighbors_max > 0 ? o.fluid_neighbors_max : 160;
+    const long long kfs = o.fluid_solids_max > 0 ? o.fluid_solids_max : 96;
+    const long long slots = o.solid_contacts_per_particle > 0 ? o.solid_contacts_per_particle : 16;
+    double mf = 0, ms = 0;
+    for (int i = 0; i < sc->n_fluid; ++i) mf = std::max(mf, sc->fluid_smoothing_length[i]);
+    for (int i = 0; i < sc->n_solid; ++i) ms = std::max(ms, sc->solid_effective_radius[i]);
+    const double cell = 2 * std::max(mf, ms);
+    long long cells = 1;
+    for (int a = 0; a < 3; ++a) cells *= sc->domain_size[a] > cell ? (long long)(sc->domain_size[a] / cell) : 1;
+    long long rows = 0;
+    for (int i = 0; i < sc->n_solid; ++i) rows += sc->solid_is_dummy[i] != 1;
+    const long long nf = sc->n_fluid, ns = sc->n_solid;
+    // per fluid particle: state, reorder buffers and both neighbour lists; per
+    // solid: state, sort and wall springs; per contact row: its slots, two
+    // list parities, springs in and out, candidates; per cell: counts and starts
+    return nf * (292 + 4 * (kff + kfs)) + ns * (248 + 48LL * sc->n_wall) +
+           rows * (56 + slots * 136 + 2 * slots * 4) + (cells + 1) * 16 + (long long)sc->n_clump * 160 +
+           std::min(64 * rows + 1024, std::max(1LL, kfs * nf)) * 4 + (1 << 20);
+}
+
 long long demsph_kernel_launches(demsph_engine* e)
 {
     if (!e) return -1;
-    return (t_kernelLaunches - e->launchBase) - e->capturedLaunches + e->replayedKernels;
+    return e->launched - e->capturedLaunches + e->replayedKernels;
 }
 
 int demsph_set_profiling(demsph_engine* e, int enable)

@@ -23,14 +23,23 @@ struct CudaError {
         if (_e != cudaSuccess) throw demsph::CudaError{_e, #call}; \
     } while (0)
 
+// A device buffer and its size.
+struct Allocation {
+    void* p;
+    size_t bytes;
+};
+
+// Stream-ordered allocation (cudaMallocAsync from the device's pool) on the
+// engine's stream: creating, growing or freeing one engine never waits for
+// the work of others on the same GPU.
 template <class T>
-inline T* dalloc(size_t n, std::vector<void*>& owned, bool zero = true)
+inline T* dalloc(size_t n, std::vector<Allocation>& owned, cudaStream_t s, bool zero = true)
 {
     T* p = nullptr;
     if (n == 0) n = 1;
-    CK(cudaMalloc(&p, sizeof(T) * n));
-    if (zero) CK(cudaMemset(p, 0, sizeof(T) * n));
-    owned.push_back(p);
+    CK(cudaMallocAsync(reinterpret_cast<void**>(&p), sizeof(T) * n, s));
+    if (zero) CK(cudaMemsetAsync(p, 0, sizeof(T) * n, s));
+    owned.push_back({p, sizeof(T) * n});
     return p;
 }
 
@@ -40,7 +49,7 @@ struct demsph_engine {
     demsph::DeviceState d{};
     int device = 0;
     cudaStream_t stream = nullptr;
-    std::vector<void*> owned;     // every cudaMalloc'd buffer
+    std::vector<demsph::Allocation> owned;  // every device buffer of the engine
     std::string err;
     int par = 1;                  // parity of the last successful solid list build
     bool forceWalk = false;       // next contact list from the reference's 27-cell walk
@@ -49,17 +58,22 @@ struct demsph_engine {
     int debug = 0;
     double hmax = 0;              // largest fluid smoothing length
     int nMassive = 0;
-    // CUDA graph of one period of steps
-    cudaGraphExec_t graph = nullptr;
-    int graphPeriod = 0, graphGap = 0, graphParity = -1;
+    // CUDA graphs of step runs, keyed by the kind of step, the contact-list
+    // parity they start from and their length (all for one dt and gap)
+    struct CachedGraph {
+        int kind, parity, length;
+        cudaGraphExec_t exec;
+        long long kernels;
+    };
+    std::vector<CachedGraph> graphs;
+    int graphGap = 0;
     double graphDt = 0;
     // contact tables as uploaded (FP32)
     std::vector<float> hzF, lnF, bdF, dampF;
     // kernel launch accounting (demsph_kernel_launches)
-    long long launchBase = 0;        // t_kernelLaunches when the engine was created
+    long long launched = 0;          // launch calls made by this engine's API calls (any thread)
     long long capturedLaunches = 0;  // launch calls recorded into graphs (not executed then)
     long long replayedKernels = 0;   // kernels executed by graph replays
-    long long graphKernels = 0;      // kernels in the current graph
     // stage timing (demsph_set_profiling)
     bool profiling = false;
     struct Timed {
@@ -77,9 +91,12 @@ struct demsph_engine {
             cudaEventDestroy(t.a);
             cudaEventDestroy(t.b);
         }
-        if (graph) cudaGraphExecDestroy(graph);
-        for (void* p : owned) cudaFree(p);
-        if (stream) cudaStreamDestroy(stream);
+        for (const auto& g : graphs) cudaGraphExecDestroy(g.exec);
+        for (const auto& a : owned) cudaFreeAsync(a.p, stream);
+        if (stream) {
+            cudaStreamSynchronize(stream);
+            cudaStreamDestroy(stream);
+        }
     }
 };
 
@@ -105,8 +122,17 @@ void splitPosition(const DeviceState& d, double3 p, int4& c, float4& h, float4& 
 
 }  // namespace demsph
 
+// Adds the launches one API call made (on its thread) to the engine's tally.
+struct LaunchTally {
+    demsph_engine* e;
+    long long t0;
+    explicit LaunchTally(demsph_engine* eng) : e(eng), t0(demsph::t_kernelLaunches) {}
+    ~LaunchTally() { e->launched += demsph::t_kernelLaunches - t0; }
+};
+
 #define ENGINE_GUARD(e)                                   \
     if (!(e) || !(e)->stream) return DEMSPH_ERR_ARGUMENT; \
+    LaunchTally _launch_tally(e);                         \
     try {                                                 \
         CK(cudaSetDevice((e)->device));
 

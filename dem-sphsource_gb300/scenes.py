@@ -309,6 +309,77 @@ def coupled_dam_break(dx=0.004, tank=(1.6, 0.4, 0.6), column=(0.4, 0.4, 0.4), n_
 
 
 # ---------------------------------------------------------------------------
+# Many scenes: the batched mix and the serving stream.
+# ---------------------------------------------------------------------------
+
+def sized_dam_break(n_fluid, column_height=0.3, steps=1000, seed=0):
+    """:func:`dam_break` with dx chosen so that a 0.4 x 0.4 x column_height
+    column holds about n_fluid particles."""
+    dx = (0.16 * column_height / n_fluid) ** (1.0 / 3.0)
+    return dam_break(dx=dx, column=(0.4, 0.4, column_height), steps=steps, seed=seed,
+                     name=f"dam_break_{n_fluid}")
+
+
+def sized_coupled(n_fluid, column_height=0.4, steps=1000, seed=0):
+    """:func:`coupled_dam_break` with dx for about n_fluid fluid particles and
+    the cube count scaled from 64 cubes per million fluid particles (at least one)."""
+    dx = (0.16 * column_height / n_fluid) ** (1.0 / 3.0)
+    cubes = max(1, int(round(64 * n_fluid / 1.0e6)))
+    return coupled_dam_break(dx=dx, column=(0.4, 0.4, column_height), n_cubes=cubes, steps=steps, seed=seed,
+                             name=f"coupled_{n_fluid}_{cubes}")
+
+
+def sized_granular(n_particles, steps=1000, seed=0):
+    """:func:`granular_settle` with about n_particles spheres and pebbles (one
+    four-pebble clump per 40 spheres)."""
+    n_clumps = max(1, n_particles // 44)
+    return granular_settle(n_spheres=n_particles - 4 * n_clumps, n_clumps=n_clumps, steps=steps, seed=seed,
+                           name=f"granular_{n_particles}")
+
+
+def batch_mix(n_scenes=256, n_range=(2000, 60000), sph_fraction=0.6, height_range=(0.2, 0.5), steps=1000,
+              seed=7):
+    """The batched workload: independent scenes, sph_fraction of them SPH dam
+    breaks and the rest coupled dam breaks, fluid counts log-uniform in
+    n_range, column heights uniform in height_range.  Returns recipes."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_scenes):
+        n = int(round(math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))))
+        hgt = float(rng.uniform(*height_range))
+        if rng.random() < sph_fraction:
+            out.append(sized_dam_break(n, hgt, steps, seed=seed * 1000 + k))
+        else:
+            out.append(sized_coupled(n, hgt, steps, seed=seed * 1000 + k))
+    return out
+
+
+def serving_stream(rate=20.0, duration=300.0, n_range=(5000, 500000), step_range=(200, 5000), seed=11):
+    """The serving workload: (arrival time s, kind, particle count, steps, seed)
+    tuples of a Poisson process of `rate` requests per second over `duration`
+    seconds; kinds SPH, DEM and coupled in equal shares, sizes log-uniform in
+    n_range, step counts uniform in step_range.  Scenes are built with
+    :func:`make_request` when they arrive."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            return out
+        n = int(round(math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))))
+        kind = ("sph", "dem", "coupled")[int(rng.integers(0, 3))]
+        out.append((t, kind, n, int(rng.integers(step_range[0], step_range[1] + 1)), int(rng.integers(1 << 30))))
+
+
+def make_request(kind, n, steps, seed):
+    if kind == "sph":
+        return sized_dam_break(n, 0.3, steps, seed)
+    if kind == "dem":
+        return sized_granular(n, steps, seed)
+    return sized_coupled(n, 0.4, steps, seed)
+
+
+# ---------------------------------------------------------------------------
 # Small scenes for parity tests and the smoke run (seconds on one CPU core).
 # ---------------------------------------------------------------------------
 

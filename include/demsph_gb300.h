@@ -229,6 +229,12 @@ DEMSPH_API int demsph_update(demsph_engine* e, double dt, int first_step, int n_
 /* The CUDA stream (cudaStream_t) the engine issues all its work on, for
    callers that time or order work around it. */
 DEMSPH_API void* demsph_stream(demsph_engine* e);
+/* Device memory the engine holds now (bytes), and an estimate, before
+   creation, of what demsph_create will allocate for a scene (without later
+   list growth or bonds).  No counterpart in the reference, whose memory is
+   sized by dataBase on the host. */
+DEMSPH_API long long demsph_device_bytes(const demsph_engine* e);
+DEMSPH_API long long demsph_estimate_bytes(const demsph_scene* scene, const demsph_options* opts);
 /* Kernels this engine has executed so far (graph replays counted by their
    kernels), as issued from the calling thread. */
 DEMSPH_API long long demsph_kernel_launches(demsph_engine* e);
@@ -284,6 +290,57 @@ DEMSPH_API int demsph_export_bonds(demsph_engine* e, int* pointed, int* pointing
                         double* contact_normal, double* contact_point, long long capacity);
 /* Shepard reference sums sumW0 (core/integrate.cu:44-47). */
 DEMSPH_API int demsph_export_fluid_sumw0(demsph_engine* e, double* sumw0);
+
+/* ---- scene server: many scenes on one GPU ----
+   No counterpart in the reference (one scene per process).  Scenes are
+   submitted with a step count, admitted first come, first served while their
+   estimated device memory fits the budget, and advanced together - each on
+   its own engine and CUDA stream, in chunks of steps replayed from CUDA graphs, by a
+   pool of worker threads - so that scenes arriving while others run join as
+   memory frees up.  Results stay on the host until released. */
+typedef struct demsph_server demsph_server;
+typedef struct demsph_server_config {
+    int device;                  /* CUDA device ordinal */
+    int workers;                 /* host threads advancing scenes; 0 = 16 */
+    int chunk_steps;             /* steps per turn of a scene; 0 = 100 */
+    long long hbm_budget_bytes;  /* device memory the admitted scenes may hold; 0 = 150 GiB */
+} demsph_server_config;
+typedef struct demsph_server_summary {
+    long long submitted, admitted, completed, failed, pending;
+    long long steps;             /* scene steps run */
+    long long particle_updates;  /* fluid particles per fluid step + solids with mass per step */
+    long long chunks;            /* turns taken (latency samples) */
+    long long bytes_in_use, peak_bytes;  /* reserved against the budget */
+    double busy_s;               /* first admission to the last completion (or now) */
+    double updates_per_s;        /* particle_updates / busy_s */
+    double p50_step_ms, p99_step_ms;     /* wall time per scene step, queueing for the GPU included */
+    double create_s, step_s, download_s; /* worker time summed over workers: engine creation and
+                                            initialisation, stepping, downloading results */
+} demsph_server_summary;
+typedef struct demsph_request_info {
+    int state;                   /* 0 pending, 1 running, 2 done, 3 failed */
+    int steps_done;
+    long long reserved_bytes;
+    double queued_s, run_s;
+} demsph_request_info;
+DEMSPH_API int demsph_server_create(const demsph_server_config* cfg, demsph_server** out);
+DEMSPH_API int demsph_server_destroy(demsph_server* s);
+/* Copies the scene; steps 1..n_steps of solverBase::update follow
+   (scene->time_step, scene->fluid_integrate_gap).  DEMSPH_ERR_CAPACITY: the
+   scene alone exceeds the budget. */
+DEMSPH_API int demsph_server_submit(demsph_server* s, const demsph_scene* scene, const demsph_options* opts,
+                                    int n_steps, long long* request_id);
+/* Waits until the request (or, for id -1, every request) has finished;
+   timeout_s < 0 waits without limit.  Returns the request's status. */
+DEMSPH_API int demsph_server_wait(demsph_server* s, long long request_id, double timeout_s);
+/* Final state of a finished request (original order, FP64, 3 per particle;
+   dRho 1 per particle); NULL skips an array. */
+DEMSPH_API int demsph_server_fetch(demsph_server* s, long long request_id, double* fluid_position,
+                                   double* fluid_velocity, double* fluid_drho, double* solid_position,
+                                   double* solid_velocity, double* solid_angular_velocity);
+DEMSPH_API int demsph_server_release(demsph_server* s, long long request_id);
+DEMSPH_API int demsph_server_request_info(demsph_server* s, long long request_id, demsph_request_info* info);
+DEMSPH_API int demsph_server_stats(demsph_server* s, demsph_server_summary* stats);
 
 /* ---- cell sort without allocation ----
    No counterpart in the reference.  Sorts n particle cell keys (device
