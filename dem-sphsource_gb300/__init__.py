@@ -64,13 +64,19 @@ class Options(C.Structure):
     """ctypes mirror of ``demsph_options``."""
 
     _fields_ = [("device", _I), ("fluid_neighbors_max", _I), ("fluid_solids_max", _I),
-                ("solid_contacts_per_particle", _I), ("fixes", _I), ("debug", _I), ("solid_verlet_skin", _D)]
+                ("solid_contacts_per_particle", _I), ("fixes", _I), ("debug", _I), ("solid_verlet_skin", _D),
+                ("fluid_lanes", _I)]
 
 
 class Counts(C.Structure):
     _fields_ = [("fluid_pairs", C.c_longlong), ("fluid_solid_pairs", C.c_longlong), ("solid_pairs", C.c_longlong),
                 ("bonds", C.c_longlong), ("bonds_intact", C.c_longlong), ("grid_cells", _I), ("grid_size", _I * 3),
                 ("cell_size", _D * 3)]
+
+
+class AuditValues(C.Structure):
+    _fields_ = [("mass", _D), ("momentum", _D * 3), ("kinetic_energy", _D), ("rotational_energy", _D),
+                ("potential_energy", _D), ("fluid_density_sum", _D)]
 
 
 class ServerConfig(C.Structure):
@@ -253,13 +259,13 @@ class Engine:
     """One scene on one GPU (the C ABI engine)."""
 
     def __init__(self, scene, device=0, fluid_neighbors_max=0, fluid_solids_max=0, solid_contacts_per_particle=0,
-                 fixes=0, debug=0, solid_verlet_skin=0.0):
+                 fixes=0, debug=0, solid_verlet_skin=0.0, fluid_lanes=0):
         """``solid_verlet_skin``: margin (m) of the solid contact candidates
         (0 = 0.2 x the smallest solid radius, < 0 = the 27-cell walk every step)."""
         self.lib = load_library()
         self.scene = scene
         opts = Options(device, fluid_neighbors_max, fluid_solids_max, solid_contacts_per_particle, fixes, debug,
-                       float(solid_verlet_skin))
+                       float(solid_verlet_skin), int(fluid_lanes))
         h = _P()
         rc = self.lib.demsph_create(C.byref(scene), C.byref(opts), C.byref(h))
         self.h = h
@@ -422,6 +428,15 @@ class Engine:
                                                            _ptr(f), C.c_longlong(m)), "fs")
         return {"prefix": prefix, "pointed": a, "pointing": b, "force": f}
 
+    def audit(self):
+        """FP64 sums over the scene: mass, momentum, kinetic / rotational /
+        potential energy, fluid density sum (demsph_audit)."""
+        a = AuditValues()
+        self._chk(self.lib.demsph_audit(self.h, C.byref(a)), "audit")
+        return {"mass": a.mass, "momentum": np.array(a.momentum[:]), "kinetic_energy": a.kinetic_energy,
+                "rotational_energy": a.rotational_energy, "potential_energy": a.potential_energy,
+                "fluid_density_sum": a.fluid_density_sum}
+
     def solid_pairs(self):
         prefix = np.zeros(self.ns, np.int32)
         self._chk(self.lib.demsph_export_solid_pairs(self.h, _ptr(prefix, _IP), *([None] * 7), C.c_longlong(0)), "ss")
@@ -454,7 +469,7 @@ def estimate_bytes(scene, **opts):
     lib = load_library()
     o = Options(0, opts.get("fluid_neighbors_max", 0), opts.get("fluid_solids_max", 0),
                 opts.get("solid_contacts_per_particle", 0), opts.get("fixes", 0), opts.get("debug", 0),
-                float(opts.get("solid_verlet_skin", 0.0)))
+                float(opts.get("solid_verlet_skin", 0.0)), int(opts.get("fluid_lanes", 0)))
     return int(lib.demsph_estimate_bytes(C.byref(scene), C.byref(o)))
 
 
@@ -487,7 +502,7 @@ class Server:
     def submit(self, scene, n_steps, **opts):
         o = Options(0, opts.get("fluid_neighbors_max", 0), opts.get("fluid_solids_max", 0),
                     opts.get("solid_contacts_per_particle", 0), opts.get("fixes", 0), opts.get("debug", 0),
-                    float(opts.get("solid_verlet_skin", 0.0)))
+                    float(opts.get("solid_verlet_skin", 0.0)), int(opts.get("fluid_lanes", 0)))
         rid = C.c_longlong()
         rc = self.lib.demsph_server_submit(self.h, C.byref(scene), C.byref(o), _I(n_steps), C.byref(rid))
         if rc != DEMSPH_OK:

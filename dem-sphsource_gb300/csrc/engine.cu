@@ -185,17 +185,23 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
         TIMED("fluid_hash_reorder");
         launchFluidHashReorder(d, s);
     }
-    {
+    // solids that never move (walls of dummy particles, fixed spheres) are
+    // hashed and sorted once, and again only after their positions are uploaded
+    const bool solidsMove = e->nMassive > 0 || e->solidSortStale;
+    if (solidsMove || e->forceWalk) {
         TIMED("solid_hash_sort");
-        launchSolidHashSort(d, fluidStep || e->forceWalk, s);
+        launchSolidHashSort(d, (fluidStep && solidsMove) || e->forceWalk || e->solidSortStale, s);
+        e->solidSortStale = false;
     }
     if (fluidStep) {
         {
             TIMED("fluid_lists");
             launchFluidLists(d, s);
         }
-        TIMED("coupling_lists");
-        launchCouplingLists(d, s);
+        if (e->nMassive > 0) {  // the coupling force moves only solids with mass
+            TIMED("coupling_lists");
+            launchCouplingLists(d, s);
+        }
     }
     e->par ^= 1;
     TIMED("solid_contact_list");
@@ -212,10 +218,11 @@ void stageBefore(demsph_engine* e, double dt)
 void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
 {
     DeviceState& d = e->d;
+    if (d.nf <= 0) return;
     const cudaStream_t s = e->stream;
     const double dtf = dt * (double)gap;
     const bool fluidStep = iStep % gap == 0;
-    if (d.nf > 0 && (iStep % (5 * gap) == 0 || iStep == 1)) {
+    if (iStep % (5 * gap) == 0 || iStep == 1) {
         TIMED("density_reinit");
         launchDensityReinit(d, iStep, s);
     }
@@ -223,7 +230,7 @@ void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
         TIMED("continuity");
         launchContinuityPass(d, 0, dtf, s);
     }
-    {
+    if (e->nMassive > 0) {
         TIMED("coupling_force");
         launchCoupling(d, fluidStep ? 1 : 0, s);
     }
@@ -388,6 +395,9 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
     *out = nullptr;
     if (sc->n_fluid < 0 || sc->n_solid < 0 || sc->n_clump < 0 || sc->n_wall < 0 || sc->n_material < 1)
         return DEMSPH_ERR_ARGUMENT;
+    if (sc->n_fluid >= MAX_LIST_INDEX || sc->n_solid >= MAX_LIST_INDEX) return DEMSPH_ERR_CAPACITY;
+    if (opt && (opt->fluid_lanes < 0 || opt->fluid_lanes > 8 || (opt->fluid_lanes & (opt->fluid_lanes - 1)) != 0))
+        return DEMSPH_ERR_ARGUMENT;
     demsph_options o{};
     if (opt) o = *opt;
     // Material ids index the contact tables (getCombinedIndex, core/hostStructs.h:369-384);
@@ -420,6 +430,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
         d.nw = sc->n_wall;
         d.kff = o.fluid_neighbors_max > 0 ? o.fluid_neighbors_max : 160;
         d.kfs = o.fluid_solids_max > 0 ? o.fluid_solids_max : 96;
+        d.lanes = o.fluid_lanes > 0 ? o.fluid_lanes : fluidLanes(d.nf);
         const int perParticle = o.solid_contacts_per_particle > 0 ? o.solid_contacts_per_particle : 16;
 
         // ---- grid: dataBase::setSpatialGrids (core/dataBase.cpp:415-432) ----

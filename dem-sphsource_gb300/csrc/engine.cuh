@@ -26,6 +26,23 @@ enum StatusBits : int {
     ST_MODE_CHANGE = 32,     // a solid left the domain: lists switch to the 27-cell walk; redo the step
 };
 
+// Neighbour list entries.  A fluid partner entry holds the partner's slot j,
+// the position t (0..26) of its cell in the reference's 27-cell walk around
+// the particle (z, y, x loops: t = 9 (dz+1) + 3 (dy+1) + (dx+1)) and whether
+// that cell is a plain in-domain cell, whose offset from the particle's cell
+// t then gives.  A solid partner entry holds the solid's index and t.  The
+// walk position restores the reference's list order on export.
+__host__ __device__ __forceinline__ unsigned ffEntry(int j, int t, bool regular)
+{
+    return ((unsigned)j << 6) | (regular ? 32u : 0u) | (unsigned)t;
+}
+__host__ __device__ __forceinline__ int ffPartner(unsigned e) { return (int)(e >> 6); }
+__host__ __device__ __forceinline__ int entryWalk(unsigned e) { return (int)(e & 31u); }
+__host__ __device__ __forceinline__ bool ffRegular(unsigned e) { return (e & 32u) != 0u; }
+__host__ __device__ __forceinline__ int fsEntry(int a, int t) { return (a << 5) | t; }
+__host__ __device__ __forceinline__ int fsPartner(int e) { return e >> 5; }
+constexpr int MAX_LIST_INDEX = 1 << 26;  // slots / solid indices the entries can hold
+
 struct GridDev {
     int gx, gy, gz, num;  // num = gx*gy*gz + 1; the last cell holds out-of-domain particles
     float3 cs;            // cell size, float part

@@ -53,6 +53,7 @@ struct demsph_engine {
     std::string err;
     int par = 1;                  // parity of the last successful solid list build
     bool forceWalk = false;       // next contact list from the reference's 27-cell walk
+    bool solidSortStale = true;   // solid cells must be recomputed although no solid has mass
     bool walkOrder[2] = {true, true};  // list of each parity is in the reference's walk order
     bool initialized = false;
     int debug = 0;

@@ -191,6 +191,67 @@ __global__ void kAddDamping(DeviceState d, int i, float cd)
     d.storque[i] = f4(T);
 }
 
+// ---- conservation audit (FP64) ----
+// Per block, FP64 sums of: mass, momentum (3), translational and rotational
+// kinetic energy, potential energy (-m g . x, x from the grid minimum) and
+// the fluid densities.  Fluids, solids with mass outside clumps, and clumps
+// as rigid bodies (their pebbles are not counted twice).
+constexpr int AUDIT_N = 8;
+constexpr int AUDIT_T = 256;
+
+__global__ void __launch_bounds__(AUDIT_T) kAudit(DeviceState d, double* partial)
+{
+    __shared__ double sh[AUDIT_N][AUDIT_T];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double q[AUDIT_N] = {0, 0, 0, 0, 0, 0, 0, 0};
+    auto add = [&](double m, double3 v, double3 x, double rot, double rho) {
+        q[0] += m;
+        q[1] += m * v.x;
+        q[2] += m * v.y;
+        q[3] += m * v.z;
+        q[4] += 0.5 * m * (v.x * v.x + v.y * v.y + v.z * v.z);
+        q[5] += rot;
+        q[6] -= m * (d.g64[0] * x.x + d.g64[1] * x.y + d.g64[2] * x.z);
+        q[7] += rho;
+    };
+    auto dfv = [](float4 h, float4 l) {
+        return make_double3((double)h.x + l.x, (double)h.y + l.y, (double)h.z + l.z);
+    };
+    if (k < d.nf) {
+        const int4 c = d.fcell[k];
+        const float4 h = d.fph[0][k], l = d.fpl[0][k];
+        const float4 par = d.fpar[k];
+        const double3 x = make_double3(c.x * d.cs[0] + ((double)h.x + l.x), c.y * d.cs[1] + ((double)h.y + l.y),
+                                       c.z * d.cs[2] + ((double)h.z + l.z));
+        add(par.w, dfv(d.fvh[0][k], d.fvl[0][k]), x, 0.0, (double)par.x + d.fdrho[0][k]);
+    } else if (k < d.nf + d.ns) {
+        const int i = k - d.nf;
+        const int4 f = d.sflags[i];
+        const float im = d.sph[i].w;
+        if (im > 0.f && f.z < 0) {
+            const double m = 1.0 / im;
+            const double3 x = solidAbsPos(d, i);
+            const double3 xr = make_double3(x.x - d.minB[0], x.y - d.minB[1], x.z - d.minB[2]);
+            const double3 w = dfv(d.swh[i], d.swl[i]);
+            const double r = d.srad[i].x;
+            add(m, dfv(d.svh[i], d.svl[i]), xr, 0.5 * 0.4 * m * r * r * (w.x * w.x + w.y * w.y + w.z * w.z), 0.0);
+        }
+    } else if (k < d.nf + d.ns + d.nc) {
+        const int c = k - d.nf - d.ns;
+        const float im = d.cinvm[c];
+        if (im > 0.f) add(1.0 / im, dfv(d.cvH[c], d.cvL[c]), dfv(d.cpH[c], d.cpL[c]), 0.0, 0.0);
+    }
+    for (int a = 0; a < AUDIT_N; ++a) sh[a][threadIdx.x] = q[a];
+    __syncthreads();
+    for (int o = AUDIT_T / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int a = 0; a < AUDIT_N; ++a) sh[a][threadIdx.x] += sh[a][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int a = 0; a < AUDIT_N; ++a) partial[(size_t)blockIdx.x * AUDIT_N + a] = sh[a][0];
+}
+
 template <class T>
 void d2h(std::vector<T>& v, const T* src, size_t n)
 {
@@ -286,7 +347,10 @@ int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel,
     if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     if (dw) CK(cudaMemcpyAsync(dw, angvel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw);
-    if (dp) CK(cudaMemsetAsync(d.rebuild, 0xff, sizeof(int), e->stream));  // candidates from the new positions
+    if (dp) {
+        CK(cudaMemsetAsync(d.rebuild, 0xff, sizeof(int), e->stream));  // candidates from the new positions
+        e->solidSortStale = true;
+    }
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)
@@ -450,12 +514,21 @@ int demsph_export_fluid_pairs(demsph_engine* e, int* prefix, int* pointed, int* 
     d2h(id, d.fid, n);
     slot.resize(n);
     for (int s = 0; s < n; ++s) slot[id[s]] = s;
+    // the reference's order: by walk position, then by sorted position in the
+    // cell (the slot: fluids are stored in (cell, index) order)
     long long w = 0;
+    std::vector<std::pair<long long, int>> order;
     for (int i = 0; i < n; ++i) {
         const int s = slot[i];
         const int m = std::min(ffc[s], d.kff);
+        order.clear();
         for (int k = 0; k < m; ++k) {
-            const int j = id[ff[(size_t)k * n + s] >> 5];
+            const unsigned v = ff[(size_t)k * n + s];
+            order.push_back({(long long)entryWalk(v) * n + ffPartner(v), ffPartner(v)});
+        }
+        std::sort(order.begin(), order.end());
+        for (const auto& o : order) {
+            const int j = id[o.second];
             if (j <= i) continue;
             if (w < cap) {
                 if (pointed) pointed[w] = i;
@@ -488,13 +561,21 @@ int demsph_export_fluid_solid_pairs(demsph_engine* e, int* prefix, int* pointed,
     slot.resize(n);
     for (int s = 0; s < n; ++s) slot[id[s]] = s;
     long long w = 0;
+    std::vector<std::pair<long long, int>> order;
     for (int i = 0; i < n; ++i) {
         const int s = slot[i];
         const int m = std::min(fsc[s], d.kfs);
+        order.clear();
         for (int k = 0; k < m; ++k) {
+            const int v = fs[(size_t)k * n + s];
+            order.push_back({(long long)entryWalk((unsigned)v) * d.ns + fsPartner(v), k});
+        }
+        std::sort(order.begin(), order.end());  // walk position, then index
+        for (const auto& o : order) {
+            const int k = o.second;
             if (w < cap) {
                 if (pointed) pointed[w] = i;
-                if (pointing) pointing[w] = fs[(size_t)k * n + s];
+                if (pointing) pointing[w] = fsPartner(fs[(size_t)k * n + s]);
                 if (force) {
                     const float4 f = pf.empty() ? make_float4(0, 0, 0, 0) : pf[(size_t)k * n + s];
                     force[3 * w] = f.x;
@@ -684,6 +765,31 @@ int demsph_export_bonds(demsph_engine* e, int* pointed, int* pointing, int* isb,
             if (point) point[3 * b + a] = pos[3 * (size_t)ab[b].x + a] + (&L[b].x)[a];
         }
     }
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_audit(demsph_engine* e, demsph_audit_values* out)
+{
+    if (!out) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    const long long n = (long long)d.nf + d.ns + d.nc;
+    const int blocks = blocksFor(std::max(1LL, n), AUDIT_T);
+    double* buf = scratchDoubles(e, (size_t)blocks * AUDIT_N);
+    ++t_kernelLaunches, kAudit<<<blocks, AUDIT_T, 0, e->stream>>>(d, buf);
+    std::vector<double> h((size_t)blocks * AUDIT_N);
+    CK(cudaMemcpyAsync(h.data(), buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    double q[AUDIT_N] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int b = 0; b < blocks; ++b)
+        for (int a = 0; a < AUDIT_N; ++a) q[a] += h[(size_t)b * AUDIT_N + a];
+    out->mass = q[0];
+    for (int a = 0; a < 3; ++a) out->momentum[a] = q[1 + a];
+    out->kinetic_energy = q[4];
+    out->rotational_energy = q[5];
+    out->potential_energy = q[6];
+    out->fluid_density_sum = q[7];
     return DEMSPH_OK;
     ENGINE_END(e)
 }

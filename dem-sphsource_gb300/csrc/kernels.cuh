@@ -25,6 +25,7 @@ struct DeviceState {
 
     // ---- fluid (slots in cell order) ----
     int nf, kff, kfs;
+    int lanes;               // threads per fluid particle in the list and pair loops
     int4* fcell;
     float4* fph[2];
     float4* fpl[2];
@@ -169,6 +170,24 @@ struct RunIf {
     const int* b = nullptr;
     __device__ __forceinline__ bool active() const { return always || (a && *a) || (b && *b); }
 };
+
+// Lanes per fluid particle in the fluid pair loops and list builder: enough
+// threads for every SM (152 SMs x 2048) when the scene is small, one lane per
+// particle when it is large.
+int fluidLanes(int nf);
+
+// Launches kernel<L> (L in 1, 2, 4, 8) over n items x L lanes.
+#define LAUNCH_LANES(kernel, L, n, threads, s, ...)                                                    \
+    do {                                                                                               \
+        const unsigned blocks_ = (unsigned)blocksFor((long long)(n) * (L), threads);                  \
+        ++t_kernelLaunches;                                                                            \
+        switch (L) {                                                                                   \
+        case 8: kernel<8><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                             \
+        case 4: kernel<4><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                             \
+        case 2: kernel<2><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                             \
+        default: kernel<1><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                            \
+        }                                                                                              \
+    } while (0)
 
 // scan.cu
 size_t scanWorkspaceInts(int n);

@@ -72,37 +72,130 @@ __device__ __forceinline__ void forStencil(int4 c, float4 h, float4 l, const Gri
 }
 
 // ---- fluid lists (full) ----
+// One particle's 27-cell walk split over a group of L lanes: lane l takes the
+// walk positions t = l, l + L, ...  The group advances in lockstep, one
+// candidate per lane per round; the accepted entries of a round are written
+// in lane order after the entries of earlier rounds (a warp ballot gives each
+// its slot), so the list is complete and its order fixed, though not the
+// walk order (exports restore that from the walk positions in the entries).
+struct LaneWalk {
+    int t, p, pe, hx, hy, hz, hash;
+    bool regular;
+};
+
+// Next candidate in lane's share of the walk over the cell ranges `start`
+// (fluid or solid cells); returns false when the share is exhausted.
+template <int L>
+__device__ __forceinline__ bool nextCandidate(LaneWalk& w, const int* __restrict__ start, int sx, int sy, int sz,
+                                              const GridDev& g, int& idx)
+{
+    while (w.p >= w.pe) {
+        w.t += L;
+        if (w.t >= 27) return false;
+        const int dx = w.t % 3 - 1, dy = (w.t / 3) % 3 - 1, dz = w.t / 9 - 1;
+        w.hx = sx + dx;
+        w.hy = sy + dy;
+        w.hz = sz + dz;
+        w.hash = w.hz * g.gy * g.gx + w.hy * g.gx + w.hx;
+        if (w.hash < 0 || w.hash >= g.num) continue;
+        w.regular = inDomain(w.hx, w.hy, w.hz, g);
+        w.p = start[w.hash];
+        w.pe = start[w.hash + 1];
+    }
+    idx = w.p++;
+    return true;
+}
+
+template <int L>
 __global__ void __launch_bounds__(T) kFluidLists(DeviceState d)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.nf || *d.status) return;
-    const int4 ci = d.fcell[i];
-    const float4 hi = d.fph[0][i];
-    const float4 li = d.fpl[0][i];
-    const dfl hI = df_make(hi.w, li.w);
-    const dfl cutS = df_add(hI, hI);  // fluid-solid: 2 h_i
+    const int th = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((th & ~31) >= d.nf * L || *d.status) return;
+    const int i = th / L, lane = th % L;
+    const bool live = i < d.nf;
+    const int groupShift = (threadIdx.x & 31) & ~(L - 1);
+    const unsigned groupBits = L == 32 ? 0xffffffffu : ((1u << L) - 1u);
+    const unsigned below = (1u << lane) - 1u;
     const int n = d.nf;
-    int nff = 0, nfs = 0;
-    forStencil(ci, hi, li, d.grid, [&](int hash, bool regular, int hx, int hy, int hz) {
-        const int4 cellHere = make_int4(hx, hy, hz, hash);
-        for (int j = d.fcellStart[hash], je = d.fcellStart[hash + 1]; j < je; ++j) {
-            if (j == i) continue;
-            const int4 cj = regular ? cellHere : d.fcell[j];
-            const float4 hj = d.fph[0][j];
-            const dfl hJ = df_make(hj.w, d.fpl[0][j].w);
-            const dfl rad = dfMax(hI, hJ);
-            if (!withinCut(ci, hi, li, cj, hj, d.fpl[0], j, df_add(rad, rad), d.grid)) continue;
-            if (nff < d.kff) d.ff[(size_t)nff * n + i] = ((unsigned)j << 5) | deltaCode(cj.x - ci.x, cj.y - ci.y, cj.z - ci.z);
-            ++nff;
+    int4 ci = make_int4(0, 0, 0, 0);
+    float4 hi = make_float4(0, 0, 0, 0), li = hi;
+    dfl hI = df_make(0.f), cutS = hI;
+    int sx = 0, sy = 0, sz = 0;
+    if (live) {
+        ci = d.fcell[i];
+        hi = d.fph[0][i];
+        li = d.fpl[0][i];
+        hI = df_make(hi.w, li.w);
+        cutS = df_add(hI, hI);  // fluid-solid: 2 h_i
+        sx = truncAxis(ci.x, hi.x, li.x);
+        sy = truncAxis(ci.y, hi.y, li.y);
+        sz = truncAxis(ci.z, hi.z, li.z);
+    }
+    // a walk position gives the partner's cell offset from the particle's own
+    // cell only when the walk is centred on that cell
+    const bool centred = sx == ci.x && sy == ci.y && sz == ci.z;
+    // fluid partners
+    int nff = 0;
+    {
+        LaneWalk w{lane - L, 0, 0, 0, 0, 0, 0, false};
+        while (true) {
+            int j = 0;
+            const bool has = live && nextCandidate<L>(w, d.fcellStart, sx, sy, sz, d.grid, j);
+            bool take = false;
+            int4 cj = make_int4(0, 0, 0, 0);
+            if (has && j != i) {
+                cj = w.regular ? make_int4(w.hx, w.hy, w.hz, w.hash) : d.fcell[j];
+                const float4 hj = d.fph[0][j];
+                // FP32 decision away from the cut (most candidates); the exact
+                // double-float test within 1e-5 of it
+                const float3 r = relF(ci, hi, cj, hj, d.grid);
+                const float c = 2.f * fmaxf(hi.w, hj.w);
+                const float d2 = dot3(r, r), c2 = c * c;
+                if (d2 < c2 * (1.f - 1.e-5f)) {
+                    take = true;
+                } else if (d2 <= c2 * (1.f + 1.e-5f)) {
+                    const dfl hJ = df_make(hj.w, d.fpl[0][j].w);
+                    const dfl rad = dfMax(hI, hJ);
+                    take = withinCut(ci, hi, li, cj, hj, d.fpl[0], j, df_add(rad, rad), d.grid);
+                }
+            }
+            const unsigned mine = (__ballot_sync(0xffffffffu, take) >> groupShift) & groupBits;
+            if (take) {
+                const int slot = nff + __popc(mine & below);
+                if (slot < d.kff) d.ff[(size_t)slot * n + i] = ffEntry(j, w.t, w.regular && centred);
+            }
+            nff += __popc(mine);
+            if (!__any_sync(0xffffffffu, has)) break;
         }
-        for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
-            const int a = d.ssorted[p];
-            const int4 ca = regular ? cellHere : d.scell[a];
-            if (!withinCut(ci, hi, li, ca, d.sph[a], d.spl, a, cutS, d.grid)) continue;
-            if (nfs < d.kfs) d.fs[(size_t)nfs * n + i] = a;
-            ++nfs;
+    }
+    // solid partners
+    int nfs = 0;
+    {
+        LaneWalk w{lane - L, 0, 0, 0, 0, 0, 0, false};
+        while (true) {
+            int p = 0;
+            const bool has = live && nextCandidate<L>(w, d.scellStart, sx, sy, sz, d.grid, p);
+            bool take = false;
+            int a = 0;
+            if (has) {
+                a = d.ssorted[p];
+                const int4 ca = w.regular ? make_int4(w.hx, w.hy, w.hz, w.hash) : d.scell[a];
+                const float4 ha = d.sph[a];
+                const float3 r = relF(ci, hi, ca, ha, d.grid);
+                const float d2 = dot3(r, r), c2 = 4.f * hi.w * hi.w;
+                if (d2 < c2 * (1.f - 1.e-5f)) take = true;
+                else if (d2 <= c2 * (1.f + 1.e-5f)) take = withinCut(ci, hi, li, ca, ha, d.spl, a, cutS, d.grid);
+            }
+            const unsigned mine = (__ballot_sync(0xffffffffu, take) >> groupShift) & groupBits;
+            if (take) {
+                const int slot = nfs + __popc(mine & below);
+                if (slot < d.kfs) d.fs[(size_t)slot * n + i] = fsEntry(a, w.t);
+            }
+            nfs += __popc(mine);
+            if (!__any_sync(0xffffffffu, has)) break;
         }
-    });
+    }
+    if (!live || lane != 0) return;
     d.ffc[i] = nff;
     d.fsc[i] = nfs;
     if (nff > d.kff) atomicOr(d.status, ST_FF_OVERFLOW);
@@ -116,7 +209,7 @@ __global__ void kCoupCount(DeviceState d)
     if (i >= d.nf || *d.status) return;
     const int m = min(d.fsc[i], d.kfs);
     for (int k = 0; k < m; ++k) {
-        const int a = d.fs[(size_t)k * d.nf + i];
+        const int a = fsPartner(d.fs[(size_t)k * d.nf + i]);
         if (d.sflags[a].w & F_HASMASS) atomicAdd(&d.coupCount[a], 1);
     }
 }
@@ -130,7 +223,7 @@ __global__ void kCoupFill(DeviceState d)
     }
     const int m = min(d.fsc[i], d.kfs);
     for (int k = 0; k < m; ++k) {
-        const int a = d.fs[(size_t)k * d.nf + i];
+        const int a = fsPartner(d.fs[(size_t)k * d.nf + i]);
         if (d.sflags[a].w & F_HASMASS) d.coupList[d.coupStart[a] + atomicAdd(&d.coupCount[a], 1)] = i;
     }
 }
@@ -383,23 +476,36 @@ __global__ void kSolidNormals(DeviceState d, double h)
     const double3 pa = solidAbsPos(d, a);
     const double PI = 3.1415926535897931;
     const double sigma = 21.0 / (16.0 * PI * h * h * h);
-    const double vFixed = pow(h / 1.3, 3);
+    const double hf = h / 1.3;
+    const double vFixed = hf * hf * hf;
+    // FP32 pre-test: candidates clearly beyond 2h skip the FP64 arithmetic
+    // (GB300's FP64 rate is a small fraction of its FP32 rate)
+    const float far2 = (float)(4.0 * h * h) * (1.f + 1.e-4f);
     double tx = 0, ty = 0, tz = 0;
     forStencil(ca, ha, la, d.grid, [&](int hash, bool, int, int, int) {
         for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
             const int b = d.ssorted[p];
+            const int4 fb = d.sflags[b];
+            const bool fixedPair = !(fa.w & F_MASSIVE) && !(fb.w & F_MASSIVE);  // both inverse mass <= 1e-10
+            const bool sameClump = fa.z >= 0 && fa.z == fb.z;
+            if (!fixedPair && !sameClump) continue;
+            const float3 r32 = relF(ca, ha, d.scell[b], d.sph[b], d.grid);
+            if (dot3(r32, r32) > far2) continue;
             const double3 pb = solidAbsPos(d, b);
             const double rx = pa.x - pb.x, ry = pa.y - pb.y, rz = pa.z - pb.z;
             const double rr = sqrt(rx * rx + ry * ry + rz * rz);
             if (rr > 2 * h) continue;
-            const int4 fb = d.sflags[b];
             double vol;
-            if (!(fa.w & F_MASSIVE) && !(fb.w & F_MASSIVE)) vol = vFixed;  // both inverse mass <= 1e-10
-            else if (fa.z >= 0 && fa.z == fb.z) vol = pow(2.0 * (double)d.srad[b].x + 2.0 * (double)d.srad[b].y, 3.0);
-            else continue;
+            if (fixedPair) {
+                vol = vFixed;
+            } else {
+                const double s2 = 2.0 * (double)d.srad[b].x + 2.0 * (double)d.srad[b].y;
+                vol = s2 * s2 * s2;
+            }
             if (rr < 1.e-10 || rr >= 2.0 * h) continue;  // gradient of W is zero
             const double q = rr / h, t = 1.0 - 0.5 * q;
-            const double dWdq = -2.0 * pow(t, 3) * (1.0 + 2.0 * q) + 2.0 * pow(t, 4);
+            const double t3 = t * t * t;
+            const double dWdq = -2.0 * t3 * (1.0 + 2.0 * q) + 2.0 * t3 * t;
             const double f = sigma * dWdq / h / rr;
             tx -= vol * f * rx;
             ty -= vol * f * ry;
@@ -416,7 +522,7 @@ __global__ void kSolidNormals(DeviceState d, double h)
 void launchFluidLists(const DeviceState& d, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    ++t_kernelLaunches, kFluidLists<<<blocksFor(d.nf, T), T, 0, s>>>(d);
+    LAUNCH_LANES(kFluidLists, d.lanes, d.nf, T, s, d);
 }
 
 void launchCouplingLists(const DeviceState& d, cudaStream_t s)

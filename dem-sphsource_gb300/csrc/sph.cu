@@ -36,8 +36,8 @@ constexpr float SIG = 21.f / (16.f * 3.14159265358979323846f);       // sigma h^
 __device__ __forceinline__ float3 fluidRel(const DeviceState& d, int ps, int i, int4 ci, float4 pi, unsigned e,
                                            int j, float4 pj)
 {
-    const unsigned code = e & 31u;
-    if (code < 27u) {
+    if (ffRegular(e)) {
+        const unsigned code = (unsigned)entryWalk(e);
         const int dx = (int)(code % 3u) - 1, dy = (int)((code / 3u) % 3u) - 1, dz = (int)(code / 9u) - 1;
         return make_float3((pi.x - pj.x) - (float)dx * d.grid.cs.x, (pi.y - pj.y) - (float)dy * d.grid.cs.y,
                            (pi.z - pj.z) - (float)dz * d.grid.cs.z);
@@ -115,6 +115,30 @@ __device__ __forceinline__ void dfAxpy(float4& xh, float4& xl, float4 vh, float4
     xh.z = z.hi; xl.z = z.lo;
 }
 
+// ---- lane groups ----
+// A fluid particle's neighbour loop is split over a group of L lanes (L a
+// power of two <= 32, chosen per scene so that small scenes still fill the
+// GPU); the lanes' compensated partial sums are added in a fixed tree, so the
+// result does not depend on timing.  Kernels return early only for whole
+// warps: the shuffles take every lane.
+template <int L>
+__device__ __forceinline__ dfl groupSum(dfl v)
+{
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+        const dfl u = df_make(__shfl_xor_sync(0xffffffffu, v.hi, o, L), __shfl_xor_sync(0xffffffffu, v.lo, o, L));
+        v = (threadIdx.x & o) ? df_add(u, v) : df_add(v, u);
+    }
+    return v;
+}
+template <int L>
+__device__ __forceinline__ float groupSum(const KahanF& k)
+{
+    if (L == 1) return k.value();
+    const dfl v = groupSum<L>(df_two_sum(k.s, -k.c));
+    return v.hi + v.lo;
+}
+
 // ---- continuity (+ optional drift) ----
 struct ContinuityArgs {
     int ps, vs, ds, dd;  // position / velocity / density source, density destination
@@ -124,45 +148,53 @@ struct ContinuityArgs {
     dfl drift;
 };
 
+template <int L>
 __global__ void __launch_bounds__(T) kContinuity(DeviceState d, ContinuityArgs a)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.nf || *d.status) return;
-    const Self o = loadSelf(d, i, a.ps, a.vs, a.ds);
-    const int n = d.nf;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((t & ~31) >= d.nf * L || *d.status) return;
+    const int i = t / L, lane = t % L;
+    const bool live = i < d.nf;
     KahanF acc;
-    const int nff = min(d.ffc[i], d.kff);
-    for (int k = 0; k < nff; ++k) {
-        const unsigned e = d.ff[(size_t)k * n + i];
-        const int j = (int)(e >> 5);
-        const float4 pj = d.fph[a.ps][j];
-        const float3 r = fluidRel(d, a.ps, i, o.c, o.p, e, j, pj);
-        const float h = 0.5f * (o.h + pj.w);
-        const float r2 = dot3(r, r);
-        if (r2 >= 4.f * h * h) continue;
-        const float4 par = d.fpar[j];
-        const float drj = d.fdrho[a.ds][j];
-        const float rhoj = par.x + drj;
-        const float Pj = drj * par.y * par.y;
-        const float Vj = par.w / rhoj;
-        const float rr = sqrtf(r2);
-        const float t = 1.f - 0.5f * rr / h;
-        const float h2 = h * h;
-        const float G = KG * t * t * t / (h2 * h2 * h);
-        const float c = 0.5f * (o.cs + par.y);
-        const float3 vij = o.v - xyz(d.fvh[a.vs][j]);
-        acc.add(-2.f * o.rho * Vj * G / (o.rho + rhoj) * (rhoj * dot3(vij, r) + (o.P - Pj) * rr / c));
+    Self o;
+    if (live) {
+        o = loadSelf(d, i, a.ps, a.vs, a.ds);
+        const int n = d.nf;
+        const int nff = min(d.ffc[i], d.kff);
+        for (int k = lane; k < nff; k += L) {
+            const unsigned e = d.ff[(size_t)k * n + i];
+            const int j = ffPartner(e);
+            const float4 pj = d.fph[a.ps][j];
+            const float3 r = fluidRel(d, a.ps, i, o.c, o.p, e, j, pj);
+            const float h = 0.5f * (o.h + pj.w);
+            const float r2 = dot3(r, r);
+            if (r2 >= 4.f * h * h) continue;
+            const float4 par = d.fpar[j];
+            const float drj = d.fdrho[a.ds][j];
+            const float rhoj = par.x + drj;
+            const float Pj = drj * par.y * par.y;
+            const float Vj = par.w / rhoj;
+            const float rr = sqrtf(r2);
+            const float tt = 1.f - 0.5f * rr / h;
+            const float h2 = h * h;
+            const float G = KG * tt * tt * tt / (h2 * h2 * h);
+            const float c = 0.5f * (o.cs + par.y);
+            const float3 vij = o.v - xyz(d.fvh[a.vs][j]);
+            acc.add(-2.f * o.rho * Vj * G / (o.rho + rhoj) * (rhoj * dot3(vij, r) + (o.P - Pj) * rr / c));
+        }
+        const int nfs = min(d.fsc[i], d.kfs);
+        const float ci2 = o.cs * o.cs;
+        for (int k = lane; k < nfs; k += L) {
+            const int sa = fsPartner(d.fs[(size_t)k * n + i]);
+            const SolidPartner sp = solidPartner(d, o.c, o.p, o.h, o.P, o.rho, o.rho0, ci2, sa);
+            if (!sp.inside) continue;
+            acc.add(-2.f * o.rho * sp.Va * sp.G / (o.rho + sp.rhoa) *
+                    (2.f * sp.rhoa * dot3(o.v - sp.v, sp.r) + (o.P - sp.Pa) * sp.rr / o.cs));
+        }
     }
-    const int nfs = min(d.fsc[i], d.kfs);
-    const float ci2 = o.cs * o.cs;
-    for (int k = 0; k < nfs; ++k) {
-        const int sa = d.fs[(size_t)k * n + i];
-        const SolidPartner s = solidPartner(d, o.c, o.p, o.h, o.P, o.rho, o.rho0, ci2, sa);
-        if (!s.inside) continue;
-        acc.add(-2.f * o.rho * s.Va * s.G / (o.rho + s.rhoa) *
-                (2.f * s.rhoa * dot3(o.v - s.v, s.r) + (o.P - s.Pa) * s.rr / o.cs));
-    }
-    d.fdrho[a.dd][i] = d.fdrho[a.ds][i] + a.dt * acc.value();
+    const float sum = groupSum<L>(acc);
+    if (!live || lane != 0) return;
+    d.fdrho[a.dd][i] = d.fdrho[a.ds][i] + a.dt * sum;
     if (a.driftTo >= 0) {
         float4 xh = d.fph[a.ps][i], xl = d.fpl[a.ps][i];
         dfAxpy(xh, xl, d.fvh[a.vs][i], d.fvl[a.vs][i], a.drift);
@@ -178,55 +210,62 @@ __global__ void __launch_bounds__(T) kContinuity(DeviceState d, ContinuityArgs a
 // ---- momentum + kick (dt_f) + drift (dt_f / 2) ----
 // Reads position [1], velocity [0], density [1]; writes acc, velocity [1] and
 // position [0] (the buffers no other thread reads in this pass).
+template <int L>
 __global__ void __launch_bounds__(T) kMomentum(DeviceState d, dfl dtf, dfl halfDtf)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.nf || *d.status) return;
-    const Self o = loadSelf(d, i, 1, 0, 1);
-    const int n = d.nf;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((t & ~31) >= d.nf * L || *d.status) return;
+    const int i = t / L, lane = t % L;
+    const bool live = i < d.nf;
     KahanF3 acc;
-    const int nff = min(d.ffc[i], d.kff);
-    for (int k = 0; k < nff; ++k) {
-        const unsigned e = d.ff[(size_t)k * n + i];
-        const int j = (int)(e >> 5);
-        const float4 pj = d.fph[1][j];
-        const float3 r = fluidRel(d, 1, i, o.c, o.p, e, j, pj);
-        const float h = 0.5f * (o.h + pj.w);
-        const float r2 = dot3(r, r);
-        if (r2 >= 4.f * h * h) continue;
-        const float4 par = d.fpar[j];
-        const float drj = d.fdrho[1][j];
-        const float rhoj = par.x + drj;
-        const float Pj = drj * par.y * par.y;
-        const float Vj = par.w / rhoj;
-        const float gj = par.z * rhoj;
-        const float rr = sqrtf(r2);
-        const float t = 1.f - 0.5f * rr / h;
-        const float h2 = h * h;
-        const float G = KG * t * t * t / (h2 * h2 * h);
-        const float c = 0.5f * (o.cs + par.y);
-        const float3 vij = o.v - xyz(d.fvh[0][j]);
-        const float dU = -dot3(vij, r) / rr;  // U_L - U_R
-        const float beta = fminf(3.f * fmaxf(dU, 0.f), c);
-        const float Ps = (o.rho * Pj + rhoj * o.P + o.rho * rhoj * beta * dU) / (o.rho + rhoj);
-        const float gbar = 2.f * o.gam * gj / (o.gam + gj);
-        const float w = 2.f * o.V * Vj * G / o.m;
-        acc.add((r * Ps - vij * gbar) * w);
+    if (live) {
+        const Self o = loadSelf(d, i, 1, 0, 1);
+        const int n = d.nf;
+        const int nff = min(d.ffc[i], d.kff);
+        for (int k = lane; k < nff; k += L) {
+            const unsigned e = d.ff[(size_t)k * n + i];
+            const int j = ffPartner(e);
+            const float4 pj = d.fph[1][j];
+            const float3 r = fluidRel(d, 1, i, o.c, o.p, e, j, pj);
+            const float h = 0.5f * (o.h + pj.w);
+            const float r2 = dot3(r, r);
+            if (r2 >= 4.f * h * h) continue;
+            const float4 par = d.fpar[j];
+            const float drj = d.fdrho[1][j];
+            const float rhoj = par.x + drj;
+            const float Pj = drj * par.y * par.y;
+            const float Vj = par.w / rhoj;
+            const float gj = par.z * rhoj;
+            const float rr = sqrtf(r2);
+            const float tt = 1.f - 0.5f * rr / h;
+            const float h2 = h * h;
+            const float G = KG * tt * tt * tt / (h2 * h2 * h);
+            const float c = 0.5f * (o.cs + par.y);
+            const float3 vij = o.v - xyz(d.fvh[0][j]);
+            const float dU = -dot3(vij, r) / rr;  // U_L - U_R
+            const float beta = fminf(3.f * fmaxf(dU, 0.f), c);
+            const float Ps = (o.rho * Pj + rhoj * o.P + o.rho * rhoj * beta * dU) / (o.rho + rhoj);
+            const float gbar = 2.f * o.gam * gj / (o.gam + gj);
+            const float w = 2.f * o.V * Vj * G / o.m;
+            acc.add((r * Ps - vij * gbar) * w);
+        }
+        const int nfs = min(d.fsc[i], d.kfs);
+        const float ci2 = o.cs * o.cs;
+        for (int k = lane; k < nfs; k += L) {
+            const int sa = fsPartner(d.fs[(size_t)k * n + i]);
+            const SolidPartner sp = solidPartner(d, o.c, o.p, o.h, o.P, o.rho, o.rho0, ci2, sa);
+            if (!sp.inside) continue;
+            const float3 via = o.v - sp.v;
+            const float dU = -2.f * dot3(via, xyz(d.snormal[sa]));
+            const float beta = fminf(3.f * fmaxf(dU, 0.f), o.cs);
+            const float Ps = (o.rho * sp.Pa + sp.rhoa * o.P + o.rho * sp.rhoa * beta * dU) / (o.rho + sp.rhoa);
+            const float w = 2.f * o.V * sp.Va * sp.G / o.m;
+            acc.add((sp.r * Ps - via * (2.f * o.gam)) * w);
+        }
     }
-    const int nfs = min(d.fsc[i], d.kfs);
-    const float ci2 = o.cs * o.cs;
-    for (int k = 0; k < nfs; ++k) {
-        const int sa = d.fs[(size_t)k * n + i];
-        const SolidPartner s = solidPartner(d, o.c, o.p, o.h, o.P, o.rho, o.rho0, ci2, sa);
-        if (!s.inside) continue;
-        const float3 via = o.v - s.v;
-        const float dU = -2.f * dot3(via, xyz(d.snormal[sa]));
-        const float beta = fminf(3.f * fmaxf(dU, 0.f), o.cs);
-        const float Ps = (o.rho * s.Pa + s.rhoa * o.P + o.rho * s.rhoa * beta * dU) / (o.rho + s.rhoa);
-        const float w = 2.f * o.V * s.Va * s.G / o.m;
-        acc.add((s.r * Ps - via * (2.f * o.gam)) * w);
-    }
-    const float3 acl = acc.sum() + d.g;
+    const float3 sum = make_float3(groupSum<L>(acc.x), groupSum<L>(acc.y), groupSum<L>(acc.z));
+    if (!live || lane != 0) return;
+    const float3 acl = sum + d.g;
     d.facc[i] = f4(acl);
     // kick: v += a dt_f
     const float4 vh0 = d.fvh[0][i], vl0 = d.fvl[0][i];
@@ -256,43 +295,50 @@ __device__ __forceinline__ dfl shepardTerm(dfl r, dfl invh)
     return df_mul(df_mul(t2, t2), df_add_f(df_mul_f(q, 2.0f), 1.0f));
 }
 
+template <int L>
 __global__ void __launch_bounds__(T) kDensityReinit(DeviceState d, int storeReference)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.nf || *d.status) return;
-    const int4 ci = d.fcell[i];
-    const float4 pi = d.fph[0][i], li = d.fpl[0][i];
-    const dfl h = df_make(pi.w, li.w);
-    const dfl invh = df_div(df_make(1.f), h);
-    const dfl twoH = df_add(h, h);
-    const int n = d.nf;
-    dfl S = df_make(1.f);
-    const int nff = min(d.ffc[i], d.kff);
-    for (int k = 0; k < nff; ++k) {
-        const unsigned e = d.ff[(size_t)k * n + i];
-        const int j = (int)(e >> 5);
-        const unsigned code = e & 31u;
-        int4 cj;
-        if (code < 27u)
-            cj = make_int4(ci.x + (int)(code % 3u) - 1, ci.y + (int)((code / 3u) % 3u) - 1, ci.z + (int)(code / 9u) - 1, 0);
-        else
-            cj = d.fcell[j];
-        const dfl r = dfNorm(relDF(ci, pi, li, cj, d.fph[0][j], d.fpl[0][j], d.grid));
-        if (df_ge0(df_sub(r, twoH))) continue;  // q >= 2
-        S = df_add(S, shepardTerm(r, invh));
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((t & ~31) >= d.nf * L || *d.status) return;
+    const int i = t / L, lane = t % L;
+    const bool live = i < d.nf;
+    dfl S = df_make(lane == 0 ? 1.f : 0.f);
+    if (live) {
+        const int4 ci = d.fcell[i];
+        const float4 pi = d.fph[0][i], li = d.fpl[0][i];
+        const dfl h = df_make(pi.w, li.w);
+        const dfl invh = df_div(df_make(1.f), h);
+        const dfl twoH = df_add(h, h);
+        const int n = d.nf;
+        const int nff = min(d.ffc[i], d.kff);
+        for (int k = lane; k < nff; k += L) {
+            const unsigned e = d.ff[(size_t)k * n + i];
+            const int j = ffPartner(e);
+            const unsigned code = (unsigned)entryWalk(e);
+            int4 cj;
+            if (ffRegular(e))
+                cj = make_int4(ci.x + (int)(code % 3u) - 1, ci.y + (int)((code / 3u) % 3u) - 1, ci.z + (int)(code / 9u) - 1, 0);
+            else
+                cj = d.fcell[j];
+            const dfl r = dfNorm(relDF(ci, pi, li, cj, d.fph[0][j], d.fpl[0][j], d.grid));
+            if (df_ge0(df_sub(r, twoH))) continue;  // q >= 2
+            S = df_add(S, shepardTerm(r, invh));
+        }
+        // V0_a / V0_i = (2 r_a / (h_i / 1.3))^3 = (2.6 r_a / h_i)^3
+        const dfl k26 = df_from_double(2.6);
+        const int nfs = min(d.fsc[i], d.kfs);
+        for (int k = lane; k < nfs; k += L) {
+            const int a = fsPartner(d.fs[(size_t)k * n + i]);
+            const dfl r = dfNorm(relDF(ci, pi, li, d.scell[a], d.sph[a], d.spl[a], d.grid));
+            if (df_ge0(df_sub(r, twoH))) continue;
+            const float4 ra = d.srad[a];
+            const dfl x = df_mul(df_mul(k26, df_make(ra.x, ra.y)), invh);
+            const dfl vr = df_mul(df_mul(x, x), x);
+            S = df_add(S, df_mul(shepardTerm(r, invh), vr));
+        }
     }
-    // V0_a / V0_i = (2 r_a / (h_i / 1.3))^3 = (2.6 r_a / h_i)^3
-    const dfl k26 = df_from_double(2.6);
-    const int nfs = min(d.fsc[i], d.kfs);
-    for (int k = 0; k < nfs; ++k) {
-        const int a = d.fs[(size_t)k * n + i];
-        const dfl r = dfNorm(relDF(ci, pi, li, d.scell[a], d.sph[a], d.spl[a], d.grid));
-        if (df_ge0(df_sub(r, twoH))) continue;
-        const float4 ra = d.srad[a];
-        const dfl x = df_mul(df_mul(k26, df_make(ra.x, ra.y)), invh);
-        const dfl vr = df_mul(df_mul(x, x), x);
-        S = df_add(S, df_mul(shepardTerm(r, invh), vr));
-    }
+    S = groupSum<L>(S);
+    if (!live || lane != 0) return;
     if (storeReference) {
         d.fsumW0[i] = make_float2(S.hi, S.lo);
     } else {
@@ -342,7 +388,7 @@ __global__ void kCouplingPairs(DeviceState d, int src, float4* out)
     const int m = min(d.fsc[i], d.kfs);
     for (int k = 0; k < m; ++k) {
         bool inside;
-        const float3 f = couplingPairForce(d, src, i, d.fs[(size_t)k * d.nf + i], inside);
+        const float3 f = couplingPairForce(d, src, i, fsPartner(d.fs[(size_t)k * d.nf + i]), inside);
         out[(size_t)k * d.nf + i] = f4(f);
     }
 }
@@ -352,7 +398,14 @@ __global__ void kCouplingPairs(DeviceState d, int src, float4* out)
 void launchDensityReinit(const DeviceState& d, int iStep, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    ++t_kernelLaunches, kDensityReinit<<<blocksFor(d.nf, T), T, 0, s>>>(d, iStep == 1 ? 1 : 0);
+    LAUNCH_LANES(kDensityReinit, d.lanes, d.nf, T, s, d, iStep == 1 ? 1 : 0);
+}
+
+int fluidLanes(int nf)
+{
+    int L = 1;
+    while (L < 8 && (long long)nf * L < 152LL * 2048) L *= 2;
+    return L;
 }
 
 void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStream_t s)
@@ -366,13 +419,13 @@ void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStrea
     } else {           // second half step: densities 1 -> 0, velocity 1 -> 0
         a.ps = 0; a.vs = 1; a.ds = 1; a.dd = 0; a.driftTo = -1; a.velCopyTo = 0;
     }
-    ++t_kernelLaunches, kContinuity<<<blocksFor(d.nf, T), T, 0, s>>>(d, a);
+    LAUNCH_LANES(kContinuity, d.lanes, d.nf, T, s, d, a);
 }
 
 void launchMomentumPass(const DeviceState& d, double dtf, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    ++t_kernelLaunches, kMomentum<<<blocksFor(d.nf, T), T, 0, s>>>(d, df_from_double(dtf), df_from_double(0.5 * dtf));
+    LAUNCH_LANES(kMomentum, d.lanes, d.nf, T, s, d, df_from_double(dtf), df_from_double(0.5 * dtf));
 }
 
 void launchCoupling(const DeviceState& d, int src, cudaStream_t s)

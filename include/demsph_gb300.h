@@ -144,6 +144,8 @@ typedef struct demsph_options {
     double solid_verlet_skin;    /* margin (m) of the solid contact candidates, rebuilt once a solid has
                                     moved half of it; 0 = 0.2 x the smallest solid radius; < 0 = no
                                     candidates: the reference's 27-cell walk every step */
+    int fluid_lanes;             /* threads per fluid particle in the fluid list and pair loops (1, 2, 4
+                                    or 8); 0 = chosen from the particle count */
 } demsph_options;
 
 typedef struct demsph_counts {
@@ -288,6 +290,22 @@ DEMSPH_API int demsph_export_solid_pairs(demsph_engine* e, int* prefix, int* poi
 DEMSPH_API int demsph_export_bonds(demsph_engine* e, int* pointed, int* pointing, int* is_bonded, double* normal_force,
                         double* torsion_torque, double* shear_force, double* bending_torque,
                         double* contact_normal, double* contact_point, long long capacity);
+/* Conservation audit, summed in FP64 on the GPU: mass, linear momentum,
+   translational kinetic energy, rotational kinetic energy of spheres (clumps
+   as rigid bodies, translation only), potential energy -m g.x (x from the
+   domain origin) and the sum of fluid densities.  Fluids, solids with mass
+   and clumps; dummy and fixed particles carry none.  No counterpart in the
+   reference. */
+typedef struct demsph_audit_values {
+    double mass;
+    double momentum[3];
+    double kinetic_energy;
+    double rotational_energy;
+    double potential_energy;
+    double fluid_density_sum;
+} demsph_audit_values;
+DEMSPH_API int demsph_audit(demsph_engine* e, demsph_audit_values* out);
+
 /* Shepard reference sums sumW0 (core/integrate.cu:44-47). */
 DEMSPH_API int demsph_export_fluid_sumw0(demsph_engine* e, double* sumw0);
 

@@ -76,12 +76,17 @@ def test_one_step_within_force_tolerance(ds, scenes, name):
     _check_step(eng, orc, sc, _spacing(recipe), 1, dt, FORCE_TOL, POS_TOL)
 
 
-@pytest.mark.parametrize("skin", SKINS)
+# (solid candidate margin, threads per fluid particle): the default, the margin
+# variants, and one thread per fluid particle (what large scenes use)
+VARIANTS = [(s, 0) for s in SKINS] + [(0.0, 1)]
+
+
+@pytest.mark.parametrize("skin,lanes", VARIANTS)
 @pytest.mark.parametrize("name", SCENES)
-def test_ten_steps_artefacts_equal_drift_bounded(ds, scenes, name, skin):
+def test_ten_steps_artefacts_equal_drift_bounded(ds, scenes, name, skin, lanes):
     """Ten update() calls through the five stage calls: integer artefacts equal
     after every step; floating-point drift within DRIFT_TOL."""
-    recipe, b, sc, eng, orc = _setup(ds, scenes, name, solid_verlet_skin=skin)
+    recipe, b, sc, eng, orc = _setup(ds, scenes, name, solid_verlet_skin=skin, fluid_lanes=lanes)
     eng.initialize()
     orc.initialize()
     dt, gap = sc.time_step, sc.fluid_integrate_gap
@@ -183,3 +188,54 @@ def test_drift_bounded_over_run(ds, scenes):
     assert err["fluid.pos"] < 1e-7, err
     assert err["solid.pos"] < 1e-7, err
     assert err["fluid.dRho"] < 1e-5, err
+
+
+@pytest.mark.parametrize("name", ("tiny_coupled", "tiny_granular"))
+def test_audit_matches_the_state(ds, scenes, name):
+    """demsph_audit's FP64 sums on the GPU equal the same sums formed on the
+    host from the downloaded state and the scene's masses."""
+    recipe, b, sc, eng, _ = _setup(ds, scenes, name)
+    eng.initialize()
+    eng.update(sc.time_step, 1, 20, sc.fluid_integrate_gap)
+    a = eng.audit()
+    arr = lambda p, n, w=1: np.ctypeslib.as_array(p, shape=(n * w,)).reshape(n, w) if w > 1 else \
+        np.ctypeslib.as_array(p, shape=(n,))
+    o = np.array(sc.domain_origin[:])
+    g = np.array(sc.gravity[:])
+    mass = px = ke = rot = pe = rho = 0.0
+    px = np.zeros(3)
+    if sc.n_fluid:
+        pos, vel, _, drho = eng.download_fluids()
+        m = (arr(sc.fluid_smoothing_length, sc.n_fluid) / 1.3) ** 3 * arr(sc.fluid_rho0, sc.n_fluid)
+        mass += m.sum()
+        px += (m[:, None] * vel).sum(0)
+        ke += 0.5 * (m * (vel * vel).sum(1)).sum()
+        pe -= (m * ((pos - o) @ g)).sum()
+        rho += (arr(sc.fluid_rho0, sc.n_fluid) + drho).sum()
+    s = eng.download_solids()
+    im = arr(sc.solid_inverse_mass, sc.n_solid)
+    clump = arr(sc.solid_clump, sc.n_solid)
+    free = (im > 0) & (clump < 0)
+    m = 1.0 / im[free]
+    mass += m.sum()
+    px += (m[:, None] * s["vel"][free]).sum(0)
+    ke += 0.5 * (m * (s["vel"][free] ** 2).sum(1)).sum()
+    r = arr(sc.solid_radius, sc.n_solid)[free]
+    rot += (0.5 * 0.4 * m * r * r * (s["angvel"][free] ** 2).sum(1)).sum()
+    pe -= (m * ((s["pos"][free] - o) @ g)).sum()
+    if sc.n_clump:
+        c = eng.download_clumps()
+        cim = arr(sc.clump_inverse_mass, sc.n_clump)
+        cm = 1.0 / cim[cim > 0]
+        mass += cm.sum()
+        px += (cm[:, None] * c["vel"][cim > 0]).sum(0)
+        ke += 0.5 * (cm * (c["vel"][cim > 0] ** 2).sum(1)).sum()
+        pe -= (cm * ((c["centroid"][cim > 0] - o) @ g)).sum()
+    rel = lambda x, y: abs(x - y) / max(abs(y), 1e-30)
+    assert rel(a["mass"], mass) < 1e-7  # fluid masses are stored in FP32
+    assert np.allclose(a["momentum"], px, rtol=1e-6, atol=1e-12 * mass)
+    assert rel(a["kinetic_energy"], ke) < 1e-6
+    assert rel(a["rotational_energy"], rot) < 1e-6 or rot == 0.0
+    assert rel(a["potential_energy"], pe) < 1e-6
+    if sc.n_fluid:
+        assert rel(a["fluid_density_sum"], rho) < 1e-7
