@@ -65,7 +65,7 @@ class Options(C.Structure):
 
     _fields_ = [("device", _I), ("fluid_neighbors_max", _I), ("fluid_solids_max", _I),
                 ("solid_contacts_per_particle", _I), ("fixes", _I), ("debug", _I), ("solid_verlet_skin", _D),
-                ("fluid_lanes", _I)]
+                ("fluid_lanes", _I), ("fluid_verlet_skin", _D)]
 
 
 class Counts(C.Structure):
@@ -259,13 +259,13 @@ class Engine:
     """One scene on one GPU (the C ABI engine)."""
 
     def __init__(self, scene, device=0, fluid_neighbors_max=0, fluid_solids_max=0, solid_contacts_per_particle=0,
-                 fixes=0, debug=0, solid_verlet_skin=0.0, fluid_lanes=0):
+                 fixes=0, debug=0, solid_verlet_skin=0.0, fluid_lanes=0, fluid_verlet_skin=0.0):
         """``solid_verlet_skin``: margin (m) of the solid contact candidates
         (0 = 0.2 x the smallest solid radius, < 0 = the 27-cell walk every step)."""
         self.lib = load_library()
         self.scene = scene
         opts = Options(device, fluid_neighbors_max, fluid_solids_max, solid_contacts_per_particle, fixes, debug,
-                       float(solid_verlet_skin), int(fluid_lanes))
+                       float(solid_verlet_skin), int(fluid_lanes), float(fluid_verlet_skin))
         h = _P()
         rc = self.lib.demsph_create(C.byref(scene), C.byref(opts), C.byref(h))
         self.h = h
@@ -469,7 +469,8 @@ def estimate_bytes(scene, **opts):
     lib = load_library()
     o = Options(0, opts.get("fluid_neighbors_max", 0), opts.get("fluid_solids_max", 0),
                 opts.get("solid_contacts_per_particle", 0), opts.get("fixes", 0), opts.get("debug", 0),
-                float(opts.get("solid_verlet_skin", 0.0)), int(opts.get("fluid_lanes", 0)))
+                float(opts.get("solid_verlet_skin", 0.0)), int(opts.get("fluid_lanes", 0)),
+                float(opts.get("fluid_verlet_skin", 0.0)))
     return int(lib.demsph_estimate_bytes(C.byref(scene), C.byref(o)))
 
 
@@ -502,7 +503,8 @@ class Server:
     def submit(self, scene, n_steps, **opts):
         o = Options(0, opts.get("fluid_neighbors_max", 0), opts.get("fluid_solids_max", 0),
                     opts.get("solid_contacts_per_particle", 0), opts.get("fixes", 0), opts.get("debug", 0),
-                    float(opts.get("solid_verlet_skin", 0.0)), int(opts.get("fluid_lanes", 0)))
+                    float(opts.get("solid_verlet_skin", 0.0)), int(opts.get("fluid_lanes", 0)),
+                float(opts.get("fluid_verlet_skin", 0.0)))
         rid = C.c_longlong()
         rc = self.lib.demsph_server_submit(self.h, C.byref(scene), C.byref(o), _I(n_steps), C.byref(rid))
         if rc != DEMSPH_OK:

@@ -526,6 +526,13 @@ __device__ __forceinline__ void checkDisplacement(const DeviceState& d, int i)
                 dz = (float)c.z * d.grid.cs.z + h.z - p0.z;
     const float half = 0.5f * d.skin;
     if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)d.rebuild = 1;
+    if (d.nf > 0) {  // the fluid candidates' solid partners
+        const float4 q0 = d.svref[r];
+        const float ex = (float)c.x * d.grid.cs.x + h.x - q0.x, ey = (float)c.y * d.grid.cs.y + h.y - q0.y,
+                    ez = (float)c.z * d.grid.cs.z + h.z - q0.z;
+        const float fh = 0.5f * d.fskin;
+        if (!(ex * ex + ey * ey + ez * ez <= fh * fh)) *(volatile int*)d.frebuild = 1;
+    }
 }
 
 __global__ void kSolidIntegrate(DeviceState d, dfl half, int before)

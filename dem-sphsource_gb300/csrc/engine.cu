@@ -139,6 +139,13 @@ void allocFluidLists(demsph_engine* e)
     if (e->debug & 1) d.fsPairForce = dalloc<float4>((size_t)d.kfs * d.nf, e->owned, e->stream);
 }
 
+void allocFluidCandidates(demsph_engine* e)
+{
+    DeviceState& d = e->d;
+    d.fvc = dalloc<unsigned>((size_t)d.kvf * d.nf, e->owned, e->stream, false);
+    d.fvsc = dalloc<int>((size_t)d.kvs * d.nf, e->owned, e->stream, false);
+}
+
 // Per-slot arrays of the contact rows (scap slots per row).
 void allocContactLists(demsph_engine* e)
 {
@@ -183,20 +190,20 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
     const bool fluidStep = d.nf > 0 && (iStep % gap == 0);
     if (fluidStep) {
         TIMED("fluid_hash_reorder");
-        launchFluidHashReorder(d, s);
+        launchFluidHashReorder(d, e->forceWalk, s);
     }
     // solids that never move (walls of dummy particles, fixed spheres) are
     // hashed and sorted once, and again only after their positions are uploaded
     const bool solidsMove = e->nMassive > 0 || e->solidSortStale;
     if (solidsMove || e->forceWalk) {
         TIMED("solid_hash_sort");
-        launchSolidHashSort(d, (fluidStep && solidsMove) || e->forceWalk || e->solidSortStale, s);
+        launchSolidHashSort(d, e->forceWalk || e->solidSortStale, fluidStep, s);
         e->solidSortStale = false;
     }
     if (fluidStep) {
         {
             TIMED("fluid_lists");
-            launchFluidLists(d, s);
+            launchFluidLists(d, e->forceWalk, s);
         }
         if (e->nMassive > 0) {  // the coupling force moves only solids with mass
             TIMED("coupling_lists");
@@ -332,6 +339,20 @@ void grow(demsph_engine* e, int status)
             CK(cudaMemsetAsync(d.rebuild, 0xff, sizeof(int), e->stream));  // rebuild on the retry
         }
     }
+    if (status & ST_FVERLET_OVERFLOW) {
+        int need[4] = {0, 0, 0, 0};
+        CK(cudaMemcpyAsync(need, d.need, sizeof(int) * 4, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        CK(cudaMemsetAsync(d.need + 2, 0, sizeof(int) * 2, e->stream));
+        void* p = d.fvc;
+        freeOne(e, p);
+        p = d.fvsc;
+        freeOne(e, p);
+        d.kvf = std::max(d.kvf, need[2] + need[2] / 2 + 1);
+        d.kvs = std::max(d.kvs, need[3] + need[3] / 2 + 1);
+        allocFluidCandidates(e);
+        CK(cudaMemsetAsync(d.frebuild, 0xff, sizeof(int), e->stream));  // rebuild on the retry
+    }
     if (status & ST_COUPLE_OVERFLOW) {
         int need = 0;
         CK(cudaMemcpyAsync(&need, d.coupStart + d.ns, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
@@ -349,8 +370,8 @@ void grow(demsph_engine* e, int status)
     dropGraph(e);
 }
 
-constexpr int ALL_OVERFLOWS =
-    ST_FF_OVERFLOW | ST_FS_OVERFLOW | ST_SS_OVERFLOW | ST_COUPLE_OVERFLOW | ST_VERLET_OVERFLOW | ST_MODE_CHANGE;
+constexpr int ALL_OVERFLOWS = ST_FF_OVERFLOW | ST_FS_OVERFLOW | ST_SS_OVERFLOW | ST_COUPLE_OVERFLOW |
+                              ST_VERLET_OVERFLOW | ST_MODE_CHANGE | ST_FVERLET_OVERFLOW;
 
 // Neighbour search of the staged API: synchronises once, grows and retries.
 int neighborSearchChecked(demsph_engine* e, int iStep, int gap)
@@ -536,6 +557,23 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.ffc = dalloc<int>(nf, e->owned, e->stream);
             d.fsc = dalloc<int>(nf, e->owned, e->stream);
             allocFluidLists(e);
+            // Verlet candidates of the fluid lists
+            d.kvf = d.kff + d.kff / 2;
+            d.kvs = d.kfs + d.kfs / 2;
+            d.fvcn = dalloc<int>(nf, e->owned, e->stream);
+            d.fvsn = dalloc<int>(nf, e->owned, e->stream);
+            d.fvref = dalloc<float4>(nf, e->owned, e->stream);
+            allocFluidCandidates(e);
+            d.fhmax = (float)mf;
+            d.fskin = (float)(o.fluid_verlet_skin > 0 ? o.fluid_verlet_skin : 0.2 * mf);
+            d.frebuild = dalloc<int>(1, e->owned, e->stream);
+            d.fslowMode = dalloc<int>(1, e->owned, e->stream);
+            {
+                const int one = 1;
+                const bool walkOnly = o.fluid_verlet_skin < 0 || d.grid.gx < 3 || d.grid.gy < 3 || d.grid.gz < 3;
+                CK(cudaMemcpyAsync(d.frebuild, &one, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+                if (walkOnly) CK(cudaMemcpyAsync(d.fslowMode, &one, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+            }
             if (nf > 0) {
                 CK(cudaMemcpyAsync(d.fcell, cell.data(), sizeof(int4) * nf, cudaMemcpyHostToDevice, e->stream));
                 CK(cudaMemcpyAsync(d.fph[0], ph.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice, e->stream));
@@ -631,9 +669,10 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.vcand = dalloc<int>((size_t)d.vcap * nr, e->owned, e->stream, false);
             d.vcnt = dalloc<int>(nr, e->owned, e->stream);
             d.vref = dalloc<float4>(nr, e->owned, e->stream);
+            d.svref = dalloc<float4>(nr, e->owned, e->stream);
             d.rebuild = dalloc<int>(1, e->owned, e->stream);
             d.slowMode = dalloc<int>(1, e->owned, e->stream);
-            d.need = dalloc<int>(2, e->owned, e->stream);
+            d.need = dalloc<int>(4, e->owned, e->stream);
             const int one = 1;
             const bool walkOnly = o.solid_verlet_skin < 0 || d.grid.gx < 3 || d.grid.gy < 3 || d.grid.gz < 3;
             CK(cudaMemcpyAsync(d.rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, e->stream));
@@ -1033,11 +1072,12 @@ long long demsph_estimate_bytes(const demsph_scene* sc, const demsph_options* op
     long long rows = 0;
     for (int i = 0; i < sc->n_solid; ++i) rows += sc->solid_is_dummy[i] != 1;
     const long long nf = sc->n_fluid, ns = sc->n_solid;
-    // per fluid particle: state, reorder buffers and both neighbour lists; per
+    // per fluid particle: state, reorder buffers, both neighbour lists and their candidates; per
     // solid: state, sort and wall springs; per contact row: its slots, two
     // list parities, springs in and out, candidates; per cell: counts and starts
-    return nf * (292 + 4 * (kff + kfs)) + ns * (248 + 48LL * sc->n_wall) +
-           rows * (56 + slots * 136 + 2 * slots * 4) + (cells + 1) * 16 + (long long)sc->n_clump * 160 +
+    const long long kvf = kff + kff / 2, kvs = kfs + kfs / 2;
+    return nf * (316 + 4 * (kff + kfs) + 4 * (kvf + kvs)) + ns * (248 + 48LL * sc->n_wall) +
+           rows * (72 + slots * 136 + 2 * slots * 4) + (cells + 1) * 16 + (long long)sc->n_clump * 160 +
            std::min(64 * rows + 1024, std::max(1LL, kfs * nf)) * 4 + (1 << 20);
 }
 

@@ -23,7 +23,8 @@ enum StatusBits : int {
     ST_SS_OVERFLOW = 4,      // a solid has more contacts (forward or reverse) than its row holds
     ST_COUPLE_OVERFLOW = 8,  // fluid-solid coupling reverse list over capacity
     ST_VERLET_OVERFLOW = 16, // a solid has more contact candidates than its row holds
-    ST_MODE_CHANGE = 32,     // a solid left the domain: lists switch to the 27-cell walk; redo the step
+    ST_MODE_CHANGE = 32,     // a particle left the domain: lists switch to the 27-cell walk; redo the step
+    ST_FVERLET_OVERFLOW = 64,// a fluid particle has more list candidates than it holds
 };
 
 // Neighbour list entries.  A fluid partner entry holds the partner's slot j,

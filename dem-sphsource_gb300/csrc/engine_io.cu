@@ -329,6 +329,7 @@ int demsph_upload_fluids(demsph_engine* e, const double* pos, const double* vel,
     if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, e->stream));
     if (dr) CK(cudaMemcpyAsync(dr, drho, sizeof(double) * d.nf, cudaMemcpyHostToDevice, e->stream));
     ++t_kernelLaunches, kFluidIn<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, dp, dv, dr);
+    if (dp) CK(cudaMemsetAsync(d.frebuild, 0xff, sizeof(int), e->stream));  // list candidates from the new positions
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)
@@ -349,6 +350,7 @@ int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel,
     ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw);
     if (dp) {
         CK(cudaMemsetAsync(d.rebuild, 0xff, sizeof(int), e->stream));  // candidates from the new positions
+        if (d.nf > 0) CK(cudaMemsetAsync(d.frebuild, 0xff, sizeof(int), e->stream));
         e->solidSortStale = true;
     }
     CK(cudaStreamSynchronize(e->stream));
@@ -465,14 +467,21 @@ int demsph_export_cell_hash(demsph_engine* e, int which, int* value, int* index,
     const int n = which == 0 ? d.nf : d.ns;
     std::vector<int> cs;
     if (which == 0) {
-        d2h(cs, d.fcellStart, (size_t)d.grid.num + 1);
+        // fluids are reordered by cell only when their list candidates are
+        // rebuilt: the (key, index) order of this step is restored here
         std::vector<int4> cell;
         std::vector<int> id;
         d2h(cell, d.fcell, n);
         d2h(id, d.fid, n);
+        std::vector<std::pair<int, int>> kv(n);
+        for (int s = 0; s < n; ++s) kv[s] = {cell[s].w, id[s]};
+        std::sort(kv.begin(), kv.end());
+        cs.assign((size_t)d.grid.num + 1, 0);
+        for (int s = 0; s < n; ++s) cs[kv[s].first + 1]++;
+        for (int k = 0; k < d.grid.num; ++k) cs[k + 1] += cs[k];
         for (int s = 0; s < n; ++s) {
-            if (value) value[s] = cell[s].w;
-            if (index) index[s] = id[s];
+            if (value) value[s] = kv[s].first;
+            if (index) index[s] = kv[s].second;
         }
     } else {
         // the solids' keys are computed every step, their device-side sort only
@@ -514,8 +523,8 @@ int demsph_export_fluid_pairs(demsph_engine* e, int* prefix, int* pointed, int* 
     d2h(id, d.fid, n);
     slot.resize(n);
     for (int s = 0; s < n; ++s) slot[id[s]] = s;
-    // the reference's order: by walk position, then by sorted position in the
-    // cell (the slot: fluids are stored in (cell, index) order)
+    // the reference's order: by walk position, then by index (its stable
+    // (cell, index) sort)
     long long w = 0;
     std::vector<std::pair<long long, int>> order;
     for (int i = 0; i < n; ++i) {
@@ -524,7 +533,7 @@ int demsph_export_fluid_pairs(demsph_engine* e, int* prefix, int* pointed, int* 
         order.clear();
         for (int k = 0; k < m; ++k) {
             const unsigned v = ff[(size_t)k * n + s];
-            order.push_back({(long long)entryWalk(v) * n + ffPartner(v), ffPartner(v)});
+            order.push_back({(long long)entryWalk(v) * n + id[ffPartner(v)], ffPartner(v)});
         }
         std::sort(order.begin(), order.end());
         for (const auto& o : order) {

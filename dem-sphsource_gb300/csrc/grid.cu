@@ -22,7 +22,16 @@ namespace {
 
 constexpr int T = 256;
 
-__global__ void kFluidHash(DeviceState d)
+__global__ void kFluidClearCounts(DeviceState d, RunIf when)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.grid.num || *d.status || !when.active()) return;
+    d.fcellCount[k] = 0;
+}
+
+// Cell keys of the fluids every fluid step; on reorder steps the whole
+// particle is copied into the gather sources and takes a slot in its cell.
+__global__ void kFluidHash(DeviceState d, RunIf sortNow)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.nf || *d.status) return;
@@ -34,6 +43,18 @@ __global__ void kFluidHash(DeviceState d)
     renormAxis(c.z, h.z, l.z, d.grid.csz);
     const int key = cellKey(c.x, c.y, c.z, d.grid);
     c.w = key;
+    if (key == d.grid.num - 1 && !*d.fslowMode) {
+        // a fluid particle left the domain: from now on its lists come from the
+        // reference's walk (which reaches it through the overflow cell); redo the step
+        *(volatile int*)d.fslowMode = 1;
+        atomicOr(d.status, ST_MODE_CHANGE);
+    }
+    if (!sortNow.active()) {
+        d.fcell[i] = c;
+        d.fph[0][i] = h;
+        d.fpl[0][i] = l;
+        return;
+    }
     // copy the whole particle into the gather sources
     d.tcell[i] = c;
     d.fph[1][i] = h;
@@ -74,10 +95,10 @@ __device__ __forceinline__ int stableRank(int p, const int* __restrict__ sorted,
     return s + rank;
 }
 
-__global__ void kFluidGather(DeviceState d)
+__global__ void kFluidGather(DeviceState d, RunIf when)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.nf || *d.status) return;
+    if (p >= d.nf || *d.status || !when.active()) return;
     int e;
     const int q = stableRank(p, d.fsortTmp, d.fkey, d.fcellStart, d.tid, e);
     d.fcell[q] = d.tcell[e];
@@ -136,17 +157,21 @@ __global__ void kSolidRank(DeviceState d, RunIf when)
 
 }  // namespace
 
-void launchFluidHashReorder(const DeviceState& d, cudaStream_t s)
+void launchFluidHashReorder(const DeviceState& d, bool force, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    cudaMemsetAsync(d.fcellCount, 0, sizeof(int) * d.grid.num, s);
-    ++t_kernelLaunches, kFluidHash<<<blocksFor(d.nf, T), T, 0, s>>>(d);
-    scanExclusive(d.fcellCount, d.fcellStart, d.grid.num, d.scanWork, s);
-    ++t_kernelLaunches, kScatter<<<blocksFor(d.nf, T), T, 0, s>>>(d.nf, d.fkey, d.fslotInCell, d.fcellStart, d.fsortTmp, d.status, RunIf{});
-    ++t_kernelLaunches, kFluidGather<<<blocksFor(d.nf, T), T, 0, s>>>(d);
+    RunIf when;
+    when.always = force ? 1 : 0;
+    when.a = d.frebuild;
+    when.b = d.fslowMode;
+    ++t_kernelLaunches, kFluidClearCounts<<<blocksFor(d.grid.num, T), T, 0, s>>>(d, when);
+    ++t_kernelLaunches, kFluidHash<<<blocksFor(d.nf, T), T, 0, s>>>(d, when);
+    scanExclusive(d.fcellCount, d.fcellStart, d.grid.num, d.scanWork, s, when);
+    ++t_kernelLaunches, kScatter<<<blocksFor(d.nf, T), T, 0, s>>>(d.nf, d.fkey, d.fslotInCell, d.fcellStart, d.fsortTmp, d.status, when);
+    ++t_kernelLaunches, kFluidGather<<<blocksFor(d.nf, T), T, 0, s>>>(d, when);
 }
 
-void launchSolidHashSort(const DeviceState& d, bool force, cudaStream_t s)
+void launchSolidHashSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s)
 {
     if (d.ns <= 0) return;
     // scellCount is zero here: cleared at creation, by kSolidRank after every
@@ -155,6 +180,10 @@ void launchSolidHashSort(const DeviceState& d, bool force, cudaStream_t s)
     when.always = force ? 1 : 0;
     when.a = d.rebuild;
     when.b = d.slowMode;
+    if (fluidStep) {
+        when.c = d.frebuild;
+        when.e = d.fslowMode;
+    }
     ++t_kernelLaunches, kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d, when);
     scanExclusive(d.scellCount, d.scellStart, d.grid.num, d.scanWork, s, when);
     ++t_kernelLaunches, kScatter<<<blocksFor(d.ns, T), T, 0, s>>>(d.ns, d.skey, d.sslotInCell, d.scellStart, d.ssortTmp, d.status, when);

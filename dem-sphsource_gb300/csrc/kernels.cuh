@@ -48,6 +48,19 @@ struct DeviceState {
     int* fsortTmp;
     int* fcellCount;         // grid.num
     int* fcellStart;         // grid.num + 1
+    // Verlet candidates of the fluid lists (slots as of the last reorder):
+    // partners within the list cut + fskin at the last rebuild
+    int kvf, kvs;            // fluid / solid candidates per fluid particle
+    unsigned* fvc;           // [k * nf + i]
+    int* fvcn;
+    int* fvsc;               // [k * nf + i] solid indices
+    int* fvsn;
+    float4* fvref;           // per fluid slot: position (from the grid origin) at the rebuild
+    float4* svref;           // per solid row: the same
+    float fskin;
+    float fhmax;             // largest fluid smoothing length
+    int* frebuild;           // 1: fluid candidates are stale (a fluid or solid moved fskin / 2)
+    int* fslowMode;          // 1: fluid lists from the 27-cell walk every fluid step
     // lists (column-major, stride nf)
     unsigned* ff;
     int* ffc;
@@ -110,7 +123,8 @@ struct DeviceState {
     float vmaxEff;           // largest effective radius of a non-dummy solid
     int* rebuild;            // 1: candidates are stale; set by the hash, cleared by a completed step
     int* slowMode;           // 1: lists come from the 27-cell walk every step (grid too small, or a solid left the domain)
-    int* need;               // [0] most contacts of a row, [1] most candidates of a row (for growing)
+    int* need;               // [0] most contacts of a row, [1] most candidates of a row,
+                             // [2] / [3] most fluid / solid candidates of a fluid particle (for growing)
 
     // ---- infinite walls ----
     int nw;
@@ -168,7 +182,15 @@ struct RunIf {
     int always = 1;
     const int* a = nullptr;
     const int* b = nullptr;
-    __device__ __forceinline__ bool active() const { return always || (a && *a) || (b && *b); }
+    const int* c = nullptr;
+    const int* e = nullptr;
+    const int* unless = nullptr;  // when set and non-zero, the kernel does nothing
+    const int* unless2 = nullptr;
+    __device__ __forceinline__ bool active() const
+    {
+        if ((unless && *unless) || (unless2 && *unless2)) return false;
+        return always || (a && *a) || (b && *b) || (c && *c) || (e && *e);
+    }
 };
 
 // Lanes per fluid particle in the fluid pair loops and list builder: enough
@@ -194,13 +216,18 @@ size_t scanWorkspaceInts(int n);
 void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s, RunIf when = RunIf{});
 
 // grid.cu
-void launchFluidHashReorder(const DeviceState& d, cudaStream_t s);
+// Fluid cell keys every fluid step; the reorder by cell only when the fluid
+// candidates are rebuilt (or the lists come from the walk).
+void launchFluidHashReorder(const DeviceState& d, bool force, cudaStream_t s);
 // Solid cell keys every step; the sort by cell only when `force`, when the
-// contact candidates are stale or when lists come from the 27-cell walk.
-void launchSolidHashSort(const DeviceState& d, bool force, cudaStream_t s);
+// contact candidates are stale, when lists come from the 27-cell walk, or -
+// on fluid steps (fluidStep) - when the fluid lists walk the cells.
+void launchSolidHashSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s);
 
 // lists.cu
-void launchFluidLists(const DeviceState& d, cudaStream_t s);
+// Fluid lists of a fluid step: from Verlet candidates (rebuilt when stale),
+// or from the reference's walk (walk = true, or once a particle has left the domain).
+void launchFluidLists(const DeviceState& d, bool walk, cudaStream_t s);
 void launchCouplingLists(const DeviceState& d, cudaStream_t s);
 // forceWalk: build from the reference's 27-cell walk (list in the reference's order)
 void launchSolidContactList(const DeviceState& d, int parity, bool forceWalk, cudaStream_t s);

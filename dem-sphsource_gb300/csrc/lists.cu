@@ -106,17 +106,66 @@ __device__ __forceinline__ bool nextCandidate(LaneWalk& w, const int* __restrict
     return true;
 }
 
+// Next cell member in lane's share of a box of cells (x0..x1, y0..y1, z0..z1,
+// all inside the domain), cells taken round-robin by the lanes.
+struct LaneBox {
+    int u, p, pe, x0, y0, z0, nx, ny, nz, hx, hy, hz, hash;
+};
 template <int L>
-__global__ void __launch_bounds__(T) kFluidLists(DeviceState d)
+__device__ __forceinline__ bool nextBoxMember(LaneBox& b, const int* __restrict__ start, const GridDev& g, int& idx)
+{
+    while (b.p >= b.pe) {
+        b.u += L;
+        if (b.u >= b.nx * b.ny * b.nz) return false;
+        b.hx = b.x0 + b.u % b.nx;
+        b.hy = b.y0 + (b.u / b.nx) % b.ny;
+        b.hz = b.z0 + b.u / (b.nx * b.ny);
+        b.hash = (b.hz * g.gy + b.hy) * g.gx + b.hx;
+        b.p = start[b.hash];
+        b.pe = start[b.hash + 1];
+    }
+    idx = b.p++;
+    return true;
+}
+
+// The cells within `reach` of a particle at cell c, offset h (clamped to the domain).
+__device__ __forceinline__ LaneBox boxAround(int lane, int L, int4 c, float4 h, float reach, const GridDev& g)
+{
+    LaneBox b;
+    b.u = lane - L;
+    b.p = b.pe = 0;
+    b.x0 = max(0, c.x + (int)floorf((h.x - reach) / g.cs.x));
+    b.y0 = max(0, c.y + (int)floorf((h.y - reach) / g.cs.y));
+    b.z0 = max(0, c.z + (int)floorf((h.z - reach) / g.cs.z));
+    const int x1 = min(g.gx - 1, c.x + (int)floorf((h.x + reach) / g.cs.x));
+    const int y1 = min(g.gy - 1, c.y + (int)floorf((h.y + reach) / g.cs.y));
+    const int z1 = min(g.gz - 1, c.z + (int)floorf((h.z + reach) / g.cs.z));
+    b.nx = max(0, x1 - b.x0 + 1);
+    b.ny = max(0, y1 - b.y0 + 1);
+    b.nz = max(0, z1 - b.z0 + 1);
+    b.hx = b.hy = b.hz = b.hash = 0;
+    return b;
+}
+
+// The walk writes either the lists themselves (BUILD_LISTS: the reference's
+// walk every fluid step) or Verlet candidates (within the cut + fskin) that
+// kFluidFilter turns into the lists on the following fluid steps.
+enum WalkMode { BUILD_LISTS = 0, BUILD_CANDIDATES = 1 };
+
+template <int L, int MODE>
+__device__ __forceinline__ void fluidWalk(const DeviceState& d, RunIf when)
 {
     const int th = blockIdx.x * blockDim.x + threadIdx.x;
-    if ((th & ~31) >= d.nf * L || *d.status) return;
+    if ((th & ~31) >= d.nf * L || *d.status || !when.active()) return;
     const int i = th / L, lane = th % L;
     const bool live = i < d.nf;
     const int groupShift = (threadIdx.x & 31) & ~(L - 1);
     const unsigned groupBits = L == 32 ? 0xffffffffu : ((1u << L) - 1u);
     const unsigned below = (1u << lane) - 1u;
     const int n = d.nf;
+    const float skin = MODE == BUILD_CANDIDATES ? d.fskin : 0.f;
+    const int capF = MODE == BUILD_CANDIDATES ? d.kvf : d.kff;
+    const int capS = MODE == BUILD_CANDIDATES ? d.kvs : d.kfs;
     int4 ci = make_int4(0, 0, 0, 0);
     float4 hi = make_float4(0, 0, 0, 0), li = hi;
     dfl hI = df_make(0.f), cutS = hI;
@@ -134,13 +183,29 @@ __global__ void __launch_bounds__(T) kFluidLists(DeviceState d)
     // a walk position gives the partner's cell offset from the particle's own
     // cell only when the walk is centred on that cell
     const bool centred = sx == ci.x && sy == ci.y && sz == ci.z;
+    // candidates: every cell within the largest cut + skin, all inside the
+    // domain (particles outside it send the lists back to the walk)
+    LaneBox boxF, boxS;
+    if (MODE == BUILD_CANDIDATES) {
+        boxF = boxAround(lane, L, ci, hi, 2.f * fmaxf(hi.w, d.fhmax) + skin, d.grid);
+        boxS = boxAround(lane, L, ci, hi, 2.f * hi.w + skin, d.grid);
+        if (!live) boxF.nx = boxS.nx = 0;
+    }
     // fluid partners
     int nff = 0;
     {
         LaneWalk w{lane - L, 0, 0, 0, 0, 0, 0, false};
         while (true) {
             int j = 0;
-            const bool has = live && nextCandidate<L>(w, d.fcellStart, sx, sy, sz, d.grid, j);
+            const bool has = live && (MODE == BUILD_CANDIDATES ? nextBoxMember<L>(boxF, d.fcellStart, d.grid, j)
+                                                               : nextCandidate<L>(w, d.fcellStart, sx, sy, sz, d.grid, j));
+            if (MODE == BUILD_CANDIDATES) {
+                w.regular = true;
+                w.hx = boxF.hx;
+                w.hy = boxF.hy;
+                w.hz = boxF.hz;
+                w.hash = boxF.hash;
+            }
             bool take = false;
             int4 cj = make_int4(0, 0, 0, 0);
             if (has && j != i) {
@@ -149,9 +214,11 @@ __global__ void __launch_bounds__(T) kFluidLists(DeviceState d)
                 // FP32 decision away from the cut (most candidates); the exact
                 // double-float test within 1e-5 of it
                 const float3 r = relF(ci, hi, cj, hj, d.grid);
-                const float c = 2.f * fmaxf(hi.w, hj.w);
+                const float c = 2.f * fmaxf(hi.w, hj.w) + skin;
                 const float d2 = dot3(r, r), c2 = c * c;
-                if (d2 < c2 * (1.f - 1.e-5f)) {
+                if (MODE == BUILD_CANDIDATES) {
+                    take = d2 <= c2 * (1.f + 1.e-4f);
+                } else if (d2 < c2 * (1.f - 1.e-5f)) {
                     take = true;
                 } else if (d2 <= c2 * (1.f + 1.e-5f)) {
                     const dfl hJ = df_make(hj.w, d.fpl[0][j].w);
@@ -162,7 +229,10 @@ __global__ void __launch_bounds__(T) kFluidLists(DeviceState d)
             const unsigned mine = (__ballot_sync(0xffffffffu, take) >> groupShift) & groupBits;
             if (take) {
                 const int slot = nff + __popc(mine & below);
-                if (slot < d.kff) d.ff[(size_t)slot * n + i] = ffEntry(j, w.t, w.regular && centred);
+                if (slot < capF) {
+                    if (MODE == BUILD_CANDIDATES) d.fvc[(size_t)slot * n + i] = (unsigned)j;
+                    else d.ff[(size_t)slot * n + i] = ffEntry(j, w.t, w.regular && centred);
+                }
             }
             nff += __popc(mine);
             if (!__any_sync(0xffffffffu, has)) break;
@@ -174,7 +244,15 @@ __global__ void __launch_bounds__(T) kFluidLists(DeviceState d)
         LaneWalk w{lane - L, 0, 0, 0, 0, 0, 0, false};
         while (true) {
             int p = 0;
-            const bool has = live && nextCandidate<L>(w, d.scellStart, sx, sy, sz, d.grid, p);
+            const bool has = live && (MODE == BUILD_CANDIDATES ? nextBoxMember<L>(boxS, d.scellStart, d.grid, p)
+                                                               : nextCandidate<L>(w, d.scellStart, sx, sy, sz, d.grid, p));
+            if (MODE == BUILD_CANDIDATES) {
+                w.regular = true;
+                w.hx = boxS.hx;
+                w.hy = boxS.hy;
+                w.hz = boxS.hz;
+                w.hash = boxS.hash;
+            }
             bool take = false;
             int a = 0;
             if (has) {
@@ -182,18 +260,148 @@ __global__ void __launch_bounds__(T) kFluidLists(DeviceState d)
                 const int4 ca = w.regular ? make_int4(w.hx, w.hy, w.hz, w.hash) : d.scell[a];
                 const float4 ha = d.sph[a];
                 const float3 r = relF(ci, hi, ca, ha, d.grid);
-                const float d2 = dot3(r, r), c2 = 4.f * hi.w * hi.w;
-                if (d2 < c2 * (1.f - 1.e-5f)) take = true;
+                const float c = 2.f * hi.w + skin;
+                const float d2 = dot3(r, r), c2 = c * c;
+                if (MODE == BUILD_CANDIDATES) take = d2 <= c2 * (1.f + 1.e-4f);
+                else if (d2 < c2 * (1.f - 1.e-5f)) take = true;
                 else if (d2 <= c2 * (1.f + 1.e-5f)) take = withinCut(ci, hi, li, ca, ha, d.spl, a, cutS, d.grid);
             }
             const unsigned mine = (__ballot_sync(0xffffffffu, take) >> groupShift) & groupBits;
             if (take) {
                 const int slot = nfs + __popc(mine & below);
-                if (slot < d.kfs) d.fs[(size_t)slot * n + i] = fsEntry(a, w.t);
+                if (slot < capS) {
+                    if (MODE == BUILD_CANDIDATES) d.fvsc[(size_t)slot * n + i] = a;
+                    else d.fs[(size_t)slot * n + i] = fsEntry(a, w.t);
+                }
             }
             nfs += __popc(mine);
             if (!__any_sync(0xffffffffu, has)) break;
         }
+    }
+    if (!live || lane != 0) return;
+    if (MODE == BUILD_CANDIDATES) {
+        d.fvcn[i] = nff;
+        d.fvsn[i] = nfs;
+        d.fvref[i] = make_float4((float)ci.x * d.grid.cs.x + hi.x, (float)ci.y * d.grid.cs.y + hi.y,
+                                 (float)ci.z * d.grid.cs.z + hi.z, 0.f);
+        if (nff > capF || nfs > capS) {
+            atomicOr(d.status, ST_FVERLET_OVERFLOW);
+            atomicMax(&d.need[2], nff);
+            atomicMax(&d.need[3], nfs);
+        }
+    } else {
+        d.ffc[i] = nff;
+        d.fsc[i] = nfs;
+        if (nff > d.kff) atomicOr(d.status, ST_FF_OVERFLOW);
+        if (nfs > d.kfs) atomicOr(d.status, ST_FS_OVERFLOW);
+    }
+}
+
+// Positions of the contact rows when the fluid candidates are built: a solid
+// moving half the fluid margin since then makes the fluid candidates stale.
+__global__ void kFluidRefSolids(DeviceState d, RunIf when)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= d.nrow || *d.status || !when.active()) return;
+    const int a = d.rowSolid[r];
+    const int4 c = d.scell[a];
+    const float4 h = d.sph[a];
+    d.svref[r] = make_float4((float)c.x * d.grid.cs.x + h.x, (float)c.y * d.grid.cs.y + h.y,
+                             (float)c.z * d.grid.cs.z + h.z, 0.f);
+}
+
+// Walk position (0..26) of cell cj in the 27-cell walk centred on ci, or -1.
+__device__ __forceinline__ int walkPosition(int4 ci, int4 cj)
+{
+    const int dx = cj.x - ci.x, dy = cj.y - ci.y, dz = cj.z - ci.z;
+    if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) return -1;
+    return (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
+}
+
+// The lists of this fluid step from the candidates (setFluidInteractionsKernel,
+// core/neighborSearch.cu:115-220, on positions the candidates cover): the
+// reference's test on the current positions, for partners in the 27 cells
+// around the particle's current cell (all particles are inside the domain
+// here, so those are the cells the reference walks).  The rebuild flag is
+// cleared: the last position update of the step raises it again.
+template <int L>
+__global__ void __launch_bounds__(T) kFluidFilter(DeviceState d)
+{
+    const int th = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((th & ~31) >= d.nf * L || *d.status || *d.fslowMode || *d.slowMode) return;
+    if (th == 0) *(volatile int*)d.frebuild = 0;
+    const int i = th / L, lane = th % L;
+    const bool live = i < d.nf;
+    const int groupShift = (threadIdx.x & 31) & ~(L - 1);
+    const unsigned groupBits = L == 32 ? 0xffffffffu : ((1u << L) - 1u);
+    const unsigned below = (1u << lane) - 1u;
+    const int n = d.nf;
+    int4 ci = make_int4(0, 0, 0, 0);
+    float4 hi = make_float4(0, 0, 0, 0), li = hi;
+    dfl hI = df_make(0.f), cutS = hI;
+    int nc = 0, ns = 0;
+    if (live) {
+        ci = d.fcell[i];
+        hi = d.fph[0][i];
+        li = d.fpl[0][i];
+        hI = df_make(hi.w, li.w);
+        cutS = df_add(hI, hI);
+        nc = min(d.fvcn[i], d.kvf);
+        ns = min(d.fvsn[i], d.kvs);
+    }
+    int nff = 0;
+    for (int base = 0; __any_sync(0xffffffffu, base < nc); base += L) {
+        const int k = base + lane;
+        bool take = false;
+        int j = 0, t = -1;
+        if (k < nc) {
+            j = (int)d.fvc[(size_t)k * n + i];
+            const int4 cj = d.fcell[j];
+            t = walkPosition(ci, cj);
+            if (t >= 0) {
+                const float4 hj = d.fph[0][j];
+                const float3 r = relF(ci, hi, cj, hj, d.grid);
+                const float c = 2.f * fmaxf(hi.w, hj.w);
+                const float d2 = dot3(r, r), c2 = c * c;
+                if (d2 < c2 * (1.f - 1.e-5f)) {
+                    take = true;
+                } else if (d2 <= c2 * (1.f + 1.e-5f)) {
+                    const dfl hJ = df_make(hj.w, d.fpl[0][j].w);
+                    const dfl rad = dfMax(hI, hJ);
+                    take = withinCut(ci, hi, li, cj, hj, d.fpl[0], j, df_add(rad, rad), d.grid);
+                }
+            }
+        }
+        const unsigned mine = (__ballot_sync(0xffffffffu, take) >> groupShift) & groupBits;
+        if (take) {
+            const int slot = nff + __popc(mine & below);
+            if (slot < d.kff) d.ff[(size_t)slot * n + i] = ffEntry(j, t, true);
+        }
+        nff += __popc(mine);
+    }
+    int nfs = 0;
+    for (int base = 0; __any_sync(0xffffffffu, base < ns); base += L) {
+        const int k = base + lane;
+        bool take = false;
+        int a = 0, t = -1;
+        if (k < ns) {
+            a = d.fvsc[(size_t)k * n + i];
+            const int4 ca = d.scell[a];
+            t = walkPosition(ci, ca);
+            if (t >= 0) {
+                const float4 ha = d.sph[a];
+                const float3 r = relF(ci, hi, ca, ha, d.grid);
+                const float d2 = dot3(r, r), c2 = 4.f * hi.w * hi.w;
+                if (d2 < c2 * (1.f - 1.e-5f)) take = true;
+                else if (d2 <= c2 * (1.f + 1.e-5f)) take = withinCut(ci, hi, li, ca, ha, d.spl, a, cutS, d.grid);
+            }
+        }
+        const unsigned mine = (__ballot_sync(0xffffffffu, take) >> groupShift) & groupBits;
+        if (take) {
+            const int slot = nfs + __popc(mine & below);
+            if (slot < d.kfs) d.fs[(size_t)slot * n + i] = fsEntry(a, t);
+        }
+        nfs += __popc(mine);
     }
     if (!live || lane != 0) return;
     d.ffc[i] = nff;
@@ -519,10 +727,37 @@ __global__ void kSolidNormals(DeviceState d, double h)
 
 }  // namespace
 
-void launchFluidLists(const DeviceState& d, cudaStream_t s)
+template <int L>
+__global__ void __launch_bounds__(T) kFluidWalkLists(DeviceState d, RunIf when)
+{
+    fluidWalk<L, BUILD_LISTS>(d, when);
+}
+template <int L>
+__global__ void __launch_bounds__(T) kFluidWalkCandidates(DeviceState d, RunIf when)
+{
+    fluidWalk<L, BUILD_CANDIDATES>(d, when);
+}
+
+void launchFluidLists(const DeviceState& d, bool walk, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    LAUNCH_LANES(kFluidLists, d.lanes, d.nf, T, s, d);
+    RunIf walkLists;  // the reference's walk every fluid step (a fluid or a solid left the domain)
+    walkLists.always = walk ? 1 : 0;
+    walkLists.a = d.fslowMode;
+    walkLists.b = d.slowMode;
+    RunIf rebuild;    // Verlet candidates, when stale
+    rebuild.always = 0;
+    rebuild.a = d.frebuild;
+    rebuild.unless = d.fslowMode;
+    rebuild.unless2 = d.slowMode;
+    if (walk) {
+        LAUNCH_LANES(kFluidWalkLists, d.lanes, d.nf, T, s, d, walkLists);
+        return;
+    }
+    LAUNCH_LANES(kFluidWalkLists, d.lanes, d.nf, T, s, d, walkLists);
+    LAUNCH_LANES(kFluidWalkCandidates, d.lanes, d.nf, T, s, d, rebuild);
+    if (d.nrow > 0) ++t_kernelLaunches, kFluidRefSolids<<<blocksFor(d.nrow, T), T, 0, s>>>(d, rebuild);
+    LAUNCH_LANES(kFluidFilter, d.lanes, d.nf, T, s, d);
 }
 
 void launchCouplingLists(const DeviceState& d, cudaStream_t s)

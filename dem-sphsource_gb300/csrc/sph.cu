@@ -280,6 +280,13 @@ __global__ void __launch_bounds__(T) kMomentum(DeviceState d, dfl dtf, dfl halfD
     dfAxpy(xh, xl, vh, vl, halfDtf);
     d.fph[0][i] = xh;
     d.fpl[0][i] = xl;
+    // the fluid candidates go stale once a particle has moved half the margin
+    const int4 c = d.fcell[i];
+    const float4 p0 = d.fvref[i];
+    const float dx = (float)c.x * d.grid.cs.x + xh.x - p0.x, dy = (float)c.y * d.grid.cs.y + xh.y - p0.y,
+                dz = (float)c.z * d.grid.cs.z + xh.z - p0.z;
+    const float half = 0.5f * d.fskin;
+    if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)d.frebuild = 1;
 }
 
 // ---- Shepard density re-initialisation (integrate.cu:3-53) ----

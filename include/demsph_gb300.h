@@ -146,6 +146,10 @@ typedef struct demsph_options {
                                     candidates: the reference's 27-cell walk every step */
     int fluid_lanes;             /* threads per fluid particle in the fluid list and pair loops (1, 2, 4
                                     or 8); 0 = chosen from the particle count */
+    double fluid_verlet_skin;    /* margin (m) of the fluid list candidates, rebuilt (with the reorder of
+                                    the fluids by cell) once a fluid or solid particle has moved half of
+                                    it; 0 = 0.2 x the largest smoothing length; < 0 = no candidates: the
+                                    reference's 27-cell walk every fluid step */
 } demsph_options;
 
 typedef struct demsph_counts {

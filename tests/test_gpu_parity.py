@@ -76,17 +76,19 @@ def test_one_step_within_force_tolerance(ds, scenes, name):
     _check_step(eng, orc, sc, _spacing(recipe), 1, dt, FORCE_TOL, POS_TOL)
 
 
-# (solid candidate margin, threads per fluid particle): the default, the margin
-# variants, and one thread per fluid particle (what large scenes use)
-VARIANTS = [(s, 0) for s in SKINS] + [(0.0, 1)]
+# (solid candidate margin, threads per fluid particle, fluid candidate margin):
+# the defaults, the solid margin variants, one thread per fluid particle (what
+# large scenes use), fluid candidates rebuilt every fluid step and the fluid walk
+VARIANTS = [(s, 0, 0.0) for s in SKINS] + [(0.0, 1, 0.0), (0.0, 0, 1.0e-9), (0.0, 0, -1.0)]
 
 
-@pytest.mark.parametrize("skin,lanes", VARIANTS)
+@pytest.mark.parametrize("skin,lanes,fskin", VARIANTS)
 @pytest.mark.parametrize("name", SCENES)
-def test_ten_steps_artefacts_equal_drift_bounded(ds, scenes, name, skin, lanes):
+def test_ten_steps_artefacts_equal_drift_bounded(ds, scenes, name, skin, lanes, fskin):
     """Ten update() calls through the five stage calls: integer artefacts equal
     after every step; floating-point drift within DRIFT_TOL."""
-    recipe, b, sc, eng, orc = _setup(ds, scenes, name, solid_verlet_skin=skin, fluid_lanes=lanes)
+    recipe, b, sc, eng, orc = _setup(ds, scenes, name, solid_verlet_skin=skin, fluid_lanes=lanes,
+                                     fluid_verlet_skin=fskin)
     eng.initialize()
     orc.initialize()
     dt, gap = sc.time_step, sc.fluid_integrate_gap
