@@ -188,22 +188,36 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
     DeviceState& d = e->d;
     const cudaStream_t s = e->stream;
     const bool fluidStep = d.nf > 0 && (iStep % gap == 0);
-    if (fluidStep) {
-        TIMED("fluid_hash_reorder");
-        launchFluidHashReorder(d, e->forceWalk, s);
-    }
     // solids that never move (walls of dummy particles, fixed spheres) are
     // hashed and sorted once, and again only after their positions are uploaded
     const bool solidsMove = e->nMassive > 0 || e->solidSortStale;
+    const bool forceSort = e->forceWalk || e->solidSortStale;
+    // Work needed only on some steps (sorting by cell, rebuilding candidates,
+    // the walk) is launched every step and decided on the device from the
+    // flags the previous step left (RunIf): the kernels return at once when
+    // their work is not needed.  (Conditional graph nodes in place of these
+    // launches measured slower on GB300, alone and with many scenes.)
+    if (fluidStep) {
+        TIMED("fluid_hash_reorder");
+        launchFluidHash(d, e->forceWalk, s);
+        launchFluidReorder(d, e->forceWalk, s);
+    }
     if (solidsMove || e->forceWalk) {
         TIMED("solid_hash_sort");
-        launchSolidHashSort(d, e->forceWalk || e->solidSortStale, fluidStep, s);
+        launchSolidHash(d, forceSort, fluidStep, s);
+        launchSolidSort(d, forceSort, fluidStep, s);
         e->solidSortStale = false;
     }
     if (fluidStep) {
         {
             TIMED("fluid_lists");
-            launchFluidLists(d, e->forceWalk, s);
+            if (e->forceWalk) {
+                launchFluidWalkLists(d, true, s);
+            } else {
+                launchFluidWalkLists(d, false, s);
+                launchFluidCandidates(d, s);
+                launchFluidFilter(d, s);
+            }
         }
         if (e->nMassive > 0) {  // the coupling force moves only solids with mass
             TIMED("coupling_lists");
@@ -213,7 +227,8 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
     e->par ^= 1;
     TIMED("solid_contact_list");
     e->walkOrder[e->par] = e->forceWalk;
-    launchSolidContactList(d, e->par, e->forceWalk, s);
+    if (!e->forceWalk) launchVerletBuild(d, s);
+    launchContactDetect(d, e->par, e->forceWalk, s);
 }
 
 void stageBefore(demsph_engine* e, double dt)
@@ -363,8 +378,9 @@ void grow(demsph_engine* e, int status)
         d.coupList = dalloc<int>(d.coupCap, e->owned, e->stream);
     }
     if (status & ST_MODE_CHANGE) {
-        // the abandoned step may have counted some solids into cells
+        // the abandoned step may have counted some particles into cells
         CK(cudaMemsetAsync(d.scellCount, 0, sizeof(int) * d.grid.num, e->stream));
+        if (d.nf > 0) CK(cudaMemsetAsync(d.fcellCount, 0, sizeof(int) * d.grid.num, e->stream));
     }
     CK(cudaMemsetAsync(d.status, 0, sizeof(int), e->stream));
     dropGraph(e);

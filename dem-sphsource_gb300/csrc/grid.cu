@@ -22,13 +22,6 @@ namespace {
 
 constexpr int T = 256;
 
-__global__ void kFluidClearCounts(DeviceState d, RunIf when)
-{
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= d.grid.num || *d.status || !when.active()) return;
-    d.fcellCount[k] = 0;
-}
-
 // Cell keys of the fluids every fluid step; on reorder steps the whole
 // particle is copied into the gather sources and takes a slot in its cell.
 __global__ void kFluidHash(DeviceState d, RunIf sortNow)
@@ -113,6 +106,7 @@ __global__ void kFluidGather(DeviceState d, RunIf when)
     const int id = d.tid[e];
     d.fid[q] = id;
     d.fslot[id] = q;
+    d.fcellCount[d.fkey[e]] = 0;  // the counts are consumed: clear them for the next reorder
 }
 
 // Cell keys of the solids every step (they are exported in the reference's
@@ -157,25 +151,34 @@ __global__ void kSolidRank(DeviceState d, RunIf when)
 
 }  // namespace
 
-void launchFluidHashReorder(const DeviceState& d, bool force, cudaStream_t s)
+static RunIf fluidReorderWhen(const DeviceState& d, bool force)
 {
-    if (d.nf <= 0) return;
     RunIf when;
     when.always = force ? 1 : 0;
     when.a = d.frebuild;
     when.b = d.fslowMode;
-    ++t_kernelLaunches, kFluidClearCounts<<<blocksFor(d.grid.num, T), T, 0, s>>>(d, when);
-    ++t_kernelLaunches, kFluidHash<<<blocksFor(d.nf, T), T, 0, s>>>(d, when);
+    return when;
+}
+
+void launchFluidHash(const DeviceState& d, bool force, cudaStream_t s)
+{
+    if (d.nf <= 0) return;
+    ++t_kernelLaunches, kFluidHash<<<blocksFor(d.nf, T), T, 0, s>>>(d, fluidReorderWhen(d, force));
+}
+
+void launchFluidReorder(const DeviceState& d, bool force, cudaStream_t s)
+{
+    if (d.nf <= 0) return;
+    // fcellCount is zero here: cleared at creation, by kFluidGather after every
+    // reorder, and by the host after a step abandoned in kFluidHash
+    const RunIf when = fluidReorderWhen(d, force);
     scanExclusive(d.fcellCount, d.fcellStart, d.grid.num, d.scanWork, s, when);
     ++t_kernelLaunches, kScatter<<<blocksFor(d.nf, T), T, 0, s>>>(d.nf, d.fkey, d.fslotInCell, d.fcellStart, d.fsortTmp, d.status, when);
     ++t_kernelLaunches, kFluidGather<<<blocksFor(d.nf, T), T, 0, s>>>(d, when);
 }
 
-void launchSolidHashSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s)
+static RunIf solidSortWhen(const DeviceState& d, bool force, bool fluidStep)
 {
-    if (d.ns <= 0) return;
-    // scellCount is zero here: cleared at creation, by kSolidRank after every
-    // sort, and by the host after a step abandoned in kSolidHash
     RunIf when;
     when.always = force ? 1 : 0;
     when.a = d.rebuild;
@@ -184,7 +187,21 @@ void launchSolidHashSort(const DeviceState& d, bool force, bool fluidStep, cudaS
         when.c = d.frebuild;
         when.e = d.fslowMode;
     }
-    ++t_kernelLaunches, kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d, when);
+    return when;
+}
+
+void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s)
+{
+    if (d.ns <= 0) return;
+    ++t_kernelLaunches, kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d, solidSortWhen(d, force, fluidStep));
+}
+
+void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s)
+{
+    if (d.ns <= 0) return;
+    // scellCount is zero here: cleared at creation, by kSolidRank after every
+    // sort, and by the host after a step abandoned in kSolidHash
+    const RunIf when = solidSortWhen(d, force, fluidStep);
     scanExclusive(d.scellCount, d.scellStart, d.grid.num, d.scanWork, s, when);
     ++t_kernelLaunches, kScatter<<<blocksFor(d.ns, T), T, 0, s>>>(d.ns, d.skey, d.sslotInCell, d.scellStart, d.ssortTmp, d.status, when);
     ++t_kernelLaunches, kSolidRank<<<blocksFor(d.ns, T), T, 0, s>>>(d, when);

@@ -216,21 +216,32 @@ size_t scanWorkspaceInts(int n);
 void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s, RunIf when = RunIf{});
 
 // grid.cu
-// Fluid cell keys every fluid step; the reorder by cell only when the fluid
-// candidates are rebuilt (or the lists come from the walk).
-void launchFluidHashReorder(const DeviceState& d, bool force, cudaStream_t s);
-// Solid cell keys every step; the sort by cell only when `force`, when the
-// contact candidates are stale, when lists come from the 27-cell walk, or -
-// on fluid steps (fluidStep) - when the fluid lists walk the cells.
-void launchSolidHashSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s);
+// Fluid cell keys every fluid step (launchFluidHash); the reorder by cell
+// (launchFluidReorder) only when `force`, when the fluid candidates are
+// rebuilt, or when the lists come from the walk.
+void launchFluidHash(const DeviceState& d, bool force, cudaStream_t s);
+void launchFluidReorder(const DeviceState& d, bool force, cudaStream_t s);
+// Solid cell keys every step (launchSolidHash); the sort by cell
+// (launchSolidSort) only when `force`, when the contact candidates are stale,
+// when lists come from the 27-cell walk, or - on fluid steps (fluidStep) -
+// when the fluid lists walk the cells.
+void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s);
+void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s);
 
 // lists.cu
-// Fluid lists of a fluid step: from Verlet candidates (rebuilt when stale),
-// or from the reference's walk (walk = true, or once a particle has left the domain).
-void launchFluidLists(const DeviceState& d, bool walk, cudaStream_t s);
+// Fluid lists of a fluid step: the reference's walk (launchFluidWalkLists:
+// walk = true, or once a particle has left the domain), or Verlet candidates
+// rebuilt when stale (launchFluidCandidates) and filtered every fluid step
+// (launchFluidFilter).
+void launchFluidWalkLists(const DeviceState& d, bool walk, cudaStream_t s);
+void launchFluidCandidates(const DeviceState& d, cudaStream_t s);
+void launchFluidFilter(const DeviceState& d, cudaStream_t s);
 void launchCouplingLists(const DeviceState& d, cudaStream_t s);
-// forceWalk: build from the reference's 27-cell walk (list in the reference's order)
-void launchSolidContactList(const DeviceState& d, int parity, bool forceWalk, cudaStream_t s);
+// Solid contact candidates, when stale (launchVerletBuild), and the contact
+// rows of the step (launchContactDetect; forceWalk: from the reference's
+// 27-cell walk, in the reference's order).
+void launchVerletBuild(const DeviceState& d, cudaStream_t s);
+void launchContactDetect(const DeviceState& d, int parity, bool forceWalk, cudaStream_t s);
 int launchBondFlags(const DeviceState& d, int parity, int* flag, int* pos, int* work, cudaStream_t s);
 void launchBondWrite(const DeviceState& d, int parity, const int* flag, const int* pos, cudaStream_t s);
 void launchSolidNormals(const DeviceState& d, double h, cudaStream_t s);

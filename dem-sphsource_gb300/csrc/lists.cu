@@ -738,25 +738,31 @@ __global__ void __launch_bounds__(T) kFluidWalkCandidates(DeviceState d, RunIf w
     fluidWalk<L, BUILD_CANDIDATES>(d, when);
 }
 
-void launchFluidLists(const DeviceState& d, bool walk, cudaStream_t s)
+void launchFluidWalkLists(const DeviceState& d, bool walk, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    RunIf walkLists;  // the reference's walk every fluid step (a fluid or a solid left the domain)
-    walkLists.always = walk ? 1 : 0;
-    walkLists.a = d.fslowMode;
-    walkLists.b = d.slowMode;
-    RunIf rebuild;    // Verlet candidates, when stale
-    rebuild.always = 0;
-    rebuild.a = d.frebuild;
-    rebuild.unless = d.fslowMode;
-    rebuild.unless2 = d.slowMode;
-    if (walk) {
-        LAUNCH_LANES(kFluidWalkLists, d.lanes, d.nf, T, s, d, walkLists);
-        return;
-    }
-    LAUNCH_LANES(kFluidWalkLists, d.lanes, d.nf, T, s, d, walkLists);
-    LAUNCH_LANES(kFluidWalkCandidates, d.lanes, d.nf, T, s, d, rebuild);
-    if (d.nrow > 0) ++t_kernelLaunches, kFluidRefSolids<<<blocksFor(d.nrow, T), T, 0, s>>>(d, rebuild);
+    RunIf when;  // the reference's walk every fluid step (a fluid or a solid left the domain)
+    when.always = walk ? 1 : 0;
+    when.a = d.fslowMode;
+    when.b = d.slowMode;
+    LAUNCH_LANES(kFluidWalkLists, d.lanes, d.nf, T, s, d, when);
+}
+
+void launchFluidCandidates(const DeviceState& d, cudaStream_t s)
+{
+    if (d.nf <= 0) return;
+    RunIf when;  // Verlet candidates, when stale
+    when.always = 0;
+    when.a = d.frebuild;
+    when.unless = d.fslowMode;
+    when.unless2 = d.slowMode;
+    LAUNCH_LANES(kFluidWalkCandidates, d.lanes, d.nf, T, s, d, when);
+    if (d.nrow > 0) ++t_kernelLaunches, kFluidRefSolids<<<blocksFor(d.nrow, T), T, 0, s>>>(d, when);
+}
+
+void launchFluidFilter(const DeviceState& d, cudaStream_t s)
+{
+    if (d.nf <= 0) return;
     LAUNCH_LANES(kFluidFilter, d.lanes, d.nf, T, s, d);
 }
 
@@ -771,10 +777,15 @@ void launchCouplingLists(const DeviceState& d, cudaStream_t s)
     ++t_kernelLaunches, kCoupSort<<<blocksFor(d.ns, 256), 256, 0, s>>>(d);
 }
 
-void launchSolidContactList(const DeviceState& d, int par, bool forceWalk, cudaStream_t s)
+void launchVerletBuild(const DeviceState& d, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    if (!forceWalk) ++t_kernelLaunches, kVerletBuild<<<blocksFor(d.nrow, T), T, 0, s>>>(d);
+    ++t_kernelLaunches, kVerletBuild<<<blocksFor(d.nrow, T), T, 0, s>>>(d);
+}
+
+void launchContactDetect(const DeviceState& d, int par, bool forceWalk, cudaStream_t s)
+{
+    if (d.nrow <= 0) return;
     ++t_kernelLaunches, kContactDetect<<<blocksFor(d.nrow, T), T, 0, s>>>(d, par, forceWalk ? 1 : 0);
 }
 
