@@ -230,6 +230,24 @@ def cpu_baseline(scene, gap, dt, budget_s, nf, n_mobile):
                       f"FP64 oracle, OpenMP over particles"}
 
 
+# ---- ranks: replicas, no exchange on the data path -------------------------------------------
+def rank_total(value, how, dist=None, device="cuda"):
+    """Combines one number over the ranks of a replica run: "max" for times
+    (the job ends with its slowest rank), "sum" for work.  Without a process
+    group it returns the value itself."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if how == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def rank_share(items, rank, world):
+    """This rank's share of independent work items (scenes): every world-th one."""
+    return items[rank::world]
+
+
 # ---- many scenes: batched (config 3) and served (config 4) -----------------------------------
 def scene_updates(scene, steps):
     nf, n_mobile, _ = mobile_counts(scene)
@@ -258,17 +276,10 @@ def run_many(args, world, rank, local):
     warm.wait(warm.submit(wsc, 10), 600.0)
     warm.close()
 
-    def reduce(v, op):
-        if not dist:
-            return v
-        t = torch.tensor([float(v)], device="cuda")
-        dist.all_reduce(t, op=op)
-        return float(t.item())
-
     budget = 150 << 30
     if args.config == 3:
         steps = args.steps if args.steps != 2000 else 1000
-        recipes = sc.batch_mix(n_scenes=args.scenes, steps=steps)[rank::world]
+        recipes = rank_share(sc.batch_mix(n_scenes=args.scenes, steps=steps), rank, world)
         built = [ds.build_scene(r) for r in recipes]
         total = sum(scene_updates(s, steps) for _, s in built)
         srv = ds.Server(device=device, workers=args.workers, hbm_budget_bytes=budget)
@@ -283,8 +294,8 @@ def run_many(args, world, rank, local):
         st = srv.stats()
         launches = None
         srv.close()
-        wall = reduce(wall, dist.ReduceOp.MAX if dist else None)
-        total = reduce(total, dist.ReduceOp.SUM if dist else None)
+        wall = rank_total(wall, "max", dist)
+        total = rank_total(total, "sum", dist)
         # plain: a spaced sample of the same scenes, one at a time, same engine path
         k = max(1, len(built) // max(1, args.plain_scenes))
         sample = built[::k][:args.plain_scenes]
@@ -325,7 +336,7 @@ def run_many(args, world, rank, local):
         return
 
     # config 4: serving
-    arrivals = sc.serving_stream(duration=args.duration)[rank::world]
+    arrivals = rank_share(sc.serving_stream(duration=args.duration), rank, world)
     srv = ds.Server(device=device, workers=args.workers, hbm_budget_bytes=budget)
     if dist:
         dist.barrier()
@@ -344,8 +355,8 @@ def run_many(args, world, rank, local):
         window = time.perf_counter() - t0
         st = srv.stats()
     srv.close()  # requests still queued or running are dropped
-    upd = reduce(st["particle_updates"], dist.ReduceOp.SUM if dist else None)
-    window = reduce(window, dist.ReduceOp.MAX if dist else None)
+    upd = rank_total(st["particle_updates"], "sum", dist)
+    window = rank_total(window, "max", dist)
     if rank != 0:
         return
     lag.sort()
@@ -457,13 +468,8 @@ def main():
     ms = ev0.elapsed_time(ev1)
     updates = updates_for(step, args.steps, gap, nf, n_mobile)
     step += args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        u = torch.tensor([float(updates)], device="cuda")
-        dist.all_reduce(u, op=dist.ReduceOp.SUM)
-        updates = float(u.item())
+    ms = rank_total(ms, "max", dist)
+    updates = rank_total(updates, "sum", dist)
     value = updates / (ms / 1000.0)
 
     # ---- stage timing pass (uncaptured, CUDA events per stage) for the roofline and latency ----
@@ -536,9 +542,7 @@ def main():
     e2e_updates = updates_for(step - ne, ne, gap, nf, n_mobile)
     e2e_val = e2e_updates / e2e_s
     if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_val = e2e_updates * world / float(t.item())
+        e2e_val = e2e_updates * world / rank_total(e2e_s, "max", dist)
 
     cb = None
     if rank == 0 and not args.no_cpu:

@@ -437,9 +437,8 @@ __device__ __forceinline__ dfl groupSumDF(dfl v, int width)
 // calClumpForceTorque (integrate.cu:860-881): a group of `width` lanes per
 // clump over its pebbles; the pebbles' forces (a m) and torques about the
 // centroid are summed in double-float, reduced in a fixed tree.
-__global__ void kClumpForce(DeviceState d, int width)
+__device__ __forceinline__ void clumpForceGroup(const DeviceState& d, int width, int t)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = t / width, lane = t % width;
     // whole warps only: the shuffles below take every lane of the warp
     if ((t & ~31) >= d.nc * width || *d.status) return;
@@ -512,35 +511,10 @@ __device__ __forceinline__ void kickSolid(const DeviceState& d, int i, dfl dt, i
     d.swl[i] = make_float4(x.lo, y.lo, z.lo, wl.w);
 }
 
-// After the last drift of a step: once a solid that can touch others has
-// moved half the candidate margin since the candidates were built, the next
-// step rebuilds them.
-__device__ __forceinline__ void checkDisplacement(const DeviceState& d, int i)
+__device__ __forceinline__ void solidIntegrateOne(const DeviceState& d, int i, dfl half, int before)
 {
-    const int r = d.srow[i];
-    if (r < 0) return;
-    const int4 c = d.scell[i];
-    const float4 h = d.sph[i];
-    const float4 p0 = d.vref[r];
-    const float dx = (float)c.x * d.grid.cs.x + h.x - p0.x, dy = (float)c.y * d.grid.cs.y + h.y - p0.y,
-                dz = (float)c.z * d.grid.cs.z + h.z - p0.z;
-    const float half = 0.5f * d.skin;
-    if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)d.rebuild = 1;
-    if (d.nf > 0) {  // the fluid candidates' solid partners
-        const float4 q0 = d.svref[r];
-        const float ex = (float)c.x * d.grid.cs.x + h.x - q0.x, ey = (float)c.y * d.grid.cs.y + h.y - q0.y,
-                    ez = (float)c.z * d.grid.cs.z + h.z - q0.z;
-        const float fh = 0.5f * d.fskin;
-        if (!(ex * ex + ey * ey + ez * ez <= fh * fh)) *(volatile int*)d.frebuild = 1;
-    }
-}
-
-__global__ void kSolidIntegrate(DeviceState d, dfl half, int before)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.ns || *d.status) return;
     const int4 f = d.sflags[i];
-    if (f.z >= 0) return;  // clump pebbles: kClumpIntegrate
+    if (f.z >= 0) return;  // clump pebbles: clumpIntegrateGroup
     if (before) {
         kickSolid(d, i, half, f);
         driftSolid(d, i, half);
@@ -548,6 +522,7 @@ __global__ void kSolidIntegrate(DeviceState d, dfl half, int before)
         driftSolid(d, i, half);
         kickSolid(d, i, half, f);
         checkDisplacement(d, i);
+        rehashSolid(d, i);
     }
 }
 
@@ -636,9 +611,8 @@ __device__ __forceinline__ void pebbleKick(const DeviceState& d, int i, float3 a
 // first lane advances the clump's state, the lanes then move the pebbles.
 //   before contact: kick, pebbles from the kicked state, centroid and pebble drift;
 //   after contact:  pebble and centroid drift, kick, pebbles from the kicked state.
-__global__ void kClumpIntegrate(DeviceState d, dfl halfDF, int before, int width)
+__device__ __forceinline__ void clumpIntegrateGroup(const DeviceState& d, dfl halfDF, int before, int width, int t)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = t / width, lane = t % width;
     // whole warps only: the shuffles below take every lane of the warp
     if ((t & ~31) >= d.nc * width || *d.status) return;
@@ -679,15 +653,42 @@ __global__ void kClumpIntegrate(DeviceState d, dfl halfDF, int before, int width
     const float3 rotn = (w0 + xyz(v[4])) * (0.5f * halfDF.hi);
     for (int i = s + lane; i < e; i += width) {
         pebbleKick(d, i, a, v[2], v[3], v[4], v[5], v[0], v[1], rotn);
-        if (before) driftSolid(d, i, halfDF);
-        else checkDisplacement(d, i);
+        if (before) {
+            driftSolid(d, i, halfDF);
+        } else {
+            checkDisplacement(d, i);
+            rehashSolid(d, i);
+        }
     }
 }
 
-__global__ void kStepDone(int* status, int* steps)
+__global__ void kClumpForce(DeviceState d, int width)
 {
-    if (*status == 0) atomicAdd(steps, 1);
+    clumpForceGroup(d, width, blockIdx.x * blockDim.x + threadIdx.x);
 }
+
+// One half-step integration of all solids (integrate.cu:964-1027): the first
+// solidBlocks blocks take one solid each per thread, the rest a group of
+// `width` lanes per clump.  clumpForce: each clump group first sums its
+// pebbles' forces (kClumpForce's work, for runs of whole steps where nothing
+// happens between the contact phase and this integration); countStep: the
+// step has completed (the status can no longer change) and is counted.
+__global__ void kIntegrate(DeviceState d, dfl half, int before, int width, int solidBlocks, int clumpForce,
+                           int countStep)
+{
+    if (countStep && blockIdx.x == 0 && threadIdx.x == 0 && *d.status == 0) atomicAdd(d.stepsDone, 1);
+    if ((int)blockIdx.x < solidBlocks) {
+        const int k = blockIdx.x * blockDim.x + threadIdx.x;
+        if (k >= d.nmove || *d.status) return;
+        solidIntegrateOne(d, d.moveList[k], half, before);
+        return;
+    }
+    const int t = (blockIdx.x - solidBlocks) * blockDim.x + threadIdx.x;
+    if (clumpForce) clumpForceGroup(d, width, t);
+    clumpIntegrateGroup(d, half, before, width, t);
+}
+
+
 
 }  // namespace
 
@@ -707,19 +708,16 @@ void launchClumpForce(const DeviceState& d, cudaStream_t s)
     const int w = d.clumpLanes;
     ++t_kernelLaunches, kClumpForce<<<blocksFor((long long)d.nc * w, 256), 256, 0, s>>>(d, w);
 }
-void launchSolidIntegrate(const DeviceState& d, double dt, bool before, cudaStream_t s)
+void launchSolidIntegrate(const DeviceState& d, double dt, bool before, bool clumpForce, bool countStep,
+                          cudaStream_t s)
 {
-    const double half = 0.5 * dt;
-    const dfl h = df_from_double(half);
-    if (d.ns > 0) ++t_kernelLaunches, kSolidIntegrate<<<blocksFor(d.ns, 256), 256, 0, s>>>(d, h, before ? 1 : 0);
-    if (d.nc > 0) {
-        const int w = d.clumpLanes;
-        ++t_kernelLaunches, kClumpIntegrate<<<blocksFor((long long)d.nc * w, 256), 256, 0, s>>>(d, h, before ? 1 : 0, w);
-    }
+    const dfl h = df_from_double(0.5 * dt);
+    const int sb = d.nmove > 0 ? blocksFor(d.nmove, 256) : 0;
+    const int cb = d.nc > 0 ? blocksFor((long long)d.nc * d.clumpLanes, 256) : 0;
+    if (sb + cb == 0 && !countStep) return;
+    ++t_kernelLaunches, kIntegrate<<<std::max(1, sb + cb), 256, 0, s>>>(d, h, before ? 1 : 0, d.clumpLanes, sb,
+                                                                       clumpForce ? 1 : 0, countStep ? 1 : 0);
 }
-void launchStepDone(const DeviceState& d, cudaStream_t s)
-{
-    ++t_kernelLaunches, kStepDone<<<1, 1, 0, s>>>(d.status, d.stepsDone);
-}
+
 
 }  // namespace demsph

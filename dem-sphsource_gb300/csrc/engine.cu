@@ -234,7 +234,7 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
 void stageBefore(demsph_engine* e, double dt)
 {
     TIMED("integrate_before");
-    launchSolidIntegrate(e->d, dt, true, e->stream);
+    launchSolidIntegrate(e->d, dt, true, false, false, e->stream);
 }
 
 void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
@@ -267,7 +267,10 @@ void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
     }
 }
 
-void stageContact(demsph_engine* e, double dt)
+// withClumpForce: the clumps' pebble forces are summed here (the staged
+// calls: the driver's hook runs between contact and integration); a whole
+// step (fullStep) sums them inside the integration that follows instead.
+void stageContact(demsph_engine* e, double dt, bool withClumpForce = true)
 {
     DeviceState& d = e->d;
     if (d.nb > 0) {
@@ -278,26 +281,28 @@ void stageContact(demsph_engine* e, double dt)
         TIMED("solid_forces");
         launchSolidForces(d, e->par, (float)dt, e->stream);
     }
-    if (d.nc > 0) {
+    if (d.nc > 0 && withClumpForce) {
         TIMED("clump_force");
         launchClumpForce(d, e->stream);
     }
 }
 
-void stageAfter(demsph_engine* e, double dt)
+void stageAfter(demsph_engine* e, double dt, bool clumpForce = false, bool countStep = false)
 {
     TIMED("integrate_after");
-    launchSolidIntegrate(e->d, dt, false, e->stream);
+    launchSolidIntegrate(e->d, dt, false, clumpForce, countStep, e->stream);
 }
 
+// One solverBase::update() without the driver's hook.  The clump force sum
+// and the step count ride on the last integration (bit for bit what the
+// staged calls compute).
 void fullStep(demsph_engine* e, double dt, int iStep, int gap)
 {
     stageNeighborSearch(e, iStep, gap);
     stageBefore(e, dt);
     stageFluid(e, dt, iStep, gap);
-    stageContact(e, dt);
-    stageAfter(e, dt);
-    launchStepDone(e->d, e->stream);
+    stageContact(e, dt, false);
+    stageAfter(e, dt, e->d.nc > 0, true);
 }
 
 // Grows whatever overflowed and clears the status.  e->par must be the parity
@@ -666,6 +671,25 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 effMax = std::max(effMax, sc->solid_effective_radius[i]);
             }
             d.nrow = (int)rowSolid.size();
+            // solids the integration advances (a dummy at rest never moves: it has no mass)
+            {
+                std::vector<int>& move = e->moveHost;
+                e->moveKind.assign(ns, 1);
+                for (int i = 0; i < ns; ++i) {
+                    if (sc->solid_clump[i] >= 0) {
+                        e->moveKind[i] = 0;
+                        continue;
+                    }
+                    if (flags[i].w & F_DUMMY) e->moveKind[i] = 2;
+                    const double3 v = v3(sc->solid_velocity, i);
+                    if (!(flags[i].w & F_DUMMY) || v.x != 0.0 || v.y != 0.0 || v.z != 0.0) move.push_back(i);
+                }
+                d.nmove = (int)move.size();
+                d.moveList = dalloc<int>(move.size(), e->owned, e->stream);
+                if (!move.empty())
+                    CK(cudaMemcpyAsync(d.moveList, move.data(), sizeof(int) * move.size(), cudaMemcpyHostToDevice,
+                                       e->stream));
+            }
             d.srow = dalloc<int>(ns, e->owned, e->stream);
             d.rowSolid = dalloc<int>(d.nrow, e->owned, e->stream);
             d.scentre = dalloc<int4>(d.nrow, e->owned, e->stream);

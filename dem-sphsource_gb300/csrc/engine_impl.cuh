@@ -54,6 +54,8 @@ struct demsph_engine {
     int par = 1;                  // parity of the last successful solid list build
     bool forceWalk = false;       // next contact list from the reference's 27-cell walk
     bool solidSortStale = true;   // solid cells must be recomputed although no solid has mass
+    std::vector<unsigned char> moveKind;  // per solid: 0 clump pebble, 1 integrated, 2 dummy (integrated when moving)
+    std::vector<int> moveHost;            // the device move list
     bool walkOrder[2] = {true, true};  // list of each parity is in the reference's walk order
     bool initialized = false;
     int debug = 0;

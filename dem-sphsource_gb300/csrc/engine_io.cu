@@ -92,6 +92,7 @@ __global__ void kFluidIn(DeviceState d, const double* pos, const double* vel, co
         l.x = ll[0]; l.y = ll[1]; l.z = ll[2];
         d.fph[0][s] = h;
         d.fpl[0][s] = l;
+        rehashFluid(d, s);
     }
     if (vel) {
         const dfl x = df_from_double(vel[3 * id]), y = df_from_double(vel[3 * id + 1]), z = df_from_double(vel[3 * id + 2]);
@@ -113,6 +114,9 @@ __global__ void kSolidIn(DeviceState d, const double* pos, const double* vel, co
         const dfl z = df_from_double(pos[3 * i + 2] - cellOrigin(d, 2, c.z));
         d.sph[i] = make_float4(x.hi, y.hi, z.hi, h.w);
         d.spl[i] = make_float4(x.lo, y.lo, z.lo, l.w);
+        // new key; candidates stale only if the solid moved half a margin
+        checkDisplacement(d, i);
+        rehashSolid(d, i);
     }
     if (vel) {
         const dfl x = df_from_double(vel[3 * i]), y = df_from_double(vel[3 * i + 1]), z = df_from_double(vel[3 * i + 2]);
@@ -329,7 +333,6 @@ int demsph_upload_fluids(demsph_engine* e, const double* pos, const double* vel,
     if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, e->stream));
     if (dr) CK(cudaMemcpyAsync(dr, drho, sizeof(double) * d.nf, cudaMemcpyHostToDevice, e->stream));
     ++t_kernelLaunches, kFluidIn<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, dp, dv, dr);
-    if (dp) CK(cudaMemsetAsync(d.frebuild, 0xff, sizeof(int), e->stream));  // list candidates from the new positions
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)
@@ -340,6 +343,28 @@ int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel,
     ENGINE_GUARD(e)
     DeviceState& d = e->d;
     if (d.ns == 0) return DEMSPH_OK;
+    if (vel) {  // dummy particles given a velocity join the integration
+        std::vector<int> move;
+        move.reserve(e->moveHost.size());
+        for (int i = 0; i < d.ns; ++i) {
+            const unsigned char k = e->moveKind[i];
+            if (k == 1 || (k == 2 && (vel[3 * i] != 0.0 || vel[3 * i + 1] != 0.0 || vel[3 * i + 2] != 0.0)))
+                move.push_back(i);
+        }
+        if (move != e->moveHost) {
+            if (move.size() != e->moveHost.size()) {
+                void* p = d.moveList;
+                freeOne(e, p);
+                d.moveList = dalloc<int>(move.size(), e->owned, e->stream);
+                d.nmove = (int)move.size();
+                dropGraph(e);  // the list is a kernel argument baked into captured graphs
+            }
+            if (!move.empty())
+                CK(cudaMemcpyAsync(d.moveList, move.data(), sizeof(int) * move.size(), cudaMemcpyHostToDevice,
+                                   e->stream));
+            e->moveHost.swap(move);
+        }
+    }
     double* buf = scratchDoubles(e, 9 * (size_t)d.ns);
     double* dp = pos ? buf : nullptr;
     double* dv = vel ? buf + 3 * (size_t)d.ns : nullptr;
@@ -348,11 +373,8 @@ int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel,
     if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     if (dw) CK(cudaMemcpyAsync(dw, angvel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw);
-    if (dp) {
-        CK(cudaMemsetAsync(d.rebuild, 0xff, sizeof(int), e->stream));  // candidates from the new positions
-        if (d.nf > 0) CK(cudaMemsetAsync(d.frebuild, 0xff, sizeof(int), e->stream));
-        e->solidSortStale = true;
-    }
+    // solids that never move are otherwise sorted only once
+    if (dp && e->nMassive == 0) e->solidSortStale = true;
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)

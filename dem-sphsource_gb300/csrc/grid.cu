@@ -139,6 +139,15 @@ __global__ void kSolidHash(DeviceState d, RunIf sortNow)
     }
 }
 
+// Each solid's slot in its cell, on steps that sort (keys computed at the end
+// of the previous step).
+__global__ void kSolidSlots(DeviceState d, RunIf when)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.ns || *d.status || !when.active()) return;
+    d.sslotInCell[i] = atomicAdd(&d.scellCount[d.skey[i]], 1);
+}
+
 __global__ void kSolidRank(DeviceState d, RunIf when)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -193,7 +202,10 @@ static RunIf solidSortWhen(const DeviceState& d, bool force, bool fluidStep)
 void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s)
 {
     if (d.ns <= 0) return;
-    ++t_kernelLaunches, kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d, solidSortWhen(d, force, fluidStep));
+    if (force)  // positions that no integration has hashed (creation, an upload)
+        ++t_kernelLaunches, kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d, solidSortWhen(d, true, fluidStep));
+    else        // keys come from the last integration of the previous step
+        ++t_kernelLaunches, kSolidSlots<<<blocksFor(d.ns, T), T, 0, s>>>(d, solidSortWhen(d, false, fluidStep));
 }
 
 void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s)

@@ -101,6 +101,8 @@ struct DeviceState {
     // A < B of row B.
     int nrow;                // solids that can be in contact (not dummy wall particles)
     int* srow;               // solid -> row, -1 for dummy particles
+    int nmove;               // solids the integration advances: all but clump pebbles (their clump
+    int* moveList;           // moves them) and dummy particles at rest (they never gain velocity)
     int* rowSolid;           // row -> solid
     int4* scentre;           // per row: centre cell of the reference's 27-cell walk at the last hash (exports)
     int scap;                // slots per row
@@ -261,8 +263,10 @@ void launchBonds(const DeviceState& d, int parity, float dt, cudaStream_t s);
 // Contact, bond, wall, coupling and gravity forces of every solid.
 void launchSolidForces(const DeviceState& d, int parity, float dt, cudaStream_t s);
 void launchClumpForce(const DeviceState& d, cudaStream_t s);
-void launchSolidIntegrate(const DeviceState& d, double dt, bool beforeContact, cudaStream_t s);
-void launchStepDone(const DeviceState& d, cudaStream_t s);
+// Half-step integration of all solids; clumpForce: sum the clumps' pebble
+// forces first (instead of launchClumpForce); countStep: count the step.
+void launchSolidIntegrate(const DeviceState& d, double dt, bool before, bool clumpForce, bool countStep,
+                          cudaStream_t s);
 
 // Absolute FP64 position of solid i (cell origin + double-float offset).
 __device__ __forceinline__ double3 solidAbsPos(const DeviceState& d, int i)
@@ -272,6 +276,76 @@ __device__ __forceinline__ double3 solidAbsPos(const DeviceState& d, int i)
     return make_double3(d.minB[0] + c.x * d.cs[0] + ((double)h.x + (double)l.x),
                         d.minB[1] + c.y * d.cs[1] + ((double)h.y + (double)l.y),
                         d.minB[2] + c.z * d.cs[2] + ((double)h.z + (double)l.z));
+}
+
+// After the last drift of a step: once a solid that can touch others has
+// moved half the candidate margin since the candidates were built, the next
+// step rebuilds them.
+__device__ __forceinline__ void checkDisplacement(const DeviceState& d, int i)
+{
+    const int r = d.srow[i];
+    if (r < 0) return;
+    const int4 c = d.scell[i];
+    const float4 h = d.sph[i];
+    const float4 p0 = d.vref[r];
+    const float dx = (float)c.x * d.grid.cs.x + h.x - p0.x, dy = (float)c.y * d.grid.cs.y + h.y - p0.y,
+                dz = (float)c.z * d.grid.cs.z + h.z - p0.z;
+    const float half = 0.5f * d.skin;
+    if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)d.rebuild = 1;
+    if (d.nf > 0) {  // the fluid candidates' solid partners
+        const float4 q0 = d.svref[r];
+        const float ex = (float)c.x * d.grid.cs.x + h.x - q0.x, ey = (float)c.y * d.grid.cs.y + h.y - q0.y,
+                    ez = (float)c.z * d.grid.cs.z + h.z - q0.z;
+        const float fh = 0.5f * d.fskin;
+        if (!(ex * ex + ey * ey + ez * ez <= fh * fh)) *(volatile int*)d.frebuild = 1;
+    }
+}
+
+// Cell key of solid i for the next step's neighbour search, at the end of
+// this step (the position it starts from): the offset is renormalised into its
+// cell, the key and the walk centre stored; a solid that can touch others and
+// has left the domain sends the next lists to the reference's walk.
+__device__ __forceinline__ void rehashSolid(const DeviceState& d, int i)
+{
+    int4 c = d.scell[i];
+    float4 h = d.sph[i], l = d.spl[i];
+    renormAxis(c.x, h.x, l.x, d.grid.csx);
+    renormAxis(c.y, h.y, l.y, d.grid.csy);
+    renormAxis(c.z, h.z, l.z, d.grid.csz);
+    const int key = cellKey(c.x, c.y, c.z, d.grid);
+    c.w = key;
+    d.scell[i] = c;
+    d.sph[i] = h;
+    d.spl[i] = l;
+    d.skey[i] = key;
+    const int row = d.srow[i];
+    if (row >= 0) {
+        d.scentre[row] = make_int4(truncAxis(c.x, h.x, l.x), truncAxis(c.y, h.y, l.y), truncAxis(c.z, h.z, l.z), 0);
+        if (key == d.grid.num - 1) *(volatile int*)d.slowMode = 1;
+    }
+}
+
+
+// The fluid counterpart for fluid slot i: renormalised offset, cell key, the
+// walk once a fluid leaves the domain, and stale list candidates once it has
+// moved half their margin.
+__device__ __forceinline__ void rehashFluid(const DeviceState& d, int i)
+{
+    int4 c = d.fcell[i];
+    float4 h = d.fph[0][i], l = d.fpl[0][i];
+    renormAxis(c.x, h.x, l.x, d.grid.csx);
+    renormAxis(c.y, h.y, l.y, d.grid.csy);
+    renormAxis(c.z, h.z, l.z, d.grid.csz);
+    c.w = cellKey(c.x, c.y, c.z, d.grid);
+    d.fcell[i] = c;
+    d.fph[0][i] = h;
+    d.fpl[0][i] = l;
+    if (c.w == d.grid.num - 1) *(volatile int*)d.fslowMode = 1;
+    const float4 p0 = d.fvref[i];
+    const float dx = (float)c.x * d.grid.cs.x + h.x - p0.x, dy = (float)c.y * d.grid.cs.y + h.y - p0.y,
+                dz = (float)c.z * d.grid.cs.z + h.z - p0.z;
+    const float half = 0.5f * d.fskin;
+    if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)d.frebuild = 1;
 }
 
 inline int blocksFor(long long n, int threads) { return (int)((n + threads - 1) / threads > 0 ? (n + threads - 1) / threads : 1); }
