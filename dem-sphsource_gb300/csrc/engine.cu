@@ -604,6 +604,11 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 CK(cudaMemcpyAsync(d.fdrho[0], drho.data(), sizeof(float) * nf, cudaMemcpyHostToDevice, e->stream));
                 CK(cudaMemcpyAsync(d.facc, acc.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice, e->stream));
                 CK(cudaMemcpyAsync(d.fpar, par.data(), sizeof(float4) * nf, cudaMemcpyHostToDevice, e->stream));
+                d.uniformFluid = 1;
+                for (int i = 1; i < nf && d.uniformFluid; ++i)
+                    d.uniformFluid = par[i].x == par[0].x && par[i].y == par[0].y && par[i].z == par[0].z &&
+                                     par[i].w == par[0].w;
+                d.fparU = par[0];
                 CK(cudaMemcpyAsync(d.fid, id.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, e->stream));
                 CK(cudaMemcpyAsync(d.fslot, id.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, e->stream));
             }

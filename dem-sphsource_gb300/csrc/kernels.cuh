@@ -26,6 +26,8 @@ struct DeviceState {
     // ---- fluid (slots in cell order) ----
     int nf, kff, kfs;
     int lanes;               // threads per fluid particle in the list and pair loops
+    int uniformFluid;        // every fluid particle has the parameters fparU (rest density, sound
+    float4 fparU;            // speed, viscosity, mass)
     int4* fcell;
     float4* fph[2];
     float4* fpl[2];
@@ -210,6 +212,19 @@ int fluidLanes(int nf);
         case 4: kernel<4><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                             \
         case 2: kernel<2><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                             \
         default: kernel<1><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                            \
+        }                                                                                              \
+    } while (0)
+
+// kernel<L, U> for a compile-time flag U.
+#define LAUNCH_LANES_U(kernel, U, L, n, threads, s, ...)                                               \
+    do {                                                                                               \
+        const unsigned blocks_ = (unsigned)blocksFor((long long)(n) * (L), threads);                  \
+        ++t_kernelLaunches;                                                                            \
+        switch (L) {                                                                                   \
+        case 8: kernel<8, U><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                          \
+        case 4: kernel<4, U><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                          \
+        case 2: kernel<2, U><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                          \
+        default: kernel<1, U><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                         \
         }                                                                                              \
     } while (0)
 

@@ -148,7 +148,7 @@ struct ContinuityArgs {
     dfl drift;
 };
 
-template <int L>
+template <int L, bool U>
 __global__ void __launch_bounds__(T) kContinuity(DeviceState d, ContinuityArgs a)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -169,7 +169,9 @@ __global__ void __launch_bounds__(T) kContinuity(DeviceState d, ContinuityArgs a
             const float h = 0.5f * (o.h + pj.w);
             const float r2 = dot3(r, r);
             if (r2 >= 4.f * h * h) continue;
-            const float4 par = d.fpar[j];
+            // U: every fluid particle has the same rest density, sound speed,
+            // viscosity and mass - one gather fewer per neighbour
+            const float4 par = U ? d.fparU : d.fpar[j];
             const float drj = d.fdrho[a.ds][j];
             const float rhoj = par.x + drj;
             const float Pj = drj * par.y * par.y;
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(T) kContinuity(DeviceState d, ContinuityArgs a
 // ---- momentum + kick (dt_f) + drift (dt_f / 2) ----
 // Reads position [1], velocity [0], density [1]; writes acc, velocity [1] and
 // position [0] (the buffers no other thread reads in this pass).
-template <int L>
+template <int L, bool U>
 __global__ void __launch_bounds__(T) kMomentum(DeviceState d, dfl dtf, dfl halfDtf)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -230,7 +232,9 @@ __global__ void __launch_bounds__(T) kMomentum(DeviceState d, dfl dtf, dfl halfD
             const float h = 0.5f * (o.h + pj.w);
             const float r2 = dot3(r, r);
             if (r2 >= 4.f * h * h) continue;
-            const float4 par = d.fpar[j];
+            // U: every fluid particle has the same rest density, sound speed,
+            // viscosity and mass - one gather fewer per neighbour
+            const float4 par = U ? d.fparU : d.fpar[j];
             const float drj = d.fdrho[1][j];
             const float rhoj = par.x + drj;
             const float Pj = drj * par.y * par.y;
@@ -426,13 +430,15 @@ void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStrea
     } else {           // second half step: densities 1 -> 0, velocity 1 -> 0
         a.ps = 0; a.vs = 1; a.ds = 1; a.dd = 0; a.driftTo = -1; a.velCopyTo = 0;
     }
-    LAUNCH_LANES(kContinuity, d.lanes, d.nf, T, s, d, a);
+    if (d.uniformFluid) LAUNCH_LANES_U(kContinuity, true, d.lanes, d.nf, T, s, d, a);
+    else LAUNCH_LANES_U(kContinuity, false, d.lanes, d.nf, T, s, d, a);
 }
 
 void launchMomentumPass(const DeviceState& d, double dtf, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    LAUNCH_LANES(kMomentum, d.lanes, d.nf, T, s, d, df_from_double(dtf), df_from_double(0.5 * dtf));
+    if (d.uniformFluid) LAUNCH_LANES_U(kMomentum, true, d.lanes, d.nf, T, s, d, df_from_double(dtf), df_from_double(0.5 * dtf));
+    else LAUNCH_LANES_U(kMomentum, false, d.lanes, d.nf, T, s, d, df_from_double(dtf), df_from_double(0.5 * dtf));
 }
 
 void launchCoupling(const DeviceState& d, int src, cudaStream_t s)

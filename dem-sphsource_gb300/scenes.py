@@ -411,6 +411,19 @@ def tiny_granular(seed=3, with_probe_fluid=True):
     return r
 
 
+def tiny_two_fluids(seed=6):
+    """:func:`tiny_dam_break` with a second, denser column beside the first
+    (its own rest density, sound speed and smoothing length)."""
+    r = tiny_dam_break(seed)
+    rng = np.random.default_rng(seed)
+    dx = 0.02
+    fp = regular_packed_points((0.16, 0.0, 0.0), (0.08, 0.12, 0.08), dx)
+    fp = fp + rng.uniform(-0.01 * dx, 0.01 * dx, size=fp.shape)
+    r.addFluid(fp, (0, 0, 0), 1.2 * dx, 1500.0, 25.0, 2.0e-6)
+    r.name = "tiny_two_fluids"
+    return r
+
+
 def tiny_escape(seed=5):
     """64 spheres on a floor wall (no side walls) and two touching spheres
     above the domain: the reference hashes those to its overflow cell

@@ -29,7 +29,7 @@ import conftest  # noqa: E402  (loads the package)
 from oracle.refrun import FIELDS, RefSolver  # noqa: E402
 
 SNAP_STEPS = (0, 1, 2, 5, 10)
-SCENES = ("tiny_dam_break", "tiny_granular", "tiny_coupled", "tiny_escape")
+SCENES = ("tiny_dam_break", "tiny_granular", "tiny_coupled", "tiny_escape", "tiny_two_fluids")
 
 
 def scene_digest(scene):

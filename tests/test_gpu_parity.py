@@ -12,7 +12,7 @@ from parity import (DRHO_TOL, DRIFT_TOL, FORCE_TOL, POS_TOL, compare_integer_art
 
 pytestmark = pytest.mark.gpu
 
-SCENES = ("tiny_dam_break", "tiny_granular", "tiny_coupled", "tiny_escape")
+SCENES = ("tiny_dam_break", "tiny_granular", "tiny_coupled", "tiny_escape", "tiny_two_fluids")
 # solid contact candidates: default margin, one so small that candidates are
 # rebuilt nearly every step, and none (the 27-cell walk every step)
 SKINS = (0.0, 1.0e-9, -1.0)
