@@ -282,7 +282,7 @@ def run_many(args, world, rank, local):
         recipes = rank_share(sc.batch_mix(n_scenes=args.scenes, steps=steps), rank, world)
         built = [ds.build_scene(r) for r in recipes]
         total = sum(scene_updates(s, steps) for _, s in built)
-        srv = ds.Server(device=device, workers=args.workers, hbm_budget_bytes=budget)
+        srv = ds.Server(device=device, workers=args.workers, hbm_budget_bytes=budget, autotune=True)
         if dist:
             dist.barrier()
         with ClockSampler(device) as clocks:
@@ -299,7 +299,7 @@ def run_many(args, world, rank, local):
         # plain: a spaced sample of the same scenes, one at a time, same engine path
         k = max(1, len(built) // max(1, args.plain_scenes))
         sample = built[::k][:args.plain_scenes]
-        plain = ds.Server(device=device, workers=1, hbm_budget_bytes=budget)
+        plain = ds.Server(device=device, workers=1, hbm_budget_bytes=budget, autotune=True)
         p_upd = sum(scene_updates(s, steps) for _, s in sample)
         t1 = time.perf_counter()
         for _, s in sample:
@@ -319,6 +319,7 @@ def run_many(args, world, rank, local):
                                       "breaks, fluid counts log-uniform in [2k, 60k], column heights uniform in "
                                       f"[0.2, 0.5] m, {steps} steps each, through the scene server",
                        "workers": args.workers, "hbm_budget_bytes": budget,
+                       "autotune": "threads per fluid particle timed per size class (demsph_autotune)",
                        "timing": "host wall clock from the first submission to the last completion (engine "
                                  "creation and initialisation included)"},
             "impl": "ours", "batched": {"value": value, "wall_s": wall, "p50_step_ms": st["p50_step_ms"],
@@ -337,7 +338,7 @@ def run_many(args, world, rank, local):
 
     # config 4: serving
     arrivals = rank_share(sc.serving_stream(duration=args.duration), rank, world)
-    srv = ds.Server(device=device, workers=args.workers, hbm_budget_bytes=budget)
+    srv = ds.Server(device=device, workers=args.workers, hbm_budget_bytes=budget, autotune=True)
     if dist:
         dist.barrier()
     lag = []

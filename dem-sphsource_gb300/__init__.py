@@ -82,7 +82,8 @@ class AuditValues(C.Structure):
 class ServerConfig(C.Structure):
     """ctypes mirror of ``demsph_server_config``."""
 
-    _fields_ = [("device", _I), ("workers", _I), ("chunk_steps", _I), ("hbm_budget_bytes", C.c_longlong)]
+    _fields_ = [("device", _I), ("workers", _I), ("chunk_steps", _I), ("hbm_budget_bytes", C.c_longlong),
+                ("autotune", _I)]
 
 
 class ServerSummary(C.Structure):
@@ -437,6 +438,13 @@ class Engine:
                 "rotational_energy": a.rotational_energy, "potential_energy": a.potential_energy,
                 "fluid_density_sum": a.fluid_density_sum}
 
+    def autotune(self):
+        """Times the fluid pair loop with 1, 2, 4 and 8 threads per particle and
+        keeps the fastest (demsph_autotune); returns the choice."""
+        lanes = _I()
+        self._chk(self.lib.demsph_autotune(self.h, C.byref(lanes)), "autotune")
+        return lanes.value
+
     def solid_pairs(self):
         prefix = np.zeros(self.ns, np.int32)
         self._chk(self.lib.demsph_export_solid_pairs(self.h, _ptr(prefix, _IP), *([None] * 7), C.c_longlong(0)), "ss")
@@ -479,9 +487,9 @@ class Server:
 
     STATES = ("pending", "running", "done", "failed")
 
-    def __init__(self, device=0, workers=0, chunk_steps=0, hbm_budget_bytes=0):
+    def __init__(self, device=0, workers=0, chunk_steps=0, hbm_budget_bytes=0, autotune=False):
         self.lib = load_library()
-        cfg = ServerConfig(device, workers, chunk_steps, int(hbm_budget_bytes))
+        cfg = ServerConfig(device, workers, chunk_steps, int(hbm_budget_bytes), 1 if autotune else 0)
         h = _P()
         rc = self.lib.demsph_server_create(C.byref(cfg), C.byref(h))
         if rc != DEMSPH_OK:

@@ -1090,6 +1090,45 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
     ENGINE_END(e)
 }
 
+// Threads per fluid particle, chosen by timing: the first continuity pass
+// (it reads the step's state and writes only buffers the next fluid step
+// overwrites) is timed with 1, 2, 4 and 8 lanes, and the fastest is kept for
+// every fluid list and pair kernel.
+int demsph_autotune(demsph_engine* e, int* lanes_out)
+{
+    ENGINE_GUARD(e)
+    REQUIRE_INIT(e);
+    DeviceState& d = e->d;
+    if (d.nf > 0) {
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        float best = 0.f;
+        int bestL = d.lanes;
+        for (int L = 1; L <= 8; L *= 2) {
+            d.lanes = L;
+            launchContinuityPass(d, 0, 1.0e-9, e->stream);  // warm-up
+            CK(cudaEventRecord(a, e->stream));
+            for (int r = 0; r < 5; ++r) launchContinuityPass(d, 0, 1.0e-9, e->stream);
+            CK(cudaEventRecord(b, e->stream));
+            CK(cudaEventSynchronize(b));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, a, b));
+            if (L == 1 || ms < best) {
+                best = ms;
+                bestL = L;
+            }
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        d.lanes = bestL;
+        dropGraph(e);  // the lane count is baked into captured launches
+    }
+    if (lanes_out) *lanes_out = d.lanes;
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
 void* demsph_stream(demsph_engine* e) { return e ? (void*)e->stream : nullptr; }
 
 long long demsph_device_bytes(const demsph_engine* e)

@@ -136,6 +136,7 @@ struct demsph_server {
     std::vector<double> stepMs;   // per chunk: milliseconds per step
     long long updates = 0, completed = 0, failed = 0, submittedN = 0, admittedN = 0, stepsRun = 0;
     double createS = 0, stepS = 0, downloadS = 0;   // worker time by activity
+    std::map<int, int> lanesByClass;   // autotuned threads per fluid particle by log2(fluid count)
     bool anyAdmitted = false;
     Clock::time_point firstAdmit, lastFinish;
 
@@ -196,8 +197,23 @@ struct demsph_server {
             double tCreate = 0, tStep = 0, tDown = 0;
             if (!r->eng) {
                 const auto t0 = Clock::now();
+                int cls = -1, known = 0;
+                if (cfg.autotune && r->scene->s.n_fluid > 0) {
+                    cls = 0;
+                    while ((2LL << cls) <= r->scene->s.n_fluid) ++cls;
+                    std::lock_guard<std::mutex> g(m);
+                    auto it = lanesByClass.find(cls);
+                    if (it != lanesByClass.end()) known = it->second;
+                }
+                if (known) r->opt.fluid_lanes = known;
                 rc = demsph_create(&r->scene->s, &r->opt, &r->eng);
                 if (rc == DEMSPH_OK) rc = demsph_initialize(r->eng);
+                if (rc == DEMSPH_OK && cls >= 0 && !known) {
+                    int lanes = 0;
+                    rc = demsph_autotune(r->eng, &lanes);
+                    std::lock_guard<std::mutex> g(m);
+                    if (rc == DEMSPH_OK) lanesByClass.emplace(cls, lanes);
+                }
                 tCreate = seconds(t0, Clock::now());
             }
             int n = 0;

@@ -232,6 +232,11 @@ DEMSPH_API int demsph_solid_integrate_after_contact(demsph_engine* e, double dt)
    for i_step = first_step .. first_step+n_steps-1, without the driver hook;
    replayed as a CUDA graph when use_graph != 0. */
 DEMSPH_API int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph);
+/* Chooses the threads per fluid particle of the fluid list and pair kernels
+   (1, 2, 4 or 8) by timing the first continuity pass with each; call after
+   demsph_initialize.  *lanes_out receives the choice (may be NULL).  No
+   counterpart in the reference. */
+DEMSPH_API int demsph_autotune(demsph_engine* e, int* lanes_out);
 /* The CUDA stream (cudaStream_t) the engine issues all its work on, for
    callers that time or order work around it. */
 DEMSPH_API void* demsph_stream(demsph_engine* e);
@@ -326,6 +331,8 @@ typedef struct demsph_server_config {
     int workers;                 /* host threads advancing scenes; 0 = 16 */
     int chunk_steps;             /* steps per turn of a scene; 0 = 100 */
     long long hbm_budget_bytes;  /* device memory the admitted scenes may hold; 0 = 150 GiB */
+    int autotune;                /* != 0: the first scene of each size class (fluid count within a
+                                    factor of 2) runs demsph_autotune, later ones reuse its choice */
 } demsph_server_config;
 typedef struct demsph_server_summary {
     long long submitted, admitted, completed, failed, pending;
