@@ -224,6 +224,7 @@ __device__ __forceinline__ void addDF3(float4& h, float4& l, float3 dv)
 
 __global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
 {
+    stepKernelBegin();
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= d.nb || *d.status) return;
     if (d.bon[b] == 0) {
@@ -316,53 +317,140 @@ __device__ __forceinline__ float wallOverlap(const DeviceState& d, int4 c, float
     return del.hi + del.lo;
 }
 
+// Position of the r-th (from 0) set bit of m; m has more than r set bits.
+__device__ __forceinline__ int nthSetBit(unsigned m, int r)
+{
+    int p = 0;
+#pragma unroll
+    for (int w = 16; w > 0; w >>= 1) {
+        const unsigned low = m & ((1u << w) - 1u);
+        const int c = __popc(low);
+        if (r >= c) {
+            r -= c;
+            m >>= w;
+            p += w;
+        } else {
+            m = low;
+        }
+    }
+    return p;
+}
+
 // Force and torque on every solid that can touch others (calSolidForceTorque,
 // core/integrate.cu:806-858, with the contact forces of :423-512, the bonds of
 // :717-804 and the walls of :514-610), one thread per row: each contact is
 // evaluated by both of its solids (pairForce, the same bits on both sides) -
 // the forward side also advances the springs - so no per-pair forces are
 // gathered.  Sums are Kahan-compensated, in index order.
-__global__ void __launch_bounds__(T) kSolidForces(DeviceState d, int par, float dt, int withCoupling)
+//
+// Rows hold few contacts and their counts vary, so a warp does not loop over
+// its rows' contacts lane by lane: it numbers the (row, contact) items of its
+// 32 rows level by level (every row's contact 0, then every row's contact 1,
+// ..., so neighbouring items are neighbouring rows of the same slot and their
+// slot arrays are read and written in whole lines) and evaluates them 32 at a
+// time, every lane on one item; each row's lane then adds the results of its
+// own items, in order, from shared memory.
+__global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, float dt, int withCoupling)
 {
+    stepKernelBegin();
+    __shared__ float4 itemF[T], itemT[T];  // 32 items per warp
+    if (*d.status) return;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= d.nrow || *d.status) return;
-    const int a = d.rowSolid[row];
-    const int4 fa = d.sflags[a];
+    const int row0 = row - lane;
+    const bool live = row < d.nrow;
+    const int a = live ? d.rowSolid[row] : 0;
     const size_t nr = (size_t)d.nrow;
+    // forward contacts (a, b) come first, then reverse ones (b, a)
+    const int n = live ? min(d.fcnt[par][row], d.scap) : 0;
+    const int total = live ? n + min(d.rcnt[row], d.scap) : 0;
+    const int levels = __reduce_max_sync(FULL, total);
+    float4* resF = itemF + (threadIdx.x & ~31);
+    float4* resT = itemT + (threadIdx.x & ~31);
     KahanF3 F, Tq;
-    // forward contacts (a, b), then reverse ones (b, a), through ONE inlined
-    // copy of pairForce: a pair's two solids run the same instructions on the
-    // same inputs and get the same bits
-    const int n = min(d.fcnt[par][row], d.scap);
-    const int total = n + min(d.rcnt[row], d.scap);
-    for (int q = 0; q < total; ++q) {
-        const bool fwdSide = q < n;
-        int A = a, B;
-        long long k;
-        if (fwdSide) {
-            k = (long long)q * nr + row;
-            B = d.fwd[par][k];
-        } else {
-            A = d.rev[(size_t)(q - n) * nr + row];
-            B = a;
-            k = forwardSlot(d, par, A, a);
-            if (k < 0) continue;
+    for (int L0 = 0; L0 < levels; L0 += 32) {
+        // lane j describes level L0 + j: the rows holding an item there, and
+        // the number of the level's first item
+        unsigned rows = 0;
+        for (int q = L0; q < min(L0 + 32, levels); ++q) {
+            const unsigned m = __ballot_sync(FULL, total > q);
+            if (lane == q - L0) rows = m;
         }
-        float3 es = xyz(d.springIn[0][k]), er = xyz(d.springIn[1][k]), et = xyz(d.springIn[2][k]);
-        const PairForce p = pairForce(d, A, B, es, er, et, dt);
-        if (fwdSide) {
-            d.springOut[0][k] = f4(es);
-            d.springOut[1][k] = f4(er);
-            d.springOut[2][k] = f4(et);
-            d.pF[k] = f4(p.F);
-            d.pT[k] = f4(p.T);
-            F.add(p.F);
-            Tq.add(p.TA);
-        } else {
-            F.add(-p.F);
-            Tq.add(-p.TB);
+        const int cnt = __popc(rows);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int first = incl - cnt, items = __shfl_sync(FULL, incl, 31);
+        for (int c0 = 0; c0 < items; c0 += 32) {
+            const int idx = c0 + lane;
+            // the item's level: the last lane whose first item is at or before it
+            int lv = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (__shfl_sync(FULL, first, lv + step) <= idx) lv += step;
+            const unsigned lrows = __shfl_sync(FULL, rows, lv);
+            const int owner = nthSetBit(lrows, idx - __shfl_sync(FULL, first, lv)) & 31;
+            const int oa = __shfl_sync(FULL, a, owner), on = __shfl_sync(FULL, n, owner);
+            const int q = L0 + lv, orow = row0 + owner;
+            float4 rF = make_float4(0.f, 0.f, 0.f, 0.f), rT = rF;
+            if (idx < items) {
+                // through ONE inlined copy of pairForce: a pair's two solids run the
+                // same instructions on the same inputs and get the same bits
+                const bool fwdSide = q < on;
+                int A = oa, B;
+                long long k;
+                if (fwdSide) {
+                    k = (long long)q * nr + orow;
+                    B = d.fwd[par][k];
+                } else {
+                    A = d.rev[(size_t)(q - on) * nr + orow];
+                    B = oa;
+                    k = forwardSlot(d, par, A, oa);
+                }
+                if (k >= 0) {
+                    float3 es = xyz(d.springIn[0][k]), er = xyz(d.springIn[1][k]), et = xyz(d.springIn[2][k]);
+                    const PairForce p = pairForce(d, A, B, es, er, et, dt);
+                    if (fwdSide) {
+                        d.springOut[0][k] = f4(es);
+                        d.springOut[1][k] = f4(er);
+                        d.springOut[2][k] = f4(et);
+                        d.pF[k] = f4(p.F);
+                        d.pT[k] = f4(p.T);
+                        rF = make_float4(p.F.x, p.F.y, p.F.z, 1.f);
+                        rT = f4(p.TA);
+                    } else {
+                        const float3 mF = -p.F, mT = -p.TB;
+                        rF = make_float4(mF.x, mF.y, mF.z, 1.f);
+                        rT = f4(mT);
+                    }
+                }
+            }
+            resF[lane] = rF;
+            resT[lane] = rT;
+            __syncwarp();
+            // each row adds its items of this chunk, level by level (its contact order)
+            const int lvLo = __shfl_sync(FULL, lv, 0), lvHi = __shfl_sync(FULL, lv, min(31, items - 1 - c0));
+            for (int l = lvLo; l <= lvHi; ++l) {
+                const unsigned m = __shfl_sync(FULL, rows, l);
+                const int pos = __shfl_sync(FULL, first, l) + __popc(m & below) - c0;
+                if ((m >> lane & 1u) && pos >= 0 && pos < 32) {
+                    const float4 f = resF[pos];
+                    if (f.w != 0.f) {  // 0: a reverse pair the forward row does not hold
+                        F.add(xyz(f));
+                        Tq.add(xyz(resT[pos]));
+                    }
+                }
+            }
+            __syncwarp();
         }
     }
+    if (!live) return;
+    const int4 fa = d.sflags[a];
     for (int q = d.bondStart[a], qe = d.bondStart[a + 1]; q < qe; ++q) {
         const int bi = d.bondList[q];
         if (d.bab[bi].x == a) {
@@ -386,7 +474,7 @@ __global__ void __launch_bounds__(T) kSolidForces(DeviceState d, int par, float 
         const float4 rad = d.srad[a];
         const float3 v = xyz(d.svh[a]), w = xyz(d.swh[a]);
         for (int k = 0; k < d.nw; ++k) {
-            const size_t h = (size_t)a * d.nw + k;
+            const size_t h = (size_t)k * d.ns + a;  // wall-major: a warp's solids are adjacent
             const float delta = wallOverlap(d, ca, ph, pl, k, rad.x, rad.y);
             if (delta < 0.f) {
                 d.wspring[0][h] = d.wspring[1][h] = d.wspring[2][h] = make_float4(0, 0, 0, 0);
@@ -475,54 +563,85 @@ __device__ __forceinline__ void clumpForceGroup(const DeviceState& d, int width,
     }
 }
 
+// Double-float x += v dt for one position (hi/lo float4 pairs, w kept).
+__device__ __forceinline__ void driftRegs(float4& h, float4& l, float4 vh, float4 vl, dfl dt)
+{
+    const dfl x = df_add(df_make(h.x, l.x), df_mul(df_make(vh.x, vl.x), dt));
+    const dfl y = df_add(df_make(h.y, l.y), df_mul(df_make(vh.y, vl.y), dt));
+    const dfl z = df_add(df_make(h.z, l.z), df_mul(df_make(vh.z, vl.z), dt));
+    h = make_float4(x.hi, y.hi, z.hi, h.w);
+    l = make_float4(x.lo, y.lo, z.lo, l.w);
+}
+
 // double-float x += v dt for one particle's position (solid arrays).
 __device__ __forceinline__ void driftSolid(const DeviceState& d, int i, dfl dt)
 {
     float4 h = d.sph[i], l = d.spl[i];
-    const float4 vh = d.svh[i], vl = d.svl[i];
-    const dfl x = df_add(df_make(h.x, l.x), df_mul(df_make(vh.x, vl.x), dt));
-    const dfl y = df_add(df_make(h.y, l.y), df_mul(df_make(vh.y, vl.y), dt));
-    const dfl z = df_add(df_make(h.z, l.z), df_mul(df_make(vh.z, vl.z), dt));
-    d.sph[i] = make_float4(x.hi, y.hi, z.hi, h.w);
-    d.spl[i] = make_float4(x.lo, y.lo, z.lo, l.w);
+    driftRegs(h, l, d.svh[i], d.svl[i], dt);
+    d.sph[i] = h;
+    d.spl[i] = l;
 }
 
-// solidVelocityAngularVelocityIntegrate (integrate.cu:883-897) for one particle.
-__device__ __forceinline__ void kickSolid(const DeviceState& d, int i, dfl dt, int4 f)
+// solidVelocityAngularVelocityIntegrate (integrate.cu:883-897) for one
+// particle: v += a dt, and w += T / (0.4 m r^2) dt unless it is fixed or has
+// no radius (spin false).
+__device__ __forceinline__ void kickRegs(float4& vh, float4& vl, float4& wh, float4& wl, float3 a, float3 tq, float r,
+                                         float im, bool spin, dfl dt)
 {
-    const float3 a = xyz(d.sacc[i]);
-    const float4 vh = d.svh[i], vl = d.svl[i];
     {
         const dfl x = df_add(df_make(vh.x, vl.x), df_mul_f(dt, a.x));
         const dfl y = df_add(df_make(vh.y, vl.y), df_mul_f(dt, a.y));
         const dfl z = df_add(df_make(vh.z, vl.z), df_mul_f(dt, a.z));
-        d.svh[i] = make_float4(x.hi, y.hi, z.hi, vh.w);
-        d.svl[i] = make_float4(x.lo, y.lo, z.lo, vl.w);
+        vh = make_float4(x.hi, y.hi, z.hi, vh.w);
+        vl = make_float4(x.lo, y.lo, z.lo, vl.w);
     }
-    const float r = d.srad[i].x;
-    const float im = d.sph[i].w;
-    if ((f.w & F_FIXED) || r < 1.e-10f) return;
-    const float3 alpha = xyz(d.storque[i]) * (im / (0.4f * r * r));
-    float4 wh = d.swh[i], wl = d.swl[i];
+    if (!spin) return;
+    const float3 alpha = tq * (im / (0.4f * r * r));
     const dfl x = df_add(df_make(wh.x, wl.x), df_mul_f(dt, alpha.x));
     const dfl y = df_add(df_make(wh.y, wl.y), df_mul_f(dt, alpha.y));
     const dfl z = df_add(df_make(wh.z, wl.z), df_mul_f(dt, alpha.z));
-    d.swh[i] = make_float4(x.hi, y.hi, z.hi, wh.w);
-    d.swl[i] = make_float4(x.lo, y.lo, z.lo, wl.w);
+    wh = make_float4(x.hi, y.hi, z.hi, wh.w);
+    wl = make_float4(x.lo, y.lo, z.lo, wl.w);
 }
 
+// One half-step of a solid that is not a clump pebble (integrate.cu:964-1027):
+// before contact kick then drift; after contact drift, kick, the displacement
+// check and the cell key of the next step.  Every input is read before
+// anything is written: the compiler cannot tell the arrays apart, so a read
+// placed after a write would wait for it.
 __device__ __forceinline__ void solidIntegrateOne(const DeviceState& d, int i, dfl half, int before)
 {
     const int4 f = d.sflags[i];
+    float4 ph = d.sph[i], pl = d.spl[i], vh = d.svh[i], vl = d.svl[i], wh = d.swh[i], wl = d.swl[i];
+    const float3 a = xyz(d.sacc[i]), tq = xyz(d.storque[i]);
+    const float r = d.srad[i].x;
+    int row = -1;
+    int4 c = make_int4(0, 0, 0, 0);
+    float4 p0 = make_float4(0, 0, 0, 0), q0 = p0;
+    if (!before) {
+        row = d.srow[i];
+        c = d.scell[i];
+        p0 = d.vref[i];
+        if (d.nf > 0) q0 = d.svref[i];
+    }
     if (f.z >= 0) return;  // clump pebbles: clumpIntegrateGroup
+    const bool spin = !((f.w & F_FIXED) || r < 1.e-10f);
     if (before) {
-        kickSolid(d, i, half, f);
-        driftSolid(d, i, half);
+        kickRegs(vh, vl, wh, wl, a, tq, r, ph.w, spin, half);
+        driftRegs(ph, pl, vh, vl, half);
+        d.sph[i] = ph;
+        d.spl[i] = pl;
     } else {
-        driftSolid(d, i, half);
-        kickSolid(d, i, half, f);
-        checkDisplacement(d, i);
-        rehashSolid(d, i);
+        driftRegs(ph, pl, vh, vl, half);
+        kickRegs(vh, vl, wh, wl, a, tq, r, ph.w, spin, half);
+        checkDisplacementOf(d, row, c, ph, p0, q0);
+        rehashSolidOf(d, i, row, c, ph, pl);
+    }
+    d.svh[i] = vh;
+    d.svl[i] = vl;
+    if (spin) {
+        d.swh[i] = wh;
+        d.swl[i] = wl;
     }
 }
 
@@ -664,6 +783,7 @@ __device__ __forceinline__ void clumpIntegrateGroup(const DeviceState& d, dfl ha
 
 __global__ void kClumpForce(DeviceState d, int width)
 {
+    stepKernelBegin();
     clumpForceGroup(d, width, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -676,6 +796,7 @@ __global__ void kClumpForce(DeviceState d, int width)
 __global__ void kIntegrate(DeviceState d, dfl half, int before, int width, int solidBlocks, int clumpForce,
                            int countStep)
 {
+    stepKernelBegin();
     if (countStep && blockIdx.x == 0 && threadIdx.x == 0 && *d.status == 0) atomicAdd(d.stepsDone, 1);
     if ((int)blockIdx.x < solidBlocks) {
         const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -695,18 +816,18 @@ __global__ void kIntegrate(DeviceState d, dfl half, int before, int width, int s
 void launchBonds(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.nb <= 0) return;
-    ++t_kernelLaunches, kBonds<<<blocksFor(d.nb, T), T, 0, s>>>(d, par, dt);
+    launchStep(kBonds, blocksFor(d.nb, T), T, s, d, par, dt);
 }
 void launchSolidForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    ++t_kernelLaunches, kSolidForces<<<blocksFor(d.nrow, T), T, 0, s>>>(d, par, dt, d.nf > 0 ? 1 : 0);
+    launchStep(kSolidForces, blocksFor(d.nrow, T), T, s, d, par, dt, d.nf > 0 ? 1 : 0);
 }
 void launchClumpForce(const DeviceState& d, cudaStream_t s)
 {
     if (d.nc <= 0) return;
     const int w = d.clumpLanes;
-    ++t_kernelLaunches, kClumpForce<<<blocksFor((long long)d.nc * w, 256), 256, 0, s>>>(d, w);
+    launchStep(kClumpForce, blocksFor((long long)d.nc * w, 256), 256, s, d, w);
 }
 void launchSolidIntegrate(const DeviceState& d, double dt, bool before, bool clumpForce, bool countStep,
                           cudaStream_t s)
@@ -715,8 +836,7 @@ void launchSolidIntegrate(const DeviceState& d, double dt, bool before, bool clu
     const int sb = d.nmove > 0 ? blocksFor(d.nmove, 256) : 0;
     const int cb = d.nc > 0 ? blocksFor((long long)d.nc * d.clumpLanes, 256) : 0;
     if (sb + cb == 0 && !countStep) return;
-    ++t_kernelLaunches, kIntegrate<<<std::max(1, sb + cb), 256, 0, s>>>(d, h, before ? 1 : 0, d.clumpLanes, sb,
-                                                                       clumpForce ? 1 : 0, countStep ? 1 : 0);
+    launchStep(kIntegrate, std::max(1, sb + cb), 256, s, d, h, before ? 1 : 0, d.clumpLanes, sb, clumpForce ? 1 : 0, countStep ? 1 : 0);
 }
 
 

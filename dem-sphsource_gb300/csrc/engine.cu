@@ -21,6 +21,7 @@
 // grows the list and re-runs from the first incomplete step.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -30,6 +31,15 @@
 #include "engine_impl.cuh"
 
 namespace demsph {
+
+bool overlapLaunches()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("DEMSPH_OVERLAP_LAUNCHES");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
 
 void freeOne(demsph_engine* e, void*& p)
 {
@@ -713,8 +723,8 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.vcap = 2 * perParticle;
             d.vcand = dalloc<int>((size_t)d.vcap * nr, e->owned, e->stream, false);
             d.vcnt = dalloc<int>(nr, e->owned, e->stream);
-            d.vref = dalloc<float4>(nr, e->owned, e->stream);
-            d.svref = dalloc<float4>(nr, e->owned, e->stream);
+            d.vref = dalloc<float4>(ns, e->owned, e->stream);
+            d.svref = dalloc<float4>(ns, e->owned, e->stream);
             d.rebuild = dalloc<int>(1, e->owned, e->stream);
             d.slowMode = dalloc<int>(1, e->owned, e->stream);
             d.need = dalloc<int>(4, e->owned, e->stream);

@@ -26,6 +26,7 @@ constexpr int T = 256;
 // particle is copied into the gather sources and takes a slot in its cell.
 __global__ void kFluidHash(DeviceState d, RunIf sortNow)
 {
+    stepKernelBegin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.nf || *d.status) return;
     int4 c = d.fcell[i];
@@ -66,6 +67,7 @@ __global__ void kFluidHash(DeviceState d, RunIf sortNow)
 __global__ void kScatter(int n, const int* __restrict__ key, const int* __restrict__ slotInCell,
                          const int* __restrict__ cellStart, int* __restrict__ out, const int* status, RunIf when)
 {
+    stepKernelBegin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || *status || !when.active()) return;
     out[cellStart[key[i]] + slotInCell[i]] = i;
@@ -90,6 +92,7 @@ __device__ __forceinline__ int stableRank(int p, const int* __restrict__ sorted,
 
 __global__ void kFluidGather(DeviceState d, RunIf when)
 {
+    stepKernelBegin();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.nf || *d.status || !when.active()) return;
     int e;
@@ -113,6 +116,7 @@ __global__ void kFluidGather(DeviceState d, RunIf when)
 // objectHash); the atomic slots only when the sort follows.
 __global__ void kSolidHash(DeviceState d, RunIf sortNow)
 {
+    stepKernelBegin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.ns || *d.status) return;
     int4 c = d.scell[i];
@@ -143,6 +147,7 @@ __global__ void kSolidHash(DeviceState d, RunIf sortNow)
 // of the previous step).
 __global__ void kSolidSlots(DeviceState d, RunIf when)
 {
+    stepKernelBegin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.ns || *d.status || !when.active()) return;
     d.sslotInCell[i] = atomicAdd(&d.scellCount[d.skey[i]], 1);
@@ -150,6 +155,7 @@ __global__ void kSolidSlots(DeviceState d, RunIf when)
 
 __global__ void kSolidRank(DeviceState d, RunIf when)
 {
+    stepKernelBegin();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= d.ns || *d.status || !when.active()) return;
     int e;
@@ -172,7 +178,7 @@ static RunIf fluidReorderWhen(const DeviceState& d, bool force)
 void launchFluidHash(const DeviceState& d, bool force, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    ++t_kernelLaunches, kFluidHash<<<blocksFor(d.nf, T), T, 0, s>>>(d, fluidReorderWhen(d, force));
+    launchStep(kFluidHash, blocksFor(d.nf, T), T, s, d, fluidReorderWhen(d, force));
 }
 
 void launchFluidReorder(const DeviceState& d, bool force, cudaStream_t s)
@@ -182,8 +188,8 @@ void launchFluidReorder(const DeviceState& d, bool force, cudaStream_t s)
     // reorder, and by the host after a step abandoned in kFluidHash
     const RunIf when = fluidReorderWhen(d, force);
     scanExclusive(d.fcellCount, d.fcellStart, d.grid.num, d.scanWork, s, when);
-    ++t_kernelLaunches, kScatter<<<blocksFor(d.nf, T), T, 0, s>>>(d.nf, d.fkey, d.fslotInCell, d.fcellStart, d.fsortTmp, d.status, when);
-    ++t_kernelLaunches, kFluidGather<<<blocksFor(d.nf, T), T, 0, s>>>(d, when);
+    launchStep(kScatter, blocksFor(d.nf, T), T, s, d.nf, d.fkey, d.fslotInCell, d.fcellStart, d.fsortTmp, d.status, when);
+    launchStep(kFluidGather, blocksFor(d.nf, T), T, s, d, when);
 }
 
 static RunIf solidSortWhen(const DeviceState& d, bool force, bool fluidStep)
@@ -203,9 +209,9 @@ void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, cudaStrea
 {
     if (d.ns <= 0) return;
     if (force)  // positions that no integration has hashed (creation, an upload)
-        ++t_kernelLaunches, kSolidHash<<<blocksFor(d.ns, T), T, 0, s>>>(d, solidSortWhen(d, true, fluidStep));
+        launchStep(kSolidHash, blocksFor(d.ns, T), T, s, d, solidSortWhen(d, true, fluidStep));
     else        // keys come from the last integration of the previous step
-        ++t_kernelLaunches, kSolidSlots<<<blocksFor(d.ns, T), T, 0, s>>>(d, solidSortWhen(d, false, fluidStep));
+        launchStep(kSolidSlots, blocksFor(d.ns, T), T, s, d, solidSortWhen(d, false, fluidStep));
 }
 
 void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s)
@@ -215,8 +221,8 @@ void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStrea
     // sort, and by the host after a step abandoned in kSolidHash
     const RunIf when = solidSortWhen(d, force, fluidStep);
     scanExclusive(d.scellCount, d.scellStart, d.grid.num, d.scanWork, s, when);
-    ++t_kernelLaunches, kScatter<<<blocksFor(d.ns, T), T, 0, s>>>(d.ns, d.skey, d.sslotInCell, d.scellStart, d.ssortTmp, d.status, when);
-    ++t_kernelLaunches, kSolidRank<<<blocksFor(d.ns, T), T, 0, s>>>(d, when);
+    launchStep(kScatter, blocksFor(d.ns, T), T, s, d.ns, d.skey, d.sslotInCell, d.scellStart, d.ssortTmp, d.status, when);
+    launchStep(kSolidRank, blocksFor(d.ns, T), T, s, d, when);
 }
 
 }  // namespace demsph

@@ -12,6 +12,43 @@ namespace demsph {
 // the engine turns deltas of it into the launch count of a run.
 inline thread_local long long t_kernelLaunches = 0;
 
+// Programmatic dependent launch.  The step's kernels are launched with
+// programmatic stream serialisation, so a kernel's blocks may be scheduled
+// while the kernel before it on the stream is still running, hiding the
+// launch gap between the ~10 short kernels of a step.  Every such kernel
+// therefore opens with stepKernelBegin(): griddepcontrol.wait holds the block
+// until the previous grid has completed and its writes are visible (before
+// this block reads or writes anything), then launch_dependents lets the next
+// kernel be scheduled.  A kernel launched without the attribute passes both
+// instructions at once.
+__device__ __forceinline__ void stepKernelBegin()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Whether step kernels overlap their launch with the previous kernel
+// (default on; DEMSPH_OVERLAP_LAUNCHES=0 in the environment turns it off).
+bool overlapLaunches();
+
+// Launches a step kernel (one that opens with stepKernelBegin) on stream s.
+template <typename... KArgs, typename... Args>
+inline void launchStep(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args)
+{
+    ++t_kernelLaunches;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = overlapLaunches() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 struct DeviceState {
     GridDev grid;
     double minB[3], cs[3];   // FP64 grid, for import and export
@@ -58,7 +95,7 @@ struct DeviceState {
     int* fvsc;               // [k * nf + i] solid indices
     int* fvsn;
     float4* fvref;           // per fluid slot: position (from the grid origin) at the rebuild
-    float4* svref;           // per solid row: the same
+    float4* svref;           // per solid (those with a contact row): the same
     float fskin;
     float fhmax;             // largest fluid smoothing length
     int* frebuild;           // 1: fluid candidates are stale (a fluid or solid moved fskin / 2)
@@ -122,7 +159,8 @@ struct DeviceState {
     int vcap;
     int* vcand;              // [k * nrow + r]
     int* vcnt;
-    float4* vref;            // position (relative to the grid origin) at the last rebuild
+    float4* vref;            // per solid (those with a contact row): position (relative to the
+                             // grid origin) at the last rebuild
     float skin;              // candidate margin; a rebuild follows once a solid moved skin / 2
     float vmaxEff;           // largest effective radius of a non-dummy solid
     int* rebuild;            // 1: candidates are stale; set by the hash, cleared by a completed step
@@ -136,7 +174,7 @@ struct DeviceState {
     float4* wnl;             // normal lo
     float2* wP;              // (p - min) . n, double-float
     int* wmat;
-    float4* wspring[3];      // ns * nw
+    float4* wspring[3];      // [k * ns + a]: wall k, solid a
 
     // ---- bonds ----
     int nb;
@@ -206,12 +244,11 @@ int fluidLanes(int nf);
 #define LAUNCH_LANES(kernel, L, n, threads, s, ...)                                                    \
     do {                                                                                               \
         const unsigned blocks_ = (unsigned)blocksFor((long long)(n) * (L), threads);                  \
-        ++t_kernelLaunches;                                                                            \
         switch (L) {                                                                                   \
-        case 8: kernel<8><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                             \
-        case 4: kernel<4><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                             \
-        case 2: kernel<2><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                             \
-        default: kernel<1><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                            \
+        case 8: launchStep(kernel<8>, blocks_, threads, s, __VA_ARGS__); break;                        \
+        case 4: launchStep(kernel<4>, blocks_, threads, s, __VA_ARGS__); break;                        \
+        case 2: launchStep(kernel<2>, blocks_, threads, s, __VA_ARGS__); break;                        \
+        default: launchStep(kernel<1>, blocks_, threads, s, __VA_ARGS__); break;                       \
         }                                                                                              \
     } while (0)
 
@@ -219,12 +256,11 @@ int fluidLanes(int nf);
 #define LAUNCH_LANES_U(kernel, U, L, n, threads, s, ...)                                               \
     do {                                                                                               \
         const unsigned blocks_ = (unsigned)blocksFor((long long)(n) * (L), threads);                  \
-        ++t_kernelLaunches;                                                                            \
         switch (L) {                                                                                   \
-        case 8: kernel<8, U><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                          \
-        case 4: kernel<4, U><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                          \
-        case 2: kernel<2, U><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                          \
-        default: kernel<1, U><<<blocks_, threads, 0, s>>>(__VA_ARGS__); break;                         \
+        case 8: launchStep(kernel<8, U>, blocks_, threads, s, __VA_ARGS__); break;                     \
+        case 4: launchStep(kernel<4, U>, blocks_, threads, s, __VA_ARGS__); break;                     \
+        case 2: launchStep(kernel<2, U>, blocks_, threads, s, __VA_ARGS__); break;                     \
+        default: launchStep(kernel<1, U>, blocks_, threads, s, __VA_ARGS__); break;                    \
         }                                                                                              \
     } while (0)
 
@@ -293,37 +329,39 @@ __device__ __forceinline__ double3 solidAbsPos(const DeviceState& d, int i)
                         d.minB[2] + c.z * d.cs[2] + ((double)h.z + (double)l.z));
 }
 
-// After the last drift of a step: once a solid that can touch others has
-// moved half the candidate margin since the candidates were built, the next
-// step rebuilds them.
-__device__ __forceinline__ void checkDisplacement(const DeviceState& d, int i)
+// After the last drift of a step: once a solid that can touch others (row >=
+// 0) has moved half the candidate margin since the candidates were built, the
+// next step rebuilds them.  c, h: its cell and offset after the drift; p0, q0:
+// vref and svref of the solid.
+__device__ __forceinline__ void checkDisplacementOf(const DeviceState& d, int row, int4 c, float4 h, float4 p0,
+                                                    float4 q0)
 {
-    const int r = d.srow[i];
-    if (r < 0) return;
-    const int4 c = d.scell[i];
-    const float4 h = d.sph[i];
-    const float4 p0 = d.vref[r];
+    if (row < 0) return;
     const float dx = (float)c.x * d.grid.cs.x + h.x - p0.x, dy = (float)c.y * d.grid.cs.y + h.y - p0.y,
                 dz = (float)c.z * d.grid.cs.z + h.z - p0.z;
     const float half = 0.5f * d.skin;
     if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)d.rebuild = 1;
     if (d.nf > 0) {  // the fluid candidates' solid partners
-        const float4 q0 = d.svref[r];
         const float ex = (float)c.x * d.grid.cs.x + h.x - q0.x, ey = (float)c.y * d.grid.cs.y + h.y - q0.y,
                     ez = (float)c.z * d.grid.cs.z + h.z - q0.z;
         const float fh = 0.5f * d.fskin;
         if (!(ex * ex + ey * ey + ez * ez <= fh * fh)) *(volatile int*)d.frebuild = 1;
     }
 }
+__device__ __forceinline__ void checkDisplacement(const DeviceState& d, int i)
+{
+    const int r = d.srow[i];
+    if (r < 0) return;
+    checkDisplacementOf(d, r, d.scell[i], d.sph[i], d.vref[i], d.nf > 0 ? d.svref[i] : make_float4(0, 0, 0, 0));
+}
 
 // Cell key of solid i for the next step's neighbour search, at the end of
 // this step (the position it starts from): the offset is renormalised into its
 // cell, the key and the walk centre stored; a solid that can touch others and
-// has left the domain sends the next lists to the reference's walk.
-__device__ __forceinline__ void rehashSolid(const DeviceState& d, int i)
+// has left the domain sends the next lists to the reference's walk.  c, h, l:
+// the solid's cell and offset after its last drift.
+__device__ __forceinline__ void rehashSolidOf(const DeviceState& d, int i, int row, int4 c, float4 h, float4 l)
 {
-    int4 c = d.scell[i];
-    float4 h = d.sph[i], l = d.spl[i];
     renormAxis(c.x, h.x, l.x, d.grid.csx);
     renormAxis(c.y, h.y, l.y, d.grid.csy);
     renormAxis(c.z, h.z, l.z, d.grid.csz);
@@ -333,11 +371,14 @@ __device__ __forceinline__ void rehashSolid(const DeviceState& d, int i)
     d.sph[i] = h;
     d.spl[i] = l;
     d.skey[i] = key;
-    const int row = d.srow[i];
     if (row >= 0) {
         d.scentre[row] = make_int4(truncAxis(c.x, h.x, l.x), truncAxis(c.y, h.y, l.y), truncAxis(c.z, h.z, l.z), 0);
         if (key == d.grid.num - 1) *(volatile int*)d.slowMode = 1;
     }
+}
+__device__ __forceinline__ void rehashSolid(const DeviceState& d, int i)
+{
+    rehashSolidOf(d, i, d.srow[i], d.scell[i], d.sph[i], d.spl[i]);
 }
 
 

@@ -301,12 +301,13 @@ __device__ __forceinline__ void fluidWalk(const DeviceState& d, RunIf when)
 // moving half the fluid margin since then makes the fluid candidates stale.
 __global__ void kFluidRefSolids(DeviceState d, RunIf when)
 {
+    stepKernelBegin();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= d.nrow || *d.status || !when.active()) return;
     const int a = d.rowSolid[r];
     const int4 c = d.scell[a];
     const float4 h = d.sph[a];
-    d.svref[r] = make_float4((float)c.x * d.grid.cs.x + h.x, (float)c.y * d.grid.cs.y + h.y,
+    d.svref[a] = make_float4((float)c.x * d.grid.cs.x + h.x, (float)c.y * d.grid.cs.y + h.y,
                              (float)c.z * d.grid.cs.z + h.z, 0.f);
 }
 
@@ -327,6 +328,7 @@ __device__ __forceinline__ int walkPosition(int4 ci, int4 cj)
 template <int L>
 __global__ void __launch_bounds__(T) kFluidFilter(DeviceState d)
 {
+    stepKernelBegin();
     const int th = blockIdx.x * blockDim.x + threadIdx.x;
     if ((th & ~31) >= d.nf * L || *d.status || *d.fslowMode || *d.slowMode) return;
     if (th == 0) *(volatile int*)d.frebuild = 0;
@@ -413,6 +415,7 @@ __global__ void __launch_bounds__(T) kFluidFilter(DeviceState d)
 // ---- fluid partners of each massive solid (coupling force) ----
 __global__ void kCoupCount(DeviceState d)
 {
+    stepKernelBegin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.nf || *d.status) return;
     const int m = min(d.fsc[i], d.kfs);
@@ -423,6 +426,7 @@ __global__ void kCoupCount(DeviceState d)
 }
 __global__ void kCoupFill(DeviceState d)
 {
+    stepKernelBegin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.nf || *d.status) return;
     if (d.coupStart[d.ns] > d.coupCap) {
@@ -438,6 +442,7 @@ __global__ void kCoupFill(DeviceState d)
 // atomics leave each solid's fluid partners in arbitrary order: sort them
 __global__ void kCoupSort(DeviceState d)
 {
+    stepKernelBegin();
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= d.ns || *d.status) return;
     const int s = d.coupStart[a], e = d.coupStart[a + 1];
@@ -504,6 +509,7 @@ __device__ __forceinline__ float3 gridPos(int4 c, float4 h, const GridDev& g)
 // plain (x, y, z) cells.
 __global__ void __launch_bounds__(T) kVerletBuild(DeviceState d)
 {
+    stepKernelBegin();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= d.nrow || *d.status || !*d.rebuild || *d.slowMode) return;
     const int a = d.rowSolid[r];
@@ -534,7 +540,7 @@ __global__ void __launch_bounds__(T) kVerletBuild(DeviceState d)
     // by index: the contact list filtered from them is then in index order
     sortSlots(d.vcand, r, d.nrow, min(n, d.vcap));
     d.vcnt[r] = n;
-    d.vref[r] = f4(gridPos(ca, ha, g));
+    d.vref[a] = f4(gridPos(ca, ha, g));
     if (n > d.vcap) {
         atomicOr(d.status, ST_VERLET_OVERFLOW);
         atomicMax(&d.need[1], n);
@@ -555,6 +561,7 @@ __global__ void __launch_bounds__(T) kVerletBuild(DeviceState d)
 // stays in walk order: bonds are numbered in it.
 __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int forceWalk)
 {
+    stepKernelBegin();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= d.nrow || *d.status) return;
     // the candidates (if this step rebuilt them) are fresh from here on; the
@@ -629,6 +636,7 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
 // bonds in the reference's list order.
 __global__ void kBondFlags(DeviceState d, int par, int* flag)
 {
+    stepKernelBegin();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)d.nrow * d.scap) return;
     const int r = (int)(i / d.scap), k = (int)(i % d.scap);
@@ -649,6 +657,7 @@ __global__ void kBondFlags(DeviceState d, int par, int* flag)
 }
 __global__ void kBondWrite(DeviceState d, int par, const int* flag, const int* pos)
 {
+    stepKernelBegin();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)d.nrow * d.scap || !flag[i]) return;
     const int r = (int)(i / d.scap), k = (int)(i % d.scap);
@@ -676,6 +685,7 @@ __global__ void kBondWrite(DeviceState d, int par, const int* flag, const int* p
 // leave ~1e-6 (a spurious unit normal).
 __global__ void kSolidNormals(DeviceState d, double h)
 {
+    stepKernelBegin();
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= d.ns) return;
     const int4 ca = d.scell[a];
@@ -730,11 +740,13 @@ __global__ void kSolidNormals(DeviceState d, double h)
 template <int L>
 __global__ void __launch_bounds__(T) kFluidWalkLists(DeviceState d, RunIf when)
 {
+    stepKernelBegin();
     fluidWalk<L, BUILD_LISTS>(d, when);
 }
 template <int L>
 __global__ void __launch_bounds__(T) kFluidWalkCandidates(DeviceState d, RunIf when)
 {
+    stepKernelBegin();
     fluidWalk<L, BUILD_CANDIDATES>(d, when);
 }
 
@@ -757,7 +769,7 @@ void launchFluidCandidates(const DeviceState& d, cudaStream_t s)
     when.unless = d.fslowMode;
     when.unless2 = d.slowMode;
     LAUNCH_LANES(kFluidWalkCandidates, d.lanes, d.nf, T, s, d, when);
-    if (d.nrow > 0) ++t_kernelLaunches, kFluidRefSolids<<<blocksFor(d.nrow, T), T, 0, s>>>(d, when);
+    if (d.nrow > 0) launchStep(kFluidRefSolids, blocksFor(d.nrow, T), T, s, d, when);
 }
 
 void launchFluidFilter(const DeviceState& d, cudaStream_t s)
@@ -770,23 +782,23 @@ void launchCouplingLists(const DeviceState& d, cudaStream_t s)
 {
     if (d.nf <= 0 || d.ns <= 0) return;
     cudaMemsetAsync(d.coupCount, 0, sizeof(int) * d.ns, s);
-    ++t_kernelLaunches, kCoupCount<<<blocksFor(d.nf, 256), 256, 0, s>>>(d);
+    launchStep(kCoupCount, blocksFor(d.nf, 256), 256, s, d);
     scanExclusive(d.coupCount, d.coupStart, d.ns, d.scanWork, s);
     cudaMemsetAsync(d.coupCount, 0, sizeof(int) * d.ns, s);
-    ++t_kernelLaunches, kCoupFill<<<blocksFor(d.nf, 256), 256, 0, s>>>(d);
-    ++t_kernelLaunches, kCoupSort<<<blocksFor(d.ns, 256), 256, 0, s>>>(d);
+    launchStep(kCoupFill, blocksFor(d.nf, 256), 256, s, d);
+    launchStep(kCoupSort, blocksFor(d.ns, 256), 256, s, d);
 }
 
 void launchVerletBuild(const DeviceState& d, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    ++t_kernelLaunches, kVerletBuild<<<blocksFor(d.nrow, T), T, 0, s>>>(d);
+    launchStep(kVerletBuild, blocksFor(d.nrow, T), T, s, d);
 }
 
 void launchContactDetect(const DeviceState& d, int par, bool forceWalk, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    ++t_kernelLaunches, kContactDetect<<<blocksFor(d.nrow, T), T, 0, s>>>(d, par, forceWalk ? 1 : 0);
+    launchStep(kContactDetect, blocksFor(d.nrow, T), T, s, d, par, forceWalk ? 1 : 0);
 }
 
 // Bond creation from the contact list (addBondData at initialisation,
@@ -797,7 +809,7 @@ int launchBondFlags(const DeviceState& d, int par, int* flag, int* pos, int* wor
 {
     const long long n = (long long)d.nrow * d.scap;
     if (n <= 0) return 0;
-    ++t_kernelLaunches, kBondFlags<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, par, flag);
+    launchStep(kBondFlags, (unsigned)((n + 255) / 256), 256, s, d, par, flag);
     scanExclusive(flag, pos, (int)n, work, s);
     int nb = 0;
     cudaMemcpyAsync(&nb, pos + n, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -809,13 +821,13 @@ void launchBondWrite(const DeviceState& d, int par, const int* flag, const int* 
 {
     const long long n = (long long)d.nrow * d.scap;
     if (n <= 0 || d.nb <= 0) return;
-    ++t_kernelLaunches, kBondWrite<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, par, flag, pos);
+    launchStep(kBondWrite, (unsigned)((n + 255) / 256), 256, s, d, par, flag, pos);
 }
 
 void launchSolidNormals(const DeviceState& d, double h, cudaStream_t s)
 {
     if (d.ns <= 0 || !(h > 0.0)) return;
-    ++t_kernelLaunches, kSolidNormals<<<blocksFor(d.ns, T), T, 0, s>>>(d, h);
+    launchStep(kSolidNormals, blocksFor(d.ns, T), T, s, d, h);
 }
 
 }  // namespace demsph

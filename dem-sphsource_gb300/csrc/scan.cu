@@ -47,6 +47,7 @@ __device__ __forceinline__ int blockExclusiveScan(int v, int& total)
 __global__ void __launch_bounds__(SCAN_THREADS) kTileSums(const int* __restrict__ in, int n, int* __restrict__ sums,
                                                           RunIf when)
 {
+    stepKernelBegin();
     if (!when.active()) return;
     const long long base = (long long)blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     int s = 0;
@@ -62,6 +63,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) kTileSums(const int* __restrict_
 __global__ void __launch_bounds__(SCAN_THREADS) kTileScan(const int* __restrict__ in, int n, int* __restrict__ out,
                                                           const int* __restrict__ offsets, RunIf when)
 {
+    stepKernelBegin();
     if (!when.active()) return;
     const long long base = (long long)blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     int v[SCAN_ITEMS];
@@ -102,14 +104,14 @@ void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s, Ru
     }
     const int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (tiles == 1) {
-        ++t_kernelLaunches, kTileScan<<<1, SCAN_THREADS, 0, s>>>(in, n, out, nullptr, when);
+        launchStep(kTileScan, 1, SCAN_THREADS, s, in, n, out, nullptr, when);
         return;
     }
     int* sums = work;
     int* offs = work + tiles;  // tiles + 1 entries
-    ++t_kernelLaunches, kTileSums<<<tiles, SCAN_THREADS, 0, s>>>(in, n, sums, when);
+    launchStep(kTileSums, tiles, SCAN_THREADS, s, in, n, sums, when);
     scanExclusive(sums, offs, tiles, offs + tiles + 1, s, when);
-    ++t_kernelLaunches, kTileScan<<<tiles, SCAN_THREADS, 0, s>>>(in, n, out, offs, when);
+    launchStep(kTileScan, tiles, SCAN_THREADS, s, in, n, out, offs, when);
 }
 
 }  // namespace demsph

@@ -151,6 +151,7 @@ struct ContinuityArgs {
 template <int L, bool U>
 __global__ void __launch_bounds__(T) kContinuity(DeviceState d, ContinuityArgs a)
 {
+    stepKernelBegin();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if ((t & ~31) >= d.nf * L || *d.status) return;
     const int i = t / L, lane = t % L;
@@ -215,6 +216,7 @@ __global__ void __launch_bounds__(T) kContinuity(DeviceState d, ContinuityArgs a
 template <int L, bool U>
 __global__ void __launch_bounds__(T) kMomentum(DeviceState d, dfl dtf, dfl halfDtf)
 {
+    stepKernelBegin();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if ((t & ~31) >= d.nf * L || *d.status) return;
     const int i = t / L, lane = t % L;
@@ -309,6 +311,7 @@ __device__ __forceinline__ dfl shepardTerm(dfl r, dfl invh)
 template <int L>
 __global__ void __launch_bounds__(T) kDensityReinit(DeviceState d, int storeReference)
 {
+    stepKernelBegin();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if ((t & ~31) >= d.nf * L || *d.status) return;
     const int i = t / L, lane = t % L;
@@ -380,6 +383,7 @@ __device__ __forceinline__ float3 couplingPairForce(const DeviceState& d, int sr
 
 __global__ void kCoupling(DeviceState d, int src)
 {
+    stepKernelBegin();
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= d.ns || *d.status) return;
     KahanF3 f;
@@ -394,6 +398,7 @@ __global__ void kCoupling(DeviceState d, int src)
 // Per-pair coupling force in the fluid's list order (for export only).
 __global__ void kCouplingPairs(DeviceState d, int src, float4* out)
 {
+    stepKernelBegin();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.nf) return;
     const int m = min(d.fsc[i], d.kfs);
@@ -444,13 +449,13 @@ void launchMomentumPass(const DeviceState& d, double dtf, cudaStream_t s)
 void launchCoupling(const DeviceState& d, int src, cudaStream_t s)
 {
     if (d.nf <= 0 || d.ns <= 0) return;
-    ++t_kernelLaunches, kCoupling<<<blocksFor(d.ns, 128), 128, 0, s>>>(d, src);
+    launchStep(kCoupling, blocksFor(d.ns, 128), 128, s, d, src);
 }
 
 void launchCouplingPairForces(const DeviceState& d, int src, float4* out, cudaStream_t s)
 {
     if (d.nf <= 0 || d.ns <= 0) return;
-    ++t_kernelLaunches, kCouplingPairs<<<blocksFor(d.nf, 128), 128, 0, s>>>(d, src, out);
+    launchStep(kCouplingPairs, blocksFor(d.nf, 128), 128, s, d, src, out);
 }
 
 }  // namespace demsph
