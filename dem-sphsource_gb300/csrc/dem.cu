@@ -15,6 +15,7 @@
 // The per-particle gather adds forward pairs and subtracts reverse pairs in
 // list order - no atomics, so results are bit-reproducible run to run.
 #include "kernels.cuh"
+#include "warp_items.cuh"
 
 namespace demsph {
 
@@ -317,25 +318,6 @@ __device__ __forceinline__ float wallOverlap(const DeviceState& d, int4 c, float
     return del.hi + del.lo;
 }
 
-// Position of the r-th (from 0) set bit of m; m has more than r set bits.
-__device__ __forceinline__ int nthSetBit(unsigned m, int r)
-{
-    int p = 0;
-#pragma unroll
-    for (int w = 16; w > 0; w >>= 1) {
-        const unsigned low = m & ((1u << w) - 1u);
-        const int c = __popc(low);
-        if (r >= c) {
-            r -= c;
-            m >>= w;
-            p += w;
-        } else {
-            m = low;
-        }
-    }
-    return p;
-}
-
 // Force and torque on every solid that can touch others (calSolidForceTorque,
 // core/integrate.cu:806-858, with the contact forces of :423-512, the bonds of
 // :717-804 and the walls of :514-610), one thread per row: each contact is
@@ -343,13 +325,9 @@ __device__ __forceinline__ int nthSetBit(unsigned m, int r)
 // the forward side also advances the springs - so no per-pair forces are
 // gathered.  Sums are Kahan-compensated, in index order.
 //
-// Rows hold few contacts and their counts vary, so a warp does not loop over
-// its rows' contacts lane by lane: it numbers the (row, contact) items of its
-// 32 rows level by level (every row's contact 0, then every row's contact 1,
-// ..., so neighbouring items are neighbouring rows of the same slot and their
-// slot arrays are read and written in whole lines) and evaluates them 32 at a
-// time, every lane on one item; each row's lane then adds the results of its
-// own items, in order, from shared memory.
+// Rows hold few contacts and their counts vary: a warp runs its rows'
+// (row, contact) items through warpItems, one lane per item, and each row's
+// lane adds its results in contact order.
 __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, float dt, int withCoupling)
 {
     stepKernelBegin();
@@ -357,7 +335,6 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
     if (*d.status) return;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     const int row0 = row - lane;
     const bool live = row < d.nrow;
@@ -366,41 +343,18 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
     // forward contacts (a, b) come first, then reverse ones (b, a)
     const int n = live ? min(d.fcnt[par][row], d.scap) : 0;
     const int total = live ? n + min(d.rcnt[row], d.scap) : 0;
-    const int levels = __reduce_max_sync(FULL, total);
     float4* resF = itemF + (threadIdx.x & ~31);
     float4* resT = itemT + (threadIdx.x & ~31);
     KahanF3 F, Tq;
-    for (int L0 = 0; L0 < levels; L0 += 32) {
-        // lane j describes level L0 + j: the rows holding an item there, and
-        // the number of the level's first item
-        unsigned rows = 0;
-        for (int q = L0; q < min(L0 + 32, levels); ++q) {
-            const unsigned m = __ballot_sync(FULL, total > q);
-            if (lane == q - L0) rows = m;
-        }
-        const int cnt = __popc(rows);
-        int incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(FULL, incl, o);
-            if (lane >= o) incl += y;
-        }
-        const int first = incl - cnt, items = __shfl_sync(FULL, incl, 31);
-        for (int c0 = 0; c0 < items; c0 += 32) {
-            const int idx = c0 + lane;
-            // the item's level: the last lane whose first item is at or before it
-            int lv = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-                if (__shfl_sync(FULL, first, lv + step) <= idx) lv += step;
-            const unsigned lrows = __shfl_sync(FULL, rows, lv);
-            const int owner = nthSetBit(lrows, idx - __shfl_sync(FULL, first, lv)) & 31;
+    warpItems(
+        total,
+        [&](int owner, int q, bool valid) {
             const int oa = __shfl_sync(FULL, a, owner), on = __shfl_sync(FULL, n, owner);
-            const int q = L0 + lv, orow = row0 + owner;
+            const int orow = row0 + owner;
             float4 rF = make_float4(0.f, 0.f, 0.f, 0.f), rT = rF;
-            if (idx < items) {
-                // through ONE inlined copy of pairForce: a pair's two solids run the
-                // same instructions on the same inputs and get the same bits
+            if (valid) {
+                // through ONE inlined copy of pairForce: a pair's two solids run
+                // the same instructions on the same inputs and get the same bits
                 const bool fwdSide = q < on;
                 int A = oa, B;
                 long long k;
@@ -432,23 +386,14 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
             }
             resF[lane] = rF;
             resT[lane] = rT;
-            __syncwarp();
-            // each row adds its items of this chunk, level by level (its contact order)
-            const int lvLo = __shfl_sync(FULL, lv, 0), lvHi = __shfl_sync(FULL, lv, min(31, items - 1 - c0));
-            for (int l = lvLo; l <= lvHi; ++l) {
-                const unsigned m = __shfl_sync(FULL, rows, l);
-                const int pos = __shfl_sync(FULL, first, l) + __popc(m & below) - c0;
-                if ((m >> lane & 1u) && pos >= 0 && pos < 32) {
-                    const float4 f = resF[pos];
-                    if (f.w != 0.f) {  // 0: a reverse pair the forward row does not hold
-                        F.add(xyz(f));
-                        Tq.add(xyz(resT[pos]));
-                    }
-                }
+        },
+        [&](int, int pos) {
+            const float4 f = resF[pos];
+            if (f.w != 0.f) {  // 0: a reverse pair the forward row does not hold
+                F.add(xyz(f));
+                Tq.add(xyz(resT[pos]));
             }
-            __syncwarp();
-        }
-    }
+        });
     if (!live) return;
     const int4 fa = d.sflags[a];
     for (int q = d.bondStart[a], qe = d.bondStart[a + 1]; q < qe; ++q) {
@@ -788,23 +733,24 @@ __global__ void kClumpForce(DeviceState d, int width)
 }
 
 // One half-step integration of all solids (integrate.cu:964-1027): the first
-// solidBlocks blocks take one solid each per thread, the rest a group of
-// `width` lanes per clump.  clumpForce: each clump group first sums its
-// pebbles' forces (kClumpForce's work, for runs of whole steps where nothing
-// happens between the contact phase and this integration); countStep: the
-// step has completed (the status can no longer change) and is counted.
-__global__ void kIntegrate(DeviceState d, dfl half, int before, int width, int solidBlocks, int clumpForce,
+// clumpBlocks blocks take a group of `width` lanes per clump (first, so their
+// longer chains of dependent reads overlap the rest), the others one solid
+// each per thread.  clumpForce: each clump group first sums its pebbles'
+// forces (kClumpForce's work, for runs of whole steps where nothing happens
+// between the contact phase and this integration); countStep: the step has
+// completed (the status can no longer change) and is counted.
+__global__ void kIntegrate(DeviceState d, dfl half, int before, int width, int clumpBlocks, int clumpForce,
                            int countStep)
 {
     stepKernelBegin();
     if (countStep && blockIdx.x == 0 && threadIdx.x == 0 && *d.status == 0) atomicAdd(d.stepsDone, 1);
-    if ((int)blockIdx.x < solidBlocks) {
-        const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((int)blockIdx.x >= clumpBlocks) {
+        const int k = (blockIdx.x - clumpBlocks) * blockDim.x + threadIdx.x;
         if (k >= d.nmove || *d.status) return;
-        solidIntegrateOne(d, d.moveList[k], half, before);
+        solidIntegrateOne(d, d.moveFirst >= 0 ? d.moveFirst + k : d.moveList[k], half, before);
         return;
     }
-    const int t = (blockIdx.x - solidBlocks) * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (clumpForce) clumpForceGroup(d, width, t);
     clumpIntegrateGroup(d, half, before, width, t);
 }
@@ -836,7 +782,8 @@ void launchSolidIntegrate(const DeviceState& d, double dt, bool before, bool clu
     const int sb = d.nmove > 0 ? blocksFor(d.nmove, 256) : 0;
     const int cb = d.nc > 0 ? blocksFor((long long)d.nc * d.clumpLanes, 256) : 0;
     if (sb + cb == 0 && !countStep) return;
-    launchStep(kIntegrate, std::max(1, sb + cb), 256, s, d, h, before ? 1 : 0, d.clumpLanes, sb, clumpForce ? 1 : 0, countStep ? 1 : 0);
+    launchStep(kIntegrate, std::max(1, sb + cb), 256, s, d, h, before ? 1 : 0, d.clumpLanes, cb, clumpForce ? 1 : 0,
+               countStep ? 1 : 0);
 }
 
 

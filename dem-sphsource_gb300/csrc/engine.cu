@@ -701,6 +701,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 }
                 d.nmove = (int)move.size();
                 d.moveList = dalloc<int>(move.size(), e->owned, e->stream);
+                d.moveFirst = consecutiveFirst(move.data(), move.size());
                 if (!move.empty())
                     CK(cudaMemcpyAsync(d.moveList, move.data(), sizeof(int) * move.size(), cudaMemcpyHostToDevice,
                                        e->stream));

@@ -352,12 +352,17 @@ int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel,
                 move.push_back(i);
         }
         if (move != e->moveHost) {
+            const int first = consecutiveFirst(move.data(), move.size());
             if (move.size() != e->moveHost.size()) {
                 void* p = d.moveList;
                 freeOne(e, p);
                 d.moveList = dalloc<int>(move.size(), e->owned, e->stream);
                 d.nmove = (int)move.size();
                 dropGraph(e);  // the list is a kernel argument baked into captured graphs
+            }
+            if (first != d.moveFirst) {
+                d.moveFirst = first;
+                dropGraph(e);
             }
             if (!move.empty())
                 CK(cudaMemcpyAsync(d.moveList, move.data(), sizeof(int) * move.size(), cudaMemcpyHostToDevice,

@@ -142,6 +142,7 @@ struct DeviceState {
     int* srow;               // solid -> row, -1 for dummy particles
     int nmove;               // solids the integration advances: all but clump pebbles (their clump
     int* moveList;           // moves them) and dummy particles at rest (they never gain velocity)
+    int moveFirst;           // >= 0: the list is moveFirst, moveFirst + 1, ... (moveList is not read)
     int* rowSolid;           // row -> solid
     int4* scentre;           // per row: centre cell of the reference's 27-cell walk at the last hash (exports)
     int scap;                // slots per row
@@ -402,6 +403,14 @@ __device__ __forceinline__ void rehashFluid(const DeviceState& d, int i)
                 dz = (float)c.z * d.grid.cs.z + h.z - p0.z;
     const float half = 0.5f * d.fskin;
     if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)d.frebuild = 1;
+}
+
+// First entry of a list of consecutive solid indices, or -1.
+inline int consecutiveFirst(const int* v, size_t n)
+{
+    for (size_t k = 1; k < n; ++k)
+        if (v[k] != v[0] + (int)k) return -1;
+    return n ? v[0] : 0;
 }
 
 inline int blocksFor(long long n, int threads) { return (int)((n + threads - 1) / threads > 0 ? (n + threads - 1) / threads : 1); }

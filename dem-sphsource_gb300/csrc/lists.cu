@@ -20,6 +20,7 @@
 //     looking the pair (A, B) up in A's previous forward segment, which holds
 //     the same springs the reference finds through B's reverse span.
 #include "kernels.cuh"
+#include "warp_items.cuh"
 
 namespace demsph {
 
@@ -562,13 +563,17 @@ __global__ void __launch_bounds__(T) kVerletBuild(DeviceState d)
 __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int forceWalk)
 {
     stepKernelBegin();
+    __shared__ int itemB[T];  // 32 candidate tests per warp: the partner, or -1
+    if (*d.status) return;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= d.nrow || *d.status) return;
+    const int r0 = r - lane;
+    const bool live = r < d.nrow;
     // the candidates (if this step rebuilt them) are fresh from here on; the
     // last drift of the step raises the flag again if a solid moves too far
     if (r == 0 && !forceWalk) *(volatile int*)d.rebuild = 0;
-    const int a = d.rowSolid[r];
-    const int4 fa = d.sflags[a];
+    const int a = live ? d.rowSolid[r] : 0;
     const int prev = par ^ 1;
     const int C = d.scap;
     const size_t nr = (size_t)d.nrow;
@@ -584,21 +589,38 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
     };
     const bool walk = forceWalk || *d.slowMode;
     if (walk) {
-        const int4 ca = d.scell[a];
-        const float4 ha = d.sph[a], la = d.spl[a];
-        forStencil(ca, ha, la, d.grid, [&](int hash, bool, int, int, int) {
-            for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
-                const int b = d.ssorted[p];
-                if (solidPairCandidate(d, a, fa, b) && solidsTouch(d, a, b)) emit(b);
-            }
-        });
-    } else {
-        const int n = min(d.vcnt[r], d.vcap);
-        for (int k = 0; k < n; ++k) {
-            const int b = d.vcand[(size_t)k * nr + r];
-            if (solidsTouch(d, a, b)) emit(b);
+        if (live) {
+            const int4 fa = d.sflags[a];
+            const int4 ca = d.scell[a];
+            const float4 ha = d.sph[a], la = d.spl[a];
+            forStencil(ca, ha, la, d.grid, [&](int hash, bool, int, int, int) {
+                for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
+                    const int b = d.ssorted[p];
+                    if (solidPairCandidate(d, a, fa, b) && solidsTouch(d, a, b)) emit(b);
+                }
+            });
         }
+    } else {
+        // the candidate tests of the warp's rows as warp items, taken back in
+        // candidate (index) order
+        int* res = itemB + (threadIdx.x & ~31);
+        warpItems(
+            live ? min(d.vcnt[r], d.vcap) : 0,
+            [&](int owner, int q, bool valid) {
+                const int oa = __shfl_sync(FULL, a, owner);
+                int hit = -1;
+                if (valid) {
+                    const int b = d.vcand[(size_t)q * nr + r0 + owner];
+                    if (solidsTouch(d, oa, b)) hit = b;
+                }
+                res[lane] = hit;
+            },
+            [&](int, int pos) {
+                const int b = res[pos];
+                if (b >= 0) emit(b);
+            });
     }
+    if (!live) return;
     d.fcnt[par][r] = nf;
     d.rcnt[r] = nb;
     if (nf > C || nb > C) {
@@ -610,6 +632,7 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
         sortSlots(d.fwd[par], r, d.nrow, nf);
         sortSlots(d.rev, r, d.nrow, nb);
     }
+    // each forward pair takes the springs of the same pair in the previous list
     const int prevCnt = min(d.fcnt[prev][r], C);
     for (int q = 0; q < nf; ++q) {
         const size_t slot = (size_t)q * nr + r;
