@@ -554,6 +554,7 @@ def main():
         cfg = dict(base_config)
         cfg.update({"solid_pairs": c.solid_pairs, "fluid_pairs_half": c.fluid_pairs,
                     "fluid_solid_pairs": c.fluid_solid_pairs, "bonds": c.bonds,
+                    "launch_shapes": eng.launch_shapes(),
                     "timing": "CUDA events on the engine stream; K steps replayed as CUDA graphs",
                     "precision": "FP32 arithmetic with Kahan sums; double-float positions, velocities, overlaps, "
                                  "bond accumulators and clump states; FP64 clump orientation"})

@@ -65,13 +65,27 @@ class Options(C.Structure):
 
     _fields_ = [("device", _I), ("fluid_neighbors_max", _I), ("fluid_solids_max", _I),
                 ("solid_contacts_per_particle", _I), ("fixes", _I), ("debug", _I), ("solid_verlet_skin", _D),
-                ("fluid_lanes", _I), ("fluid_verlet_skin", _D)]
+                ("fluid_lanes", _I), ("fluid_verlet_skin", _D), ("contact_rows_per_warp", _I)]
+
+
+def _options(device=0, **opts):
+    """Options from keyword arguments (the field names; missing ones 0)."""
+    o = Options()
+    o.device = int(device)
+    for name, typ in Options._fields_:
+        if name in opts and name != "device":
+            setattr(o, name, float(opts[name]) if typ is _D else int(opts[name]))
+    return o
 
 
 class Counts(C.Structure):
     _fields_ = [("fluid_pairs", C.c_longlong), ("fluid_solid_pairs", C.c_longlong), ("solid_pairs", C.c_longlong),
                 ("bonds", C.c_longlong), ("bonds_intact", C.c_longlong), ("grid_cells", _I), ("grid_size", _I * 3),
                 ("cell_size", _D * 3)]
+
+
+class LaunchShapes(C.Structure):
+    _fields_ = [("fluid_lanes", _I), ("clump_lanes", _I), ("contact_force_rows", _I), ("contact_detect_rows", _I)]
 
 
 class AuditValues(C.Structure):
@@ -259,14 +273,18 @@ def build_scene(recipe, n_material=10):
 class Engine:
     """One scene on one GPU (the C ABI engine)."""
 
-    def __init__(self, scene, device=0, fluid_neighbors_max=0, fluid_solids_max=0, solid_contacts_per_particle=0,
-                 fixes=0, debug=0, solid_verlet_skin=0.0, fluid_lanes=0, fluid_verlet_skin=0.0):
-        """``solid_verlet_skin``: margin (m) of the solid contact candidates
-        (0 = 0.2 x the smallest solid radius, < 0 = the 27-cell walk every step)."""
+    def __init__(self, scene, device=0, **opts):
+        """Keyword options are the fields of ``demsph_options`` (0 = default):
+        fluid_neighbors_max, fluid_solids_max, solid_contacts_per_particle,
+        fixes, debug, solid_verlet_skin (margin (m) of the solid contact
+        candidates; < 0 = the 27-cell walk every step), fluid_lanes,
+        fluid_verlet_skin, contact_rows_per_warp."""
+        unknown = set(opts) - {n for n, _ in Options._fields_}
+        if unknown:
+            raise TypeError(f"unknown engine options: {sorted(unknown)}")
         self.lib = load_library()
         self.scene = scene
-        opts = Options(device, fluid_neighbors_max, fluid_solids_max, solid_contacts_per_particle, fixes, debug,
-                       float(solid_verlet_skin), int(fluid_lanes), float(fluid_verlet_skin))
+        opts = _options(device, **opts)
         h = _P()
         rc = self.lib.demsph_create(C.byref(scene), C.byref(opts), C.byref(h))
         self.h = h
@@ -445,6 +463,12 @@ class Engine:
         self._chk(self.lib.demsph_autotune(self.h, C.byref(lanes)), "autotune")
         return lanes.value
 
+    def launch_shapes(self):
+        """{fluid_lanes, clump_lanes, contact_force_rows, contact_detect_rows} in use."""
+        v = LaunchShapes()
+        self._chk(self.lib.demsph_get_launch_shapes(self.h, C.byref(v)), "launch_shapes")
+        return {n: getattr(v, n) for n, _ in LaunchShapes._fields_}
+
     def solid_pairs(self):
         prefix = np.zeros(self.ns, np.int32)
         self._chk(self.lib.demsph_export_solid_pairs(self.h, _ptr(prefix, _IP), *([None] * 7), C.c_longlong(0)), "ss")
@@ -475,10 +499,7 @@ class Engine:
 def estimate_bytes(scene, **opts):
     """Device memory demsph_create will allocate for the scene (an estimate)."""
     lib = load_library()
-    o = Options(0, opts.get("fluid_neighbors_max", 0), opts.get("fluid_solids_max", 0),
-                opts.get("solid_contacts_per_particle", 0), opts.get("fixes", 0), opts.get("debug", 0),
-                float(opts.get("solid_verlet_skin", 0.0)), int(opts.get("fluid_lanes", 0)),
-                float(opts.get("fluid_verlet_skin", 0.0)))
+    o = _options(0, **opts)
     return int(lib.demsph_estimate_bytes(C.byref(scene), C.byref(o)))
 
 
@@ -509,10 +530,7 @@ class Server:
             pass
 
     def submit(self, scene, n_steps, **opts):
-        o = Options(0, opts.get("fluid_neighbors_max", 0), opts.get("fluid_solids_max", 0),
-                    opts.get("solid_contacts_per_particle", 0), opts.get("fixes", 0), opts.get("debug", 0),
-                    float(opts.get("solid_verlet_skin", 0.0)), int(opts.get("fluid_lanes", 0)),
-                float(opts.get("fluid_verlet_skin", 0.0)))
+        o = _options(0, **opts)
         rid = C.c_longlong()
         rc = self.lib.demsph_server_submit(self.h, C.byref(scene), C.byref(o), _I(n_steps), C.byref(rid))
         if rc != DEMSPH_OK:

@@ -335,14 +335,18 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
     if (*d.status) return;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row0 = row - lane;
-    const bool live = row < d.nrow;
+    // lanes 0 .. forceRows - 1 of each warp own a row
+    const int row0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * d.forceRows;
+    const int row = row0 + lane;
+    const bool live = lane < d.forceRows && row < d.nrow;
     const int a = live ? d.rowSolid[row] : 0;
     const size_t nr = (size_t)d.nrow;
     // forward contacts (a, b) come first, then reverse ones (b, a)
     const int n = live ? min(d.fcnt[par][row], d.scap) : 0;
-    const int total = live ? n + min(d.rcnt[row], d.scap) : 0;
+    const int contacts = live ? n + min(d.rcnt[row], d.scap) : 0;
+    // then the row's bonds (their forces come from kBonds)
+    const int bondFirst = live ? d.bondStart[a] : 0;
+    const int total = contacts + (live ? d.bondStart[a + 1] - bondFirst : 0);
     float4* resF = itemF + (threadIdx.x & ~31);
     float4* resT = itemT + (threadIdx.x & ~31);
     KahanF3 F, Tq;
@@ -350,9 +354,10 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
         total,
         [&](int owner, int q, bool valid) {
             const int oa = __shfl_sync(FULL, a, owner), on = __shfl_sync(FULL, n, owner);
+            const int oc = __shfl_sync(FULL, contacts, owner), ob = __shfl_sync(FULL, bondFirst, owner);
             const int orow = row0 + owner;
             float4 rF = make_float4(0.f, 0.f, 0.f, 0.f), rT = rF;
-            if (valid) {
+            if (valid && q < oc) {
                 // through ONE inlined copy of pairForce: a pair's two solids run
                 // the same instructions on the same inputs and get the same bits
                 const bool fwdSide = q < on;
@@ -383,6 +388,17 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
                         rT = f4(mT);
                     }
                 }
+            } else if (valid) {
+                const int bi = d.bondList[ob + q - oc];
+                float3 bF = xyz(d.bF[bi]), bT;
+                if (d.bab[bi].x == oa) {
+                    bT = xyz(d.bTA[bi]);
+                } else {
+                    bF = -bF;
+                    bT = -xyz(d.bTB[bi]);
+                }
+                rF = make_float4(bF.x, bF.y, bF.z, 1.f);
+                rT = f4(bT);
             }
             resF[lane] = rF;
             resT[lane] = rT;
@@ -396,49 +412,62 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
         });
     if (!live) return;
     const int4 fa = d.sflags[a];
-    for (int q = d.bondStart[a], qe = d.bondStart[a + 1]; q < qe; ++q) {
-        const int bi = d.bondList[q];
-        if (d.bab[bi].x == a) {
-            F.add(xyz(d.bF[bi]));
-            Tq.add(xyz(d.bTA[bi]));
-        } else {
-            F.add(-xyz(d.bF[bi]));
-            Tq.add(-xyz(d.bTB[bi]));
-        }
-    }
     if (withCoupling) F.add(-xyz(d.sfcoup[a]));
     const float4 ph = d.sph[a];
     const float im = ph.w;
     float3 acc = F.sum() * im;
     if ((fa.w & F_HASMASS) && fa.z < 0) acc = acc + d.g;
     float3 tq = Tq.sum();
-    // infinite walls (integrate.cu:514-610)
+    // infinite walls (integrate.cu:514-610).  wmask bit k (walls below 32):
+    // the springs of wall k may be non-zero; a clear bit spares reading and
+    // re-zeroing them.
     if (d.nw > 0 && !(fa.w & F_DUMMY) && !(fa.w & F_FIXED)) {
         const int4 ca = d.scell[a];
         const float4 pl = d.spl[a];
         const float4 rad = d.srad[a];
         const float3 v = xyz(d.svh[a]), w = xyz(d.swh[a]);
+        const unsigned mask0 = d.wmask[a];
+        unsigned mask = mask0;
+        const float3 pf = make_float3((float)ca.x * d.grid.cs.x + ph.x, (float)ca.y * d.grid.cs.y + ph.y,
+                                      (float)ca.z * d.grid.cs.z + ph.z);
         for (int k = 0; k < d.nw; ++k) {
             const size_t h = (size_t)k * d.ns + a;  // wall-major: a warp's solids are adjacent
-            const float delta = wallOverlap(d, ca, ph, pl, k, rad.x, rad.y);
+            const bool held = k >= 32 || ((mask >> k) & 1u);
+            // FP32 pre-test: a sphere clearly off the wall (by far more than
+            // the FP32 rounding of this estimate) has a negative exact overlap
+            const float3 nf = xyz(d.wnh[k]);
+            const float Pf = d.wP[k].x;
+            const float est = rad.x - (dot3(nf, pf) - Pf);
+            const float tol = 4.e-6f * (fabsf(pf.x) + fabsf(pf.y) + fabsf(pf.z) + fabsf(Pf) + rad.x);
+            const float delta = est < -tol ? -1.f : wallOverlap(d, ca, ph, pl, k, rad.x, rad.y);
             if (delta < 0.f) {
-                d.wspring[0][h] = d.wspring[1][h] = d.wspring[2][h] = make_float4(0, 0, 0, 0);
+                if (held) {
+                    d.wspring[0][h] = d.wspring[1][h] = d.wspring[2][h] = make_float4(0, 0, 0, 0);
+                    if (k < 32) mask &= ~(1u << k);
+                }
                 if (d.fixes & DEMSPH_FIX_WALL_LOOP) continue;
                 break;
             }
             const float3 n = xyz(d.wnh[k]);
             const float3 lever = n * (-(rad.x - delta));
             const float3 vc = v + cross3(w, lever);
-            float3 es = xyz(d.wspring[0][h]), er = xyz(d.wspring[1][h]), et = xyz(d.wspring[2][h]);
+            float3 es = make_float3(0.f, 0.f, 0.f), er = es, et = es;
+            if (held) {
+                es = xyz(d.wspring[0][h]);
+                er = xyz(d.wspring[1][h]);
+                et = xyz(d.wspring[2][h]);
+            }
             float3 Fw = make_float3(0.f, 0.f, 0.f), Fwt = Fw, Tw = Fw;
             const int slot = tableSlot(d.tab, fa.x, d.wmat[k]);
             contactLaw(d.tab, slot, Fw, Fwt, Tw, es, er, et, vc, w, n, delta, 1.f / im, rad.x, dt);
             d.wspring[0][h] = f4(es);
             d.wspring[1][h] = f4(er);
             d.wspring[2][h] = f4(et);
+            if (k < 32) mask |= 1u << k;
             acc = acc + Fw * im;
             tq = tq + Tw + cross3(n, Fwt) * (-(rad.x - delta));
         }
+        if (mask != mask0) d.wmask[a] = mask;
     }
     d.sacc[a] = f4(acc);
     d.storque[a] = f4(tq);
@@ -767,7 +796,7 @@ void launchBonds(const DeviceState& d, int par, float dt, cudaStream_t s)
 void launchSolidForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    launchStep(kSolidForces, blocksFor(d.nrow, T), T, s, d, par, dt, d.nf > 0 ? 1 : 0);
+    launchStep(kSolidForces, blocksFor(d.nrow, d.forceRows * (T / 32)), T, s, d, par, dt, d.nf > 0 ? 1 : 0);
 }
 void launchClumpForce(const DeviceState& d, cudaStream_t s)
 {

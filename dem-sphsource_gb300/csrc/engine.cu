@@ -450,6 +450,9 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
     if (sc->n_fluid >= MAX_LIST_INDEX || sc->n_solid >= MAX_LIST_INDEX) return DEMSPH_ERR_CAPACITY;
     if (opt && (opt->fluid_lanes < 0 || opt->fluid_lanes > 8 || (opt->fluid_lanes & (opt->fluid_lanes - 1)) != 0))
         return DEMSPH_ERR_ARGUMENT;
+    if (opt && opt->contact_rows_per_warp != 0 && opt->contact_rows_per_warp != 4 && opt->contact_rows_per_warp != 8 &&
+        opt->contact_rows_per_warp != 16 && opt->contact_rows_per_warp != 32)
+        return DEMSPH_ERR_ARGUMENT;
     demsph_options o{};
     if (opt) o = *opt;
     // Material ids index the contact tables (getCombinedIndex, core/hostStructs.h:369-384);
@@ -729,6 +732,9 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.rebuild = dalloc<int>(1, e->owned, e->stream);
             d.slowMode = dalloc<int>(1, e->owned, e->stream);
             d.need = dalloc<int>(4, e->owned, e->stream);
+            d.rowStats = dalloc<int>(3, e->owned, e->stream);
+            d.forceRows = d.detectRows = o.contact_rows_per_warp > 0 ? o.contact_rows_per_warp : 32;
+            e->adaptRows = o.contact_rows_per_warp == 0;
             const int one = 1;
             const bool walkOnly = o.solid_verlet_skin < 0 || d.grid.gx < 3 || d.grid.gy < 3 || d.grid.gz < 3;
             CK(cudaMemcpyAsync(d.rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, e->stream));
@@ -773,6 +779,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.wP = dalloc<float2>(nw, e->owned, e->stream);
             d.wmat = dalloc<int>(nw, e->owned, e->stream);
             for (int k = 0; k < 3; ++k) d.wspring[k] = dalloc<float4>((size_t)ns * nw, e->owned, e->stream);
+            d.wmask = dalloc<unsigned>(ns, e->owned, e->stream);
             if (nw > 0) {
                 CK(cudaMemcpyAsync(d.wnh, nh.data(), sizeof(float4) * nw, cudaMemcpyHostToDevice, e->stream));
                 CK(cudaMemcpyAsync(d.wnl, nl.data(), sizeof(float4) * nw, cudaMemcpyHostToDevice, e->stream));
@@ -1045,6 +1052,31 @@ static const demsph_engine::CachedGraph& graphFor(demsph_engine* e, int kind, in
     return e->graphs.back();
 }
 
+// Rows per warp of the contact kernels for about 192 items per warp (a warp
+// also does per-row work for each of its rows, so fewer rows pay only when
+// rows hold many items; measured on GB300 with 0.6 and ~12 items per row);
+// kept while the current value is within a factor of the ideal one (a change
+// re-captures the graphs).
+static int rowsPerWarp(double itemsPerRow, int current)
+{
+    const double ideal = 192.0 / std::max(itemsPerRow, 0.25);
+    if (ideal >= 0.75 * current && ideal <= 2.5 * current) return current;
+    int r = 32;
+    while (r > 4 && r > ideal) r >>= 1;
+    return r;
+}
+
+static void adaptRowsPerWarp(demsph_engine* e, const int* stats)
+{
+    DeviceState& d = e->d;
+    const int fr = rowsPerWarp((double)stats[0] / stats[2], d.forceRows);
+    const int dr = rowsPerWarp((double)stats[1] / stats[2], d.detectRows);
+    if (fr == d.forceRows && dr == d.detectRows) return;
+    d.forceRows = fr;
+    d.detectRows = dr;
+    dropGraph(e);  // the launch shapes and the state are baked into the graphs
+}
+
 int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph)
 {
     if (gap < 1 || n_steps < 0) return DEMSPH_ERR_ARGUMENT;
@@ -1085,10 +1117,16 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
                 run -= len;
             }
         }
+        int rowStats[3] = {0, 0, 0};
+        if (graphs && d.nrow > 0 && e->adaptRows) {
+            launchRowStats(d, e->par, e->stream);
+            CK(cudaMemcpyAsync(rowStats, d.rowStats, sizeof(rowStats), cudaMemcpyDeviceToHost, e->stream));
+        }
         int done = 0;
         const int st = readStatus(e, &done);
         if (st == 0) {
             step = s;
+            if (rowStats[2] > 0) adaptRowsPerWarp(e, rowStats);
             continue;
         }
         if (st & ~ALL_OVERFLOWS) return fail(e, DEMSPH_ERR_STATE, "unexpected device status " + std::to_string(st));
@@ -1099,6 +1137,16 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
     CK(cudaGetLastError());
     return DEMSPH_OK;
     ENGINE_END(e)
+}
+
+int demsph_get_launch_shapes(const demsph_engine* e, demsph_launch_shapes* out)
+{
+    if (!e || !out) return DEMSPH_ERR_ARGUMENT;
+    out->fluid_lanes = e->d.lanes;
+    out->clump_lanes = e->d.clumpLanes;
+    out->contact_force_rows = e->d.forceRows;
+    out->contact_detect_rows = e->d.detectRows;
+    return DEMSPH_OK;
 }
 
 // Threads per fluid particle, chosen by timing: the first continuity pass

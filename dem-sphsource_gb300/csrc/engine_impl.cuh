@@ -53,6 +53,7 @@ struct demsph_engine {
     std::string err;
     int par = 1;                  // parity of the last successful solid list build
     bool forceWalk = false;       // next contact list from the reference's 27-cell walk
+    bool adaptRows = true;        // contact rows per warp follow the contacts per row
     bool solidSortStale = true;   // solid cells must be recomputed although no solid has mass
     std::vector<unsigned char> moveKind;  // per solid: 0 clump pebble, 1 integrated, 2 dummy (integrated when moving)
     std::vector<int> moveHost;            // the device move list

@@ -168,6 +168,11 @@ struct DeviceState {
     int* slowMode;           // 1: lists come from the 27-cell walk every step (grid too small, or a solid left the domain)
     int* need;               // [0] most contacts of a row, [1] most candidates of a row,
                              // [2] / [3] most fluid / solid candidates of a fluid particle (for growing)
+    // rows per warp of the contact-force and contact-detection kernels (4..32):
+    // fewer rows when rows hold many items, so that busy scenes still fill the
+    // GPU; results do not depend on them
+    int forceRows, detectRows;
+    int* rowStats;           // [0] contact items, [1] candidates, [2] rows, over a sample of rows
 
     // ---- infinite walls ----
     int nw;
@@ -176,6 +181,7 @@ struct DeviceState {
     float2* wP;              // (p - min) . n, double-float
     int* wmat;
     float4* wspring[3];      // [k * ns + a]: wall k, solid a
+    unsigned* wmask;         // per solid: bit k (k < 32) set while the springs of wall k may be non-zero
 
     // ---- bonds ----
     int nb;
@@ -296,6 +302,8 @@ void launchCouplingLists(const DeviceState& d, cudaStream_t s);
 // 27-cell walk, in the reference's order).
 void launchVerletBuild(const DeviceState& d, cudaStream_t s);
 void launchContactDetect(const DeviceState& d, int parity, bool forceWalk, cudaStream_t s);
+// Contact items and candidates over a sample of rows, into rowStats.
+void launchRowStats(const DeviceState& d, int parity, cudaStream_t s);
 int launchBondFlags(const DeviceState& d, int parity, int* flag, int* pos, int* work, cudaStream_t s);
 void launchBondWrite(const DeviceState& d, int parity, const int* flag, const int* pos, cudaStream_t s);
 void launchSolidNormals(const DeviceState& d, double h, cudaStream_t s);

@@ -567,9 +567,10 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
     if (*d.status) return;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    const int r0 = r - lane;
-    const bool live = r < d.nrow;
+    // lanes 0 .. detectRows - 1 of each warp own a row
+    const int r0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * d.detectRows;
+    const int r = r0 + lane;
+    const bool live = lane < d.detectRows && r < d.nrow;
     // the candidates (if this step rebuilt them) are fresh from here on; the
     // last drift of the step raises the flag again if a solid moves too far
     if (r == 0 && !forceWalk) *(volatile int*)d.rebuild = 0;
@@ -650,6 +651,38 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
         d.springIn[0][slot] = s0;
         d.springIn[1][slot] = s1;
         d.springIn[2][slot] = s2;
+    }
+}
+
+// Contact items (forward + reverse contacts, bonds) and candidates per row over at most 4096
+// evenly spaced rows: the host sizes the rows per warp of the contact kernels
+// from them.
+__global__ void kRowStats(DeviceState d, int par)
+{
+    stepKernelBegin();
+    __shared__ int sums[3][8];
+    const int stride = max(1, d.nrow / 4096);
+    int items = 0, cand = 0, rows = 0;
+    for (int r = threadIdx.x * stride; r < d.nrow; r += blockDim.x * stride) {
+        const int a = d.rowSolid[r];
+        items += min(d.fcnt[par][r], d.scap) + min(d.rcnt[r], d.scap) + d.bondStart[a + 1] - d.bondStart[a];
+        cand += min(d.vcnt[r], d.vcap);
+        ++rows;
+    }
+    items = __reduce_add_sync(0xffffffffu, items);
+    cand = __reduce_add_sync(0xffffffffu, cand);
+    rows = __reduce_add_sync(0xffffffffu, rows);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        sums[0][w] = items;
+        sums[1][w] = cand;
+        sums[2][w] = rows;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        int t = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sums[threadIdx.x][k];
+        d.rowStats[threadIdx.x] = t;
     }
 }
 
@@ -821,7 +854,13 @@ void launchVerletBuild(const DeviceState& d, cudaStream_t s)
 void launchContactDetect(const DeviceState& d, int par, bool forceWalk, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    launchStep(kContactDetect, blocksFor(d.nrow, T), T, s, d, par, forceWalk ? 1 : 0);
+    launchStep(kContactDetect, blocksFor(d.nrow, d.detectRows * (T / 32)), T, s, d, par, forceWalk ? 1 : 0);
+}
+
+void launchRowStats(const DeviceState& d, int par, cudaStream_t s)
+{
+    if (d.nrow <= 0) return;
+    launchStep(kRowStats, 1, 256, s, d, par);
 }
 
 // Bond creation from the contact list (addBondData at initialisation,

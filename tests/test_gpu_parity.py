@@ -177,6 +177,30 @@ def test_contact_candidates_do_not_change_results(ds, scenes, name):
             assert np.array_equal(s1[k], s0[k]), k
 
 
+@pytest.mark.parametrize("name", ("tiny_granular", "tiny_coupled"))
+def test_contact_rows_per_warp_do_not_change_results(ds, scenes, name):
+    """The contact kernels hand a warp's (row, contact) items to its lanes
+    whatever the rows per warp: 4, 32 and the adaptive choice (re-made after
+    every update call) give the same contact lists and state, bit for bit."""
+    recipe = getattr(scenes, name)()
+    b, sc = ds.build_scene(recipe)
+    engines = [ds.Engine(sc, contact_rows_per_warp=r) for r in (32, 4, 0)]
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for e in engines:
+        e.initialize()
+        for k in range(6):
+            e.update(dt, 1 + 10 * k, 10, gap, use_graph=True)
+    ref = engines[0].solid_pairs()
+    s0 = engines[0].download_solids()
+    for e in engines[1:]:
+        got = e.solid_pairs()
+        for k in ref:
+            assert np.array_equal(got[k], ref[k]), k
+        s1 = e.download_solids()
+        for k in s0:
+            assert np.array_equal(s1[k], s0[k]), k
+
+
 def test_drift_bounded_over_run(ds, scenes):
     """Forty steps of the coupled scene: the engine stays within bounded
     distance of the FP64 oracle (no systematic FP32 drift)."""
