@@ -167,6 +167,9 @@ def stage_bytes(stage, c):
         # per active solid: cell ph pl rad flags 80 + list and candidate counts 12 + walk
         # centre 8; per pair: partner ids 8 + previous springs 48 in + springs 48 out + history id 8
         "solid_contact_list": 100 * Ns + 112 * P,
+        # predicated: per launch that rebuilds, per active solid: cell ph pl rad flags 80 +
+        # candidates written (about twice the contacts) + reference position 16
+        "solid_candidates": 96 * Ns + 16 * P,
         # per solid and step: cell ph pl read and written 96 + key 4 + walk centre 16 (the sort
         # by cell runs only when lists need it)
         "solid_hash_sort": 116 * c["n_solid"],
@@ -177,7 +180,11 @@ def stage_bytes(stage, c):
         "continuity": (4 * (kff + kfs) + 200) * Nf,
         "momentum": (4 * (kff + kfs) + 260) * Nf,
         "density_reinit": (4 * (kff + kfs) + 120) * Nf,
-        "fluid_lists": (4 * (kff + kfs) + 64) * Nf,
+        # per fluid particle: candidate ids read (about 4/3 of the partners) + list entries
+        # written + own position 32
+        "fluid_lists": (4 * 4 * (kff + kfs) // 3 + 4 * (kff + kfs) + 32) * Nf,
+        # predicated: per launch that rebuilds, candidate ids written + own data 64
+        "fluid_candidates": (4 * 4 * (kff + kfs) // 3 + 64) * Nf,
         "fluid_hash_reorder": 496 * Nf,
         "coupling_lists": 8 * kfs * Nf,
         "coupling_force": 64 * c.get("coupling_pairs", 0) + 96 * Ns,

@@ -85,7 +85,7 @@ class Counts(C.Structure):
 
 
 class LaunchShapes(C.Structure):
-    _fields_ = [("fluid_lanes", _I), ("clump_lanes", _I), ("contact_force_rows", _I), ("contact_detect_rows", _I)]
+    _fields_ = [("fluid_lanes", _I), ("clump_lanes", _I), ("contact_force_rows", _I)]
 
 
 class AuditValues(C.Structure):
@@ -464,7 +464,7 @@ class Engine:
         return lanes.value
 
     def launch_shapes(self):
-        """{fluid_lanes, clump_lanes, contact_force_rows, contact_detect_rows} in use."""
+        """{fluid_lanes, clump_lanes, contact_force_rows} in use."""
         v = LaunchShapes()
         self._chk(self.lib.demsph_get_launch_shapes(self.h, C.byref(v)), "launch_shapes")
         return {n: getattr(v, n) for n, _ in LaunchShapes._fields_}

@@ -219,15 +219,18 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
         e->solidSortStale = false;
     }
     if (fluidStep) {
-        {
+        if (e->forceWalk) {
             TIMED("fluid_lists");
-            if (e->forceWalk) {
-                launchFluidWalkLists(d, true, s);
-            } else {
-                launchFluidWalkLists(d, false, s);
-                launchFluidCandidates(d, s);
-                launchFluidFilter(d, s);
+            launchFluidWalk(d, true, s);
+        } else {
+            {
+                // the walk (once a fluid left the domain) or the candidate
+                // rebuild: returns at once when neither is needed
+                TIMED("fluid_candidates");
+                launchFluidWalk(d, false, s);
             }
+            TIMED("fluid_lists");
+            launchFluidFilter(d, s);
         }
         if (e->nMassive > 0) {  // the coupling force moves only solids with mass
             TIMED("coupling_lists");
@@ -235,9 +238,12 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
         }
     }
     e->par ^= 1;
-    TIMED("solid_contact_list");
     e->walkOrder[e->par] = e->forceWalk;
-    if (!e->forceWalk) launchVerletBuild(d, s);
+    if (!e->forceWalk) {
+        TIMED("solid_candidates");  // returns at once unless the candidates are stale
+        launchVerletBuild(d, s);
+    }
+    TIMED("solid_contact_list");
     launchContactDetect(d, e->par, e->forceWalk, s);
 }
 
@@ -733,7 +739,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.slowMode = dalloc<int>(1, e->owned, e->stream);
             d.need = dalloc<int>(4, e->owned, e->stream);
             d.rowStats = dalloc<int>(3, e->owned, e->stream);
-            d.forceRows = d.detectRows = o.contact_rows_per_warp > 0 ? o.contact_rows_per_warp : 32;
+            d.forceRows = o.contact_rows_per_warp > 0 ? o.contact_rows_per_warp : 32;
             e->adaptRows = o.contact_rows_per_warp == 0;
             const int one = 1;
             const bool walkOnly = o.solid_verlet_skin < 0 || d.grid.gx < 3 || d.grid.gy < 3 || d.grid.gz < 3;
@@ -1069,12 +1075,10 @@ static int rowsPerWarp(double itemsPerRow, int current)
 static void adaptRowsPerWarp(demsph_engine* e, const int* stats)
 {
     DeviceState& d = e->d;
-    const int fr = rowsPerWarp((double)stats[0] / stats[2], d.forceRows);
-    const int dr = rowsPerWarp((double)stats[1] / stats[2], d.detectRows);
-    if (fr == d.forceRows && dr == d.detectRows) return;
+    const int fr = rowsPerWarp((double)stats[0] / stats[1], d.forceRows);
+    if (fr == d.forceRows) return;
     d.forceRows = fr;
-    d.detectRows = dr;
-    dropGraph(e);  // the launch shapes and the state are baked into the graphs
+    dropGraph(e);  // the launch shape and the state are baked into the graphs
 }
 
 int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph)
@@ -1117,7 +1121,7 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
                 run -= len;
             }
         }
-        int rowStats[3] = {0, 0, 0};
+        int rowStats[2] = {0, 0};
         if (graphs && d.nrow > 0 && e->adaptRows) {
             launchRowStats(d, e->par, e->stream);
             CK(cudaMemcpyAsync(rowStats, d.rowStats, sizeof(rowStats), cudaMemcpyDeviceToHost, e->stream));
@@ -1126,7 +1130,7 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
         const int st = readStatus(e, &done);
         if (st == 0) {
             step = s;
-            if (rowStats[2] > 0) adaptRowsPerWarp(e, rowStats);
+            if (rowStats[1] > 0) adaptRowsPerWarp(e, rowStats);
             continue;
         }
         if (st & ~ALL_OVERFLOWS) return fail(e, DEMSPH_ERR_STATE, "unexpected device status " + std::to_string(st));
@@ -1145,7 +1149,6 @@ int demsph_get_launch_shapes(const demsph_engine* e, demsph_launch_shapes* out)
     out->fluid_lanes = e->d.lanes;
     out->clump_lanes = e->d.clumpLanes;
     out->contact_force_rows = e->d.forceRows;
-    out->contact_detect_rows = e->d.detectRows;
     return DEMSPH_OK;
 }
 

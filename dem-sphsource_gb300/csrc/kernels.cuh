@@ -168,11 +168,11 @@ struct DeviceState {
     int* slowMode;           // 1: lists come from the 27-cell walk every step (grid too small, or a solid left the domain)
     int* need;               // [0] most contacts of a row, [1] most candidates of a row,
                              // [2] / [3] most fluid / solid candidates of a fluid particle (for growing)
-    // rows per warp of the contact-force and contact-detection kernels (4..32):
-    // fewer rows when rows hold many items, so that busy scenes still fill the
-    // GPU; results do not depend on them
-    int forceRows, detectRows;
-    int* rowStats;           // [0] contact items, [1] candidates, [2] rows, over a sample of rows
+    // rows per warp of the contact-force kernel (4..32): fewer rows when rows
+    // hold many items, so that busy scenes still fill the GPU; results do not
+    // depend on it
+    int forceRows;
+    int* rowStats;           // [0] contact items, [1] rows, over a sample of rows
 
     // ---- infinite walls ----
     int nw;
@@ -289,12 +289,11 @@ void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, cudaStrea
 void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s);
 
 // lists.cu
-// Fluid lists of a fluid step: the reference's walk (launchFluidWalkLists:
-// walk = true, or once a particle has left the domain), or Verlet candidates
-// rebuilt when stale (launchFluidCandidates) and filtered every fluid step
-// (launchFluidFilter).
-void launchFluidWalkLists(const DeviceState& d, bool walk, cudaStream_t s);
-void launchFluidCandidates(const DeviceState& d, cudaStream_t s);
+// Fluid lists of a fluid step: the reference's walk (walk = true, or once a
+// particle has left the domain) or Verlet candidates rebuilt when stale, in
+// one launch (launchFluidWalk); otherwise the candidates are filtered every
+// fluid step (launchFluidFilter).
+void launchFluidWalk(const DeviceState& d, bool walk, cudaStream_t s);
 void launchFluidFilter(const DeviceState& d, cudaStream_t s);
 void launchCouplingLists(const DeviceState& d, cudaStream_t s);
 // Solid contact candidates, when stale (launchVerletBuild), and the contact
@@ -302,7 +301,7 @@ void launchCouplingLists(const DeviceState& d, cudaStream_t s);
 // 27-cell walk, in the reference's order).
 void launchVerletBuild(const DeviceState& d, cudaStream_t s);
 void launchContactDetect(const DeviceState& d, int parity, bool forceWalk, cudaStream_t s);
-// Contact items and candidates over a sample of rows, into rowStats.
+// Contact items over a sample of rows, into rowStats.
 void launchRowStats(const DeviceState& d, int parity, cudaStream_t s);
 int launchBondFlags(const DeviceState& d, int parity, int* flag, int* pos, int* work, cudaStream_t s);
 void launchBondWrite(const DeviceState& d, int parity, const int* flag, const int* pos, cudaStream_t s);

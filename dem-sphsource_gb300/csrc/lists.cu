@@ -20,7 +20,6 @@
 //     looking the pair (A, B) up in A's previous forward segment, which holds
 //     the same springs the reference finds through B's reverse span.
 #include "kernels.cuh"
-#include "warp_items.cuh"
 
 namespace demsph {
 
@@ -298,20 +297,6 @@ __device__ __forceinline__ void fluidWalk(const DeviceState& d, RunIf when)
     }
 }
 
-// Positions of the contact rows when the fluid candidates are built: a solid
-// moving half the fluid margin since then makes the fluid candidates stale.
-__global__ void kFluidRefSolids(DeviceState d, RunIf when)
-{
-    stepKernelBegin();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= d.nrow || *d.status || !when.active()) return;
-    const int a = d.rowSolid[r];
-    const int4 c = d.scell[a];
-    const float4 h = d.sph[a];
-    d.svref[a] = make_float4((float)c.x * d.grid.cs.x + h.x, (float)c.y * d.grid.cs.y + h.y,
-                             (float)c.z * d.grid.cs.z + h.z, 0.f);
-}
-
 // Walk position (0..26) of cell cj in the 27-cell walk centred on ci, or -1.
 __device__ __forceinline__ int walkPosition(int4 ci, int4 cj)
 {
@@ -563,18 +548,13 @@ __global__ void __launch_bounds__(T) kVerletBuild(DeviceState d)
 __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int forceWalk)
 {
     stepKernelBegin();
-    __shared__ int itemB[T];  // 32 candidate tests per warp: the partner, or -1
-    if (*d.status) return;
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    // lanes 0 .. detectRows - 1 of each warp own a row
-    const int r0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * d.detectRows;
-    const int r = r0 + lane;
-    const bool live = lane < d.detectRows && r < d.nrow;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= d.nrow || *d.status) return;
     // the candidates (if this step rebuilt them) are fresh from here on; the
     // last drift of the step raises the flag again if a solid moves too far
     if (r == 0 && !forceWalk) *(volatile int*)d.rebuild = 0;
-    const int a = live ? d.rowSolid[r] : 0;
+    const int a = d.rowSolid[r];
+    const int4 fa = d.sflags[a];
     const int prev = par ^ 1;
     const int C = d.scap;
     const size_t nr = (size_t)d.nrow;
@@ -590,38 +570,21 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
     };
     const bool walk = forceWalk || *d.slowMode;
     if (walk) {
-        if (live) {
-            const int4 fa = d.sflags[a];
-            const int4 ca = d.scell[a];
-            const float4 ha = d.sph[a], la = d.spl[a];
-            forStencil(ca, ha, la, d.grid, [&](int hash, bool, int, int, int) {
-                for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
-                    const int b = d.ssorted[p];
-                    if (solidPairCandidate(d, a, fa, b) && solidsTouch(d, a, b)) emit(b);
-                }
-            });
-        }
+        const int4 ca = d.scell[a];
+        const float4 ha = d.sph[a], la = d.spl[a];
+        forStencil(ca, ha, la, d.grid, [&](int hash, bool, int, int, int) {
+            for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
+                const int b = d.ssorted[p];
+                if (solidPairCandidate(d, a, fa, b) && solidsTouch(d, a, b)) emit(b);
+            }
+        });
     } else {
-        // the candidate tests of the warp's rows as warp items, taken back in
-        // candidate (index) order
-        int* res = itemB + (threadIdx.x & ~31);
-        warpItems(
-            live ? min(d.vcnt[r], d.vcap) : 0,
-            [&](int owner, int q, bool valid) {
-                const int oa = __shfl_sync(FULL, a, owner);
-                int hit = -1;
-                if (valid) {
-                    const int b = d.vcand[(size_t)q * nr + r0 + owner];
-                    if (solidsTouch(d, oa, b)) hit = b;
-                }
-                res[lane] = hit;
-            },
-            [&](int, int pos) {
-                const int b = res[pos];
-                if (b >= 0) emit(b);
-            });
+        const int n = min(d.vcnt[r], d.vcap);
+        for (int k = 0; k < n; ++k) {
+            const int b = d.vcand[(size_t)k * nr + r];
+            if (solidsTouch(d, a, b)) emit(b);
+        }
     }
-    if (!live) return;
     d.fcnt[par][r] = nf;
     d.rcnt[r] = nb;
     if (nf > C || nb > C) {
@@ -633,7 +596,6 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
         sortSlots(d.fwd[par], r, d.nrow, nf);
         sortSlots(d.rev, r, d.nrow, nb);
     }
-    // each forward pair takes the springs of the same pair in the previous list
     const int prevCnt = min(d.fcnt[prev][r], C);
     for (int q = 0; q < nf; ++q) {
         const size_t slot = (size_t)q * nr + r;
@@ -654,32 +616,29 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
     }
 }
 
-// Contact items (forward + reverse contacts, bonds) and candidates per row over at most 4096
-// evenly spaced rows: the host sizes the rows per warp of the contact kernels
-// from them.
+// Contact items (forward and reverse contacts, bonds) per row over at most
+// 4096 evenly spaced rows: the host sizes the rows per warp of the contact
+// force kernel from them.
 __global__ void kRowStats(DeviceState d, int par)
 {
     stepKernelBegin();
-    __shared__ int sums[3][8];
+    __shared__ int sums[2][8];
     const int stride = max(1, d.nrow / 4096);
-    int items = 0, cand = 0, rows = 0;
+    int items = 0, rows = 0;
     for (int r = threadIdx.x * stride; r < d.nrow; r += blockDim.x * stride) {
         const int a = d.rowSolid[r];
         items += min(d.fcnt[par][r], d.scap) + min(d.rcnt[r], d.scap) + d.bondStart[a + 1] - d.bondStart[a];
-        cand += min(d.vcnt[r], d.vcap);
         ++rows;
     }
     items = __reduce_add_sync(0xffffffffu, items);
-    cand = __reduce_add_sync(0xffffffffu, cand);
     rows = __reduce_add_sync(0xffffffffu, rows);
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
         sums[0][w] = items;
-        sums[1][w] = cand;
-        sums[2][w] = rows;
+        sums[1][w] = rows;
     }
     __syncthreads();
-    if (threadIdx.x < 3) {
+    if (threadIdx.x < 2) {
         int t = 0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sums[threadIdx.x][k];
         d.rowStats[threadIdx.x] = t;
@@ -793,39 +752,44 @@ __global__ void kSolidNormals(DeviceState d, double h)
 
 }  // namespace
 
+// The fluid walk of a fluid step in one launch: the reference's walk (at
+// initialisation, and every fluid step once a fluid or a solid has left the
+// domain), else the Verlet candidates when they are stale - with the contact
+// rows' positions at the rebuild (a solid moving half the fluid margin since
+// then makes the candidates stale) - else nothing.
 template <int L>
-__global__ void __launch_bounds__(T) kFluidWalkLists(DeviceState d, RunIf when)
+__global__ void __launch_bounds__(T) kFluidWalk(DeviceState d, RunIf lists, RunIf cands)
 {
     stepKernelBegin();
-    fluidWalk<L, BUILD_LISTS>(d, when);
-}
-template <int L>
-__global__ void __launch_bounds__(T) kFluidWalkCandidates(DeviceState d, RunIf when)
-{
-    stepKernelBegin();
-    fluidWalk<L, BUILD_CANDIDATES>(d, when);
-}
-
-void launchFluidWalkLists(const DeviceState& d, bool walk, cudaStream_t s)
-{
-    if (d.nf <= 0) return;
-    RunIf when;  // the reference's walk every fluid step (a fluid or a solid left the domain)
-    when.always = walk ? 1 : 0;
-    when.a = d.fslowMode;
-    when.b = d.slowMode;
-    LAUNCH_LANES(kFluidWalkLists, d.lanes, d.nf, T, s, d, when);
+    if (lists.active()) {
+        fluidWalk<L, BUILD_LISTS>(d, lists);
+        return;
+    }
+    if (!cands.active()) return;
+    fluidWalk<L, BUILD_CANDIDATES>(d, cands);
+    if (*d.status) return;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < d.nrow; r += gridDim.x * blockDim.x) {
+        const int a = d.rowSolid[r];
+        const int4 c = d.scell[a];
+        const float4 h = d.sph[a];
+        d.svref[a] = make_float4((float)c.x * d.grid.cs.x + h.x, (float)c.y * d.grid.cs.y + h.y,
+                                 (float)c.z * d.grid.cs.z + h.z, 0.f);
+    }
 }
 
-void launchFluidCandidates(const DeviceState& d, cudaStream_t s)
+void launchFluidWalk(const DeviceState& d, bool walk, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    RunIf when;  // Verlet candidates, when stale
-    when.always = 0;
-    when.a = d.frebuild;
-    when.unless = d.fslowMode;
-    when.unless2 = d.slowMode;
-    LAUNCH_LANES(kFluidWalkCandidates, d.lanes, d.nf, T, s, d, when);
-    if (d.nrow > 0) launchStep(kFluidRefSolids, blocksFor(d.nrow, T), T, s, d, when);
+    RunIf lists;  // the reference's walk every fluid step (a fluid or a solid left the domain)
+    lists.always = walk ? 1 : 0;
+    lists.a = d.fslowMode;
+    lists.b = d.slowMode;
+    RunIf cands;  // Verlet candidates, when stale
+    cands.always = 0;
+    cands.a = d.frebuild;
+    cands.unless = d.fslowMode;
+    cands.unless2 = d.slowMode;
+    LAUNCH_LANES(kFluidWalk, d.lanes, d.nf, T, s, d, lists, cands);
 }
 
 void launchFluidFilter(const DeviceState& d, cudaStream_t s)
@@ -854,7 +818,7 @@ void launchVerletBuild(const DeviceState& d, cudaStream_t s)
 void launchContactDetect(const DeviceState& d, int par, bool forceWalk, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    launchStep(kContactDetect, blocksFor(d.nrow, d.detectRows * (T / 32)), T, s, d, par, forceWalk ? 1 : 0);
+    launchStep(kContactDetect, blocksFor(d.nrow, T), T, s, d, par, forceWalk ? 1 : 0);
 }
 
 void launchRowStats(const DeviceState& d, int par, cudaStream_t s)

@@ -150,9 +150,9 @@ typedef struct demsph_options {
                                     the fluids by cell) once a fluid or solid particle has moved half of
                                     it; 0 = 0.2 x the largest smoothing length; < 0 = no candidates: the
                                     reference's 27-cell walk every fluid step */
-    int contact_rows_per_warp;   /* contact rows per warp of the solid contact-force and contact-detection
-                                    kernels (4, 8, 16 or 32); 0 = adapted to the contacts per row after
-                                    every update.  Results do not depend on it */
+    int contact_rows_per_warp;   /* contact rows per warp of the solid contact-force kernel (4, 8, 16 or
+                                    32); 0 = adapted to the contacts and bonds per row after every update.
+                                    Results do not depend on it */
 } demsph_options;
 
 typedef struct demsph_counts {
@@ -242,12 +242,11 @@ DEMSPH_API int demsph_update(demsph_engine* e, double dt, int first_step, int n_
 DEMSPH_API int demsph_autotune(demsph_engine* e, int* lanes_out);
 /* Launch shapes in use (no counterpart in the reference, whose kernels use fixed
    block sizes): threads per fluid particle, threads per clump, and contact rows
-   per warp of the contact-force and contact-detection kernels. */
+   per warp of the contact-force kernel. */
 typedef struct demsph_launch_shapes {
     int fluid_lanes;
     int clump_lanes;
     int contact_force_rows;
-    int contact_detect_rows;
 } demsph_launch_shapes;
 DEMSPH_API int demsph_get_launch_shapes(const demsph_engine* e, demsph_launch_shapes* out);
 /* The CUDA stream (cudaStream_t) the engine issues all its work on, for
