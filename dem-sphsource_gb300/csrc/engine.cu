@@ -1122,7 +1122,7 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
             }
         }
         int rowStats[2] = {0, 0};
-        if (graphs && d.nrow > 0 && e->adaptRows) {
+        if (graphs && d.nrow > 0 && e->adaptRows && n_steps >= 8) {  // long runs only
             launchRowStats(d, e->par, e->stream);
             CK(cudaMemcpyAsync(rowStats, d.rowStats, sizeof(rowStats), cudaMemcpyDeviceToHost, e->stream));
         }

@@ -107,19 +107,42 @@ __device__ __forceinline__ bool nextCandidate(LaneWalk& w, const int* __restrict
 }
 
 // Next cell member in lane's share of a box of cells (x0..x1, y0..y1, z0..z1,
-// all inside the domain), cells taken round-robin by the lanes.
+// all inside the domain), cells taken round-robin by the lanes.  Cells whose
+// nearest point is beyond the reach (the box's corners and edges) are
+// skipped: no particle in them can be a candidate.
 struct LaneBox {
     int u, p, pe, x0, y0, z0, nx, ny, nz, hx, hy, hz, hash;
+    int ix, iy, iz;  // box-local index of cell u, advanced without dividing
+    int4 c;        // the particle's cell
+    float4 h;      // and its offset in it
+    float reach2;  // squared reach, widened past the FP32 rounding of the cell gaps
 };
+__device__ __forceinline__ float cellGap(int k, int c, float h, float cs)
+{
+    const float lo = (float)(k - c) * cs - h, hi = h - (float)(k - c + 1) * cs;
+    return fmaxf(0.f, fmaxf(lo, hi));
+}
 template <int L>
 __device__ __forceinline__ bool nextBoxMember(LaneBox& b, const int* __restrict__ start, const GridDev& g, int& idx)
 {
     while (b.p >= b.pe) {
         b.u += L;
         if (b.u >= b.nx * b.ny * b.nz) return false;
-        b.hx = b.x0 + b.u % b.nx;
-        b.hy = b.y0 + (b.u / b.nx) % b.ny;
-        b.hz = b.z0 + b.u / (b.nx * b.ny);
+        b.ix += L;
+        while (b.ix >= b.nx) {
+            b.ix -= b.nx;
+            ++b.iy;
+        }
+        while (b.iy >= b.ny) {
+            b.iy -= b.ny;
+            ++b.iz;
+        }
+        b.hx = b.x0 + b.ix;
+        b.hy = b.y0 + b.iy;
+        b.hz = b.z0 + b.iz;
+        const float gx = cellGap(b.hx, b.c.x, b.h.x, g.cs.x), gy = cellGap(b.hy, b.c.y, b.h.y, g.cs.y),
+                    gz = cellGap(b.hz, b.c.z, b.h.z, g.cs.z);
+        if (gx * gx + gy * gy + gz * gz > b.reach2) continue;
         b.hash = (b.hz * g.gy + b.hy) * g.gx + b.hx;
         b.p = start[b.hash];
         b.pe = start[b.hash + 1];
@@ -144,6 +167,14 @@ __device__ __forceinline__ LaneBox boxAround(int lane, int L, int4 c, float4 h, 
     b.ny = max(0, y1 - b.y0 + 1);
     b.nz = max(0, z1 - b.z0 + 1);
     b.hx = b.hy = b.hz = b.hash = 0;
+    b.ix = lane - L;  // cell u = lane - L: one advance of L reaches the lane's first cell
+    b.iy = b.iz = 0;
+    b.c = c;
+    b.h = h;
+    // the candidate test keeps partners up to 1e-4 past the reach (squared);
+    // the gaps carry a few FP32 roundings of the cell size
+    const float wide = reach * 1.001f + 1.e-5f * (g.cs.x + g.cs.y + g.cs.z);
+    b.reach2 = wide * wide;
     return b;
 }
 
@@ -617,18 +648,21 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
 }
 
 // Contact items (forward and reverse contacts, bonds) per row over at most
-// 4096 evenly spaced rows: the host sizes the rows per warp of the contact
-// force kernel from them.
+// 4096 evenly spaced rows, one row per thread, summed into rowStats (zeroed by
+// the caller): the host sizes the rows per warp of the contact force kernel
+// from them.
+constexpr int ROW_SAMPLES = 4096;
 __global__ void kRowStats(DeviceState d, int par)
 {
     stepKernelBegin();
     __shared__ int sums[2][8];
-    const int stride = max(1, d.nrow / 4096);
+    const int stride = max(1, d.nrow / ROW_SAMPLES);
+    const int r = (blockIdx.x * blockDim.x + threadIdx.x) * stride;
     int items = 0, rows = 0;
-    for (int r = threadIdx.x * stride; r < d.nrow; r += blockDim.x * stride) {
+    if (r < d.nrow) {
         const int a = d.rowSolid[r];
-        items += min(d.fcnt[par][r], d.scap) + min(d.rcnt[r], d.scap) + d.bondStart[a + 1] - d.bondStart[a];
-        ++rows;
+        items = min(d.fcnt[par][r], d.scap) + min(d.rcnt[r], d.scap) + d.bondStart[a + 1] - d.bondStart[a];
+        rows = 1;
     }
     items = __reduce_add_sync(0xffffffffu, items);
     rows = __reduce_add_sync(0xffffffffu, rows);
@@ -641,7 +675,7 @@ __global__ void kRowStats(DeviceState d, int par)
     if (threadIdx.x < 2) {
         int t = 0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sums[threadIdx.x][k];
-        d.rowStats[threadIdx.x] = t;
+        atomicAdd(&d.rowStats[threadIdx.x], t);
     }
 }
 
@@ -824,7 +858,8 @@ void launchContactDetect(const DeviceState& d, int par, bool forceWalk, cudaStre
 void launchRowStats(const DeviceState& d, int par, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    launchStep(kRowStats, 1, 256, s, d, par);
+    cudaMemsetAsync(d.rowStats, 0, 2 * sizeof(int), s);
+    launchStep(kRowStats, ROW_SAMPLES / 256, 256, s, d, par);
 }
 
 // Bond creation from the contact list (addBondData at initialisation,
