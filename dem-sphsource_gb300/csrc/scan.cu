@@ -1,7 +1,8 @@
 // Exclusive prefix sums over int arrays (cell counts -> cell starts, per-
-// particle list counts -> CSR offsets).  Reduce-then-scan in three launches
-// (block sums, scan of block sums, block scans plus offsets); for up to 4096
-// elements a single block does it in one launch.  No inter-block waiting, so
+// particle list counts -> CSR offsets).  Up to 524,288 elements one block
+// does it in one launch (kTileScan up to 4096, kScanBlock beyond); longer
+// arrays reduce-then-scan in three launches (block sums, scan of block sums,
+// block scans plus offsets).  No inter-block waiting, so
 // nothing can spin.  Replaces the reference's thrust::inclusive_scan
 // (core/neighborSearch.cu:11-17).
 #include <cuda_runtime.h>
@@ -83,6 +84,42 @@ __global__ void __launch_bounds__(SCAN_THREADS) kTileScan(const int* __restrict_
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = (offsets ? offsets[blockIdx.x] : 0) + total;
 }
 
+// The whole scan in one block, for up to SINGLE_MAX elements: tiles of
+// 1024 x 16 consecutive elements in turn, each thread scanning its 16 and the
+// block its thread totals, with the running total carried between tiles.
+// One launch instead of three (most launches of the sort by cell return at
+// once: the launch count is what costs).
+constexpr int SINGLE_ITEMS = 16;
+constexpr int SINGLE_TILE = SCAN_THREADS * SINGLE_ITEMS;
+constexpr int SINGLE_MAX = 32 * SINGLE_TILE;
+
+__global__ void __launch_bounds__(SCAN_THREADS) kScanBlock(const int* __restrict__ in, int n, int* __restrict__ out,
+                                                           RunIf when)
+{
+    stepKernelBegin();
+    if (!when.active()) return;
+    int carry = 0;
+    for (int base = 0; base < n; base += SINGLE_TILE) {
+        const int first = base + threadIdx.x * SINGLE_ITEMS;
+        int v[SINGLE_ITEMS];
+        int sum = 0;
+#pragma unroll
+        for (int k = 0; k < SINGLE_ITEMS; ++k) {
+            v[k] = first + k < n ? in[first + k] : 0;
+            sum += v[k];
+        }
+        int total;
+        int run = carry + blockExclusiveScan(sum, total);
+#pragma unroll
+        for (int k = 0; k < SINGLE_ITEMS; ++k) {
+            if (first + k < n) out[first + k] = run;
+            run += v[k];
+        }
+        carry += total;
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
 }  // namespace
 
 size_t scanWorkspaceInts(int n)
@@ -100,6 +137,10 @@ void scanExclusive(const int* in, int* out, int n, int* work, cudaStream_t s, Ru
 {
     if (n <= 0) {
         cudaMemsetAsync(out, 0, sizeof(int), s);
+        return;
+    }
+    if (n <= SINGLE_MAX && n > SCAN_TILE) {
+        launchStep(kScanBlock, 1, SCAN_THREADS, s, in, n, out, when);
         return;
     }
     const int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
