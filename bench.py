@@ -167,9 +167,6 @@ def stage_bytes(stage, c):
         # per active solid: cell ph pl rad flags 80 + list and candidate counts 12 + walk
         # centre 8; per pair: partner ids 8 + previous springs 48 in + springs 48 out + history id 8
         "solid_contact_list": 100 * Ns + 112 * P,
-        # predicated: per launch that rebuilds, per active solid: cell ph pl rad flags 80 +
-        # candidates written (about twice the contacts) + reference position 16
-        "solid_candidates": 96 * Ns + 16 * P,
         # per solid and step: cell ph pl read and written 96 + key 4 + walk centre 16 (the sort
         # by cell runs only when lists need it)
         "solid_hash_sort": 116 * c["n_solid"],

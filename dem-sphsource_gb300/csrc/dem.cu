@@ -333,6 +333,10 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
     stepKernelBegin();
     __shared__ float4 itemF[T], itemT[T];  // 32 items per warp
     if (*d.status) return;
+    // every row's contact detection has seen the rebuild flag: the candidates
+    // are fresh from here on, and the last drift of the step raises the flag
+    // again once a solid moves too far
+    if (blockIdx.x == 0 && threadIdx.x == 0) *(volatile int*)d.rebuild = 0;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     // lanes 0 .. forceRows - 1 of each warp own a row

@@ -239,11 +239,7 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
     }
     e->par ^= 1;
     e->walkOrder[e->par] = e->forceWalk;
-    if (!e->forceWalk) {
-        TIMED("solid_candidates");  // returns at once unless the candidates are stale
-        launchVerletBuild(d, s);
-    }
-    TIMED("solid_contact_list");
+    TIMED("solid_contact_list");  // with the candidate rebuild when they are stale
     launchContactDetect(d, e->par, e->forceWalk, s);
 }
 

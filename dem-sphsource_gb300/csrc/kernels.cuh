@@ -164,7 +164,7 @@ struct DeviceState {
                              // grid origin) at the last rebuild
     float skin;              // candidate margin; a rebuild follows once a solid moved skin / 2
     float vmaxEff;           // largest effective radius of a non-dummy solid
-    int* rebuild;            // 1: candidates are stale; set by the hash, cleared by a completed step
+    int* rebuild;            // 1: candidates are stale; set by the last drift, cleared by kSolidForces
     int* slowMode;           // 1: lists come from the 27-cell walk every step (grid too small, or a solid left the domain)
     int* need;               // [0] most contacts of a row, [1] most candidates of a row,
                              // [2] / [3] most fluid / solid candidates of a fluid particle (for growing)
@@ -296,10 +296,9 @@ void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStrea
 void launchFluidWalk(const DeviceState& d, bool walk, cudaStream_t s);
 void launchFluidFilter(const DeviceState& d, cudaStream_t s);
 void launchCouplingLists(const DeviceState& d, cudaStream_t s);
-// Solid contact candidates, when stale (launchVerletBuild), and the contact
-// rows of the step (launchContactDetect; forceWalk: from the reference's
-// 27-cell walk, in the reference's order).
-void launchVerletBuild(const DeviceState& d, cudaStream_t s);
+// The contact rows of the step, each row first rebuilding its candidates when
+// they are stale (launchContactDetect; forceWalk: from the reference's 27-cell
+// walk, in the reference's order).
 void launchContactDetect(const DeviceState& d, int parity, bool forceWalk, cudaStream_t s);
 // Contact items over a sample of rows, into rowStats.
 void launchRowStats(const DeviceState& d, int parity, cudaStream_t s);

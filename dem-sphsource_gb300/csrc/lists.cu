@@ -524,11 +524,8 @@ __device__ __forceinline__ float3 gridPos(int4 c, float4 h, const GridDev& g)
 // eff_a + eff_b + skin then).  All non-dummy solids are inside the domain
 // here (otherwise the lists come from the 27-cell walk), so the cells are
 // plain (x, y, z) cells.
-__global__ void __launch_bounds__(T) kVerletBuild(DeviceState d)
+__device__ __forceinline__ void verletBuildRow(const DeviceState& d, int r)
 {
-    stepKernelBegin();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= d.nrow || *d.status || !*d.rebuild || *d.slowMode) return;
     const int a = d.rowSolid[r];
     const int4 fa = d.sflags[a];
     const int4 ca = d.scell[a];
@@ -581,9 +578,10 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
     stepKernelBegin();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= d.nrow || *d.status) return;
-    // the candidates (if this step rebuilt them) are fresh from here on; the
-    // last drift of the step raises the flag again if a solid moves too far
-    if (r == 0 && !forceWalk) *(volatile int*)d.rebuild = 0;
+    const bool walk = forceWalk || *d.slowMode;
+    // stale candidates are rebuilt first, row by row (the contact force
+    // kernel clears the flag once every row has read it)
+    if (!walk && *d.rebuild) verletBuildRow(d, r);
     const int a = d.rowSolid[r];
     const int4 fa = d.sflags[a];
     const int prev = par ^ 1;
@@ -599,7 +597,6 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
             ++nb;
         }
     };
-    const bool walk = forceWalk || *d.slowMode;
     if (walk) {
         const int4 ca = d.scell[a];
         const float4 ha = d.sph[a], la = d.spl[a];
@@ -841,12 +838,6 @@ void launchCouplingLists(const DeviceState& d, cudaStream_t s)
     cudaMemsetAsync(d.coupCount, 0, sizeof(int) * d.ns, s);
     launchStep(kCoupFill, blocksFor(d.nf, 256), 256, s, d);
     launchStep(kCoupSort, blocksFor(d.ns, 256), 256, s, d);
-}
-
-void launchVerletBuild(const DeviceState& d, cudaStream_t s)
-{
-    if (d.nrow <= 0) return;
-    launchStep(kVerletBuild, blocksFor(d.nrow, T), T, s, d);
 }
 
 void launchContactDetect(const DeviceState& d, int par, bool forceWalk, cudaStream_t s)
