@@ -345,6 +345,9 @@ __device__ __forceinline__ int walkPosition(int4 ci, int4 cj)
 template <int L>
 __global__ void __launch_bounds__(T) kFluidFilter(DeviceState d)
 {
+    // one lane per particle walks a long candidate list: 4 rounds of reads in
+    // flight; with 4 or 8 lanes a round already covers many candidates
+    constexpr int FILTER_UNROLL = L == 1 ? 4 : (L == 2 ? 2 : 1);
     stepKernelBegin();
     const int th = blockIdx.x * blockDim.x + threadIdx.x;
     if ((th & ~31) >= d.nf * L || *d.status || *d.fslowMode || *d.slowMode) return;
@@ -368,35 +371,52 @@ __global__ void __launch_bounds__(T) kFluidFilter(DeviceState d)
         nc = min(d.fvcn[i], d.kvf);
         ns = min(d.fvsn[i], d.kvs);
     }
+    // candidates are taken FILTER_UNROLL rounds of L at a time: the rounds'
+    // reads are issued together, their results compacted round by round (the
+    // list order of one round per iteration)
     int nff = 0;
-    for (int base = 0; __any_sync(0xffffffffu, base < nc); base += L) {
-        const int k = base + lane;
-        bool take = false;
-        int j = 0, t = -1;
-        if (k < nc) {
-            j = (int)d.fvc[(size_t)k * n + i];
-            const int4 cj = d.fcell[j];
-            t = walkPosition(ci, cj);
-            if (t >= 0) {
-                const float4 hj = d.fph[0][j];
-                const float3 r = relF(ci, hi, cj, hj, d.grid);
-                const float c = 2.f * fmaxf(hi.w, hj.w);
-                const float d2 = dot3(r, r), c2 = c * c;
-                if (d2 < c2 * (1.f - 1.e-5f)) {
-                    take = true;
-                } else if (d2 <= c2 * (1.f + 1.e-5f)) {
-                    const dfl hJ = df_make(hj.w, d.fpl[0][j].w);
-                    const dfl rad = dfMax(hI, hJ);
-                    take = withinCut(ci, hi, li, cj, hj, d.fpl[0], j, df_add(rad, rad), d.grid);
-                }
+    for (int base = 0; __any_sync(0xffffffffu, base < nc); base += FILTER_UNROLL * L) {
+        int j[FILTER_UNROLL];
+        int4 cj[FILTER_UNROLL];
+        float4 hj[FILTER_UNROLL];
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const int k = base + u * L + lane;
+            j[u] = k < nc ? (int)d.fvc[(size_t)k * n + i] : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            if (j[u] >= 0) {
+                cj[u] = d.fcell[j[u]];
+                hj[u] = d.fph[0][j[u]];
             }
         }
-        const unsigned mine = (__ballot_sync(0xffffffffu, take) >> groupShift) & groupBits;
-        if (take) {
-            const int slot = nff + __popc(mine & below);
-            if (slot < d.kff) d.ff[(size_t)slot * n + i] = ffEntry(j, t, true);
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            bool take = false;
+            int t = -1;
+            if (j[u] >= 0) {
+                t = walkPosition(ci, cj[u]);
+                if (t >= 0) {
+                    const float3 r = relF(ci, hi, cj[u], hj[u], d.grid);
+                    const float c = 2.f * fmaxf(hi.w, hj[u].w);
+                    const float d2 = dot3(r, r), c2 = c * c;
+                    if (d2 < c2 * (1.f - 1.e-5f)) {
+                        take = true;
+                    } else if (d2 <= c2 * (1.f + 1.e-5f)) {
+                        const dfl hJ = df_make(hj[u].w, d.fpl[0][j[u]].w);
+                        const dfl rad = dfMax(hI, hJ);
+                        take = withinCut(ci, hi, li, cj[u], hj[u], d.fpl[0], j[u], df_add(rad, rad), d.grid);
+                    }
+                }
+            }
+            const unsigned mine = (__ballot_sync(0xffffffffu, take) >> groupShift) & groupBits;
+            if (take) {
+                const int slot = nff + __popc(mine & below);
+                if (slot < d.kff) d.ff[(size_t)slot * n + i] = ffEntry(j[u], t, true);
+            }
+            nff += __popc(mine);
         }
-        nff += __popc(mine);
     }
     int nfs = 0;
     for (int base = 0; __any_sync(0xffffffffu, base < ns); base += L) {
