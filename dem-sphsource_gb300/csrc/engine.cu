@@ -700,9 +700,14 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                         e->moveKind[i] = 0;
                         continue;
                     }
-                    if (flags[i].w & F_DUMMY) e->moveKind[i] = 2;
                     const double3 v = v3(sc->solid_velocity, i);
-                    if (!(flags[i].w & F_DUMMY) || v.x != 0.0 || v.y != 0.0 || v.z != 0.0) move.push_back(i);
+                    const bool moving = v.x != 0.0 || v.y != 0.0 || v.z != 0.0;
+                    if (flags[i].w & F_DUMMY) {
+                        e->moveKind[i] = 2;
+                        e->dummyIdx.push_back(i);
+                        e->dummyMoving.push_back(moving ? 1 : 0);
+                    }
+                    if (!(flags[i].w & F_DUMMY) || moving) move.push_back(i);
                 }
                 d.nmove = (int)move.size();
                 d.moveList = dalloc<int>(move.size(), e->owned, e->stream);

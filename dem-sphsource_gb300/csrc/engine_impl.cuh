@@ -57,6 +57,8 @@ struct demsph_engine {
     bool solidSortStale = true;   // solid cells must be recomputed although no solid has mass
     std::vector<unsigned char> moveKind;  // per solid: 0 clump pebble, 1 integrated, 2 dummy (integrated when moving)
     std::vector<int> moveHost;            // the device move list
+    std::vector<int> dummyIdx;            // the dummy particles (moveKind 2), and whether each is
+    std::vector<unsigned char> dummyMoving;  // in the move list (given a velocity)
     bool walkOrder[2] = {true, true};  // list of each parity is in the reference's walk order
     bool initialized = false;
     int debug = 0;

@@ -343,7 +343,19 @@ int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel,
     ENGINE_GUARD(e)
     DeviceState& d = e->d;
     if (d.ns == 0) return DEMSPH_OK;
-    if (vel) {  // dummy particles given a velocity join the integration
+    // dummy particles given a velocity join the integration: the move list
+    // changes only when a dummy particle starts or stops moving
+    bool moveChanged = false;
+    if (vel)
+        for (size_t q = 0; q < e->dummyIdx.size(); ++q) {
+            const size_t i = (size_t)e->dummyIdx[q];
+            const unsigned char m = (vel[3 * i] != 0.0 || vel[3 * i + 1] != 0.0 || vel[3 * i + 2] != 0.0) ? 1 : 0;
+            if (m != e->dummyMoving[q]) {
+                e->dummyMoving[q] = m;
+                moveChanged = true;
+            }
+        }
+    if (moveChanged) {
         std::vector<int> move;
         move.reserve(e->moveHost.size());
         for (int i = 0; i < d.ns; ++i) {
