@@ -411,6 +411,22 @@ def tiny_granular(seed=3, with_probe_fluid=True):
     return r
 
 
+def tiny_granular_wide(cells=700_000, seed=3):
+    """:func:`tiny_granular` in a domain widened (empty cells around the grains)
+    to about ``cells`` grid cells, so the sort by cell scans long cell arrays:
+    one block up to 524,288 cells, three launches beyond."""
+    r = tiny_granular(seed)
+    idx = next(k for k, (fn, _) in enumerate(r.calls) if fn == "setDomain")
+    o, s = r.calls[idx][1]
+    base = s[0] * s[1] * s[2]
+    # cells of 2 x the largest effective radius (1.2 mm + margin): scale x and y
+    cell = 2.4e-3
+    k = max(1.0, float(np.sqrt(cells * cell ** 3 / base)))
+    r.calls[idx] = ("setDomain", (o, (s[0] * k, s[1] * k, s[2])))
+    r.name = f"tiny_granular_wide_{cells}"
+    return r
+
+
 def tiny_two_fluids(seed=6):
     """:func:`tiny_dam_break` with a second, denser column beside the first
     (its own rest density, sound speed and smoothing length)."""

@@ -201,6 +201,31 @@ def test_contact_rows_per_warp_do_not_change_results(ds, scenes, name):
             assert np.array_equal(s1[k], s0[k]), k
 
 
+@pytest.mark.parametrize("cells,lo,hi", [(200_000, 4096, 524_288), (1_000_000, 524_288, 2_500_000)])
+def test_large_grids_sort_like_the_oracle(ds, scenes, cells, lo, hi):
+    """The sort by cell scans the cell counts in one block up to 524,288
+    cells and in three launches beyond: a granular scene in a widened domain
+    gives the oracle's cell spans, sorted order and contact lists at
+    initialisation and after every one of ten steps (the candidates are
+    rebuilt, and the solids re-sorted, along the way)."""
+    recipe = scenes.tiny_granular_wide(cells)
+    b, sc = ds.build_scene(recipe)
+    eng = ds.Engine(sc, solid_verlet_skin=1.0e-9)  # rebuild (and sort) nearly every step
+    orc = oracle_for(sc)
+    eng.initialize()
+    orc.initialize()
+    assert lo < eng.counts().grid_cells <= hi
+    bad, _ = compare_integer_artefacts(eng, orc)
+    assert bad == [], f"integer artefacts differ after initialize: {bad}"
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for step in range(1, 11):
+        eng.step(dt, step, gap)
+        orc.update(dt, step, 1, gap)
+        bad, _ = compare_integer_artefacts(eng, orc, skip_fluid_hash=(step % gap != 0))
+        assert bad == [], f"step {step}: integer artefacts differ: {bad}"
+        _check_step(eng, orc, sc, _spacing(recipe), step, dt, DRIFT_TOL, 1e-8)
+
+
 def test_drift_bounded_over_run(ds, scenes):
     """Forty steps of the coupled scene: the engine stays within bounded
     distance of the FP64 oracle (no systematic FP32 drift)."""
