@@ -740,6 +740,11 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.slowMode = dalloc<int>(1, e->owned, e->stream);
             d.need = dalloc<int>(4, e->owned, e->stream);
             d.rowStats = dalloc<int>(3, e->owned, e->stream);
+            d.gridBar = dalloc<unsigned>(2, e->owned, e->stream);
+            {
+                const char* v = std::getenv("DEMSPH_COOPERATIVE_SORT");
+                d.sortBlocks = (v && v[0] == '0') ? 0 : cooperativeSortBlocks();
+            }
             d.forceRows = o.contact_rows_per_warp > 0 ? o.contact_rows_per_warp : 32;
             e->adaptRows = o.contact_rows_per_warp == 0;
             const int one = 1;

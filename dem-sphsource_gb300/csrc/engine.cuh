@@ -25,6 +25,7 @@ enum StatusBits : int {
     ST_VERLET_OVERFLOW = 16, // a solid has more contact candidates than its row holds
     ST_MODE_CHANGE = 32,     // a particle left the domain: lists switch to the 27-cell walk; redo the step
     ST_FVERLET_OVERFLOW = 64,// a fluid particle has more list candidates than it holds
+    ST_BARRIER_TIMEOUT = 128,// a grid barrier of a cooperative launch gave up waiting (an error)
 };
 
 // Neighbour list entries.  A fluid partner entry holds the partner's slot j,

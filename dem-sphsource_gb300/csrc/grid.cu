@@ -14,6 +14,8 @@
 // Fluids are then physically reordered (gathered) into that order; solids keep
 // their original order and use the sorted index.  The solid hash also checks
 // how far each solid has moved since its contact candidates were built.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace demsph {
@@ -164,7 +166,80 @@ __global__ void kSolidRank(DeviceState d, RunIf when)
     d.scellCount[d.skey[e]] = 0;  // the counts are consumed: clear them for the next sort
 }
 
+// The sort by cell of a step in ONE launch (keys from the last integration):
+// the slots in the cells, the scan of the counts into the cell starts, the
+// scatter and the stable rank of kSolidSlots, scanExclusive, kScatter and
+// kSolidRank, as phases of a cooperative launch separated by grid barriers.
+// Steps that do not sort pay one launch that returns at once instead of four.
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_TILE = SORT_THREADS * 16;
+
+__global__ void __launch_bounds__(SORT_THREADS) kSolidSortCoop(DeviceState d, RunIf when)
+{
+    stepKernelBegin();
+    // uniform over the blocks: no phase changes these flags or the status
+    if (*d.status || !when.active()) return;
+    unsigned gen = ((volatile unsigned*)d.gridBar)[1];
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.ns; i += stride)
+        d.sslotInCell[i] = atomicAdd(&d.scellCount[d.skey[i]], 1);
+    if (!gridBarrier(d.gridBar, gen, d.status)) return;
+    // cell starts: tile sums, then each tile scanned from the sum of the tiles before it
+    const int num = d.grid.num, tiles = (num + SORT_TILE - 1) / SORT_TILE;
+    int* tileSum = d.scanWork;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const int first = t * SORT_TILE + threadIdx.x * 16;
+        int sum = 0;
+        for (int k = 0; k < 16; ++k)
+            if (first + k < num) sum += d.scellCount[first + k];
+        int total;
+        blockScan<SORT_THREADS>(sum, total);
+        if (threadIdx.x == 0) tileSum[t] = total;
+    }
+    if (!gridBarrier(d.gridBar, gen, d.status)) return;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+        int before = 0;
+        for (int q = threadIdx.x; q < t; q += blockDim.x) before += tileSum[q];
+        int offset;
+        blockScan<SORT_THREADS>(before, offset);
+        const int first = t * SORT_TILE + threadIdx.x * 16;
+        int v[16];
+        int sum = 0;
+        for (int k = 0; k < 16; ++k) {
+            v[k] = first + k < num ? d.scellCount[first + k] : 0;
+            sum += v[k];
+        }
+        int total;
+        int run = offset + blockScan<SORT_THREADS>(sum, total);
+        for (int k = 0; k < 16; ++k) {
+            if (first + k < num) d.scellStart[first + k] = run;
+            run += v[k];
+        }
+        if (t == tiles - 1 && threadIdx.x == 0) d.scellStart[num] = offset + total;
+    }
+    if (!gridBarrier(d.gridBar, gen, d.status)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.ns; i += stride)
+        d.ssortTmp[d.scellStart[d.skey[i]] + d.sslotInCell[i]] = i;
+    if (!gridBarrier(d.gridBar, gen, d.status)) return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < d.ns; p += stride) {
+        int e;
+        const int q = stableRank(p, d.ssortTmp, d.skey, d.scellStart, nullptr, e);
+        d.ssorted[q] = e;
+        d.scellCount[d.skey[e]] = 0;  // the counts are consumed: clear them for the next sort
+    }
+}
+
 }  // namespace
+
+int cooperativeSortBlocks()
+{
+    int dev = 0, sms = 0, perSm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kSolidSortCoop, SORT_THREADS, 0) != cudaSuccess)
+        return 0;
+    // two blocks per SM at most: room for other scenes' kernels beside it
+    return std::max(0, sms * std::min(perSm, 2));
+}
 
 static RunIf fluidReorderWhen(const DeviceState& d, bool force)
 {
@@ -210,13 +285,18 @@ void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, cudaStrea
     if (d.ns <= 0) return;
     if (force)  // positions that no integration has hashed (creation, an upload)
         launchStep(kSolidHash, blocksFor(d.ns, T), T, s, d, solidSortWhen(d, true, fluidStep));
-    else        // keys come from the last integration of the previous step
+    else if (d.sortBlocks <= 0)  // keys come from the last integration of the previous step
         launchStep(kSolidSlots, blocksFor(d.ns, T), T, s, d, solidSortWhen(d, false, fluidStep));
 }
 
 void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s)
 {
     if (d.ns <= 0) return;
+    if (!force && d.sortBlocks > 0) {
+        // the slots were not taken by launchSolidHash: the cooperative launch does everything
+        launchCooperative(kSolidSortCoop, (unsigned)d.sortBlocks, SORT_THREADS, s, d, solidSortWhen(d, false, fluidStep));
+        return;
+    }
     // scellCount is zero here: cleared at creation, by kSolidRank after every
     // sort, and by the host after a step abandoned in kSolidHash
     const RunIf when = solidSortWhen(d, force, fluidStep);

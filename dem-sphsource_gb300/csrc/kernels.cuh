@@ -31,6 +31,92 @@ __device__ __forceinline__ void stepKernelBegin()
 // (default on; DEMSPH_OVERLAP_LAUNCHES=0 in the environment turns it off).
 bool overlapLaunches();
 
+// Launches a step kernel whose blocks wait on one another (grid barriers) as
+// a cooperative launch: all its blocks are resident at once, or the launch
+// fails.  Returns false when the launch was refused.
+template <typename... KArgs, typename... Args>
+inline bool launchCooperative(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args)
+{
+    ++t_kernelLaunches;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...) == cudaSuccess;
+}
+
+// Barrier over all blocks of a cooperative launch.  bar[0] counts arrivals,
+// bar[1] is the generation; `gen` is the generation this block waits past
+// (read from bar[1] when the launch began, before any barrier of the launch
+// could complete).  The wait is bounded: after about 0.5 s it records
+// ST_BARRIER_TIMEOUT and returns false, and the block should return.
+__device__ __forceinline__ bool gridBarrier(unsigned* bar, unsigned& gen, int* status)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        __threadfence();
+        if (atomicAdd(&bar[0], 1u) + 1u == gridDim.x) {
+            bar[0] = 0u;
+            __threadfence();
+            atomicExch(&bar[1], gen + 1u);
+        } else {
+            int spins = 0;
+            while (((volatile unsigned*)bar)[1] == gen) {
+                if (++spins > (1 << 22)) {
+                    atomicOr(status, ST_BARRIER_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    ++gen;
+    return ok != 0;
+}
+
+// Block-wide exclusive scan of one value per thread (THREADS threads);
+// returns the thread's prefix and sets the block total.  Safe to call again
+// right away (it ends with a barrier).
+template <int THREADS>
+__device__ __forceinline__ int blockScan(int v, int& total)
+{
+    __shared__ int warpSums[THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warpSums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int t = lane < THREADS / 32 ? warpSums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < THREADS / 32) warpSums[lane] = t;
+    }
+    __syncthreads();
+    const int before = warp ? warpSums[warp - 1] : 0;
+    total = warpSums[THREADS / 32 - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
 // Launches a step kernel (one that opens with stepKernelBegin) on stream s.
 template <typename... KArgs, typename... Args>
 inline void launchStep(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args)
@@ -173,6 +259,8 @@ struct DeviceState {
     // depend on it
     int forceRows;
     int* rowStats;           // [0] contact items, [1] rows, over a sample of rows
+    unsigned* gridBar;       // [2]: grid barrier of the cooperative sort (arrivals, generation)
+    int sortBlocks;          // blocks of the cooperative sort (0: the four-launch sort)
 
     // ---- infinite walls ----
     int nw;
@@ -287,6 +375,10 @@ void launchFluidReorder(const DeviceState& d, bool force, cudaStream_t s);
 // when the fluid lists walk the cells.
 void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s);
 void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s);
+// Blocks of the one-launch cooperative sort on this device (0 when it cannot
+// be used); DEMSPH_COOPERATIVE_SORT=0 in the environment keeps the four-launch
+// sort.
+int cooperativeSortBlocks();
 
 // lists.cu
 // Fluid lists of a fluid step: the reference's walk (walk = true, or once a
