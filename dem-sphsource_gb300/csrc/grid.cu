@@ -24,13 +24,10 @@ namespace {
 
 constexpr int T = 256;
 
-// Cell keys of the fluids every fluid step; on reorder steps the whole
+// Cell key of fluid slot i every fluid step; on reorder steps the whole
 // particle is copied into the gather sources and takes a slot in its cell.
-__global__ void kFluidHash(DeviceState d, RunIf sortNow)
+__device__ __forceinline__ void fluidHashOne(const DeviceState& d, int i, const RunIf& sortNow)
 {
-    stepKernelBegin();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.nf || *d.status) return;
     int4 c = d.fcell[i];
     float4 h = d.fph[0][i];
     float4 l = d.fpl[0][i];
@@ -66,6 +63,14 @@ __global__ void kFluidHash(DeviceState d, RunIf sortNow)
     d.fslotInCell[i] = atomicAdd(&d.fcellCount[key], 1);
 }
 
+__global__ void kFluidHash(DeviceState d, RunIf sortNow)
+{
+    stepKernelBegin();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nf || *d.status) return;
+    fluidHashOne(d, i, sortNow);
+}
+
 __global__ void kScatter(int n, const int* __restrict__ key, const int* __restrict__ slotInCell,
                          const int* __restrict__ cellStart, int* __restrict__ out, const int* status, RunIf when)
 {
@@ -92,11 +97,8 @@ __device__ __forceinline__ int stableRank(int p, const int* __restrict__ sorted,
     return s + rank;
 }
 
-__global__ void kFluidGather(DeviceState d, RunIf when)
+__device__ __forceinline__ void fluidGatherOne(const DeviceState& d, int p)
 {
-    stepKernelBegin();
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= d.nf || *d.status || !when.active()) return;
     int e;
     const int q = stableRank(p, d.fsortTmp, d.fkey, d.fcellStart, d.tid, e);
     d.fcell[q] = d.tcell[e];
@@ -112,6 +114,14 @@ __global__ void kFluidGather(DeviceState d, RunIf when)
     d.fid[q] = id;
     d.fslot[id] = q;
     d.fcellCount[d.fkey[e]] = 0;  // the counts are consumed: clear them for the next reorder
+}
+
+__global__ void kFluidGather(DeviceState d, RunIf when)
+{
+    stepKernelBegin();
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.nf || *d.status || !when.active()) return;
+    fluidGatherOne(d, p);
 }
 
 // Cell keys of the solids every step (they are exported in the reference's
@@ -174,6 +184,47 @@ __global__ void kSolidRank(DeviceState d, RunIf when)
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_TILE = SORT_THREADS * 16;
 
+// Exclusive scan of counts[0..num) into starts[0..num] by all blocks of a
+// cooperative launch: tile sums, a grid barrier, then each tile scanned from
+// the sum of the tiles before it, and a closing barrier.  False when a
+// barrier gave up (the caller returns).
+__device__ bool cooperativeScan(const int* __restrict__ counts, int* __restrict__ starts, int num, int* tileSum,
+                                unsigned* bar, unsigned& gen, int* status)
+{
+    const int tiles = (num + SORT_TILE - 1) / SORT_TILE;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const int first = t * SORT_TILE + threadIdx.x * 16;
+        int sum = 0;
+        for (int k = 0; k < 16; ++k)
+            if (first + k < num) sum += counts[first + k];
+        int total;
+        blockScan<SORT_THREADS>(sum, total);
+        if (threadIdx.x == 0) tileSum[t] = total;
+    }
+    if (!gridBarrier(bar, gen, status)) return false;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+        int before = 0;
+        for (int q = threadIdx.x; q < t; q += blockDim.x) before += tileSum[q];
+        int offset;
+        blockScan<SORT_THREADS>(before, offset);
+        const int first = t * SORT_TILE + threadIdx.x * 16;
+        int v[16];
+        int sum = 0;
+        for (int k = 0; k < 16; ++k) {
+            v[k] = first + k < num ? counts[first + k] : 0;
+            sum += v[k];
+        }
+        int total;
+        int run = offset + blockScan<SORT_THREADS>(sum, total);
+        for (int k = 0; k < 16; ++k) {
+            if (first + k < num) starts[first + k] = run;
+            run += v[k];
+        }
+        if (t == tiles - 1 && threadIdx.x == 0) starts[num] = offset + total;
+    }
+    return gridBarrier(bar, gen, status);
+}
+
 __global__ void __launch_bounds__(SORT_THREADS) kSolidSortCoop(DeviceState d, RunIf when)
 {
     stepKernelBegin();
@@ -184,40 +235,7 @@ __global__ void __launch_bounds__(SORT_THREADS) kSolidSortCoop(DeviceState d, Ru
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.ns; i += stride)
         d.sslotInCell[i] = atomicAdd(&d.scellCount[d.skey[i]], 1);
     if (!gridBarrier(d.gridBar, gen, d.status)) return;
-    // cell starts: tile sums, then each tile scanned from the sum of the tiles before it
-    const int num = d.grid.num, tiles = (num + SORT_TILE - 1) / SORT_TILE;
-    int* tileSum = d.scanWork;
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
-        const int first = t * SORT_TILE + threadIdx.x * 16;
-        int sum = 0;
-        for (int k = 0; k < 16; ++k)
-            if (first + k < num) sum += d.scellCount[first + k];
-        int total;
-        blockScan<SORT_THREADS>(sum, total);
-        if (threadIdx.x == 0) tileSum[t] = total;
-    }
-    if (!gridBarrier(d.gridBar, gen, d.status)) return;
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
-        int before = 0;
-        for (int q = threadIdx.x; q < t; q += blockDim.x) before += tileSum[q];
-        int offset;
-        blockScan<SORT_THREADS>(before, offset);
-        const int first = t * SORT_TILE + threadIdx.x * 16;
-        int v[16];
-        int sum = 0;
-        for (int k = 0; k < 16; ++k) {
-            v[k] = first + k < num ? d.scellCount[first + k] : 0;
-            sum += v[k];
-        }
-        int total;
-        int run = offset + blockScan<SORT_THREADS>(sum, total);
-        for (int k = 0; k < 16; ++k) {
-            if (first + k < num) d.scellStart[first + k] = run;
-            run += v[k];
-        }
-        if (t == tiles - 1 && threadIdx.x == 0) d.scellStart[num] = offset + total;
-    }
-    if (!gridBarrier(d.gridBar, gen, d.status)) return;
+    if (!cooperativeScan(d.scellCount, d.scellStart, d.grid.num, d.scanWork, d.gridBar, gen, d.status)) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.ns; i += stride)
         d.ssortTmp[d.scellStart[d.skey[i]] + d.sslotInCell[i]] = i;
     if (!gridBarrier(d.gridBar, gen, d.status)) return;
@@ -227,6 +245,27 @@ __global__ void __launch_bounds__(SORT_THREADS) kSolidSortCoop(DeviceState d, Ru
         d.ssorted[q] = e;
         d.scellCount[d.skey[e]] = 0;  // the counts are consumed: clear them for the next sort
     }
+}
+
+// The fluid hash of a fluid step and, when the fluids are reordered, the
+// reorder (scan of the counts, scatter, stable gather) in ONE cooperative
+// launch.  Whether to reorder is decided after the hash, from flags and a
+// status no later phase changes: a fluid leaving the domain in the hash sets
+// the status (the step is redone) and every block returns.
+__global__ void __launch_bounds__(SORT_THREADS) kFluidReorderCoop(DeviceState d, RunIf when)
+{
+    stepKernelBegin();
+    if (*d.status) return;
+    unsigned gen = ((volatile unsigned*)d.gridBar)[1];
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nf; i += stride) fluidHashOne(d, i, when);
+    if (!gridBarrier(d.gridBar, gen, d.status)) return;
+    if (*(volatile int*)d.status || !when.active()) return;
+    if (!cooperativeScan(d.fcellCount, d.fcellStart, d.grid.num, d.scanWork, d.gridBar, gen, d.status)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nf; i += stride)
+        d.fsortTmp[d.fcellStart[d.fkey[i]] + d.fslotInCell[i]] = i;
+    if (!gridBarrier(d.gridBar, gen, d.status)) return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < d.nf; p += stride) fluidGatherOne(d, p);
 }
 
 }  // namespace
@@ -253,12 +292,16 @@ static RunIf fluidReorderWhen(const DeviceState& d, bool force)
 void launchFluidHash(const DeviceState& d, bool force, cudaStream_t s)
 {
     if (d.nf <= 0) return;
+    if (d.sortBlocks > 0) {  // hash and reorder in one cooperative launch
+        launchCooperative(kFluidReorderCoop, (unsigned)d.sortBlocks, SORT_THREADS, s, d, fluidReorderWhen(d, force));
+        return;
+    }
     launchStep(kFluidHash, blocksFor(d.nf, T), T, s, d, fluidReorderWhen(d, force));
 }
 
 void launchFluidReorder(const DeviceState& d, bool force, cudaStream_t s)
 {
-    if (d.nf <= 0) return;
+    if (d.nf <= 0 || d.sortBlocks > 0) return;
     // fcellCount is zero here: cleared at creation, by kFluidGather after every
     // reorder, and by the host after a step abandoned in kFluidHash
     const RunIf when = fluidReorderWhen(d, force);
