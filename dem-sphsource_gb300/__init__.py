@@ -496,6 +496,17 @@ class Engine:
         return out
 
 
+def selftest_barrier(device=0, missing=1):
+    """Runs the grid-barrier self-test (demsph_selftest_barrier); returns the
+    device status bits (128 when the barrier wait ran out)."""
+    lib = load_library()
+    st = _I()
+    rc = lib.demsph_selftest_barrier(_I(device), _I(missing), C.byref(st))
+    if rc != DEMSPH_OK:
+        raise DemSphError(rc, "demsph_selftest_barrier")
+    return st.value
+
+
 def estimate_bytes(scene, **opts):
     """Device memory demsph_create will allocate for the scene (an estimate)."""
     lib = load_library()

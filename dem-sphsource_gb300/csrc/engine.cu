@@ -415,6 +415,7 @@ int neighborSearchChecked(demsph_engine* e, int iStep, int gap)
         const int st = readStatus(e);
         if (st == 0) return DEMSPH_OK;
         e->par = parBefore;
+        if (st & ST_BARRIER_TIMEOUT) return fail(e, DEMSPH_ERR_TIMEOUT, "a grid barrier of a cooperative launch gave up waiting");
         if (st & ~ALL_OVERFLOWS) return fail(e, DEMSPH_ERR_STATE, "unexpected device status " + std::to_string(st));
         grow(e, st);
     }
@@ -442,6 +443,14 @@ const char* demsph_status_string(int s)
 
 const char* demsph_last_error(const demsph_engine* e) { return e ? e->err.c_str() : ""; }
 const char* demsph_version(void) { return "demsph_gb300 0.1 (sm_103a)"; }
+
+int demsph_selftest_barrier(int device, int missing, int* status_out)
+{
+    if (!status_out || missing < 0 || missing > 1000) return DEMSPH_ERR_ARGUMENT;
+    *status_out = 0;
+    if (cudaSetDevice(device) != cudaSuccess) return DEMSPH_ERR_NO_DEVICE;
+    return selftestBarrier(missing, status_out);
+}
 
 int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engine** out)
 {
@@ -1139,6 +1148,7 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
             if (rowStats[1] > 0) adaptRowsPerWarp(e, rowStats);
             continue;
         }
+        if (st & ST_BARRIER_TIMEOUT) return fail(e, DEMSPH_ERR_TIMEOUT, "a grid barrier of a cooperative launch gave up waiting");
         if (st & ~ALL_OVERFLOWS) return fail(e, DEMSPH_ERR_STATE, "unexpected device status " + std::to_string(st));
         step += done;                        // steps before the failed one completed
         e->par = startPar ^ (done & 1);      // every step builds one contact list

@@ -270,6 +270,35 @@ __global__ void __launch_bounds__(SORT_THREADS) kFluidReorderCoop(DeviceState d,
 
 }  // namespace
 
+namespace {
+// The barrier self-test: the blocks wait for `expected` arrivals with a short
+// limit (a missing block makes the wait run out, nothing else).
+__global__ void kBarrierProbe(unsigned* bar, int* status, unsigned expected, int spinLimit)
+{
+    unsigned gen = ((volatile unsigned*)bar)[1];
+    gridBarrierN(bar, gen, status, expected, spinLimit);
+}
+}  // namespace
+
+int selftestBarrier(int missing, int* statusOut)
+{
+    unsigned* bar = nullptr;
+    int* status = nullptr;
+    int rc = DEMSPH_OK;
+    if (cudaMalloc(&bar, 2 * sizeof(unsigned)) != cudaSuccess || cudaMalloc(&status, sizeof(int)) != cudaSuccess ||
+        cudaMemset(bar, 0, 2 * sizeof(unsigned)) != cudaSuccess || cudaMemset(status, 0, sizeof(int)) != cudaSuccess) {
+        rc = DEMSPH_ERR_CUDA;
+    } else if (!launchCooperative(kBarrierProbe, 2, 32, (cudaStream_t)0, bar, status, 2u + (unsigned)missing,
+                                  1 << 16) ||
+               cudaDeviceSynchronize() != cudaSuccess ||
+               cudaMemcpy(statusOut, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        rc = DEMSPH_ERR_CUDA;
+    }
+    cudaFree(bar);
+    cudaFree(status);
+    return rc;
+}
+
 int cooperativeSortBlocks()
 {
     int dev = 0, sms = 0, perSm = 0;

@@ -51,26 +51,28 @@ inline bool launchCooperative(void (*kernel)(KArgs...), unsigned grid, unsigned 
     return cudaLaunchKernelEx(&cfg, kernel, args...) == cudaSuccess;
 }
 
-// Barrier over all blocks of a cooperative launch.  bar[0] counts arrivals,
-// bar[1] is the generation; `gen` is the generation this block waits past
-// (read from bar[1] when the launch began, before any barrier of the launch
-// could complete).  The wait is bounded: after about 0.5 s it records
+// Barrier over all blocks of a cooperative launch.  bar[0] counts arrivals
+// (the last of `expected` resets it), bar[1] is the generation; `gen` is the
+// generation this block waits past (read from bar[1] when the launch began,
+// before any barrier of the launch could complete).  The wait is bounded:
+// after spinLimit polls (about 0.5 s for gridBarrier's limit) it records
 // ST_BARRIER_TIMEOUT and returns false, and the block should return.
-__device__ __forceinline__ bool gridBarrier(unsigned* bar, unsigned& gen, int* status)
+__device__ __forceinline__ bool gridBarrierN(unsigned* bar, unsigned& gen, int* status, unsigned expected,
+                                             int spinLimit)
 {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         ok = 1;
         __threadfence();
-        if (atomicAdd(&bar[0], 1u) + 1u == gridDim.x) {
+        if (atomicAdd(&bar[0], 1u) + 1u == expected) {
             bar[0] = 0u;
             __threadfence();
             atomicExch(&bar[1], gen + 1u);
         } else {
             int spins = 0;
             while (((volatile unsigned*)bar)[1] == gen) {
-                if (++spins > (1 << 22)) {
+                if (++spins > spinLimit) {
                     atomicOr(status, ST_BARRIER_TIMEOUT);
                     ok = 0;
                     break;
@@ -83,6 +85,10 @@ __device__ __forceinline__ bool gridBarrier(unsigned* bar, unsigned& gen, int* s
     __syncthreads();
     ++gen;
     return ok != 0;
+}
+__device__ __forceinline__ bool gridBarrier(unsigned* bar, unsigned& gen, int* status)
+{
+    return gridBarrierN(bar, gen, status, gridDim.x, 1 << 22);
 }
 
 // Block-wide exclusive scan of one value per thread (THREADS threads);
@@ -379,6 +385,9 @@ void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStrea
 // be used); DEMSPH_COOPERATIVE_SORT=0 in the environment keeps the four-launch
 // sort.
 int cooperativeSortBlocks();
+// Runs two blocks of a cooperative launch at a grid barrier that waits for
+// 2 + missing of them, with a short wait limit; stores the status bits.
+int selftestBarrier(int missing, int* statusOut);
 
 // lists.cu
 // Fluid lists of a fluid step: the reference's walk (walk = true, or once a

@@ -175,6 +175,14 @@ DEMSPH_API const char* demsph_status_string(int status);
 DEMSPH_API const char* demsph_last_error(const demsph_engine* e);
 /* Library version string. */
 DEMSPH_API const char* demsph_version(void);
+/* Self-test of the bounded grid barrier the cooperative sorts use (no
+   counterpart in the reference): two blocks of a cooperative launch wait at a
+   barrier for 2 + missing arrivals, with a wait limit of a few milliseconds.
+   With missing > 0 the wait runs out and the kernel records the timeout and
+   returns (no fault, no hang); *status_out receives the device status bits:
+   128 (barrier timeout) then, 0 when missing = 0.  Returns DEMSPH_OK when the
+   launch itself ran. */
+DEMSPH_API int demsph_selftest_barrier(int device, int missing, int* status_out);
 
 /* ---- scene builder: the reference's setup API (core/dataBase.h:33-219) ---- */
 /* HostSolidContactModel(n_material) as in solverBase::initialize (core/solverBase.cpp:16). */
