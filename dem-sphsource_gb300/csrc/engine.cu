@@ -631,8 +631,13 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 d.uniformFluid = 1;
                 for (int i = 1; i < nf && d.uniformFluid; ++i)
                     d.uniformFluid = par[i].x == par[0].x && par[i].y == par[0].y && par[i].z == par[0].z &&
-                                     par[i].w == par[0].w;
+                                     par[i].w == par[0].w && ph[i].w == ph[0].w && pl[i].w == pl[0].w;
                 d.fparU = par[0];
+                {
+                    const float h = ph[0].w;
+                    const float kg = 5.f * 21.f / (16.f * 3.14159265358979323846f);
+                    d.fconstU = make_float4(4.f * h * h, 0.5f / h, kg / (h * h * h * h * h), 1.f / par[0].y);
+                }
                 CK(cudaMemcpyAsync(d.fid, id.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, e->stream));
                 CK(cudaMemcpyAsync(d.fslot, id.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, e->stream));
             }

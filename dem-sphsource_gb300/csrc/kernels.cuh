@@ -156,7 +156,8 @@ struct DeviceState {
     int nf, kff, kfs;
     int lanes;               // threads per fluid particle in the list and pair loops
     int uniformFluid;        // every fluid particle has the parameters fparU (rest density, sound
-    float4 fparU;            // speed, viscosity, mass)
+    float4 fparU;            // speed, viscosity, mass) and the same smoothing length
+    float4 fconstU;          // with them: 4 h^2, 0.5 / h, KG / h^5, 1 / sound speed
     int4* fcell;
     float4* fph[2];
     float4* fpl[2];

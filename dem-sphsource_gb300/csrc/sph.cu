@@ -149,7 +149,7 @@ struct ContinuityArgs {
 };
 
 template <int L, bool U>
-__global__ void __launch_bounds__(T) kContinuity(DeviceState d, ContinuityArgs a)
+__global__ void __launch_bounds__(T, L == 1 ? 12 : 10) kContinuity(DeviceState d, ContinuityArgs a)
 {
     stepKernelBegin();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -162,28 +162,45 @@ __global__ void __launch_bounds__(T) kContinuity(DeviceState d, ContinuityArgs a
         o = loadSelf(d, i, a.ps, a.vs, a.ds);
         const int n = d.nf;
         const int nff = min(d.ffc[i], d.kff);
+        // U: every fluid particle has the same rest density, sound speed,
+        // viscosity, mass and smoothing length - one gather fewer per
+        // neighbour, and the kernel's constants and the shared sound speed
+        // taken out of the loop (one division per pair instead of five)
+        const float negTwoRhoM = -2.f * o.rho * d.fparU.w;
         for (int k = lane; k < nff; k += L) {
             const unsigned e = d.ff[(size_t)k * n + i];
             const int j = ffPartner(e);
             const float4 pj = d.fph[a.ps][j];
             const float3 r = fluidRel(d, a.ps, i, o.c, o.p, e, j, pj);
-            const float h = 0.5f * (o.h + pj.w);
             const float r2 = dot3(r, r);
-            if (r2 >= 4.f * h * h) continue;
-            // U: every fluid particle has the same rest density, sound speed,
-            // viscosity and mass - one gather fewer per neighbour
-            const float4 par = U ? d.fparU : d.fpar[j];
-            const float drj = d.fdrho[a.ds][j];
-            const float rhoj = par.x + drj;
-            const float Pj = drj * par.y * par.y;
-            const float Vj = par.w / rhoj;
-            const float rr = sqrtf(r2);
-            const float tt = 1.f - 0.5f * rr / h;
-            const float h2 = h * h;
-            const float G = KG * tt * tt * tt / (h2 * h2 * h);
-            const float c = 0.5f * (o.cs + par.y);
-            const float3 vij = o.v - xyz(d.fvh[a.vs][j]);
-            acc.add(-2.f * o.rho * Vj * G / (o.rho + rhoj) * (rhoj * dot3(vij, r) + (o.P - Pj) * rr / c));
+            if constexpr (U) {
+                // the shared constants are read from the kernel parameters
+                if (r2 >= d.fconstU.x) continue;
+                const float drj = d.fdrho[a.ds][j];
+                const float rhoj = d.fparU.x + drj;
+                const float Pj = drj * d.fparU.y * d.fparU.y;
+                const float rr = sqrtf(r2);
+                const float tt = 1.f - rr * d.fconstU.y;
+                const float G = d.fconstU.z * tt * tt * tt;
+                const float3 vij = o.v - xyz(d.fvh[a.vs][j]);
+                acc.add(negTwoRhoM * G / (rhoj * (o.rho + rhoj)) *
+                        (rhoj * dot3(vij, r) + (o.P - Pj) * rr * d.fconstU.w));
+            } else {
+                const float h = 0.5f * (o.h + pj.w);
+                if (r2 >= 4.f * h * h) continue;
+                const float4 par = d.fpar[j];
+                const float drj = d.fdrho[a.ds][j];
+                const float rhoj = par.x + drj;
+                const float Pj = drj * par.y * par.y;
+                const float Vj = par.w / rhoj;
+                const float rr = sqrtf(r2);
+                const float tt = 1.f - 0.5f * rr / h;
+                const float h2 = h * h;
+                const float G = KG * tt * tt * tt / (h2 * h2 * h);
+                const float c = 0.5f * (o.cs + par.y);
+                const float3 vij = o.v - xyz(d.fvh[a.vs][j]);
+                acc.add(-2.f * o.rho * Vj * G / (o.rho + rhoj) * (rhoj * dot3(vij, r) + (o.P - Pj) * rr / c));
+            }
         }
         const int nfs = min(d.fsc[i], d.kfs);
         const float ci2 = o.cs * o.cs;
@@ -226,34 +243,53 @@ __global__ void __launch_bounds__(T) kMomentum(DeviceState d, dfl dtf, dfl halfD
         const Self o = loadSelf(d, i, 1, 0, 1);
         const int n = d.nf;
         const int nff = min(d.ffc[i], d.kff);
+        // U: the same parameters and smoothing length for every particle (see
+        // kContinuity): three divisions per pair instead of seven
+        const float twoNuRhoI = 2.f * d.fparU.z * o.rho, twoVi = 2.f * o.V;
         for (int k = lane; k < nff; k += L) {
             const unsigned e = d.ff[(size_t)k * n + i];
             const int j = ffPartner(e);
             const float4 pj = d.fph[1][j];
             const float3 r = fluidRel(d, 1, i, o.c, o.p, e, j, pj);
-            const float h = 0.5f * (o.h + pj.w);
             const float r2 = dot3(r, r);
-            if (r2 >= 4.f * h * h) continue;
-            // U: every fluid particle has the same rest density, sound speed,
-            // viscosity and mass - one gather fewer per neighbour
-            const float4 par = U ? d.fparU : d.fpar[j];
-            const float drj = d.fdrho[1][j];
-            const float rhoj = par.x + drj;
-            const float Pj = drj * par.y * par.y;
-            const float Vj = par.w / rhoj;
-            const float gj = par.z * rhoj;
-            const float rr = sqrtf(r2);
-            const float tt = 1.f - 0.5f * rr / h;
-            const float h2 = h * h;
-            const float G = KG * tt * tt * tt / (h2 * h2 * h);
-            const float c = 0.5f * (o.cs + par.y);
-            const float3 vij = o.v - xyz(d.fvh[0][j]);
-            const float dU = -dot3(vij, r) / rr;  // U_L - U_R
-            const float beta = fminf(3.f * fmaxf(dU, 0.f), c);
-            const float Ps = (o.rho * Pj + rhoj * o.P + o.rho * rhoj * beta * dU) / (o.rho + rhoj);
-            const float gbar = 2.f * o.gam * gj / (o.gam + gj);
-            const float w = 2.f * o.V * Vj * G / o.m;
-            acc.add((r * Ps - vij * gbar) * w);
+            if constexpr (U) {
+                if (r2 >= d.fconstU.x) continue;
+                const float drj = d.fdrho[1][j];
+                const float rhoj = d.fparU.x + drj;
+                const float Pj = drj * d.fparU.y * d.fparU.y;
+                const float rr = sqrtf(r2);
+                const float tt = 1.f - rr * d.fconstU.y;
+                const float G = d.fconstU.z * tt * tt * tt;
+                const float3 vij = o.v - xyz(d.fvh[0][j]);
+                const float dU = -dot3(vij, r) / rr;  // U_L - U_R
+                const float beta = fminf(3.f * fmaxf(dU, 0.f), d.fparU.y);
+                const float invSum = 1.f / (o.rho + rhoj);
+                const float Ps = (o.rho * Pj + rhoj * o.P + o.rho * rhoj * beta * dU) * invSum;
+                const float gbar = twoNuRhoI * rhoj * invSum;  // 2 g_i g_j / (g_i + g_j), g = nu rho
+                const float w = twoVi * G / rhoj;              // 2 V_i V_j G / m, V_j = m / rho_j
+                acc.add((r * Ps - vij * gbar) * w);
+            } else {
+                const float h = 0.5f * (o.h + pj.w);
+                if (r2 >= 4.f * h * h) continue;
+                const float4 par = d.fpar[j];
+                const float drj = d.fdrho[1][j];
+                const float rhoj = par.x + drj;
+                const float Pj = drj * par.y * par.y;
+                const float Vj = par.w / rhoj;
+                const float gj = par.z * rhoj;
+                const float rr = sqrtf(r2);
+                const float tt = 1.f - 0.5f * rr / h;
+                const float h2 = h * h;
+                const float G = KG * tt * tt * tt / (h2 * h2 * h);
+                const float c = 0.5f * (o.cs + par.y);
+                const float3 vij = o.v - xyz(d.fvh[0][j]);
+                const float dU = -dot3(vij, r) / rr;  // U_L - U_R
+                const float beta = fminf(3.f * fmaxf(dU, 0.f), c);
+                const float Ps = (o.rho * Pj + rhoj * o.P + o.rho * rhoj * beta * dU) / (o.rho + rhoj);
+                const float gbar = 2.f * o.gam * gj / (o.gam + gj);
+                const float w = 2.f * o.V * Vj * G / o.m;
+                acc.add((r * Ps - vij * gbar) * w);
+            }
         }
         const int nfs = min(d.fsc[i], d.kfs);
         const float ci2 = o.cs * o.cs;
