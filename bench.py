@@ -584,17 +584,12 @@ def main():
         bo += fp.nbytes + fv.nbytes + fd.nbytes
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    s_io = (sp, sv, sw) if scene.n_solid else None
+    f_io = (fp, fv, fd) if nf else None
     for k in range(ne):
-        if scene.n_solid:
-            eng.upload_solids(sp, sv, sw)
-        if nf:
-            eng.upload_fluids(fp, fv, fd)
-        eng.update(dt, step, 1, gap, use_graph=False)
+        # upload the state, one step, download the state: one C-ABI call, one synchronisation
+        eng.update_io(dt, step, 1, gap, use_graph=True, fluid_in=f_io, solid_in=s_io, fluid_out=f_io, solid_out=s_io)
         step += 1
-        if scene.n_solid:
-            eng.download_solids(out={"pos": sp, "vel": sv, "angvel": sw})
-        if nf:
-            eng.download_fluids(out=(fp, fv, None, fd))
     e2e_s = time.perf_counter() - t0
     e2e_updates = updates_for(step - ne, ne, gap, nf, n_mobile)
     e2e_val = e2e_updates / e2e_s
@@ -625,8 +620,8 @@ def main():
             "roofline": roofline, "cpu_baseline": cb,
             "e2e": {"value": e2e_val, "unit": "particle-updates/s", "h2d_bytes_per_step": bi,
                     "d2h_bytes_per_step": bo, "steps": ne,
-                    "path": "demsph_upload_* + demsph_update(1 step) + demsph_download_* per step, pinned host "
-                            "buffers, FP64 reference layout"},
+                    "path": "demsph_update_io per step: upload the state, one step, download the state, one "
+                            "synchronisation; pinned host buffers, FP64 reference layout"},
             "gpu_launches": launches, "clocks": clocks.summary(),
         }
         print(json.dumps(out))

@@ -343,6 +343,19 @@ class Engine:
         self._chk(self.lib.demsph_update(self.h, _D(dt), _I(first_step), _I(n_steps), _I(gap), _I(1 if use_graph else 0)),
                   "demsph_update")
 
+    def update_io(self, dt, first_step, n_steps, gap, use_graph=True, fluid_in=None, solid_in=None,
+                  fluid_out=None, solid_out=None):
+        """demsph_update_io: uploads ``fluid_in`` (pos, vel, drho) and ``solid_in``
+        (pos, vel, angvel) (any entry may be None), advances the steps and
+        downloads into ``fluid_out`` / ``solid_out`` (same tuples), with one
+        synchronisation."""
+        def ptrs(t, k):
+            t = t if t is not None else (None,) * k
+            return [None if a is None else _ptr(a) for a in t]
+        args = ptrs(fluid_in, 3) + ptrs(solid_in, 3) + ptrs(fluid_out, 3) + ptrs(solid_out, 3)
+        self._chk(self.lib.demsph_update_io(self.h, _D(dt), _I(first_step), _I(n_steps), _I(gap),
+                                            _I(1 if use_graph else 0), *args), "demsph_update_io")
+
     def synchronize(self):
         self._chk(self.lib.demsph_synchronize(self.h), "demsph_synchronize")
 

@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -1101,11 +1102,13 @@ static void adaptRowsPerWarp(demsph_engine* e, const int* stats)
     dropGraph(e);  // the launch shape and the state are baked into the graphs
 }
 
-int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph)
+// The steps of demsph_update; `afterSteps` (when given) is enqueued after the
+// steps of every attempt, before the one synchronisation that reads the
+// status, so a transfer it enqueues sees the state of the completed steps (an
+// attempt that overflowed is followed by one that enqueues it again).
+static int runUpdate(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph,
+                     const std::function<void()>* afterSteps)
 {
-    if (gap < 1 || n_steps < 0) return DEMSPH_ERR_ARGUMENT;
-    ENGINE_GUARD(e)
-    REQUIRE_INIT(e);
     DeviceState& d = e->d;
     const int end = first_step + n_steps;
     int step = first_step;
@@ -1146,6 +1149,7 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
             launchRowStats(d, e->par, e->stream);
             CK(cudaMemcpyAsync(rowStats, d.rowStats, sizeof(rowStats), cudaMemcpyDeviceToHost, e->stream));
         }
+        if (afterSteps) (*afterSteps)();
         int done = 0;
         const int st = readStatus(e, &done);
         if (st == 0) {
@@ -1159,8 +1163,42 @@ int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int 
         e->par = startPar ^ (done & 1);      // every step builds one contact list
         grow(e, st);
     }
+    if (afterSteps && n_steps == 0) {
+        (*afterSteps)();
+        CK(cudaStreamSynchronize(e->stream));
+    }
     CK(cudaGetLastError());
     return DEMSPH_OK;
+}
+
+int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph)
+{
+    if (gap < 1 || n_steps < 0) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    REQUIRE_INIT(e);
+    return runUpdate(e, dt, first_step, n_steps, gap, use_graph, nullptr);
+    ENGINE_END(e)
+}
+
+int demsph_update_io(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph,
+                     const double* fluid_pos_in, const double* fluid_vel_in, const double* fluid_drho_in,
+                     const double* solid_pos_in, const double* solid_vel_in, const double* solid_angvel_in,
+                     double* fluid_pos_out, double* fluid_vel_out, double* fluid_drho_out, double* solid_pos_out,
+                     double* solid_vel_out, double* solid_angvel_out)
+{
+    if (gap < 1 || n_steps < 0) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    REQUIRE_INIT(e);
+    if (fluid_pos_in || fluid_vel_in || fluid_drho_in) enqueueUploadFluids(e, fluid_pos_in, fluid_vel_in, fluid_drho_in);
+    if (solid_pos_in || solid_vel_in || solid_angvel_in)
+        enqueueUploadSolids(e, solid_pos_in, solid_vel_in, solid_angvel_in);
+    const std::function<void()> download = [&] {
+        if (fluid_pos_out || fluid_vel_out || fluid_drho_out)
+            enqueueDownloadFluids(e, fluid_pos_out, fluid_vel_out, nullptr, fluid_drho_out);
+        if (solid_pos_out || solid_vel_out || solid_angvel_out)
+            enqueueDownloadSolids(e, solid_pos_out, solid_vel_out, nullptr, nullptr, nullptr, solid_angvel_out);
+    };
+    return runUpdate(e, dt, first_step, n_steps, gap, use_graph, &download);
     ENGINE_END(e)
 }
 

@@ -123,6 +123,13 @@ inline int cudaFail(demsph_engine* e, const CudaError& c)
 void freeOne(demsph_engine* e, void*& p);
 void dropGraph(demsph_engine* e);
 int readStatus(demsph_engine* e, int* stepsDone = nullptr);
+// Host transfers of the state enqueued on the engine's stream, without
+// synchronising (engine_io.cu).
+void enqueueDownloadFluids(demsph_engine* e, double* pos, double* vel, double* acc, double* drho);
+void enqueueDownloadSolids(demsph_engine* e, double* pos, double* vel, double* acc, double* normal, double* torque,
+                           double* angvel);
+void enqueueUploadFluids(demsph_engine* e, const double* pos, const double* vel, const double* drho);
+void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel, const double* angvel);
 double* scratchDoubles(demsph_engine* e, size_t n);
 void splitPosition(const DeviceState& d, double3 p, int4& c, float4& h, float4& l);
 

@@ -265,13 +265,15 @@ void d2h(std::vector<T>& v, const T* src, size_t n)
 
 }  // namespace
 
-extern "C" {
+namespace demsph {
 
-int demsph_download_fluids(demsph_engine* e, double* pos, double* vel, double* acc, double* drho)
+// The host transfers of the state, enqueued on the engine's stream (the
+// public calls below add the synchronisation; demsph_update_io enqueues them
+// around its steps and synchronises once).
+void enqueueDownloadFluids(demsph_engine* e, double* pos, double* vel, double* acc, double* drho)
 {
-    ENGINE_GUARD(e)
     DeviceState& d = e->d;
-    if (d.nf == 0) return DEMSPH_OK;
+    if (d.nf == 0) return;
     const size_t n = d.nf;
     double* buf = scratchDoubles(e, 10 * n);
     ++t_kernelLaunches, kFluidOut<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, buf);
@@ -279,52 +281,25 @@ int demsph_download_fluids(demsph_engine* e, double* pos, double* vel, double* a
     for (int k = 0; k < 3; ++k)
         if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + 3 * n * k, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
     if (drho) CK(cudaMemcpyAsync(drho, buf + 9 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
-    CK(cudaStreamSynchronize(e->stream));
-    return DEMSPH_OK;
-    ENGINE_END(e)
 }
 
-int demsph_download_solids(demsph_engine* e, double* pos, double* vel, double* acc, double* normal, double* torque,
+void enqueueDownloadSolids(demsph_engine* e, double* pos, double* vel, double* acc, double* normal, double* torque,
                            double* angvel)
 {
-    ENGINE_GUARD(e)
     DeviceState& d = e->d;
-    if (d.ns == 0) return DEMSPH_OK;
+    if (d.ns == 0) return;
     const size_t n3 = 3 * (size_t)d.ns;
     double* buf = scratchDoubles(e, 6 * n3);
     ++t_kernelLaunches, kSolidOut<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, buf);
     double* outs[6] = {pos, vel, acc, normal, torque, angvel};
     for (int k = 0; k < 6; ++k)
         if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + n3 * k, sizeof(double) * n3, cudaMemcpyDeviceToHost, e->stream));
-    CK(cudaStreamSynchronize(e->stream));
-    return DEMSPH_OK;
-    ENGINE_END(e)
 }
 
-int demsph_download_clumps(demsph_engine* e, double* centroid, double* vel, double* acc, double* angvel,
-                           double* torque, double* orientation)
+void enqueueUploadFluids(demsph_engine* e, const double* pos, const double* vel, const double* drho)
 {
-    ENGINE_GUARD(e)
     DeviceState& d = e->d;
-    CK(cudaStreamSynchronize(e->stream));
-    const size_t n = d.nc;
-    if (n == 0) return DEMSPH_OK;
-    double* buf = scratchDoubles(e, 19 * n);
-    ++t_kernelLaunches, kClumpOut<<<blocksFor((long long)n, 128), 128, 0, e->stream>>>(d, buf);
-    double* outs[5] = {centroid, vel, acc, angvel, torque};
-    for (int k = 0; k < 5; ++k)
-        if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + 3 * n * k, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
-    if (orientation) CK(cudaMemcpyAsync(orientation, buf + 15 * n, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, e->stream));
-    CK(cudaStreamSynchronize(e->stream));
-    return DEMSPH_OK;
-    ENGINE_END(e)
-}
-
-int demsph_upload_fluids(demsph_engine* e, const double* pos, const double* vel, const double* drho)
-{
-    ENGINE_GUARD(e)
-    DeviceState& d = e->d;
-    if (d.nf == 0) return DEMSPH_OK;
+    if (d.nf == 0) return;
     double* buf = scratchDoubles(e, 7 * (size_t)d.nf);
     double* dp = pos ? buf : nullptr;
     double* dv = vel ? buf + 3 * (size_t)d.nf : nullptr;
@@ -333,16 +308,12 @@ int demsph_upload_fluids(demsph_engine* e, const double* pos, const double* vel,
     if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, e->stream));
     if (dr) CK(cudaMemcpyAsync(dr, drho, sizeof(double) * d.nf, cudaMemcpyHostToDevice, e->stream));
     ++t_kernelLaunches, kFluidIn<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, dp, dv, dr);
-    CK(cudaStreamSynchronize(e->stream));
-    return DEMSPH_OK;
-    ENGINE_END(e)
 }
 
-int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel, const double* angvel)
+void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel, const double* angvel)
 {
-    ENGINE_GUARD(e)
     DeviceState& d = e->d;
-    if (d.ns == 0) return DEMSPH_OK;
+    if (d.ns == 0) return;
     // dummy particles given a velocity join the integration: the move list
     // changes only when a dummy particle starts or stops moving
     bool moveChanged = false;
@@ -376,10 +347,14 @@ int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel,
                 d.moveFirst = first;
                 dropGraph(e);
             }
-            if (!move.empty())
-                CK(cudaMemcpyAsync(d.moveList, move.data(), sizeof(int) * move.size(), cudaMemcpyHostToDevice,
-                                   e->stream));
-            e->moveHost.swap(move);
+            if (!move.empty()) {
+                // the host vector must outlive the asynchronous copy: keep it as the engine's copy
+                e->moveHost.swap(move);
+                CK(cudaMemcpyAsync(d.moveList, e->moveHost.data(), sizeof(int) * e->moveHost.size(),
+                                   cudaMemcpyHostToDevice, e->stream));
+            } else {
+                e->moveHost.swap(move);
+            }
         }
     }
     double* buf = scratchDoubles(e, 9 * (size_t)d.ns);
@@ -392,6 +367,64 @@ int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel,
     ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw);
     // solids that never move are otherwise sorted only once
     if (dp && e->nMassive == 0) e->solidSortStale = true;
+}
+
+}  // namespace demsph
+
+extern "C" {
+
+
+int demsph_download_fluids(demsph_engine* e, double* pos, double* vel, double* acc, double* drho)
+{
+    ENGINE_GUARD(e)
+    enqueueDownloadFluids(e, pos, vel, acc, drho);
+    CK(cudaStreamSynchronize(e->stream));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_download_solids(demsph_engine* e, double* pos, double* vel, double* acc, double* normal, double* torque,
+                           double* angvel)
+{
+    ENGINE_GUARD(e)
+    enqueueDownloadSolids(e, pos, vel, acc, normal, torque, angvel);
+    CK(cudaStreamSynchronize(e->stream));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_download_clumps(demsph_engine* e, double* centroid, double* vel, double* acc, double* angvel,
+                           double* torque, double* orientation)
+{
+    ENGINE_GUARD(e)
+    DeviceState& d = e->d;
+    CK(cudaStreamSynchronize(e->stream));
+    const size_t n = d.nc;
+    if (n == 0) return DEMSPH_OK;
+    double* buf = scratchDoubles(e, 19 * n);
+    ++t_kernelLaunches, kClumpOut<<<blocksFor((long long)n, 128), 128, 0, e->stream>>>(d, buf);
+    double* outs[5] = {centroid, vel, acc, angvel, torque};
+    for (int k = 0; k < 5; ++k)
+        if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + 3 * n * k, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (orientation) CK(cudaMemcpyAsync(orientation, buf + 15 * n, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_upload_fluids(demsph_engine* e, const double* pos, const double* vel, const double* drho)
+{
+    ENGINE_GUARD(e)
+    enqueueUploadFluids(e, pos, vel, drho);
+    CK(cudaStreamSynchronize(e->stream));
+    return DEMSPH_OK;
+    ENGINE_END(e)
+}
+
+int demsph_upload_solids(demsph_engine* e, const double* pos, const double* vel, const double* angvel)
+{
+    ENGINE_GUARD(e)
+    enqueueUploadSolids(e, pos, vel, angvel);
     CK(cudaStreamSynchronize(e->stream));
     return DEMSPH_OK;
     ENGINE_END(e)

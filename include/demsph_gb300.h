@@ -243,6 +243,19 @@ DEMSPH_API int demsph_solid_integrate_after_contact(demsph_engine* e, double dt)
    for i_step = first_step .. first_step+n_steps-1, without the driver hook;
    replayed as a CUDA graph when use_graph != 0. */
 DEMSPH_API int demsph_update(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph);
+/* demsph_update for callers that exchange the state with the host every call
+   (a coupled external solver): uploads the given host arrays (FP64, the
+   layouts of demsph_upload_fluids / demsph_upload_solids; NULL = keep),
+   advances the steps, downloads into the given host arrays (the layouts of
+   demsph_download_fluids / demsph_download_solids; NULL = skip), and
+   synchronises once.  A list overflow is handled as in demsph_update (the
+   transfer out follows the completed steps).  No counterpart in the
+   reference. */
+DEMSPH_API int demsph_update_io(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph,
+                                const double* fluid_pos_in, const double* fluid_vel_in, const double* fluid_drho_in,
+                                const double* solid_pos_in, const double* solid_vel_in, const double* solid_angvel_in,
+                                double* fluid_pos_out, double* fluid_vel_out, double* fluid_drho_out,
+                                double* solid_pos_out, double* solid_vel_out, double* solid_angvel_out);
 /* Chooses the threads per fluid particle of the fluid list and pair kernels
    (1, 2, 4 or 8) by timing the first continuity pass with each; call after
    demsph_initialize.  *lanes_out receives the choice (may be NULL).  No

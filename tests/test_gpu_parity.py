@@ -122,6 +122,44 @@ def test_graph_batch_equals_staged_calls(ds, scenes, name):
             assert np.array_equal(s1[k], s2[k]), k
 
 
+@pytest.mark.parametrize("name", ("tiny_coupled", "tiny_granular", "tiny_dam_break"))
+def test_update_io_equals_separate_transfers(ds, scenes, name):
+    """demsph_update_io (upload, steps, download, one synchronisation) gives the
+    bits of demsph_upload_* + demsph_update + demsph_download_*."""
+    recipe, b, sc, e1, _ = _setup(ds, scenes, name)
+    e2 = ds.Engine(sc)
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for e in (e1, e2):
+        e.initialize()
+        e.update(dt, 1, 3, gap)
+    nf, ns = sc.n_fluid, sc.n_solid
+    f1 = tuple(np.zeros(s) for s in ((nf, 3), (nf, 3), (nf,))) if nf else None
+    s1 = tuple(np.zeros((ns, 3)) for _ in range(3)) if ns else None
+    f2 = tuple(a.copy() for a in f1) if nf else None
+    s2 = tuple(a.copy() for a in s1) if ns else None
+    if nf:
+        e1.download_fluids(out=(f1[0], f1[1], None, f1[2]))
+        e2.download_fluids(out=(f2[0], f2[1], None, f2[2]))
+    if ns:
+        e1.download_solids(out={"pos": s1[0], "vel": s1[1], "angvel": s1[2]})
+        e2.download_solids(out={"pos": s2[0], "vel": s2[1], "angvel": s2[2]})
+    for step in range(4, 10):
+        if ns:
+            e1.upload_solids(*s1)
+        if nf:
+            e1.upload_fluids(*f1)
+        e1.update(dt, step, 1, gap)
+        if ns:
+            e1.download_solids(out={"pos": s1[0], "vel": s1[1], "angvel": s1[2]})
+        if nf:
+            e1.download_fluids(out=(f1[0], f1[1], None, f1[2]))
+        e2.update_io(dt, step, 1, gap, fluid_in=f2, solid_in=s2, fluid_out=f2, solid_out=s2)
+        for a, c in zip(f1 or (), f2 or ()):
+            assert np.array_equal(a, c)
+        for a, c in zip(s1 or (), s2 or ()):
+            assert np.array_equal(a, c)
+
+
 @pytest.mark.parametrize("name", SCENES)
 def test_deterministic(ds, scenes, name):
     recipe, b, sc, e1, _ = _setup(ds, scenes, name)
