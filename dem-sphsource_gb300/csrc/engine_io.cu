@@ -46,29 +46,47 @@ __global__ void kFluidOut(DeviceState d, double* out)
 }
 
 // Planar FP64 output: pos vel acc normal torque angvel, 3n each.
-__global__ void kSolidOut(DeviceState d, double* out)
+// The solid state in FP64 for export: position, velocity, acceleration,
+// normal, torque, spin, each 3 x ns at out + k * 3 ns, for the outputs whose
+// bit k is set in `want`.
+__global__ void kSolidOut(DeviceState d, double* out, unsigned want)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.ns) return;
     const size_t n3 = 3 * (size_t)d.ns;
-    const int4 c = d.scell[i];
-    const float4 h = d.sph[i], l = d.spl[i];
-    const float4 vh = d.svh[i], vl = d.svl[i], wh = d.swh[i], wl = d.swl[i];
-    const float4 a = d.sacc[i], nr = d.snormal[i], t = d.storque[i];
     double* o = out + 3 * (size_t)i;
-    o[0] = cellOrigin(d, 0, c.x) + ((double)h.x + (double)l.x);
-    o[1] = cellOrigin(d, 1, c.y) + ((double)h.y + (double)l.y);
-    o[2] = cellOrigin(d, 2, c.z) + ((double)h.z + (double)l.z);
+    if (want & 1u) {
+        const int4 c = d.scell[i];
+        const float4 h = d.sph[i], l = d.spl[i];
+        o[0] = cellOrigin(d, 0, c.x) + ((double)h.x + (double)l.x);
+        o[1] = cellOrigin(d, 1, c.y) + ((double)h.y + (double)l.y);
+        o[2] = cellOrigin(d, 2, c.z) + ((double)h.z + (double)l.z);
+    }
     o += n3;
-    o[0] = (double)vh.x + vl.x; o[1] = (double)vh.y + vl.y; o[2] = (double)vh.z + vl.z;
+    if (want & 2u) {
+        const float4 vh = d.svh[i], vl = d.svl[i];
+        o[0] = (double)vh.x + vl.x; o[1] = (double)vh.y + vl.y; o[2] = (double)vh.z + vl.z;
+    }
     o += n3;
-    o[0] = a.x; o[1] = a.y; o[2] = a.z;
+    if (want & 4u) {
+        const float4 a = d.sacc[i];
+        o[0] = a.x; o[1] = a.y; o[2] = a.z;
+    }
     o += n3;
-    o[0] = nr.x; o[1] = nr.y; o[2] = nr.z;
+    if (want & 8u) {
+        const float4 nr = d.snormal[i];
+        o[0] = nr.x; o[1] = nr.y; o[2] = nr.z;
+    }
     o += n3;
-    o[0] = t.x; o[1] = t.y; o[2] = t.z;
+    if (want & 16u) {
+        const float4 t = d.storque[i];
+        o[0] = t.x; o[1] = t.y; o[2] = t.z;
+    }
     o += n3;
-    o[0] = (double)wh.x + wl.x; o[1] = (double)wh.y + wl.y; o[2] = (double)wh.z + wl.z;
+    if (want & 32u) {
+        const float4 wh = d.swh[i], wl = d.swl[i];
+        o[0] = (double)wh.x + wl.x; o[1] = (double)wh.y + wl.y; o[2] = (double)wh.z + wl.z;
+    }
 }
 
 // Writes the state given in original order (FP64) into the engine.
@@ -290,8 +308,11 @@ void enqueueDownloadSolids(demsph_engine* e, double* pos, double* vel, double* a
     if (d.ns == 0) return;
     const size_t n3 = 3 * (size_t)d.ns;
     double* buf = scratchDoubles(e, 6 * n3);
-    ++t_kernelLaunches, kSolidOut<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, buf);
     double* outs[6] = {pos, vel, acc, normal, torque, angvel};
+    unsigned want = 0;
+    for (int k = 0; k < 6; ++k)
+        if (outs[k]) want |= 1u << k;
+    ++t_kernelLaunches, kSolidOut<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, buf, want);
     for (int k = 0; k < 6; ++k)
         if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + n3 * k, sizeof(double) * n3, cudaMemcpyDeviceToHost, e->stream));
 }
