@@ -908,6 +908,8 @@ int demsph_destroy(demsph_engine* e)
     return DEMSPH_OK;
 }
 
+static void adaptRowsPerWarp(demsph_engine* e, const int* stats);
+
 int demsph_initialize(demsph_engine* e)
 {
     ENGINE_GUARD(e)
@@ -969,6 +971,14 @@ int demsph_initialize(demsph_engine* e)
         d.bondList = dalloc<int>(list.size(), e->owned, e->stream);
         if (d.ns > 0) CK(cudaMemcpyAsync(d.bondStart, start.data(), sizeof(int) * (d.ns + 1), cudaMemcpyHostToDevice, e->stream));
         if (!list.empty()) CK(cudaMemcpyAsync(d.bondList, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, e->stream));
+    }
+    // the contact-force rows per warp from the first contact lists
+    if (d.nrow > 0 && e->adaptRows) {
+        int stats[2] = {0, 0};
+        launchRowStats(d, e->par, e->stream);
+        CK(cudaMemcpyAsync(stats, d.rowStats, sizeof(stats), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        if (stats[1] > 0) adaptRowsPerWarp(e, stats);
     }
     // normals of walls and clump pebbles (setSolidNormal), kernel length = largest fluid h
     launchSolidNormals(d, e->hmax, e->stream);
