@@ -264,6 +264,32 @@ def test_large_grids_sort_like_the_oracle(ds, scenes, cells, lo, hi):
         _check_step(eng, orc, sc, _spacing(recipe), step, dt, DRIFT_TOL, 1e-8)
 
 
+@pytest.mark.parametrize("name", ("tiny_granular", "tiny_coupled", "tiny_dam_break"))
+def test_cooperative_sorts_equal_launch_per_phase_sorts(ds, scenes, name, monkeypatch):
+    """The one-launch cooperative sorts (solid sort by cell; fluid hash and
+    reorder) give the same bits as the launch-per-phase sorts they replace
+    (DEMSPH_COOPERATIVE_SORT=0, read when an engine is created), over forty
+    steps with candidates rebuilt, and so sorts run, nearly every step."""
+    recipe = getattr(scenes, name)()
+    b, sc = ds.build_scene(recipe)
+    engines = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("DEMSPH_COOPERATIVE_SORT", flag)
+        engines.append(ds.Engine(sc, solid_verlet_skin=1.0e-9, fluid_verlet_skin=1.0e-9))
+    monkeypatch.delenv("DEMSPH_COOPERATIVE_SORT")
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for e in engines:
+        e.initialize()
+        e.update(dt, 1, 40, gap, use_graph=True)
+    if sc.n_fluid:
+        for a, c in zip(engines[0].download_fluids(), engines[1].download_fluids()):
+            assert np.array_equal(a, c)
+    if sc.n_solid:
+        s0, s1 = engines[0].download_solids(), engines[1].download_solids()
+        for k in s0:
+            assert np.array_equal(s0[k], s1[k]), k
+
+
 def test_drift_bounded_over_run(ds, scenes):
     """Forty steps of the coupled scene: the engine stays within bounded
     distance of the FP64 oracle (no systematic FP32 drift)."""
