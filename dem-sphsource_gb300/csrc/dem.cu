@@ -190,7 +190,7 @@ __device__ __forceinline__ PairForce pairForce(const DeviceState& d, int a, int 
 // or -1 when the pair is not in a's row.
 __device__ __forceinline__ long long forwardSlot(const DeviceState& d, int par, int a, int b)
 {
-    const int r = d.srow[a];
+    const int r = rowOf(d, a);
     if (r < 0) return -1;
     const int n = min(d.fcnt[par][r], d.scap);
     for (int q = 0; q < n; ++q) {
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
     const int row0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * d.forceRows;
     const int row = row0 + lane;
     const bool live = lane < d.forceRows && row < d.nrow;
-    const int a = live ? d.rowSolid[row] : 0;
+    const int a = live ? solidOf(d, row) : 0;
     const size_t nr = (size_t)d.nrow;
     // forward contacts (a, b) come first, then reverse ones (b, a)
     const int n = live ? min(d.fcnt[par][row], d.scap) : 0;
@@ -597,7 +597,7 @@ __device__ __forceinline__ void solidIntegrateOne(const DeviceState& d, int i, d
     int4 c = make_int4(0, 0, 0, 0);
     float4 p0 = make_float4(0, 0, 0, 0), q0 = p0;
     if (!before) {
-        row = d.srow[i];
+        row = rowOf(d, i);
         c = d.scell[i];
         p0 = d.vref[i];
         if (d.nf > 0) q0 = d.svref[i];

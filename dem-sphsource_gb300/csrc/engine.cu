@@ -733,6 +733,8 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             }
             d.srow = dalloc<int>(ns, e->owned, e->stream);
             d.rowSolid = dalloc<int>(d.nrow, e->owned, e->stream);
+            d.rowsAreSolids = d.nrow == ns ? 1 : 0;
+            for (int r = 0; r < d.nrow && d.rowsAreSolids; ++r) d.rowsAreSolids = rowSolid[r] == r;
             d.scentre = dalloc<int4>(d.nrow, e->owned, e->stream);
             if (ns > 0) CK(cudaMemcpyAsync(d.srow, srow.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, e->stream));
             if (d.nrow > 0)

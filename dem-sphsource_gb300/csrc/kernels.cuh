@@ -233,6 +233,7 @@ struct DeviceState {
     // A < B of row B.
     int nrow;                // solids that can be in contact (not dummy wall particles)
     int* srow;               // solid -> row, -1 for dummy particles
+    int rowsAreSolids;       // 1: every solid has a row, row r is solid r (no dummy particles)
     int nmove;               // solids the integration advances: all but clump pebbles (their clump
     int* moveList;           // moves them) and dummy particles at rest (they never gain velocity)
     int moveFirst;           // >= 0: the list is moveFirst, moveFirst + 1, ... (moveList is not read)
@@ -438,6 +439,11 @@ __device__ __forceinline__ double3 solidAbsPos(const DeviceState& d, int i)
                         d.minB[2] + c.z * d.cs[2] + ((double)h.z + (double)l.z));
 }
 
+// Row of solid a (-1 for a dummy particle) and solid of row r: the identity,
+// without a read, when every solid has a row.
+__device__ __forceinline__ int rowOf(const DeviceState& d, int a) { return d.rowsAreSolids ? a : d.srow[a]; }
+__device__ __forceinline__ int solidOf(const DeviceState& d, int r) { return d.rowsAreSolids ? r : d.rowSolid[r]; }
+
 // After the last drift of a step: once a solid that can touch others (row >=
 // 0) has moved half the candidate margin since the candidates were built, the
 // next step rebuilds them.  c, h: its cell and offset after the drift; p0, q0:
@@ -459,7 +465,7 @@ __device__ __forceinline__ void checkDisplacementOf(const DeviceState& d, int ro
 }
 __device__ __forceinline__ void checkDisplacement(const DeviceState& d, int i)
 {
-    const int r = d.srow[i];
+    const int r = rowOf(d, i);
     if (r < 0) return;
     checkDisplacementOf(d, r, d.scell[i], d.sph[i], d.vref[i], d.nf > 0 ? d.svref[i] : make_float4(0, 0, 0, 0));
 }
@@ -487,7 +493,7 @@ __device__ __forceinline__ void rehashSolidOf(const DeviceState& d, int i, int r
 }
 __device__ __forceinline__ void rehashSolid(const DeviceState& d, int i)
 {
-    rehashSolidOf(d, i, d.srow[i], d.scell[i], d.sph[i], d.spl[i]);
+    rehashSolidOf(d, i, rowOf(d, i), d.scell[i], d.sph[i], d.spl[i]);
 }
 
 

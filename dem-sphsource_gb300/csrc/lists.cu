@@ -546,7 +546,7 @@ __device__ __forceinline__ float3 gridPos(int4 c, float4 h, const GridDev& g)
 // plain (x, y, z) cells.
 __device__ __forceinline__ void verletBuildRow(const DeviceState& d, int r)
 {
-    const int a = d.rowSolid[r];
+    const int a = solidOf(d, r);
     const int4 fa = d.sflags[a];
     const int4 ca = d.scell[a];
     const float4 ha = d.sph[a];
@@ -602,7 +602,7 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
     // stale candidates are rebuilt first, row by row (the contact force
     // kernel clears the flag once every row has read it)
     if (!walk && *d.rebuild) verletBuildRow(d, r);
-    const int a = d.rowSolid[r];
+    const int a = solidOf(d, r);
     const int4 fa = d.sflags[a];
     const int prev = par ^ 1;
     const int C = d.scap;
@@ -677,7 +677,7 @@ __global__ void kRowStats(DeviceState d, int par)
     const int r = (blockIdx.x * blockDim.x + threadIdx.x) * stride;
     int items = 0, rows = 0;
     if (r < d.nrow) {
-        const int a = d.rowSolid[r];
+        const int a = solidOf(d, r);
         items = min(d.fcnt[par][r], d.scap) + min(d.rcnt[r], d.scap) + d.bondStart[a + 1] - d.bondStart[a];
         rows = 1;
     }
@@ -708,7 +708,7 @@ __global__ void kBondFlags(DeviceState d, int par, int* flag)
     const int r = (int)(i / d.scap), k = (int)(i % d.scap);
     int ok = 0;
     if (k < min(d.fcnt[par][r], d.scap)) {
-        const int a = d.rowSolid[r], b = d.fwd[par][(size_t)k * d.nrow + r];
+        const int a = solidOf(d, r), b = d.fwd[par][(size_t)k * d.nrow + r];
         const float4 ra = d.srad[a], rb = d.srad[b];
         const dfl dist = dfNorm(relDF(d.scell[a], d.sph[a], d.spl[a], d.scell[b], d.sph[b], d.spl[b], d.grid));
         // skip when r_a + r_b + 1e-10 <= |x_a - x_b|
@@ -728,7 +728,7 @@ __global__ void kBondWrite(DeviceState d, int par, const int* flag, const int* p
     if (i >= (long long)d.nrow * d.scap || !flag[i]) return;
     const int r = (int)(i / d.scap), k = (int)(i % d.scap);
     const int b = pos[i];
-    const int ii = d.rowSolid[r], j = d.fwd[par][(size_t)k * d.nrow + r];
+    const int ii = solidOf(d, r), j = d.fwd[par][(size_t)k * d.nrow + r];
     const DF3 rr = relDF(d.scell[ii], d.sph[ii], d.spl[ii], d.scell[j], d.sph[j], d.spl[j], d.grid);
     const dfl dist = dfNorm(rr);
     const float dd = dist.hi;
@@ -820,7 +820,7 @@ __global__ void __launch_bounds__(T) kFluidWalk(DeviceState d, RunIf lists, RunI
     fluidWalk<L, BUILD_CANDIDATES>(d, cands);
     if (*d.status) return;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < d.nrow; r += gridDim.x * blockDim.x) {
-        const int a = d.rowSolid[r];
+        const int a = solidOf(d, r);
         const int4 c = d.scell[a];
         const float4 h = d.sph[a];
         d.svref[a] = make_float4((float)c.x * d.grid.cs.x + h.x, (float)c.y * d.grid.cs.y + h.y,
