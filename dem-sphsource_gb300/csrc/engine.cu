@@ -760,7 +760,12 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.gridBar = dalloc<unsigned>(2, e->owned, e->stream);
             {
                 const char* v = std::getenv("DEMSPH_COOPERATIVE_SORT");
-                d.sortBlocks = (v && v[0] == '0') ? 0 : cooperativeSortBlocks();
+                // at most two blocks per SM, and no more than two elements per
+                // thread need: small scenes leave the GPU to the others
+                const long long n = std::max<long long>(d.nf, ns);
+                d.sortBlocks = (v && v[0] == '0') ? 0
+                                                 : (int)std::min<long long>(cooperativeSortBlocks(),
+                                                                            std::max<long long>(1, (n + 511) / 512));
             }
             d.forceRows = o.contact_rows_per_warp > 0 ? o.contact_rows_per_warp : 32;
             e->adaptRows = o.contact_rows_per_warp == 0;
