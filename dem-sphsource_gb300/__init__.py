@@ -88,6 +88,10 @@ class LaunchShapes(C.Structure):
     _fields_ = [("fluid_lanes", _I), ("clump_lanes", _I), ("contact_force_rows", _I)]
 
 
+class RunStats(C.Structure):
+    _fields_ = [("list_growths", C.c_longlong), ("resumed_steps", C.c_longlong), ("fused_passes", C.c_longlong)]
+
+
 class AuditValues(C.Structure):
     _fields_ = [("mass", _D), ("momentum", _D * 3), ("kinetic_energy", _D), ("rotational_energy", _D),
                 ("potential_energy", _D), ("fluid_density_sum", _D)]
@@ -481,6 +485,12 @@ class Engine:
         v = LaunchShapes()
         self._chk(self.lib.demsph_get_launch_shapes(self.h, C.byref(v)), "launch_shapes")
         return {n: getattr(v, n) for n, _ in LaunchShapes._fields_}
+
+    def run_stats(self):
+        """{list_growths, resumed_steps, fused_passes} of the update runs so far."""
+        v = RunStats()
+        self._chk(self.lib.demsph_get_run_stats(self.h, C.byref(v)), "run_stats")
+        return {n: getattr(v, n) for n, _ in RunStats._fields_}
 
     def solid_pairs(self):
         prefix = np.zeros(self.ns, np.int32)

@@ -584,10 +584,14 @@ __device__ __forceinline__ void kickRegs(float4& vh, float4& vl, float4& wh, flo
 
 // One half-step of a solid that is not a clump pebble (integrate.cu:964-1027):
 // before contact kick then drift; after contact drift, kick, the displacement
-// check and the cell key of the next step.  Every input is read before
-// anything is written: the compiler cannot tell the arrays apart, so a read
-// placed after a write would wait for it.
-__device__ __forceinline__ void solidIntegrateOne(const DeviceState& d, int i, dfl half, int before)
+// check and the cell key of the next step; fused, the after-contact half, its
+// end-of-step offset to sphE/splE, then the next step's before-contact half
+// from the same registers (the same operations on the same values as the two
+// separate passes).  Every input is read before anything is written: the
+// compiler cannot tell the arrays apart, so a read placed after a write would
+// wait for it.
+template <int MODE>
+__device__ __forceinline__ void solidIntegrateOne(const DeviceState& d, int i, dfl half)
 {
     const int4 f = d.sflags[i];
     float4 ph = d.sph[i], pl = d.spl[i], vh = d.svh[i], vl = d.svl[i], wh = d.swh[i], wl = d.swl[i];
@@ -596,7 +600,7 @@ __device__ __forceinline__ void solidIntegrateOne(const DeviceState& d, int i, d
     int row = -1;
     int4 c = make_int4(0, 0, 0, 0);
     float4 p0 = make_float4(0, 0, 0, 0), q0 = p0;
-    if (!before) {
+    if (MODE != INTEGRATE_BEFORE) {
         row = rowOf(d, i);
         c = d.scell[i];
         p0 = d.vref[i];
@@ -604,16 +608,18 @@ __device__ __forceinline__ void solidIntegrateOne(const DeviceState& d, int i, d
     }
     if (f.z >= 0) return;  // clump pebbles: clumpIntegrateGroup
     const bool spin = !((f.w & F_FIXED) || r < 1.e-10f);
-    if (before) {
+    if (MODE != INTEGRATE_BEFORE) {
+        driftRegs(ph, pl, vh, vl, half);
+        kickRegs(vh, vl, wh, wl, a, tq, r, ph.w, spin, half);
+        checkDisplacementOf(d, row, c, ph, p0, q0);
+        rehashSolidTo(d, i, row, c, ph, pl, MODE == INTEGRATE_FUSED ? d.sphE : d.sph,
+                      MODE == INTEGRATE_FUSED ? d.splE : d.spl);
+    }
+    if (MODE != INTEGRATE_AFTER) {
         kickRegs(vh, vl, wh, wl, a, tq, r, ph.w, spin, half);
         driftRegs(ph, pl, vh, vl, half);
         d.sph[i] = ph;
         d.spl[i] = pl;
-    } else {
-        driftRegs(ph, pl, vh, vl, half);
-        kickRegs(vh, vl, wh, wl, a, tq, r, ph.w, spin, half);
-        checkDisplacementOf(d, row, c, ph, p0, q0);
-        rehashSolidOf(d, i, row, c, ph, pl);
     }
     d.svh[i] = vh;
     d.svl[i] = vl;
@@ -708,7 +714,10 @@ __device__ __forceinline__ void pebbleKick(const DeviceState& d, int i, float3 a
 // first lane advances the clump's state, the lanes then move the pebbles.
 //   before contact: kick, pebbles from the kicked state, centroid and pebble drift;
 //   after contact:  pebble and centroid drift, kick, pebbles from the kicked state.
-__device__ __forceinline__ void clumpIntegrateGroup(const DeviceState& d, dfl halfDF, int before, int width, int t)
+//   withEnd (after contact): the pebbles' end-of-step offsets also go to
+//   sphE/splE (a fused pass, whose before-contact half follows).
+__device__ __forceinline__ void clumpIntegrateGroup(const DeviceState& d, dfl halfDF, int before, int width, int t,
+                                                    bool withEnd = false)
 {
     const int c = t / width, lane = t % width;
     // whole warps only: the shuffles below take every lane of the warp
@@ -754,7 +763,7 @@ __device__ __forceinline__ void clumpIntegrateGroup(const DeviceState& d, dfl ha
             driftSolid(d, i, halfDF);
         } else {
             checkDisplacement(d, i);
-            rehashSolid(d, i);
+            rehashSolid(d, i, withEnd);
         }
     }
 }
@@ -765,27 +774,35 @@ __global__ void kClumpForce(DeviceState d, int width)
     clumpForceGroup(d, width, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// One half-step integration of all solids (integrate.cu:964-1027): the first
+// One half-step integration of all solids (integrate.cu:964-1027), or, fused,
+// the closing half of one step and the opening half of the next: the first
 // clumpBlocks blocks take a group of `width` lanes per clump (first, so their
 // longer chains of dependent reads overlap the rest), the others one solid
 // each per thread.  clumpForce: each clump group first sums its pebbles'
 // forces (kClumpForce's work, for runs of whole steps where nothing happens
 // between the contact phase and this integration); countStep: the step has
 // completed (the status can no longer change) and is counted.
-__global__ void kIntegrate(DeviceState d, dfl half, int before, int width, int clumpBlocks, int clumpForce,
-                           int countStep)
+template <int MODE>
+__global__ void kIntegrate(DeviceState d, dfl half, int width, int clumpBlocks, int clumpForce, int countStep)
 {
     stepKernelBegin();
     if (countStep && blockIdx.x == 0 && threadIdx.x == 0 && *d.status == 0) atomicAdd(d.stepsDone, 1);
     if ((int)blockIdx.x >= clumpBlocks) {
         const int k = (blockIdx.x - clumpBlocks) * blockDim.x + threadIdx.x;
         if (k >= d.nmove || *d.status) return;
-        solidIntegrateOne(d, d.moveFirst >= 0 ? d.moveFirst + k : d.moveList[k], half, before);
+        solidIntegrateOne<MODE>(d, d.moveFirst >= 0 ? d.moveFirst + k : d.moveList[k], half);
         return;
     }
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (clumpForce) clumpForceGroup(d, width, t);
-    clumpIntegrateGroup(d, half, before, width, t);
+    if (MODE == INTEGRATE_FUSED) {
+        // the group's lanes take the same pebbles in both halves, and lane 0
+        // re-reads the clump state it wrote: each reads its own writes
+        clumpIntegrateGroup(d, half, 0, width, t, true);
+        clumpIntegrateGroup(d, half, 1, width, t);
+    } else {
+        clumpIntegrateGroup(d, half, MODE == INTEGRATE_BEFORE ? 1 : 0, width, t);
+    }
 }
 
 
@@ -808,15 +825,20 @@ void launchClumpForce(const DeviceState& d, cudaStream_t s)
     const int w = d.clumpLanes;
     launchStep(kClumpForce, blocksFor((long long)d.nc * w, 256), 256, s, d, w);
 }
-void launchSolidIntegrate(const DeviceState& d, double dt, bool before, bool clumpForce, bool countStep,
+void launchSolidIntegrate(const DeviceState& d, double dt, int mode, bool clumpForce, bool countStep,
                           cudaStream_t s)
 {
     const dfl h = df_from_double(0.5 * dt);
     const int sb = d.nmove > 0 ? blocksFor(d.nmove, 256) : 0;
     const int cb = d.nc > 0 ? blocksFor((long long)d.nc * d.clumpLanes, 256) : 0;
     if (sb + cb == 0 && !countStep) return;
-    launchStep(kIntegrate, std::max(1, sb + cb), 256, s, d, h, before ? 1 : 0, d.clumpLanes, cb, clumpForce ? 1 : 0,
-               countStep ? 1 : 0);
+    const int blocks = std::max(1, sb + cb), cf = clumpForce ? 1 : 0, cs = countStep ? 1 : 0;
+    if (mode == INTEGRATE_FUSED)
+        launchStep(kIntegrate<INTEGRATE_FUSED>, blocks, 256, s, d, h, d.clumpLanes, cb, cf, cs);
+    else if (mode == INTEGRATE_BEFORE)
+        launchStep(kIntegrate<INTEGRATE_BEFORE>, blocks, 256, s, d, h, d.clumpLanes, cb, cf, cs);
+    else
+        launchStep(kIntegrate<INTEGRATE_AFTER>, blocks, 256, s, d, h, d.clumpLanes, cb, cf, cs);
 }
 
 

@@ -194,9 +194,15 @@ struct StageTimer {
 #define TIMED(tag) StageTimer _stage_timer(e, tag)
 
 // ---- the five stages ----
-void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
+// endView: the solids' integration has already opened this step (a fused
+// pass): the search reads their end-of-step offsets from sphE/splE.
+void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = false)
 {
-    DeviceState& d = e->d;
+    DeviceState d = e->d;
+    if (endView) {
+        d.sph = d.sphE;
+        d.spl = d.splE;
+    }
     const cudaStream_t s = e->stream;
     const bool fluidStep = d.nf > 0 && (iStep % gap == 0);
     // solids that never move (walls of dummy particles, fixed spheres) are
@@ -247,7 +253,7 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap)
 void stageBefore(demsph_engine* e, double dt)
 {
     TIMED("integrate_before");
-    launchSolidIntegrate(e->d, dt, true, false, false, e->stream);
+    launchSolidIntegrate(e->d, dt, INTEGRATE_BEFORE, false, false, e->stream);
 }
 
 void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
@@ -303,19 +309,51 @@ void stageContact(demsph_engine* e, double dt, bool withClumpForce = true)
 void stageAfter(demsph_engine* e, double dt, bool clumpForce = false, bool countStep = false)
 {
     TIMED("integrate_after");
-    launchSolidIntegrate(e->d, dt, false, clumpForce, countStep, e->stream);
+    launchSolidIntegrate(e->d, dt, INTEGRATE_AFTER, clumpForce, countStep, e->stream);
 }
 
 // One solverBase::update() without the driver's hook.  The clump force sum
 // and the step count ride on the last integration (bit for bit what the
-// staged calls compute).
-void fullStep(demsph_engine* e, double dt, int iStep, int gap)
+// staged calls compute).  opened: the solids' before-contact half of this
+// step has run already (a step resumed after an overflow in its search).
+void fullStep(demsph_engine* e, double dt, int iStep, int gap, bool opened = false)
 {
-    stageNeighborSearch(e, iStep, gap);
-    stageBefore(e, dt);
+    stageNeighborSearch(e, iStep, gap, opened);
+    if (!opened) stageBefore(e, dt);
     stageFluid(e, dt, iStep, gap);
     stageContact(e, dt, false);
     stageAfter(e, dt, e->d.nc > 0, true);
+}
+
+// `length` >= 2 whole steps of plain DEM (no fluid step among them) where
+// each step but the last closes with the integration pass that also opens the
+// next step.  The neighbour search that sits between the two halves in
+// solverBase::update moves nothing and reads only the solids' end-of-step
+// positions (which the pass leaves in sphE/splE); the before-contact half
+// depends on nothing the search writes.  So the state after every step is
+// bit for bit that of fullStep.  The solids no integration moves (dummy
+// particles at rest) get their sphE/splE copy once, after the first search.
+void fusedSteps(demsph_engine* e, double dt, int iStep, int length, int gap)
+{
+    DeviceState& d = e->d;
+    stageNeighborSearch(e, iStep, gap);
+    const long long pebbles = std::count(e->moveKind.begin(), e->moveKind.end(), (unsigned char)0);
+    if (d.ns - d.nmove - pebbles > 0) {
+        CK(cudaMemcpyAsync(d.sphE, d.sph, sizeof(float4) * d.ns, cudaMemcpyDeviceToDevice, e->stream));
+        CK(cudaMemcpyAsync(d.splE, d.spl, sizeof(float4) * d.ns, cudaMemcpyDeviceToDevice, e->stream));
+    }
+    stageBefore(e, dt);
+    for (int k = 0; k < length; ++k) {
+        stageFluid(e, dt, iStep + k, gap);
+        stageContact(e, dt, false);
+        if (k == length - 1) break;
+        {
+            TIMED("integrate_after");
+            launchSolidIntegrate(d, dt, INTEGRATE_FUSED, d.nc > 0, true, e->stream);
+        }
+        stageNeighborSearch(e, iStep + k + 1, gap, true);
+    }
+    stageAfter(e, dt, d.nc > 0, true);
 }
 
 // Grows whatever overflowed and clears the status.  e->par must be the parity
@@ -679,6 +717,8 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.scell = dalloc<int4>(ns, e->owned, e->stream);
             d.sph = dalloc<float4>(ns, e->owned, e->stream);
             d.spl = dalloc<float4>(ns, e->owned, e->stream);
+            d.sphE = dalloc<float4>(ns, e->owned, e->stream);
+            d.splE = dalloc<float4>(ns, e->owned, e->stream);
             d.svh = dalloc<float4>(ns, e->owned, e->stream);
             d.svl = dalloc<float4>(ns, e->owned, e->stream);
             d.swh = dalloc<float4>(ns, e->owned, e->stream);
@@ -766,6 +806,10 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 d.sortBlocks = (v && v[0] == '0') ? 0
                                                  : (int)std::min<long long>(cooperativeSortBlocks(),
                                                                             std::max<long long>(1, (n + 511) / 512));
+            }
+            {
+                const char* v = std::getenv("DEMSPH_FUSE_INTEGRATION");
+                e->fuseIntegration = !(v && v[0] == '0');
             }
             d.forceRows = o.contact_rows_per_warp > 0 ? o.contact_rows_per_warp : 32;
             e->adaptRows = o.contact_rows_per_warp == 0;
@@ -1083,11 +1127,17 @@ static const demsph_engine::CachedGraph& graphFor(demsph_engine* e, int kind, in
     const int parity = e->par;
     cudaGraph_t g;
     const long long before = t_kernelLaunches;
+    // runs of plain DEM steps fuse each step's closing integration with the
+    // next one's opening (fluid steps are captured one at a time)
+    const bool fused = e->fuseIntegration && kind == 0 && length >= 2;
     CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < length; ++k) fullStep(e, dt, step + k, gap);
+    if (fused)
+        fusedSteps(e, dt, step, length, gap);
+    else
+        for (int k = 0; k < length; ++k) fullStep(e, dt, step + k, gap);
     CK(cudaStreamEndCapture(e->stream, &g));
     e->par = parity;  // nothing ran: the parity is where it was
-    demsph_engine::CachedGraph c{kind, parity, length, nullptr, t_kernelLaunches - before};
+    demsph_engine::CachedGraph c{kind, parity, length, nullptr, t_kernelLaunches - before, fused};
     e->capturedLaunches += c.kernels;
     const cudaError_t ie = cudaGraphInstantiate(&c.exec, g, 0);
     cudaGraphDestroy(g);
@@ -1133,6 +1183,7 @@ static int runUpdate(demsph_engine* e, double dt, int first_step, int n_steps, i
         if (attempt > 32) return fail(e, DEMSPH_ERR_CAPACITY, "list overflow persists after growing");
         CK(cudaMemsetAsync(d.stepsDone, 0, sizeof(int), e->stream));
         const int startPar = e->par;
+        const bool startOpened = e->resumeOpened;
         const bool graphs = use_graph && !e->profiling;
         if (graphs && (e->graphDt != dt || e->graphGap != gap)) {
             dropGraph(e);
@@ -1140,10 +1191,14 @@ static int runUpdate(demsph_engine* e, double dt, int first_step, int n_steps, i
             e->graphGap = gap;
         }
         int s = step;
+        // the first step of each fused graph launched: an overflow in the
+        // search of any later step of it leaves that step opened
+        std::vector<std::pair<int, int>> fusedRuns;
         while (s < end) {
             const int kind = stepKind(d, s, gap);
-            if (!graphs || s == 1) {  // step 1 stores the Shepard reference sums: run it as it is
-                fullStep(e, dt, s++, gap);
+            if (!graphs || s == 1 || e->resumeOpened) {  // step 1 stores the Shepard reference sums: run it as it is
+                fullStep(e, dt, s++, gap, e->resumeOpened);
+                e->resumeOpened = false;
                 continue;
             }
             // a run of plain DEM steps replays 10- and 2-step graphs (parity
@@ -1156,6 +1211,10 @@ static int runUpdate(demsph_engine* e, double dt, int first_step, int n_steps, i
                 const auto& g = graphFor(e, kind, len, dt, s, gap);
                 CK(cudaGraphLaunch(g.exec, e->stream));
                 e->replayedKernels += g.kernels;
+                if (g.fused) {
+                    fusedRuns.emplace_back(s, len);
+                    e->runStats.fused_passes += len - 1;
+                }
                 e->par ^= (len & 1);
                 s += len;
                 run -= len;
@@ -1178,6 +1237,15 @@ static int runUpdate(demsph_engine* e, double dt, int first_step, int n_steps, i
         if (st & ~ALL_OVERFLOWS) return fail(e, DEMSPH_ERR_STATE, "unexpected device status " + std::to_string(st));
         step += done;                        // steps before the failed one completed
         e->par = startPar ^ (done & 1);      // every step builds one contact list
+        // every overflow is raised in a neighbour search; in a fused graph the
+        // search of a step other than its first runs after the pass that
+        // opened that step (and a resumed step stays opened when its own
+        // search overflows again)
+        e->resumeOpened = done == 0 && startOpened;
+        for (const auto& r : fusedRuns)
+            if (step > r.first && step < r.first + r.second) e->resumeOpened = true;
+        if (e->resumeOpened) ++e->runStats.resumed_steps;
+        ++e->runStats.list_growths;
         grow(e, st);
     }
     if (afterSteps && n_steps == 0) {
@@ -1225,6 +1293,13 @@ int demsph_get_launch_shapes(const demsph_engine* e, demsph_launch_shapes* out)
     out->fluid_lanes = e->d.lanes;
     out->clump_lanes = e->d.clumpLanes;
     out->contact_force_rows = e->d.forceRows;
+    return DEMSPH_OK;
+}
+
+int demsph_get_run_stats(const demsph_engine* e, demsph_run_stats* out)
+{
+    if (!e || !out) return DEMSPH_ERR_ARGUMENT;
+    *out = e->runStats;
     return DEMSPH_OK;
 }
 

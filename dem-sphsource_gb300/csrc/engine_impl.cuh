@@ -70,7 +70,15 @@ struct demsph_engine {
         int kind, parity, length;
         cudaGraphExec_t exec;
         long long kernels;
+        bool fused;  // its steps after the first open with the previous step's closing integration
     };
+    // Graphs of two or more plain DEM steps integrate the end of one step and
+    // the start of the next in one pass (DEMSPH_FUSE_INTEGRATION=0 keeps two).
+    bool fuseIntegration = true;
+    // The step the next attempt starts with already had its before-contact
+    // half applied (a fused pass ran before its neighbour search overflowed).
+    bool resumeOpened = false;
+    demsph_run_stats runStats{};
     std::vector<CachedGraph> graphs;
     int graphGap = 0;
     double graphDt = 0;

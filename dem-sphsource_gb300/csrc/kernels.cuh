@@ -209,6 +209,12 @@ struct DeviceState {
     int4* scell;
     float4* sph;             // offset hi, w = inverse mass
     float4* spl;
+    // End-of-step offsets (hi, lo) while sph/spl already hold the next step's
+    // midpoint: the integration that closes a step and opens the next one in
+    // one pass (INTEGRATE_FUSED) leaves them here for the neighbour search
+    // between the two halves, which then reads these in place of sph/spl.
+    float4* sphE;
+    float4* splE;
     float4* svh;
     float4* svl;
     float4* swh;
@@ -424,9 +430,15 @@ void launchBonds(const DeviceState& d, int parity, float dt, cudaStream_t s);
 // Contact, bond, wall, coupling and gravity forces of every solid.
 void launchSolidForces(const DeviceState& d, int parity, float dt, cudaStream_t s);
 void launchClumpForce(const DeviceState& d, cudaStream_t s);
+// Kinds of solid integration pass: the half step after the contact forces
+// (closing a step), the half step before them (opening one), or both in one
+// pass - the closing half of step n, then the opening half of step n + 1 from
+// the same forces (the neighbour search of step n + 1, which moves nothing,
+// runs after it on the end-of-step offsets in sphE/splE).
+enum IntegrateMode { INTEGRATE_AFTER = 0, INTEGRATE_BEFORE = 1, INTEGRATE_FUSED = 2 };
 // Half-step integration of all solids; clumpForce: sum the clumps' pebble
 // forces first (instead of launchClumpForce); countStep: count the step.
-void launchSolidIntegrate(const DeviceState& d, double dt, bool before, bool clumpForce, bool countStep,
+void launchSolidIntegrate(const DeviceState& d, double dt, int mode, bool clumpForce, bool countStep,
                           cudaStream_t s);
 
 // Absolute FP64 position of solid i (cell origin + double-float offset).
@@ -475,7 +487,11 @@ __device__ __forceinline__ void checkDisplacement(const DeviceState& d, int i)
 // cell, the key and the walk centre stored; a solid that can touch others and
 // has left the domain sends the next lists to the reference's walk.  c, h, l:
 // the solid's cell and offset after its last drift.
-__device__ __forceinline__ void rehashSolidOf(const DeviceState& d, int i, int row, int4 c, float4 h, float4 l)
+// rehashSolidTo leaves the renormalised offset in h, l and stores it to
+// outH, outL (sph, spl; sphE, splE when the next step's first half is
+// integrated in the same pass).
+__device__ __forceinline__ void rehashSolidTo(const DeviceState& d, int i, int row, int4 c, float4& h, float4& l,
+                                              float4* outH, float4* outL)
 {
     renormAxis(c.x, h.x, l.x, d.grid.csx);
     renormAxis(c.y, h.y, l.y, d.grid.csy);
@@ -483,17 +499,27 @@ __device__ __forceinline__ void rehashSolidOf(const DeviceState& d, int i, int r
     const int key = cellKey(c.x, c.y, c.z, d.grid);
     c.w = key;
     d.scell[i] = c;
-    d.sph[i] = h;
-    d.spl[i] = l;
+    outH[i] = h;
+    outL[i] = l;
     d.skey[i] = key;
     if (row >= 0) {
         d.scentre[row] = make_int4(truncAxis(c.x, h.x, l.x), truncAxis(c.y, h.y, l.y), truncAxis(c.z, h.z, l.z), 0);
         if (key == d.grid.num - 1) *(volatile int*)d.slowMode = 1;
     }
 }
-__device__ __forceinline__ void rehashSolid(const DeviceState& d, int i)
+__device__ __forceinline__ void rehashSolidOf(const DeviceState& d, int i, int row, int4 c, float4 h, float4 l)
 {
-    rehashSolidOf(d, i, rowOf(d, i), d.scell[i], d.sph[i], d.spl[i]);
+    rehashSolidTo(d, i, row, c, h, l, d.sph, d.spl);
+}
+// withEnd: the end-of-step offset also goes to sphE, splE.
+__device__ __forceinline__ void rehashSolid(const DeviceState& d, int i, bool withEnd = false)
+{
+    float4 h = d.sph[i], l = d.spl[i];
+    rehashSolidTo(d, i, rowOf(d, i), d.scell[i], h, l, d.sph, d.spl);
+    if (withEnd) {
+        d.sphE[i] = h;
+        d.splE[i] = l;
+    }
 }
 
 

@@ -495,3 +495,30 @@ def tiny_coupled(seed=4, gap=3):
     r.setSimulationParameterNumFrames(1)
     r.meta.update(dt=dt, steps=40, gap=gap, dx=dx)
     return r
+
+
+def tiny_converging(n=4, spacing=2.3e-3, radius=1.0e-3, rate=1200.0, steps=40):
+    """An n x n x n lattice of equal spheres with 0.3 mm gaps whose velocities
+    point at the lattice centre (v = -rate (x - centre)), no gravity, no walls,
+    no fluid: every sphere meets its lattice neighbours within a few steps of
+    the others, so the contact rows fill from empty in the middle of a run."""
+    r = Recipe("tiny_converging")
+    ax = (np.arange(n) + 0.5) * spacing
+    p = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), axis=-1).reshape(-1, 3)
+    c = 0.5 * n * spacing
+    m = 3 * spacing
+    r.setDomain((-m, -m, -m), (n * spacing + 2 * m,) * 3)
+    r.setGravity((0.0, 0.0, 0.0))
+    Es, Gs = hertz_from_E_nu(1.0e8, 0.3)
+    r.setHertzianContactModel(0, 0, Es, Gs, 0.5, 0.0, 0.0, 0.4, 0.0, 0.0)
+    density = 2500.0
+    for k in range(len(p)):
+        r.addSolid(p[k:k + 1], tuple(-rate * (p[k] - c)), radius, density, 0)
+    G = 1.0e8 / (2 * 1.3)
+    t_r = math.pi * radius * math.sqrt(density / G) / (0.1631 * 0.3 + 0.8766)
+    dt = 0.1 * t_r
+    r.setSimulationParameterTimeStep(dt)
+    r.setSimulationParameterMaximumTime((steps - 0.5) * dt)
+    r.setSimulationParameterNumFrames(1)
+    r.meta.update(dt=dt, steps=steps, gap=1, dx=spacing)
+    return r

@@ -270,6 +270,17 @@ typedef struct demsph_launch_shapes {
     int contact_force_rows;
 } demsph_launch_shapes;
 DEMSPH_API int demsph_get_launch_shapes(const demsph_engine* e, demsph_launch_shapes* out);
+/* Counters of the engine's update runs since creation (no counterpart in the
+   reference): list growths after an overflow, steps resumed from their
+   midpoint (their opening half step had run, in a pass that also closed the
+   step before, when the neighbour search overflowed), and integration passes
+   that closed one step and opened the next. */
+typedef struct demsph_run_stats {
+    long long list_growths;
+    long long resumed_steps;
+    long long fused_passes;
+} demsph_run_stats;
+DEMSPH_API int demsph_get_run_stats(const demsph_engine* e, demsph_run_stats* out);
 /* The CUDA stream (cudaStream_t) the engine issues all its work on, for
    callers that time or order work around it. */
 DEMSPH_API void* demsph_stream(demsph_engine* e);

@@ -290,6 +290,70 @@ def test_cooperative_sorts_equal_launch_per_phase_sorts(ds, scenes, name, monkey
             assert np.array_equal(s0[k], s1[k]), k
 
 
+def _dry_granular(scenes):
+    return scenes.tiny_granular(with_probe_fluid=False)
+
+
+def _same_state_and_lists(e0, e1):
+    if e0.nf:
+        for a, c in zip(e0.download_fluids(), e1.download_fluids()):
+            assert np.array_equal(a, c)
+    if e0.ns:
+        s0, s1 = e0.download_solids(), e1.download_solids()
+        for k in s0:
+            assert np.array_equal(s0[k], s1[k]), k
+        p0, p1 = e0.solid_pairs(), e1.solid_pairs()
+        for k in p0:
+            assert np.array_equal(p0[k], p1[k]), k
+
+
+@pytest.mark.parametrize("name", ("tiny_converging", "dry_granular", "tiny_coupled"))
+def test_fused_integration_equals_separate_passes(ds, scenes, name, monkeypatch):
+    """Graphs of plain DEM steps close each step and open the next in one
+    integration pass, with the neighbour search in between reading the
+    end-of-step offsets; forty steps give the bits of the two separate passes
+    (DEMSPH_FUSE_INTEGRATION=0, read when an engine is created) and of the
+    staged calls."""
+    recipe = _dry_granular(scenes) if name == "dry_granular" else getattr(scenes, name)()
+    b, sc = ds.build_scene(recipe)
+    engines = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("DEMSPH_FUSE_INTEGRATION", flag)
+        engines.append(ds.Engine(sc))
+    monkeypatch.delenv("DEMSPH_FUSE_INTEGRATION")
+    staged = ds.Engine(sc)
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for e in engines + [staged]:
+        e.initialize()
+    for e in engines:
+        e.update(dt, 1, 40, gap, use_graph=True)
+    for s in range(1, 41):
+        staged.step(dt, s, gap)
+    assert engines[0].run_stats()["fused_passes"] > 0
+    assert engines[1].run_stats()["fused_passes"] == 0
+    _same_state_and_lists(engines[0], engines[1])
+    _same_state_and_lists(engines[0], staged)
+
+
+def test_overflow_inside_a_fused_run_resumes_the_opened_step(ds, scenes):
+    """In the converging lattice every sphere gains three forward contacts
+    at step 15, inside the graph of steps 12-21; with one contact slot per row
+    that step's search overflows after the fused pass has opened it.  The
+    engine grows the rows and resumes the step from its midpoint (no second
+    opening half step): the result equals a run with ample rows, bit for bit."""
+    b, sc = ds.build_scene(scenes.tiny_converging())
+    small = ds.Engine(sc, solid_contacts_per_particle=1)
+    big = ds.Engine(sc)
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for e in (small, big):
+        e.initialize()
+        e.update(dt, 1, 40, gap, use_graph=True)
+    st = small.run_stats()
+    assert st["resumed_steps"] >= 1 and st["list_growths"] >= 1, st
+    assert big.run_stats()["list_growths"] == 0
+    _same_state_and_lists(small, big)
+
+
 def test_drift_bounded_over_run(ds, scenes):
     """Forty steps of the coupled scene: the engine stays within bounded
     distance of the FP64 oracle (no systematic FP32 drift)."""
