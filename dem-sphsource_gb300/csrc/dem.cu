@@ -15,6 +15,7 @@
 // The per-particle gather adds forward pairs and subtracts reverse pairs in
 // list order - no atomics, so results are bit-reproducible run to run.
 #include "kernels.cuh"
+#include "contact_rows.cuh"
 #include "warp_items.cuh"
 
 namespace demsph {
@@ -22,7 +23,6 @@ namespace demsph {
 namespace {
 
 constexpr int T = 128;
-enum FlagBits { F_DUMMY = 1, F_FIXED = 2, F_MASSIVE = 4, F_HASMASS = 8 };
 constexpr float SQRT56 = 0.912870929175276855f;  // sqrt(5/6)
 
 // Tangential (sliding / rolling) spring with Coulomb cap (SPHKernelDEMContactModel.h:170-193).
@@ -318,6 +318,85 @@ __device__ __forceinline__ float wallOverlap(const DeviceState& d, int4 c, float
     return del.hi + del.lo;
 }
 
+// The rest of a row's force and torque once its contact and bond items are
+// summed: the coupling force, gravity and the infinite walls
+// (integrate.cu:514-610); stores the acceleration and torque.  Wall springs
+// come from the previous contact phase's parity and go to this step's
+// (wmask bit k, walls below 32: wall k's springs may be non-zero), so a step
+// abandoned after an overflow leaves the springs it started from.
+__device__ __forceinline__ void solidRowTail(const DeviceState& d, int par, int a, KahanF3& F, KahanF3& Tq,
+                                             int withCoupling, float dt)
+{
+    const int prev = par ^ 1;
+    const int4 fa = d.sflags[a];
+    if (withCoupling) F.add(-xyz(d.sfcoup[a]));
+    const float4 ph = d.sph[a];
+    const float im = ph.w;
+    float3 acc = F.sum() * im;
+    if ((fa.w & F_HASMASS) && fa.z < 0) acc = acc + d.g;
+    float3 tq = Tq.sum();
+    if (d.nw > 0 && !(fa.w & F_DUMMY) && !(fa.w & F_FIXED)) {
+        const int4 ca = d.scell[a];
+        const float4 pl = d.spl[a];
+        const float4 rad = d.srad[a];
+        const float3 v = xyz(d.svh[a]), w = xyz(d.swh[a]);
+        const unsigned held0 = d.wmask[prev][a];
+        unsigned mask = 0;
+        const float3 pf = make_float3((float)ca.x * d.grid.cs.x + ph.x, (float)ca.y * d.grid.cs.y + ph.y,
+                                      (float)ca.z * d.grid.cs.z + ph.z);
+        int k = 0;
+        for (; k < d.nw; ++k) {
+            const size_t h = (size_t)k * d.ns + a;  // wall-major: a warp's solids are adjacent
+            const bool held = k >= 32 || ((held0 >> k) & 1u);
+            // FP32 pre-test: a sphere clearly off the wall (by far more than
+            // the FP32 rounding of this estimate) has a negative exact overlap
+            const float3 nf = xyz(d.wnh[k]);
+            const float Pf = d.wP[k].x;
+            const float est = rad.x - (dot3(nf, pf) - Pf);
+            const float tol = 4.e-6f * (fabsf(pf.x) + fabsf(pf.y) + fabsf(pf.z) + fabsf(Pf) + rad.x);
+            const float delta = est < -tol ? -1.f : wallOverlap(d, ca, ph, pl, k, rad.x, rad.y);
+            if (delta < 0.f) {
+                // no contact: the springs are zero (bit k stays clear; walls
+                // from 32 on have no bit and store the zeros)
+                if (k >= 32) d.wspring[par][0][h] = d.wspring[par][1][h] = d.wspring[par][2][h] = make_float4(0, 0, 0, 0);
+                if (d.fixes & DEMSPH_FIX_WALL_LOOP) continue;
+                break;
+            }
+            const float3 n = xyz(d.wnh[k]);
+            const float3 lever = n * (-(rad.x - delta));
+            const float3 vc = v + cross3(w, lever);
+            float3 es = make_float3(0.f, 0.f, 0.f), er = es, et = es;
+            if (held) {
+                es = xyz(d.wspring[prev][0][h]);
+                er = xyz(d.wspring[prev][1][h]);
+                et = xyz(d.wspring[prev][2][h]);
+            }
+            float3 Fw = make_float3(0.f, 0.f, 0.f), Fwt = Fw, Tw = Fw;
+            const int slot = tableSlot(d.tab, fa.x, d.wmat[k]);
+            contactLaw(d.tab, slot, Fw, Fwt, Tw, es, er, et, vc, w, n, delta, 1.f / im, rad.x, dt);
+            d.wspring[par][0][h] = f4(es);
+            d.wspring[par][1][h] = f4(er);
+            d.wspring[par][2][h] = f4(et);
+            if (k < 32) mask |= 1u << k;
+            acc = acc + Fw * im;
+            tq = tq + Tw + cross3(n, Fwt) * (-(rad.x - delta));
+        }
+        // the walls after the first one not touched keep their springs (the
+        // reference returns from its wall loop there)
+        for (++k; k < d.nw; ++k) {
+            if (k < 32 && !((held0 >> k) & 1u)) continue;
+            const size_t h = (size_t)k * d.ns + a;
+            d.wspring[par][0][h] = d.wspring[prev][0][h];
+            d.wspring[par][1][h] = d.wspring[prev][1][h];
+            d.wspring[par][2][h] = d.wspring[prev][2][h];
+            if (k < 32) mask |= 1u << k;
+        }
+        d.wmask[par][a] = mask;
+    }
+    d.sacc[a] = f4(acc);
+    d.storque[a] = f4(tq);
+}
+
 // Force and torque on every solid that can touch others (calSolidForceTorque,
 // core/integrate.cu:806-858, with the contact forces of :423-512, the bonds of
 // :717-804 and the walls of :514-610), one thread per row: each contact is
@@ -328,26 +407,82 @@ __device__ __forceinline__ float wallOverlap(const DeviceState& d, int4 c, float
 // Rows hold few contacts and their counts vary: a warp runs its rows'
 // (row, contact) items through warpItems, one lane per item, and each row's
 // lane adds its results in contact order.
-__global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, float dt, int withCoupling)
+//
+// MERGED (kContactDetect's work in the same launch, for plain DEM steps
+// opened by a fused integration pass; 32 rows per warp): each lane first
+// builds its row's list from the candidates (rebuilt when stale) on the
+// end-of-step offsets sphE/splE, exactly as kContactDetect does; both solids
+// of a pair then take its springs from the previous list (springOut of the
+// other parity) - the same values kContactDetect's remap would hand them.
+// The candidates and the contact test are symmetric in the two solids, so
+// the forward row of every reverse pair holds it.  In the walk mode they need
+// not be: the launch then raises ST_SPLIT_CONTACTS before writing anything,
+// and the step is redone with the two launches.
+template <bool MERGED>
+__global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, float dt, int withCoupling,
+                                                     int rowsPerWarp)
 {
     stepKernelBegin();
     __shared__ float4 itemF[T], itemT[T];  // 32 items per warp
     if (*d.status) return;
-    // every row's contact detection has seen the rebuild flag: the candidates
-    // are fresh from here on, and the last drift of the step raises the flag
-    // again once a solid moves too far
-    if (blockIdx.x == 0 && threadIdx.x == 0) *(volatile int*)d.rebuild = 0;
+    if (MERGED && *d.slowMode) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(d.status, ST_SPLIT_CONTACTS);
+        return;
+    }
+    const int prev = par ^ 1;
+    // this step's flag has been read by every row's contact detection (the
+    // launch before, or this launch's rows - then it is cleared by the next
+    // step's launch); the step before's flag is free for this step's closing
+    // drift to raise
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (!MERGED) *(volatile int*)&d.rebuild[par] = 0;
+        *(volatile int*)&d.rebuild[prev] = 0;
+    }
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    // lanes 0 .. forceRows - 1 of each warp own a row
-    const int row0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * d.forceRows;
+    // lanes 0 .. rowsPerWarp - 1 of each warp own a row
+    const int row0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rowsPerWarp;
     const int row = row0 + lane;
-    const bool live = lane < d.forceRows && row < d.nrow;
+    const bool live = lane < rowsPerWarp && row < d.nrow;
     const int a = live ? solidOf(d, row) : 0;
     const size_t nr = (size_t)d.nrow;
     // forward contacts (a, b) come first, then reverse ones (b, a)
-    const int n = live ? min(d.fcnt[par][row], d.scap) : 0;
-    const int contacts = live ? n + min(d.rcnt[row], d.scap) : 0;
+    int n = 0, contacts = 0;
+    if (MERGED) {
+        if (live) {
+            DeviceState atEnd = d;  // the end-of-step offsets
+            atEnd.sph = d.sphE;
+            atEnd.spl = d.splE;
+            if (d.rebuild[par]) verletBuildRow(atEnd, row);
+            const int C = d.scap;
+            int nf = 0, nb = 0;
+            const int nc = min(d.vcnt[row], d.vcap);
+            for (int k = 0; k < nc; ++k) {
+                const int b = d.vcand[(size_t)k * nr + row];
+                if (!solidsTouch(atEnd, a, b)) continue;
+                if (b > a) {
+                    if (nf < C) d.fwd[par][(size_t)nf * nr + row] = b;
+                    ++nf;
+                } else {
+                    if (nb < C) d.rev[(size_t)nb * nr + row] = b;
+                    ++nb;
+                }
+            }
+            d.fcnt[par][row] = nf;
+            d.rcnt[row] = nb;
+            if (nf > C || nb > C) {
+                atomicOr(d.status, ST_SS_OVERFLOW);
+                atomicMax(&d.need[0], max(nf, nb));
+                nf = nb = 0;
+            }
+            n = nf;
+            contacts = nf + nb;
+        }
+        __syncwarp();  // the row's list entries, for the lanes that evaluate them
+    } else if (live) {
+        n = min(d.fcnt[par][row], d.scap);
+        contacts = n + min(d.rcnt[row], d.scap);
+    }
     // then the row's bonds (their forces come from kBonds)
     const int bondFirst = live ? d.bondStart[a] : 0;
     const int total = contacts + (live ? d.bondStart[a + 1] - bondFirst : 0);
@@ -373,15 +508,27 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
                 } else {
                     A = d.rev[(size_t)(q - on) * nr + orow];
                     B = oa;
-                    k = forwardSlot(d, par, A, oa);
+                    k = MERGED ? 0 : forwardSlot(d, par, A, oa);
                 }
                 if (k >= 0) {
-                    float3 es = xyz(d.springIn[0][k]), er = xyz(d.springIn[1][k]), et = xyz(d.springIn[2][k]);
+                    float3 es = make_float3(0.f, 0.f, 0.f), er = es, et = es;
+                    if (MERGED) {
+                        const long long ko = forwardSlot(d, prev, A, B);  // the pair in the previous list
+                        if (ko >= 0) {
+                            es = xyz(d.springOut[prev][0][ko]);
+                            er = xyz(d.springOut[prev][1][ko]);
+                            et = xyz(d.springOut[prev][2][ko]);
+                        }
+                    } else {
+                        es = xyz(d.springIn[0][k]);
+                        er = xyz(d.springIn[1][k]);
+                        et = xyz(d.springIn[2][k]);
+                    }
                     const PairForce p = pairForce(d, A, B, es, er, et, dt);
                     if (fwdSide) {
-                        d.springOut[0][k] = f4(es);
-                        d.springOut[1][k] = f4(er);
-                        d.springOut[2][k] = f4(et);
+                        d.springOut[par][0][k] = f4(es);
+                        d.springOut[par][1][k] = f4(er);
+                        d.springOut[par][2][k] = f4(et);
                         d.pF[k] = f4(p.F);
                         d.pT[k] = f4(p.T);
                         rF = make_float4(p.F.x, p.F.y, p.F.z, 1.f);
@@ -415,66 +562,7 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
             }
         });
     if (!live) return;
-    const int4 fa = d.sflags[a];
-    if (withCoupling) F.add(-xyz(d.sfcoup[a]));
-    const float4 ph = d.sph[a];
-    const float im = ph.w;
-    float3 acc = F.sum() * im;
-    if ((fa.w & F_HASMASS) && fa.z < 0) acc = acc + d.g;
-    float3 tq = Tq.sum();
-    // infinite walls (integrate.cu:514-610).  wmask bit k (walls below 32):
-    // the springs of wall k may be non-zero; a clear bit spares reading and
-    // re-zeroing them.
-    if (d.nw > 0 && !(fa.w & F_DUMMY) && !(fa.w & F_FIXED)) {
-        const int4 ca = d.scell[a];
-        const float4 pl = d.spl[a];
-        const float4 rad = d.srad[a];
-        const float3 v = xyz(d.svh[a]), w = xyz(d.swh[a]);
-        const unsigned mask0 = d.wmask[a];
-        unsigned mask = mask0;
-        const float3 pf = make_float3((float)ca.x * d.grid.cs.x + ph.x, (float)ca.y * d.grid.cs.y + ph.y,
-                                      (float)ca.z * d.grid.cs.z + ph.z);
-        for (int k = 0; k < d.nw; ++k) {
-            const size_t h = (size_t)k * d.ns + a;  // wall-major: a warp's solids are adjacent
-            const bool held = k >= 32 || ((mask >> k) & 1u);
-            // FP32 pre-test: a sphere clearly off the wall (by far more than
-            // the FP32 rounding of this estimate) has a negative exact overlap
-            const float3 nf = xyz(d.wnh[k]);
-            const float Pf = d.wP[k].x;
-            const float est = rad.x - (dot3(nf, pf) - Pf);
-            const float tol = 4.e-6f * (fabsf(pf.x) + fabsf(pf.y) + fabsf(pf.z) + fabsf(Pf) + rad.x);
-            const float delta = est < -tol ? -1.f : wallOverlap(d, ca, ph, pl, k, rad.x, rad.y);
-            if (delta < 0.f) {
-                if (held) {
-                    d.wspring[0][h] = d.wspring[1][h] = d.wspring[2][h] = make_float4(0, 0, 0, 0);
-                    if (k < 32) mask &= ~(1u << k);
-                }
-                if (d.fixes & DEMSPH_FIX_WALL_LOOP) continue;
-                break;
-            }
-            const float3 n = xyz(d.wnh[k]);
-            const float3 lever = n * (-(rad.x - delta));
-            const float3 vc = v + cross3(w, lever);
-            float3 es = make_float3(0.f, 0.f, 0.f), er = es, et = es;
-            if (held) {
-                es = xyz(d.wspring[0][h]);
-                er = xyz(d.wspring[1][h]);
-                et = xyz(d.wspring[2][h]);
-            }
-            float3 Fw = make_float3(0.f, 0.f, 0.f), Fwt = Fw, Tw = Fw;
-            const int slot = tableSlot(d.tab, fa.x, d.wmat[k]);
-            contactLaw(d.tab, slot, Fw, Fwt, Tw, es, er, et, vc, w, n, delta, 1.f / im, rad.x, dt);
-            d.wspring[0][h] = f4(es);
-            d.wspring[1][h] = f4(er);
-            d.wspring[2][h] = f4(et);
-            if (k < 32) mask |= 1u << k;
-            acc = acc + Fw * im;
-            tq = tq + Tw + cross3(n, Fwt) * (-(rad.x - delta));
-        }
-        if (mask != mask0) d.wmask[a] = mask;
-    }
-    d.sacc[a] = f4(acc);
-    d.storque[a] = f4(tq);
+    solidRowTail(d, par, a, F, Tq, withCoupling, dt);
 }
 
 // x_i - centroid of pebble i as double-float per axis, then float.
@@ -591,7 +679,7 @@ __device__ __forceinline__ void kickRegs(float4& vh, float4& vl, float4& wh, flo
 // compiler cannot tell the arrays apart, so a read placed after a write would
 // wait for it.
 template <int MODE>
-__device__ __forceinline__ void solidIntegrateOne(const DeviceState& d, int i, dfl half)
+__device__ __forceinline__ void solidIntegrateOne(const DeviceState& d, int i, dfl half, int* stale)
 {
     const int4 f = d.sflags[i];
     float4 ph = d.sph[i], pl = d.spl[i], vh = d.svh[i], vl = d.svl[i], wh = d.swh[i], wl = d.swl[i];
@@ -611,7 +699,7 @@ __device__ __forceinline__ void solidIntegrateOne(const DeviceState& d, int i, d
     if (MODE != INTEGRATE_BEFORE) {
         driftRegs(ph, pl, vh, vl, half);
         kickRegs(vh, vl, wh, wl, a, tq, r, ph.w, spin, half);
-        checkDisplacementOf(d, row, c, ph, p0, q0);
+        checkDisplacementOf(d, stale, row, c, ph, p0, q0);
         rehashSolidTo(d, i, row, c, ph, pl, MODE == INTEGRATE_FUSED ? d.sphE : d.sph,
                       MODE == INTEGRATE_FUSED ? d.splE : d.spl);
     }
@@ -717,7 +805,7 @@ __device__ __forceinline__ void pebbleKick(const DeviceState& d, int i, float3 a
 //   withEnd (after contact): the pebbles' end-of-step offsets also go to
 //   sphE/splE (a fused pass, whose before-contact half follows).
 __device__ __forceinline__ void clumpIntegrateGroup(const DeviceState& d, dfl halfDF, int before, int width, int t,
-                                                    bool withEnd = false)
+                                                    int* stale, bool withEnd = false)
 {
     const int c = t / width, lane = t % width;
     // whole warps only: the shuffles below take every lane of the warp
@@ -762,7 +850,7 @@ __device__ __forceinline__ void clumpIntegrateGroup(const DeviceState& d, dfl ha
         if (before) {
             driftSolid(d, i, halfDF);
         } else {
-            checkDisplacement(d, i);
+            checkDisplacement(d, stale, i);
             rehashSolid(d, i, withEnd);
         }
     }
@@ -783,14 +871,16 @@ __global__ void kClumpForce(DeviceState d, int width)
 // between the contact phase and this integration); countStep: the step has
 // completed (the status can no longer change) and is counted.
 template <int MODE>
-__global__ void kIntegrate(DeviceState d, dfl half, int width, int clumpBlocks, int clumpForce, int countStep)
+__global__ void kIntegrate(DeviceState d, dfl half, int width, int clumpBlocks, int clumpForce, int countStep,
+                           int par)
 {
     stepKernelBegin();
+    int* stale = d.rebuild + (par ^ 1);  // the next step's candidate flag
     if (countStep && blockIdx.x == 0 && threadIdx.x == 0 && *d.status == 0) atomicAdd(d.stepsDone, 1);
     if ((int)blockIdx.x >= clumpBlocks) {
         const int k = (blockIdx.x - clumpBlocks) * blockDim.x + threadIdx.x;
         if (k >= d.nmove || *d.status) return;
-        solidIntegrateOne<MODE>(d, d.moveFirst >= 0 ? d.moveFirst + k : d.moveList[k], half);
+        solidIntegrateOne<MODE>(d, d.moveFirst >= 0 ? d.moveFirst + k : d.moveList[k], half, stale);
         return;
     }
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -798,10 +888,10 @@ __global__ void kIntegrate(DeviceState d, dfl half, int width, int clumpBlocks, 
     if (MODE == INTEGRATE_FUSED) {
         // the group's lanes take the same pebbles in both halves, and lane 0
         // re-reads the clump state it wrote: each reads its own writes
-        clumpIntegrateGroup(d, half, 0, width, t, true);
-        clumpIntegrateGroup(d, half, 1, width, t);
+        clumpIntegrateGroup(d, half, 0, width, t, stale, true);
+        clumpIntegrateGroup(d, half, 1, width, t, stale);
     } else {
-        clumpIntegrateGroup(d, half, MODE == INTEGRATE_BEFORE ? 1 : 0, width, t);
+        clumpIntegrateGroup(d, half, MODE == INTEGRATE_BEFORE ? 1 : 0, width, t, stale);
     }
 }
 
@@ -817,7 +907,13 @@ void launchBonds(const DeviceState& d, int par, float dt, cudaStream_t s)
 void launchSolidForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    launchStep(kSolidForces, blocksFor(d.nrow, d.forceRows * (T / 32)), T, s, d, par, dt, d.nf > 0 ? 1 : 0);
+    launchStep(kSolidForces<false>, blocksFor(d.nrow, d.forceRows * (T / 32)), T, s, d, par, dt, d.nf > 0 ? 1 : 0,
+               d.forceRows);
+}
+void launchContactForces(const DeviceState& d, int par, float dt, cudaStream_t s)
+{
+    if (d.nrow <= 0) return;
+    launchStep(kSolidForces<true>, blocksFor(d.nrow, T), T, s, d, par, dt, d.nf > 0 ? 1 : 0, 32);
 }
 void launchClumpForce(const DeviceState& d, cudaStream_t s)
 {
@@ -825,7 +921,7 @@ void launchClumpForce(const DeviceState& d, cudaStream_t s)
     const int w = d.clumpLanes;
     launchStep(kClumpForce, blocksFor((long long)d.nc * w, 256), 256, s, d, w);
 }
-void launchSolidIntegrate(const DeviceState& d, double dt, int mode, bool clumpForce, bool countStep,
+void launchSolidIntegrate(const DeviceState& d, double dt, int mode, int par, bool clumpForce, bool countStep,
                           cudaStream_t s)
 {
     const dfl h = df_from_double(0.5 * dt);
@@ -834,11 +930,11 @@ void launchSolidIntegrate(const DeviceState& d, double dt, int mode, bool clumpF
     if (sb + cb == 0 && !countStep) return;
     const int blocks = std::max(1, sb + cb), cf = clumpForce ? 1 : 0, cs = countStep ? 1 : 0;
     if (mode == INTEGRATE_FUSED)
-        launchStep(kIntegrate<INTEGRATE_FUSED>, blocks, 256, s, d, h, d.clumpLanes, cb, cf, cs);
+        launchStep(kIntegrate<INTEGRATE_FUSED>, blocks, 256, s, d, h, d.clumpLanes, cb, cf, cs, par);
     else if (mode == INTEGRATE_BEFORE)
-        launchStep(kIntegrate<INTEGRATE_BEFORE>, blocks, 256, s, d, h, d.clumpLanes, cb, cf, cs);
+        launchStep(kIntegrate<INTEGRATE_BEFORE>, blocks, 256, s, d, h, d.clumpLanes, cb, cf, cs, par);
     else
-        launchStep(kIntegrate<INTEGRATE_AFTER>, blocks, 256, s, d, h, d.clumpLanes, cb, cf, cs);
+        launchStep(kIntegrate<INTEGRATE_AFTER>, blocks, 256, s, d, h, d.clumpLanes, cb, cf, cs, par);
 }
 
 

@@ -168,7 +168,7 @@ void allocContactLists(demsph_engine* e)
     for (int p = 0; p < 2; ++p) d.fwd[p] = dalloc<int>(c, e->owned, e->stream);
     for (int k = 0; k < 3; ++k) {
         d.springIn[k] = dalloc<float4>(c, e->owned, e->stream);
-        d.springOut[k] = dalloc<float4>(c, e->owned, e->stream);
+        for (int p = 0; p < 2; ++p) d.springOut[p][k] = dalloc<float4>(c, e->owned, e->stream);
     }
 }
 
@@ -196,8 +196,11 @@ struct StageTimer {
 // ---- the five stages ----
 // endView: the solids' integration has already opened this step (a fused
 // pass): the search reads their end-of-step offsets from sphE/splE.
-void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = false)
+// detect false: the contact list is left to the contact stage's one launch
+// (launchContactForces).
+void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = false, bool detect = true)
 {
+    const int npar = e->par ^ 1;  // the parity of the list this step builds
     DeviceState d = e->d;
     if (endView) {
         d.sph = d.sphE;
@@ -221,8 +224,8 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = fa
     }
     if (solidsMove || e->forceWalk) {
         TIMED("solid_hash_sort");
-        launchSolidHash(d, forceSort, fluidStep, s);
-        launchSolidSort(d, forceSort, fluidStep, s);
+        launchSolidHash(d, forceSort, fluidStep, npar, s);
+        launchSolidSort(d, forceSort, fluidStep, npar, s);
         e->solidSortStale = false;
     }
     if (fluidStep) {
@@ -244,8 +247,9 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = fa
             launchCouplingLists(d, s);
         }
     }
-    e->par ^= 1;
+    e->par = npar;
     e->walkOrder[e->par] = e->forceWalk;
+    if (!detect) return;
     TIMED("solid_contact_list");  // with the candidate rebuild when they are stale
     launchContactDetect(d, e->par, e->forceWalk, s);
 }
@@ -253,7 +257,7 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = fa
 void stageBefore(demsph_engine* e, double dt)
 {
     TIMED("integrate_before");
-    launchSolidIntegrate(e->d, dt, INTEGRATE_BEFORE, false, false, e->stream);
+    launchSolidIntegrate(e->d, dt, INTEGRATE_BEFORE, e->par, false, false, e->stream);
 }
 
 void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
@@ -309,7 +313,7 @@ void stageContact(demsph_engine* e, double dt, bool withClumpForce = true)
 void stageAfter(demsph_engine* e, double dt, bool clumpForce = false, bool countStep = false)
 {
     TIMED("integrate_after");
-    launchSolidIntegrate(e->d, dt, INTEGRATE_AFTER, clumpForce, countStep, e->stream);
+    launchSolidIntegrate(e->d, dt, INTEGRATE_AFTER, e->par, clumpForce, countStep, e->stream);
 }
 
 // One solverBase::update() without the driver's hook.  The clump force sum
@@ -333,9 +337,13 @@ void fullStep(demsph_engine* e, double dt, int iStep, int gap, bool opened = fal
 // depends on nothing the search writes.  So the state after every step is
 // bit for bit that of fullStep.  The solids no integration moves (dummy
 // particles at rest) get their sphE/splE copy once, after the first search.
+// Without bonds (kBonds reads the contact list) the opened steps build their
+// contact list in the contact stage, in the launch of the contact forces: the
+// fluid stage of a plain DEM step (the coupling force) does not read it.
 void fusedSteps(demsph_engine* e, double dt, int iStep, int length, int gap)
 {
     DeviceState& d = e->d;
+    const bool merge = e->mergeContacts && d.nb == 0 && d.nrow > 0;
     stageNeighborSearch(e, iStep, gap);
     const long long pebbles = std::count(e->moveKind.begin(), e->moveKind.end(), (unsigned char)0);
     if (d.ns - d.nmove - pebbles > 0) {
@@ -345,13 +353,13 @@ void fusedSteps(demsph_engine* e, double dt, int iStep, int length, int gap)
     stageBefore(e, dt);
     for (int k = 0; k < length; ++k) {
         stageFluid(e, dt, iStep + k, gap);
-        stageContact(e, dt, false);
+        if (k > 0 && merge)
+            launchContactForces(d, e->par, (float)dt, e->stream);
+        else
+            stageContact(e, dt, false);
         if (k == length - 1) break;
-        {
-            TIMED("integrate_after");
-            launchSolidIntegrate(d, dt, INTEGRATE_FUSED, d.nc > 0, true, e->stream);
-        }
-        stageNeighborSearch(e, iStep + k + 1, gap, true);
+        launchSolidIntegrate(d, dt, INTEGRATE_FUSED, e->par, d.nc > 0, true, e->stream);
+        stageNeighborSearch(e, iStep + k + 1, gap, true, !merge);
     }
     stageAfter(e, dt, d.nc > 0, true);
 }
@@ -389,16 +397,18 @@ void grow(demsph_engine* e, int status)
             const int keep = e->par;
             const size_t old = (size_t)d.scap * nr;
             int* keepFwd = d.fwd[keep];
-            float4* keepSpring[3] = {d.springOut[0], d.springOut[1], d.springOut[2]};
+            float4* keepSpring[3] = {d.springOut[keep][0], d.springOut[keep][1], d.springOut[keep][2]};
             d.fwd[keep] = nullptr;
-            for (int k = 0; k < 3; ++k) d.springOut[k] = nullptr;
-            void* ptrs[] = {d.rev, d.pF, d.pT, d.fwd[keep ^ 1], d.springIn[0], d.springIn[1], d.springIn[2]};
+            for (int k = 0; k < 3; ++k) d.springOut[keep][k] = nullptr;
+            void* ptrs[] = {d.rev, d.pF, d.pT, d.fwd[keep ^ 1], d.springIn[0], d.springIn[1], d.springIn[2],
+                            d.springOut[keep ^ 1][0], d.springOut[keep ^ 1][1], d.springOut[keep ^ 1][2]};
             for (void* p : ptrs) freeOne(e, p);
             d.scap = std::max(d.scap * 2, need[0] + need[0] / 2 + 1);
             allocContactLists(e);
             CK(cudaMemcpyAsync(d.fwd[keep], keepFwd, sizeof(int) * old, cudaMemcpyDeviceToDevice, e->stream));
             for (int k = 0; k < 3; ++k)
-                CK(cudaMemcpyAsync(d.springOut[k], keepSpring[k], sizeof(float4) * old, cudaMemcpyDeviceToDevice, e->stream));
+                CK(cudaMemcpyAsync(d.springOut[keep][k], keepSpring[k], sizeof(float4) * old,
+                                   cudaMemcpyDeviceToDevice, e->stream));
             void* olds[] = {keepFwd, keepSpring[0], keepSpring[1], keepSpring[2]};
             for (void* p : olds) freeOne(e, p);
         }
@@ -407,7 +417,7 @@ void grow(demsph_engine* e, int status)
             freeOne(e, p);
             d.vcap = std::max(d.vcap * 2, need[1] + need[1] / 2 + 1);
             d.vcand = dalloc<int>((size_t)d.vcap * nr, e->owned, e->stream, false);
-            CK(cudaMemsetAsync(d.rebuild, 0xff, sizeof(int), e->stream));  // rebuild on the retry
+            CK(cudaMemsetAsync(d.rebuild, 0xff, 2 * sizeof(int), e->stream));  // rebuild on the retry
         }
     }
     if (status & ST_FVERLET_OVERFLOW) {
@@ -433,6 +443,7 @@ void grow(demsph_engine* e, int status)
         d.coupCap = (int)std::min<long long>(2000000000LL, (long long)(need * 1.5) + 1024);
         d.coupList = dalloc<int>(d.coupCap, e->owned, e->stream);
     }
+    if (status & ST_SPLIT_CONTACTS) e->mergeContacts = false;  // the lists come from the walk from now on
     if (status & ST_MODE_CHANGE) {
         // the abandoned step may have counted some particles into cells
         CK(cudaMemsetAsync(d.scellCount, 0, sizeof(int) * d.grid.num, e->stream));
@@ -443,7 +454,7 @@ void grow(demsph_engine* e, int status)
 }
 
 constexpr int ALL_OVERFLOWS = ST_FF_OVERFLOW | ST_FS_OVERFLOW | ST_SS_OVERFLOW | ST_COUPLE_OVERFLOW |
-                              ST_VERLET_OVERFLOW | ST_MODE_CHANGE | ST_FVERLET_OVERFLOW;
+                              ST_VERLET_OVERFLOW | ST_MODE_CHANGE | ST_FVERLET_OVERFLOW | ST_SPLIT_CONTACTS;
 
 // Neighbour search of the staged API: synchronises once, grows and retries.
 int neighborSearchChecked(demsph_engine* e, int iStep, int gap)
@@ -793,7 +804,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.vcnt = dalloc<int>(nr, e->owned, e->stream);
             d.vref = dalloc<float4>(ns, e->owned, e->stream);
             d.svref = dalloc<float4>(ns, e->owned, e->stream);
-            d.rebuild = dalloc<int>(1, e->owned, e->stream);
+            d.rebuild = dalloc<int>(2, e->owned, e->stream);
             d.slowMode = dalloc<int>(1, e->owned, e->stream);
             d.need = dalloc<int>(4, e->owned, e->stream);
             d.rowStats = dalloc<int>(3, e->owned, e->stream);
@@ -815,7 +826,12 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             e->adaptRows = o.contact_rows_per_warp == 0;
             const int one = 1;
             const bool walkOnly = o.solid_verlet_skin < 0 || d.grid.gx < 3 || d.grid.gy < 3 || d.grid.gz < 3;
-            CK(cudaMemcpyAsync(d.rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+            {
+                const char* v = std::getenv("DEMSPH_MERGE_CONTACTS");
+                e->mergeContacts = !(v && v[0] == '0') && !walkOnly;
+            }
+            const int both[2] = {1, 1};
+            CK(cudaMemcpyAsync(d.rebuild, both, sizeof(both), cudaMemcpyHostToDevice, e->stream));
             if (walkOnly) CK(cudaMemcpyAsync(d.slowMode, &one, sizeof(int), cudaMemcpyHostToDevice, e->stream));
             d.coupCount = dalloc<int>(ns, e->owned, e->stream);
             d.coupStart = dalloc<int>((size_t)ns + 1, e->owned, e->stream);
@@ -856,8 +872,10 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.wnl = dalloc<float4>(nw, e->owned, e->stream);
             d.wP = dalloc<float2>(nw, e->owned, e->stream);
             d.wmat = dalloc<int>(nw, e->owned, e->stream);
-            for (int k = 0; k < 3; ++k) d.wspring[k] = dalloc<float4>((size_t)ns * nw, e->owned, e->stream);
-            d.wmask = dalloc<unsigned>(ns, e->owned, e->stream);
+            for (int p = 0; p < 2; ++p) {
+                for (int k = 0; k < 3; ++k) d.wspring[p][k] = dalloc<float4>((size_t)ns * nw, e->owned, e->stream);
+                d.wmask[p] = dalloc<unsigned>(ns, e->owned, e->stream);
+            }
             if (nw > 0) {
                 CK(cudaMemcpyAsync(d.wnh, nh.data(), sizeof(float4) * nw, cudaMemcpyHostToDevice, e->stream));
                 CK(cudaMemcpyAsync(d.wnl, nl.data(), sizeof(float4) * nw, cudaMemcpyHostToDevice, e->stream));
@@ -1237,10 +1255,11 @@ static int runUpdate(demsph_engine* e, double dt, int first_step, int n_steps, i
         if (st & ~ALL_OVERFLOWS) return fail(e, DEMSPH_ERR_STATE, "unexpected device status " + std::to_string(st));
         step += done;                        // steps before the failed one completed
         e->par = startPar ^ (done & 1);      // every step builds one contact list
-        // every overflow is raised in a neighbour search; in a fused graph the
-        // search of a step other than its first runs after the pass that
-        // opened that step (and a resumed step stays opened when its own
-        // search overflows again)
+        // every overflow is raised in a neighbour search or the contact list
+        // of the contact stage; in a fused graph both run, for every step but
+        // the first, after the pass that opened that step (and a resumed step
+        // stays opened when its own search overflows again).  Nothing else of
+        // a plain DEM step before the contact stage changes state.
         e->resumeOpened = done == 0 && startOpened;
         for (const auto& r : fusedRuns)
             if (step > r.first && step < r.first + r.second) e->resumeOpened = true;

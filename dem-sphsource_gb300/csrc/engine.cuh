@@ -26,6 +26,7 @@ enum StatusBits : int {
     ST_MODE_CHANGE = 32,     // a particle left the domain: lists switch to the 27-cell walk; redo the step
     ST_FVERLET_OVERFLOW = 64,// a fluid particle has more list candidates than it holds
     ST_BARRIER_TIMEOUT = 128,// a grid barrier of a cooperative launch gave up waiting (an error)
+    ST_SPLIT_CONTACTS = 256, // the one-launch contact list + forces met the walk mode: redo the step in two
 };
 
 // Neighbour list entries.  A fluid partner entry holds the partner's slot j,

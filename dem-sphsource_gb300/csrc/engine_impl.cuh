@@ -10,8 +10,6 @@
 
 namespace demsph {
 
-enum SolidFlagBits { F_DUMMY = 1, F_FIXED = 2, F_MASSIVE = 4, F_HASMASS = 8 };
-
 struct CudaError {
     cudaError_t e;
     const char* what;
@@ -75,6 +73,11 @@ struct demsph_engine {
     // Graphs of two or more plain DEM steps integrate the end of one step and
     // the start of the next in one pass (DEMSPH_FUSE_INTEGRATION=0 keeps two).
     bool fuseIntegration = true;
+    // In those graphs the steps a fused pass opens build their contact list
+    // and contact forces in one launch when the scene has no bonds and the
+    // lists come from candidates (DEMSPH_MERGE_CONTACTS=0 keeps two launches;
+    // off for good once the lists come from the walk).
+    bool mergeContacts = true;
     // The step the next attempt starts with already had its before-contact
     // half applied (a fused pass ran before its neighbour search overflowed).
     bool resumeOpened = false;

@@ -120,7 +120,7 @@ __global__ void kFluidIn(DeviceState d, const double* pos, const double* vel, co
     if (drho) d.fdrho[0][s] = (float)drho[id];
 }
 
-__global__ void kSolidIn(DeviceState d, const double* pos, const double* vel, const double* w)
+__global__ void kSolidIn(DeviceState d, const double* pos, const double* vel, const double* w, int* stale)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.ns) return;
@@ -133,7 +133,7 @@ __global__ void kSolidIn(DeviceState d, const double* pos, const double* vel, co
         d.sph[i] = make_float4(x.hi, y.hi, z.hi, h.w);
         d.spl[i] = make_float4(x.lo, y.lo, z.lo, l.w);
         // new key; candidates stale only if the solid moved half a margin
-        checkDisplacement(d, i);
+        checkDisplacement(d, stale, i);
         rehashSolid(d, i);
     }
     if (vel) {
@@ -385,7 +385,8 @@ void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel,
     if (dp) CK(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     if (dw) CK(cudaMemcpyAsync(dw, angvel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
-    ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw);
+    // the flag of the step that follows (its list takes the other parity)
+    ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw, d.rebuild + (e->par ^ 1));
     // solids that never move are otherwise sorted only once
     if (dp && e->nMassive == 0) e->solidSortStale = true;
 }
@@ -717,9 +718,9 @@ int demsph_export_solid_pairs(demsph_engine* e, int* prefix, int* pointed, int* 
     const size_t all = (size_t)C * nr;
     if (force) d2h(F, d.pF, all);
     if (torque) d2h(T, d.pT, all);
-    if (sliding) d2h(S0, d.springOut[0], all);
-    if (rolling) d2h(S1, d.springOut[1], all);
-    if (torsion) d2h(S2, d.springOut[2], all);
+    if (sliding) d2h(S0, d.springOut[par][0], all);
+    if (rolling) d2h(S1, d.springOut[par][1], all);
+    if (torsion) d2h(S2, d.springOut[par][2], all);
     // the reference adds each bond's force and torque onto its pair's
     // (integrate.cu:802-803); the engine keeps them per bond
     if ((force || torque) && d.nb > 0) {

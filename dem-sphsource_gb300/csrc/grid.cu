@@ -339,11 +339,11 @@ void launchFluidReorder(const DeviceState& d, bool force, cudaStream_t s)
     launchStep(kFluidGather, blocksFor(d.nf, T), T, s, d, when);
 }
 
-static RunIf solidSortWhen(const DeviceState& d, bool force, bool fluidStep)
+static RunIf solidSortWhen(const DeviceState& d, bool force, bool fluidStep, int par)
 {
     RunIf when;
     when.always = force ? 1 : 0;
-    when.a = d.rebuild;
+    when.a = d.rebuild + par;
     when.b = d.slowMode;
     if (fluidStep) {
         when.c = d.frebuild;
@@ -352,26 +352,27 @@ static RunIf solidSortWhen(const DeviceState& d, bool force, bool fluidStep)
     return when;
 }
 
-void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s)
+void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, int par, cudaStream_t s)
 {
     if (d.ns <= 0) return;
     if (force)  // positions that no integration has hashed (creation, an upload)
-        launchStep(kSolidHash, blocksFor(d.ns, T), T, s, d, solidSortWhen(d, true, fluidStep));
+        launchStep(kSolidHash, blocksFor(d.ns, T), T, s, d, solidSortWhen(d, true, fluidStep, par));
     else if (d.sortBlocks <= 0)  // keys come from the last integration of the previous step
-        launchStep(kSolidSlots, blocksFor(d.ns, T), T, s, d, solidSortWhen(d, false, fluidStep));
+        launchStep(kSolidSlots, blocksFor(d.ns, T), T, s, d, solidSortWhen(d, false, fluidStep, par));
 }
 
-void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s)
+void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, int par, cudaStream_t s)
 {
     if (d.ns <= 0) return;
     if (!force && d.sortBlocks > 0) {
         // the slots were not taken by launchSolidHash: the cooperative launch does everything
-        launchCooperative(kSolidSortCoop, (unsigned)d.sortBlocks, SORT_THREADS, s, d, solidSortWhen(d, false, fluidStep));
+        launchCooperative(kSolidSortCoop, (unsigned)d.sortBlocks, SORT_THREADS, s, d,
+                          solidSortWhen(d, false, fluidStep, par));
         return;
     }
     // scellCount is zero here: cleared at creation, by kSolidRank after every
     // sort, and by the host after a step abandoned in kSolidHash
-    const RunIf when = solidSortWhen(d, force, fluidStep);
+    const RunIf when = solidSortWhen(d, force, fluidStep, par);
     scanExclusive(d.scellCount, d.scellStart, d.grid.num, d.scanWork, s, when);
     launchStep(kScatter, blocksFor(d.ns, T), T, s, d.ns, d.skey, d.sslotInCell, d.scellStart, d.ssortTmp, d.status, when);
     launchStep(kSolidRank, blocksFor(d.ns, T), T, s, d, when);

@@ -8,6 +8,10 @@
 
 namespace demsph {
 
+// Bits of a solid's flags word (sflags .w): a dummy wall particle, a solid
+// with zero inverse mass (fixed), one with mass above 1e-10, one with any mass.
+enum SolidFlagBits { F_DUMMY = 1, F_FIXED = 2, F_MASSIVE = 4, F_HASMASS = 8 };
+
 // Kernel launches issued by this thread (every launch site increments it);
 // the engine turns deltas of it into the launch count of a run.
 inline thread_local long long t_kernelLaunches = 0;
@@ -251,9 +255,11 @@ struct DeviceState {
     int* rev;                // partner id A of each reverse slot
     int* rcnt;
     // sliding, rolling, torsion springs per forward slot: as remapped from the
-    // previous list (In) and after this step's contact forces (Out)
+    // previous list (In) and after the contact forces of the step whose list
+    // has parity p (Out[p]); a step reads only the other parity's Out, so a
+    // step abandoned after an overflow leaves the history it started from
     float4* springIn[3];
-    float4* springOut[3];
+    float4* springOut[2][3];
     float4* pF;              // pair contact force on A, as the reference stores it (exports)
     float4* pT;              // pair contact torque (rolling + torsion), as the reference stores it (exports)
     // Verlet candidates: partners within cut + skin at the last rebuild, by id
@@ -264,7 +270,8 @@ struct DeviceState {
                              // grid origin) at the last rebuild
     float skin;              // candidate margin; a rebuild follows once a solid moved skin / 2
     float vmaxEff;           // largest effective radius of a non-dummy solid
-    int* rebuild;            // 1: candidates are stale; set by the last drift, cleared by kSolidForces
+    int* rebuild;            // [p] 1: the candidates are stale for the step whose list has parity p;
+                             // set by the drift that ends the step before, cleared after the step
     int* slowMode;           // 1: lists come from the 27-cell walk every step (grid too small, or a solid left the domain)
     int* need;               // [0] most contacts of a row, [1] most candidates of a row,
                              // [2] / [3] most fluid / solid candidates of a fluid particle (for growing)
@@ -282,8 +289,10 @@ struct DeviceState {
     float4* wnl;             // normal lo
     float2* wP;              // (p - min) . n, double-float
     int* wmat;
-    float4* wspring[3];      // [k * ns + a]: wall k, solid a
-    unsigned* wmask;         // per solid: bit k (k < 32) set while the springs of wall k may be non-zero
+    // wall springs after the contact phase of the step whose list has parity
+    // p (the step reads the other parity): [p][j][k * ns + a], wall k, solid a
+    float4* wspring[2][3];
+    unsigned* wmask[2];      // [p] per solid: bit k (k < 32) set while the springs of wall k may be non-zero
 
     // ---- bonds ----
     int nb;
@@ -387,8 +396,9 @@ void launchFluidReorder(const DeviceState& d, bool force, cudaStream_t s);
 // (launchSolidSort) only when `force`, when the contact candidates are stale,
 // when lists come from the 27-cell walk, or - on fluid steps (fluidStep) -
 // when the fluid lists walk the cells.
-void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s);
-void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, cudaStream_t s);
+// par: the parity of the contact list the step builds (its rebuild flag).
+void launchSolidHash(const DeviceState& d, bool force, bool fluidStep, int par, cudaStream_t s);
+void launchSolidSort(const DeviceState& d, bool force, bool fluidStep, int par, cudaStream_t s);
 // Blocks of the one-launch cooperative sort on this device (0 when it cannot
 // be used); DEMSPH_COOPERATIVE_SORT=0 in the environment keeps the four-launch
 // sort.
@@ -429,6 +439,13 @@ void launchCouplingPairForces(const DeviceState& d, int src, float4* out, cudaSt
 void launchBonds(const DeviceState& d, int parity, float dt, cudaStream_t s);
 // Contact, bond, wall, coupling and gravity forces of every solid.
 void launchSolidForces(const DeviceState& d, int parity, float dt, cudaStream_t s);
+// The contact list of a plain DEM step opened by a fused integration pass and
+// its contact forces in one launch (no bonds; candidates, not the walk):
+// each row filters its candidates on the end-of-step offsets (sphE/splE) and
+// the contact forces then act at the midpoint (sph/spl), springs remapped by
+// both sides of a pair from the previous list.  Raises ST_SPLIT_CONTACTS,
+// before any write, when the lists must come from the walk.
+void launchContactForces(const DeviceState& d, int parity, float dt, cudaStream_t s);
 void launchClumpForce(const DeviceState& d, cudaStream_t s);
 // Kinds of solid integration pass: the half step after the contact forces
 // (closing a step), the half step before them (opening one), or both in one
@@ -438,7 +455,9 @@ void launchClumpForce(const DeviceState& d, cudaStream_t s);
 enum IntegrateMode { INTEGRATE_AFTER = 0, INTEGRATE_BEFORE = 1, INTEGRATE_FUSED = 2 };
 // Half-step integration of all solids; clumpForce: sum the clumps' pebble
 // forces first (instead of launchClumpForce); countStep: count the step.
-void launchSolidIntegrate(const DeviceState& d, double dt, int mode, bool clumpForce, bool countStep,
+// par: the parity of the contact list of the step a closing half ends (its
+// margin check raises d.rebuild[par ^ 1], the next step's flag).
+void launchSolidIntegrate(const DeviceState& d, double dt, int mode, int par, bool clumpForce, bool countStep,
                           cudaStream_t s);
 
 // Absolute FP64 position of solid i (cell origin + double-float offset).
@@ -458,16 +477,17 @@ __device__ __forceinline__ int solidOf(const DeviceState& d, int r) { return d.r
 
 // After the last drift of a step: once a solid that can touch others (row >=
 // 0) has moved half the candidate margin since the candidates were built, the
-// next step rebuilds them.  c, h: its cell and offset after the drift; p0, q0:
-// vref and svref of the solid.
-__device__ __forceinline__ void checkDisplacementOf(const DeviceState& d, int row, int4 c, float4 h, float4 p0,
-                                                    float4 q0)
+// next step rebuilds them (stale: that step's flag, d.rebuild[next parity]).
+// c, h: its cell and offset after the drift; p0, q0: vref and svref of the
+// solid.
+__device__ __forceinline__ void checkDisplacementOf(const DeviceState& d, int* stale, int row, int4 c, float4 h,
+                                                    float4 p0, float4 q0)
 {
     if (row < 0) return;
     const float dx = (float)c.x * d.grid.cs.x + h.x - p0.x, dy = (float)c.y * d.grid.cs.y + h.y - p0.y,
                 dz = (float)c.z * d.grid.cs.z + h.z - p0.z;
     const float half = 0.5f * d.skin;
-    if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)d.rebuild = 1;
+    if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)stale = 1;
     if (d.nf > 0) {  // the fluid candidates' solid partners
         const float ex = (float)c.x * d.grid.cs.x + h.x - q0.x, ey = (float)c.y * d.grid.cs.y + h.y - q0.y,
                     ez = (float)c.z * d.grid.cs.z + h.z - q0.z;
@@ -475,11 +495,12 @@ __device__ __forceinline__ void checkDisplacementOf(const DeviceState& d, int ro
         if (!(ex * ex + ey * ey + ez * ez <= fh * fh)) *(volatile int*)d.frebuild = 1;
     }
 }
-__device__ __forceinline__ void checkDisplacement(const DeviceState& d, int i)
+__device__ __forceinline__ void checkDisplacement(const DeviceState& d, int* stale, int i)
 {
     const int r = rowOf(d, i);
     if (r < 0) return;
-    checkDisplacementOf(d, r, d.scell[i], d.sph[i], d.vref[i], d.nf > 0 ? d.svref[i] : make_float4(0, 0, 0, 0));
+    checkDisplacementOf(d, stale, r, d.scell[i], d.sph[i], d.vref[i],
+                        d.nf > 0 ? d.svref[i] : make_float4(0, 0, 0, 0));
 }
 
 // Cell key of solid i for the next step's neighbour search, at the end of

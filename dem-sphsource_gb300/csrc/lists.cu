@@ -20,6 +20,7 @@
 //     looking the pair (A, B) up in A's previous forward segment, which holds
 //     the same springs the reference finds through B's reverse span.
 #include "kernels.cuh"
+#include "contact_rows.cuh"
 
 namespace demsph {
 
@@ -27,7 +28,6 @@ namespace {
 
 constexpr int T = 128;
 
-enum FlagBits { F_DUMMY = 1, F_FIXED = 2, F_MASSIVE = 4, F_HASMASS = 8 };  // see engine.cu
 
 __device__ __forceinline__ unsigned deltaCode(int dx, int dy, int dz)
 {
@@ -36,21 +36,6 @@ __device__ __forceinline__ unsigned deltaCode(int dx, int dy, int dz)
 }
 
 __device__ __forceinline__ dfl dfMax(dfl a, dfl b) { return (a.hi > b.hi || (a.hi == b.hi && a.lo >= b.lo)) ? a : b; }
-
-// |x_a - x_b| <= cut (cut in double-float): FP32 decision outside a 1e-5
-// relative band, double-float inside it.
-__device__ __forceinline__ bool withinCut(int4 ca, float4 ha, float4 la, int4 cb, float4 hb, const float4* lbPtr,
-                                          int jb, dfl cut, const GridDev& g)
-{
-    const float3 r = relF(ca, ha, cb, hb, g);
-    const float d2 = dot3(r, r);
-    const float c2 = cut.hi * cut.hi;
-    if (d2 > c2 * (1.f + 1.e-5f)) return false;
-    if (d2 < c2 * (1.f - 1.e-5f)) return true;
-    const float4 lb = lbPtr[jb];
-    const dfl dist = dfNorm(relDF(ca, ha, la, cb, hb, lb, g));
-    return df_ge0(df_sub(cut, dist));
-}
 
 // Stencil walk shared by all list builders: calls f(hash, regular, hx, hy, hz)
 // for the 27 cells around the (truncated) cell of a point, in the reference's
@@ -495,92 +480,6 @@ __global__ void kCoupSort(DeviceState d)
 }
 
 // ---- solid contact lists ----
-// Filters of core/neighborSearch.cu:246-263 for candidate b of particle a.
-__device__ __forceinline__ bool solidPairCandidate(const DeviceState& d, int a, int4 fa, int b)
-{
-    if (b == a) return false;
-    const int4 fb = d.sflags[b];
-    if (fb.w & F_DUMMY) return false;
-    if (fa.z >= 0 && fa.z == fb.z) return false;           // same clump
-    if ((fa.w & F_FIXED) && (fb.w & F_FIXED)) return false;  // both fixed
-    return true;
-}
-
-// The reference's contact test |x_a - x_b| <= eff_a + eff_b
-// (core/neighborSearch.cu:264-270), always evaluated with the lower index
-// first, so that the rows of both solids reach the same decision bit for bit.
-__device__ __forceinline__ bool solidsTouch(const DeviceState& d, int a, int b)
-{
-    const int lo = a < b ? a : b, hi = a < b ? b : a;
-    const float4 rl = d.srad[lo], rh = d.srad[hi];
-    const dfl cut = df_add(df_make(rl.z, rl.w), df_make(rh.z, rh.w));
-    return withinCut(d.scell[lo], d.sph[lo], d.spl[lo], d.scell[hi], d.sph[hi], d.spl, hi, cut, d.grid);
-}
-
-// Insertion sort of the n slots [k * nrow + r] of one row (n is small).
-__device__ __forceinline__ void sortSlots(int* v, int r, int nrow, int n)
-{
-    const size_t nr = (size_t)nrow;
-    for (int k = 1; k < n; ++k) {
-        const int x = v[(size_t)k * nr + r];
-        int q = k - 1;
-        while (q >= 0 && v[(size_t)q * nr + r] > x) {
-            v[(size_t)(q + 1) * nr + r] = v[(size_t)q * nr + r];
-            --q;
-        }
-        v[(size_t)(q + 1) * nr + r] = x;
-    }
-}
-
-__device__ __forceinline__ float3 gridPos(int4 c, float4 h, const GridDev& g)
-{
-    return make_float3((float)c.x * g.cs.x + h.x, (float)c.y * g.cs.y + h.y, (float)c.z * g.cs.z + h.z);
-}
-
-// Verlet candidates of one row: every solid passing the reference's filters
-// within eff_a + eff_b + skin, found in the cells that box overlaps.  Runs only
-// on steps where the hash found a solid displaced by more than skin / 2 since
-// the last rebuild (so every pair within eff_a + eff_b now was within
-// eff_a + eff_b + skin then).  All non-dummy solids are inside the domain
-// here (otherwise the lists come from the 27-cell walk), so the cells are
-// plain (x, y, z) cells.
-__device__ __forceinline__ void verletBuildRow(const DeviceState& d, int r)
-{
-    const int a = solidOf(d, r);
-    const int4 fa = d.sflags[a];
-    const int4 ca = d.scell[a];
-    const float4 ha = d.sph[a];
-    const float effA = d.srad[a].z;
-    const float reach = effA + d.vmaxEff + d.skin;
-    const GridDev& g = d.grid;
-    const int x0 = max(0, ca.x + (int)floorf((ha.x - reach) / g.cs.x)), x1 = min(g.gx - 1, ca.x + (int)floorf((ha.x + reach) / g.cs.x));
-    const int y0 = max(0, ca.y + (int)floorf((ha.y - reach) / g.cs.y)), y1 = min(g.gy - 1, ca.y + (int)floorf((ha.y + reach) / g.cs.y));
-    const int z0 = max(0, ca.z + (int)floorf((ha.z - reach) / g.cs.z)), z1 = min(g.gz - 1, ca.z + (int)floorf((ha.z + reach) / g.cs.z));
-    int n = 0;
-    for (int z = z0; z <= z1; ++z)
-        for (int y = y0; y <= y1; ++y)
-            for (int x = x0; x <= x1; ++x) {
-                const int hash = (z * g.gy + y) * g.gx + x;
-                for (int p = d.scellStart[hash], pe = d.scellStart[hash + 1]; p < pe; ++p) {
-                    const int b = d.ssorted[p];
-                    if (!solidPairCandidate(d, a, fa, b)) continue;
-                    const float3 rr = relF(ca, ha, make_int4(x, y, z, hash), d.sph[b], g);
-                    const float c = (effA + d.srad[b].z + d.skin) * 1.0001f;
-                    if (dot3(rr, rr) > c * c) continue;
-                    if (n < d.vcap) d.vcand[(size_t)n * d.nrow + r] = b;
-                    ++n;
-                }
-            }
-    // by index: the contact list filtered from them is then in index order
-    sortSlots(d.vcand, r, d.nrow, min(n, d.vcap));
-    d.vcnt[r] = n;
-    d.vref[a] = f4(gridPos(ca, ha, g));
-    if (n > d.vcap) {
-        atomicOr(d.status, ST_VERLET_OVERFLOW);
-        atomicMax(&d.need[1], n);
-    }
-}
-
 // One row's contacts of this step (setSolid2SolidInteractionsKernel,
 // core/neighborSearch.cu:222-312): the partners that pass the reference's
 // test, either from the Verlet candidates or - for grids under 3 cells on an
@@ -601,7 +500,7 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
     const bool walk = forceWalk || *d.slowMode;
     // stale candidates are rebuilt first, row by row (the contact force
     // kernel clears the flag once every row has read it)
-    if (!walk && *d.rebuild) verletBuildRow(d, r);
+    if (!walk && d.rebuild[par]) verletBuildRow(d, r);
     const int a = solidOf(d, r);
     const int4 fa = d.sflags[a];
     const int prev = par ^ 1;
@@ -652,9 +551,9 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
         for (int k = 0; k < prevCnt; ++k) {
             const size_t ps = (size_t)k * nr + r;
             if (d.fwd[prev][ps] == b) {
-                s0 = d.springOut[0][ps];
-                s1 = d.springOut[1][ps];
-                s2 = d.springOut[2][ps];
+                s0 = d.springOut[prev][0][ps];
+                s1 = d.springOut[prev][1][ps];
+                s2 = d.springOut[prev][2][ps];
                 break;
             }
         }

@@ -440,12 +440,14 @@ def tiny_two_fluids(seed=6):
     return r
 
 
-def tiny_escape(seed=5):
+def tiny_escape(seed=5, with_probe_fluid=True):
     """64 spheres on a floor wall (no side walls) and two touching spheres
     above the domain: the reference hashes those to its overflow cell
     (core/neighborSearch.h:44-53) and finds their contact only because that
     cell's key is one of the keys its 27-cell walk visits from the corner cell
-    below them, so the lists must come from that walk."""
+    below them, so the lists must come from that walk.  The probe fluid
+    particle is there for the reference's wall normals (see
+    :func:`tiny_granular`)."""
     r = granular_settle(n_spheres=64, n_clumps=0, box=(0.01, 0.01), spacing=2.3e-3, steps=50, seed=seed,
                         z0=1.0e-3, velocity=(0.05, -0.03, -0.2), name="tiny_escape")
     r.calls = [c for c in r.calls if not (c[0] == "addInfiniteWall" and tuple(c[1][1]) != (0.0, 0.0, 1.0))]
@@ -453,8 +455,9 @@ def tiny_escape(seed=5):
     top = o[2] + sz[2]
     p = np.array([[o[0] + 1.0e-3, o[1] + 1.0e-3, top + 0.9e-3], [o[0] + 2.4e-3, o[1] + 1.0e-3, top + 0.9e-3]])
     r.addSolid(p, (0, 0, -0.3), 8.0e-4, 2500.0, 0)
-    r.addFluid(np.array([[o[0] + sz[0] - 1e-3, o[1] + sz[1] - 1e-3, o[2] + 1e-3]]), (0, 0, 0), 5.0e-4, 1000.0,
-               20.0, 1.0e-6)
+    if with_probe_fluid:
+        r.addFluid(np.array([[o[0] + sz[0] - 1e-3, o[1] + sz[1] - 1e-3, o[2] + 1e-3]]), (0, 0, 0), 5.0e-4, 1000.0,
+                   20.0, 1.0e-6)
     return r
 
 

@@ -307,21 +307,27 @@ def _same_state_and_lists(e0, e1):
             assert np.array_equal(p0[k], p1[k]), k
 
 
-@pytest.mark.parametrize("name", ("tiny_converging", "dry_granular", "tiny_coupled"))
-def test_fused_integration_equals_separate_passes(ds, scenes, name, monkeypatch):
+@pytest.mark.parametrize("name,skin", [("tiny_converging", 0.0), ("dry_granular", 0.0), ("dry_granular", 1.0e-9),
+                                       ("tiny_coupled", 0.0)])
+def test_fused_integration_equals_separate_passes(ds, scenes, name, skin, monkeypatch):
     """Graphs of plain DEM steps close each step and open the next in one
     integration pass, with the neighbour search in between reading the
-    end-of-step offsets; forty steps give the bits of the two separate passes
-    (DEMSPH_FUSE_INTEGRATION=0, read when an engine is created) and of the
-    staged calls."""
+    end-of-step offsets, and (without bonds) build the contact list of an
+    opened step in the launch of its contact forces; forty steps give the
+    bits of the two separate passes (DEMSPH_FUSE_INTEGRATION=0), of the fused
+    pass with two contact launches (DEMSPH_MERGE_CONTACTS=0; both read when an
+    engine is created) and of the staged calls; with a 1 nm candidate margin
+    the opened steps also rebuild their candidates in that launch."""
     recipe = _dry_granular(scenes) if name == "dry_granular" else getattr(scenes, name)()
     b, sc = ds.build_scene(recipe)
     engines = []
-    for flag in ("1", "0"):
-        monkeypatch.setenv("DEMSPH_FUSE_INTEGRATION", flag)
-        engines.append(ds.Engine(sc))
+    for fuse, merge in (("1", "1"), ("0", "1"), ("1", "0")):
+        monkeypatch.setenv("DEMSPH_FUSE_INTEGRATION", fuse)
+        monkeypatch.setenv("DEMSPH_MERGE_CONTACTS", merge)
+        engines.append(ds.Engine(sc, solid_verlet_skin=skin))
     monkeypatch.delenv("DEMSPH_FUSE_INTEGRATION")
-    staged = ds.Engine(sc)
+    monkeypatch.delenv("DEMSPH_MERGE_CONTACTS")
+    staged = ds.Engine(sc, solid_verlet_skin=skin)
     dt, gap = sc.time_step, sc.fluid_integrate_gap
     for e in engines + [staged]:
         e.initialize()
@@ -331,8 +337,26 @@ def test_fused_integration_equals_separate_passes(ds, scenes, name, monkeypatch)
         staged.step(dt, s, gap)
     assert engines[0].run_stats()["fused_passes"] > 0
     assert engines[1].run_stats()["fused_passes"] == 0
-    _same_state_and_lists(engines[0], engines[1])
-    _same_state_and_lists(engines[0], staged)
+    for e in engines[1:] + [staged]:
+        _same_state_and_lists(engines[0], e)
+
+
+def test_walk_mode_splits_the_merged_contact_launch(ds, scenes):
+    """Two solids start above the domain, so the lists come from the walk:
+    the first step a fused pass opens finds the one-launch contact list
+    unusable, raises its status before writing anything, and is resumed from
+    its midpoint with two launches (as every later step is).  Thirty steps give
+    the bits of the staged calls."""
+    b, sc = ds.build_scene(scenes.tiny_escape(with_probe_fluid=False))
+    e, staged = ds.Engine(sc), ds.Engine(sc)
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for x in (e, staged):
+        x.initialize()
+    e.update(dt, 1, 30, gap, use_graph=True)
+    for s in range(1, 31):
+        staged.step(dt, s, gap)
+    assert e.run_stats()["resumed_steps"] >= 1
+    _same_state_and_lists(e, staged)
 
 
 def test_overflow_inside_a_fused_run_resumes_the_opened_step(ds, scenes):
