@@ -364,6 +364,8 @@ def run_many(args, world, rank, local):
                                       "breaks, fluid counts log-uniform in [2k, 60k], column heights uniform in "
                                       f"[0.2, 0.5] m, {steps} steps each, through the scene server",
                        "workers": args.workers, "hbm_budget_bytes": budget,
+                       "graphs": "a scene replays CUDA graphs only while it is the only active one; in the mix "
+                                 "its kernels are launched directly",
                        "autotune": "threads per fluid particle timed per size class (demsph_autotune)",
                        "timing": "host wall clock from the first submission to the last completion (engine "
                                  "creation and initialisation included)"},
@@ -414,7 +416,8 @@ def run_many(args, world, rank, local):
                    "description": f"Poisson arrivals at 20/s for {args.duration:g} s (the workload names 300 s); "
                                   "SPH, DEM and coupled scenes in equal shares, sizes log-uniform in [5k, 500k], "
                                   "steps uniform in [200, 5000]; 150 GiB admission budget",
-                   "workers": args.workers},
+                   "workers": args.workers,
+                   "graphs": "a scene replays CUDA graphs only while it is the only active one"},
         "impl": "ours",
         "serving": {"submitted": submitted, "admitted": st["admitted"], "completed": st["completed"],
                     "p50_step_ms": st["p50_step_ms"], "p99_step_ms": st["p99_step_ms"],
@@ -437,7 +440,7 @@ def main():
     ap.add_argument("--plain-scenes", type=int, default=32,
                     help="batched workload: scenes (evenly spaced in the list) also run one at a time")
     ap.add_argument("--duration", type=float, default=60.0, help="serving workload: seconds of arrivals")
-    ap.add_argument("--workers", type=int, default=32, help="batched/serving: server worker threads")
+    ap.add_argument("--workers", type=int, default=8, help="batched/serving: server worker threads")
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--profile-steps", type=int, default=40)
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline stepping")

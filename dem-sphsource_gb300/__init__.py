@@ -101,7 +101,7 @@ class ServerConfig(C.Structure):
     """ctypes mirror of ``demsph_server_config``."""
 
     _fields_ = [("device", _I), ("workers", _I), ("chunk_steps", _I), ("hbm_budget_bytes", C.c_longlong),
-                ("autotune", _I)]
+                ("autotune", _I), ("graphs", _I)]
 
 
 class ServerSummary(C.Structure):
@@ -542,9 +542,11 @@ class Server:
 
     STATES = ("pending", "running", "done", "failed")
 
-    def __init__(self, device=0, workers=0, chunk_steps=0, hbm_budget_bytes=0, autotune=False):
+    def __init__(self, device=0, workers=0, chunk_steps=0, hbm_budget_bytes=0, autotune=False, graphs=0):
+        """graphs: CUDA graphs for a scene's turns - 0 only while it is the
+        only active scene, 1 always, -1 never."""
         self.lib = load_library()
-        cfg = ServerConfig(device, workers, chunk_steps, int(hbm_budget_bytes), 1 if autotune else 0)
+        cfg = ServerConfig(device, workers, chunk_steps, int(hbm_budget_bytes), 1 if autotune else 0, int(graphs))
         h = _P()
         rc = self.lib.demsph_server_create(C.byref(cfg), C.byref(h))
         if rc != DEMSPH_OK:

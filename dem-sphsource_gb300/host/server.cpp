@@ -7,8 +7,11 @@
 // for list growth) stays inside the configured budget; each admitted scene
 // gets its own engine, hence its own CUDA stream and stream-ordered memory.
 // Worker threads take turns advancing the scenes in chunks of steps
-// (demsph_update, replaying CUDA graphs), so the kernels of different scenes
-// overlap on the device, and a scene that arrives while others run is
+// (demsph_update), so the kernels of different scenes overlap on the device.
+// A scene replays CUDA graphs while it is the only active one; in a mix it
+// launches its kernels directly (graph capture and instantiation next to
+// other scenes' work cost hundreds of times more than on an idle GPU, more
+// than the graphs save).  A scene that arrives while others run is
 // admitted as soon as memory frees up (continuous batching).  A finished
 // scene's final state is downloaded, its engine destroyed and its memory
 // released before the next admission.
@@ -135,6 +138,7 @@ struct demsph_server {
     // statistics
     std::vector<double> stepMs;   // per chunk: milliseconds per step
     long long updates = 0, completed = 0, failed = 0, submittedN = 0, admittedN = 0, stepsRun = 0;
+    long long activeN = 0;        // admitted requests not yet finished
     double createS = 0, stepS = 0, downloadS = 0;   // worker time by activity
     std::map<int, int> lanesByClass;   // autotuned threads per fluid particle by log2(fluid count)
     bool anyAdmitted = false;
@@ -152,6 +156,7 @@ struct demsph_server {
             used += r.reserved;
             peak = std::max(peak, used);
             ++admittedN;
+            ++activeN;
             if (!anyAdmitted) {
                 anyAdmitted = true;
                 firstAdmit = r.admitted;
@@ -177,6 +182,7 @@ struct demsph_server {
         r.finished = Clock::now();
         lastFinish = r.finished;
         used -= r.reserved;
+        --activeN;
         if (s == State::Done) ++completed;
         else ++failed;
         admit();
@@ -191,6 +197,7 @@ struct demsph_server {
             cv.wait(lock, [&] { return stop || (r = pick()) != nullptr; });
             if (stop) return;
             r->busy = true;
+            const int useGraph = cfg.graphs > 0 || (cfg.graphs == 0 && activeN == 1) ? 1 : 0;
             lock.unlock();
             int rc = DEMSPH_OK;
             std::string err;
@@ -222,7 +229,7 @@ struct demsph_server {
             if (rc == DEMSPH_OK) {
                 n = std::min(cfg.chunk_steps, r->steps - r->next + 1);
                 const auto t0 = Clock::now();
-                rc = demsph_update(r->eng, r->dt, r->next, n, r->gap, 1);
+                rc = demsph_update(r->eng, r->dt, r->next, n, r->gap, useGraph);
                 tStep = seconds(t0, Clock::now());
                 ms = 1e3 * tStep / std::max(1, n);
                 long long fluidSteps = 0;
@@ -292,9 +299,9 @@ int demsph_server_create(const demsph_server_config* cfg, demsph_server** out)
     demsph_server_config c{};
     if (cfg) c = *cfg;
     if (c.hbm_budget_bytes <= 0) c.hbm_budget_bytes = 150LL << 30;
-    if (c.workers <= 0) c.workers = 16;
+    if (c.workers <= 0) c.workers = 8;  // the mix measured fastest with 8 to 16 (16 host cores)
     if (c.chunk_steps <= 0) c.chunk_steps = 100;
-    if (c.workers > 256) return DEMSPH_ERR_ARGUMENT;
+    if (c.workers > 256 || c.graphs < -1 || c.graphs > 1) return DEMSPH_ERR_ARGUMENT;
     auto* s = new demsph_server;
     s->cfg = c;
     for (int k = 0; k < c.workers; ++k) s->workers.emplace_back([s] { s->work(); });

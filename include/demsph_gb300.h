@@ -372,11 +372,16 @@ DEMSPH_API int demsph_export_fluid_sumw0(demsph_engine* e, double* sumw0);
 typedef struct demsph_server demsph_server;
 typedef struct demsph_server_config {
     int device;                  /* CUDA device ordinal */
-    int workers;                 /* host threads advancing scenes; 0 = 16 */
+    int workers;                 /* host threads advancing scenes; 0 = 8 */
     int chunk_steps;             /* steps per turn of a scene; 0 = 100 */
     long long hbm_budget_bytes;  /* device memory the admitted scenes may hold; 0 = 150 GiB */
     int autotune;                /* != 0: the first scene of each size class (fluid count within a
                                     factor of 2) runs demsph_autotune, later ones reuse its choice */
+    int graphs;                  /* CUDA graphs for a turn: 0 = only when the scene is the only
+                                    active one (default), 1 = always, -1 = never.  Capturing and
+                                    instantiating graphs while other scenes' kernels run was measured
+                                    hundreds of times slower than on an idle GPU, so scenes in a mix
+                                    launch their kernels directly (the same results, bit for bit) */
 } demsph_server_config;
 typedef struct demsph_server_summary {
     long long submitted, admitted, completed, failed, pending;

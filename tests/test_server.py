@@ -54,6 +54,13 @@ def test_server_reports_failure_without_a_gpu(ds, scenes):
         srv.close()
 
 
+def test_server_rejects_an_unknown_graph_mode(ds):
+    for bad in (2, -2):
+        with pytest.raises(ds.DemSphError) as e:
+            ds.Server(workers=1, graphs=bad)
+        assert e.value.status == 1  # DEMSPH_ERR_ARGUMENT
+
+
 def test_server_rejects_a_scene_over_the_budget(ds, scenes):
     _, sc = ds.build_scene(scenes.tiny_coupled())
     srv = ds.Server(workers=1, hbm_budget_bytes=ds.estimate_bytes(sc) // 2)
@@ -66,9 +73,13 @@ def test_server_rejects_a_scene_over_the_budget(ds, scenes):
 
 
 @pytest.mark.gpu
-def test_mix_equals_alone(ds, scenes):
+@pytest.mark.parametrize("graphs", [0, 1, -1])
+def test_mix_equals_alone(ds, scenes, graphs):
+    """In the mix, scenes launch directly (graphs 0: several are active; -1)
+    or replay graphs (1); each result has the bits of the scene run alone
+    from graphs."""
     built = [(ds.build_scene(getattr(scenes, name)()), steps) for name, steps in MIX]
-    srv = ds.Server(workers=4, chunk_steps=7)
+    srv = ds.Server(workers=4, chunk_steps=7, graphs=graphs)
     try:
         ids = [srv.submit(sc, steps) for (_, sc), steps in built]
         srv.wait(-1, 600.0)
