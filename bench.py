@@ -23,6 +23,8 @@ state from pinned host memory, runs the step and downloads it again.
 the dominant stage's algorithmic bytes to the measured HBM copy bandwidth.
 `cpu_baseline` is the FP64 oracle (a CPU restatement of the reference's step;
 the reference has no CPU solver) on all host cores, on a bounded sample.
+`fp64_error` compares a second engine, run through the same steps from the
+same initial state, with the oracle's state at the end of that sample.
 
 --impl reference times that CPU implementation alone on the same workload
 (the reference's own code is CUDA and is not available on the GPU machine).
@@ -272,7 +274,48 @@ def cpu_baseline(scene, gap, dt, budget_s, nf, n_mobile):
     ups = updates_for(2, n, gap, nf, n_mobile) / el
     return {"value": ups, "unit": "particle-updates/s", "cores": threads, "kind": "port",
             "sample": f"{n} consecutive steps (2..{n + 1}) of the full workload after one warm-up step; "
-                      f"FP64 oracle, OpenMP over particles"}
+                      f"FP64 oracle, OpenMP over particles"}, orc, n + 1
+
+
+def fp64_errors(ds, scene, orc, steps, dt, gap, device):
+    """Error of the GPU step against the FP64 oracle after the CPU sample's
+    steps (1..steps from the workload's initial state): a second engine runs
+    the same steps through the timed path (graph replay), and each field's
+    largest error is taken over all particles, scaled as named in `scale`."""
+    import numpy as np
+    g = 9.81
+    eng = ds.Engine(scene, device=device)
+    eng.initialize()
+    eng.update(dt, 1, steps, gap, use_graph=True)
+    eng.synchronize()
+    t = steps * dt
+    err = {}
+
+    def rel_rows(a, b, floor):
+        return float(np.max(np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), floor)))
+
+    if scene.n_fluid:
+        pos, vel, acc, drho = eng.download_fluids()
+        h = float(np.ctypeslib.as_array(scene.fluid_smoothing_length, shape=(scene.n_fluid,)).min())
+        v64 = orc.get("fluid.vel")
+        err["fluid.pos"] = float(np.max(np.abs(pos - orc.get("fluid.pos")))) / h
+        err["fluid.vel"] = float(np.max(np.abs(vel - v64))) / max(float(np.abs(v64).max()), g * t)
+        err["fluid.acc"] = rel_rows(acc, orc.get("fluid.acc"), g)
+        err["fluid.dRho"] = float(np.max(np.abs(drho - orc.get("fluid.dRho")))) / 1000.0
+    if scene.n_solid:
+        s = eng.download_solids()
+        r = float(np.ctypeslib.as_array(scene.solid_radius, shape=(scene.n_solid,)).min())
+        v64 = orc.get("solid.vel")
+        w64 = orc.get("solid.angvel")
+        err["solid.pos"] = float(np.max(np.abs(s["pos"] - orc.get("solid.pos")))) / r
+        err["solid.vel"] = float(np.max(np.abs(s["vel"] - v64))) / max(float(np.abs(v64).max()), g * t)
+        err["solid.acc"] = rel_rows(s["acc"], orc.get("solid.acc"), g)
+        err["solid.angvel"] = float(np.max(np.abs(s["angvel"] - w64))) / max(float(np.abs(w64).max()), g * t / r)
+    eng.close()
+    return {"steps": steps, "fields": err,
+            "scale": "largest |GPU - FP64| over the particles, divided by: the smallest smoothing length (fluid.pos) "
+                     "or radius (solid.pos); the largest FP64 speed or g t (vel); the FP64 value per particle, at "
+                     "least g (acc: force per mass); rho0 = 1000 (dRho); the largest FP64 spin or g t / r (angvel)"}
 
 
 # ---- ranks: replicas, no exchange on the data path -------------------------------------------
@@ -467,7 +510,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_baseline(scene, gap, dt, args.cpu_budget, nf, n_mobile)
+        cb = cpu_baseline(scene, gap, dt, args.cpu_budget, nf, n_mobile)[0]
         step_ms = None
         upd_per_step = updates_for(1, 10 * gap, gap, nf, n_mobile) / (10 * gap)
         if cb["value"] > 0:
@@ -599,9 +642,11 @@ def main():
     if dist:
         e2e_val = e2e_updates * world / rank_total(e2e_s, "max", dist)
 
-    cb = None
+    cb = err64 = None
     if rank == 0 and not args.no_cpu:
-        cb = cpu_baseline(scene, gap, dt, args.cpu_budget, nf, n_mobile)
+        cb, orc, orc_steps = cpu_baseline(scene, gap, dt, args.cpu_budget, nf, n_mobile)
+        err64 = fp64_errors(ds, scene, orc, orc_steps, dt, gap, device)
+        del orc
 
     if rank == 0:
         per_step.sort()
@@ -620,7 +665,7 @@ def main():
             "p50_step_ms": per_step[len(per_step) // 2] if per_step else None,
             "p99_step_ms": per_step[min(len(per_step) - 1, int(math.ceil(0.99 * len(per_step))) - 1)]
             if per_step else None,
-            "roofline": roofline, "cpu_baseline": cb,
+            "roofline": roofline, "cpu_baseline": cb, "fp64_error": err64,
             "e2e": {"value": e2e_val, "unit": "particle-updates/s", "h2d_bytes_per_step": bi,
                     "d2h_bytes_per_step": bo, "steps": ne,
                     "path": "demsph_update_io per step: upload the state, one step, download the state, one "
