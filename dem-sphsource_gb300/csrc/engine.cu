@@ -260,7 +260,9 @@ void stageBefore(demsph_engine* e, double dt)
     launchSolidIntegrate(e->d, dt, INTEGRATE_BEFORE, e->par, false, false, e->stream);
 }
 
-void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
+// countStep: the fluid stage ends the step (see fullStep) and its last pass
+// counts it.
+void stageFluid(demsph_engine* e, double dt, int iStep, int gap, bool countStep = false)
 {
     DeviceState& d = e->d;
     if (d.nf <= 0) return;
@@ -286,7 +288,7 @@ void stageFluid(demsph_engine* e, double dt, int iStep, int gap)
             launchMomentumPass(d, dtf, s);
         }
         TIMED("continuity");
-        launchContinuityPass(d, 1, dtf, s);
+        launchContinuityPass(d, 1, dtf, s, countStep);
     }
 }
 
@@ -322,11 +324,17 @@ void stageAfter(demsph_engine* e, double dt, bool clumpForce = false, bool count
 // step has run already (a step resumed after an overflow in its search).
 void fullStep(demsph_engine* e, double dt, int iStep, int gap, bool opened = false)
 {
+    // a fluid step after whose fluid stage nothing runs (no solid is
+    // integrated, touches another or is bonded, no clump) is counted by the
+    // last continuity pass instead of a launch of its own
+    const DeviceState& d = e->d;
+    const bool countInFluid =
+        d.nf > 0 && iStep % gap == 0 && d.nmove == 0 && d.nc == 0 && d.nb == 0 && d.nrow <= 0;
     stageNeighborSearch(e, iStep, gap, opened);
     if (!opened) stageBefore(e, dt);
-    stageFluid(e, dt, iStep, gap);
+    stageFluid(e, dt, iStep, gap, countInFluid);
     stageContact(e, dt, false);
-    stageAfter(e, dt, e->d.nc > 0, true);
+    stageAfter(e, dt, e->d.nc > 0, !countInFluid);
 }
 
 // `length` >= 2 whole steps of plain DEM (no fluid step among them) where

@@ -429,7 +429,8 @@ void launchSolidNormals(const DeviceState& d, double h, cudaStream_t s);
 void launchDensityReinit(const DeviceState& d, int iStep, cudaStream_t s);
 // which = 0: first half step (densities 0 -> 1, positions drift 0 -> 1);
 // which = 1: second half step (densities 1 -> 0, velocities 1 -> 0).
-void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStream_t s);
+// countStep: the pass counts the step in stepsDone (the last kernel of a step)
+void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStream_t s, bool countStep = false);
 // momentum + kick (dt_f) + drift (dt_f / 2): reads buffers [1], writes velocity [1], position [0].
 void launchMomentumPass(const DeviceState& d, double dtf, cudaStream_t s);
 void launchCoupling(const DeviceState& d, int src, cudaStream_t s);

@@ -144,6 +144,7 @@ struct ContinuityArgs {
     int ps, vs, ds, dd;  // position / velocity / density source, density destination
     int driftTo;         // -1: no drift; else position buffer receiving x + v * drift
     int velCopyTo;       // -1: none; else velocity buffer receiving a copy of this particle's velocity
+    int countStep;       // 1: the pass ends the step (nothing after it can raise a status): count it
     float dt;
     dfl drift;
 };
@@ -152,6 +153,7 @@ template <int L, bool U>
 __global__ void __launch_bounds__(T, L == 1 ? 12 : 10) kContinuity(DeviceState d, ContinuityArgs a)
 {
     stepKernelBegin();
+    if (a.countStep && blockIdx.x == 0 && threadIdx.x == 0 && *d.status == 0) atomicAdd(d.stepsDone, 1);
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if ((t & ~31) >= d.nf * L || *d.status) return;
     const int i = t / L, lane = t % L;
@@ -460,10 +462,11 @@ int fluidLanes(int nf)
     return L;
 }
 
-void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStream_t s)
+void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStream_t s, bool countStep)
 {
     if (d.nf <= 0) return;
     ContinuityArgs a;
+    a.countStep = countStep ? 1 : 0;
     a.dt = (float)(0.5 * dtf);
     a.drift = df_from_double(0.5 * dtf);
     if (which == 0) {  // first half step: densities 0 -> 1, drift positions 0 -> 1
