@@ -342,6 +342,15 @@ def scene_updates(scene, steps):
     return updates_for(1, steps, scene.fluid_integrate_gap, nf, n_mobile)
 
 
+RECIPES_AHEAD = 24  # serving: scene recipes made ahead of their arrival
+
+
+def _serving_recipe(kind, n, steps, seed):
+    """A serving request's recipe (in a spawned process)."""
+    import dem_sphsource_gb300.scenes as sc
+    return sc.make_request(kind, n, steps, seed)
+
+
 def run_many(args, world, rank, local):
     """Config 3: the batched mix through the scene server, against the same
     scenes run one at a time.  Config 4: a Poisson stream of requests served
@@ -426,25 +435,44 @@ def run_many(args, world, rank, local):
         }))
         return
 
-    # config 4: serving
+    # config 4: serving.  The scene recipes (the particle lattices) are made by
+    # a few spawned processes up to RECIPES_AHEAD arrivals ahead; the
+    # submitting thread turns each into a scene before its arrival time and
+    # submits it at that time.
+    import multiprocessing as mp
     arrivals = rank_share(sc.serving_stream(duration=args.duration), rank, world)
+    pool = mp.get_context("spawn").Pool(max(1, min(6, (os.cpu_count() or 2) // 2)), initializer=_package)
+    made = {}
+    nxt = [0]  # the first arrival whose recipe is not yet asked for
+
+    def schedule(upto):
+        while nxt[0] < min(upto, len(arrivals)):
+            _, kind, n, steps, seed = arrivals[nxt[0]]
+            made[nxt[0]] = pool.apply_async(_serving_recipe, (kind, n, steps, seed))
+            nxt[0] += 1
+
+    lag = []
+    schedule(RECIPES_AHEAD)
+    for k in range(min(RECIPES_AHEAD, len(arrivals))):
+        made[k].wait()
     srv = ds.Server(device=device, workers=args.workers, hbm_budget_bytes=budget, autotune=True)
     if dist:
         dist.barrier()
-    lag = []
     submitted = 0
     with ClockSampler(device) as clocks:
         t0 = time.perf_counter()
-        for (ta, kind, n, steps, seed) in arrivals:
+        for k, (ta, kind, n, steps, seed) in enumerate(arrivals):
+            _, s = ds.build_scene(made.pop(k).get())
             now = time.perf_counter() - t0
             if ta > now:
                 time.sleep(ta - now)
-            _, s = ds.build_scene(sc.make_request(kind, n, steps, seed))
             srv.submit(s, steps)
             submitted += 1
             lag.append(time.perf_counter() - t0 - ta)
+            schedule(k + 1 + RECIPES_AHEAD)
         window = time.perf_counter() - t0
         st = srv.stats()
+    pool.terminate()
     srv.close()  # requests still queued or running are dropped
     upd = rank_total(st["particle_updates"], "sum", dist)
     window = rank_total(window, "max", dist)
