@@ -134,11 +134,15 @@ int checkDevice(demsph_engine* e, int dev)
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return fail(e, DEMSPH_ERR_NO_DEVICE, "no CUDA device");
     if (dev < 0 || dev >= n) return fail(e, DEMSPH_ERR_ARGUMENT, "device index out of range");
-    cudaDeviceProp p;
-    if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return fail(e, DEMSPH_ERR_NO_DEVICE, "cannot query device");
-    if (p.major * 10 + p.minor != 103)
+    // two attributes, not cudaGetDeviceProperties (which queries them all: a
+    // cost every engine creation of a server would pay)
+    int major = 0, minor = 0;
+    if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess)
+        return fail(e, DEMSPH_ERR_NO_DEVICE, "cannot query device");
+    if (major * 10 + minor != 103)
         return fail(e, DEMSPH_ERR_NO_DEVICE, "this library is built for sm_103a (GB300); the device is sm_" +
-                                                 std::to_string(p.major * 10 + p.minor));
+                                                 std::to_string(major * 10 + minor));
     return DEMSPH_OK;
 }
 
