@@ -419,18 +419,28 @@ __device__ __forceinline__ float3 couplingPairForce(const DeviceState& d, int sr
     return (s.r * Ps - via * (2.f * o.gam)) * (2.f * o.V * s.Va * s.G);
 }
 
+// Only contact rows can hold solids with mass, the only solids with fluid
+// partners here (the coupling lists take no others); L lanes of a row take
+// its partners in turn, each Kahan-summing its share, and the shares are
+// added in a fixed tree (groupSum).
+template <int L>
 __global__ void kCoupling(DeviceState d, int src)
 {
     stepKernelBegin();
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= d.ns || *d.status) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((t & ~31) >= d.nrow * L || *d.status) return;  // whole warps: the group sums shuffle
+    const int row = t / L, lane = t % L;
+    const bool live = row < d.nrow;
+    const int a = live ? solidOf(d, row) : 0;
     KahanF3 f;
-    for (int p = d.coupStart[a], e = d.coupStart[a + 1]; p < e; ++p) {
-        bool inside;
-        const float3 fi = couplingPairForce(d, src, d.coupList[p], a, inside);
-        if (inside) f.add(fi);
-    }
-    d.sfcoup[a] = f4(f.sum());
+    if (live)
+        for (int p = d.coupStart[a] + lane, e = d.coupStart[a + 1]; p < e; p += L) {
+            bool inside;
+            const float3 fi = couplingPairForce(d, src, d.coupList[p], a, inside);
+            if (inside) f.add(fi);
+        }
+    const float x = groupSum<L>(f.x), y = groupSum<L>(f.y), z = groupSum<L>(f.z);
+    if (live && lane == 0) d.sfcoup[a] = make_float4(x, y, z, 0.f);
 }
 
 // Per-pair coupling force in the fluid's list order (for export only).
@@ -487,8 +497,9 @@ void launchMomentumPass(const DeviceState& d, double dtf, cudaStream_t s)
 
 void launchCoupling(const DeviceState& d, int src, cudaStream_t s)
 {
-    if (d.nf <= 0 || d.ns <= 0) return;
-    launchStep(kCoupling, blocksFor(d.ns, 128), 128, s, d, src);
+    if (d.nf <= 0 || d.ns <= 0 || d.nrow <= 0) return;
+    constexpr int L = 8;  // lanes per row: rows hold tens of fluid partners
+    launchStep(kCoupling<L>, blocksFor((long long)d.nrow * L, 256), 256, s, d, src);
 }
 
 void launchCouplingPairForces(const DeviceState& d, int src, float4* out, cudaStream_t s)
