@@ -492,18 +492,39 @@ __global__ void kCoupSort(DeviceState d)
 // history remap of the reference, from the springs the last contact phase
 // left in the previous list's slots).  At initialisation (forceWalk) the list
 // stays in walk order: bonds are numbered in it.
-__global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int forceWalk)
+// The spring history of the forward pairs q = first, first + step, ... of row
+// r from the previous list (the pair's springs there, or zeros).
+__device__ __forceinline__ void remapSprings(const DeviceState& d, int par, int r, int nf, int first, int step)
 {
-    stepKernelBegin();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= d.nrow || *d.status) return;
-    const bool walk = forceWalk || *d.slowMode;
+    const int prev = par ^ 1;
+    const size_t nr = (size_t)d.nrow;
+    const int prevCnt = min(d.fcnt[prev][r], d.scap);
+    for (int q = first; q < nf; q += step) {
+        const size_t slot = (size_t)q * nr + r;
+        const int b = d.fwd[par][slot];
+        float4 s0 = make_float4(0, 0, 0, 0), s1 = s0, s2 = s0;
+        for (int k = 0; k < prevCnt; ++k) {
+            const size_t ps = (size_t)k * nr + r;
+            if (d.fwd[prev][ps] == b) {
+                s0 = d.springOut[prev][0][ps];
+                s1 = d.springOut[prev][1][ps];
+                s2 = d.springOut[prev][2][ps];
+                break;
+            }
+        }
+        d.springIn[0][slot] = s0;
+        d.springIn[1][slot] = s1;
+        d.springIn[2][slot] = s2;
+    }
+}
+
+__device__ __forceinline__ void detectRow(const DeviceState& d, int par, int forceWalk, bool walk, int r)
+{
     // stale candidates are rebuilt first, row by row (the contact force
     // kernel clears the flag once every row has read it)
     if (!walk && d.rebuild[par]) verletBuildRow(d, r);
     const int a = solidOf(d, r);
     const int4 fa = d.sflags[a];
-    const int prev = par ^ 1;
     const int C = d.scap;
     const size_t nr = (size_t)d.nrow;
     int nf = 0, nb = 0;
@@ -543,24 +564,80 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
         sortSlots(d.fwd[par], r, d.nrow, nf);
         sortSlots(d.rev, r, d.nrow, nb);
     }
-    const int prevCnt = min(d.fcnt[prev][r], C);
-    for (int q = 0; q < nf; ++q) {
-        const size_t slot = (size_t)q * nr + r;
-        const int b = d.fwd[par][slot];
-        float4 s0 = make_float4(0, 0, 0, 0), s1 = s0, s2 = s0;
-        for (int k = 0; k < prevCnt; ++k) {
-            const size_t ps = (size_t)k * nr + r;
-            if (d.fwd[prev][ps] == b) {
-                s0 = d.springOut[prev][0][ps];
-                s1 = d.springOut[prev][1][ps];
-                s2 = d.springOut[prev][2][ps];
-                break;
+    remapSprings(d, par, r, nf, 0, 1);
+}
+
+
+// L lanes per row (rows with many candidates): the lanes test the candidates
+// in turn and a ballot keeps the lists in candidate order, exactly the lists
+// of one lane per row; each lane then remaps the history of every L-th
+// forward pair.  The reference's walk (at initialisation, or once a solid has
+// left the domain) and stale candidates (their rebuild) run on the row's
+// first lane.
+template <int L>
+__global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int forceWalk)
+{
+    stepKernelBegin();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((t & ~31) >= d.nrow * L || *d.status) return;  // whole warps: the ballots take every lane
+    const int r = t / L, lane = t % L;
+    const bool live = r < d.nrow;
+    const bool walk = forceWalk || *d.slowMode;
+    if (L == 1 || walk) {
+        if (live && lane == 0) detectRow(d, par, forceWalk, walk, r);
+        return;
+    }
+    // stale candidates are rebuilt first (the contact force kernel clears the
+    // flag once every row has read it)
+    if (live && lane == 0 && d.rebuild[par]) verletBuildRow(d, r);
+    __syncwarp();  // the rebuilt candidates, for the row's other lanes
+    const unsigned FULL = 0xffffffffu;
+    const int groupShift = (threadIdx.x & 31) & ~(L - 1);
+    const unsigned groupBits = (1u << L) - 1u;
+    const unsigned below = (1u << lane) - 1u;
+    const int C = d.scap;
+    const size_t nr = (size_t)d.nrow;
+    const int a = live ? solidOf(d, r) : 0;
+    const int n = live ? min(d.vcnt[r], d.vcap) : 0;
+    int nf = 0, nb = 0;
+    for (int base = 0; __any_sync(FULL, base < n); base += L) {
+        const int k = base + lane;
+        int b = 0;
+        bool tf = false, tb = false;
+        if (k < n) {
+            b = d.vcand[(size_t)k * nr + r];
+            if (solidsTouch(d, a, b)) {
+                tf = b > a;
+                tb = !tf;
             }
         }
-        d.springIn[0][slot] = s0;
-        d.springIn[1][slot] = s1;
-        d.springIn[2][slot] = s2;
+        const unsigned mf = (__ballot_sync(FULL, tf) >> groupShift) & groupBits;
+        const unsigned mb = (__ballot_sync(FULL, tb) >> groupShift) & groupBits;
+        if (tf) {
+            const int q = nf + __popc(mf & below);
+            if (q < C) d.fwd[par][(size_t)q * nr + r] = b;
+        }
+        if (tb) {
+            const int q = nb + __popc(mb & below);
+            if (q < C) d.rev[(size_t)q * nr + r] = b;
+        }
+        nf += __popc(mf);
+        nb += __popc(mb);
     }
+    __syncwarp();  // the list entries, for the lanes that remap them
+    if (!live) return;
+    if (lane == 0) {
+        d.fcnt[par][r] = nf;
+        d.rcnt[r] = nb;
+    }
+    if (nf > C || nb > C) {
+        if (lane == 0) {
+            atomicOr(d.status, ST_SS_OVERFLOW);
+            atomicMax(&d.need[0], max(nf, nb));
+        }
+        return;
+    }
+    remapSprings(d, par, r, nf, lane, L);
 }
 
 // Contact items (forward and reverse contacts, bonds) per row over at most
@@ -762,7 +839,12 @@ void launchCouplingLists(const DeviceState& d, cudaStream_t s)
 void launchContactDetect(const DeviceState& d, int par, bool forceWalk, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    launchStep(kContactDetect, blocksFor(d.nrow, T), T, s, d, par, forceWalk ? 1 : 0);
+    // rows holding many contacts and bonds (the force kernel's rows per warp
+    // adapted down to 16 or fewer) have many candidates: four lanes per row
+    if (d.forceRows <= 16)
+        launchStep(kContactDetect<4>, blocksFor((long long)d.nrow * 4, T), T, s, d, par, forceWalk ? 1 : 0);
+    else
+        launchStep(kContactDetect<1>, blocksFor(d.nrow, T), T, s, d, par, forceWalk ? 1 : 0);
 }
 
 void launchRowStats(const DeviceState& d, int par, cudaStream_t s)
