@@ -1,36 +1,45 @@
 #!/usr/bin/env python3
 """Benchmark: particle-updates/s of the coupled DEM-SPH step on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config 0|1|2]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config 0|1|2|3|4]
 
-One step is one solverBase::update() of the scene (core/solverBase.cpp:47-67):
-neighbour search, the two solid half-step integrations, the fluid step (every
-`gap` steps) and the contact phase.  particle-updates/s counts every mobile
-particle once per step it is advanced: N_fluid for each fluid step plus the
-solids with non-zero inverse mass for every step (dummy wall particles are
-not counted).
+One bench step is one fluid period of the scene: `gap` solverBase::update()
+calls (core/solverBase.cpp:47-67), the last of them the fluid step (the
+reference integrates the fluid when step % gap == 0, core/integrate.cu:385-421);
+for a scene with gap 1 that is one update() call.  Each update() runs the
+neighbour search, the two solid half-step integrations, the fluid work of the
+step and the contact phase.  particle-updates/s counts every mobile particle
+once per update it is advanced: N_fluid per fluid step plus the solids with
+non-zero inverse mass per update (dummy wall particles are not counted).
 
 Workloads (synthetic, seeded, generated by dem-sphsource_gb300/scenes.py):
-  0  48k-fluid WCSPH dam break (dx 0.01 m, 3-layer dummy walls)
-  1  Hertz-Mindlin settle: 200k lognormal spheres + 5k four-pebble clumps (default)
-  2  coupled dam break: 1.0M fluid (dx 0.004 m) against 64 bonded 8^3 cubes
+  0  48k-fluid WCSPH dam break (dx 0.01 m, 3-layer dummy walls), gap 1
+  1  Hertz-Mindlin settle: 200k lognormal spheres + 5k four-pebble clumps, gap 1,
+     timed from a contact-dense bed (--settle-steps of the settle run first, untimed)
+  2  coupled dam break: 1.0M fluid (dx 0.004 m) against 64 bonded 8^3 cubes, gap 28 (default)
+  3  256-scene batched mix through the scene server
+  4  Poisson serving stream through the scene server
 
-`value` is measured with the scene resident in HBM: K steps replayed as CUDA
-graphs on the engine's stream, bracketed by CUDA events.  `e2e` is the same
-metric through the C ABI with host buffers: every step uploads the dynamic
-state from pinned host memory, runs the step and downloads it again.
-`roofline` times each stage with CUDA events (an uncaptured pass) and relates
-the dominant stage's algorithmic bytes to the measured HBM copy bandwidth.
-`cpu_baseline` is the FP64 oracle (a CPU restatement of the reference's step;
-the reference has no CPU solver) on all host cores, on a bounded sample.
-`fp64_error` compares a second engine, run through the same steps from the
-same initial state, with the oracle's state at the end of that sample.
+`value` is measured with the scene resident in HBM: K bench steps replayed as
+CUDA graphs on the engine's stream, bracketed by CUDA events (the inputs are
+far larger than L2 for configs 1 and 2; config 0's state fits in L2, and the
+line says so).  `e2e` is the same metric through the C ABI with host buffers:
+every bench step uploads the dynamic state from pinned host memory, runs the
+step and downloads it again (demsph_update_io).  `roofline` times each stage
+with CUDA events (an uncaptured pass) and relates the dominant stage's
+algorithmic bytes to the measured HBM copy bandwidth.  `cpu_baseline` is the
+FP64 oracle (a CPU restatement of the reference's step; the reference has no
+CPU solver) on all host cores, on a bounded sample of whole bench steps, from
+a scene the oracle assembles itself (oracle/scene.py).  `fp64_error` compares
+a second engine, run through the same steps from the same state, with the
+oracle's state at the end of that sample.
 
---impl reference times that CPU implementation alone on the same workload
-(the reference's own code is CUDA and is not available on the GPU machine).
-Under torchrun (N > 1) every rank runs an independent replica of the scene on
-its own GPU (the step has no inter-GPU exchange); `value` is the sum over ranks
-divided by the slowest rank's time.
+--impl reference times that CPU implementation on the same workload: W + K
+bench steps (fewer if they would not fit --ref-budget seconds; the line then
+says how many it timed), without loading the product library.  Under torchrun
+(N > 1) every rank runs an independent replica of the scene on its own GPU
+(the step has no inter-GPU exchange); `value` is the sum over ranks divided by
+the slowest rank's time; the reference arm runs on rank 0 only.
 """
 from __future__ import annotations
 
@@ -62,23 +71,34 @@ def _package():
     return mod
 
 
+def _scenes():
+    """dem-sphsource_gb300/scenes.py alone (numpy only): the workload recipes,
+    without the package and its library."""
+    name = "demsph_scenes"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, os.path.join(ROOT, "dem-sphsource_gb300", "scenes.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
 WORKLOADS = {
     0: ("dam_break_48k", "WCSPH dam break: tank 1.6x0.4x0.6 m, column 0.4x0.4x0.3 m, dx 0.01 m, 3-layer walls"),
-    1: ("granular_settle_200k_5k", "Hertz-Mindlin settle: 200k lognormal spheres (median 1 mm, sigma 0.2) + 5k "
-                                   "4-pebble clumps, floor + 4 walls"),
-    2: ("coupled_dam_break_1M_64cubes", "1.0M fluid (dx 0.004 m) dam break onto 64 bonded 8^3 sphere cubes"),
+    1: ("granular_settle_200k_5k", "Hertz-Mindlin settle: 200k lognormal spheres (median 1 mm, sigma 0.2, radii "
+                                   "clipped to [0.6, 1.2] mm: a 2.5 mm lattice cannot hold 2 mm radii without "
+                                   "overlaps) + 5k 4-pebble clumps, floor + 4 walls"),
+    2: ("coupled_dam_break_1M_64cubes", "1.0M fluid (dx 0.004 m) dam break onto 64 bonded 8^3 sphere cubes; bond "
+                                        "strength per cube from 9 levels in [0.5, 2.0] MPa (the reference keys "
+                                        "strength by material pair)"),
 }
+SETTLE_STEPS = {1: 60000}  # config 1: untimed steps of the settle before the timed window
 
 
 def make_recipe(config):
-    import dem_sphsource_gb300.scenes as scenes
-    if config == 0:
-        return scenes.dam_break()
-    if config == 1:
-        return scenes.granular_settle()
-    if config == 2:
-        return scenes.coupled_dam_break()
-    raise ValueError(config)
+    sc = _scenes()
+    return {0: sc.dam_break, 1: sc.granular_settle, 2: sc.coupled_dam_break}[config]()
 
 
 def mobile_counts(scene):
@@ -100,22 +120,89 @@ def updates_for(first, n, gap, nf, n_mobile):
     return nf * fluid_steps + n_mobile * n
 
 
+def workload_config(config, scene, args, settle):
+    """The config dict both arms print: the workload and its sizes, computed
+    from the scene's arrays (the product's or the oracle's: the same bits)."""
+    name, desc = WORKLOADS[config]
+    nf, n_mobile, n_dummy = mobile_counts(scene)
+    gap = scene.fluid_integrate_gap
+    cfg = {"workload": name, "description": desc, "n_fluid": nf, "n_solid_mobile": n_mobile,
+           "n_dummy_wall": n_dummy, "n_clump": scene.n_clump, "dt": scene.time_step, "fluid_integrate_gap": gap,
+           "step": (f"one fluid period: {gap} solverBase::update() calls, the last of them the fluid step"
+                    if gap > 1 else "one solverBase::update() call"),
+           "updates_per_step": updates_for(1, gap, gap, nf, n_mobile),
+           "state": (f"the bed after {settle} untimed steps of the settle (contact-dense), springs and all"
+                     if settle else "the workload's initial state, then the warm-up steps"),
+           "l2": "inputs larger than L2 (129 MB)" if config in (1, 2) else
+                 "the scene's state (about 20 MB) fits in L2 (129 MB): not flushed between steps",
+           "parallelism": f"replicas x{args.gpus}"}
+    return cfg
+
+
+def scene_state(scene):
+    """{name: writable numpy view} of the dynamic state arrays of a scene
+    (either ctypes mirror of demsph_scene), for restarting from a state."""
+    import ctypes as C
+    import numpy as np
+
+    def view(ptr, n, w):
+        if not n or not ptr:
+            return None
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_double)), shape=(n, w))
+    ns, nc = scene.n_solid, scene.n_clump
+    return {"solid.pos": view(scene.solid_position, ns, 3), "solid.vel": view(scene.solid_velocity, ns, 3),
+            "solid.acc": view(scene.solid_acceleration, ns, 3), "solid.torque": view(scene.solid_torque, ns, 3),
+            "solid.angvel": view(scene.solid_angular_velocity, ns, 3),
+            "clump.centroid": view(scene.clump_centroid, nc, 3), "clump.vel": view(scene.clump_velocity, nc, 3),
+            "clump.acc": view(scene.clump_acceleration, nc, 3), "clump.angvel": view(scene.clump_angular_velocity, nc, 3),
+            "clump.torque": view(scene.clump_torque, nc, 3)}
+
+
+def engine_state(eng):
+    """The solid and clump state of an engine, in the names of scene_state."""
+    s = eng.download_solids()
+    out = {"solid.pos": s["pos"], "solid.vel": s["vel"], "solid.acc": s["acc"], "solid.torque": s["torque"],
+           "solid.angvel": s["angvel"]}
+    if eng.nc:
+        c = eng.download_clumps()
+        out.update({"clump.centroid": c["centroid"], "clump.vel": c["vel"], "clump.acc": c["acc"],
+                    "clump.angvel": c["angvel"], "clump.torque": c["torque"]})
+    return out
+
+
+def restart_scene(scene, state):
+    """Writes a state (engine_state) into a scene's arrays: an engine or oracle
+    created from the scene then starts from that state (contact springs and
+    wall springs start at zero, as at any scene start)."""
+    views = scene_state(scene)
+    for k, v in state.items():
+        if views.get(k) is not None and v is not None:
+            views[k][...] = v
+
+
 # ---- clocks during the timed region -------------------------------------------------------
 class ClockSampler:
+    """nvidia-smi samples of the SM clock and throttle reasons while the GPU
+    works.  The window covers the timed region (up to mark_end) plus, when the
+    caller keeps the same load going after it, that tail, so a timed region
+    shorter than the sampling period still has samples; the summary says how
+    many came from each."""
     FIELDS = ("clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
               "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
               "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 20
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.t_end = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + ",".join(self.FIELDS),
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
@@ -125,7 +212,10 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def mark_end(self):
+        self.t_end = time.perf_counter()
 
     def __exit__(self, *a):
         if self.proc:
@@ -137,8 +227,9 @@ class ClockSampler:
 
     def summary(self):
         sm, smax, reasons = [], [], set()
+        in_region = 0
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for ln in self.lines:
+        for t, ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < len(self.FIELDS):
                 continue
@@ -147,13 +238,16 @@ class ClockSampler:
                 smax.append(float(parts[1]))
             except ValueError:
                 continue
+            if self.t_end is None or t <= self.t_end:
+                in_region += 1
             for nm, val in zip(names, parts[4:8]):
                 if val.lower() == "active":
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "samples_in_timed_region": in_region,
+                "window": "the timed region plus about 1 s of the same bench steps replayed right after it"}
 
 
 # ---- algorithmic bytes per stage (compulsory traffic) -------------------------
@@ -255,38 +349,107 @@ def load_traffic(stage):
 
 
 # ---- CPU baseline: the FP64 oracle ------------------------------------------------------------
-def cpu_baseline(scene, gap, dt, budget_s, nf, n_mobile):
+def oracle_scene(recipe, state=None):
+    """The workload assembled by the oracle itself (oracle/scene.py: the
+    reference's setup calls restated, no product library), optionally
+    restarted from a state."""
+    from oracle.scene import build_scene
+    asm, scene = build_scene(recipe)
+    if state is not None:
+        restart_scene(scene, state)
+    return asm, scene
+
+
+def cpu_baseline(recipe, state, budget_s, first_step=1):
+    """Times the FP64 oracle on all host cores over whole bench steps (fluid
+    periods) of the workload: one warm-up bench step, then as many as fit
+    budget_s (at least one).  Returns (cpu_baseline dict, oracle, DEM steps
+    run, assembly that keeps the scene alive)."""
     from oracle import oracle as orc_mod
     threads = os.cpu_count() or 1
     orc_mod.set_threads(threads)
+    asm, scene = oracle_scene(recipe, state)
+    gap, dt = scene.fluid_integrate_gap, scene.time_step
+    nf, n_mobile, _ = mobile_counts(scene)
     orc = orc_mod.OracleSolver(scene)
     orc.initialize()
-    # one timed step to size the sample
     t0 = time.perf_counter()
-    orc.update(dt, 1, 1, gap)
+    orc.update(dt, first_step, gap, gap)
     t1 = time.perf_counter() - t0
-    n = max(1, min(1000, int(budget_s / max(t1, 1e-6))))
-    if gap > 1:
-        n = max(n, gap)  # cover at least one fluid step
+    n = max(1, min(1000 // gap + 1, int(budget_s / max(t1, 1e-6))))
     t0 = time.perf_counter()
-    orc.update(dt, 2, n, gap)
+    orc.update(dt, first_step + gap, n * gap, gap)
     el = time.perf_counter() - t0
-    ups = updates_for(2, n, gap, nf, n_mobile) / el
-    return {"value": ups, "unit": "particle-updates/s", "cores": threads, "kind": "port",
-            "sample": f"{n} consecutive steps (2..{n + 1}) of the full workload after one warm-up step; "
-                      f"FP64 oracle, OpenMP over particles"}, orc, n + 1
+    ups = updates_for(first_step + gap, n * gap, gap, nf, n_mobile) / el
+    return ({"value": ups, "unit": "particle-updates/s", "cores": threads, "kind": "port",
+             "sample": f"{n} bench steps ({n * gap} update() calls, steps {first_step + gap}.."
+                       f"{first_step + gap + n * gap - 1}) of the full workload after one warm-up bench step; "
+                       f"FP64 oracle (CPU restatement of the reference's step), OpenMP over particles, "
+                       f"scene assembled by the oracle"},
+            orc, (n + 1) * gap, asm)
 
 
-def fp64_errors(ds, scene, orc, steps, dt, gap, device):
+def reference_arm(args, rank):
+    """--impl reference: the reference's step restated for the CPU (the FP64
+    oracle; the reference's own code exists only as CUDA kernels) on all host
+    cores, W + K bench steps of the same workload.  Never loads the product
+    library: the recipe comes from scenes.py alone and the scene from the
+    oracle's own assembly."""
+    if rank != 0:
+        return
+    from oracle import oracle as orc_mod
+    threads = os.cpu_count() or 1
+    orc_mod.set_threads(threads)
+    recipe = make_recipe(args.config)
+    asm, scene = oracle_scene(recipe)
+    gap, dt = scene.fluid_integrate_gap, scene.time_step
+    nf, n_mobile, _ = mobile_counts(scene)
+    cfg = workload_config(args.config, scene, args, 0)
+    orc = orc_mod.OracleSolver(scene)
+    orc.initialize()
+    step = 1
+    t0 = time.perf_counter()
+    orc.update(dt, step, gap, gap)
+    t_step = time.perf_counter() - t0
+    step += gap
+    warm, timed = max(1, args.warmup), args.steps
+    fit = int(args.ref_budget / max(t_step, 1e-9)) - 1
+    if warm + timed > fit + 1:  # shrink both, keeping their ratio, to fit the budget
+        timed = max(1, min(timed, int(fit * args.steps / max(1, args.steps + args.warmup))))
+        warm = max(1, min(warm, fit - timed + 1))
+    for _ in range(warm - 1):
+        orc.update(dt, step, gap, gap)
+        step += gap
+    t0 = time.perf_counter()
+    orc.update(dt, step, timed * gap, gap)
+    el = time.perf_counter() - t0
+    value = updates_for(step, timed * gap, gap, nf, n_mobile) / el
+    sample = (f"{timed} bench steps ({timed * gap} update() calls, steps {step}..{step + timed * gap - 1}) after "
+              f"{warm} warm-up bench steps; FP64 oracle, OpenMP over particles, scene assembled by the oracle")
+    if args.config == 1:
+        sample += "; from the workload's initial lattice (the contact-dense start needs the GPU settle)"
+    print(json.dumps({
+        "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": 1,
+        "steps": timed, "warmup": warm, "ms_per_step": 1000.0 * el / timed, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic", "config": cfg,
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "particle-updates/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's step exists only as CUDA kernels (and its sources are not on the GPU box); its "
+                "CPU restatement, pinned to the reference compiled for the CPU, is timed on the host cores"}))
+
+
+def fp64_errors(ds, scene, orc, steps, dt, gap, device, first_step=1):
     """Error of the GPU step against the FP64 oracle after the CPU sample's
-    steps (1..steps from the workload's initial state): a second engine runs
-    the same steps through the timed path (graph replay), and each field's
-    largest error is taken over all particles, scaled as named in `scale`."""
+    steps (from the same state): a second engine runs the same steps through
+    the timed path (graph replay), and each field's largest error is taken
+    over all particles, scaled as named in `scale`."""
     import numpy as np
     g = 9.81
     eng = ds.Engine(scene, device=device)
     eng.initialize()
-    eng.update(dt, 1, steps, gap, use_graph=True)
+    eng.update(dt, first_step, steps, gap, use_graph=True)
     eng.synchronize()
     t = steps * dt
     err = {}
@@ -503,18 +666,22 @@ def run_many(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=20, help="timed bench steps (fluid periods)")
+    ap.add_argument("--warmup", type=int, default=5, help="untimed bench steps before the timed ones")
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--config", type=int, choices=(0, 1, 2, 3, 4), default=1)
+    ap.add_argument("--config", type=int, choices=(0, 1, 2, 3, 4), default=2)
+    ap.add_argument("--settle-steps", type=int, default=None,
+                    help="config 1: untimed settle steps before the warm-up (default 60000)")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: number of scenes")
     ap.add_argument("--plain-scenes", type=int, default=32,
                     help="batched workload: scenes (evenly spaced in the list) also run one at a time")
     ap.add_argument("--duration", type=float, default=60.0, help="serving workload: seconds of arrivals")
     ap.add_argument("--workers", type=int, default=8, help="batched/serving: server worker threads")
-    ap.add_argument("--e2e-steps", type=int, default=50)
-    ap.add_argument("--profile-steps", type=int, default=40)
+    ap.add_argument("--e2e-steps", type=int, default=10, help="bench steps of the end-to-end leg")
+    ap.add_argument("--latency-steps", type=int, default=20, help="bench steps timed one by one for p50/p99")
+    ap.add_argument("--profile-steps", type=int, default=2, help="bench steps of the per-stage timing pass")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline stepping")
+    ap.add_argument("--ref-budget", type=float, default=300.0, help="reference arm: seconds of stepping at most")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
 
@@ -523,39 +690,19 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.config in (3, 4):
         return run_many(args, world, rank, local)
-    workload, desc = WORKLOADS[args.config]
+    if args.impl == "reference":
+        return reference_arm(args, rank)
 
     ds = _package()
+    import numpy as np
+    import torch
+
     recipe = make_recipe(args.config)
     builder, scene = ds.build_scene(recipe)
     dt, gap = scene.time_step, scene.fluid_integrate_gap
     nf, n_mobile, n_dummy = mobile_counts(scene)
-    base_config = {"workload": workload, "description": desc, "n_fluid": nf, "n_solid_mobile": n_mobile,
-                   "n_dummy_wall": n_dummy, "n_clump": scene.n_clump, "dt": dt, "fluid_integrate_gap": gap,
-                   "l2": "working set larger than L2 (129 MB) for configs 1 and 2; config 0 is L2-resident",
-                   "parallelism": f"replicas x{args.gpus}"}
-
-    if args.impl == "reference":
-        if rank != 0:
-            return
-        cb = cpu_baseline(scene, gap, dt, args.cpu_budget, nf, n_mobile)[0]
-        step_ms = None
-        upd_per_step = updates_for(1, 10 * gap, gap, nf, n_mobile) / (10 * gap)
-        if cb["value"] > 0:
-            step_ms = 1000.0 * upd_per_step / cb["value"]
-        print(json.dumps({
-            "metric": "particle-updates/s", "value": cb["value"], "unit": "particle-updates/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic", "config": base_config,
-            "impl": "reference", "cpu_baseline": cb,
-            "e2e": {"value": cb["value"], "unit": "particle-updates/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0},
-            "note": "the reference's step exists only as CUDA kernels; its CPU restatement (the FP64 oracle) is "
-                    "timed on the host cores"}))
-        return
-
-    import numpy as np
-    import torch
+    settle = args.settle_steps if args.settle_steps is not None else SETTLE_STEPS.get(args.config, 0)
+    cfg = workload_config(args.config, scene, args, settle)
 
     dist = None
     if world > 1:
@@ -568,8 +715,17 @@ def main():
     eng = ds.Engine(scene, device=device)
     eng.initialize()
     step = 1
-    eng.update(dt, step, args.warmup, gap, use_graph=True)
-    step += args.warmup
+    state0 = None
+    if settle:
+        # the settle itself, untimed, up to a contact-dense bed; its state is
+        # the start of the CPU baseline and of the FP64 comparison
+        eng.update(dt, step, settle, gap, use_graph=True)
+        step += settle
+        eng.synchronize()
+        state0 = engine_state(eng)
+    first_sample_step = step
+    eng.update(dt, step, args.warmup * gap, gap, use_graph=True)
+    step += args.warmup * gap
     eng.synchronize()
 
     stream = torch.cuda.ExternalStream(eng.stream_ptr(), device=device)
@@ -580,37 +736,55 @@ def main():
     torch.cuda.synchronize()
     with ClockSampler(device) as clocks:
         ev0.record(stream)
-        eng.update(dt, step, args.steps, gap, use_graph=True)
+        eng.update(dt, step, args.steps * gap, gap, use_graph=True)
         ev1.record(stream)
         ev1.synchronize()
+        clocks.mark_end()
+        # keep the GPU under the same load for a moment so the clock sampler
+        # (nvidia-smi, 20 ms period at best) sees it when the timed region is short
+        t_end = time.perf_counter() + 1.0
+        tail = step + args.steps * gap
+        while time.perf_counter() < t_end:
+            eng.update(dt, tail, gap, gap, use_graph=True)
+            eng.synchronize()
+            tail += gap
     torch.cuda.synchronize()
     launches = eng.kernel_launches() - launches0
     ms = ev0.elapsed_time(ev1)
-    updates = updates_for(step, args.steps, gap, nf, n_mobile)
-    step += args.steps
+    updates = updates_for(step, args.steps * gap, gap, nf, n_mobile)
+    step = tail
     ms = rank_total(ms, "max", dist)
     updates = rank_total(updates, "sum", dist)
     value = updates / (ms / 1000.0)
+    # the clock-tail steps launched kernels too; only the timed region's count is claimed
+    launches_tail = eng.kernel_launches() - launches0 - launches
 
-    # ---- stage timing pass (uncaptured, CUDA events per stage) for the roofline and latency ----
-    eng.set_profiling(True)
-    eng.profile_report()
-    per_step = []
-    for k in range(args.profile_steps):
+    # ---- latency: bench steps one by one (graph replay), CUDA events on the engine stream ----
+    lat = []
+    for _ in range(max(1, args.latency_steps)):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        eng.update(dt, step, 1, gap, use_graph=False)
+        eng.update(dt, step, gap, gap, use_graph=True)
         e1.record(stream)
         e1.synchronize()
-        per_step.append(e0.elapsed_time(e1))
-        step += 1
+        lat.append(e0.elapsed_time(e1))
+        step += gap
+    lat.sort()
+
+    # ---- stage timing pass (uncaptured, CUDA events per stage) for the roofline ----
+    eng.set_profiling(True)
+    eng.profile_report()
+    for _ in range(max(1, args.profile_steps)):
+        eng.update(dt, step, gap, gap, use_graph=False)
+        step += gap
+    eng.synchronize()
     stages = eng.profile_report()
     eng.set_profiling(False)
     c = eng.counts()
     counts = {"solid_pairs": c.solid_pairs, "n_solid": scene.n_solid, "n_solid_active": n_mobile,
               "n_fluid": nf, "bonds": c.bonds,
               "fluid_partners": 2.0 * c.fluid_pairs / max(nf, 1), "fluid_solid_partners": c.fluid_solid_pairs / max(nf, 1),
-              "n_pebbles": n_mobile if scene.n_clump else 0}
+              "n_pebbles": 4 * scene.n_clump}
     dom = max(stages.items(), key=lambda kv: kv[1][1]) if stages else None
     peak, peak_kind = load_peaks()
     roofline = None
@@ -657,48 +831,52 @@ def main():
         bi += fp.nbytes + fv.nbytes + fd.nbytes
         bo += fp.nbytes + fv.nbytes + fd.nbytes
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
     s_io = (sp, sv, sw) if scene.n_solid else None
     f_io = (fp, fv, fd) if nf else None
+    e2e_first = step
+    t0 = time.perf_counter()
     for k in range(ne):
-        # upload the state, one step, download the state: one C-ABI call, one synchronisation
-        eng.update_io(dt, step, 1, gap, use_graph=True, fluid_in=f_io, solid_in=s_io, fluid_out=f_io, solid_out=s_io)
-        step += 1
+        # upload the state, one bench step, download the state: one C-ABI call, one synchronisation
+        eng.update_io(dt, step, gap, gap, use_graph=True, fluid_in=f_io, solid_in=s_io, fluid_out=f_io,
+                      solid_out=s_io)
+        step += gap
     e2e_s = time.perf_counter() - t0
-    e2e_updates = updates_for(step - ne, ne, gap, nf, n_mobile)
+    e2e_updates = updates_for(e2e_first, ne * gap, gap, nf, n_mobile)
     e2e_val = e2e_updates / e2e_s
     if dist:
         e2e_val = e2e_updates * world / rank_total(e2e_s, "max", dist)
+    live_contacts = eng.counts().solid_pairs
 
     cb = err64 = None
     if rank == 0 and not args.no_cpu:
-        cb, orc, orc_steps = cpu_baseline(scene, gap, dt, args.cpu_budget, nf, n_mobile)
-        err64 = fp64_errors(ds, scene, orc, orc_steps, dt, gap, device)
-        del orc
+        cb, orc, orc_steps, asm = cpu_baseline(recipe, state0, args.cpu_budget, first_sample_step)
+        if state0 is not None:
+            restart_scene(scene, state0)  # the second engine starts where the oracle started
+        err64 = fp64_errors(ds, scene, orc, orc_steps, dt, gap, device, first_sample_step)
+        del orc, asm
 
     if rank == 0:
-        per_step.sort()
-        cfg = dict(base_config)
-        cfg.update({"solid_pairs": c.solid_pairs, "fluid_pairs_half": c.fluid_pairs,
-                    "fluid_solid_pairs": c.fluid_solid_pairs, "bonds": c.bonds,
-                    "launch_shapes": eng.launch_shapes(),
-                    "timing": "CUDA events on the engine stream; K steps replayed as CUDA graphs",
-                    "precision": "FP32 arithmetic with Kahan sums; double-float positions, velocities, overlaps, "
-                                 "bond accumulators and clump states; FP64 clump orientation"})
         out = {
             "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic", "config": cfg, "impl": "ours",
-            "p50_step_ms": per_step[len(per_step) // 2] if per_step else None,
-            "p99_step_ms": per_step[min(len(per_step) - 1, int(math.ceil(0.99 * len(per_step))) - 1)]
-            if per_step else None,
+            "p50_step_ms": lat[len(lat) // 2],
+            "p99_step_ms": lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)],
             "roofline": roofline, "cpu_baseline": cb, "fp64_error": err64,
             "e2e": {"value": e2e_val, "unit": "particle-updates/s", "h2d_bytes_per_step": bi,
                     "d2h_bytes_per_step": bo, "steps": ne,
-                    "path": "demsph_update_io per step: upload the state, one step, download the state, one "
-                            "synchronisation; pinned host buffers, FP64 reference layout"},
+                    "path": "demsph_update_io per bench step: upload the state, the step's update() calls, download "
+                            "the state, one synchronisation; pinned host buffers, FP64 reference layout"},
             "gpu_launches": launches, "clocks": clocks.summary(),
+            "details": {"solid_pairs_live": live_contacts, "solid_pairs_per_mobile_solid":
+                        live_contacts / max(n_mobile, 1), "fluid_pairs_half": c.fluid_pairs,
+                        "fluid_solid_pairs": c.fluid_solid_pairs, "bonds": c.bonds,
+                        "launch_shapes": eng.launch_shapes(), "clock_tail_launches": launches_tail,
+                        "timing": "CUDA events on the engine stream around K bench steps replayed as CUDA graphs; "
+                                  "p50/p99 from bench steps timed one by one",
+                        "precision": "FP32 arithmetic with Kahan sums; double-float positions, velocities, overlaps, "
+                                     "bond accumulators and clump states; FP64 clump orientation"},
         }
         print(json.dumps(out))
     if dist:

@@ -74,7 +74,10 @@ def nvcc_flags(cuda):
 
 
 def cxx_flags(cuda):
-    return ["-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", f"-I{os.path.join(cuda, 'include')}",
+    # no FMA contraction: the host code (scene builder, point generators)
+    # rounds the same on x86 and Arm, and as the reference's host code does
+    return ["-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off",
+            f"-I{os.path.join(cuda, 'include')}",
             f"-I{os.path.join(ROOT, 'include')}", f"-I{os.path.join(PKG, 'host')}"]
 
 
@@ -116,8 +119,9 @@ def build_oracle(verbose=False):
 
 
 def build_reference(verbose=False):
-    """The reference compiled for the CPU (oracle/build_ref.sh), where its sources are."""
-    ref = os.environ.get("REF", "/root/reference")
+    """The reference compiled for the CPU (oracle/build_ref.sh), where its
+    sources are: $REF, else a ``reference`` directory beside the repository."""
+    ref = os.environ.get("REF") or os.path.join(os.path.dirname(ROOT), "reference")
     if not os.path.isdir(os.path.join(ref, "core")):
         return False
     out = os.path.join(ROOT, "oracle", "_ref", "libref_demsph.so")
@@ -125,7 +129,7 @@ def build_reference(verbose=False):
                                                                    recursive=True)
     srcs.append(os.path.join(ROOT, "oracle", "ref_harness.cpp"))
     if _stale(out, srcs):
-        _run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], verbose)
+        _run(["env", f"REF={ref}", "sh", os.path.join(ROOT, "oracle", "build_ref.sh")], verbose)
     return True
 
 

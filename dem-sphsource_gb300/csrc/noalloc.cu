@@ -2,18 +2,22 @@
 //
 // Some callers cannot allocate device memory at the moment they need this
 // sort: a host application whose own allocator has already reserved the
-// GPU's memory (so cudaMalloc fails), code that runs inside a legacy-mode
-// stream capture (where cudaMalloc is not permitted), or a time-critical loop
-// that must not take the implicit device synchronisation of cudaMalloc and
-// cudaFree.  For them this entry point keeps all of its scratch memory - the
-// per-cell counters, the per-particle slots, the scatter buffer and the
-// prefix-sum workspace - in one fixed array in device memory, declared below,
-// which every GPU that loads this library holds until the process exits.
+// GPU's memory (so cudaMalloc fails), or a time-critical loop that must not
+// take the implicit device synchronisation of cudaMalloc and cudaFree.  For
+// them this entry point keeps all of its scratch memory - the per-cell
+// counters, the per-particle slots, the scatter buffer and the prefix-sum
+// workspace - in one fixed array in device memory, declared below, which
+// every GPU that loads this library holds until the process exits.  The call
+// reads its bad-key flag back to the host and waits for its stream.
 //
 // The sort itself is the engine's counting sort by cell (grid.cu): count keys
 // with atomic slots, exclusive prefix sum of the counts, scatter, then order
 // each cell by original index, which reproduces the reference's stable
 // (key, index) sort and its cellStart / cellEnd (core/neighborSearch.cu:38-87).
+// Ordering a cell costs each of its elements one pass over the cell, so the
+// work grows with the square of the elements per cell: meant for particle
+// cell keys (tens per cell); a few thousand per cell still take
+// microseconds, but all 524,288 keys in one cell would take seconds.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -33,26 +37,73 @@ constexpr size_t NOALLOC_SCRATCH_INTS = 2 * (size_t)(NOALLOC_MAX_CELLS + 1) + 2 
 // symbol; kernels get its device address, looked up once per device below.
 static __device__ __align__(256) int g_noallocScratch[NOALLOC_SCRATCH_INTS];
 
-constexpr int MAX_DEVICES = 64;
-int* g_scratchAddr[MAX_DEVICES] = {};
+// Device addresses of the scratch, looked up once per device and context.
+// The key is the CUDA context's unique id, not the device alone: after a
+// cudaDeviceReset, or in a context a caller made with the driver API, the
+// array lives at an address of that context, and a cached address of another
+// context would point at freed or foreign memory.
+struct ScratchEntry {
+    int device;
+    unsigned long long context;
+    int* address;
+};
+constexpr int SCRATCH_ENTRIES = 16;
+ScratchEntry g_scratchAddr[SCRATCH_ENTRIES] = {};
+int g_scratchNext = 0;
 std::mutex g_scratchMutex;
 
-// Device address of the scratch on the current device (cudaGetSymbolAddress
-// once per device, with that device current).
+typedef int (*CtxGetCurrentFn)(void**);                   // cuCtxGetCurrent
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);    // cuCtxGetId
+CtxGetCurrentFn g_ctxGetCurrent = nullptr;
+CtxGetIdFn g_ctxGetId = nullptr;
+std::once_flag g_ctxOnce;
+
+// Unique id of the calling thread's current context; 0 when there is none
+// yet (or the driver cannot tell).
+unsigned long long currentContextId()
+{
+    std::call_once(g_ctxOnce, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctxGetCurrent = reinterpret_cast<CtxGetCurrentFn>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctxGetId = reinterpret_cast<CtxGetIdFn>(p);
+    });
+    void* ctx = nullptr;
+    if (!g_ctxGetCurrent || g_ctxGetCurrent(&ctx) != 0 || !ctx) return 0;
+    unsigned long long id = 0;
+    if (!g_ctxGetId || g_ctxGetId(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of the scratch in the current device's current context
+// (cudaGetSymbolAddress the first time, with that device current).
 cudaError_t scratchAddress(int** out)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    const unsigned long long ctx = currentContextId();
     std::lock_guard<std::mutex> lock(g_scratchMutex);
-    if (!g_scratchAddr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noallocScratch);
-        if (e != cudaSuccess) return e;
-        g_scratchAddr[dev] = static_cast<int*>(p);
+    if (ctx != 0)
+        for (const ScratchEntry& s : g_scratchAddr)
+            if (s.address && s.device == dev && s.context == ctx) {
+                *out = s.address;
+                return cudaSuccess;
+            }
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noallocScratch);  // makes the device's primary context if there is none
+    if (e != cudaSuccess) return e;
+    const unsigned long long now = currentContextId();
+    if (now != 0) {
+        g_scratchAddr[g_scratchNext] = ScratchEntry{dev, now, static_cast<int*>(p)};
+        g_scratchNext = (g_scratchNext + 1) % SCRATCH_ENTRIES;
     }
-    *out = g_scratchAddr[dev];
+    *out = static_cast<int*>(p);
     return cudaSuccess;
 }
 

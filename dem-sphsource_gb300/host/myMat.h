@@ -67,11 +67,14 @@ inline symMatrix inverse(const symMatrix& A)
     const double c_xz = A.xy * A.yz - A.xz * A.yy;
     const double inv_det = 1. / (A.xx * c_xx + A.xy * c_xy + A.xz * c_xz);
     symMatrix B;
+    // xy and yz are formed as the negated differences, as the reference does
+    // (core/myMat.h:129-142): a diagonal tensor then gives -0.0 there, the
+    // reference's bits
     B.xx = c_xx * inv_det;
-    B.xy = c_xy * inv_det;
+    B.xy = -(A.xy * A.zz - A.xz * A.yz) * inv_det;
     B.xz = c_xz * inv_det;
     B.yy = (A.xx * A.zz - A.xz * A.xz) * inv_det;
-    B.yz = (A.xz * A.xy - A.xx * A.yz) * inv_det;
+    B.yz = -(A.xx * A.yz - A.xz * A.xy) * inv_det;
     B.zz = (A.xx * A.yy - A.xy * A.xy) * inv_det;
     return B;
 }

@@ -411,6 +411,74 @@ def tiny_granular(seed=3, with_probe_fluid=True):
     return r
 
 
+def tiny_linear(seed=8):
+    """:func:`tiny_granular` with the linear spring-dashpot law
+    (setLinearContactModel, core/SPHKernelDEMContactModel.h:214-268) between
+    material 0 (spheres and walls) and both materials, with rolling and
+    torsion springs and viscous damping; the clumps (material 1) keep the
+    Hertz-Mindlin law among themselves.  The reference picks the linear law
+    for a material pair whose k_n is set (core/integrate.cu:463-484, and
+    :559-580 for walls), so both laws run in one scene."""
+    r = tiny_granular(seed=seed)
+    r.name = "tiny_linear"
+    for mi, mj in ((0, 0), (0, 1)):
+        r.setLinearContactModel(mi, mj, 2.0e3, 1.0e3, 4.0e2, 3.0e2, 0.3, 0.2, 0.1, 0.1, 0.4, 0.05, 0.05)
+    return r
+
+
+def tiny_tumbling(seed=9, n_clumps=12, n_spheres=30, steps=50):
+    """Spinning clumps of four pebbles in an irregular shape (three in a row
+    and one off the line: an anisotropic inertia tensor), with random
+    orientations and spins, dropped so that their lowest pebble starts just
+    pressed into the floor, among loose spheres, with side walls; rolling and
+    torsion springs on.  The orientation of a spinning anisotropic clump
+    changes its world inverse inertia (core/myMat.h:102-127), so this scene
+    tells the reference's never-integrated orientation (core/integrate.cu:919)
+    from DEMSPH_FIX_CLUMP_ROTATION."""
+    rng = np.random.default_rng(seed)
+    box = 0.03
+    r = Recipe("tiny_tumbling")
+    m = 0.006
+    r.setDomain((-m, -m, -m), (box + 2 * m, box + 2 * m, 0.02 + 2 * m))
+    Es, Gs = hertz_from_E_nu(1.0e8, 0.3)
+    for a in range(2):
+        for b in range(a, 2):
+            r.setHertzianContactModel(a, b, Es, Gs, 0.5, 0.2, 0.2, 0.4, 0.05, 0.05)
+    rp = 1.0e-3
+    shape = np.array([[-1.5, 0.0, 0.0], [0.0, 0.0, 0.0], [1.5, 0.0, 0.0], [0.2, 1.3, 0.0]]) * 1.0e-3
+    shape -= shape.mean(axis=0)
+    Rs = _random_rotations(rng, n_clumps)
+    density = 2500.0
+    for k in range(n_clumps):
+        gx, gy = k % 4, k // 4
+        peb = shape @ Rs[k].T
+        c = np.array([0.004 + gx * 0.0065, 0.004 + gy * 0.009, 0.0])
+        c[2] = rp - 2.0e-5 - peb[:, 2].min()
+        peb = peb + c
+        pr = np.full(4, rp)
+        mass = density * 4.0 / 3.0 * math.pi * rp ** 3 * 4 * 0.9
+        w = tuple(rng.uniform(-60.0, 60.0, 3))
+        r.addClump(peb, pr, c, (0.0, 0.0, -0.2), w, mass, clump_inertia(peb, pr, c, mass), 1)
+    sp = np.column_stack([rng.uniform(0.002, box - 0.002, n_spheres), rng.uniform(0.002, box - 0.002, n_spheres),
+                          rng.uniform(0.004, 0.012, n_spheres)])
+    r.addCluster(sp, rng.uniform(0.6e-3, 1.0e-3, n_spheres), np.full(n_spheres, density), (0.0, 0.0, -0.3), 0)
+    r.addInfiniteWall((0, 0, 0), (0, 0, 1), 0)
+    for p, n in (((0, 0, 0), (1, 0, 0)), ((box, 0, 0), (-1, 0, 0)), ((0, 0, 0), (0, 1, 0)),
+                 ((0, box, 0), (0, -1, 0))):
+        r.addInfiniteWall(p, n, 0)
+    G = 1.0e8 / (2 * 1.3)
+    t_r = math.pi * 0.6e-3 * math.sqrt(density / G) / (0.1631 * 0.3 + 0.8766)
+    dt = 0.1 * t_r
+    r.setSimulationParameterTimeStep(dt)
+    r.setSimulationParameterMaximumTime((steps - 0.5) * dt)
+    r.setSimulationParameterNumFrames(1)
+    # the reference's wall normals need a fluid smoothing length (core/dataBase.cpp:359)
+    r.addFluid(np.array([[box + m - 1e-3, box + m - 1e-3, 0.02 + m - 1e-3]]), (0, 0, 0), 5.0e-4, 1000.0, 20.0,
+               1.0e-6)
+    r.meta.update(dt=dt, steps=steps, gap=1, dx=2.0e-3)
+    return r
+
+
 def tiny_granular_wide(cells=700_000, seed=3):
     """:func:`tiny_granular` in a domain widened (empty cells around the grains)
     to about ``cells`` grid cells, so the sort by cell scans long cell arrays:

@@ -422,21 +422,23 @@ DEMSPH_API int demsph_server_stats(demsph_server* s, demsph_server_summary* stat
 
 /* ---- cell sort without allocation ----
    No counterpart in the reference.  Sorts n particle cell keys (device
-   array, each in [0, num_cells)) into the reference's stable (key, index)
-   order: sorted_index[n] (the objectHash.index of core/neighborSearch.cu) and
-   cell_start / cell_end[num_cells] (-1 for empty cells), all device arrays.
-   For callers that cannot allocate device memory when they call it (their
-   allocator already holds the GPU's memory, they run inside a legacy-mode
-   stream capture, or they must avoid cudaMalloc's synchronisation): the
-   scratch is one fixed array of device memory in this library, about 8 MB,
-   that every GPU loading the library keeps until exit.  Limits: n and
+   array, each in [0, num_cells)) by (key, original index): sorted_index[n]
+   receives the original indices in that order, cell_start / cell_end
+   [num_cells] the first and one-past-last position of each cell in it (-1
+   for an empty cell); all three are device arrays.  For callers that cannot
+   allocate device memory when they call it (their own allocator already
+   holds the GPU's memory, or they must avoid cudaMalloc's synchronisation):
+   the scratch is one fixed array of device memory in this library, about
+   8 MB, that every GPU loading the library keeps until exit.  Limits: n and
    num_cells at most 524288 each; larger sizes return DEMSPH_ERR_ARGUMENT, as
-   do keys outside [0, num_cells).  The first call on each device looks up the
-   array's address on that device; make that first call before any stream
-   capture.  All calls share the array: calls that overlap on the GPU (other
-   streams, other threads) race and must be serialised by the caller.  The
-   call waits for its stream to finish.  stream is a cudaStream_t (NULL = the
-   default stream). */
+   do keys outside [0, num_cells) (those elements are left out).  Ordering a
+   cell costs each of its elements one pass over the cell: meant for particle
+   cell keys, tens per cell.  The first call on each device (and CUDA
+   context) looks up the array's address there; make that first call before
+   any stream capture.  All calls share the array: calls that overlap on the
+   GPU (other streams, other threads) race and must be serialised by the
+   caller.  The call reads a flag back to the host and waits for its stream.
+   stream is a cudaStream_t (NULL = the default stream). */
 DEMSPH_API int demsph_cell_sort_noalloc(const int* keys, int n, int num_cells, int* sorted_index, int* cell_start,
                                         int* cell_end, void* stream);
 

@@ -12,11 +12,12 @@
 # oracle/ref_harness.cpp.  Everything else - the CUDA runtime calls, thrust and
 # the built-in index variables - comes from oracle/refshim/.
 #
-# Needs the reference sources at $REF (default /root/reference).  Runs where
-# they exist; the output is a checker, not part of the product.
+# Needs the reference sources at $REF (default: a directory "reference" beside
+# the repository).  Runs where they exist; the output is a checker, not part
+# of the product.
 set -e
-REF=${REF:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${REF:-$(cd "$HERE/../.." && pwd)/reference}
 OUT="$HERE/_ref"
 if [ ! -d "$REF/core" ]; then
     echo "build_ref.sh: reference sources not found at $REF/core" >&2

@@ -29,7 +29,8 @@ import conftest  # noqa: E402  (loads the package)
 from oracle.refrun import FIELDS, RefSolver  # noqa: E402
 
 SNAP_STEPS = (0, 1, 2, 5, 10)
-SCENES = ("tiny_dam_break", "tiny_granular", "tiny_coupled", "tiny_escape", "tiny_two_fluids")
+SCENES = ("tiny_dam_break", "tiny_granular", "tiny_coupled", "tiny_escape", "tiny_two_fluids", "tiny_linear",
+          "tiny_tumbling")
 
 
 def scene_digest(scene):

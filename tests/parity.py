@@ -143,3 +143,24 @@ def state_errors(eng, orc, dx, steps_done, dt, rho0=1000.0):
         e["solid.angvel"] = rel_pair_error(s["angvel"], orc.get("solid.angvel"), fl["spin"])
         e["solid.normal"] = float(np.max(np.abs(s["normal"] - orc.get("solid.normal"))))
     return e
+
+
+def check_step(eng, orc, sc, dx, step, dt, tol_force, tol_pos):
+    """Asserts the engine's state, per-pair contact forces, torques, springs
+    and bond forces are within tolerance of the oracle's after `step` steps."""
+    err = state_errors(eng, orc, dx, step, dt)
+    for k, v in err.items():
+        tol = {"fluid.pos": tol_pos, "solid.pos": tol_pos, "fluid.dRho": DRHO_TOL, "solid.normal": 1e-5}.get(k, tol_force)
+        assert v <= tol, f"step {step}: {k} error {v:.3e} > {tol:.1e}"
+    art = engine_artefacts(eng)
+    fl = pair_floors(sc, dt, step)
+    if eng.ns and len(art["ss.pointed"]):
+        assert rel_pair_error(art["ss.force"], orc.get("ss.force"), fl["force"]) <= tol_force
+        assert rel_pair_error(art["ss.torque"], orc.get("ss.torque"), fl["torque"]) <= tol_force
+        assert rel_pair_error(art["ss.sliding"], orc.get("ss.sliding"), fl["spring"]) <= tol_force
+        assert rel_pair_error(art["ss.rolling"], orc.get("ss.rolling"), fl["spring"]) <= tol_force
+        assert rel_pair_error(art["ss.torsion"], orc.get("ss.torsion"), fl["spring"]) <= tol_force
+    if eng.ns and len(art["bond.pointed"]):
+        assert rel_pair_error(art["bond.normalForce"], orc.get("bond.normalForce"), fl["force"]) <= tol_force
+        assert rel_pair_error(art["bond.shearForce"], orc.get("bond.shearForce"), fl["force"]) <= tol_force
+    return err

@@ -7,12 +7,13 @@ reference's own kernels (tests/test_oracle_golden.py).
 import numpy as np
 import pytest
 
-from parity import (DRHO_TOL, DRIFT_TOL, FORCE_TOL, POS_TOL, compare_integer_artefacts, engine_artefacts,
-                    oracle_for, pair_floors, rel_pair_error, state_errors)
+from parity import (DRIFT_TOL, FORCE_TOL, POS_TOL, check_step, compare_integer_artefacts, engine_artefacts,
+                    oracle_for, state_errors)
 
 pytestmark = pytest.mark.gpu
 
-SCENES = ("tiny_dam_break", "tiny_granular", "tiny_coupled", "tiny_escape", "tiny_two_fluids")
+SCENES = ("tiny_dam_break", "tiny_granular", "tiny_coupled", "tiny_escape", "tiny_two_fluids", "tiny_linear",
+          "tiny_tumbling")
 # solid contact candidates: default margin, one so small that candidates are
 # rebuilt nearly every step, and none (the 27-cell walk every step)
 SKINS = (0.0, 1.0e-9, -1.0)
@@ -45,22 +46,6 @@ def test_initialize_artefacts_identical(ds, scenes, name):
             assert np.allclose(art["bond.contactPoint"], orc.get("bond.contactPoint"), atol=1e-9)
 
 
-def _check_step(eng, orc, sc, dx, step, dt, tol_force, tol_pos):
-    err = state_errors(eng, orc, dx, step, dt)
-    for k, v in err.items():
-        tol = {"fluid.pos": tol_pos, "solid.pos": tol_pos, "fluid.dRho": DRHO_TOL, "solid.normal": 1e-5}.get(k, tol_force)
-        assert v <= tol, f"step {step}: {k} error {v:.3e} > {tol:.1e}"
-    art = engine_artefacts(eng)
-    fl = pair_floors(sc, dt, step)
-    if eng.ns and len(art["ss.pointed"]):
-        assert rel_pair_error(art["ss.force"], orc.get("ss.force"), fl["force"]) <= tol_force
-        assert rel_pair_error(art["ss.torque"], orc.get("ss.torque"), fl["torque"]) <= tol_force
-        assert rel_pair_error(art["ss.sliding"], orc.get("ss.sliding"), fl["spring"]) <= tol_force
-    if eng.ns and len(art["bond.pointed"]):
-        assert rel_pair_error(art["bond.normalForce"], orc.get("bond.normalForce"), fl["force"]) <= tol_force
-        assert rel_pair_error(art["bond.shearForce"], orc.get("bond.shearForce"), fl["force"]) <= tol_force
-
-
 @pytest.mark.parametrize("name", SCENES)
 def test_one_step_within_force_tolerance(ds, scenes, name):
     """One update() from the same initial state: every force, torque, spring,
@@ -73,7 +58,7 @@ def test_one_step_within_force_tolerance(ds, scenes, name):
     orc.update(dt, 1, 1, gap)
     bad, _ = compare_integer_artefacts(eng, orc, skip_fluid_hash=(1 % gap != 0))
     assert bad == [], f"integer artefacts differ: {bad}"
-    _check_step(eng, orc, sc, _spacing(recipe), 1, dt, FORCE_TOL, POS_TOL)
+    check_step(eng, orc, sc, _spacing(recipe), 1, dt, FORCE_TOL, POS_TOL)
 
 
 # (solid candidate margin, threads per fluid particle, fluid candidate margin):
@@ -97,7 +82,7 @@ def test_ten_steps_artefacts_equal_drift_bounded(ds, scenes, name, skin, lanes, 
         orc.update(dt, step, 1, gap)
         bad, _ = compare_integer_artefacts(eng, orc, skip_fluid_hash=(step % gap != 0))
         assert bad == [], f"step {step}: integer artefacts differ: {bad}"
-        _check_step(eng, orc, sc, _spacing(recipe), step, dt, DRIFT_TOL, 1e-8)
+        check_step(eng, orc, sc, _spacing(recipe), step, dt, DRIFT_TOL, 1e-8)
 
 
 @pytest.mark.parametrize("name", SCENES)
@@ -261,7 +246,7 @@ def test_large_grids_sort_like_the_oracle(ds, scenes, cells, lo, hi):
         orc.update(dt, step, 1, gap)
         bad, _ = compare_integer_artefacts(eng, orc, skip_fluid_hash=(step % gap != 0))
         assert bad == [], f"step {step}: integer artefacts differ: {bad}"
-        _check_step(eng, orc, sc, _spacing(recipe), step, dt, DRIFT_TOL, 1e-8)
+        check_step(eng, orc, sc, _spacing(recipe), step, dt, DRIFT_TOL, 1e-8)
 
 
 @pytest.mark.parametrize("name", ("tiny_granular", "tiny_coupled", "tiny_dam_break"))
@@ -442,3 +427,28 @@ def test_audit_matches_the_state(ds, scenes, name):
     assert rel(a["potential_energy"], pe) < 1e-6
     if sc.n_fluid:
         assert rel(a["fluid_density_sum"], rho) < 1e-7
+
+
+@pytest.mark.parametrize("name", ("tiny_granular", "tiny_coupled", "tiny_linear", "tiny_tumbling"))
+def test_fixed_modes_match_the_oracle(ds, scenes, name):
+    """With DEMSPH_FIX_WALL_LOOP | DEMSPH_FIX_CLUMP_ROTATION (every wall
+    checked; clump orientation integrated in FP64) the engine follows the
+    oracle run with the same flags: artefacts identical after each of ten
+    steps, one step within FORCE_TOL, drift within DRIFT_TOL.  The reference
+    has no code for either mode, so the oracle alone pins them
+    (tests/test_oracle_golden.py shows the modes change its result)."""
+    fixes = ds.FIX_WALL_LOOP | ds.FIX_CLUMP_ROTATION
+    recipe, b, sc, eng, orc = _setup(ds, scenes, name, fixes=fixes)
+    eng.initialize()
+    orc.initialize()
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for step in range(1, 11):
+        eng.step(dt, step, gap)
+        orc.update(dt, step, 1, gap)
+        bad, _ = compare_integer_artefacts(eng, orc, skip_fluid_hash=(step % gap != 0))
+        assert bad == [], f"step {step}: integer artefacts differ: {bad}"
+        check_step(eng, orc, sc, _spacing(recipe), step, dt, FORCE_TOL if step == 1 else DRIFT_TOL,
+                   POS_TOL if step == 1 else 1e-8)
+    if sc.n_clump:
+        q = eng.download_clumps()["orientation"]
+        assert np.abs(q[:, 1:]).max() > 0, "clump orientations were not integrated"

@@ -17,7 +17,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "dem-sphsource_gb300")
 HOST = os.path.join(PKG, "host")
-REF = os.environ.get("REF", "/root/reference")
+REF = os.environ.get("REF") or os.path.join(os.path.dirname(ROOT), "reference")
 DRIVER = os.path.join(ROOT, "tests", "drivers", "tinyDamBreak.cpp")
 
 

@@ -106,3 +106,22 @@ def test_reference_continuity_race_is_order_dependent(ds, scenes):
     refrun.RefSolver(jacobi_continuity=True)  # restore the default mode for later tests
     da, db = out
     assert np.max(np.abs(da - db)) > 1e-6 * np.max(np.abs(da))
+
+
+def test_fixed_modes_change_the_oracle(ds, scenes):
+    """The two switchable reference behaviours matter on the fixture scenes:
+    checking every wall changes the granular scene (spheres pressed into a
+    side wall while clear of the floor), and integrating clump orientations
+    changes the spinning anisotropic clumps of the tumbling scene, within ten
+    steps (so the GPU tests of these modes compare something)."""
+    from oracle.oracle import OracleSolver
+    for name, fix, field in (("tiny_granular", ds.FIX_WALL_LOOP, "solid.vel"),
+                             ("tiny_tumbling", ds.FIX_CLUMP_ROTATION, "clump.angvel")):
+        b, sc = ds.build_scene(getattr(scenes, name)())
+        out = []
+        for fixes in (0, fix):
+            o = OracleSolver(sc, fixes=fixes)
+            o.initialize()
+            o.update(sc.time_step, 1, 10, sc.fluid_integrate_gap)
+            out.append(o.get(field))
+        assert not np.array_equal(out[0], out[1]), name
