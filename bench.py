@@ -88,17 +88,21 @@ WORKLOADS = {
     0: ("dam_break_48k", "WCSPH dam break: tank 1.6x0.4x0.6 m, column 0.4x0.4x0.3 m, dx 0.01 m, 3-layer walls"),
     1: ("granular_settle_200k_5k", "Hertz-Mindlin settle: 200k lognormal spheres (median 1 mm, sigma 0.2, radii "
                                    "clipped to [0.6, 1.2] mm: a 2.5 mm lattice cannot hold 2 mm radii without "
-                                   "overlaps) + 5k 4-pebble clumps, floor + 4 walls"),
+                                   "overlaps) + 5k 4-pebble clumps, floor wall, box sides of fixed 1 mm spheres "
+                                   "(infinite side walls would hold only grains touching the floor: the reference "
+                                   "stops its wall loop at the first wall not touched)"),
     2: ("coupled_dam_break_1M_64cubes", "1.0M fluid (dx 0.004 m) dam break onto 64 bonded 8^3 sphere cubes; bond "
                                         "strength per cube from 9 levels in [0.5, 2.0] MPa (the reference keys "
                                         "strength by material pair)"),
 }
-SETTLE_STEPS = {1: 60000}  # config 1: untimed steps of the settle before the timed window
+SETTLE_STEPS = {1: 200000}  # config 1: untimed steps of the settle (0.33 s) before the timed window
 
 
 def make_recipe(config):
     sc = _scenes()
-    return {0: sc.dam_break, 1: sc.granular_settle, 2: sc.coupled_dam_break}[config]()
+    if config == 1:
+        return sc.granular_settle(side_walls="spheres")
+    return {0: sc.dam_break, 2: sc.coupled_dam_break}[config]()
 
 
 def mobile_counts(scene):
@@ -284,6 +288,22 @@ def stage_bytes(stage, c):
         "bonds": 160 * Nb,
         "clump_force": 64 * c.get("n_pebbles", 0),
     }
+    if c.get("tiles"):
+        # membership bits: no per-partner list reads; per fluid particle its own
+        # state, its bit words (4 B each) and, per solid partner, the list entry
+        # and the solid's state (96 B); the partners' fluid state is shared by
+        # neighbouring particles' walks (L1 and L2 reads)
+        w = c["bit_words"]
+        table.update({
+            # own ph pl vh vl drho fsc read 72 + drho ph pl written 36 ... (rounded up to whole float4s)
+            "continuity": (128 + 4 * w + 68 * kfs) * Nf,
+            # own ph pl vh vl drho fsc read 72 + acc vh vl ph pl written 80
+            "momentum": (160 + 4 * w + 96 * kfs) * Nf,
+            # own cell ph pl sumW0 drho read 64 + drho written
+            "density_reinit": (72 + 4 * w + 96 * kfs) * Nf,
+            # own cell ph pl read 48 + bits, counts, solid list entries written
+            "fluid_lists": (56 + 4 * w + 4 * kfs) * Nf,
+        })
     return table.get(stage)
 
 
@@ -671,7 +691,7 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--config", type=int, choices=(0, 1, 2, 3, 4), default=2)
     ap.add_argument("--settle-steps", type=int, default=None,
-                    help="config 1: untimed settle steps before the warm-up (default 60000)")
+                    help="config 1: untimed settle steps before the warm-up (default 200000)")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: number of scenes")
     ap.add_argument("--plain-scenes", type=int, default=32,
                     help="batched workload: scenes (evenly spaced in the list) also run one at a time")
@@ -781,10 +801,17 @@ def main():
     stages = eng.profile_report()
     eng.set_profiling(False)
     c = eng.counts()
+    shapes = eng.launch_shapes()
     counts = {"solid_pairs": c.solid_pairs, "n_solid": scene.n_solid, "n_solid_active": n_mobile,
               "n_fluid": nf, "bonds": c.bonds,
               "fluid_partners": 2.0 * c.fluid_pairs / max(nf, 1), "fluid_solid_partners": c.fluid_solid_pairs / max(nf, 1),
-              "n_pebbles": 4 * scene.n_clump}
+              "n_pebbles": 4 * scene.n_clump, "tiles": shapes.get("fluid_bit_lists", 0) > 0}
+    if counts["tiles"]:
+        # a particle's walk candidates: 27 cells of cell volume / particle volume
+        # (a fluid particle's volume is (h / 1.3)^3, its mass rho0 (h / 1.3)^3)
+        h = float(np.ctypeslib.as_array(scene.fluid_smoothing_length, shape=(nf,))[0])
+        per_cell = c.cell_size[0] * c.cell_size[1] * c.cell_size[2] / (h / 1.3) ** 3
+        counts["bit_words"] = math.ceil(27.0 * per_cell / 32.0)
     dom = max(stages.items(), key=lambda kv: kv[1][1]) if stages else None
     peak, peak_kind = load_peaks()
     roofline = None

@@ -85,7 +85,8 @@ class Counts(C.Structure):
 
 
 class LaunchShapes(C.Structure):
-    _fields_ = [("fluid_lanes", _I), ("clump_lanes", _I), ("contact_force_rows", _I)]
+    _fields_ = [("fluid_lanes", _I), ("clump_lanes", _I), ("contact_force_rows", _I), ("fluid_bit_lists", _I),
+                ("fluid_bit_words", _I)]
 
 
 class RunStats(C.Structure):
@@ -481,7 +482,8 @@ class Engine:
         return lanes.value
 
     def launch_shapes(self):
-        """{fluid_lanes, clump_lanes, contact_force_rows} in use."""
+        """{fluid_lanes, clump_lanes, contact_force_rows, fluid_bit_lists, fluid_bit_words} in use
+        (the last two 0 when the fluid lists are lists, not membership bits)."""
         v = LaunchShapes()
         self._chk(self.lib.demsph_get_launch_shapes(self.h, C.byref(v)), "launch_shapes")
         return {n: getattr(v, n) for n, _ in LaunchShapes._fields_}

@@ -60,12 +60,13 @@ def _run(cmd, verbose):
     return r.stdout + r.stderr
 
 
-# Per-file flags.  The fluid pair loops (sph.cu) divide and take square roots
+# Per-file flags.  The fluid pair loops (sph.cu, sph_tiles.cu) divide and take square roots
 # several times per pair; their approximate forms (a few ulp, far inside the
 # stated tolerance against the FP64 oracle) replace the IEEE-rounded ones.
 # The double-float helpers call the correctly rounded intrinsics explicitly
 # and are unaffected.
-FILE_FLAGS = {"sph.cu": ["-prec-div=false", "-prec-sqrt=false"]}
+FILE_FLAGS = {"sph.cu": ["-prec-div=false", "-prec-sqrt=false"],
+              "sph_tiles.cu": ["-prec-div=false", "-prec-sqrt=false"]}
 
 
 def nvcc_flags(cuda):

@@ -80,7 +80,13 @@ void splitPosition(const DeviceState& d, double3 p, int4& c, float4& h, float4& 
     for (int a = 0; a < 3; ++a) {
         const double u = (q[a] - d.minB[a]) / d.cs[a];
         const int k = u >= 0 ? (int)u : (int)std::floor(u);
-        const double o = q[a] - (d.minB[a] + (double)k * d.cs[a]);
+        double o = q[a] - (d.minB[a] + (double)k * d.cs[a]);
+        // A point on a cell boundary (a lattice of wall particles can put
+        // some exactly there) gets the reference's cell from the rounded
+        // quotient above, while the offset, rounded too, may fall just outside
+        // [0, cs) and would move the point to the neighbouring cell at the next
+        // hash: keep it inside (a shift of at most ~1e-14 of the cell size).
+        if (u >= 0.0) o = std::min(std::max(o, 0.0), d.cs[a] * (1.0 - 0x1p-44));
         ci[a] = k;
         const dfl s = df_from_double(o);
         hi[a] = s.hi;
@@ -149,7 +155,8 @@ int checkDevice(demsph_engine* e, int dev)
 void allocFluidLists(demsph_engine* e)
 {
     DeviceState& d = e->d;
-    d.ff = dalloc<unsigned>((size_t)d.kff * d.nf, e->owned, e->stream, false);
+    // in tile mode the fluid list exists only for exports (made on demand)
+    if (!d.fluidTiles) d.ff = dalloc<unsigned>((size_t)d.kff * d.nf, e->owned, e->stream, false);
     d.fs = dalloc<int>((size_t)d.kfs * d.nf, e->owned, e->stream, false);
     if (e->debug & 1) d.fsPairForce = dalloc<float4>((size_t)d.kfs * d.nf, e->owned, e->stream);
 }
@@ -174,6 +181,60 @@ void allocContactLists(demsph_engine* e)
         d.springIn[k] = dalloc<float4>(c, e->owned, e->stream);
         for (int p = 0; p < 2; ++p) d.springOut[p][k] = dalloc<float4>(c, e->owned, e->stream);
     }
+}
+
+// Tile mode of the fluid lists and pair loops (sph_tiles.cu) is used when
+// every fluid particle has the same parameters, the grid has at least three
+// cells along every axis (the walk's cells are then distinct), every particle
+// starts inside the domain (a particle outside it sends the lists to the
+// reference's walk), the walk is not asked for (fluid_verlet_skin < 0), and
+// DEMSPH_FLUID_TILES=1 is set in the environment (the list kernels measured
+// faster, so they stay the default).
+bool tileModeWanted(const demsph_scene* sc, const DeviceState& d, const demsph_options& o)
+{
+    const char* v = std::getenv("DEMSPH_FLUID_TILES");
+    if (!(v && v[0] == '1') || o.fluid_verlet_skin < 0 || sc->n_fluid <= 0) return false;
+    if (d.grid.gx < 3 || d.grid.gy < 3 || d.grid.gz < 3) return false;
+    for (int i = 1; i < sc->n_fluid; ++i)
+        if (sc->fluid_smoothing_length[i] != sc->fluid_smoothing_length[0] || sc->fluid_rho0[i] != sc->fluid_rho0[0] ||
+            sc->fluid_sound_speed[i] != sc->fluid_sound_speed[0] || sc->fluid_nu[i] != sc->fluid_nu[0])
+            return false;
+    const int g[3] = {d.grid.gx, d.grid.gy, d.grid.gz};
+    auto inside = [&](const double* p, int n) {
+        for (int i = 0; i < n; ++i)
+            for (int a = 0; a < 3; ++a) {
+                const double u = (p[3 * i + a] - d.minB[a]) / d.cs[a];
+                if (!(u >= 0.0) || (int)u >= g[a]) return false;
+            }
+        return true;
+    };
+    return inside(sc->fluid_position, sc->n_fluid) && inside(sc->solid_position, sc->n_solid);
+}
+
+// Bit words per particle from the initial fluid cells: room for the largest
+// walk (with a margin for compression; more is added on overflow).
+void sizeTiles(demsph_engine* e, const std::vector<int4>& cell)
+{
+    DeviceState& d = e->d;
+    const GridDev& g = d.grid;
+    std::vector<int> count((size_t)g.num, 0);
+    for (const int4& c : cell) count[((size_t)c.z * g.gy + c.y) * g.gx + c.x]++;
+    int most = 0;
+    for (int z = 0; z < g.gz; ++z)
+        for (int y = 0; y < g.gy; ++y)
+            for (int x = 0; x < g.gx; ++x) {
+                if (!count[((size_t)z * g.gy + y) * g.gx + x]) continue;
+                int walk = 0;
+                for (int dz = -1; dz <= 1; ++dz)
+                    for (int dy = -1; dy <= 1; ++dy)
+                        for (int dx = -1; dx <= 1; ++dx) {
+                            const int X = x + dx, Y = y + dy, Z = z + dz;
+                            if (X < 0 || X >= g.gx || Y < 0 || Y >= g.gy || Z < 0 || Z >= g.gz) continue;
+                            walk += count[((size_t)Z * g.gy + Y) * g.gx + X];
+                        }
+                most = std::max(most, walk);
+            }
+    d.kbits = (most + most / 4 + 31) / 32 + 1;
 }
 
 // ---- stage timing ----
@@ -204,6 +265,7 @@ struct StageTimer {
 // (launchContactForces).
 void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = false, bool detect = true)
 {
+    e->keysAdvanced = false;  // this search's keys are the current ones until an integration rehashes
     const int npar = e->par ^ 1;  // the parity of the list this step builds
     DeviceState d = e->d;
     if (endView) {
@@ -222,9 +284,12 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = fa
     // their work is not needed.  (Conditional graph nodes in place of these
     // launches measured slower on GB300, alone and with many scenes.)
     if (fluidStep) {
+        // tile mode sorts the fluids by cell every fluid step (its tiles are
+        // the reference's walk cells); frebuild, never cleared in tile mode,
+        // also has the solids sorted on every fluid step
         TIMED("fluid_hash_reorder");
-        launchFluidHash(d, e->forceWalk, s);
-        launchFluidReorder(d, e->forceWalk, s);
+        launchFluidHash(d, e->forceWalk || d.fluidTiles, s);
+        launchFluidReorder(d, e->forceWalk || d.fluidTiles, s);
     }
     if (solidsMove || e->forceWalk) {
         TIMED("solid_hash_sort");
@@ -233,7 +298,11 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = fa
         e->solidSortStale = false;
     }
     if (fluidStep) {
-        if (e->forceWalk) {
+        if (d.fluidTiles) {
+            // membership bits and solid partner lists of this step, on the tiles
+            TIMED("fluid_lists");
+            launchFluidTileLists(d, s);
+        } else if (e->forceWalk) {
             TIMED("fluid_lists");
             launchFluidWalk(d, true, s);
         } else {
@@ -318,6 +387,7 @@ void stageContact(demsph_engine* e, double dt, bool withClumpForce = true)
 
 void stageAfter(demsph_engine* e, double dt, bool clumpForce = false, bool countStep = false)
 {
+    e->keysAdvanced = true;  // the rehash keeps the search's keys in skeySearch
     TIMED("integrate_after");
     launchSolidIntegrate(e->d, dt, INTEGRATE_AFTER, e->par, clumpForce, countStep, e->stream);
 }
@@ -455,7 +525,24 @@ void grow(demsph_engine* e, int status)
         d.coupCap = (int)std::min<long long>(2000000000LL, (long long)(need * 1.5) + 1024);
         d.coupList = dalloc<int>(d.coupCap, e->owned, e->stream);
     }
+    if (status & ST_FBITS_OVERFLOW) {
+        int need = 0;
+        CK(cudaMemcpyAsync(&need, d.need + 4, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        CK(cudaMemsetAsync(d.need + 4, 0, sizeof(int), e->stream));
+        void* p = d.fbits;
+        freeOne(e, p);
+        d.kbits = std::max(2 * d.kbits, (need + 31) / 32 + 1);
+        d.fbits = dalloc<unsigned>((size_t)d.kbits * d.nf, e->owned, e->stream, false);
+    }
     if (status & ST_SPLIT_CONTACTS) e->mergeContacts = false;  // the lists come from the walk from now on
+    if ((status & ST_MODE_CHANGE) && d.fluidTiles) {
+        // a particle left the domain: the lists come from the reference's walk
+        // (the list kernels) from now on
+        d.fluidTiles = 0;
+        if (!d.ff) d.ff = dalloc<unsigned>((size_t)d.kff * d.nf, e->owned, e->stream, false);
+        if (!d.fvc) allocFluidCandidates(e);
+    }
     if (status & ST_MODE_CHANGE) {
         // the abandoned step may have counted some particles into cells
         CK(cudaMemsetAsync(d.scellCount, 0, sizeof(int) * d.grid.num, e->stream));
@@ -466,7 +553,8 @@ void grow(demsph_engine* e, int status)
 }
 
 constexpr int ALL_OVERFLOWS = ST_FF_OVERFLOW | ST_FS_OVERFLOW | ST_SS_OVERFLOW | ST_COUPLE_OVERFLOW |
-                              ST_VERLET_OVERFLOW | ST_MODE_CHANGE | ST_FVERLET_OVERFLOW | ST_SPLIT_CONTACTS;
+                              ST_VERLET_OVERFLOW | ST_MODE_CHANGE | ST_FVERLET_OVERFLOW | ST_SPLIT_CONTACTS |
+                              ST_FBITS_OVERFLOW;
 
 // Neighbour search of the staged API: synchronises once, grows and retries.
 int neighborSearchChecked(demsph_engine* e, int iStep, int gap)
@@ -663,14 +751,21 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.fcellStart = dalloc<int>((size_t)d.grid.num + 1, e->owned, e->stream);
             d.ffc = dalloc<int>(nf, e->owned, e->stream);
             d.fsc = dalloc<int>(nf, e->owned, e->stream);
+            d.fluidTiles = tileModeWanted(sc, d, o) ? 1 : 0;
             allocFluidLists(e);
-            // Verlet candidates of the fluid lists
+            // Verlet candidates of the fluid lists (list mode)
             d.kvf = d.kff + d.kff / 2;
             d.kvs = d.kfs + d.kfs / 2;
             d.fvcn = dalloc<int>(nf, e->owned, e->stream);
             d.fvsn = dalloc<int>(nf, e->owned, e->stream);
             d.fvref = dalloc<float4>(nf, e->owned, e->stream);
-            allocFluidCandidates(e);
+            if (d.fluidTiles) {
+                sizeTiles(e, cell);
+                d.fbits = dalloc<unsigned>((size_t)d.kbits * nf, e->owned, e->stream, false);
+                d.fwalk = dalloc<int>(nf, e->owned, e->stream);
+            } else {
+                allocFluidCandidates(e);
+            }
             d.fhmax = (float)mf;
             d.fskin = (float)(o.fluid_verlet_skin > 0 ? o.fluid_verlet_skin : 0.2 * mf);
             d.frebuild = dalloc<int>(1, e->owned, e->stream);
@@ -753,6 +848,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.srad = dalloc<float4>(ns, e->owned, e->stream);
             d.sflags = dalloc<int4>(ns, e->owned, e->stream);
             d.skey = dalloc<int>(ns, e->owned, e->stream);
+            d.skeySearch = dalloc<int>(ns, e->owned, e->stream);
             d.sslotInCell = dalloc<int>(ns, e->owned, e->stream);
             d.ssorted = dalloc<int>(ns, e->owned, e->stream);
             d.ssortTmp = dalloc<int>(ns, e->owned, e->stream);
@@ -799,6 +895,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.rowsAreSolids = d.nrow == ns ? 1 : 0;
             for (int r = 0; r < d.nrow && d.rowsAreSolids; ++r) d.rowsAreSolids = rowSolid[r] == r;
             d.scentre = dalloc<int4>(d.nrow, e->owned, e->stream);
+            d.scentreSearch = dalloc<int4>(d.nrow, e->owned, e->stream);
             if (ns > 0) CK(cudaMemcpyAsync(d.srow, srow.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, e->stream));
             if (d.nrow > 0)
                 CK(cudaMemcpyAsync(d.rowSolid, rowSolid.data(), sizeof(int) * d.nrow, cudaMemcpyHostToDevice, e->stream));
@@ -818,7 +915,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             d.svref = dalloc<float4>(ns, e->owned, e->stream);
             d.rebuild = dalloc<int>(2, e->owned, e->stream);
             d.slowMode = dalloc<int>(1, e->owned, e->stream);
-            d.need = dalloc<int>(4, e->owned, e->stream);
+            d.need = dalloc<int>(5, e->owned, e->stream);
             d.rowStats = dalloc<int>(3, e->owned, e->stream);
             d.gridBar = dalloc<unsigned>(2, e->owned, e->stream);
             {
@@ -1324,6 +1421,8 @@ int demsph_get_launch_shapes(const demsph_engine* e, demsph_launch_shapes* out)
     out->fluid_lanes = e->d.lanes;
     out->clump_lanes = e->d.clumpLanes;
     out->contact_force_rows = e->d.forceRows;
+    out->fluid_bit_lists = e->d.fluidTiles ? 1 : 0;
+    out->fluid_bit_words = e->d.fluidTiles ? e->d.kbits : 0;
     return DEMSPH_OK;
 }
 

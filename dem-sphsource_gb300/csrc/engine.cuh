@@ -27,6 +27,7 @@ enum StatusBits : int {
     ST_FVERLET_OVERFLOW = 64,// a fluid particle has more list candidates than it holds
     ST_BARRIER_TIMEOUT = 128,// a grid barrier of a cooperative launch gave up waiting (an error)
     ST_SPLIT_CONTACTS = 256, // the one-launch contact list + forces met the walk mode: redo the step in two
+    ST_FBITS_OVERFLOW = 512, // a fluid particle's walk has more candidates than its membership bits hold
 };
 
 // Neighbour list entries.  A fluid partner entry holds the partner's slot j,

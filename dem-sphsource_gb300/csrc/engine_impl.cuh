@@ -81,6 +81,10 @@ struct demsph_engine {
     // The step the next attempt starts with already had its before-contact
     // half applied (a fused pass ran before its neighbour search overflowed).
     bool resumeOpened = false;
+    // An integration has rehashed the solids since the last neighbour search:
+    // the keys and walk centres of that search are in skeySearch /
+    // scentreSearch (exports read them there)
+    bool keysAdvanced = false;
     demsph_run_stats runStats{};
     std::vector<CachedGraph> graphs;
     int graphGap = 0;

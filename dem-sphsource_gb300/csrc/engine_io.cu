@@ -579,9 +579,10 @@ int demsph_export_cell_hash(demsph_engine* e, int which, int* value, int* index,
         }
     } else {
         // the solids' keys are computed every step, their device-side sort only
-        // when a list needs it: the (key, index) order is restored here
+        // when a list needs it: the (key, index) order is restored here, from
+        // the keys the last neighbour search used
         std::vector<int> key, order(n);
-        d2h(key, d.skey, n);
+        d2h(key, e->keysAdvanced ? d.skeySearch : d.skey, n);
         for (int i = 0; i < n; ++i) order[i] = i;
         std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
         cs.assign((size_t)d.grid.num + 1, 0);
@@ -612,6 +613,20 @@ int demsph_export_fluid_pairs(demsph_engine* e, int* prefix, int* pointed, int* 
     const int n = d.nf;
     std::vector<unsigned> ff;
     std::vector<int> ffc, id, slot;
+    if (d.fluidTiles && n > 0) {
+        // tile mode keeps the lists as membership bits: write them out as list
+        // entries (in a buffer made for exports) first
+        d2h(ffc, d.ffc, n);
+        const int most = *std::max_element(ffc.begin(), ffc.end());
+        if (!d.ff || most > d.kff) {
+            void* p = d.ff;
+            freeOne(e, p);
+            d.kff = std::max(d.kff, most);
+            d.ff = dalloc<unsigned>((size_t)d.kff * n, e->owned, e->stream, false);
+        }
+        launchBitsToLists(d, e->stream);
+        CK(cudaStreamSynchronize(e->stream));
+    }
     d2h(ff, d.ff, (size_t)d.kff * n);
     d2h(ffc, d.ffc, n);
     d2h(id, d.fid, n);
@@ -711,8 +726,8 @@ int demsph_export_solid_pairs(demsph_engine* e, int* prefix, int* pointed, int* 
     d2h(rs, d.rowSolid, nr);
     const bool walkOrder = e->walkOrder[par];
     if (!walkOrder) {
-        d2h(key, d.skey, ns);
-        d2h(centre, d.scentre, nr);
+        d2h(key, e->keysAdvanced ? d.skeySearch : d.skey, ns);
+        d2h(centre, e->keysAdvanced ? d.scentreSearch : d.scentre, nr);
     }
     std::vector<float4> F, T, S0, S1, S2;
     const size_t all = (size_t)C * nr;

@@ -143,9 +143,14 @@ __global__ void kSolidHash(DeviceState d, RunIf sortNow)
     d.sph[i] = h;
     d.spl[i] = l;
     d.skey[i] = key;
+    d.skeySearch[i] = key;  // this search uses these keys
     if (sortNow.active()) d.sslotInCell[i] = atomicAdd(&d.scellCount[key], 1);
     const int row = d.srow[i];
-    if (row >= 0) d.scentre[row] = make_int4(truncAxis(c.x, h.x, l.x), truncAxis(c.y, h.y, l.y), truncAxis(c.z, h.z, l.z), 0);
+    if (row >= 0) {
+        const int4 centre = make_int4(truncAxis(c.x, h.x, l.x), truncAxis(c.y, h.y, l.y), truncAxis(c.z, h.z, l.z), 0);
+        d.scentre[row] = centre;
+        d.scentreSearch[row] = centre;
+    }
     if (key == d.grid.num - 1 && row >= 0 && !*d.slowMode) {
         // a solid that can touch others left the domain: from now on the lists
         // come from the reference's walk, which finds it through the overflow

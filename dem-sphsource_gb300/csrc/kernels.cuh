@@ -145,6 +145,25 @@ inline void launchStep(void (*kernel)(KArgs...), unsigned grid, unsigned block, 
     cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
+// launchStep with dynamic shared memory.
+template <typename... KArgs, typename... Args>
+inline void launchStepSmem(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                           Args... args)
+{
+    ++t_kernelLaunches;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = overlapLaunches() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 struct DeviceState {
     GridDev grid;
     double minB[3], cs[3];   // FP64 grid, for import and export
@@ -197,7 +216,16 @@ struct DeviceState {
     float fhmax;             // largest fluid smoothing length
     int* frebuild;           // 1: fluid candidates are stale (a fluid or solid moved fskin / 2)
     int* fslowMode;          // 1: fluid lists from the 27-cell walk every fluid step
-    // lists (column-major, stride nf)
+    // Membership bits (sph_tiles.cu, opt-in): with fluidTiles set the fluids
+    // are sorted by cell every fluid step and list membership is kept as one
+    // bit per candidate of each particle's 27-cell walk ([w * nf + i], kbits
+    // words); the pair loops iterate the bits
+    int fluidTiles;
+    unsigned* fbits;
+    int* fwalk;              // candidates of each fluid slot's walk
+    int kbits;
+    // lists (column-major, stride nf); with membership bits ff is made from
+    // the bits for exports only
     unsigned* ff;
     int* ffc;
     int* fs;
@@ -249,6 +277,12 @@ struct DeviceState {
     int moveFirst;           // >= 0: the list is moveFirst, moveFirst + 1, ... (moveList is not read)
     int* rowSolid;           // row -> solid
     int4* scentre;           // per row: centre cell of the reference's 27-cell walk at the last hash (exports)
+    // The keys and walk centres the last neighbour search used: the closing
+    // integration of a step rehashes the solids it moved (keys for the next
+    // search) and keeps the previous values here, which the reference's
+    // objectHash and list order of that step are (exports)
+    int* skeySearch;
+    int4* scentreSearch;
     int scap;                // slots per row
     int* fwd[2];             // partner id B of each forward slot
     int* fcnt[2];            // forward slots used per row
@@ -274,7 +308,8 @@ struct DeviceState {
                              // set by the drift that ends the step before, cleared after the step
     int* slowMode;           // 1: lists come from the 27-cell walk every step (grid too small, or a solid left the domain)
     int* need;               // [0] most contacts of a row, [1] most candidates of a row,
-                             // [2] / [3] most fluid / solid candidates of a fluid particle (for growing)
+                             // [2] / [3] most fluid / solid candidates of a fluid particle,
+                             // [4] most walk candidates of a fluid particle in tile mode (for growing)
     // rows per warp of the contact-force kernel (4..32): fewer rows when rows
     // hold many items, so that busy scenes still fill the GPU; results do not
     // depend on it
@@ -415,6 +450,17 @@ int selftestBarrier(int missing, int* statusOut);
 void launchFluidWalk(const DeviceState& d, bool walk, cudaStream_t s);
 void launchFluidFilter(const DeviceState& d, cudaStream_t s);
 void launchCouplingLists(const DeviceState& d, cudaStream_t s);
+
+// sph_tiles.cu: the fluid lists as membership bits and the pair loops over
+// them (opt-in).  launchFluidTileLists (fluid steps, after the reorder and
+// the solid sort): the membership bits and the solid partner lists.
+void launchFluidTileLists(const DeviceState& d, cudaStream_t s);
+void launchTileContinuity(const DeviceState& d, int which, double dtf, cudaStream_t s, bool countStep);
+void launchTileMomentum(const DeviceState& d, double dtf, cudaStream_t s);
+void launchTileShepard(const DeviceState& d, int iStep, cudaStream_t s);
+// The reference's fluid list (entries in walk order, as the list kernels
+// write them) from the membership bits, for exports.
+void launchBitsToLists(const DeviceState& d, cudaStream_t s);
 // The contact rows of the step, each row first rebuilding its candidates when
 // they are stale (launchContactDetect; forceWalk: from the reference's 27-cell
 // walk, in the reference's order).
@@ -523,8 +569,10 @@ __device__ __forceinline__ void rehashSolidTo(const DeviceState& d, int i, int r
     d.scell[i] = c;
     outH[i] = h;
     outL[i] = l;
+    d.skeySearch[i] = d.skey[i];
     d.skey[i] = key;
     if (row >= 0) {
+        d.scentreSearch[row] = d.scentre[row];
         d.scentre[row] = make_int4(truncAxis(c.x, h.x, l.x), truncAxis(c.y, h.y, l.y), truncAxis(c.z, h.z, l.z), 0);
         if (key == d.grid.num - 1) *(volatile int*)d.slowMode = 1;
     }

@@ -202,9 +202,18 @@ def clump_inertia(pebbles, radii, centroid, mass):
 
 def granular_settle(n_spheres=200_000, n_clumps=5_000, box=(0.1, 0.1), spacing=2.5e-3, r_median=1.0e-3,
                     sigma=0.2, r_clip=(0.6e-3, 1.2e-3), E=1.0e8, poisson=0.3, res=0.5, mu_s=0.4, density=2500.0,
-                    steps=20_000, jitter=0.05, seed=1, z0=None, velocity=(0, 0, 0), name=None):
+                    steps=20_000, jitter=0.05, seed=1, z0=None, velocity=(0, 0, 0), name=None,
+                    side_walls="infinite"):
     """Dry Hertz-Mindlin settle: lognormal spheres on a jittered lattice plus 4-pebble
-    clumps (tetrahedral, uniformly random orientation) above them, on a floor wall."""
+    clumps (tetrahedral, uniformly random orientation) above them, on a floor wall.
+
+    side_walls: "infinite" adds four infinite walls after the floor; "spheres"
+    lines the four sides with fixed spheres (density 0, radius 1 mm, touching
+    on a square lattice) instead.  The reference's wall loop stops at the first
+    wall a particle does not touch (core/integrate.cu:540), so infinite side
+    walls after the floor hold only particles that touch the floor: a settling
+    column leaks through them; walls of fixed spheres contain it under the
+    reference's own rules."""
     rng = np.random.default_rng(seed)
     r = Recipe(name or f"granular_settle_{n_spheres}_{n_clumps}")
     nx, ny = int(round(box[0] / spacing)), int(round(box[1] / spacing))
@@ -243,9 +252,22 @@ def granular_settle(n_spheres=200_000, n_clumps=5_000, box=(0.1, 0.1), spacing=2
         mass = density * 4.0 / 3.0 * math.pi * r_p ** 3 * 4 * 0.8  # overlapping pebbles: ~80% of 4 spheres
         r.addClump(peb, pr, c, (0, 0, 0), (0, 0, 0), mass, clump_inertia(peb, pr, c, mass), 1)
     r.addInfiniteWall((0, 0, 0), (0, 0, 1), 0)
-    for p, n in (((0, 0, 0), (1, 0, 0)), ((box[0], 0, 0), (-1, 0, 0)), ((0, 0, 0), (0, 1, 0)),
-                 ((0, box[1], 0), (0, -1, 0))):
-        r.addInfiniteWall(p, n, 0)
+    if side_walls == "infinite":
+        for p, n in (((0, 0, 0), (1, 0, 0)), ((box[0], 0, 0), (-1, 0, 0)), ((0, 0, 0), (0, 1, 0)),
+                     ((0, box[1], 0), (0, -1, 0))):
+            r.addInfiniteWall(p, n, 0)
+    else:
+        rw = 1.0e-3
+        zs = np.arange(rw, height + rw, 2 * rw)
+        ys = np.arange(-rw, box[1] + 2 * rw, 2 * rw)
+        xs = np.arange(rw, box[0], 2 * rw)
+        Y, Z = np.meshgrid(ys, zs, indexing="ij")
+        X, Z2 = np.meshgrid(xs, zs, indexing="ij")
+        walls = [np.stack([np.full(Y.size, -rw), Y.ravel(), Z.ravel()], 1),
+                 np.stack([np.full(Y.size, box[0] + rw), Y.ravel(), Z.ravel()], 1),
+                 np.stack([X.ravel(), np.full(X.size, -rw), Z2.ravel()], 1),
+                 np.stack([X.ravel(), np.full(X.size, box[1] + rw), Z2.ravel()], 1)]
+        r.addSolid(np.concatenate(walls), (0, 0, 0), rw, 0.0, 0)
     rmin = float(radii.min())
     G = E / (2 * (1 + poisson))
     t_r = math.pi * rmin * math.sqrt(density / G) / (0.1631 * poisson + 0.8766)
@@ -334,7 +356,7 @@ def sized_granular(n_particles, steps=1000, seed=0):
     four-pebble clump per 40 spheres)."""
     n_clumps = max(1, n_particles // 44)
     return granular_settle(n_spheres=n_particles - 4 * n_clumps, n_clumps=n_clumps, steps=steps, seed=seed,
-                           name=f"granular_{n_particles}")
+                           name=f"granular_{n_particles}", side_walls="spheres")
 
 
 def batch_mix(n_scenes=256, n_range=(2000, 60000), sph_fraction=0.6, height_range=(0.2, 0.5), steps=1000,

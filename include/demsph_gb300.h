@@ -263,11 +263,15 @@ DEMSPH_API int demsph_update_io(demsph_engine* e, double dt, int first_step, int
 DEMSPH_API int demsph_autotune(demsph_engine* e, int* lanes_out);
 /* Launch shapes in use (no counterpart in the reference, whose kernels use fixed
    block sizes): threads per fluid particle, threads per clump, and contact rows
-   per warp of the contact-force kernel. */
+   per warp of the contact-force kernel; whether the fluid lists are kept as
+   membership bits (DEMSPH_FLUID_TILES=1 at creation) and their words per
+   fluid particle (both 0 with the list kernels). */
 typedef struct demsph_launch_shapes {
     int fluid_lanes;
     int clump_lanes;
     int contact_force_rows;
+    int fluid_bit_lists;
+    int fluid_bit_words;
 } demsph_launch_shapes;
 DEMSPH_API int demsph_get_launch_shapes(const demsph_engine* e, demsph_launch_shapes* out);
 /* Counters of the engine's update runs since creation (no counterpart in the

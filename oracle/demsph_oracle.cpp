@@ -1220,6 +1220,8 @@ long oracle_get(void* h, const char* name, void* out, long cap)
     if (s == "clump.acc") return v3(o.cacc);
     if (s == "clump.angvel") return v3(o.cw);
     if (s == "clump.torque") return v3(o.ctorq);
+    if (s == "clump.orientation")  // q0 q1 q2 q3 per clump
+        return copyOut(o.cq.empty() ? nullptr : &o.cq[0].q0, 4 * (long)o.cq.size(), out, cap) / 4;
     if (s == "ff.pointed") return vi(o.ff.pointed);
     if (s == "ff.pointing") return vi(o.ff.pointing);
     if (s == "ff.hash.index") return vi(o.ff.rev.index);

@@ -14,7 +14,11 @@ import os
 
 import numpy as np
 
-from .refrun import FIELDS
+from .refrun import FIELDS as REF_FIELDS
+
+# the reference's arrays plus what only the oracle keeps (the clump
+# orientation: the reference never integrates it)
+FIELDS = dict(REF_FIELDS, **{"clump.orientation": (np.float64, 4)})
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle_demsph.so")
@@ -104,4 +108,4 @@ class OracleSolver:
             raise KeyError(name)
         out = np.zeros(n * comp, dtype=dt)
         self.lib.oracle_get(self.h, name.encode(), out.ctypes.data_as(_P), n * comp)
-        return out.reshape(n, comp) if comp == 3 else out
+        return out.reshape(n, comp) if comp > 1 else out

@@ -85,7 +85,7 @@ def test_granular_200k_one_step_from_a_contact_dense_bed(ds, scenes):
     step: the contact list (several contacts per sphere) is identical and
     every contact force, torque and spring is within FORCE_TOL."""
     bench = _bench()
-    recipe = scenes.granular_settle()
+    recipe = bench.make_recipe(1)  # the benchmark's settle: floor wall, sides of fixed spheres
     b, sc = ds.build_scene(recipe)
     dt, gap = sc.time_step, sc.fluid_integrate_gap
     settle = ds.Engine(sc)

@@ -61,17 +61,21 @@ def test_one_step_within_force_tolerance(ds, scenes, name):
     check_step(eng, orc, sc, _spacing(recipe), 1, dt, FORCE_TOL, POS_TOL)
 
 
-# (solid candidate margin, threads per fluid particle, fluid candidate margin):
-# the defaults, the solid margin variants, one thread per fluid particle (what
-# large scenes use), fluid candidates rebuilt every fluid step and the fluid walk
-VARIANTS = [(s, 0, 0.0) for s in SKINS] + [(0.0, 1, 0.0), (0.0, 0, 1.0e-9), (0.0, 0, -1.0)]
+# (solid candidate margin, threads per fluid particle, fluid candidate margin,
+# membership bits): the defaults (list kernels), the solid margin variants,
+# one thread per fluid particle (what large scenes use), fluid candidates
+# rebuilt every fluid step, the fluid walk, and the fluid lists kept as
+# membership bits (DEMSPH_FLUID_TILES=1) with two solid margins
+VARIANTS = [(s, 0, 0.0, "0") for s in SKINS] + [(0.0, 1, 0.0, "0"), (0.0, 0, 1.0e-9, "0"), (0.0, 0, -1.0, "0"),
+                                                 (0.0, 0, 0.0, "1"), (1.0e-9, 0, 0.0, "1")]
 
 
-@pytest.mark.parametrize("skin,lanes,fskin", VARIANTS)
+@pytest.mark.parametrize("skin,lanes,fskin,tiles", VARIANTS)
 @pytest.mark.parametrize("name", SCENES)
-def test_ten_steps_artefacts_equal_drift_bounded(ds, scenes, name, skin, lanes, fskin):
+def test_ten_steps_artefacts_equal_drift_bounded(ds, scenes, name, skin, lanes, fskin, tiles, monkeypatch):
     """Ten update() calls through the five stage calls: integer artefacts equal
     after every step; floating-point drift within DRIFT_TOL."""
+    monkeypatch.setenv("DEMSPH_FLUID_TILES", tiles)
     recipe, b, sc, eng, orc = _setup(ds, scenes, name, solid_verlet_skin=skin, fluid_lanes=lanes,
                                      fluid_verlet_skin=fskin)
     eng.initialize()
@@ -447,8 +451,41 @@ def test_fixed_modes_match_the_oracle(ds, scenes, name):
         orc.update(dt, step, 1, gap)
         bad, _ = compare_integer_artefacts(eng, orc, skip_fluid_hash=(step % gap != 0))
         assert bad == [], f"step {step}: integer artefacts differ: {bad}"
+        # with every wall checked, grains pressed into the side walls at the
+        # start fly off: positions are held to 1e-7 of the spacing after step 1
         check_step(eng, orc, sc, _spacing(recipe), step, dt, FORCE_TOL if step == 1 else DRIFT_TOL,
-                   POS_TOL if step == 1 else 1e-8)
-    if sc.n_clump:
+                   POS_TOL if step == 1 else 1e-7)
+    if name == "tiny_tumbling":  # its clumps spin from the start
         q = eng.download_clumps()["orientation"]
         assert np.abs(q[:, 1:]).max() > 0, "clump orientations were not integrated"
+        assert np.allclose(q, orc.get("clump.orientation"), rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", ("tiny_dam_break", "tiny_coupled"))
+def test_tile_and_list_pair_loops_agree(ds, scenes, name, monkeypatch):
+    """The fluid lists kept as membership bits with the pair loops over them
+    (DEMSPH_FLUID_TILES=1, read when an engine is created) and the list
+    kernels (the default) over twenty steps: the same fluid-fluid and
+    fluid-solid lists bit for bit (the bits written out as lists), and states
+    within the per-step force tolerance of each other (the sums add the same
+    terms in another order)."""
+    b, sc = ds.build_scene(getattr(scenes, name)())
+    engines = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("DEMSPH_FLUID_TILES", flag)
+        engines.append(ds.Engine(sc))
+    monkeypatch.delenv("DEMSPH_FLUID_TILES")
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for e in engines:
+        e.initialize()
+        e.update(dt, 1, 20, gap, use_graph=True)
+    a, c = engines[0].fluid_pairs(), engines[1].fluid_pairs()
+    for k in a:
+        assert np.array_equal(a[k], c[k]), k
+    a, c = engines[0].fluid_solid_pairs(), engines[1].fluid_solid_pairs()
+    for k in ("prefix", "pointed", "pointing"):
+        assert np.array_equal(a[k], c[k]), k
+    (p0, v0, a0, r0), (p1, v1, a1, r1) = engines[0].download_fluids(), engines[1].download_fluids()
+    assert np.max(np.linalg.norm(a0 - a1, axis=1) / np.maximum(np.linalg.norm(a1, axis=1), 9.81)) <= FORCE_TOL
+    assert np.max(np.abs(r0 - r1)) <= 1e-6 * 1000.0
+    assert np.max(np.abs(p0 - p1)) <= 1e-9
