@@ -44,6 +44,71 @@ __device__ __forceinline__ float3 fluidRel(const DeviceState& d, int ps, int i, 
     return relF(ci, pi, d.fcell[j], pj, d.grid);
 }
 
+// ---- batched partner loops ----
+// Entries per lane read before any of their partners is used: a lane reads
+// B list entries, then the B partners' state, then adds the B pair terms in
+// list order.  B gathers per lane are in flight instead of one (the loop is
+// bound by the latency of the list stream and the dependent gathers, not by
+// bandwidth), and every sum is that of the one-by-one loop, bit for bit.
+// Depths and block counts measured on GB300 (ms per fluid period of the 1.0M
+// coupled dam break, one lane per particle; depth 1 = the one-by-one loop):
+// depth 1 with 12 continuity blocks 3.889, depth 2 with 8 continuity and 6
+// momentum blocks 3.829, depth 4 3.89-4.15 (continuity spills at 8 blocks),
+// depth 8 4.43.  The 48k dam break (eight lanes) is flat within 3 %.
+#ifndef DEMSPH_PAIR_BATCH
+#define DEMSPH_PAIR_BATCH 2       // entries per batch, one or two lanes per particle
+#endif
+#ifndef DEMSPH_PAIR_BATCH_WIDE
+#define DEMSPH_PAIR_BATCH_WIDE 2  // entries per batch, four or more lanes per particle
+#endif
+#ifndef DEMSPH_CONTINUITY_BLOCKS
+#define DEMSPH_CONTINUITY_BLOCKS 8  // resident blocks of T per SM the registers allow
+#endif
+#ifndef DEMSPH_MOMENTUM_BLOCKS
+#define DEMSPH_MOMENTUM_BLOCKS 6
+#endif
+template <int L>
+constexpr int batchDepth() { return L >= 4 ? DEMSPH_PAIR_BATCH_WIDE : DEMSPH_PAIR_BATCH; }
+
+template <int L, int B, class Gather, class Term>
+__device__ __forceinline__ void forFluidPartners(const unsigned* __restrict__ ff, int n, int i, int lane, int m,
+                                                 Gather gather, Term term)
+{
+    for (int k0 = lane; k0 < m; k0 += B * L) {
+        unsigned e[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) e[u] = k0 + u * L < m ? __ldcs(ff + (size_t)(k0 + u * L) * n + i) : 0u;
+        decltype(gather(0u)) g[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (k0 + u * L < m) g[u] = gather(e[u]);
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (k0 + u * L < m) term(e[u], g[u]);
+    }
+}
+
+// A fluid partner's state read by the continuity and momentum terms (the
+// buffers a pass reads are not written by it: read-only loads).  par only for
+// scenes whose fluids differ (U false).
+template <bool U>
+struct FluidPartner {
+    float4 p, v, par;
+    float dr;
+};
+
+template <bool U>
+__device__ __forceinline__ FluidPartner<U> gatherFluid(const DeviceState& d, int j, const float4* __restrict__ ph,
+                                                       const float4* __restrict__ vh, const float* __restrict__ dr)
+{
+    FluidPartner<U> q;
+    q.p = __ldg(ph + j);
+    q.v = __ldg(vh + j);
+    q.dr = __ldg(dr + j);
+    if constexpr (!U) q.par = __ldg(d.fpar + j);
+    return q;
+}
+
 // ---- lane groups ----
 // A fluid particle's neighbour loop is split over a group of L lanes (L a
 // power of two <= 32, chosen per scene so that small scenes still fill the
@@ -79,7 +144,7 @@ struct ContinuityArgs {
 };
 
 template <int L, bool U>
-__global__ void __launch_bounds__(T, L == 1 ? 12 : 10) kContinuity(DeviceState d, ContinuityArgs a)
+__global__ void __launch_bounds__(T, DEMSPH_CONTINUITY_BLOCKS) kContinuity(DeviceState d, ContinuityArgs a)
 {
     stepKernelBegin();
     if (a.countStep && blockIdx.x == 0 && threadIdx.x == 0 && *d.status == 0) atomicAdd(d.stepsDone, 1);
@@ -98,41 +163,40 @@ __global__ void __launch_bounds__(T, L == 1 ? 12 : 10) kContinuity(DeviceState d
         // neighbour, and the kernel's constants and the shared sound speed
         // taken out of the loop (one division per pair instead of five)
         const float negTwoRhoM = -2.f * o.rho * d.fparU.w;
-        for (int k = lane; k < nff; k += L) {
-            const unsigned e = d.ff[(size_t)k * n + i];
-            const int j = ffPartner(e);
-            const float4 pj = d.fph[a.ps][j];
-            const float3 r = fluidRel(d, a.ps, i, o.c, o.p, e, j, pj);
-            const float r2 = dot3(r, r);
-            if constexpr (U) {
-                // the shared constants are read from the kernel parameters
-                if (r2 >= d.fconstU.x) continue;
-                const float drj = d.fdrho[a.ds][j];
-                const float rhoj = d.fparU.x + drj;
-                const float Pj = drj * d.fparU.y * d.fparU.y;
-                const float rr = sqrtf(r2);
-                const float tt = 1.f - rr * d.fconstU.y;
-                const float G = d.fconstU.z * tt * tt * tt;
-                const float3 vij = o.v - xyz(d.fvh[a.vs][j]);
-                acc.add(negTwoRhoM * G / (rhoj * (o.rho + rhoj)) *
-                        (rhoj * dot3(vij, r) + (o.P - Pj) * rr * d.fconstU.w));
-            } else {
-                const float h = 0.5f * (o.h + pj.w);
-                if (r2 >= 4.f * h * h) continue;
-                const float4 par = d.fpar[j];
-                const float drj = d.fdrho[a.ds][j];
-                const float rhoj = par.x + drj;
-                const float Pj = drj * par.y * par.y;
-                const float Vj = par.w / rhoj;
-                const float rr = sqrtf(r2);
-                const float tt = 1.f - 0.5f * rr / h;
-                const float h2 = h * h;
-                const float G = KG * tt * tt * tt / (h2 * h2 * h);
-                const float c = 0.5f * (o.cs + par.y);
-                const float3 vij = o.v - xyz(d.fvh[a.vs][j]);
-                acc.add(-2.f * o.rho * Vj * G / (o.rho + rhoj) * (rhoj * dot3(vij, r) + (o.P - Pj) * rr / c));
-            }
-        }
+        const float4* __restrict__ ph = d.fph[a.ps];
+        const float4* __restrict__ vh = d.fvh[a.vs];
+        const float* __restrict__ drh = d.fdrho[a.ds];
+        forFluidPartners<L, batchDepth<L>()>(
+            d.ff, n, i, lane, nff, [&](unsigned e) { return gatherFluid<U>(d, ffPartner(e), ph, vh, drh); },
+            [&](unsigned e, const FluidPartner<U>& q) {
+                const float3 r = fluidRel(d, a.ps, i, o.c, o.p, e, ffPartner(e), q.p);
+                const float r2 = dot3(r, r);
+                if constexpr (U) {
+                    // the shared constants are read from the kernel parameters
+                    if (r2 >= d.fconstU.x) return;
+                    const float rhoj = d.fparU.x + q.dr;
+                    const float Pj = q.dr * d.fparU.y * d.fparU.y;
+                    const float rr = sqrtf(r2);
+                    const float tt = 1.f - rr * d.fconstU.y;
+                    const float G = d.fconstU.z * tt * tt * tt;
+                    const float3 vij = o.v - xyz(q.v);
+                    acc.add(negTwoRhoM * G / (rhoj * (o.rho + rhoj)) *
+                            (rhoj * dot3(vij, r) + (o.P - Pj) * rr * d.fconstU.w));
+                } else {
+                    const float h = 0.5f * (o.h + q.p.w);
+                    if (r2 >= 4.f * h * h) return;
+                    const float rhoj = q.par.x + q.dr;
+                    const float Pj = q.dr * q.par.y * q.par.y;
+                    const float Vj = q.par.w / rhoj;
+                    const float rr = sqrtf(r2);
+                    const float tt = 1.f - 0.5f * rr / h;
+                    const float h2 = h * h;
+                    const float G = KG * tt * tt * tt / (h2 * h2 * h);
+                    const float c = 0.5f * (o.cs + q.par.y);
+                    const float3 vij = o.v - xyz(q.v);
+                    acc.add(-2.f * o.rho * Vj * G / (o.rho + rhoj) * (rhoj * dot3(vij, r) + (o.P - Pj) * rr / c));
+                }
+            });
         const int nfs = min(d.fsc[i], d.kfs);
         const float ci2 = o.cs * o.cs;
         for (int k = lane; k < nfs; k += L) {
@@ -162,7 +226,7 @@ __global__ void __launch_bounds__(T, L == 1 ? 12 : 10) kContinuity(DeviceState d
 // Reads position [1], velocity [0], density [1]; writes acc, velocity [1] and
 // position [0] (the buffers no other thread reads in this pass).
 template <int L, bool U>
-__global__ void __launch_bounds__(T) kMomentum(DeviceState d, dfl dtf, dfl halfDtf)
+__global__ void __launch_bounds__(T, DEMSPH_MOMENTUM_BLOCKS) kMomentum(DeviceState d, dfl dtf, dfl halfDtf)
 {
     stepKernelBegin();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -177,51 +241,48 @@ __global__ void __launch_bounds__(T) kMomentum(DeviceState d, dfl dtf, dfl halfD
         // U: the same parameters and smoothing length for every particle (see
         // kContinuity): three divisions per pair instead of seven
         const float twoNuRhoI = 2.f * d.fparU.z * o.rho, twoVi = 2.f * o.V;
-        for (int k = lane; k < nff; k += L) {
-            const unsigned e = d.ff[(size_t)k * n + i];
-            const int j = ffPartner(e);
-            const float4 pj = d.fph[1][j];
-            const float3 r = fluidRel(d, 1, i, o.c, o.p, e, j, pj);
-            const float r2 = dot3(r, r);
-            if constexpr (U) {
-                if (r2 >= d.fconstU.x) continue;
-                const float drj = d.fdrho[1][j];
-                const float rhoj = d.fparU.x + drj;
-                const float Pj = drj * d.fparU.y * d.fparU.y;
-                const float rr = sqrtf(r2);
-                const float tt = 1.f - rr * d.fconstU.y;
-                const float G = d.fconstU.z * tt * tt * tt;
-                const float3 vij = o.v - xyz(d.fvh[0][j]);
-                const float dU = -dot3(vij, r) / rr;  // U_L - U_R
-                const float beta = fminf(3.f * fmaxf(dU, 0.f), d.fparU.y);
-                const float invSum = 1.f / (o.rho + rhoj);
-                const float Ps = (o.rho * Pj + rhoj * o.P + o.rho * rhoj * beta * dU) * invSum;
-                const float gbar = twoNuRhoI * rhoj * invSum;  // 2 g_i g_j / (g_i + g_j), g = nu rho
-                const float w = twoVi * G / rhoj;              // 2 V_i V_j G / m, V_j = m / rho_j
-                acc.add((r * Ps - vij * gbar) * w);
-            } else {
-                const float h = 0.5f * (o.h + pj.w);
-                if (r2 >= 4.f * h * h) continue;
-                const float4 par = d.fpar[j];
-                const float drj = d.fdrho[1][j];
-                const float rhoj = par.x + drj;
-                const float Pj = drj * par.y * par.y;
-                const float Vj = par.w / rhoj;
-                const float gj = par.z * rhoj;
-                const float rr = sqrtf(r2);
-                const float tt = 1.f - 0.5f * rr / h;
-                const float h2 = h * h;
-                const float G = KG * tt * tt * tt / (h2 * h2 * h);
-                const float c = 0.5f * (o.cs + par.y);
-                const float3 vij = o.v - xyz(d.fvh[0][j]);
-                const float dU = -dot3(vij, r) / rr;  // U_L - U_R
-                const float beta = fminf(3.f * fmaxf(dU, 0.f), c);
-                const float Ps = (o.rho * Pj + rhoj * o.P + o.rho * rhoj * beta * dU) / (o.rho + rhoj);
-                const float gbar = 2.f * o.gam * gj / (o.gam + gj);
-                const float w = 2.f * o.V * Vj * G / o.m;
-                acc.add((r * Ps - vij * gbar) * w);
-            }
-        }
+        forFluidPartners<L, batchDepth<L>()>(
+            d.ff, n, i, lane, nff,
+            [&](unsigned e) { return gatherFluid<U>(d, ffPartner(e), d.fph[1], d.fvh[0], d.fdrho[1]); },
+            [&](unsigned e, const FluidPartner<U>& q) {
+                const float3 r = fluidRel(d, 1, i, o.c, o.p, e, ffPartner(e), q.p);
+                const float r2 = dot3(r, r);
+                if constexpr (U) {
+                    if (r2 >= d.fconstU.x) return;
+                    const float rhoj = d.fparU.x + q.dr;
+                    const float Pj = q.dr * d.fparU.y * d.fparU.y;
+                    const float rr = sqrtf(r2);
+                    const float tt = 1.f - rr * d.fconstU.y;
+                    const float G = d.fconstU.z * tt * tt * tt;
+                    const float3 vij = o.v - xyz(q.v);
+                    const float dU = -dot3(vij, r) / rr;  // U_L - U_R
+                    const float beta = fminf(3.f * fmaxf(dU, 0.f), d.fparU.y);
+                    const float invSum = 1.f / (o.rho + rhoj);
+                    const float Ps = (o.rho * Pj + rhoj * o.P + o.rho * rhoj * beta * dU) * invSum;
+                    const float gbar = twoNuRhoI * rhoj * invSum;  // 2 g_i g_j / (g_i + g_j), g = nu rho
+                    const float w = twoVi * G / rhoj;              // 2 V_i V_j G / m, V_j = m / rho_j
+                    acc.add((r * Ps - vij * gbar) * w);
+                } else {
+                    const float h = 0.5f * (o.h + q.p.w);
+                    if (r2 >= 4.f * h * h) return;
+                    const float rhoj = q.par.x + q.dr;
+                    const float Pj = q.dr * q.par.y * q.par.y;
+                    const float Vj = q.par.w / rhoj;
+                    const float gj = q.par.z * rhoj;
+                    const float rr = sqrtf(r2);
+                    const float tt = 1.f - 0.5f * rr / h;
+                    const float h2 = h * h;
+                    const float G = KG * tt * tt * tt / (h2 * h2 * h);
+                    const float c = 0.5f * (o.cs + q.par.y);
+                    const float3 vij = o.v - xyz(q.v);
+                    const float dU = -dot3(vij, r) / rr;  // U_L - U_R
+                    const float beta = fminf(3.f * fmaxf(dU, 0.f), c);
+                    const float Ps = (o.rho * Pj + rhoj * o.P + o.rho * rhoj * beta * dU) / (o.rho + rhoj);
+                    const float gbar = 2.f * o.gam * gj / (o.gam + gj);
+                    const float w = 2.f * o.V * Vj * G / o.m;
+                    acc.add((r * Ps - vij * gbar) * w);
+                }
+            });
         const int nfs = min(d.fsc[i], d.kfs);
         const float ci2 = o.cs * o.cs;
         for (int k = lane; k < nfs; k += L) {
@@ -279,19 +340,27 @@ __global__ void __launch_bounds__(T) kDensityReinit(DeviceState d, int storeRefe
         const dfl twoH = df_add(h, h);
         const int n = d.nf;
         const int nff = min(d.ffc[i], d.kff);
-        for (int k = lane; k < nff; k += L) {
-            const unsigned e = d.ff[(size_t)k * n + i];
-            const int j = ffPartner(e);
-            const unsigned code = (unsigned)entryWalk(e);
-            int4 cj;
-            if (ffRegular(e))
-                cj = make_int4(ci.x + (int)(code % 3u) - 1, ci.y + (int)((code / 3u) % 3u) - 1, ci.z + (int)(code / 9u) - 1, 0);
-            else
-                cj = d.fcell[j];
-            const dfl r = dfNorm(relDF(ci, pi, li, cj, d.fph[0][j], d.fpl[0][j], d.grid));
-            if (df_ge0(df_sub(r, twoH))) continue;  // q >= 2
-            S = df_add(S, shepardTerm(r, invh));
-        }
+        struct PartnerPosition {
+            float4 h, l;
+        };
+        forFluidPartners<L, batchDepth<L>()>(
+            d.ff, n, i, lane, nff,
+            [&](unsigned e) {
+                const int j = ffPartner(e);
+                return PartnerPosition{__ldg(d.fph[0] + j), __ldg(d.fpl[0] + j)};
+            },
+            [&](unsigned e, const PartnerPosition& q) {
+                const unsigned code = (unsigned)entryWalk(e);
+                int4 cj;
+                if (ffRegular(e))
+                    cj = make_int4(ci.x + (int)(code % 3u) - 1, ci.y + (int)((code / 3u) % 3u) - 1,
+                                   ci.z + (int)(code / 9u) - 1, 0);
+                else
+                    cj = d.fcell[ffPartner(e)];
+                const dfl r = dfNorm(relDF(ci, pi, li, cj, q.h, q.l, d.grid));
+                if (df_ge0(df_sub(r, twoH))) return;  // q >= 2
+                S = df_add(S, shepardTerm(r, invh));
+            });
         // V0_a / V0_i = (2 r_a / (h_i / 1.3))^3 = (2.6 r_a / h_i)^3
         const dfl k26 = df_from_double(2.6);
         const int nfs = min(d.fsc[i], d.kfs);
