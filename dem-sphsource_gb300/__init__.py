@@ -150,6 +150,10 @@ def load_library():
     lib.demsph_stream.argtypes = [_P]
     lib.demsph_kernel_launches.restype = C.c_longlong
     lib.demsph_kernel_launches.argtypes = [_P]
+    lib.demsph_frame_writer_open.argtypes = [_P, _P, C.c_char_p, C.POINTER(_P)]
+    lib.demsph_frame_writer_write.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_double]
+    lib.demsph_frame_writer_flush.argtypes = [_P]
+    lib.demsph_frame_writer_close.argtypes = [_P]
     lib.demsph_device_bytes.restype = C.c_longlong
     lib.demsph_device_bytes.argtypes = [_P]
     lib.demsph_estimate_bytes.restype = C.c_longlong
@@ -273,6 +277,43 @@ def build_scene(recipe, n_material=10):
     b = Builder(n_material)
     recipe.apply(b)
     return b, b.scene()
+
+
+FRAME_FLUID, FRAME_SOLID, FRAME_FLUID2SOLID, FRAME_ALL = 1, 2, 4, 7
+
+
+class FrameWriter:
+    """The frame files of class solverBase (fluid_NNNN.vtu, solid_NNNN.vtu,
+    fluid2Solid_NNNN.vtu in `directory`) of one engine as binary VTU, written
+    by a background thread (demsph_frame_writer_*).  Close it before the
+    engine."""
+
+    def __init__(self, engine, directory):
+        self.engine = engine
+        self.lib = engine.lib
+        h = _P()
+        engine._chk(self.lib.demsph_frame_writer_open(engine.h, C.addressof(engine.scene), str(directory).encode(),
+                                                      C.byref(h)), "demsph_frame_writer_open")
+        self.h = h
+
+    def write(self, what, frame, step, time):
+        """Enqueues the files of the kinds in `what` (FRAME_* bits); returns at once."""
+        self.engine._chk(self.lib.demsph_frame_writer_write(self.h, what, frame, step, time),
+                         "demsph_frame_writer_write")
+
+    def flush(self):
+        self.engine._chk(self.lib.demsph_frame_writer_flush(self.h), "demsph_frame_writer_flush")
+
+    def close(self):
+        if getattr(self, "h", None):
+            h, self.h = self.h, None
+            self.engine._chk(self.lib.demsph_frame_writer_close(h), "demsph_frame_writer_close")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 class Engine:

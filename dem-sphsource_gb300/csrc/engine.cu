@@ -587,6 +587,7 @@ const char* demsph_status_string(int s)
     case DEMSPH_ERR_CAPACITY: return "list capacity exceeded";
     case DEMSPH_ERR_OUT_OF_MEMORY: return "out of device memory";
     case DEMSPH_ERR_TIMEOUT: return "device wait timed out";
+    case DEMSPH_ERR_IO: return "file error";
     default: return "unknown status";
     }
 }

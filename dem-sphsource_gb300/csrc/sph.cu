@@ -31,15 +31,36 @@ namespace {
 constexpr int T = 128;
 using namespace sph;
 
-// Relative position of fluid partner entry e of slot i.
-__device__ __forceinline__ float3 fluidRel(const DeviceState& d, int ps, int i, int4 ci, float4 pi, unsigned e,
+#ifndef DEMSPH_WALK_TABLE
+#define DEMSPH_WALK_TABLE 1  // 1: the 27 cell offsets come from a table in shared memory
+#endif
+
+// Offset of walk cell `code` (dx, dy, dz in -1..1, code = (dz+1) 9 + (dy+1) 3 + dx+1)
+// times the cell size.
+__device__ __forceinline__ float4 walkOffsetOf(unsigned code, float3 cs)
+{
+    const int dx = (int)(code % 3u) - 1, dy = (int)((code / 3u) % 3u) - 1, dz = (int)(code / 9u) - 1;
+    return make_float4((float)dx * cs.x, (float)dy * cs.y, (float)dz * cs.z, 0.f);
+}
+
+// The table of the 27 offsets in a block's shared memory (filled before the
+// block's first early return).
+__device__ __forceinline__ void fillWalkTable(float4* tab, float3 cs)
+{
+    if (DEMSPH_WALK_TABLE) {
+        if (threadIdx.x < 27) tab[threadIdx.x] = walkOffsetOf(threadIdx.x, cs);
+        __syncthreads();
+    }
+}
+
+// Relative position of fluid partner entry e of slot i (tab: the offsets'
+// table; the products are exact, so the table changes no bit).
+__device__ __forceinline__ float3 fluidRel(const DeviceState& d, const float4* tab, int4 ci, float4 pi, unsigned e,
                                            int j, float4 pj)
 {
     if (ffRegular(e)) {
-        const unsigned code = (unsigned)entryWalk(e);
-        const int dx = (int)(code % 3u) - 1, dy = (int)((code / 3u) % 3u) - 1, dz = (int)(code / 9u) - 1;
-        return make_float3((pi.x - pj.x) - (float)dx * d.grid.cs.x, (pi.y - pj.y) - (float)dy * d.grid.cs.y,
-                           (pi.z - pj.z) - (float)dz * d.grid.cs.z);
+        const float4 o = DEMSPH_WALK_TABLE ? tab[entryWalk(e)] : walkOffsetOf((unsigned)entryWalk(e), d.grid.cs);
+        return make_float3((pi.x - pj.x) - o.x, (pi.y - pj.y) - o.y, (pi.z - pj.z) - o.z);
     }
     return relF(ci, pi, d.fcell[j], pj, d.grid);
 }
@@ -67,6 +88,12 @@ __device__ __forceinline__ float3 fluidRel(const DeviceState& d, int ps, int i, 
 #ifndef DEMSPH_MOMENTUM_BLOCKS
 #define DEMSPH_MOMENTUM_BLOCKS 6
 #endif
+#ifndef DEMSPH_PAIR_AHEAD
+#define DEMSPH_PAIR_AHEAD 1  // 1: the next batch's entries are read while this batch computes
+#endif
+#ifndef DEMSPH_PAIR_L2_AHEAD
+#define DEMSPH_PAIR_L2_AHEAD 0  // > 0: the list line that many batches ahead is prefetched into L2
+#endif
 template <int L>
 constexpr int batchDepth() { return L >= 4 ? DEMSPH_PAIR_BATCH_WIDE : DEMSPH_PAIR_BATCH; }
 
@@ -74,10 +101,24 @@ template <int L, int B, class Gather, class Term>
 __device__ __forceinline__ void forFluidPartners(const unsigned* __restrict__ ff, int n, int i, int lane, int m,
                                                  Gather gather, Term term)
 {
+    const size_t stride = (size_t)L * n;  // from entry k of slot i to entry k + L
+    const unsigned* p = ff + (size_t)lane * n + i;
+    unsigned next[B];
+    if (DEMSPH_PAIR_AHEAD) {
+#pragma unroll
+        for (int u = 0; u < B; ++u) next[u] = lane + u * L < m ? __ldcs(p + u * stride) : 0u;
+    }
     for (int k0 = lane; k0 < m; k0 += B * L) {
         unsigned e[B];
 #pragma unroll
-        for (int u = 0; u < B; ++u) e[u] = k0 + u * L < m ? __ldcs(ff + (size_t)(k0 + u * L) * n + i) : 0u;
+        for (int u = 0; u < B; ++u) e[u] = DEMSPH_PAIR_AHEAD ? next[u] : (k0 + u * L < m ? __ldcs(p + u * stride) : 0u);
+        p += B * stride;
+        if (DEMSPH_PAIR_AHEAD) {
+#pragma unroll
+            for (int u = 0; u < B; ++u) next[u] = k0 + (B + u) * L < m ? __ldcs(p + u * stride) : 0u;
+        }
+        if (DEMSPH_PAIR_L2_AHEAD > 0 && k0 + DEMSPH_PAIR_L2_AHEAD * B * L < m)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(p + (size_t)(DEMSPH_PAIR_L2_AHEAD - 1) * B * stride));
         decltype(gather(0u)) g[B];
 #pragma unroll
         for (int u = 0; u < B; ++u)
@@ -147,6 +188,8 @@ template <int L, bool U>
 __global__ void __launch_bounds__(T, DEMSPH_CONTINUITY_BLOCKS) kContinuity(DeviceState d, ContinuityArgs a)
 {
     stepKernelBegin();
+    __shared__ float4 walkTab[27];
+    fillWalkTable(walkTab, d.grid.cs);
     if (a.countStep && blockIdx.x == 0 && threadIdx.x == 0 && *d.status == 0) atomicAdd(d.stepsDone, 1);
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if ((t & ~31) >= d.nf * L || *d.status) return;
@@ -169,7 +212,7 @@ __global__ void __launch_bounds__(T, DEMSPH_CONTINUITY_BLOCKS) kContinuity(Devic
         forFluidPartners<L, batchDepth<L>()>(
             d.ff, n, i, lane, nff, [&](unsigned e) { return gatherFluid<U>(d, ffPartner(e), ph, vh, drh); },
             [&](unsigned e, const FluidPartner<U>& q) {
-                const float3 r = fluidRel(d, a.ps, i, o.c, o.p, e, ffPartner(e), q.p);
+                const float3 r = fluidRel(d, walkTab, o.c, o.p, e, ffPartner(e), q.p);
                 const float r2 = dot3(r, r);
                 if constexpr (U) {
                     // the shared constants are read from the kernel parameters
@@ -229,6 +272,8 @@ template <int L, bool U>
 __global__ void __launch_bounds__(T, DEMSPH_MOMENTUM_BLOCKS) kMomentum(DeviceState d, dfl dtf, dfl halfDtf)
 {
     stepKernelBegin();
+    __shared__ float4 walkTab[27];
+    fillWalkTable(walkTab, d.grid.cs);
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if ((t & ~31) >= d.nf * L || *d.status) return;
     const int i = t / L, lane = t % L;
@@ -245,7 +290,7 @@ __global__ void __launch_bounds__(T, DEMSPH_MOMENTUM_BLOCKS) kMomentum(DeviceSta
             d.ff, n, i, lane, nff,
             [&](unsigned e) { return gatherFluid<U>(d, ffPartner(e), d.fph[1], d.fvh[0], d.fdrho[1]); },
             [&](unsigned e, const FluidPartner<U>& q) {
-                const float3 r = fluidRel(d, 1, i, o.c, o.p, e, ffPartner(e), q.p);
+                const float3 r = fluidRel(d, walkTab, o.c, o.p, e, ffPartner(e), q.p);
                 const float r2 = dot3(r, r);
                 if constexpr (U) {
                     if (r2 >= d.fconstU.x) return;

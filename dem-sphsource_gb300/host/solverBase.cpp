@@ -107,6 +107,7 @@ void solverBase::solve()
         simPara.iStep++;
     }
     check(demsph_synchronize(engine), "solve");
+    if (frames) check(demsph_frame_writer_flush(frames), "frame files");
 }
 
 // core/solverBase.cpp:13-44
@@ -132,6 +133,7 @@ void solverBase::initialize()
     if (wantsPairForces && !keepPairForces) {
         // the driver writes fluid2Solid frames: rebuild once, keeping per-pair coupling forces
         keepPairForces = true;
+        closeFrames();  // the writer belongs to the engine being replaced
         buildEngine();
     }
     std::cout << "Initialization completed." << std::endl;
@@ -160,9 +162,32 @@ void solverBase::frame()
     outputData();
 }
 
+// Frames of a kind through the binary writer, opened on first use for the
+// current engine.
+bool solverBase::binaryFrame(int kind)
+{
+    if (!binaryOutput || !engine) return false;
+    if (!frames) {
+        demsph_scene v;
+        scene.view(&v);
+        check(demsph_frame_writer_open(engine, &v, dir.c_str(), &frames), "frame files");
+    }
+    check(demsph_frame_writer_write(frames, kind, simPara.iFrame, simPara.iStep, getTime()), "frame files");
+    return true;
+}
+
+void solverBase::closeFrames()
+{
+    if (!frames) return;
+    const int st = demsph_frame_writer_close(frames);
+    frames = nullptr;
+    if (st != DEMSPH_OK) std::cerr << "frame files: " << demsph_last_error(engine) << std::endl;
+}
+
 // core/solverBase.cpp:69-171
 void solverBase::outputFluidVTU()
 {
+    if (binaryFrame(DEMSPH_FRAME_FLUID)) return;
     if (simPara.iFrame > 0) downloadFluids();
     const HostFluid& f = scene.hos.fluids;
     VertexFile v(dir, "fluid", simPara.iFrame, getTime(), simPara.iStep, f.points.num, "smooth length");
@@ -176,6 +201,7 @@ void solverBase::outputFluidVTU()
 // core/solverBase.cpp:172-257
 void solverBase::outputSolidVTU()
 {
+    if (binaryFrame(DEMSPH_FRAME_SOLID)) return;
     if (simPara.iFrame > 0) downloadSolids();
     const HostSolid& s = scene.hos.solids;
     VertexFile v(dir, "solid", simPara.iFrame, getTime(), simPara.iStep, s.points.num, "radius");
@@ -193,6 +219,9 @@ void solverBase::outputSolidVTU()
 void solverBase::outputFluid2SolidVTU()
 {
     if (simPara.iFrame == 0) wantsPairForces = true;
+    // frame 0 holds no pairs (the reference's host list is empty before the
+    // first step): that file is the ASCII one
+    if (simPara.iFrame > 0 && binaryFrame(DEMSPH_FRAME_FLUID2SOLID)) return;
     if (simPara.iFrame > 0) {
         downloadSolids();
         downloadFluids();

@@ -21,18 +21,22 @@
 class DEMSPH_API solverBase : public dataBase {
 public:
     solverBase() : dataBase() {}
-    ~solverBase() override {}
+    ~solverBase() override { closeFrames(); }
 
     void solve();
 
 protected:
     void setProblemName(const std::string& name) { dir = name + "Output"; }
 
-    // Frame files <problem>Output/{fluid,solid,fluid2Solid}_NNNN.vtu (ASCII VTK
-    // unstructured grids of vertices, the reference's names and fields).
+    // Frame files <problem>Output/{fluid,solid,fluid2Solid}_NNNN.vtu (VTK
+    // unstructured grids of vertices, the reference's names and fields):
+    // ASCII written on this thread as in the reference, or - after
+    // setBinaryOutput(true) - binary VTU packed on the GPU and written by a
+    // background thread while the steps go on (demsph_frame_writer).
     void outputFluidVTU();
     void outputSolidVTU();
     void outputFluid2SolidVTU();
+    void setBinaryOutput(bool on) { binaryOutput = on; }
 
     virtual void conditionInitialize() {}
     virtual void outputData() {}
@@ -44,6 +48,11 @@ private:
     bool updateIsDefault{false};   // set by the default update() when it runs
     bool batched{false};           // steps between frames go to demsph_update
     bool wantsPairForces{false};   // outputFluid2SolidVTU was called at frame 0
+    bool binaryOutput{false};      // frames through the binary writer
+    demsph_frame_writer* frames{nullptr};
+
+    bool binaryFrame(int kind);    // true: the frame went to the binary writer
+    void closeFrames();
 
     void initialize();
     virtual void update();

@@ -54,7 +54,8 @@ typedef enum demsph_status {
     DEMSPH_ERR_NO_DEVICE = 4,     /* no usable CUDA device / wrong architecture */
     DEMSPH_ERR_CAPACITY = 5,      /* a neighbour or contact list overflowed; the engine grew it, re-run the step */
     DEMSPH_ERR_OUT_OF_MEMORY = 6,
-    DEMSPH_ERR_TIMEOUT = 7        /* a bounded device-side wait gave up */
+    DEMSPH_ERR_TIMEOUT = 7,       /* a bounded device-side wait gave up */
+    DEMSPH_ERR_IO = 8             /* a file could not be created or written */
 } demsph_status;
 
 /* Reference behaviours that can be switched off (all kept by default). */
@@ -324,6 +325,35 @@ DEMSPH_API int demsph_set_contact_models(demsph_engine* e, const demsph_scene* t
 DEMSPH_API int demsph_set_clump_velocity(demsph_engine* e, int clump, const double v[3]);            /* dataBase.h:169-182 */
 DEMSPH_API int demsph_add_external_force(demsph_engine* e, int solid, const double force[3]);        /* dataBase.cpp:179-195 */
 DEMSPH_API int demsph_add_global_damping(demsph_engine* e, int solid, double c_d);                   /* dataBase.cpp:197-224 */
+
+/* ---- frame files of class solverBase (core/solverBase.cpp:69-333) ----
+   <dir>/fluid_NNNN.vtu, solid_NNNN.vtu and fluid2Solid_NNNN.vtu with the
+   reference's arrays, names and order, written as binary VTU (appended raw
+   data, UInt64 headers) instead of ASCII.  A write packs the frame's FP32
+   arrays on the engine's stream and returns; a background thread of the
+   writer copies them into pinned memory and writes the files while the
+   following steps run.  Each kind keeps two frames in flight: a write waits
+   while the file of the same kind two frames back is not yet written.  The
+   static arrays (smoothing length, radius, clusterID, clumpID) are taken from
+   `scene` (the engine's scene) at open.  fluid2Solid forces are the per-pair
+   coupling forces of the last step when the engine keeps them (options.debug
+   bit 0), else zeros.  Close the writer before destroying its engine.  Errors
+   of the writer thread are returned by the next write, flush or close
+   (DEMSPH_ERR_IO, message in demsph_last_error of the engine). */
+typedef struct demsph_frame_writer demsph_frame_writer;
+#define DEMSPH_FRAME_FLUID 1          /* outputFluidVTU       (core/solverBase.cpp:69-170) */
+#define DEMSPH_FRAME_SOLID 2          /* outputSolidVTU       (core/solverBase.cpp:172-257) */
+#define DEMSPH_FRAME_FLUID2SOLID 4    /* outputFluid2SolidVTU (core/solverBase.cpp:259-333) */
+#define DEMSPH_FRAME_ALL 7
+DEMSPH_API int demsph_frame_writer_open(demsph_engine* e, const demsph_scene* scene, const char* dir,
+                                        demsph_frame_writer** out);
+/* Enqueues the files of the kinds in `what` for frame number `frame` (the
+   NNNN of the names), with TIME and STEP field data. */
+DEMSPH_API int demsph_frame_writer_write(demsph_frame_writer* w, int what, int frame, int step, double time);
+/* Waits until every enqueued file is written. */
+DEMSPH_API int demsph_frame_writer_flush(demsph_frame_writer* w);
+/* Flushes, stops the thread and frees the writer (also after an error). */
+DEMSPH_API int demsph_frame_writer_close(demsph_frame_writer* w);
 
 /* ---- artefacts in the reference's index space and order (for parity) ---- */
 DEMSPH_API int demsph_get_counts(demsph_engine* e, demsph_counts* out);
