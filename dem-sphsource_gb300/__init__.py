@@ -102,14 +102,16 @@ class ServerConfig(C.Structure):
     """ctypes mirror of ``demsph_server_config``."""
 
     _fields_ = [("device", _I), ("workers", _I), ("chunk_steps", _I), ("hbm_budget_bytes", C.c_longlong),
-                ("autotune", _I), ("graphs", _I)]
+                ("autotune", _I), ("graphs", _I), ("batch", _I), ("batch_round_steps", _I)]
 
 
 class ServerSummary(C.Structure):
     _fields_ = [(k, C.c_longlong) for k in ("submitted", "admitted", "completed", "failed", "pending", "steps",
                                              "particle_updates", "chunks", "bytes_in_use", "peak_bytes")] + \
                [(k, _D) for k in ("busy_s", "updates_per_s", "p50_step_ms", "p99_step_ms", "create_s", "step_s",
-                                  "download_s")]
+                                  "download_s")] + \
+               [(k, C.c_longlong) for k in ("batch_rounds", "batch_graph_builds")] + \
+               [(k, _D) for k in ("batch_capture_s", "batch_instantiate_s", "batch_launch_s")]
 
 
 class RequestInfo(C.Structure):
@@ -150,6 +152,13 @@ def load_library():
     lib.demsph_stream.argtypes = [_P]
     lib.demsph_kernel_launches.restype = C.c_longlong
     lib.demsph_kernel_launches.argtypes = [_P]
+    lib.demsph_batch_create.argtypes = [_I, C.POINTER(_P)]
+    lib.demsph_batch_destroy.argtypes = [_P]
+    lib.demsph_batch_update.argtypes = [_P, C.POINTER(_P), _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_D),
+                                        C.POINTER(_I), C.POINTER(_I)]
+    lib.demsph_batch_get_info.argtypes = [_P, _P]
+    lib.demsph_batch_last_error.argtypes = [_P]
+    lib.demsph_batch_last_error.restype = C.c_char_p
     lib.demsph_frame_writer_open.argtypes = [_P, _P, C.c_char_p, C.POINTER(_P)]
     lib.demsph_frame_writer_write.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_double]
     lib.demsph_frame_writer_flush.argtypes = [_P]
@@ -580,16 +589,65 @@ def estimate_bytes(scene, **opts):
     return int(lib.demsph_estimate_bytes(C.byref(scene), C.byref(o)))
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [(k, C.c_longlong) for k in ("launches", "graph_builds", "members", "nodes")] + \
+               [(k, _D) for k in ("capture_s", "instantiate_s", "launch_s")]
+
+
+class Batch:
+    """Many engines advanced in one CUDA graph launch (demsph_batch_*)."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = _P()
+        rc = self.lib.demsph_batch_create(device, C.byref(h))
+        if rc != DEMSPH_OK:
+            raise DemSphError(rc, "demsph_batch_create")
+        self.h = h
+
+    def update(self, engines, first_steps, n_steps, dts, gaps):
+        """Advances engines[k] by n_steps[k] steps from first_steps[k]; returns
+        the per-engine status list (raises if the launch itself failed)."""
+        k = len(engines)
+        arr = (_P * k)(*[e.h.value for e in engines])
+        st = (_I * k)()
+        rc = self.lib.demsph_batch_update(self.h, arr, k, (_I * k)(*first_steps), (_I * k)(*n_steps),
+                                          (_D * k)(*dts), (_I * k)(*gaps), st)
+        if rc != DEMSPH_OK:
+            raise DemSphError(rc, "demsph_batch_update: " + self.lib.demsph_batch_last_error(self.h).decode())
+        return list(st)
+
+    def info(self):
+        i = BatchInfo()
+        self.lib.demsph_batch_get_info(self.h, C.addressof(i))
+        return {k: getattr(i, k) for k, _ in BatchInfo._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.demsph_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Server:
     """Many scenes on one GPU (demsph_server_*): submit, wait, fetch."""
 
     STATES = ("pending", "running", "done", "failed")
 
-    def __init__(self, device=0, workers=0, chunk_steps=0, hbm_budget_bytes=0, autotune=False, graphs=0):
+    def __init__(self, device=0, workers=0, chunk_steps=0, hbm_budget_bytes=0, autotune=False, graphs=0,
+                 batch=False, batch_round_steps=0):
         """graphs: CUDA graphs for a scene's turns - 0 only while it is the
-        only active scene, 1 always, -1 never."""
+        only active scene, 1 always, -1 never.  batch: every active scene
+        advances in one graph launch per round (demsph_batch_update), rounds
+        of about batch_round_steps steps."""
         self.lib = load_library()
-        cfg = ServerConfig(device, workers, chunk_steps, int(hbm_budget_bytes), 1 if autotune else 0, int(graphs))
+        cfg = ServerConfig(device, workers, chunk_steps, int(hbm_budget_bytes), 1 if autotune else 0, int(graphs),
+                           1 if batch else 0, int(batch_round_steps))
         h = _P()
         rc = self.lib.demsph_server_create(C.byref(cfg), C.byref(h))
         if rc != DEMSPH_OK:

@@ -20,6 +20,7 @@
 // the previous step (re-hashing and re-ordering are idempotent).  The host
 // grows the list and re-runs from the first incomplete step.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -55,6 +56,8 @@ void dropGraph(demsph_engine* e)
 {
     for (const auto& g : e->graphs) cudaGraphExecDestroy(g.exec);
     e->graphs.clear();
+    for (const auto& r : e->rounds) cudaGraphDestroy(r.graph);
+    e->rounds.clear();
 }
 
 double* scratchDoubles(demsph_engine* e, size_t n)
@@ -1552,6 +1555,325 @@ int demsph_profile_report(demsph_engine* e, char* buf, int cap)
     buf[n] = 0;
     return DEMSPH_OK;
     ENGINE_END(e)
+}
+
+}  // extern "C"
+
+// ---- many engines advanced by one graph launch (demsph_batch_*) ----
+//
+// No counterpart in the reference, which runs one scene per process.  Each
+// engine of a batch contributes a round: `n` steps from `first`, captured once
+// as a graph of exactly the launches its own graph replays make (plain DEM
+// runs fused, fluid steps one by one), so a scene's state after a batched
+// round is bit for bit its state after the same steps alone.  The batch's
+// graph holds every member's round as a child graph (independent branches:
+// the scenes' kernels overlap on the device), then one report kernel that
+// copies each member's status and completed-step count into mapped host
+// memory.  The launch is re-instantiated only when a member's round changes
+// (another length, phase or parity, or a member whose graphs were dropped by
+// list growth); rounds that are whole multiples of the Shepard period (5 gap
+// steps) and of even length keep their phase and parity, so a steady batch
+// launches the same executable graph round after round.  A member whose round
+// overflowed a list resumes alone after its lists grow (demsph_update's path),
+// before the call returns.
+namespace {
+
+long long g_roundIds = 0;  // ids of captured rounds (batch keys); guarded by g_roundMutex
+std::mutex g_roundMutex;
+
+__global__ void kBatchReport(int* const* where, int n, int2* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_int2(*where[2 * i], *where[2 * i + 1]);
+}
+
+// The round of `n` steps of engine e from step `first` (captured on first use).
+const demsph_engine::RoundGraph& roundFor(demsph_engine* e, double dt, int first, int n, int gap)
+{
+    const DeviceState& d = e->d;
+    const int period = d.nf > 0 ? 5 * gap : 1;
+    const int phase = first % period;
+    for (const auto& r : e->rounds)
+        if (r.phase == phase && r.length == n && r.parity == e->par && r.gap == gap && r.dt == dt) return r;
+    demsph_engine::RoundGraph r{phase, n, e->par, gap, dt, nullptr, 0, 0, {}};
+    {
+        std::lock_guard<std::mutex> g(g_roundMutex);
+        r.id = ++g_roundIds;
+    }
+    const int parity = e->par;
+    const long long before = t_kernelLaunches;
+    CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+        CK(cudaMemsetAsync(d.stepsDone, 0, sizeof(int), e->stream));
+        for (int s = first, end = first + n; s < end;) {
+            int run = 1;
+            if (stepKind(d, s, gap) == 0)
+                while (s + run < end && stepKind(d, s + run, gap) == 0) ++run;
+            if (run >= 2 && e->fuseIntegration) {
+                fusedSteps(e, dt, s, run, gap);
+                r.fusedRuns.emplace_back(s - first, run);
+            } else {
+                for (int k = 0; k < run; ++k) fullStep(e, dt, s + k, gap);
+            }
+            s += run;
+        }
+    } catch (...) {
+        cudaGraph_t junk = nullptr;
+        cudaStreamEndCapture(e->stream, &junk);
+        if (junk) cudaGraphDestroy(junk);
+        e->par = parity;
+        throw;
+    }
+    CK(cudaStreamEndCapture(e->stream, &r.graph));
+    e->par = parity;  // nothing ran
+    r.kernels = t_kernelLaunches - before;
+    e->capturedLaunches += r.kernels;
+    e->rounds.push_back(std::move(r));
+    return e->rounds.back();
+}
+
+}  // namespace
+
+struct demsph_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    // the graph launched last, the mapped status array it writes (per member
+    // {status, steps done}) and the device array of the members' status and
+    // step-count addresses it reads
+    cudaGraphExec_t exec = nullptr;
+    int2* report = nullptr;
+    int2* reportDev = nullptr;
+    int** where = nullptr;
+    // executable graphs of recent member sets (the current one first): a set
+    // that comes back (rounds cycling through phases) is not instantiated again
+    struct Cached {
+        std::vector<long long> key;
+        cudaGraphExec_t exec;
+        int2* report;   // the mapped status array the graph writes
+        int** where;    // the status addresses it reads
+    };
+    std::vector<Cached> cache;
+    demsph_batch_info info{};
+    std::string err;
+};
+
+extern "C" {
+
+int demsph_batch_create(int device, demsph_batch** out)
+{
+    if (!out) return DEMSPH_ERR_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return DEMSPH_ERR_NO_DEVICE;
+    auto* b = new demsph_batch;
+    b->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete b;
+        return DEMSPH_ERR_CUDA;
+    }
+    *out = b;
+    return DEMSPH_OK;
+}
+
+int demsph_batch_destroy(demsph_batch* b)
+{
+    if (!b) return DEMSPH_ERR_ARGUMENT;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (auto& c : b->cache) {
+        cudaGraphExecDestroy(c.exec);
+        cudaFreeHost(c.report);
+        cudaFree(c.where);
+    }
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return DEMSPH_OK;
+}
+
+const char* demsph_batch_last_error(const demsph_batch* b) { return b ? b->err.c_str() : "no batch"; }
+
+int demsph_batch_get_info(const demsph_batch* b, demsph_batch_info* out)
+{
+    if (!b || !out) return DEMSPH_ERR_ARGUMENT;
+    *out = b->info;
+    return DEMSPH_OK;
+}
+
+int demsph_batch_update(demsph_batch* b, demsph_engine* const* engines, int count, const int* first_step,
+                        const int* n_steps, const double* dt, const int* gap, int* status_out)
+{
+    if (!b || count < 0 || (count > 0 && (!engines || !first_step || !n_steps || !dt || !gap || !status_out)))
+        return DEMSPH_ERR_ARGUMENT;
+    struct Member {
+        int i;
+        demsph_engine* e;
+        const demsph_engine::RoundGraph* r;
+        int startPar;
+    };
+    std::vector<Member> members;
+    auto engineFail = [&](int i, demsph_engine* e, const CudaError& c) { status_out[i] = cudaFail(e, c); };
+    for (int i = 0; i < count; ++i) {
+        demsph_engine* e = engines[i];
+        status_out[i] = DEMSPH_OK;
+        if (!e || !e->stream || gap[i] < 1 || n_steps[i] < 0 || first_step[i] < 1) {
+            status_out[i] = DEMSPH_ERR_ARGUMENT;
+            continue;
+        }
+        if (!e->initialized) {
+            status_out[i] = fail(e, DEMSPH_ERR_STATE, "batch: engine not initialised");
+            continue;
+        }
+        if (e->device != b->device) {
+            status_out[i] = fail(e, DEMSPH_ERR_ARGUMENT, "batch: engine on another device");
+            continue;
+        }
+        LaunchTally tally(e);
+        try {
+            CK(cudaSetDevice(e->device));
+            int first = first_step[i], n = n_steps[i];
+            if (e->graphDt != dt[i] || e->graphGap != gap[i]) {
+                dropGraph(e);
+                e->graphDt = dt[i];
+                e->graphGap = gap[i];
+            }
+            // step 1 (it stores the Shepard reference sums), a step opened by a
+            // fused pass before an overflow, and profiled runs go alone
+            if (n > 0 && (first == 1 || e->resumeOpened || e->profiling)) {
+                const int alone = e->profiling ? n : 1;
+                const int rc = runUpdate(e, dt[i], first, alone, gap[i], 1, nullptr);
+                if (rc != DEMSPH_OK) {
+                    status_out[i] = rc;
+                    continue;
+                }
+                first += alone;
+                n -= alone;
+            }
+            if (n == 0) continue;
+            CK(cudaStreamSynchronize(e->stream));  // the member's own work before the batch
+            const auto tc = std::chrono::steady_clock::now();
+            const auto& r = roundFor(e, dt[i], first, n, gap[i]);
+            b->info.capture_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - tc).count();
+            members.push_back({i, e, &r, e->par});
+        } catch (const CudaError& c) {
+            engineFail(i, e, c);
+        }
+    }
+    if (members.empty()) return DEMSPH_OK;
+    const int m = (int)members.size();
+    try {
+        CK(cudaSetDevice(b->device));
+        std::vector<long long> key(m);
+        for (int k = 0; k < m; ++k) key[k] = members[k].r->id;
+        size_t hit = 0;
+        while (hit < b->cache.size() && b->cache[hit].key != key) ++hit;
+        if (hit < b->cache.size()) {
+            std::rotate(b->cache.begin(), b->cache.begin() + hit, b->cache.begin() + hit + 1);
+        } else {
+            const auto ti = std::chrono::steady_clock::now();
+            constexpr size_t KEEP = 4;
+            while (b->cache.size() >= KEEP) {  // the least recently used goes
+                auto& c = b->cache.back();
+                CK(cudaGraphExecDestroy(c.exec));
+                CK(cudaFreeHost(c.report));
+                CK(cudaFree(c.where));
+                b->cache.pop_back();
+            }
+            // each graph writes its own status array (mapped host memory)
+            CK(cudaHostAlloc(reinterpret_cast<void**>(&b->report), sizeof(int2) * m, cudaHostAllocMapped));
+            CK(cudaHostGetDevicePointer(reinterpret_cast<void**>(&b->reportDev), b->report, 0));
+            CK(cudaMalloc(reinterpret_cast<void**>(&b->where), sizeof(int*) * 2 * m));
+            std::vector<int*> where(2 * m);
+            for (int k = 0; k < m; ++k) {
+                where[2 * k] = members[k].e->d.status;
+                where[2 * k + 1] = members[k].e->d.stepsDone;
+            }
+            CK(cudaMemcpy(b->where, where.data(), sizeof(int*) * 2 * m, cudaMemcpyHostToDevice));
+            cudaGraph_t g;
+            CK(cudaGraphCreate(&g, 0));
+            std::vector<cudaGraphNode_t> nodes(m);
+            size_t total = 0;
+            for (int k = 0; k < m; ++k) {
+                CK(cudaGraphAddChildGraphNode(&nodes[k], g, nullptr, 0, members[k].r->graph));
+                size_t c = 0;
+                CK(cudaGraphGetNodes(members[k].r->graph, nullptr, &c));
+                total += c;
+            }
+            int** whereArg = b->where;
+            int nArg = m;
+            int2* outArg = b->reportDev;
+            void* args[] = {&whereArg, &nArg, &outArg};
+            cudaKernelNodeParams kp{};
+            kp.func = reinterpret_cast<void*>(kBatchReport);
+            kp.gridDim = dim3((unsigned)((m + 127) / 128));
+            kp.blockDim = dim3(128);
+            kp.kernelParams = args;
+            cudaGraphNode_t rep;
+            CK(cudaGraphAddKernelNode(&rep, g, nodes.data(), nodes.size(), &kp));
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess) {
+                cudaFreeHost(b->report);
+                cudaFree(b->where);
+            }
+            CK(ie);
+            b->cache.insert(b->cache.begin(), {key, exec, b->report, b->where});
+            ++b->info.graph_builds;
+            b->info.members = m;
+            b->info.nodes = (long long)total + 1;
+            b->info.instantiate_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - ti).count();
+        }
+        b->exec = b->cache.front().exec;
+        b->report = b->cache.front().report;
+        const auto tl = std::chrono::steady_clock::now();
+        CK(cudaGraphLaunch(b->exec, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+        b->info.launch_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - tl).count();
+        ++b->info.launches;
+    } catch (const CudaError& c) {
+        b->err = std::string(c.what) + ": " + cudaGetErrorString(c.e);
+        for (const auto& mb : members) status_out[mb.i] = cudaFail(mb.e, c);
+        return c.e == cudaErrorMemoryAllocation ? DEMSPH_ERR_OUT_OF_MEMORY : DEMSPH_ERR_CUDA;
+    }
+    for (int k = 0; k < m; ++k) {
+        const Member& mb = members[k];
+        demsph_engine* e = mb.e;
+        const int i = mb.i;
+        const int first = first_step[i] + (n_steps[i] - mb.r->length), n = mb.r->length, g = gap[i];
+        const int st = b->report[k].x, done = b->report[k].y;
+        e->replayedKernels += mb.r->kernels;
+        for (const auto& fr : mb.r->fusedRuns) e->runStats.fused_passes += fr.second - 1;
+        if (st == 0) {
+            e->par = mb.startPar ^ (n & 1);
+            continue;
+        }
+        LaunchTally tally(e);
+        try {
+            CK(cudaSetDevice(e->device));
+            if (st & ST_BARRIER_TIMEOUT) {
+                status_out[i] = fail(e, DEMSPH_ERR_TIMEOUT, "a grid barrier of a cooperative launch gave up waiting");
+                continue;
+            }
+            if (st & ~ALL_OVERFLOWS) {
+                status_out[i] = fail(e, DEMSPH_ERR_STATE, "unexpected device status " + std::to_string(st));
+                continue;
+            }
+            // as demsph_update after an overflow: the steps before the failed
+            // one completed; a step a fused pass opened resumes opened
+            const int step = first + done;
+            e->par = mb.startPar ^ (done & 1);
+            e->resumeOpened = false;
+            for (const auto& fr : mb.r->fusedRuns)
+                if (step > first + fr.first && step < first + fr.first + fr.second) e->resumeOpened = true;
+            if (e->resumeOpened) ++e->runStats.resumed_steps;
+            ++e->runStats.list_growths;
+            grow(e, st);
+            status_out[i] = runUpdate(e, dt[i], step, first + n - step, g, 1, nullptr);
+        } catch (const CudaError& c) {
+            engineFail(i, e, c);
+        }
+    }
+    return DEMSPH_OK;
 }
 
 }  // extern "C"

@@ -87,6 +87,18 @@ struct demsph_engine {
     bool keysAdvanced = false;
     demsph_run_stats runStats{};
     std::vector<CachedGraph> graphs;
+    // Step rounds captured for demsph_batch_update (graphs, not instantiated:
+    // a batch takes them as child graphs), keyed like the cached graphs plus
+    // the round's phase in the fluid and Shepard schedule.
+    struct RoundGraph {
+        int phase, length, parity, gap;
+        double dt;
+        cudaGraph_t graph;
+        long long id;     // unique over all engines: batches key on it
+        long long kernels;
+        std::vector<std::pair<int, int>> fusedRuns;  // (offset from the round's first step, length)
+    };
+    std::vector<RoundGraph> rounds;
     int graphGap = 0;
     double graphDt = 0;
     // contact tables as uploaded (FP32)
@@ -113,6 +125,7 @@ struct demsph_engine {
             cudaEventDestroy(t.b);
         }
         for (const auto& g : graphs) cudaGraphExecDestroy(g.exec);
+        for (const auto& r : rounds) cudaGraphDestroy(r.graph);
         for (const auto& a : owned) cudaFreeAsync(a.p, stream);
         if (stream) {
             cudaStreamSynchronize(stream);

@@ -11,7 +11,10 @@
 // A scene replays CUDA graphs while it is the only active one; in a mix it
 // launches its kernels directly (graph capture and instantiation next to
 // other scenes' work cost hundreds of times more than on an idle GPU, more
-// than the graphs save).  A scene that arrives while others run is
+// than the graphs save).  In batch mode one thread advances every active
+// scene together instead, a round of steps per scene in one graph launch
+// (demsph_batch_update); the workers then create engines (and run each
+// scene's first step) and download finished scenes.  A scene that arrives while others run is
 // admitted as soon as memory frees up (continuous batching).  A finished
 // scene's final state is downloaded, its engine destroyed and its memory
 // released before the next admission.
@@ -141,6 +144,10 @@ struct demsph_server {
     long long activeN = 0;        // admitted requests not yet finished
     double createS = 0, stepS = 0, downloadS = 0;   // worker time by activity
     std::map<int, int> lanesByClass;   // autotuned threads per fluid particle by log2(fluid count)
+    std::thread batcher;               // batch mode: the thread launching the rounds
+    long long batchRounds = 0;
+    demsph_batch_info batchInfo{};     // batch mode: the batch's figures (refreshed after each round)
+    Clock::time_point lastJoin;        // batch mode: when the batch's membership last grew
     bool anyAdmitted = false;
     Clock::time_point firstAdmit, lastFinish;
 
@@ -165,15 +172,143 @@ struct demsph_server {
     }
 
     // The active request not being advanced that waited longest (lock held).
+    // In batch mode the workers take only requests without an engine and
+    // requests whose steps are all done.
     Request* pick()
     {
         Request* best = nullptr;
         for (auto& kv : reqs) {
             Request& r = *kv.second;
             if (r.state != State::Active || r.busy) continue;
+            if (cfg.batch && r.eng && r.next <= r.steps) continue;
             if (!best || r.lastRun < best->lastRun) best = &r;
         }
         return best;
+    }
+
+    // Batch mode: steps of a scene's round - whole Shepard periods (5 gap
+    // steps with fluid), an even count (the contact-list parity repeats), about
+    // batch_round_steps - so that its captured round repeats.
+    int roundSteps(const Request& r) const
+    {
+        const int per = r.scene->s.n_fluid > 0 ? 5 * r.gap : 1;
+        const int target = cfg.batch_round_steps;
+        int n = per * std::max(1, (target + per / 2) / per);
+        if (n & 1) n *= 2;
+        return std::min(n, r.steps - r.next + 1);
+    }
+
+    void batchLoop()
+    {
+        demsph_batch* b = nullptr;
+        const int brc = demsph_batch_create(cfg.device, &b);
+        std::unique_lock<std::mutex> lock(m);
+        std::vector<Request*> mem;
+        std::vector<demsph_engine*> eng;
+        std::vector<int> first, n, gap, st;
+        std::vector<double> dt;
+        std::vector<long long> ids;  // the members of the last round
+        while (true) {
+            auto ready = [&](const Request& r) {
+                return r.state == State::Active && !r.busy && r.eng && r.next <= r.steps;
+            };
+            auto creating = [&] {
+                for (auto& kv : reqs)
+                    if (kv.second->state == State::Active && !kv.second->eng) return true;
+                return false;
+            };
+            cv.wait(lock, [&] {
+                if (stop) return true;
+                for (auto& kv : reqs)
+                    if (ready(*kv.second)) return true;
+                return false;
+            });
+            if (stop) break;
+            if (brc != DEMSPH_OK) {  // no batch: the requests fail
+                for (auto& kv : reqs) {
+                    Request& r = *kv.second;
+                    if (!ready(r)) continue;
+                    r.status = brc;
+                    r.error = "demsph_batch_create failed";
+                    demsph_destroy(r.eng);
+                    r.eng = nullptr;
+                    finish(r, State::Failed);
+                }
+                continue;
+            }
+            // members: last round's members still running, plus newcomers -
+            // newcomers join when no engine is being created, or 1 s after the
+            // membership last grew (each change instantiates a new graph; the
+            // first round waits the same way for the engines being created)
+            if (ids.empty() && lastJoin == Clock::time_point{}) lastJoin = Clock::now();
+            const bool admitNew = !creating() || seconds(lastJoin, Clock::now()) > 1.0;
+            mem.clear();
+            bool grew = false;
+            for (auto& kv : reqs) {
+                Request& r = *kv.second;
+                if (!ready(r)) continue;
+                const bool old = std::find(ids.begin(), ids.end(), r.id) != ids.end();
+                if (!old && !admitNew) continue;
+                grew |= !old;
+                mem.push_back(&r);
+            }
+            if (mem.empty()) {  // only newcomers, held back: wait for them briefly
+                cv.wait_for(lock, std::chrono::milliseconds(10));
+                continue;
+            }
+            if (grew) lastJoin = Clock::now();
+            const size_t k = mem.size();
+            eng.resize(k);
+            first.resize(k);
+            n.resize(k);
+            gap.resize(k);
+            st.resize(k);
+            dt.resize(k);
+            ids.clear();
+            for (size_t q = 0; q < k; ++q) {
+                Request& r = *mem[q];
+                r.busy = true;
+                eng[q] = r.eng;
+                first[q] = r.next;
+                n[q] = roundSteps(r);
+                gap[q] = r.gap;
+                dt[q] = r.dt;
+                ids.push_back(r.id);
+            }
+            lock.unlock();
+            const auto t0 = Clock::now();
+            const int rc = demsph_batch_update(b, eng.data(), (int)k, first.data(), n.data(), dt.data(), gap.data(),
+                                               st.data());
+            const double wall = seconds(t0, Clock::now());
+            lock.lock();
+            ++batchRounds;
+            stepS += wall;
+            demsph_batch_get_info(b, &batchInfo);
+            for (size_t q = 0; q < k; ++q) {
+                Request& r = *mem[q];
+                r.busy = false;
+                r.lastRun = Clock::now();
+                const int code = rc != DEMSPH_OK ? rc : st[q];
+                if (code != DEMSPH_OK) {
+                    r.status = code;
+                    r.error = demsph_last_error(r.eng);
+                    demsph_destroy(r.eng);
+                    r.eng = nullptr;
+                    finish(r, State::Failed);
+                    continue;
+                }
+                long long fluidSteps = 0;
+                for (int s2 = r.next; s2 < r.next + n[q]; ++s2) fluidSteps += (s2 % r.gap == 0);
+                updates += fluidSteps * r.scene->s.n_fluid + (long long)n[q] * r.mobile;
+                stepsRun += n[q];
+                stepMs.push_back(1e3 * wall / std::max(1, n[q]));
+                r.next += n[q];
+            }
+            cv.notify_all();  // finished scenes go to the workers
+        }
+        if (b) demsph_batch_get_info(b, &batchInfo);
+        lock.unlock();
+        if (b) demsph_batch_destroy(b);
     }
 
     void finish(Request& r, State s)
@@ -226,7 +361,16 @@ struct demsph_server {
             int n = 0;
             long long upd = 0;
             double ms = 0;
-            if (rc == DEMSPH_OK) {
+            if (rc == DEMSPH_OK && cfg.batch && r->next == 1) {
+                // the first step alone (it stores the Shepard reference sums),
+                // so that the batch's rounds all start past it
+                const auto t0 = Clock::now();
+                rc = demsph_update(r->eng, r->dt, 1, 1, r->gap, 0);
+                tStep = seconds(t0, Clock::now());
+                n = 1;
+                ms = 1e3 * tStep;
+                upd = (1 % r->gap == 0 ? r->scene->s.n_fluid : 0) + r->mobile;
+            } else if (rc == DEMSPH_OK && !cfg.batch) {
                 n = std::min(cfg.chunk_steps, r->steps - r->next + 1);
                 const auto t0 = Clock::now();
                 rc = demsph_update(r->eng, r->dt, r->next, n, r->gap, useGraph);
@@ -260,7 +404,7 @@ struct demsph_server {
                 continue;
             }
             r->next += n;
-            stepMs.push_back(ms);
+            if (n > 0) stepMs.push_back(ms);
             updates += upd;
             stepsRun += n;
             if (done) finish(*r, State::Done);
@@ -301,10 +445,12 @@ int demsph_server_create(const demsph_server_config* cfg, demsph_server** out)
     if (c.hbm_budget_bytes <= 0) c.hbm_budget_bytes = 150LL << 30;
     if (c.workers <= 0) c.workers = 8;  // the mix measured fastest with 8 to 16 (16 host cores)
     if (c.chunk_steps <= 0) c.chunk_steps = 100;
+    if (c.batch_round_steps <= 0) c.batch_round_steps = 20;
     if (c.workers > 256 || c.graphs < -1 || c.graphs > 1) return DEMSPH_ERR_ARGUMENT;
     auto* s = new demsph_server;
     s->cfg = c;
     for (int k = 0; k < c.workers; ++k) s->workers.emplace_back([s] { s->work(); });
+    if (c.batch) s->batcher = std::thread([s] { s->batchLoop(); });
     *out = s;
     return DEMSPH_OK;
 }
@@ -318,6 +464,7 @@ int demsph_server_destroy(demsph_server* s)
     }
     s->cv.notify_all();
     for (auto& t : s->workers) t.join();
+    if (s->batcher.joinable()) s->batcher.join();
     for (auto& kv : s->reqs)
         if (kv.second->eng) demsph_destroy(kv.second->eng);
     delete s;
@@ -442,6 +589,11 @@ int demsph_server_stats(demsph_server* s, demsph_server_summary* st)
     st->step_s = s->stepS;
     st->download_s = s->downloadS;
     st->peak_bytes = s->peak;
+    st->batch_rounds = s->batchInfo.launches;
+    st->batch_graph_builds = s->batchInfo.graph_builds;
+    st->batch_capture_s = s->batchInfo.capture_s;
+    st->batch_instantiate_s = s->batchInfo.instantiate_s;
+    st->batch_launch_s = s->batchInfo.launch_s;
     if (s->anyAdmitted) {
         const auto end = (s->completed + s->failed == s->admittedN && s->pending.empty()) ? s->lastFinish : Clock::now();
         st->busy_s = seconds(s->firstAdmit, end);

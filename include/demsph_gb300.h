@@ -396,6 +396,38 @@ DEMSPH_API int demsph_audit(demsph_engine* e, demsph_audit_values* out);
 /* Shepard reference sums sumW0 (core/integrate.cu:44-47). */
 DEMSPH_API int demsph_export_fluid_sumw0(demsph_engine* e, double* sumw0);
 
+/* ---- many scenes in one graph launch ----
+   No counterpart in the reference (one scene per process).  One call advances
+   engines[0..count) by n_steps[k] steps from first_step[k] each (time step
+   dt[k], fluid gap gap[k]), all in one CUDA graph launch: each engine's round
+   of steps is a child graph, captured once per (phase in the fluid and
+   Shepard schedule, length, contact-list parity, dt, gap), the children run as
+   independent branches, and the executable graph is reused while every
+   member's round repeats (rounds of even length that are multiples of
+   5 gap steps repeat).  Every scene's state afterwards is bit for bit its state
+   after demsph_update over the same steps.  Step 1 and profiled runs go
+   through demsph_update first; a member whose lists overflowed grows them and
+   finishes its steps alone before the call returns.  status_out[k] receives
+   each engine's status (its message in demsph_last_error); the return value
+   is DEMSPH_OK unless the launch itself failed.  All engines on the batch's
+   device; none may be used by another thread during the call. */
+typedef struct demsph_batch demsph_batch;
+typedef struct demsph_batch_info {
+    long long launches;      /* graph launches so far */
+    long long graph_builds;  /* executable graphs instantiated (member rounds changed) */
+    long long members;       /* engines in the last built graph */
+    long long nodes;         /* nodes in it */
+    double capture_s;        /* host time spent capturing members' rounds */
+    double instantiate_s;    /* host time spent building and instantiating the batch graphs */
+    double launch_s;         /* host time from each launch to its completion */
+} demsph_batch_info;
+DEMSPH_API int demsph_batch_create(int device, demsph_batch** out);
+DEMSPH_API int demsph_batch_destroy(demsph_batch* b);
+DEMSPH_API int demsph_batch_update(demsph_batch* b, demsph_engine* const* engines, int count, const int* first_step,
+                                   const int* n_steps, const double* dt, const int* gap, int* status_out);
+DEMSPH_API int demsph_batch_get_info(const demsph_batch* b, demsph_batch_info* out);
+DEMSPH_API const char* demsph_batch_last_error(const demsph_batch* b);
+
 /* ---- scene server: many scenes on one GPU ----
    No counterpart in the reference (one scene per process).  Scenes are
    submitted with a step count, admitted first come, first served while their
@@ -416,6 +448,11 @@ typedef struct demsph_server_config {
                                     instantiating graphs while other scenes' kernels run was measured
                                     hundreds of times slower than on an idle GPU, so scenes in a mix
                                     launch their kernels directly (the same results, bit for bit) */
+    int batch;                   /* != 0: one host thread advances all active scenes together, each
+                                    round one demsph_batch_update launch (rounds of about
+                                    batch_round_steps steps, whole Shepard periods); workers then
+                                    only create engines and download results */
+    int batch_round_steps;       /* 0 = 20 */
 } demsph_server_config;
 typedef struct demsph_server_summary {
     long long submitted, admitted, completed, failed, pending;
@@ -428,6 +465,8 @@ typedef struct demsph_server_summary {
     double p50_step_ms, p99_step_ms;     /* wall time per scene step, queueing for the GPU included */
     double create_s, step_s, download_s; /* worker time summed over workers: engine creation and
                                             initialisation, stepping, downloading results */
+    long long batch_rounds, batch_graph_builds;    /* batch mode: launches, graphs instantiated */
+    double batch_capture_s, batch_instantiate_s, batch_launch_s;  /* batch mode: time in each */
 } demsph_server_summary;
 typedef struct demsph_request_info {
     int state;                   /* 0 pending, 1 running, 2 done, 3 failed */

@@ -72,14 +72,24 @@ def test_server_rejects_a_scene_over_the_budget(ds, scenes):
         srv.close()
 
 
+def test_batch_needs_a_gpu(ds):
+    """No GPU here: creating a batch reports DEMSPH_ERR_NO_DEVICE."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(ds.DemSphError) as e:
+        ds.Batch(0)
+    assert e.value.status == 4
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("graphs", [0, 1, -1])
-def test_mix_equals_alone(ds, scenes, graphs):
-    """In the mix, scenes launch directly (graphs 0: several are active; -1)
-    or replay graphs (1); each result has the bits of the scene run alone
-    from graphs."""
+@pytest.mark.parametrize("graphs,batch", [(0, False), (1, False), (-1, False), (0, True)])
+def test_mix_equals_alone(ds, scenes, graphs, batch):
+    """In the mix, scenes launch directly (graphs 0: several are active; -1),
+    replay graphs (1), or advance together in one graph launch per round
+    (batch); each result has the bits of the scene run alone from graphs."""
     built = [(ds.build_scene(getattr(scenes, name)()), steps) for name, steps in MIX]
-    srv = ds.Server(workers=4, chunk_steps=7, graphs=graphs)
+    srv = ds.Server(workers=4, chunk_steps=7, graphs=graphs, batch=batch, batch_round_steps=10)
     try:
         ids = [srv.submit(sc, steps) for (_, sc), steps in built]
         srv.wait(-1, 600.0)
@@ -166,3 +176,94 @@ def test_autotuning_server_completes_the_mix(ds, scenes):
                 assert np.allclose(got["solid_pos"], s["pos"], rtol=0, atol=1e-9)
     finally:
         srv.close()
+
+
+def _batched(ds, built, rounds, **opts):
+    """Engines of `built` [(scene, steps)] advanced by a Batch in rounds of
+    (at most) the given lengths, cycling; returns the engines and the batch."""
+    engines = [ds.Engine(sc, **opts) for sc, _ in built]
+    for e in engines:
+        e.initialize()
+    b = ds.Batch(0)
+    nxt = [1] * len(built)
+    r = 0
+    while any(n <= steps for n, (_, steps) in zip(nxt, built)):
+        live = [k for k, (sc, steps) in enumerate(built) if nxt[k] <= steps]
+        ln = [min(rounds[r % len(rounds)], built[k][1] - nxt[k] + 1) for k in live]
+        st = b.update([engines[k] for k in live], [nxt[k] for k in live], ln,
+                      [built[k][0].time_step for k in live], [built[k][0].fluid_integrate_gap for k in live])
+        assert st == [0] * len(live)
+        for k, n in zip(live, ln):
+            nxt[k] += n
+        r += 1
+    return engines, b
+
+
+def _state(eng, sc):
+    f = eng.download_fluids() if sc.n_fluid else None
+    s = eng.download_solids() if sc.n_solid else None
+    return f, s
+
+
+def _equal(a, b):
+    (fa, sa), (fb, sb) = a, b
+    if fa is not None:
+        for x, y in zip(fa, fb):
+            assert np.array_equal(x, y)
+    if sa is not None:
+        for k in ("pos", "vel", "angvel", "acc", "torque"):
+            assert np.array_equal(sa[k], sb[k]), k
+
+
+@pytest.mark.gpu
+def test_batch_rounds_equal_alone(ds, scenes):
+    """demsph_batch_update over scenes of different kinds and gaps, rounds of
+    odd and even lengths, from step 1: every state equals the scene run alone,
+    bit for bit."""
+    built = [(sc, steps) for ((_, sc), steps) in [(ds.build_scene(getattr(scenes, n)()), st) for n, st in MIX]]
+    engines, b = _batched(ds, built, [7, 10, 3, 30])
+    for e, (sc, steps) in zip(engines, built):
+        alone = ds.Engine(sc)
+        alone.initialize()
+        alone.update(sc.time_step, 1, steps, sc.fluid_integrate_gap, use_graph=True)
+        _equal(_state(e, sc), _state(alone, sc))
+    assert b.info()["launches"] > 0
+
+
+@pytest.mark.gpu
+def test_batch_reuses_its_graph_for_repeating_rounds(ds, scenes):
+    """Rounds that are whole Shepard periods of even length repeat: after the
+    first rounds the same executable graph is launched again."""
+    _, a = ds.build_scene(scenes.tiny_dam_break())
+    _, c = ds.build_scene(scenes.tiny_granular())
+    built = [(a, 1 + 8 * 10), (c, 1 + 8 * 10)]
+    engines = [ds.Engine(sc) for sc, _ in built]
+    for e, (sc, _) in zip(engines, built):
+        e.initialize()
+        e.update(sc.time_step, 1, 1, sc.fluid_integrate_gap)
+    b = ds.Batch(0)
+    for r in range(8):
+        st = b.update(engines, [2 + 10 * r] * 2, [10, 10], [a.time_step, c.time_step],
+                      [a.fluid_integrate_gap, c.fluid_integrate_gap])
+        assert st == [0, 0]
+    info = b.info()
+    # a list growth in the first rounds drops the member's graphs (a rebuild)
+    assert info["launches"] == 8 and info["graph_builds"] <= 3 and info["members"] == 2
+
+
+@pytest.mark.gpu
+def test_batch_member_overflow_grows_and_matches(ds, scenes):
+    """Lists too small for the scene: members overflow inside the batched
+    round, grow their lists, finish the round alone and end bit for bit where
+    the same engine options end alone."""
+    opts = dict(fluid_neighbors_max=8, fluid_solids_max=2, solid_contacts_per_particle=1)
+    built = [(ds.build_scene(scenes.tiny_coupled())[1], 40), (ds.build_scene(scenes.tiny_granular())[1], 40)]
+    engines, _ = _batched(ds, built, [20], **opts)
+    grown = 0
+    for e, (sc, steps) in zip(engines, built):
+        grown += e.run_stats()["list_growths"]
+        alone = ds.Engine(sc, **opts)
+        alone.initialize()
+        alone.update(sc.time_step, 1, steps, sc.fluid_integrate_gap, use_graph=True)
+        _equal(_state(e, sc), _state(alone, sc))
+    assert grown > 0
