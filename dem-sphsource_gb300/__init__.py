@@ -374,6 +374,15 @@ class Engine:
     def neighbor_search(self, i_step, gap):
         self._chk(self.lib.demsph_neighbor_search(self.h, _I(i_step), _I(gap)), "demsph_neighbor_search")
 
+    def append(self, current, additions):
+        """Adds the particles of scene `additions` while the simulation runs
+        (demsph_append); `current` is the scene as it stands (its parameters
+        and tables; the state is the engine's).  Returns the new counts."""
+        self._chk(self.lib.demsph_append(self.h, C.byref(current), C.byref(additions)), "demsph_append")
+        self.nf += additions.n_fluid
+        self.ns += additions.n_solid
+        return self.nf, self.ns
+
     def solid_integrate_before_contact(self, dt):
         self._chk(self.lib.demsph_solid_integrate_before_contact(self.h, _D(dt)), "before_contact")
 

@@ -637,6 +637,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
         *out = e;  // keep the message readable
         return rc;
     }
+    e->opt = o;
     try {
         e->device = o.device;
         CK(cudaSetDevice(o.device));
@@ -1874,6 +1875,358 @@ int demsph_batch_update(demsph_batch* b, demsph_engine* const* engines, int coun
         }
     }
     return DEMSPH_OK;
+}
+
+}  // extern "C"
+
+// ---- particles added while a simulation runs (demsph_append) ----
+//
+// dataBase::addFluidData / addSolidData after the start (core/dataBase.cpp:
+// 226-268) re-upload the whole state with the new particles appended and
+// recompute the spatial grid; addCluster then searches again and bonds the new
+// cluster (core/dataBase.cpp:83-113, 307-343).  Here an engine for the whole
+// scene is made on the same device and the old engine's histories are carried
+// into it on the device: the contact list of the last step with its springs
+// (as the previous list, so the first search remaps them pair by pair), the
+// bonds and their states, the wall and pebble normals, and the Shepard
+// reference sums.  As in the reference: the new particles come after the old
+// ones in index order, the wall springs start again from zero (it rebuilds
+// solid2InfiniteWall), new solids have zero normals (setSolidNormal runs only
+// at the start), and only pairs of a new cluster above the last bonded index
+// are bonded.  Two differences, both stated in the header: the neighbour lists
+// are rebuilt at once for every kind of addition (the reference rebuilds them
+// at the next search, or at once for a cluster), and the new fluids' Shepard
+// reference sums are taken at the append (the reference leaves them zero, and
+// its next re-initialisation divides by them).
+namespace {
+
+__global__ void kCarryContacts(DeviceState o, int op, DeviceState n, int np)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= o.nrow) return;
+    const int a = solidOf(o, r);
+    const int nr = rowOf(n, a);
+    if (nr < 0) return;
+    const int cnt = min(min(o.fcnt[op][r], o.scap), n.scap);
+    for (int q = 0; q < cnt; ++q) {
+        const size_t src = (size_t)q * o.nrow + r, dst = (size_t)q * n.nrow + nr;
+        n.fwd[np][dst] = o.fwd[op][src];
+        for (int j = 0; j < 3; ++j) n.springOut[np][j][dst] = o.springOut[op][j][src];
+    }
+    n.fcnt[np][nr] = cnt;
+}
+
+__global__ void kSlotOfId(DeviceState n, int* slotOf)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n.nf) slotOf[n.fid[s]] = s;
+}
+
+__global__ void kCarrySumW0(DeviceState o, DeviceState n, const int* slotOf)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < o.nf) n.fsumW0[slotOf[o.fid[s]]] = o.fsumW0[s];
+}
+
+template <class T>
+std::vector<T> fetch(const T* p, size_t n, cudaStream_t s)
+{
+    std::vector<T> v(n);
+    if (n) CK(cudaMemcpyAsync(v.data(), p, sizeof(T) * n, cudaMemcpyDeviceToHost, s));
+    return v;
+}
+
+template <class T>
+void put(T* p, const std::vector<T>& v, cudaStream_t s)
+{
+    if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+}
+
+// The bonds of engine n: the old engine's bonds as they stand, then - when the
+// addition holds a cluster - the bonds initialisation makes in n for pairs
+// whose first solid is above the last bonded one (addBondData after the
+// start, core/dataBase.cpp:307-343); and the per-solid bond lists.
+void carryBonds(demsph_engine* old, demsph_engine* n, bool cluster)
+{
+    DeviceState& o = old->d;
+    DeviceState& d = n->d;
+    const cudaStream_t s = n->stream;
+    const int nbOld = o.nb;
+    std::vector<int2> ab = fetch(o.bab, nbOld, old->stream);
+    std::vector<int> on = fetch(o.bon, nbOld, old->stream);
+    std::vector<float4> st[7] = {fetch(o.bFnTt, nbOld, old->stream), fetch(o.bFsH, nbOld, old->stream),
+                                 fetch(o.bFsL, nbOld, old->stream), fetch(o.bTbH, nbOld, old->stream),
+                                 fetch(o.bTbL, nbOld, old->stream), fetch(o.bN, nbOld, old->stream),
+                                 fetch(o.bLever, nbOld, old->stream)};
+    CK(cudaStreamSynchronize(old->stream));
+    const long long nslots = (long long)d.nrow * d.scap;
+    if (cluster && nslots > 0 && nslots <= 2000000000LL) {
+        // every bond initialisation would make, in n's arrays (then filtered)
+        std::vector<Allocation> tmp;
+        int* flag = dalloc<int>((size_t)nslots + 1, tmp, s);
+        int* pos = dalloc<int>((size_t)nslots + 1, tmp, s);
+        int* work = dalloc<int>(scanWorkspaceInts((int)nslots), tmp, s);
+        const int nb = launchBondFlags(d, n->par, flag, pos, work, s);
+        if (nb > 0) {
+            DeviceState t = d;
+            std::vector<Allocation> arr;
+            t.bab = dalloc<int2>(nb, arr, s);
+            t.bon = dalloc<int>(nb, arr, s);
+            t.bFnTt = dalloc<float4>(nb, arr, s);
+            t.bFsH = dalloc<float4>(nb, arr, s);
+            t.bFsL = dalloc<float4>(nb, arr, s);
+            t.bTbH = dalloc<float4>(nb, arr, s);
+            t.bTbL = dalloc<float4>(nb, arr, s);
+            t.bN = dalloc<float4>(nb, arr, s);
+            t.bLever = dalloc<float4>(nb, arr, s);
+            t.bF = dalloc<float4>(nb, arr, s);
+            t.bTA = dalloc<float4>(nb, arr, s);
+            t.bTB = dalloc<float4>(nb, arr, s);
+            t.nb = nb;
+            launchBondWrite(t, n->par, flag, pos, s);
+            std::vector<int2> nab = fetch(t.bab, nb, s);
+            std::vector<int> non = fetch(t.bon, nb, s);
+            std::vector<float4> nst[7] = {fetch(t.bFnTt, nb, s), fetch(t.bFsH, nb, s), fetch(t.bFsL, nb, s),
+                                          fetch(t.bTbH, nb, s), fetch(t.bTbL, nb, s), fetch(t.bN, nb, s),
+                                          fetch(t.bLever, nb, s)};
+            CK(cudaStreamSynchronize(s));
+            const int last = nbOld > 0 ? ab.back().x : -1;
+            for (int b = 0; b < nb; ++b) {
+                if (nab[b].x <= last) continue;
+                ab.push_back(nab[b]);
+                on.push_back(non[b]);
+                for (int k = 0; k < 7; ++k) st[k].push_back(nst[k][b]);
+            }
+            for (const auto& a : arr) cudaFreeAsync(a.p, s);
+        }
+        CK(cudaStreamSynchronize(s));
+        for (const auto& a : tmp) cudaFreeAsync(a.p, s);
+    }
+    const int nb = (int)ab.size();
+    d.nb = nb;
+    if (nb > 0) {
+        d.bab = dalloc<int2>(nb, n->owned, s);
+        d.bon = dalloc<int>(nb, n->owned, s);
+        d.bFnTt = dalloc<float4>(nb, n->owned, s);
+        d.bFsH = dalloc<float4>(nb, n->owned, s);
+        d.bFsL = dalloc<float4>(nb, n->owned, s);
+        d.bTbH = dalloc<float4>(nb, n->owned, s);
+        d.bTbL = dalloc<float4>(nb, n->owned, s);
+        d.bN = dalloc<float4>(nb, n->owned, s);
+        d.bLever = dalloc<float4>(nb, n->owned, s);
+        d.bF = dalloc<float4>(nb, n->owned, s);
+        d.bTA = dalloc<float4>(nb, n->owned, s);
+        d.bTB = dalloc<float4>(nb, n->owned, s);
+        put(d.bab, ab, s);
+        put(d.bon, on, s);
+        float4* dst[7] = {d.bFnTt, d.bFsH, d.bFsL, d.bTbH, d.bTbL, d.bN, d.bLever};
+        for (int k = 0; k < 7; ++k) put(dst[k], st[k], s);
+    }
+    // bonds of each solid, in bond order (as demsph_initialize)
+    std::vector<int> start((size_t)d.ns + 1, 0), list(2 * (size_t)nb);
+    for (const int2& p : ab) {
+        start[p.x + 1]++;
+        start[p.y + 1]++;
+    }
+    for (int i = 0; i < d.ns; ++i) start[i + 1] += start[i];
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int b = 0; b < nb; ++b) {
+        list[fill[ab[b].x]++] = b;
+        list[fill[ab[b].y]++] = b;
+    }
+    d.bondStart = dalloc<int>((size_t)d.ns + 1, n->owned, s);
+    d.bondList = dalloc<int>(list.size(), n->owned, s);
+    put(d.bondStart, start, s);
+    put(d.bondList, list, s);
+    CK(cudaStreamSynchronize(s));
+}
+
+}  // namespace
+
+extern "C" {
+
+int demsph_append(demsph_engine* e, const demsph_scene* cur, const demsph_scene* add)
+{
+    if (!cur || !add) return DEMSPH_ERR_ARGUMENT;
+    ENGINE_GUARD(e)
+    REQUIRE_INIT(e);
+    DeviceState& d = e->d;
+    if (cur->n_fluid != d.nf || cur->n_solid != d.ns || cur->n_clump != d.nc || cur->n_wall != d.nw)
+        return fail(e, DEMSPH_ERR_ARGUMENT, "append: the current scene's counts differ from the engine's");
+    if (add->n_clump != 0 || add->n_wall != 0)
+        return fail(e, DEMSPH_ERR_ARGUMENT,
+                    "append: walls and clumps can only be added before the simulation starts");
+    if (add->n_fluid < 0 || add->n_solid < 0 || (add->n_fluid == 0 && add->n_solid == 0))
+        return fail(e, DEMSPH_ERR_ARGUMENT, "append: nothing to add");
+    for (int i = 0; i < add->n_solid; ++i)
+        if (add->solid_material[i] < 0 || add->solid_material[i] >= cur->n_material)
+            return fail(e, DEMSPH_ERR_ARGUMENT, "append: material index exceeds the number of materials");
+    CK(cudaStreamSynchronize(e->stream));
+    const size_t nf0 = d.nf, ns0 = d.ns, nc = d.nc, af = add->n_fluid, as = add->n_solid;
+    const size_t nf = nf0 + af, ns = ns0 + as;
+    // the state as it stands, FP64 in original order
+    std::vector<double> fpos(3 * nf), fvel(3 * nf), facc(3 * nf), fdr(nf);
+    std::vector<double> spos(3 * ns), svel(3 * ns), sacc(3 * ns), snrm(3 * ns), stq(3 * ns), sw(3 * ns);
+    enqueueDownloadFluids(e, fpos.data(), fvel.data(), facc.data(), fdr.data());
+    enqueueDownloadSolids(e, spos.data(), svel.data(), sacc.data(), snrm.data(), stq.data(), sw.data());
+    CK(cudaStreamSynchronize(e->stream));
+    std::vector<double> cc(3 * nc), cv(3 * nc), ca(3 * nc), cw(3 * nc), ct(3 * nc), cq(4 * nc);
+    if (nc) {
+        const int rc = demsph_download_clumps(e, cc.data(), cv.data(), ca.data(), cw.data(), ct.data(), cq.data());
+        if (rc != DEMSPH_OK) return rc;
+    }
+    // the whole scene: the current one's parameters and state, then the additions
+    auto cat = [](std::vector<double>& v, size_t at, const double* src, size_t n, double fill) {
+        for (size_t k = 0; k < n; ++k) v[at + k] = src ? src[k] : fill;
+    };
+    std::vector<double> fh(nf), rho0(nf), c(nf), nu(nf);
+    cat(fh, 0, cur->fluid_smoothing_length, nf0, 0);
+    cat(rho0, 0, cur->fluid_rho0, nf0, 0);
+    cat(c, 0, cur->fluid_sound_speed, nf0, 0);
+    cat(nu, 0, cur->fluid_nu, nf0, 0);
+    cat(fpos, 3 * nf0, add->fluid_position, 3 * af, 0);
+    cat(fvel, 3 * nf0, add->fluid_velocity, 3 * af, 0);
+    cat(facc, 3 * nf0, add->fluid_acceleration, 3 * af, 0);
+    cat(fdr, nf0, add->fluid_drho, af, 0);
+    cat(fh, nf0, add->fluid_smoothing_length, af, 0);
+    cat(rho0, nf0, add->fluid_rho0, af, 0);
+    cat(c, nf0, add->fluid_sound_speed, af, 0);
+    cat(nu, nf0, add->fluid_nu, af, 0);
+    std::vector<double> seff(ns), srad(ns), sim(ns);
+    std::vector<int> smat(ns), sclu(ns), sclump(ns), sdum(ns);
+    cat(seff, 0, cur->solid_effective_radius, ns0, 0);
+    cat(srad, 0, cur->solid_radius, ns0, 0);
+    cat(sim, 0, cur->solid_inverse_mass, ns0, 0);
+    cat(spos, 3 * ns0, add->solid_position, 3 * as, 0);
+    cat(svel, 3 * ns0, add->solid_velocity, 3 * as, 0);
+    cat(sacc, 3 * ns0, add->solid_acceleration, 3 * as, 0);
+    cat(snrm, 3 * ns0, nullptr, 3 * as, 0);  // new solids: zero normals
+    cat(stq, 3 * ns0, add->solid_torque, 3 * as, 0);
+    cat(sw, 3 * ns0, add->solid_angular_velocity, 3 * as, 0);
+    cat(seff, ns0, add->solid_effective_radius, as, 0);
+    cat(srad, ns0, add->solid_radius, as, 0);
+    cat(sim, ns0, add->solid_inverse_mass, as, 0);
+    bool cluster = false;
+    for (size_t i = 0; i < ns0; ++i) {
+        smat[i] = cur->solid_material[i];
+        sclu[i] = cur->solid_cluster ? cur->solid_cluster[i] : -1;
+        sclump[i] = cur->solid_clump ? cur->solid_clump[i] : -1;
+        sdum[i] = cur->solid_is_dummy ? cur->solid_is_dummy[i] : 0;
+    }
+    for (size_t i = 0; i < as; ++i) {
+        smat[ns0 + i] = add->solid_material[i];
+        sclu[ns0 + i] = add->solid_cluster ? add->solid_cluster[i] : -1;
+        sclump[ns0 + i] = -1;
+        sdum[ns0 + i] = add->solid_is_dummy ? add->solid_is_dummy[i] : 0;
+        cluster |= sclu[ns0 + i] >= 0;
+    }
+    demsph_scene sc = *cur;
+    for (int a = 0; a < 3; ++a) sc.gravity[a] = d.g64[a];  // as set at run time
+    sc.n_fluid = (int)nf;
+    sc.fluid_position = fpos.data();
+    sc.fluid_velocity = fvel.data();
+    sc.fluid_acceleration = facc.data();
+    sc.fluid_smoothing_length = fh.data();
+    sc.fluid_rho0 = rho0.data();
+    sc.fluid_drho = fdr.data();
+    sc.fluid_sound_speed = c.data();
+    sc.fluid_nu = nu.data();
+    sc.n_solid = (int)ns;
+    sc.solid_position = spos.data();
+    sc.solid_velocity = svel.data();
+    sc.solid_acceleration = sacc.data();
+    sc.solid_normal = snrm.data();
+    sc.solid_torque = stq.data();
+    sc.solid_angular_velocity = sw.data();
+    sc.solid_effective_radius = seff.data();
+    sc.solid_radius = srad.data();
+    sc.solid_inverse_mass = sim.data();
+    sc.solid_material = smat.data();
+    sc.solid_cluster = sclu.data();
+    sc.solid_clump = sclump.data();
+    sc.solid_is_dummy = sdum.data();
+    if (nc) {
+        sc.clump_centroid = cc.data();
+        sc.clump_velocity = cv.data();
+        sc.clump_acceleration = ca.data();
+        sc.clump_angular_velocity = cw.data();
+        sc.clump_torque = ct.data();
+        sc.clump_orientation = cq.data();
+    }
+    // the same options, with the lists as large as they have grown
+    demsph_options o = e->opt;
+    o.device = e->device;
+    o.fluid_neighbors_max = std::max(o.fluid_neighbors_max, d.kff);
+    o.fluid_solids_max = std::max(o.fluid_solids_max, d.kfs);
+    o.solid_contacts_per_particle = std::max(o.solid_contacts_per_particle, d.scap);
+    demsph_engine* n = nullptr;
+    int rc = demsph_create(&sc, &o, &n);
+    if (rc != DEMSPH_OK) {
+        const std::string msg = n ? n->err : std::string(demsph_status_string(rc));
+        if (n) demsph_destroy(n);
+        return fail(e, rc, "append: " + msg);
+    }
+    try {
+        DeviceState& nd = n->d;
+        const cudaStream_t s = n->stream;
+        // the last contact list and its springs as n's previous list
+        if (d.nrow > 0 && nd.nrow > 0)
+            ++t_kernelLaunches, kCarryContacts<<<blocksFor(d.nrow, 128), 128, 0, s>>>(d, e->par, nd, n->par);
+        CK(cudaStreamSynchronize(s));
+        n->forceWalk = true;  // the list in the reference's walk order (bonds are numbered in it)
+        rc = neighborSearchChecked(n, 0, 1);
+        n->forceWalk = false;
+        if (rc != DEMSPH_OK) throw rc;
+        carryBonds(e, n, cluster);
+        if (nd.nrow > 0 && n->adaptRows) {
+            int stats[2] = {0, 0};
+            launchRowStats(nd, n->par, s);
+            CK(cudaMemcpyAsync(stats, nd.rowStats, sizeof(stats), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (stats[1] > 0) adaptRowsPerWarp(n, stats);
+        }
+        // old solids keep their normals (the scene carried them), new ones zero
+        if (ns) {
+            std::vector<float4> nr(ns);
+            for (size_t i = 0; i < ns; ++i)
+                nr[i] = make_float4((float)snrm[3 * i], (float)snrm[3 * i + 1], (float)snrm[3 * i + 2], 0.f);
+            put(nd.snormal, nr, s);
+        }
+        // Shepard reference sums: every fluid's at the append, then the old ones'
+        if (nf) {
+            launchDensityReinit(nd, 1, s);
+            if (nf0) {
+                std::vector<Allocation> tmp;
+                int* slotOf = dalloc<int>(nf, tmp, s, false);
+                ++t_kernelLaunches, kSlotOfId<<<blocksFor((long long)nf, 256), 256, 0, s>>>(nd, slotOf);
+                CK(cudaStreamSynchronize(e->stream));
+                ++t_kernelLaunches, kCarrySumW0<<<blocksFor((long long)nf0, 256), 256, 0, s>>>(d, nd, slotOf);
+                CK(cudaStreamSynchronize(s));
+                for (const auto& a : tmp) cudaFreeAsync(a.p, s);
+            }
+        }
+        CK(cudaStreamSynchronize(s));
+        CK(cudaGetLastError());
+        n->initialized = true;
+        n->profiling = e->profiling;
+        n->runStats = e->runStats;
+        n->launched = e->launched;
+        n->capturedLaunches = e->capturedLaunches;
+        n->replayedKernels = e->replayedKernels;
+    } catch (int code) {
+        const std::string msg = n->err;
+        demsph_destroy(n);
+        return fail(e, code, "append: " + msg);
+    } catch (const CudaError& ce) {
+        const std::string msg = std::string(ce.what) + ": " + cudaGetErrorString(ce.e);
+        demsph_destroy(n);
+        return fail(e, ce.e == cudaErrorMemoryAllocation ? DEMSPH_ERR_OUT_OF_MEMORY : DEMSPH_ERR_CUDA, "append: " + msg);
+    }
+    // the handle now holds the new engine; the old one's memory goes
+    e->swapWith(*n);
+    demsph_destroy(n);
+    return DEMSPH_OK;
+    ENGINE_END(e)
 }
 
 }  // extern "C"

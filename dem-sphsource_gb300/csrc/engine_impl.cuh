@@ -45,6 +45,7 @@ inline T* dalloc(size_t n, std::vector<Allocation>& owned, cudaStream_t s, bool 
 
 struct demsph_engine {
     demsph::DeviceState d{};
+    demsph_options opt{};         // the options the engine was created with
     int device = 0;
     cudaStream_t stream = nullptr;
     std::vector<demsph::Allocation> owned;  // every device buffer of the engine
@@ -117,6 +118,54 @@ struct demsph_engine {
     // scratch for downloads (device, grown on demand)
     double* dscratch = nullptr;
     size_t dscratchN = 0;
+
+    // Exchanges everything two engines hold (device memory, stream, graphs,
+    // state), field by field: demsph_append hands the caller's handle the
+    // engine it made.  Every field must be listed here.
+    void swapWith(demsph_engine& o)
+    {
+        using std::swap;
+        swap(d, o.d);
+        swap(opt, o.opt);
+        swap(device, o.device);
+        swap(stream, o.stream);
+        swap(owned, o.owned);
+        swap(err, o.err);
+        swap(par, o.par);
+        swap(forceWalk, o.forceWalk);
+        swap(adaptRows, o.adaptRows);
+        swap(solidSortStale, o.solidSortStale);
+        swap(moveKind, o.moveKind);
+        swap(moveHost, o.moveHost);
+        swap(dummyIdx, o.dummyIdx);
+        swap(dummyMoving, o.dummyMoving);
+        swap(walkOrder[0], o.walkOrder[0]);
+        swap(walkOrder[1], o.walkOrder[1]);
+        swap(initialized, o.initialized);
+        swap(debug, o.debug);
+        swap(hmax, o.hmax);
+        swap(nMassive, o.nMassive);
+        swap(fuseIntegration, o.fuseIntegration);
+        swap(mergeContacts, o.mergeContacts);
+        swap(resumeOpened, o.resumeOpened);
+        swap(keysAdvanced, o.keysAdvanced);
+        swap(runStats, o.runStats);
+        swap(graphs, o.graphs);
+        swap(rounds, o.rounds);
+        swap(graphGap, o.graphGap);
+        swap(graphDt, o.graphDt);
+        swap(hzF, o.hzF);
+        swap(lnF, o.lnF);
+        swap(bdF, o.bdF);
+        swap(dampF, o.dampF);
+        swap(launched, o.launched);
+        swap(capturedLaunches, o.capturedLaunches);
+        swap(replayedKernels, o.replayedKernels);
+        swap(profiling, o.profiling);
+        swap(timed, o.timed);
+        swap(dscratch, o.dscratch);
+        swap(dscratchN, o.dscratchN);
+    }
 
     ~demsph_engine()
     {

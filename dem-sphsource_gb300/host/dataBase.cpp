@@ -123,30 +123,75 @@ void dataBase::setClumpVelocity(int index, double3 velocity)
     }
 }
 
-// ---- particles and walls (core/dataBase.cpp:3-177).  Before the start only. ----
+// ---- particles and walls (core/dataBase.cpp:3-177) ----
+// Fluids and solids added after the start go to the running engine
+// (demsph_append: addFluidData / addSolidData with iStep > 0,
+// core/dataBase.cpp:226-268); walls and clumps only before the start.
 #define REFUSE_WHILE_RUNNING(what)                                                                   \
     if (running()) {                                                                                 \
         std::cout << "Error: " what " cannot be added after the simulation starts." << std::endl;   \
         return;                                                                                      \
     }
+#define APPEND_WHILE_RUNNING(call)                                          \
+    const int nf0_ = scene.hos.fluids.points.num, ns0_ = scene.hos.solids.points.num; \
+    const int st_ = (call);                                                 \
+    report(st_);                                                            \
+    if (st_ == DEMSPH_OK && running()) appendRunning(nf0_, ns0_);
+
+void dataBase::appendRunning(int nf0, int ns0)
+{
+    demsph_scene v;
+    scene.view(&v);
+    demsph_scene cur = v, add = v;
+    cur.n_fluid = nf0;
+    cur.n_solid = ns0;
+    add.n_fluid = v.n_fluid - nf0;
+    add.n_solid = v.n_solid - ns0;
+    add.n_clump = 0;
+    add.n_wall = 0;
+    if (add.n_fluid == 0 && add.n_solid == 0) return;
+    auto v3 = [](const double* p, int k) { return p ? p + 3 * (size_t)k : p; };
+    auto d1 = [](const double* p, int k) { return p ? p + k : p; };
+    auto i1 = [](const int* p, int k) { return p ? p + k : p; };
+    add.fluid_position = v3(v.fluid_position, nf0);
+    add.fluid_velocity = v3(v.fluid_velocity, nf0);
+    add.fluid_acceleration = v3(v.fluid_acceleration, nf0);
+    add.fluid_smoothing_length = d1(v.fluid_smoothing_length, nf0);
+    add.fluid_rho0 = d1(v.fluid_rho0, nf0);
+    add.fluid_drho = d1(v.fluid_drho, nf0);
+    add.fluid_sound_speed = d1(v.fluid_sound_speed, nf0);
+    add.fluid_nu = d1(v.fluid_nu, nf0);
+    add.solid_position = v3(v.solid_position, ns0);
+    add.solid_velocity = v3(v.solid_velocity, ns0);
+    add.solid_acceleration = v3(v.solid_acceleration, ns0);
+    add.solid_normal = v3(v.solid_normal, ns0);
+    add.solid_torque = v3(v.solid_torque, ns0);
+    add.solid_angular_velocity = v3(v.solid_angular_velocity, ns0);
+    add.solid_effective_radius = d1(v.solid_effective_radius, ns0);
+    add.solid_radius = d1(v.solid_radius, ns0);
+    add.solid_inverse_mass = d1(v.solid_inverse_mass, ns0);
+    add.solid_material = i1(v.solid_material, ns0);
+    add.solid_cluster = i1(v.solid_cluster, ns0);
+    add.solid_clump = i1(v.solid_clump, ns0);
+    add.solid_is_dummy = i1(v.solid_is_dummy, ns0);
+    check(demsph_append(engine, &cur, &add), "add");
+    ++engineEpoch;
+}
 
 void dataBase::addFluid(std::vector<double3> p, double3 velocity, double smoothLength, double density,
                         double soundSpeed, double kinematicViscosity)
 {
-    REFUSE_WHILE_RUNNING("fluid particles")
-    report(scene.addFluid(p, velocity, smoothLength, density, soundSpeed, kinematicViscosity));
+    APPEND_WHILE_RUNNING(scene.addFluid(p, velocity, smoothLength, density, soundSpeed, kinematicViscosity))
 }
 
 void dataBase::addDummyParticleWall(std::vector<double3> p, double spacing)
 {
-    REFUSE_WHILE_RUNNING("wall particles")
-    report(scene.addDummyParticleWall(p, spacing));
+    APPEND_WHILE_RUNNING(scene.addDummyParticleWall(p, spacing))
 }
 
 void dataBase::addSolid(std::vector<double3> p, double3 velocity, double radius, double density, int materialID)
 {
-    REFUSE_WHILE_RUNNING("solid particles")
-    report(scene.addSolid(p, velocity, radius, density, materialID));
+    APPEND_WHILE_RUNNING(scene.addSolid(p, velocity, radius, density, materialID))
 }
 
 void dataBase::addInfiniteWall(double3 p, double3 normal, int materialID)
@@ -164,8 +209,7 @@ void dataBase::addCylinderWall(double3 p, double3 axis, double3 angularVelocity,
 void dataBase::addCluster(std::vector<double3> p, std::vector<double> radius, std::vector<double> density,
                           double3 velocity, int materialID)
 {
-    REFUSE_WHILE_RUNNING("clusters")
-    report(scene.addCluster(p, radius, density, velocity, materialID));
+    APPEND_WHILE_RUNNING(scene.addCluster(p, radius, density, velocity, materialID))
 }
 
 void dataBase::addClump(std::vector<double3> p, std::vector<double> radius, double3 centroidPosition,
@@ -176,6 +220,7 @@ void dataBase::addClump(std::vector<double3> p, std::vector<double> radius, doub
     report(scene.addClump(p, radius, centroidPosition, velocity, angularVelocity, mass, inertiaTensor, materialID));
 }
 #undef REFUSE_WHILE_RUNNING
+#undef APPEND_WHILE_RUNNING
 
 // core/dataBase.cpp:179-195
 void dataBase::addExternalForce(int index, double3 force)
@@ -284,6 +329,7 @@ void dataBase::downloadFluidSolidPairs()
 // core/solverBase.cpp:13-44) ----
 void dataBase::buildEngine()
 {
+    ++engineEpoch;
     releaseEngine();
     demsph_scene v;
     scene.view(&v);

@@ -84,6 +84,7 @@ private:
     simulationParameter simPara;
     int deviceIndex{0};
     bool keepPairForces{false};   // per-pair coupling forces kept for fluid2Solid output
+    int engineEpoch{0};           // counts engine changes (builds and run-time additions)
 
     // Prints the builder's message when a set-up call was refused.
     void report(int status);
@@ -96,6 +97,9 @@ private:
     void downloadSolids();
     void downloadFluids();
     void downloadFluidSolidPairs();
+    // The particles the host arrays gained beyond (nf0, ns0) go to the running
+    // engine (addFluidData / addSolidData after the start).
+    void appendRunning(int nf0, int ns0);
 
     friend class solverBase;
 };

@@ -167,7 +167,9 @@ void solverBase::frame()
 bool solverBase::binaryFrame(int kind)
 {
     if (!binaryOutput || !engine) return false;
+    if (frames && framesEpoch != engineEpoch) closeFrames();  // particles were added: new counts
     if (!frames) {
+        framesEpoch = engineEpoch;
         demsph_scene v;
         scene.view(&v);
         check(demsph_frame_writer_open(engine, &v, dir.c_str(), &frames), "frame files");

@@ -50,6 +50,7 @@ private:
     bool wantsPairForces{false};   // outputFluid2SolidVTU was called at frame 0
     bool binaryOutput{false};      // frames through the binary writer
     demsph_frame_writer* frames{nullptr};
+    int framesEpoch{-1};           // the engine the writer was opened for
 
     bool binaryFrame(int kind);    // true: the frame went to the binary writer
     void closeFrames();

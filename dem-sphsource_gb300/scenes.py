@@ -590,6 +590,28 @@ def tiny_coupled(seed=4, gap=3):
     return r
 
 
+def tiny_additions(base=None):
+    """Particles added to tiny_coupled while it runs (dataBase::addFluid,
+    addCluster and addSolid after the start): a 3x3x3 block of fluid over the
+    dry end of the tank, a bonded 2x2x2 cluster on the floor and a single
+    sphere above the clump.  Returns (additions, whole): the additions alone
+    (the base's domain and contact models with the new particles only) and
+    the base with them added in the same order."""
+    base = base or tiny_coupled()
+    dx = base.meta["dx"]
+    blocks = Recipe("blocks")
+    fp = regular_packed_points((0.16, 0.02, 0.05), (0.03, 0.03, 0.03), dx)
+    blocks.addFluid(fp, (0, 0, 0), 1.3 * dx, 1000.0, 20.0, 1.0e-6)
+    sr = 2.0e-3
+    pts = regular_packed_points((0.17, 0.05, 0.0), (4 * sr, 4 * sr, 4 * sr), 2 * sr)
+    blocks.addCluster(pts, np.full(len(pts), sr), np.full(len(pts), 2500.0), (0, 0, 0), 1)
+    blocks.addSolid(np.array([[0.12, 0.06, 0.02]]), (0, 0, 0), sr, 2500.0, 0)
+    setters = [c for c in base.calls if not c[0].startswith("add")]
+    add = Recipe(base.name + "_additions", setters + blocks.calls, dict(base.meta))
+    whole = Recipe(base.name + "_whole", base.calls + blocks.calls, dict(base.meta))
+    return add, whole
+
+
 def tiny_converging(n=4, spacing=2.3e-3, radius=1.0e-3, rate=1200.0, steps=40):
     """An n x n x n lattice of equal spheres with 0.3 mm gaps whose velocities
     point at the lattice centre (v = -rate (x - centre)), no gravity, no walls,

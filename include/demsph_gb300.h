@@ -355,6 +355,25 @@ DEMSPH_API int demsph_frame_writer_flush(demsph_frame_writer* w);
 /* Flushes, stops the thread and frees the writer (also after an error). */
 DEMSPH_API int demsph_frame_writer_close(demsph_frame_writer* w);
 
+/* ---- particles added while the simulation runs ----
+   dataBase::addFluid / addSolid / addCluster / addDummyParticleWall after the
+   start (dataBase::addFluidData / addSolidData with iStep > 0,
+   core/dataBase.cpp:226-268; addCluster's search and bonds, :83-113 and
+   :307-343).  `current` is the scene as it stands - its parameters, its
+   contact tables and its clump and wall data (the dynamic state is taken from
+   the engine); `additions` holds the new fluids and solids (no walls and no
+   clumps: DEMSPH_ERR_ARGUMENT, as the reference refuses walls after the
+   start).  They follow the old particles in index order.  As in the
+   reference: the spatial grid is recomputed, the contact springs carry over,
+   wall springs start from zero, new solids have zero normals, and a new
+   cluster is bonded above the last bonded solid.  Unlike the reference: the
+   lists are searched at once (the reference searches at the next step, or at
+   once for a cluster), and new fluids take their Shepard reference sums at
+   the append (the reference leaves them zero and divides by them at its next
+   re-initialisation).  The handle stays valid; the engine behind it is new
+   (graphs are captured again). */
+DEMSPH_API int demsph_append(demsph_engine* e, const demsph_scene* current, const demsph_scene* additions);
+
 /* ---- artefacts in the reference's index space and order (for parity) ---- */
 DEMSPH_API int demsph_get_counts(demsph_engine* e, demsph_counts* out);
 /* objectHash after buildHashSpans (core/neighborSearch.cu:71-113): per particle

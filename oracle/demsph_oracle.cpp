@@ -313,6 +313,7 @@ struct PairList {
 struct Oracle {
     int fixes = 0;
     Grid grid;
+    double domOrg[3] = {0, 0, 0}, domSize[3] = {0, 0, 0};  // setSpatialGrids' domain (re-gridding on append)
     V3 g;
     Tables tab;
     // fluid
@@ -525,26 +526,33 @@ void neighborSearch(Oracle& o, int iStep, int gap)
 
 // ---- fluid (core/integrate.cu:3-421) ----
 
+// Shepard sum of fluid i over its lists (integrate.cu:3-43).
+double shepardSum(const Oracle& o, int i)
+{
+    const V3 ri = o.fpos[i];
+    const double hi = o.fh[i];
+    const double V0i = std::pow(hi / 1.3, 3);
+    double sumW = wendland(0, hi);
+    for (int k = i ? o.ff.prefix[i - 1] : 0; k < o.ff.prefix[i]; ++k)
+        sumW += wendland(len(ri - o.fpos[o.ff.pointing[k]]), hi);
+    if (o.ff.rev.start[i] != -1)
+        for (int k = o.ff.rev.start[i]; k < o.ff.rev.end[i]; ++k)
+            sumW += wendland(len(ri - o.fpos[o.ff.pointed[o.ff.rev.index[k]]]), hi);
+    for (int k = i ? o.fs.prefix[i - 1] : 0; k < o.fs.prefix[i]; ++k) {
+        const int a = o.fs.pointing[k];
+        const double V0a = std::pow(2. * o.srad[a], 3);
+        sumW += wendland(len(ri - o.spos[a]), hi) * V0a / V0i;
+    }
+    return sumW;
+}
+
 // Shepard density re-initialisation (integrate.cu:3-53).
 void densityReinit(Oracle& o, int iStep)
 {
 #pragma omp parallel for
     for (int i = 0; i < o.nf; ++i) {
-        const V3 ri = o.fpos[i];
-        const double hi = o.fh[i];
-        const double V0i = std::pow(hi / 1.3, 3);
-        double sumW = wendland(0, hi);
+        const double sumW = shepardSum(o, i);
         const double rhoStar = o.rho0[i] + o.drho[i];
-        for (int k = i ? o.ff.prefix[i - 1] : 0; k < o.ff.prefix[i]; ++k)
-            sumW += wendland(len(ri - o.fpos[o.ff.pointing[k]]), hi);
-        if (o.ff.rev.start[i] != -1)
-            for (int k = o.ff.rev.start[i]; k < o.ff.rev.end[i]; ++k)
-                sumW += wendland(len(ri - o.fpos[o.ff.pointed[o.ff.rev.index[k]]]), hi);
-        for (int k = i ? o.fs.prefix[i - 1] : 0; k < o.fs.prefix[i]; ++k) {
-            const int a = o.fs.pointing[k];
-            const double V0a = std::pow(2. * o.srad[a], 3);
-            sumW += wendland(len(ri - o.spos[a]), hi) * V0a / V0i;
-        }
         if (iStep == 1) {
             o.sumW0[i] = sumW;
         } else {
@@ -960,10 +968,14 @@ void afterContact(Oracle& o, double dt)  // solidIntegrateAfterContact (integrat
 
 // addBondData at initialisation (core/dataBase.cpp:270-308): bonds for
 // touching same-cluster pairs of the solid list whose bond modulus is set.
-void addBonds(Oracle& o)
+// Bonds between touching spheres of one cluster (addBondData,
+// core/dataBase.cpp:270-346); after the start only pairs whose first solid is
+// above `above` (the last bonded one) are considered.
+void addBonds(Oracle& o, int above = -1)
 {
     for (int k = 0; k < o.ss.num(); ++k) {
         const int i = o.ss.pointed[k], j = o.ss.pointing[k];
+        if (i <= above) continue;
         const V3 pi = o.spos[i], pj = o.spos[j];
         const double ri = o.srad[i], rj = o.srad[j];
         if (ri + rj + 1.e-10 <= len(pi - pj)) continue;
@@ -1131,6 +1143,10 @@ void* oracle_create(const demsph_scene* s, int fixes)
     o->tab.hz.assign(s->hertzian, s->hertzian + 8 * nslot);
     o->tab.ln.assign(s->linear, s->linear + 11 * nslot);
     o->tab.bd.assign(s->bonded, s->bonded + 6 * nslot);
+    for (int a = 0; a < 3; ++a) {
+        o->domOrg[a] = s->domain_origin[a];
+        o->domSize[a] = s->domain_size[a];
+    }
     setGrid(*o, *s);
     return o;
 }
@@ -1144,6 +1160,67 @@ void oracle_initialize(void* h)
     neighborSearch(o, 0, 1);
     addBonds(o);
     setNormals(o);
+}
+
+// Particles added after the start (dataBase::addFluidData / addSolidData
+// with iStep > 0, core/dataBase.cpp:226-268, and addCluster's search and
+// bonds, :83-113, :307-343), as the engine's demsph_append does it: the new
+// particles follow the old ones in index order with their given state; the
+// grid is recomputed; wall springs start from zero (the reference rebuilds
+// solid2InfiniteWall); new solids have zero normals; the lists are searched
+// at once (the contact springs remapped from the last list); a new cluster is
+// bonded above the last bonded solid; new fluids take their Shepard reference
+// sums now.  Walls and clumps cannot be added: returns 1 and leaves the state.
+int oracle_append(void* h, const demsph_scene* a)
+{
+    Oracle& o = *static_cast<Oracle*>(h);
+    if (!a || a->n_clump != 0 || a->n_wall != 0 || (a->n_fluid <= 0 && a->n_solid <= 0)) return 1;
+    for (int i = 0; i < a->n_solid; ++i)
+        if (a->solid_material[i] < 0 || a->solid_material[i] >= o.tab.nMat) return 1;
+    const int nf0 = o.nf;
+    for (int i = 0; i < a->n_fluid; ++i) {
+        o.fpos.push_back(at3(a->fluid_position, i));
+        o.fvel.push_back(at3(a->fluid_velocity, i));
+        o.facc.push_back(at3(a->fluid_acceleration, i));
+        o.fh.push_back(a->fluid_smoothing_length[i]);
+        o.rho0.push_back(a->fluid_rho0[i]);
+        o.drho.push_back(a->fluid_drho ? a->fluid_drho[i] : 0.);
+        o.cs.push_back(a->fluid_sound_speed[i]);
+        o.nu.push_back(a->fluid_nu[i]);
+        o.sumW0.push_back(0.);
+    }
+    o.nf += a->n_fluid;
+    bool cluster = false;
+    for (int i = 0; i < a->n_solid; ++i) {
+        o.spos.push_back(at3(a->solid_position, i));
+        o.svel.push_back(at3(a->solid_velocity, i));
+        o.sacc.push_back(at3(a->solid_acceleration, i));
+        o.snorm.push_back(mk(0, 0, 0));
+        o.storq.push_back(at3(a->solid_torque, i));
+        o.sw.push_back(at3(a->solid_angular_velocity, i));
+        o.seff.push_back(a->solid_effective_radius[i]);
+        o.srad.push_back(a->solid_radius[i]);
+        o.sinvm.push_back(a->solid_inverse_mass[i]);
+        o.smat.push_back(a->solid_material[i]);
+        o.sclu.push_back(a->solid_cluster ? a->solid_cluster[i] : -1);
+        o.sclump.push_back(-1);
+        o.sdum.push_back(a->solid_is_dummy ? a->solid_is_dummy[i] : 0);
+        cluster |= o.sclu.back() >= 0;
+    }
+    o.ns += a->n_solid;
+    o.wslide.assign((size_t)o.ns * o.nw, mk(0, 0, 0));
+    o.wroll = o.wslide;
+    o.wtors = o.wslide;
+    demsph_scene dom{};
+    for (int k = 0; k < 3; ++k) {
+        dom.domain_origin[k] = o.domOrg[k];
+        dom.domain_size[k] = o.domSize[k];
+    }
+    setGrid(o, dom);
+    neighborSearch(o, 0, 1);
+    if (cluster) addBonds(o, o.bA.empty() ? -1 : o.bA.back());
+    for (int i = nf0; i < o.nf; ++i) o.sumW0[i] = shepardSum(o, i);
+    return 0;
 }
 
 void oracle_neighbor_search(void* h, int iStep, int gap) { neighborSearch(*static_cast<Oracle*>(h), iStep, gap); }

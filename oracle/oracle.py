@@ -45,6 +45,8 @@ def load():
         for n in ("oracle_destroy", "oracle_initialize"):
             getattr(lib, n).argtypes = [_P]
         lib.oracle_neighbor_search.argtypes = [_P, _I, _I]
+        lib.oracle_append.argtypes = [_P, _P]
+        lib.oracle_append.restype = _I
         lib.oracle_solid_integrate_before_contact.argtypes = [_P, _D]
         lib.oracle_fluid_integrate.argtypes = [_P, _D, _I, _I]
         lib.oracle_solid_contact_after_fluid_integrate.argtypes = [_P, _D]
@@ -85,6 +87,12 @@ class OracleSolver:
 
     def neighbor_search(self, i_step, gap):
         self.lib.oracle_neighbor_search(self.h, i_step, gap)
+
+    def append(self, additions):
+        """Particles of the scene `additions` added after the start (oracle_append)."""
+        if self.lib.oracle_append(self.h, C.cast(C.byref(additions), _P)) != 0:
+            raise ValueError("oracle_append: walls and clumps cannot be added after the start")
+        self._keep = getattr(self, "_keep", []) + [additions]
 
     def solid_integrate_before_contact(self, dt):
         self.lib.oracle_solid_integrate_before_contact(self.h, dt)

@@ -2,19 +2,24 @@
 // the reference is (driver/cases/damBreak.cpp): a water column, three layers
 // of dummy wall particles, a floor wall and a clump of spheres in the flow.
 //
-//   tinyDamBreak <output-name> [staged]
+//   tinyDamBreak <output-name> [staged] [binary] [append]
 //
 // With "staged" the driver overrides handleDataAfterCalculateContact(), which
 // makes solverBase call the five step functions one by one; without it the
 // steps between two frames run as one batched call.  Both must write the
-// same frames.
+// same frames.  "binary" writes the frames as binary VTU from the background
+// writer; "append" adds a block of fluid and a bonded cluster at frame 2
+// (dataBase::addFluid / addCluster while the simulation runs).
 #include <cstring>
 
 #include "solverBase.h"
 
 class tinyDamBreak : public solverBase {
 public:
-    explicit tinyDamBreak(const char* name, bool staged) : name_(name), staged_(staged) {}
+    tinyDamBreak(const char* name, bool staged, bool binary, bool append)
+        : name_(name), staged_(staged), binary_(binary), append_(append)
+    {
+    }
 
     double particle_spacing = 0.02;
     double particle_radius = 0.5 * particle_spacing;
@@ -23,6 +28,7 @@ public:
     void conditionInitialize() override
     {
         setProblemName(name_);
+        setBinaryOutput(binary_);
         const double s = particle_spacing;
         setDomain(make_double3(-3. * s, -3. * s, -3. * s), make_double3(0.4 + 6. * s, 0.12 + 6. * s, 0.2 + 6. * s));
         std::vector<double3> fp = getRegularPackedPoints(make_double3(0, 0, 0), make_double3(0.12, 0.12, 0.1), s);
@@ -66,16 +72,32 @@ public:
     {
         outputFluidVTU();
         outputSolidVTU();
+        if (append_ && ++frames_ == 3) {  // at frame 2: particles added while the simulation runs
+            const double s = particle_spacing;
+            addFluid(getRegularPackedPoints(make_double3(0.3, 0.02, 0.1), make_double3(0.06, 0.06, 0.06), s),
+                     make_double3(0, 0, 0), 1.3 * s, 1000., 20., 1.e-6);
+            std::vector<double3> cp = getRegularPackedPoints(make_double3(0.15, 0.04, 0.0),
+                                                             make_double3(0.04, 0.04, 0.04), 2 * particle_radius);
+            addCluster(cp, std::vector<double>(cp.size(), particle_radius), std::vector<double>(cp.size(), 800.),
+                       make_double3(0, 0, 0), 1);
+        }
     }
 
 private:
     const char* name_;
-    bool staged_;
+    bool staged_, binary_, append_;
+    int frames_ = 0;
 };
 
 int main(int argc, char** argv)
 {
-    tinyDamBreak problem(argc > 1 ? argv[1] : "tinyDamBreak", argc > 2 && std::strcmp(argv[2], "staged") == 0);
+    bool staged = false, binary = false, append = false;
+    for (int k = 2; k < argc; ++k) {
+        staged |= std::strcmp(argv[k], "staged") == 0;
+        binary |= std::strcmp(argv[k], "binary") == 0;
+        append |= std::strcmp(argv[k], "append") == 0;
+    }
+    tinyDamBreak problem(argc > 1 ? argv[1] : "tinyDamBreak", staged, binary, append);
     problem.solve();
     return 0;
 }

@@ -111,3 +111,53 @@ def test_driver_frames_batched_equal_staged(ds, tmp_path):
     assert np.all(np.isfinite(last["Points"]))
     # the column has started to fall: its mean height has gone down
     assert last["Points"][2::3].mean() < first["Points"][2::3].mean()
+
+
+@pytest.mark.gpu
+def test_driver_binary_frames_equal_the_ascii_ones(ds, tmp_path):
+    """setBinaryOutput(true): the frames are written as binary VTU by the
+    background writer; read back, every array equals the ASCII frame's
+    (which prints the FP64 value with ten decimals into a Float32 array)."""
+    from vtu import read_vtu as read_any
+    exe = str(tmp_path / "tinyDamBreak")
+    compile_driver(DRIVER, exe, ds)
+    for mode in ("ascii", "bin"):
+        r = subprocess.run([exe, mode] + (["binary"] if mode == "bin" else []), cwd=tmp_path, capture_output=True,
+                           text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+    for kind in ("fluid", "solid"):
+        for i in range(5):
+            a = read_any(tmp_path / "asciiOutput" / f"{kind}_{i:04d}.vtu")
+            b = read_any(tmp_path / "binOutput" / f"{kind}_{i:04d}.vtu")
+            assert 'format="appended"' in b["_header"]
+            assert a["STEP"] == b["STEP"]
+            for k, v in a.items():
+                if k.startswith("_") or k in ("TIME", "STEP"):
+                    continue
+                assert v.shape == b[k].shape, (kind, i, k)
+                if v.dtype.kind == "f":
+                    # the decimal text rounds once more than the binary value
+                    np.testing.assert_allclose(b[k], v, rtol=2e-7, atol=1e-9, err_msg=f"{kind} {i} {k}")
+                else:
+                    assert np.array_equal(b[k], v), (kind, i, k)
+
+
+@pytest.mark.gpu
+def test_driver_adds_particles_while_running(ds, tmp_path):
+    """addFluid and addCluster at frame 2 of a running driver: the later frames
+    hold the new particles (the frame writer follows the larger engine), and
+    the run stays finite."""
+    from vtu import read_vtu as read_any
+    exe = str(tmp_path / "tinyDamBreak")
+    compile_driver(DRIVER, exe, ds)
+    for mode in ("add", "addbin"):
+        r = subprocess.run([exe, mode, "append"] + (["binary"] if mode == "addbin" else []), cwd=tmp_path,
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        out = tmp_path / f"{mode}Output"
+        n = [read_any(out / f"fluid_{i:04d}.vtu")["Points"].shape[0] for i in range(5)]
+        m = [read_any(out / f"solid_{i:04d}.vtu")["Points"].shape[0] for i in range(5)]
+        assert n[0] == n[1] == n[2] < n[3] == n[4] and n[3] - n[2] == 27
+        assert m[0] == m[1] == m[2] < m[3] == m[4] and m[3] - m[2] == 8
+        last = read_any(out / "fluid_0004.vtu")
+        assert np.isfinite(last["Points"]).all() and np.isfinite(last["velocity"]).all()
