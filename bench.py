@@ -358,14 +358,17 @@ def fp32_peak_tflops(torch):
         torch.backends.cuda.matmul.allow_tf32 = prev
 
 
-def load_traffic(stage):
-    """Measured DRAM bytes per unit for a stage, from the committed ncu summary."""
+def load_traffic(stage, workload):
+    """Measured DRAM bytes per unit for a stage on a workload, from the
+    committed ncu summary; another workload's figure for the stage when this
+    one was not captured (its source says which)."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(p) as f:
-            return json.load(f).get(stage)
+            by = json.load(f).get(stage) or {}
     except (OSError, ValueError):
         return None
+    return by.get(workload) or next(iter(by.values()), None)
 
 
 # ---- CPU baseline: the FP64 oracle ------------------------------------------------------------
@@ -856,13 +859,14 @@ def main():
         avg_ms = tot_ms / max(n_launch, 1)
         alg = stage_bytes(name, counts)
         achieved = alg / (avg_ms / 1000.0) / 1e9 if alg else None
-        tr = load_traffic(name)
+        tr = load_traffic(name, cfg["workload"])
         traffic = None
         if tr and tr.get("bytes_per_unit") is not None:
             traffic = tr["bytes_per_unit"] * counts.get(tr.get("unit_count", "solid_pairs"), 0)
         total_ms = sum(v[1] for v in stages.values())
         roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                    "traffic_source": tr.get("source") if tr else None,
                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                     "fallback 6.8 TB/s", "avg_launch_ms": avg_ms, "algorithmic_bytes_per_launch": alg,
                     "stage_share": {k: round(v[1] / total_ms, 4) for k, v in sorted(stages.items(),
