@@ -266,7 +266,10 @@ struct StageTimer {
 // pass): the search reads their end-of-step offsets from sphE/splE.
 // detect false: the contact list is left to the contact stage's one launch
 // (launchContactForces).
-void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = false, bool detect = true)
+// beforeDetect: enqueued after the sorts and lists, before the contact
+// detection (a fork to the side stream).
+void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = false, bool detect = true,
+                         const std::function<void()>* beforeDetect = nullptr)
 {
     e->keysAdvanced = false;  // this search's keys are the current ones until an integration rehashes
     const int npar = e->par ^ 1;  // the parity of the list this step builds
@@ -325,6 +328,7 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = fa
     }
     e->par = npar;
     e->walkOrder[e->par] = e->forceWalk;
+    if (beforeDetect) (*beforeDetect)();
     if (!detect) return;
     TIMED("solid_contact_list");  // with the candidate rebuild when they are stale
     launchContactDetect(d, e->par, e->forceWalk, s);
@@ -436,15 +440,33 @@ void fusedSteps(demsph_engine* e, double dt, int iStep, int length, int gap)
         CK(cudaMemcpyAsync(d.splE, d.spl, sizeof(float4) * d.ns, cudaMemcpyDeviceToDevice, e->stream));
     }
     stageBefore(e, dt);
+    // the coupling force of an opened step reads the fluids and the solids as
+    // the fused pass leaves them, and nothing the search writes: it runs on
+    // the side stream beside the contact detection (and the coupling force
+    // of a plain DEM step is all its fluid stage does)
+    const bool branch = !merge && !e->profiling && e->nMassive > 0 && d.nf > 0 && d.ns > 0 && d.nrow > 0;
+    const std::function<void()> fork = [&] {
+        CK(cudaEventRecord(e->forkEv, e->stream));
+        CK(cudaStreamWaitEvent(e->side, e->forkEv, 0));
+        launchCoupling(d, 0, e->side);
+        if (d.fsPairForce) launchCouplingPairForces(d, 0, d.fsPairForce, e->side);
+        CK(cudaEventRecord(e->joinEv, e->side));
+    };
+    bool forked = false;
     for (int k = 0; k < length; ++k) {
-        stageFluid(e, dt, iStep + k, gap);
+        if (forked)
+            CK(cudaStreamWaitEvent(e->stream, e->joinEv, 0));
+        else
+            stageFluid(e, dt, iStep + k, gap);
+        forked = false;
         if (k > 0 && merge)
             launchContactForces(d, e->par, (float)dt, e->stream);
         else
             stageContact(e, dt, false);
         if (k == length - 1) break;
         launchSolidIntegrate(d, dt, INTEGRATE_FUSED, e->par, d.nc > 0, true, e->stream);
-        stageNeighborSearch(e, iStep + k + 1, gap, true, !merge);
+        stageNeighborSearch(e, iStep + k + 1, gap, true, !merge, branch ? &fork : nullptr);
+        forked = branch;
     }
     stageAfter(e, dt, d.nc > 0, true);
 }
@@ -643,6 +665,9 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
         CK(cudaSetDevice(o.device));
         keepPoolMemory(o.device);
         CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&e->forkEv, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&e->joinEv, cudaEventDisableTiming));
         DeviceState& d = e->d;
         d.fixes = o.fixes;
         d.nf = sc->n_fluid;

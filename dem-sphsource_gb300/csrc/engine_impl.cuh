@@ -48,6 +48,11 @@ struct demsph_engine {
     demsph_options opt{};         // the options the engine was created with
     int device = 0;
     cudaStream_t stream = nullptr;
+    // a second stream and two events: inside runs of plain DEM steps the
+    // coupling force of a step runs beside its contact detection (a branch of
+    // the captured graph, joined before the contact forces)
+    cudaStream_t side = nullptr;
+    cudaEvent_t forkEv = nullptr, joinEv = nullptr;
     std::vector<demsph::Allocation> owned;  // every device buffer of the engine
     std::string err;
     int par = 1;                  // parity of the last successful solid list build
@@ -129,6 +134,9 @@ struct demsph_engine {
         swap(opt, o.opt);
         swap(device, o.device);
         swap(stream, o.stream);
+        swap(side, o.side);
+        swap(forkEv, o.forkEv);
+        swap(joinEv, o.joinEv);
         swap(owned, o.owned);
         swap(err, o.err);
         swap(par, o.par);
@@ -176,6 +184,12 @@ struct demsph_engine {
         for (const auto& g : graphs) cudaGraphExecDestroy(g.exec);
         for (const auto& r : rounds) cudaGraphDestroy(r.graph);
         for (const auto& a : owned) cudaFreeAsync(a.p, stream);
+        if (side) {
+            cudaStreamSynchronize(side);
+            cudaStreamDestroy(side);
+        }
+        if (forkEv) cudaEventDestroy(forkEv);
+        if (joinEv) cudaEventDestroy(joinEv);
         if (stream) {
             cudaStreamSynchronize(stream);
             cudaStreamDestroy(stream);
