@@ -375,13 +375,17 @@ void stageFluid(demsph_engine* e, double dt, int iStep, int gap, bool countStep 
 // withClumpForce: the clumps' pebble forces are summed here (the staged
 // calls: the driver's hook runs between contact and integration); a whole
 // step (fullStep) sums them inside the integration that follows instead.
-void stageContact(demsph_engine* e, double dt, bool withClumpForce = true)
+// beforeForces: enqueued between the bonds and the contact forces (the join
+// of a side-stream branch whose result only the contact forces read).
+void stageContact(demsph_engine* e, double dt, bool withClumpForce = true,
+                  const std::function<void()>* beforeForces = nullptr)
 {
     DeviceState& d = e->d;
     if (d.nb > 0) {
         TIMED("bonds");
         launchBonds(d, e->par, (float)dt, e->stream);
     }
+    if (beforeForces) (*beforeForces)();
     {
         TIMED("solid_forces");
         launchSolidForces(d, e->par, (float)dt, e->stream);
@@ -452,17 +456,17 @@ void fusedSteps(demsph_engine* e, double dt, int iStep, int length, int gap)
         if (d.fsPairForce) launchCouplingPairForces(d, 0, d.fsPairForce, e->side);
         CK(cudaEventRecord(e->joinEv, e->side));
     };
+    // the join: the contact forces (which read the coupling force) wait for
+    // the branch; the bonds before them do not
+    const std::function<void()> join = [&] { CK(cudaStreamWaitEvent(e->stream, e->joinEv, 0)); };
     bool forked = false;
     for (int k = 0; k < length; ++k) {
-        if (forked)
-            CK(cudaStreamWaitEvent(e->stream, e->joinEv, 0));
-        else
-            stageFluid(e, dt, iStep + k, gap);
-        forked = false;
+        if (!forked) stageFluid(e, dt, iStep + k, gap);
         if (k > 0 && merge)
             launchContactForces(d, e->par, (float)dt, e->stream);
         else
-            stageContact(e, dt, false);
+            stageContact(e, dt, false, forked ? &join : nullptr);
+        forked = false;
         if (k == length - 1) break;
         launchSolidIntegrate(d, dt, INTEGRATE_FUSED, e->par, d.nc > 0, true, e->stream);
         stageNeighborSearch(e, iStep + k + 1, gap, true, !merge, branch ? &fork : nullptr);
