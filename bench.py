@@ -135,12 +135,19 @@ def workload_config(config, scene, args, settle):
            "step": (f"one fluid period: {gap} solverBase::update() calls, the last of them the fluid step"
                     if gap > 1 else "one solverBase::update() call"),
            "updates_per_step": updates_for(1, gap, gap, nf, n_mobile),
-           "state": (f"the bed after {settle} untimed steps of the settle (contact-dense), springs and all"
-                     if settle else "the workload's initial state, then the warm-up steps"),
            "l2": "inputs larger than L2 (129 MB)" if config in (1, 2) else
                  "the scene's state (about 20 MB) fits in L2 (129 MB): not flushed between steps",
            "parallelism": f"replicas x{args.gpus}"}
     return cfg
+
+
+def workload_state(args, settle):
+    """Where the timed steps start (a sibling of `config` in the line: the
+    reference arm starts from the initial state, the GPU arm can settle first)."""
+    return ((f"the bed after {settle} untimed steps of the settle (contact-dense), springs and all"
+             if settle else "the workload's initial state") +
+            f", then {args.warmup} warm-up, {args.latency_steps} latency and {args.profile_steps} profiled "
+            "bench steps before the timed ones")
 
 
 def scene_state(scene):
@@ -435,7 +442,9 @@ def reference_arm(args, rank):
     orc.update(dt, step, gap, gap)
     t_step = time.perf_counter() - t0
     step += gap
-    warm, timed = max(1, args.warmup), args.steps
+    # untimed bench steps: the GPU arm's warm-up, latency and profiled ones, so
+    # that both arms time the same steps of the run
+    warm, timed = max(1, args.warmup + args.latency_steps + args.profile_steps), args.steps
     fit = int(args.ref_budget / max(t_step, 1e-9)) - 1
     if warm + timed > fit + 1:  # shrink both, keeping their ratio, to fit the budget
         timed = max(1, min(timed, int(fit * args.steps / max(1, args.steps + args.warmup))))
@@ -455,6 +464,8 @@ def reference_arm(args, rank):
         "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": 1,
         "steps": timed, "warmup": warm, "ms_per_step": 1000.0 * el / timed, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic", "config": cfg,
+        "state": f"the workload's initial state, then {warm} untimed bench steps before the timed ones (the GPU "
+                 "arm's warm-up, latency and profiled steps)",
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "particle-updates/s", "cores": threads, "kind": "port",
                          "sample": sample},
@@ -789,6 +800,33 @@ def main():
 
     stream = torch.cuda.ExternalStream(eng.stream_ptr(), device=device)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # ---- latency, then the stage timing, right before the timed region (the
+    # same phase of the run: the clock tail after the timed region advances the
+    # scene by up to a second of steps) ----
+    # latency: bench steps one by one (graph replay), CUDA events on the engine stream
+    lat = []
+    for _ in range(max(1, args.latency_steps)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.update(dt, step, gap, gap, use_graph=True)
+        e1.record(stream)
+        e1.synchronize()
+        lat.append(e0.elapsed_time(e1))
+        step += gap
+    lat.sort()
+
+    # ---- stage timing pass (uncaptured, CUDA events per stage) for the roofline ----
+    eng.set_profiling(True)
+    eng.profile_report()
+    for _ in range(max(1, args.profile_steps)):
+        eng.update(dt, step, gap, gap, use_graph=False)
+        step += gap
+    eng.synchronize()
+    stages = eng.profile_report()
+    eng.set_profiling(False)
+    c = eng.counts()
+    shapes = eng.launch_shapes()
+    eng.synchronize()
     launches0 = eng.kernel_launches()
     if dist:
         dist.barrier()
@@ -818,29 +856,6 @@ def main():
     # the clock-tail steps launched kernels too; only the timed region's count is claimed
     launches_tail = eng.kernel_launches() - launches0 - launches
 
-    # ---- latency: bench steps one by one (graph replay), CUDA events on the engine stream ----
-    lat = []
-    for _ in range(max(1, args.latency_steps)):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        eng.update(dt, step, gap, gap, use_graph=True)
-        e1.record(stream)
-        e1.synchronize()
-        lat.append(e0.elapsed_time(e1))
-        step += gap
-    lat.sort()
-
-    # ---- stage timing pass (uncaptured, CUDA events per stage) for the roofline ----
-    eng.set_profiling(True)
-    eng.profile_report()
-    for _ in range(max(1, args.profile_steps)):
-        eng.update(dt, step, gap, gap, use_graph=False)
-        step += gap
-    eng.synchronize()
-    stages = eng.profile_report()
-    eng.set_profiling(False)
-    c = eng.counts()
-    shapes = eng.launch_shapes()
     counts = {"solid_pairs": c.solid_pairs, "n_solid": scene.n_solid, "n_solid_active": n_mobile,
               "n_fluid": nf, "bonds": c.bonds,
               "fluid_partners": 2.0 * c.fluid_pairs / max(nf, 1), "fluid_solid_partners": c.fluid_solid_pairs / max(nf, 1),
@@ -927,7 +942,7 @@ def main():
             "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-            "data": "synthetic", "config": cfg, "impl": "ours",
+            "data": "synthetic", "config": cfg, "state": workload_state(args, settle), "impl": "ours",
             "p50_step_ms": lat[len(lat) // 2],
             "p99_step_ms": lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)],
             "roofline": roofline, "cpu_baseline": cb, "fp64_error": err64,

@@ -228,31 +228,38 @@ __global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
     stepKernelBegin();
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= d.nb || *d.status) return;
-    if (d.bon[b] == 0) {
+    // Every load the update needs is issued before the bond's checks (a broken
+    // bond, a pair that left the contact list), which end in stores: the
+    // loads then wait for one another only through the pair's indices, not
+    // behind the search of the contact list.
+    const int2 ab = d.bab[b];
+    const int bonded = d.bon[b];
+    const float4 FnTt0 = d.bFnTt[b], FsH0 = d.bFsH[b], FsL0 = d.bFsL[b], TbH0 = d.bTbH[b], TbL0 = d.bTbL[b];
+    const float3 n0 = xyz(d.bN[b]);
+    const int i = ab.x, j = ab.y;
+    const PairGeom g = pairGeometry(d, i, j);
+    const float3 wi = xyz(d.swh[i]), wj = xyz(d.swh[j]);
+    const float3 vc = contactVel(d, i, j, g.leverA, g.leverB);
+    const float3 wr = spinDiff(d, i, j);
+    const float4 ri = d.srad[i], rj = d.srad[j];
+    const int ms = tableSlot(d.tab, d.sflags[i].x, d.sflags[j].x);
+    const long long slot = forwardSlot(d, par, i, j);
+    if (bonded == 0) {
         d.bFnTt[b] = make_float4(0, 0, 0, 0);
         d.bFsH[b] = d.bFsL[b] = d.bTbH[b] = d.bTbL[b] = make_float4(0, 0, 0, 0);
         d.bN[b] = make_float4(0, 0, 0, 0);
         d.bF[b] = d.bTA[b] = d.bTB[b] = make_float4(0, 0, 0, 0);
         return;
     }
-    const int2 ab = d.bab[b];
-    const int i = ab.x, j = ab.y;
-    const long long slot = forwardSlot(d, par, i, j);
     if (slot < 0) {  // the pair left the contact list: the bond breaks
         d.bon[b] = 0;
         d.bF[b] = d.bTA[b] = d.bTB[b] = make_float4(0, 0, 0, 0);
         return;
     }
-    const PairGeom g = pairGeometry(d, i, j);
     const float3 n = g.n;
-    const float3 n0 = xyz(d.bN[b]);
-    const float3 wi = xyz(d.swh[i]), wj = xyz(d.swh[j]);
-    const float3 vc = contactVel(d, i, j, g.leverA, g.leverB);
-    const float4 ri = d.srad[i], rj = d.srad[j];
-    const int ms = tableSlot(d.tab, d.sflags[i].x, d.sflags[j].x);
     const float* B = d.tab.bd + 6 * ms;  // gamma E knks sigma C mu
-    float4 FnTt = d.bFnTt[b];
-    float4 FsH = d.bFsH[b], FsL = d.bFsL[b], TbH = d.bTbH[b], TbL = d.bTbL[b];
+    const float4 FnTt = FnTt0;
+    float4 FsH = FsH0, FsL = FsL0, TbH = TbH0, TbL = TbL0;
     // rotate shear force / bending torque with the normal, then about it
     const float3 th1 = cross3(n0, n);
     rotateDF(FsH, FsL, th1);
@@ -271,7 +278,6 @@ __global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
     const float3 dtg = vc * dt - dn;
     dfl Fn = df_add_f(df_make(FnTt.x, FnTt.y), -dot3(dn * (kn * Ab), n));
     addDF3(FsH, FsL, dtg * (-ks * Ab));
-    const float3 wr = spinDiff(d, i, j);
     const float3 dn2 = n * (dot3(wr, n) * dt);
     const float3 dt2 = wr * dt - dn2;
     dfl Tt = df_add_f(df_make(FnTt.z, FnTt.w), -dot3(dn2 * (ks * Jb), n));
