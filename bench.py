@@ -144,8 +144,12 @@ def workload_config(config, scene, args, settle):
 def workload_state(args, settle):
     """Where the timed steps start (a sibling of `config` in the line: the
     reference arm starts from the initial state, the GPU arm can settle first)."""
-    return ((f"the bed after {settle} untimed steps of the settle (contact-dense), springs and all"
-             if settle else "the workload's initial state") +
+    if getattr(args, "load_state", None):
+        start = f"the state saved in {os.path.basename(args.load_state)} (springs from zero)"
+    else:
+        start = (f"the bed after {settle} untimed steps of the settle (contact-dense), springs and all"
+                 if settle else "the workload's initial state")
+    return (start +
             f", then {args.warmup} warm-up, {args.latency_steps} latency and {args.profile_steps} profiled "
             "bench steps before the timed ones")
 
@@ -750,6 +754,9 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline stepping")
     ap.add_argument("--ref-budget", type=float, default=300.0, help="reference arm: seconds of stepping at most")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--save-state", default=None, help="config 1: writes the settled bed (.npz) for --load-state")
+    ap.add_argument("--load-state", default=None,
+                    help="starts from a state written by --save-state instead of settling (for profiling runs)")
     ap.add_argument("--clock-tail", type=float, default=1.0,
                     help="seconds of the same bench steps replayed after the timed region so that the clock sampler "
                          "sees the load (0 for a run under a profiler)")
@@ -782,10 +789,18 @@ def main():
     device = local if world > 1 else 0
     torch.cuda.set_device(device)
 
-    eng = ds.Engine(scene, device=device)
-    eng.initialize()
     step = 1
     state0 = None
+    if args.load_state:
+        # a state saved by --save-state (the settled bed): the engine starts
+        # from it (contact and wall springs from zero, as at any start)
+        z = np.load(args.load_state)
+        state0 = {k: z[k] for k in z.files if k != "step"}
+        step = int(z["step"])
+        restart_scene(scene, state0)
+        settle = 0
+    eng = ds.Engine(scene, device=device)
+    eng.initialize()
     if settle:
         # the settle itself, untimed, up to a contact-dense bed; its state is
         # the start of the CPU baseline and of the FP64 comparison
@@ -793,6 +808,8 @@ def main():
         step += settle
         eng.synchronize()
         state0 = engine_state(eng)
+        if args.save_state:
+            np.savez(args.save_state, step=step, **state0)
     first_sample_step = step
     eng.update(dt, step, args.warmup * gap, gap, use_graph=True)
     step += args.warmup * gap
