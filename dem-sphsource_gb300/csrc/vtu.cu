@@ -453,6 +453,10 @@ int demsph_frame_writer_write(demsph_frame_writer* w, int what, int frame, int s
         if (!w->error.empty()) return fail(e, DEMSPH_ERR_IO, "frame writer: " + w->error);
     }
     DeviceState& d = e->d;
+    // the slots and static arrays are sized for the counts at open
+    // (demsph_append changes them: open a writer for the new counts)
+    if (d.nf != w->nf || d.ns != w->ns)
+        return fail(e, DEMSPH_ERR_STATE, "frame writer: the engine's particle counts changed since it was opened");
     for (int k = 0; k < KINDS; ++k) {
         if (!(what & (1 << k))) continue;
         const int si = w->next[k];

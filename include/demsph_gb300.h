@@ -337,7 +337,8 @@ DEMSPH_API int demsph_add_global_damping(demsph_engine* e, int solid, double c_d
    static arrays (smoothing length, radius, clusterID, clumpID) are taken from
    `scene` (the engine's scene) at open.  fluid2Solid forces are the per-pair
    coupling forces of the last step when the engine keeps them (options.debug
-   bit 0), else zeros.  Close the writer before destroying its engine.  Errors
+   bit 0), else zeros.  Close the writer before destroying its engine; after
+   demsph_append a write returns DEMSPH_ERR_STATE (open a new writer).  Errors
    of the writer thread are returned by the next write, flush or close
    (DEMSPH_ERR_IO, message in demsph_last_error of the engine). */
 typedef struct demsph_frame_writer demsph_frame_writer;

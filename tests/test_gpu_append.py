@@ -57,3 +57,26 @@ def test_append_refuses_walls_and_clumps(ds, scenes):
         eng.append(sc, sc)  # holds a clump and a wall
     assert e.value.status == 1
     eng.update(sc.time_step, 4, 3, sc.fluid_integrate_gap)  # the engine is unchanged and usable
+
+
+def test_frame_writer_refuses_after_an_append(ds, scenes, tmp_path):
+    """A writer sized for the counts at its opening refuses frames once
+    particles were added (its slots would be too small); a new writer works."""
+    _, sc = ds.build_scene(scenes.tiny_coupled())
+    add, whole = _additions(ds, scenes)
+    eng = ds.Engine(sc)
+    eng.initialize()
+    eng.update(sc.time_step, 1, 3, sc.fluid_integrate_gap)
+    fw = ds.FrameWriter(eng, tmp_path / "a")
+    fw.write(ds.FRAME_ALL, 0, 3, 0.0)
+    fw.flush()
+    eng.append(sc, add)
+    eng.scene = whole
+    with pytest.raises(ds.DemSphError) as e:
+        fw.write(ds.FRAME_ALL, 1, 3, 0.0)
+    assert e.value.status == 2
+    fw.close()
+    with ds.FrameWriter(eng, tmp_path / "b") as fw2:
+        fw2.write(ds.FRAME_ALL, 1, 3, 0.0)
+    from vtu import read_vtu
+    assert read_vtu(tmp_path / "b" / "fluid_0001.vtu")["Points"].shape[0] == whole.n_fluid
