@@ -1740,6 +1740,15 @@ int demsph_batch_update(demsph_batch* b, demsph_engine* const* engines, int coun
         const demsph_engine::RoundGraph* r;
         int startPar;
     };
+    {
+        // an engine listed twice would have two rounds in one launch
+        std::vector<demsph_engine*> sorted(engines, engines + count);
+        std::sort(sorted.begin(), sorted.end());
+        if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) {
+            b->err = "batch: an engine is listed twice";
+            return DEMSPH_ERR_ARGUMENT;
+        }
+    }
     std::vector<Member> members;
     auto engineFail = [&](int i, demsph_engine* e, const CudaError& c) { status_out[i] = cudaFail(e, c); };
     for (int i = 0; i < count; ++i) {
@@ -2087,9 +2096,21 @@ int demsph_append(demsph_engine* e, const demsph_scene* cur, const demsph_scene*
                     "append: walls and clumps can only be added before the simulation starts");
     if (add->n_fluid < 0 || add->n_solid < 0 || (add->n_fluid == 0 && add->n_solid == 0))
         return fail(e, DEMSPH_ERR_ARGUMENT, "append: nothing to add");
-    for (int i = 0; i < add->n_solid; ++i)
+    if (add->n_fluid > 0 && (!add->fluid_position || !add->fluid_smoothing_length || !add->fluid_rho0 ||
+                             !add->fluid_sound_speed || !add->fluid_nu))
+        return fail(e, DEMSPH_ERR_ARGUMENT, "append: the added fluids need positions, smoothing lengths, densities, "
+                                            "sound speeds and viscosities");
+    if (add->n_solid > 0 && (!add->solid_position || !add->solid_radius || !add->solid_effective_radius ||
+                             !add->solid_inverse_mass || !add->solid_material))
+        return fail(e, DEMSPH_ERR_ARGUMENT, "append: the added solids need positions, radii, effective radii, "
+                                            "inverse masses and materials");
+    for (int i = 0; i < add->n_solid; ++i) {
         if (add->solid_material[i] < 0 || add->solid_material[i] >= cur->n_material)
             return fail(e, DEMSPH_ERR_ARGUMENT, "append: material index exceeds the number of materials");
+        if (add->solid_clump && add->solid_clump[i] >= 0)
+            return fail(e, DEMSPH_ERR_ARGUMENT,
+                        "append: walls and clumps can only be added before the simulation starts");
+    }
     CK(cudaStreamSynchronize(e->stream));
     const size_t nf0 = d.nf, ns0 = d.ns, nc = d.nc, af = add->n_fluid, as = add->n_solid;
     const size_t nf = nf0 + af, ns = ns0 + as;

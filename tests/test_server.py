@@ -246,6 +246,9 @@ def test_batch_reuses_its_graph_for_repeating_rounds(ds, scenes):
         st = b.update(engines, [2 + 10 * r] * 2, [10, 10], [a.time_step, c.time_step],
                       [a.fluid_integrate_gap, c.fluid_integrate_gap])
         assert st == [0, 0]
+    with pytest.raises(ds.DemSphError) as e:  # an engine twice in one launch
+        b.update([engines[0], engines[0]], [82, 82], [2, 2], [a.time_step] * 2, [a.fluid_integrate_gap] * 2)
+    assert e.value.status == 1
     info = b.info()
     # a list growth in the first rounds drops the member's graphs (a rebuild)
     assert info["launches"] == 8 and info["graph_builds"] <= 3 and info["members"] == 2
