@@ -832,11 +832,12 @@ def main():
         step += gap
     lat.sort()
 
-    # ---- stage timing pass (uncaptured, CUDA events per stage) for the roofline ----
+    # ---- stage timing pass for the roofline: the graphs' own launches (the
+    # fused runs of the timed region) issued directly, CUDA events per stage ----
     eng.set_profiling(True)
     eng.profile_report()
     for _ in range(max(1, args.profile_steps)):
-        eng.update(dt, step, gap, gap, use_graph=False)
+        eng.update(dt, step, gap, gap, use_graph=True)
         step += gap
     eng.synchronize()
     stages = eng.profile_report()

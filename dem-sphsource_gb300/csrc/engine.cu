@@ -462,13 +462,18 @@ void fusedSteps(demsph_engine* e, double dt, int iStep, int length, int gap)
     bool forked = false;
     for (int k = 0; k < length; ++k) {
         if (!forked) stageFluid(e, dt, iStep + k, gap);
-        if (k > 0 && merge)
+        if (k > 0 && merge) {
+            TIMED("solid_forces");  // with the contact list of the step
             launchContactForces(d, e->par, (float)dt, e->stream);
-        else
+        } else {
             stageContact(e, dt, false, forked ? &join : nullptr);
+        }
         forked = false;
         if (k == length - 1) break;
-        launchSolidIntegrate(d, dt, INTEGRATE_FUSED, e->par, d.nc > 0, true, e->stream);
+        {
+            TIMED("integrate_after");  // the closing half of this step and the opening half of the next
+            launchSolidIntegrate(d, dt, INTEGRATE_FUSED, e->par, d.nc > 0, true, e->stream);
+        }
         stageNeighborSearch(e, iStep + k + 1, gap, true, !merge, branch ? &fork : nullptr);
         forked = branch;
     }
@@ -1346,6 +1351,10 @@ static int runUpdate(demsph_engine* e, double dt, int first_step, int n_steps, i
         const int startPar = e->par;
         const bool startOpened = e->resumeOpened;
         const bool graphs = use_graph && !e->profiling;
+        // profiled runs that ask for graphs launch the graphs' bodies directly
+        // (the same fused runs, each stage timed): the stage times are those of
+        // the steps the graphs run
+        const bool eagerFused = use_graph && e->profiling;
         if (graphs && (e->graphDt != dt || e->graphGap != gap)) {
             dropGraph(e);
             e->graphDt = dt;
@@ -1357,7 +1366,7 @@ static int runUpdate(demsph_engine* e, double dt, int first_step, int n_steps, i
         std::vector<std::pair<int, int>> fusedRuns;
         while (s < end) {
             const int kind = stepKind(d, s, gap);
-            if (!graphs || s == 1 || e->resumeOpened) {  // step 1 stores the Shepard reference sums: run it as it is
+            if ((!graphs && !eagerFused) || s == 1 || e->resumeOpened) {  // step 1 stores the Shepard reference sums: run it as it is
                 fullStep(e, dt, s++, gap, e->resumeOpened);
                 e->resumeOpened = false;
                 continue;
@@ -1369,14 +1378,24 @@ static int runUpdate(demsph_engine* e, double dt, int first_step, int n_steps, i
                 while (s + run < end && stepKind(d, s + run, gap) == 0) ++run;
             while (run > 0) {
                 const int len = kind != 0 ? 1 : (run >= 10 ? 10 : (run >= 2 ? 2 : 1));
-                const auto& g = graphFor(e, kind, len, dt, s, gap);
-                CK(cudaGraphLaunch(g.exec, e->stream));
-                e->replayedKernels += g.kernels;
-                if (g.fused) {
+                bool fusedRun;
+                if (eagerFused) {
+                    fusedRun = e->fuseIntegration && kind == 0 && len >= 2;
+                    if (fusedRun)
+                        fusedSteps(e, dt, s, len, gap);
+                    else
+                        for (int k = 0; k < len; ++k) fullStep(e, dt, s + k, gap);  // the steps flip the parity
+                } else {
+                    const auto& g = graphFor(e, kind, len, dt, s, gap);
+                    CK(cudaGraphLaunch(g.exec, e->stream));
+                    e->replayedKernels += g.kernels;
+                    fusedRun = g.fused;
+                    e->par ^= (len & 1);
+                }
+                if (fusedRun) {
                     fusedRuns.emplace_back(s, len);
                     e->runStats.fused_passes += len - 1;
                 }
-                e->par ^= (len & 1);
                 s += len;
                 run -= len;
             }

@@ -330,6 +330,31 @@ def test_fused_integration_equals_separate_passes(ds, scenes, name, skin, monkey
         _same_state_and_lists(engines[0], e)
 
 
+@pytest.mark.parametrize("name", ("dry_granular", "tiny_coupled", "tiny_converging"))
+def test_profiled_update_runs_the_graph_bodies(ds, scenes, name):
+    """With stage timing on, demsph_update issues the launches its graphs
+    hold (fused runs included) one by one, each stage timed: forty steps give
+    the bits and lists of the graph replay, and the fused integration pass has
+    its own timed launches."""
+    recipe = _dry_granular(scenes) if name == "dry_granular" else getattr(scenes, name)()
+    b, sc = ds.build_scene(recipe)
+    opts = dict(solid_contacts_per_particle=1) if name == "tiny_converging" else {}
+    timed, plain = ds.Engine(sc, **opts), ds.Engine(sc, **opts)
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for e in (timed, plain):
+        e.initialize()
+    timed.set_profiling(True)
+    timed.profile_report()
+    timed.update(dt, 1, 40, gap, use_graph=True)
+    stages = timed.profile_report()
+    timed.set_profiling(False)
+    plain.update(dt, 1, 40, gap, use_graph=True)
+    assert timed.run_stats()["fused_passes"] == plain.run_stats()["fused_passes"] > 0
+    assert timed.run_stats()["resumed_steps"] == plain.run_stats()["resumed_steps"]
+    assert stages["integrate_after"][0] >= 40 and stages["solid_forces"][0] >= 40, stages
+    _same_state_and_lists(timed, plain)
+
+
 def test_walk_mode_splits_the_merged_contact_launch(ds, scenes):
     """Two solids start above the domain, so the lists come from the walk:
     the first step a fused pass opens finds the one-launch contact list
