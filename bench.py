@@ -272,9 +272,18 @@ def stage_bytes(stage, c):
     kff = c.get("fluid_partners", 0.0)
     kfs = c.get("fluid_solid_partners", 0.0)
     table = {
-        # per pair, from both sides: partner id 4 + springs in 48 + springs out 48 + F T 32;
-        # per active solid: cell ph pl vh vl wh wl rad flags 144 + counts 8 + acc torque out 32
-        "solid_forces": 132 * P + 184 * Ns,
+        # per pair, once: partner id 4 + springs in 48 + springs out 48 + F T TA TB out 64; per
+        # active solid: cell ph pl vh vl wh wl rad flags 144 + count 4; per bond: 160 (below)
+        "pair_forces": 164 * P + 148 * Ns + 160 * Nb,
+        # per pair, from both sides: F and the torque on the side 32 each; per bond and side:
+        # id 4 + pair 8 + F T 32; per active solid: counts 8 + bond range 8 + flags 16 + mass 16
+        # + coupling force 16 + acc torque out 32
+        "solid_forces": 64 * P + 88 * Nb + 96 * Ns,
+        # the list and the forces of a step opened by a fused pass in one launch, each pair from
+        # both sides: partner ids written 8 + springs in 48 + springs out 48 + F T 32; per active
+        # solid: candidates' count 4 + cell ph pl at the step's end and middle, vh vl wh wl, rad
+        # flags 176 + counts out 8 + acc torque out 32
+        "contact_forces": 136 * P + 220 * Ns,
         # per active solid: cell ph pl rad flags 80 + list and candidate counts 12 + walk
         # centre 8; per pair: partner ids 8 + previous springs 48 in + springs 48 out + history id 8
         "solid_contact_list": 100 * Ns + 112 * P,
@@ -296,7 +305,6 @@ def stage_bytes(stage, c):
         "fluid_hash_reorder": 496 * Nf,
         "coupling_lists": 8 * kfs * Nf,
         "coupling_force": 64 * c.get("coupling_pairs", 0) + 96 * Ns,
-        "bonds": 160 * Nb,
         "clump_force": 64 * c.get("n_pebbles", 0),
     }
     if c.get("tiles"):
@@ -748,9 +756,10 @@ def main():
     ap.add_argument("--round-steps", type=int, default=20, help="batched workload: steps per scene and round")
     ap.add_argument("--e2e-steps", type=int, default=10, help="bench steps of the end-to-end leg")
     ap.add_argument("--latency-steps", type=int, default=20, help="bench steps timed one by one for p50/p99")
-    ap.add_argument("--profile-steps", type=int, default=5,
-                    help="bench steps of the per-stage timing pass (5: one Shepard re-initialisation period, so "
-                         "the stage shares weigh it as the timed region does)")
+    ap.add_argument("--profile-steps", type=int, default=10,
+                    help="bench steps of the per-stage timing pass, in one call (10: two Shepard "
+                         "re-initialisation periods, so the stage shares weigh it as the timed region does, and "
+                         "runs of plain DEM steps split into the timed region's 10-step runs)")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline stepping")
     ap.add_argument("--ref-budget", type=float, default=300.0, help="reference arm: seconds of stepping at most")
     ap.add_argument("--no-cpu", action="store_true")
@@ -836,9 +845,9 @@ def main():
     # fused runs of the timed region) issued directly, CUDA events per stage ----
     eng.set_profiling(True)
     eng.profile_report()
-    for _ in range(max(1, args.profile_steps)):
-        eng.update(dt, step, gap, gap, use_graph=True)
-        step += gap
+    # (one call: the runs of plain DEM steps are split as in the timed region's call)
+    eng.update(dt, step, max(1, args.profile_steps) * gap, gap, use_graph=True)
+    step += max(1, args.profile_steps) * gap
     eng.synchronize()
     stages = eng.profile_report()
     eng.set_profiling(False)

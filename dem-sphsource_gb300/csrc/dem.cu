@@ -223,11 +223,10 @@ __device__ __forceinline__ void addDF3(float4& h, float4& l, float3 dv)
     l = make_float4(x.lo, y.lo, z.lo, l.w);
 }
 
-__global__ void __launch_bounds__(T) kBonds(DeviceState d, int par, float dt)
+// One parallel bond's update (integrate.cu:717-804): its state, force and
+// torques on both solids.
+__device__ __forceinline__ void bondUpdate(const DeviceState& d, int par, float dt, int b)
 {
-    stepKernelBegin();
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= d.nb || *d.status) return;
     // Every load the update needs is issued before the bond's checks (a broken
     // bond, a pair that left the contact list), which end in stores: the
     // loads then wait for one another only through the pair's indices, not
@@ -403,46 +402,33 @@ __device__ __forceinline__ void solidRowTail(const DeviceState& d, int par, int 
     d.storque[a] = f4(tq);
 }
 
-// Force and torque on every solid that can touch others (calSolidForceTorque,
-// core/integrate.cu:806-858, with the contact forces of :423-512, the bonds of
-// :717-804 and the walls of :514-610), one thread per row: each contact is
-// evaluated by both of its solids (pairForce, the same bits on both sides) -
-// the forward side also advances the springs - so no per-pair forces are
-// gathered.  Sums are Kahan-compensated, in index order.
+// The contact forces of a step (calSolidContactForceTorque,
+// core/integrate.cu:423-512), each contact evaluated once, by the row of its
+// lower solid A (forward slot k): the springs advance, the slot keeps the
+// force on A, the contact torque as the reference stores it and the torque on
+// A with its lever arm, and the pair's slot in B's reverse list (found by
+// its id, while the force is evaluated) gets minus the force and minus the
+// torque on B with its lever arm.  The bonds (blocks from contactBlocks on)
+// are updated in the same launch: kSolidForces reads both.
 //
-// Rows hold few contacts and their counts vary: a warp runs its rows'
-// (row, contact) items through warpItems, one lane per item, and each row's
-// lane adds its results in contact order.
-//
-// MERGED (kContactDetect's work in the same launch, for plain DEM steps
-// opened by a fused integration pass; 32 rows per warp): each lane first
-// builds its row's list from the candidates (rebuilt when stale) on the
-// end-of-step offsets sphE/splE, exactly as kContactDetect does; both solids
-// of a pair then take its springs from the previous list (springOut of the
-// other parity) - the same values kContactDetect's remap would hand them.
-// The candidates and the contact test are symmetric in the two solids, so
-// the forward row of every reverse pair holds it.  In the walk mode they need
-// not be: the launch then raises ST_SPLIT_CONTACTS before writing anything,
-// and the step is redone with the two launches.
-template <bool MERGED>
-__global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, float dt, int withCoupling,
-                                                     int rowsPerWarp)
+// Rows hold few contacts and their counts vary: a warp shares its rows'
+// forward contacts out through warpItems, one lane per contact.
+__global__ void __launch_bounds__(T, 6) kPairForces(DeviceState d, int par, float dt, int rowsPerWarp,
+                                                    int contactBlocks)
 {
     stepKernelBegin();
-    __shared__ float4 itemF[T], itemT[T];  // 32 items per warp
     if (*d.status) return;
-    if (MERGED && *d.slowMode) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(d.status, ST_SPLIT_CONTACTS);
+    if ((int)blockIdx.x >= contactBlocks) {
+        const int b = ((int)blockIdx.x - contactBlocks) * blockDim.x + threadIdx.x;
+        if (b < d.nb) bondUpdate(d, par, dt, b);
         return;
     }
-    const int prev = par ^ 1;
     // this step's flag has been read by every row's contact detection (the
-    // launch before, or this launch's rows - then it is cleared by the next
-    // step's launch); the step before's flag is free for this step's closing
+    // launch before); the step before's flag is free for this step's closing
     // drift to raise
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (!MERGED) *(volatile int*)&d.rebuild[par] = 0;
-        *(volatile int*)&d.rebuild[prev] = 0;
+        *(volatile int*)&d.rebuild[par] = 0;
+        *(volatile int*)&d.rebuild[par ^ 1] = 0;
     }
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -452,44 +438,69 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
     const bool live = lane < rowsPerWarp && row < d.nrow;
     const int a = live ? solidOf(d, row) : 0;
     const size_t nr = (size_t)d.nrow;
-    // forward contacts (a, b) come first, then reverse ones (b, a)
-    int n = 0, contacts = 0;
-    if (MERGED) {
-        if (live) {
-            DeviceState atEnd = d;  // the end-of-step offsets
-            atEnd.sph = d.sphE;
-            atEnd.spl = d.splE;
-            if (d.rebuild[par]) verletBuildRow(atEnd, row);
-            const int C = d.scap;
-            int nf = 0, nb = 0;
-            const int nc = min(d.vcnt[row], d.vcap);
-            for (int k = 0; k < nc; ++k) {
-                const int b = d.vcand[(size_t)k * nr + row];
-                if (!solidsTouch(atEnd, a, b)) continue;
-                if (b > a) {
-                    if (nf < C) d.fwd[par][(size_t)nf * nr + row] = b;
-                    ++nf;
-                } else {
-                    if (nb < C) d.rev[(size_t)nb * nr + row] = b;
-                    ++nb;
+    const int n = live ? min(d.fcnt[par][row], d.scap) : 0;
+    warpItems(n, [&](int owner, int q, bool valid) {
+        const int A = __shfl_sync(FULL, a, owner);
+        if (!valid) return;
+        const size_t k = (size_t)q * nr + (row0 + owner);
+        const int B = d.fwd[par][k];
+        const float3 es0 = xyz(d.springIn[0][k]), er0 = xyz(d.springIn[1][k]), et0 = xyz(d.springIn[2][k]);
+        // B's reverse slot of the pair (a reverse list has no entry for it
+        // when B's detection did not find it)
+        const int rb = rowOf(d, B);
+        long long kr = -1;
+        if (rb >= 0)
+            for (int m = min(d.rcnt[rb], d.scap), u = 0; u < m; ++u)
+                if (d.rev[(size_t)u * nr + rb] == A) {
+                    kr = (long long)u * nr + rb;
+                    break;
                 }
-            }
-            d.fcnt[par][row] = nf;
-            d.rcnt[row] = nb;
-            if (nf > C || nb > C) {
-                atomicOr(d.status, ST_SS_OVERFLOW);
-                atomicMax(&d.need[0], max(nf, nb));
-                nf = nb = 0;
-            }
-            n = nf;
-            contacts = nf + nb;
+        float3 es = es0, er = er0, et = et0;
+        const PairForce p = pairForce(d, A, B, es, er, et, dt);
+        d.springOut[par][0][k] = f4(es);
+        d.springOut[par][1][k] = f4(er);
+        d.springOut[par][2][k] = f4(et);
+        d.pF[k] = f4(p.F);
+        d.pT[k] = f4(p.T);
+        d.pTA[k] = f4(p.TA);
+        if (kr >= 0) {
+            const float3 mF = -p.F;
+            d.revF[kr] = make_float4(mF.x, mF.y, mF.z, 1.f);
+            d.revT[kr] = f4(-p.TB);
         }
-        __syncwarp();  // the row's list entries, for the lanes that evaluate them
-    } else if (live) {
+    });
+}
+
+// Force and torque on every solid that can touch others (calSolidForceTorque,
+// core/integrate.cu:806-858, with the walls of :514-610), one thread per row,
+// from the pair results of kPairForces: the forward contacts (the force on A
+// and its torque), then the reverse ones (minus the force, minus the torque
+// on B; a reverse slot that no forward row holds was left marked by the
+// detection and adds nothing), then the bonds.  Sums are Kahan-compensated,
+// in that order - no atomics.
+//
+// A warp runs its rows' items through warpItems, one lane per item, and each
+// row's lane adds its results in item order.
+__global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, float dt, int withCoupling,
+                                                     int rowsPerWarp)
+{
+    stepKernelBegin();
+    __shared__ float4 itemF[T], itemT[T];  // 32 items per warp
+    if (*d.status) return;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    // lanes 0 .. rowsPerWarp - 1 of each warp own a row
+    const int row0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rowsPerWarp;
+    const int row = row0 + lane;
+    const bool live = lane < rowsPerWarp && row < d.nrow;
+    const int a = live ? solidOf(d, row) : 0;
+    const size_t nr = (size_t)d.nrow;
+    // forward contacts (a, b) come first, then reverse ones (b, a), then bonds
+    int n = 0, contacts = 0;
+    if (live) {
         n = min(d.fcnt[par][row], d.scap);
         contacts = n + min(d.rcnt[row], d.scap);
     }
-    // then the row's bonds (their forces come from kBonds)
     const int bondFirst = live ? d.bondStart[a] : 0;
     const int total = contacts + (live ? d.bondStart[a + 1] - bondFirst : 0);
     float4* resF = itemF + (threadIdx.x & ~31);
@@ -502,49 +513,15 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
             const int oc = __shfl_sync(FULL, contacts, owner), ob = __shfl_sync(FULL, bondFirst, owner);
             const int orow = row0 + owner;
             float4 rF = make_float4(0.f, 0.f, 0.f, 0.f), rT = rF;
-            if (valid && q < oc) {
-                // through ONE inlined copy of pairForce: a pair's two solids run
-                // the same instructions on the same inputs and get the same bits
-                const bool fwdSide = q < on;
-                int A = oa, B;
-                long long k;
-                if (fwdSide) {
-                    k = (long long)q * nr + orow;
-                    B = d.fwd[par][k];
-                } else {
-                    A = d.rev[(size_t)(q - on) * nr + orow];
-                    B = oa;
-                    k = MERGED ? 0 : forwardSlot(d, par, A, oa);
-                }
-                if (k >= 0) {
-                    float3 es = make_float3(0.f, 0.f, 0.f), er = es, et = es;
-                    if (MERGED) {
-                        const long long ko = forwardSlot(d, prev, A, B);  // the pair in the previous list
-                        if (ko >= 0) {
-                            es = xyz(d.springOut[prev][0][ko]);
-                            er = xyz(d.springOut[prev][1][ko]);
-                            et = xyz(d.springOut[prev][2][ko]);
-                        }
-                    } else {
-                        es = xyz(d.springIn[0][k]);
-                        er = xyz(d.springIn[1][k]);
-                        et = xyz(d.springIn[2][k]);
-                    }
-                    const PairForce p = pairForce(d, A, B, es, er, et, dt);
-                    if (fwdSide) {
-                        d.springOut[par][0][k] = f4(es);
-                        d.springOut[par][1][k] = f4(er);
-                        d.springOut[par][2][k] = f4(et);
-                        d.pF[k] = f4(p.F);
-                        d.pT[k] = f4(p.T);
-                        rF = make_float4(p.F.x, p.F.y, p.F.z, 1.f);
-                        rT = f4(p.TA);
-                    } else {
-                        const float3 mF = -p.F, mT = -p.TB;
-                        rF = make_float4(mF.x, mF.y, mF.z, 1.f);
-                        rT = f4(mT);
-                    }
-                }
+            if (valid && q < on) {
+                const size_t k = (size_t)q * nr + orow;
+                const float4 f = d.pF[k];
+                rF = make_float4(f.x, f.y, f.z, 1.f);
+                rT = d.pTA[k];
+            } else if (valid && q < oc) {
+                const size_t k = (size_t)(q - on) * nr + orow;
+                rF = d.revF[k];  // w 0: a reverse pair the forward row does not hold
+                rT = d.revT[k];
             } else if (valid) {
                 const int bi = d.bondList[ob + q - oc];
                 float3 bF = xyz(d.bF[bi]), bT;
@@ -562,7 +539,132 @@ __global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, flo
         },
         [&](int, int pos) {
             const float4 f = resF[pos];
-            if (f.w != 0.f) {  // 0: a reverse pair the forward row does not hold
+            if (f.w != 0.f) {
+                F.add(xyz(f));
+                Tq.add(xyz(resT[pos]));
+            }
+        });
+    if (!live) return;
+    solidRowTail(d, par, a, F, Tq, withCoupling, dt);
+}
+
+// The contact list of a plain DEM step opened by a fused integration pass
+// and its contact forces in one launch (no bonds; 32 rows per warp): each
+// lane first builds its row's list from the candidates (rebuilt when stale)
+// on the end-of-step offsets sphE/splE, exactly as kContactDetect does; a
+// warp then runs its rows' contacts through warpItems, one lane per contact,
+// each contact evaluated by both of its solids with its springs from the
+// previous list (springOut of the other parity - the values kContactDetect's
+// remap would hand them): the same instructions on the same inputs give both
+// sides the bits kPairForces gives the pair, and the per-row sums are those
+// of kSolidForces, in the same order.  The candidates and the contact test
+// are symmetric in the two solids, so the forward row of every reverse pair
+// holds it.  In the walk mode they need not be: the launch then raises
+// ST_SPLIT_CONTACTS before writing anything, and the step is redone with the
+// separate launches.
+__global__ void __launch_bounds__(T, 6) kContactForces(DeviceState d, int par, float dt, int withCoupling)
+{
+    stepKernelBegin();
+    __shared__ float4 itemF[T], itemT[T];  // 32 items per warp
+    if (*d.status) return;
+    if (*d.slowMode) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(d.status, ST_SPLIT_CONTACTS);
+        return;
+    }
+    const int prev = par ^ 1;
+    // this step's flag is cleared by the next step's launch (this launch's
+    // rows read it); the step before's flag is free for this step's closing
+    // drift to raise
+    if (blockIdx.x == 0 && threadIdx.x == 0) *(volatile int*)&d.rebuild[prev] = 0;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int row0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    const int row = row0 + lane;
+    const bool live = row < d.nrow;
+    const int a = live ? solidOf(d, row) : 0;
+    const size_t nr = (size_t)d.nrow;
+    // forward contacts (a, b) come first, then reverse ones (b, a)
+    int n = 0, contacts = 0;
+    if (live) {
+        DeviceState atEnd = d;  // the end-of-step offsets
+        atEnd.sph = d.sphE;
+        atEnd.spl = d.splE;
+        if (d.rebuild[par]) verletBuildRow(atEnd, row);
+        const int C = d.scap;
+        int nf = 0, nb = 0;
+        const int nc = min(d.vcnt[row], d.vcap);
+        for (int k = 0; k < nc; ++k) {
+            const int b = d.vcand[(size_t)k * nr + row];
+            if (!solidsTouch(atEnd, a, b)) continue;
+            if (b > a) {
+                if (nf < C) d.fwd[par][(size_t)nf * nr + row] = b;
+                ++nf;
+            } else {
+                if (nb < C) d.rev[(size_t)nb * nr + row] = b;
+                ++nb;
+            }
+        }
+        d.fcnt[par][row] = nf;
+        d.rcnt[row] = nb;
+        if (nf > C || nb > C) {
+            atomicOr(d.status, ST_SS_OVERFLOW);
+            atomicMax(&d.need[0], max(nf, nb));
+            nf = nb = 0;
+        }
+        n = nf;
+        contacts = nf + nb;
+    }
+    __syncwarp();  // the row's list entries, for the lanes that evaluate them
+    float4* resF = itemF + (threadIdx.x & ~31);
+    float4* resT = itemT + (threadIdx.x & ~31);
+    KahanF3 F, Tq;
+    warpItems(
+        contacts,
+        [&](int owner, int q, bool valid) {
+            const int oa = __shfl_sync(FULL, a, owner), on = __shfl_sync(FULL, n, owner);
+            const int orow = row0 + owner;
+            float4 rF = make_float4(0.f, 0.f, 0.f, 0.f), rT = rF;
+            if (valid) {
+                // through ONE inlined copy of pairForce: a pair's two solids run
+                // the same instructions on the same inputs and get the same bits
+                const bool fwdSide = q < on;
+                int A = oa, B;
+                size_t k = 0;
+                if (fwdSide) {
+                    k = (size_t)q * nr + orow;
+                    B = d.fwd[par][k];
+                } else {
+                    A = d.rev[(size_t)(q - on) * nr + orow];
+                    B = oa;
+                }
+                float3 es = make_float3(0.f, 0.f, 0.f), er = es, et = es;
+                const long long ko = forwardSlot(d, prev, A, B);  // the pair in the previous list
+                if (ko >= 0) {
+                    es = xyz(d.springOut[prev][0][ko]);
+                    er = xyz(d.springOut[prev][1][ko]);
+                    et = xyz(d.springOut[prev][2][ko]);
+                }
+                const PairForce p = pairForce(d, A, B, es, er, et, dt);
+                if (fwdSide) {
+                    d.springOut[par][0][k] = f4(es);
+                    d.springOut[par][1][k] = f4(er);
+                    d.springOut[par][2][k] = f4(et);
+                    d.pF[k] = f4(p.F);
+                    d.pT[k] = f4(p.T);
+                    rF = make_float4(p.F.x, p.F.y, p.F.z, 1.f);
+                    rT = f4(p.TA);
+                } else {
+                    const float3 mF = -p.F, mT = -p.TB;
+                    rF = make_float4(mF.x, mF.y, mF.z, 1.f);
+                    rT = f4(mT);
+                }
+            }
+            resF[lane] = rF;
+            resT[lane] = rT;
+        },
+        [&](int, int pos) {
+            const float4 f = resF[pos];
+            if (f.w != 0.f) {
                 F.add(xyz(f));
                 Tq.add(xyz(resT[pos]));
             }
@@ -905,21 +1007,23 @@ __global__ void kIntegrate(DeviceState d, dfl half, int width, int clumpBlocks, 
 
 }  // namespace
 
-void launchBonds(const DeviceState& d, int par, float dt, cudaStream_t s)
+void launchPairForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
-    if (d.nb <= 0) return;
-    launchStep(kBonds, blocksFor(d.nb, T), T, s, d, par, dt);
+    const int cb = d.nrow > 0 ? blocksFor(d.nrow, d.forceRows * (T / 32)) : 0;
+    const int bb = d.nb > 0 ? blocksFor(d.nb, T) : 0;
+    if (cb + bb == 0) return;
+    launchStep(kPairForces, cb + bb, T, s, d, par, dt, d.forceRows, cb);
 }
 void launchSolidForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    launchStep(kSolidForces<false>, blocksFor(d.nrow, d.forceRows * (T / 32)), T, s, d, par, dt, d.nf > 0 ? 1 : 0,
+    launchStep(kSolidForces, blocksFor(d.nrow, d.forceRows * (T / 32)), T, s, d, par, dt, d.nf > 0 ? 1 : 0,
                d.forceRows);
 }
 void launchContactForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    launchStep(kSolidForces<true>, blocksFor(d.nrow, T), T, s, d, par, dt, d.nf > 0 ? 1 : 0, 32);
+    launchStep(kContactForces, blocksFor(d.nrow, T), T, s, d, par, dt, d.nf > 0 ? 1 : 0);
 }
 void launchClumpForce(const DeviceState& d, cudaStream_t s)
 {

@@ -179,6 +179,9 @@ void allocContactLists(demsph_engine* e)
     d.rev = dalloc<int>(c, e->owned, e->stream);
     d.pF = dalloc<float4>(c, e->owned, e->stream);
     d.pT = dalloc<float4>(c, e->owned, e->stream);
+    d.pTA = dalloc<float4>(c, e->owned, e->stream);
+    d.revF = dalloc<float4>(c, e->owned, e->stream);
+    d.revT = dalloc<float4>(c, e->owned, e->stream);
     for (int p = 0; p < 2; ++p) d.fwd[p] = dalloc<int>(c, e->owned, e->stream);
     for (int k = 0; k < 3; ++k) {
         d.springIn[k] = dalloc<float4>(c, e->owned, e->stream);
@@ -375,15 +378,16 @@ void stageFluid(demsph_engine* e, double dt, int iStep, int gap, bool countStep 
 // withClumpForce: the clumps' pebble forces are summed here (the staged
 // calls: the driver's hook runs between contact and integration); a whole
 // step (fullStep) sums them inside the integration that follows instead.
-// beforeForces: enqueued between the bonds and the contact forces (the join
-// of a side-stream branch whose result only the contact forces read).
+// beforeForces: enqueued between the pair forces (with the bonds) and the
+// per-solid sums (the join of a side-stream branch whose result only the
+// sums read).
 void stageContact(demsph_engine* e, double dt, bool withClumpForce = true,
                   const std::function<void()>* beforeForces = nullptr)
 {
     DeviceState& d = e->d;
-    if (d.nb > 0) {
-        TIMED("bonds");
-        launchBonds(d, e->par, (float)dt, e->stream);
+    {
+        TIMED("pair_forces");  // with the bonds
+        launchPairForces(d, e->par, (float)dt, e->stream);
     }
     if (beforeForces) (*beforeForces)();
     {
@@ -430,7 +434,7 @@ void fullStep(demsph_engine* e, double dt, int iStep, int gap, bool opened = fal
 // depends on nothing the search writes.  So the state after every step is
 // bit for bit that of fullStep.  The solids no integration moves (dummy
 // particles at rest) get their sphE/splE copy once, after the first search.
-// Without bonds (kBonds reads the contact list) the opened steps build their
+// Without bonds (a bond reads the contact list) the opened steps build their
 // contact list in the contact stage, in the launch of the contact forces: the
 // fluid stage of a plain DEM step (the coupling force) does not read it.
 void fusedSteps(demsph_engine* e, double dt, int iStep, int length, int gap)
@@ -456,14 +460,14 @@ void fusedSteps(demsph_engine* e, double dt, int iStep, int length, int gap)
         if (d.fsPairForce) launchCouplingPairForces(d, 0, d.fsPairForce, e->side);
         CK(cudaEventRecord(e->joinEv, e->side));
     };
-    // the join: the contact forces (which read the coupling force) wait for
-    // the branch; the bonds before them do not
+    // the join: the per-solid sums (which read the coupling force) wait for
+    // the branch; the pair forces and bonds before them do not
     const std::function<void()> join = [&] { CK(cudaStreamWaitEvent(e->stream, e->joinEv, 0)); };
     bool forked = false;
     for (int k = 0; k < length; ++k) {
         if (!forked) stageFluid(e, dt, iStep + k, gap);
         if (k > 0 && merge) {
-            TIMED("solid_forces");  // with the contact list of the step
+            TIMED("contact_forces");  // with the contact list of the step
             launchContactForces(d, e->par, (float)dt, e->stream);
         } else {
             stageContact(e, dt, false, forked ? &join : nullptr);
@@ -516,7 +520,7 @@ void grow(demsph_engine* e, int status)
             float4* keepSpring[3] = {d.springOut[keep][0], d.springOut[keep][1], d.springOut[keep][2]};
             d.fwd[keep] = nullptr;
             for (int k = 0; k < 3; ++k) d.springOut[keep][k] = nullptr;
-            void* ptrs[] = {d.rev, d.pF, d.pT, d.fwd[keep ^ 1], d.springIn[0], d.springIn[1], d.springIn[2],
+            void* ptrs[] = {d.rev, d.pF, d.pT, d.pTA, d.revF, d.revT, d.fwd[keep ^ 1], d.springIn[0], d.springIn[1], d.springIn[2],
                             d.springOut[keep ^ 1][0], d.springOut[keep ^ 1][1], d.springOut[keep ^ 1][2]};
             for (void* p : ptrs) freeOne(e, p);
             d.scap = std::max(d.scap * 2, need[0] + need[0] / 2 + 1);
@@ -1557,7 +1561,7 @@ long long demsph_estimate_bytes(const demsph_scene* sc, const demsph_options* op
     // list parities, springs in and out, candidates; per cell: counts and starts
     const long long kvf = kff + kff / 2, kvs = kfs + kfs / 2;
     return nf * (316 + 4 * (kff + kfs) + 4 * (kvf + kvs)) + ns * (248 + 48LL * sc->n_wall) +
-           rows * (72 + slots * 136 + 2 * slots * 4) + (cells + 1) * 16 + (long long)sc->n_clump * 160 +
+           rows * (72 + slots * 184 + 2 * slots * 4) + (cells + 1) * 16 + (long long)sc->n_clump * 160 +
            std::min(64 * rows + 1024, std::max(1LL, kfs * nf)) * 4 + (1 << 20);
 }
 

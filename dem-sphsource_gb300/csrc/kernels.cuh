@@ -296,6 +296,12 @@ struct DeviceState {
     float4* springOut[2][3];
     float4* pF;              // pair contact force on A, as the reference stores it (exports)
     float4* pT;              // pair contact torque (rolling + torsion), as the reference stores it (exports)
+    float4* pTA;             // torque of the pair's contact on A, with its lever arm
+    // per reverse slot: minus the pair's force and minus its torque on B (with
+    // its lever arm); w 1 once the forward row's pair force wrote it, 0 as the
+    // detection leaves it
+    float4* revF;
+    float4* revT;
     // Verlet candidates: partners within cut + skin at the last rebuild, by id
     int vcap;
     int* vcand;              // [k * nrow + r]
@@ -483,8 +489,10 @@ void launchCoupling(const DeviceState& d, int src, cudaStream_t s);
 void launchCouplingPairForces(const DeviceState& d, int src, float4* out, cudaStream_t s);
 
 // dem.cu
-void launchBonds(const DeviceState& d, int parity, float dt, cudaStream_t s);
-// Contact, bond, wall, coupling and gravity forces of every solid.
+// The step's contact forces, once per contact, and the bonds.
+void launchPairForces(const DeviceState& d, int parity, float dt, cudaStream_t s);
+// Contact, bond, wall, coupling and gravity forces of every solid, summed
+// from the pair results of launchPairForces.
 void launchSolidForces(const DeviceState& d, int parity, float dt, cudaStream_t s);
 // The contact list of a plain DEM step opened by a fused integration pass and
 // its contact forces in one launch (no bonds; candidates, not the walk):

@@ -564,6 +564,7 @@ __device__ __forceinline__ void detectRow(const DeviceState& d, int par, int for
         sortSlots(d.fwd[par], r, d.nrow, nf);
         sortSlots(d.rev, r, d.nrow, nb);
     }
+    for (int q = 0; q < nb; ++q) d.revF[(size_t)q * nr + r].w = 0.f;  // until a forward row's pair force writes it
     remapSprings(d, par, r, nf, 0, 1);
 }
 
@@ -619,7 +620,10 @@ __global__ void __launch_bounds__(T) kContactDetect(DeviceState d, int par, int 
         }
         if (tb) {
             const int q = nb + __popc(mb & below);
-            if (q < C) d.rev[(size_t)q * nr + r] = b;
+            if (q < C) {
+                d.rev[(size_t)q * nr + r] = b;
+                d.revF[(size_t)q * nr + r].w = 0.f;  // until the forward row's pair force writes it
+            }
         }
         nf += __popc(mf);
         nb += __popc(mb);

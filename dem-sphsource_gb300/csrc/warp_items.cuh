@@ -41,8 +41,10 @@ __device__ __forceinline__ int nthSetBit(unsigned m, int r)
 //     warp shuffles - with the full mask - before testing `valid`.
 //   take(q, pos): called on the owning lane for each of its items q, in
 //     increasing q, with the shared slot pos (0..31) holding its result.
-template <typename Eval, typename Take>
-__device__ __forceinline__ void warpItems(int total, Eval&& eval, Take&& take)
+// Without take (warpItems(total, eval)) the items only share out the work:
+// eval stores its results itself.
+template <bool WithTake, typename Eval, typename Take>
+__device__ __forceinline__ void warpItemsImpl(int total, Eval&& eval, Take&& take)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -74,17 +76,30 @@ __device__ __forceinline__ void warpItems(int total, Eval&& eval, Take&& take)
             const unsigned lrows = __shfl_sync(FULL, rows, lv);
             const int owner = nthSetBit(lrows, idx - __shfl_sync(FULL, first, lv)) & 31;
             eval(owner, L0 + lv, idx < items);
-            __syncwarp();
-            // each lane takes its items of this chunk, level by level
-            const int lvLo = __shfl_sync(FULL, lv, 0), lvHi = __shfl_sync(FULL, lv, min(31, items - 1 - c0));
-            for (int l = lvLo; l <= lvHi; ++l) {
-                const unsigned m = __shfl_sync(FULL, rows, l);
-                const int pos = __shfl_sync(FULL, first, l) + __popc(m & below) - c0;
-                if ((m >> lane & 1u) && pos >= 0 && pos < 32) take(L0 + l, pos);
+            if constexpr (WithTake) {
+                __syncwarp();
+                // each lane takes its items of this chunk, level by level
+                const int lvLo = __shfl_sync(FULL, lv, 0), lvHi = __shfl_sync(FULL, lv, min(31, items - 1 - c0));
+                for (int l = lvLo; l <= lvHi; ++l) {
+                    const unsigned m = __shfl_sync(FULL, rows, l);
+                    const int pos = __shfl_sync(FULL, first, l) + __popc(m & below) - c0;
+                    if ((m >> lane & 1u) && pos >= 0 && pos < 32) take(L0 + l, pos);
+                }
+                __syncwarp();
             }
-            __syncwarp();
         }
     }
+}
+
+template <typename Eval, typename Take>
+__device__ __forceinline__ void warpItems(int total, Eval&& eval, Take&& take)
+{
+    warpItemsImpl<true>(total, eval, take);
+}
+template <typename Eval>
+__device__ __forceinline__ void warpItems(int total, Eval&& eval)
+{
+    warpItemsImpl<false>(total, eval, [](int, int) {});
 }
 
 }  // namespace demsph
