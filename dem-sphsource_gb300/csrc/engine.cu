@@ -777,6 +777,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 d.fvl[b] = dalloc<float4>(nf, e->owned, e->stream);
                 d.fdrho[b] = dalloc<float>(nf, e->owned, e->stream);
             }
+            for (int b = 0; b < 3; ++b) d.fpd[b] = dalloc<float4>(nf, e->owned, e->stream);
             d.facc = dalloc<float4>(nf, e->owned, e->stream);
             d.fpar = dalloc<float4>(nf, e->owned, e->stream);
             d.fsumW0 = dalloc<float2>(nf, e->owned, e->stream);
@@ -1560,7 +1561,7 @@ long long demsph_estimate_bytes(const demsph_scene* sc, const demsph_options* op
     // solid: state, sort and wall springs; per contact row: its slots, two
     // list parities, springs in and out, candidates; per cell: counts and starts
     const long long kvf = kff + kff / 2, kvs = kfs + kfs / 2;
-    return nf * (316 + 4 * (kff + kfs) + 4 * (kvf + kvs)) + ns * (248 + 48LL * sc->n_wall) +
+    return nf * (364 + 4 * (kff + kfs) + 4 * (kvf + kvs)) + ns * (248 + 48LL * sc->n_wall) +
            rows * (72 + slots * 184 + 2 * slots * 4) + (cells + 1) * 16 + (long long)sc->n_clump * 160 +
            std::min(64 * rows + 1024, std::max(1LL, kfs * nf)) * 4 + (1 << 20);
 }

@@ -187,6 +187,11 @@ struct DeviceState {
     float4* fvh[2];
     float4* fvl[2];
     float* fdrho[2];
+    // partner records of the uniform-fluid pair loops (position offset xyz,
+    // density w: one 16-byte gather): [0] position 0 with density 0 (the
+    // first continuity pass), [1] position 1 with density 1 (momentum), [2]
+    // position 0 with density 1 (the second continuity pass)
+    float4* fpd[3];
     float4* facc;
     float4* fpar;
     float2* fsumW0;          // Shepard reference sum / sigma(h), double-float

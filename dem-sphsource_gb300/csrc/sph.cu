@@ -130,8 +130,9 @@ __device__ __forceinline__ void forFluidPartners(const unsigned* __restrict__ ff
 }
 
 // A fluid partner's state read by the continuity and momentum terms (the
-// buffers a pass reads are not written by it: read-only loads).  par only for
-// scenes whose fluids differ (U false).
+// buffers a pass reads are not written by it: read-only loads).  Uniform
+// fluids (U) read the position and density as one partner record (pd, the
+// pass's fpd); par only for scenes whose fluids differ (U false).
 template <bool U>
 struct FluidPartner {
     float4 p, v, par;
@@ -140,13 +141,19 @@ struct FluidPartner {
 
 template <bool U>
 __device__ __forceinline__ FluidPartner<U> gatherFluid(const DeviceState& d, int j, const float4* __restrict__ ph,
-                                                       const float4* __restrict__ vh, const float* __restrict__ dr)
+                                                       const float4* __restrict__ vh, const float* __restrict__ dr,
+                                                       const float4* __restrict__ pd)
 {
     FluidPartner<U> q;
-    q.p = __ldg(ph + j);
+    if constexpr (U) {
+        q.p = __ldg(pd + j);
+        q.dr = q.p.w;
+    } else {
+        q.p = __ldg(ph + j);
+        q.dr = __ldg(dr + j);
+        q.par = __ldg(d.fpar + j);
+    }
     q.v = __ldg(vh + j);
-    q.dr = __ldg(dr + j);
-    if constexpr (!U) q.par = __ldg(d.fpar + j);
     return q;
 }
 
@@ -177,6 +184,8 @@ __device__ __forceinline__ float groupSum(const KahanF& k)
 // ---- continuity (+ optional drift) ----
 struct ContinuityArgs {
     int ps, vs, ds, dd;  // position / velocity / density source, density destination
+    int rec;             // partner records read (uniform fluids): fpd[rec] holds position ps, density ds
+    int recOut;          // -1: none; else fpd[recOut] receives the drifted position and density dd
     int driftTo;         // -1: no drift; else position buffer receiving x + v * drift
     int velCopyTo;       // -1: none; else velocity buffer receiving a copy of this particle's velocity
     int countStep;       // 1: the pass ends the step (nothing after it can raise a status): count it
@@ -209,8 +218,9 @@ __global__ void __launch_bounds__(T, DEMSPH_CONTINUITY_BLOCKS) kContinuity(Devic
         const float4* __restrict__ ph = d.fph[a.ps];
         const float4* __restrict__ vh = d.fvh[a.vs];
         const float* __restrict__ drh = d.fdrho[a.ds];
+        const float4* __restrict__ pd = d.fpd[a.rec];
         forFluidPartners<L, batchDepth<L>()>(
-            d.ff, n, i, lane, nff, [&](unsigned e) { return gatherFluid<U>(d, ffPartner(e), ph, vh, drh); },
+            d.ff, n, i, lane, nff, [&](unsigned e) { return gatherFluid<U>(d, ffPartner(e), ph, vh, drh, pd); },
             [&](unsigned e, const FluidPartner<U>& q) {
                 const float3 r = fluidRel(d, walkTab, o.c, o.p, e, ffPartner(e), q.p);
                 const float r2 = dot3(r, r);
@@ -252,12 +262,14 @@ __global__ void __launch_bounds__(T, DEMSPH_CONTINUITY_BLOCKS) kContinuity(Devic
     }
     const float sum = groupSum<L>(acc);
     if (!live || lane != 0) return;
-    d.fdrho[a.dd][i] = d.fdrho[a.ds][i] + a.dt * sum;
+    const float drho = d.fdrho[a.ds][i] + a.dt * sum;
+    d.fdrho[a.dd][i] = drho;
     if (a.driftTo >= 0) {
         float4 xh = d.fph[a.ps][i], xl = d.fpl[a.ps][i];
         dfAxpy(xh, xl, d.fvh[a.vs][i], d.fvl[a.vs][i], a.drift);
         d.fph[a.driftTo][i] = xh;
         d.fpl[a.driftTo][i] = xl;
+        if (U && a.recOut >= 0) d.fpd[a.recOut][i] = make_float4(xh.x, xh.y, xh.z, drho);
     }
     if (a.velCopyTo >= 0) {
         d.fvh[a.velCopyTo][i] = d.fvh[a.vs][i];
@@ -288,7 +300,7 @@ __global__ void __launch_bounds__(T, DEMSPH_MOMENTUM_BLOCKS) kMomentum(DeviceSta
         const float twoNuRhoI = 2.f * d.fparU.z * o.rho, twoVi = 2.f * o.V;
         forFluidPartners<L, batchDepth<L>()>(
             d.ff, n, i, lane, nff,
-            [&](unsigned e) { return gatherFluid<U>(d, ffPartner(e), d.fph[1], d.fvh[0], d.fdrho[1]); },
+            [&](unsigned e) { return gatherFluid<U>(d, ffPartner(e), d.fph[1], d.fvh[0], d.fdrho[1], d.fpd[1]); },
             [&](unsigned e, const FluidPartner<U>& q) {
                 const float3 r = fluidRel(d, walkTab, o.c, o.p, e, ffPartner(e), q.p);
                 const float r2 = dot3(r, r);
@@ -359,6 +371,7 @@ __global__ void __launch_bounds__(T, DEMSPH_MOMENTUM_BLOCKS) kMomentum(DeviceSta
     dfAxpy(xh, xl, vh, vl, halfDtf);
     d.fph[0][i] = xh;
     d.fpl[0][i] = xl;
+    if (U) d.fpd[2][i] = make_float4(xh.x, xh.y, xh.z, d.fdrho[1][i]);  // the second continuity pass's partners
     // the fluid candidates go stale once a particle has moved half the margin
     const int4 c = d.fcell[i];
     const float4 p0 = d.fvref[i];
@@ -366,6 +379,17 @@ __global__ void __launch_bounds__(T, DEMSPH_MOMENTUM_BLOCKS) kMomentum(DeviceSta
                 dz = (float)c.z * d.grid.cs.z + xh.z - p0.z;
     const float half = 0.5f * d.fskin;
     if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)d.frebuild = 1;
+}
+
+// The first continuity pass's partner records: position 0 and density 0 as
+// the step's search and Shepard re-initialisation leave them.
+__global__ void kPackPartners(DeviceState d)
+{
+    stepKernelBegin();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nf || *d.status) return;
+    const float4 x = d.fph[0][i];
+    d.fpd[0][i] = make_float4(x.x, x.y, x.z, d.fdrho[0][i]);
 }
 
 template <int L>
@@ -512,9 +536,10 @@ void launchContinuityPass(const DeviceState& d, int which, double dtf, cudaStrea
     a.dt = (float)(0.5 * dtf);
     a.drift = df_from_double(0.5 * dtf);
     if (which == 0) {  // first half step: densities 0 -> 1, drift positions 0 -> 1
-        a.ps = 0; a.vs = 0; a.ds = 0; a.dd = 1; a.driftTo = 1; a.velCopyTo = -1;
+        a.ps = 0; a.vs = 0; a.ds = 0; a.dd = 1; a.driftTo = 1; a.velCopyTo = -1; a.rec = 0; a.recOut = 1;
+        if (d.uniformFluid) launchStep(kPackPartners, blocksFor(d.nf, 256), 256, s, d);
     } else {           // second half step: densities 1 -> 0, velocity 1 -> 0
-        a.ps = 0; a.vs = 1; a.ds = 1; a.dd = 0; a.driftTo = -1; a.velCopyTo = 0;
+        a.ps = 0; a.vs = 1; a.ds = 1; a.dd = 0; a.driftTo = -1; a.velCopyTo = 0; a.rec = 2; a.recOut = -1;
     }
     if (d.uniformFluid) LAUNCH_LANES_U(kContinuity, true, d.lanes, d.nf, T, s, d, a);
     else LAUNCH_LANES_U(kContinuity, false, d.lanes, d.nf, T, s, d, a);
