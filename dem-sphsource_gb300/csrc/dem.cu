@@ -477,74 +477,73 @@ __global__ void __launch_bounds__(T, 6) kPairForces(DeviceState d, int par, floa
 // and its torque), then the reverse ones (minus the force, minus the torque
 // on B; a reverse slot that no forward row holds was left marked by the
 // detection and adds nothing), then the bonds.  Sums are Kahan-compensated,
-// in that order - no atomics.
-//
-// A warp runs its rows' items through warpItems, one lane per item, and each
-// row's lane adds its results in item order.
-__global__ void __launch_bounds__(T, 6) kSolidForces(DeviceState d, int par, float dt, int withCoupling,
-                                                     int rowsPerWarp)
+// in that order - no atomics.  Every item is a few loads: they are issued
+// GATHER_BATCH at a time before their sums (the slots [k * nrow + row] of
+// neighbouring rows are neighbouring words).
+constexpr int GATHER_BATCH = 4;
+__global__ void __launch_bounds__(T) kSolidForces(DeviceState d, int par, float dt, int withCoupling)
 {
     stepKernelBegin();
-    __shared__ float4 itemF[T], itemT[T];  // 32 items per warp
     if (*d.status) return;
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    // lanes 0 .. rowsPerWarp - 1 of each warp own a row
-    const int row0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * rowsPerWarp;
-    const int row = row0 + lane;
-    const bool live = lane < rowsPerWarp && row < d.nrow;
-    const int a = live ? solidOf(d, row) : 0;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= d.nrow) return;
+    const int a = solidOf(d, row);
     const size_t nr = (size_t)d.nrow;
-    // forward contacts (a, b) come first, then reverse ones (b, a), then bonds
-    int n = 0, contacts = 0;
-    if (live) {
-        n = min(d.fcnt[par][row], d.scap);
-        contacts = n + min(d.rcnt[row], d.scap);
-    }
-    const int bondFirst = live ? d.bondStart[a] : 0;
-    const int total = contacts + (live ? d.bondStart[a + 1] - bondFirst : 0);
-    float4* resF = itemF + (threadIdx.x & ~31);
-    float4* resT = itemT + (threadIdx.x & ~31);
+    const int n = min(d.fcnt[par][row], d.scap), m = min(d.rcnt[row], d.scap);
+    const int b0 = d.bondStart[a], b1 = d.bondStart[a + 1];
     KahanF3 F, Tq;
-    warpItems(
-        total,
-        [&](int owner, int q, bool valid) {
-            const int oa = __shfl_sync(FULL, a, owner), on = __shfl_sync(FULL, n, owner);
-            const int oc = __shfl_sync(FULL, contacts, owner), ob = __shfl_sync(FULL, bondFirst, owner);
-            const int orow = row0 + owner;
-            float4 rF = make_float4(0.f, 0.f, 0.f, 0.f), rT = rF;
-            if (valid && q < on) {
-                const size_t k = (size_t)q * nr + orow;
-                const float4 f = d.pF[k];
-                rF = make_float4(f.x, f.y, f.z, 1.f);
-                rT = d.pTA[k];
-            } else if (valid && q < oc) {
-                const size_t k = (size_t)(q - on) * nr + orow;
-                rF = d.revF[k];  // w 0: a reverse pair the forward row does not hold
-                rT = d.revT[k];
-            } else if (valid) {
-                const int bi = d.bondList[ob + q - oc];
-                float3 bF = xyz(d.bF[bi]), bT;
-                if (d.bab[bi].x == oa) {
-                    bT = xyz(d.bTA[bi]);
-                } else {
-                    bF = -bF;
-                    bT = -xyz(d.bTB[bi]);
-                }
-                rF = make_float4(bF.x, bF.y, bF.z, 1.f);
-                rT = f4(bT);
+    for (int q0 = 0; q0 < n; q0 += GATHER_BATCH) {
+        float4 f[GATHER_BATCH], t[GATHER_BATCH];
+#pragma unroll
+        for (int u = 0; u < GATHER_BATCH; ++u)
+            if (q0 + u < n) {
+                const size_t k = (size_t)(q0 + u) * nr + row;
+                f[u] = d.pF[k];
+                t[u] = d.pTA[k];
             }
-            resF[lane] = rF;
-            resT[lane] = rT;
-        },
-        [&](int, int pos) {
-            const float4 f = resF[pos];
-            if (f.w != 0.f) {
-                F.add(xyz(f));
-                Tq.add(xyz(resT[pos]));
+#pragma unroll
+        for (int u = 0; u < GATHER_BATCH; ++u)
+            if (q0 + u < n) {
+                F.add(xyz(f[u]));
+                Tq.add(xyz(t[u]));
             }
-        });
-    if (!live) return;
+    }
+    for (int q0 = 0; q0 < m; q0 += GATHER_BATCH) {
+        float4 f[GATHER_BATCH], t[GATHER_BATCH];
+#pragma unroll
+        for (int u = 0; u < GATHER_BATCH; ++u)
+            if (q0 + u < m) {
+                const size_t k = (size_t)(q0 + u) * nr + row;
+                f[u] = d.revF[k];
+                t[u] = d.revT[k];
+            }
+#pragma unroll
+        for (int u = 0; u < GATHER_BATCH; ++u)
+            if (q0 + u < m && f[u].w != 0.f) {  // w 0: a reverse pair the forward row does not hold
+                F.add(xyz(f[u]));
+                Tq.add(xyz(t[u]));
+            }
+    }
+    for (int q0 = b0; q0 < b1; q0 += GATHER_BATCH) {
+        int bi[GATHER_BATCH];
+#pragma unroll
+        for (int u = 0; u < GATHER_BATCH; ++u) bi[u] = q0 + u < b1 ? d.bondList[q0 + u] : 0;
+        float4 f[GATHER_BATCH], t[GATHER_BATCH];
+        bool sideA[GATHER_BATCH];
+#pragma unroll
+        for (int u = 0; u < GATHER_BATCH; ++u)
+            if (q0 + u < b1) {
+                f[u] = d.bF[bi[u]];
+                sideA[u] = d.bab[bi[u]].x == a;
+                t[u] = sideA[u] ? d.bTA[bi[u]] : d.bTB[bi[u]];
+            }
+#pragma unroll
+        for (int u = 0; u < GATHER_BATCH; ++u)
+            if (q0 + u < b1) {
+                F.add(sideA[u] ? xyz(f[u]) : -xyz(f[u]));
+                Tq.add(sideA[u] ? xyz(t[u]) : -xyz(t[u]));
+            }
+    }
     solidRowTail(d, par, a, F, Tq, withCoupling, dt);
 }
 
@@ -1017,8 +1016,7 @@ void launchPairForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 void launchSolidForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
     if (d.nrow <= 0) return;
-    launchStep(kSolidForces, blocksFor(d.nrow, d.forceRows * (T / 32)), T, s, d, par, dt, d.nf > 0 ? 1 : 0,
-               d.forceRows);
+    launchStep(kSolidForces, blocksFor(d.nrow, T), T, s, d, par, dt, d.nf > 0 ? 1 : 0);
 }
 void launchContactForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 {
