@@ -770,6 +770,7 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 id[i] = i;
             }
             d.fcell = dalloc<int4>(nf, e->owned, e->stream);
+            d.fcp = dalloc<float4>(nf, e->owned, e->stream);
             for (int b = 0; b < 2; ++b) {
                 d.fph[b] = dalloc<float4>(nf, e->owned, e->stream);
                 d.fpl[b] = dalloc<float4>(nf, e->owned, e->stream);
@@ -834,6 +835,8 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                     d.uniformFluid = par[i].x == par[0].x && par[i].y == par[0].y && par[i].z == par[0].z &&
                                      par[i].w == par[0].w && ph[i].w == ph[0].w && pl[i].w == pl[0].w;
                 d.fparU = par[0];
+                d.cellPack = d.uniformFluid && !d.fluidTiles && d.grid.gx <= 2048 && d.grid.gy <= 2048 &&
+                             d.grid.gz <= 1024 ? 1 : 0;
                 {
                     const float h = ph[0].w;
                     const float kg = 5.f * 21.f / (16.f * 3.14159265358979323846f);
@@ -1561,7 +1564,7 @@ long long demsph_estimate_bytes(const demsph_scene* sc, const demsph_options* op
     // solid: state, sort and wall springs; per contact row: its slots, two
     // list parities, springs in and out, candidates; per cell: counts and starts
     const long long kvf = kff + kff / 2, kvs = kfs + kfs / 2;
-    return nf * (364 + 4 * (kff + kfs) + 4 * (kvf + kvs)) + ns * (248 + 48LL * sc->n_wall) +
+    return nf * (380 + 4 * (kff + kfs) + 4 * (kvf + kvs)) + ns * (248 + 48LL * sc->n_wall) +
            rows * (72 + slots * 184 + 2 * slots * 4) + (cells + 1) * 16 + (long long)sc->n_clump * 160 +
            std::min(64 * rows + 1024, std::max(1LL, kfs * nf)) * 4 + (1 << 20);
 }

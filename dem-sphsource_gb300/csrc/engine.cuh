@@ -142,6 +142,18 @@ __device__ __forceinline__ float3 toF3(DF3 r)
     return make_float3(r.x.hi + r.x.lo, r.y.hi + r.y.lo, r.z.hi + r.z.lo);
 }
 // x_a - x_b in FP32 (hi parts only): exact cell term, ~1e-7 relative.
+// A cell inside the grid (x < 2048, y < 2048, z < 1024) as the bits of one
+// float, and back (the key, w, is not kept).
+__device__ __forceinline__ float packCell(int4 c)
+{
+    return __uint_as_float((unsigned)c.x | ((unsigned)c.y << 11) | ((unsigned)c.z << 22));
+}
+__device__ __forceinline__ int4 unpackCell(float w)
+{
+    const unsigned b = __float_as_uint(w);
+    return make_int4((int)(b & 2047u), (int)((b >> 11) & 2047u), (int)(b >> 22), 0);
+}
+
 __device__ __forceinline__ float3 relF(int4 ca, float4 ha, int4 cb, float4 hb, const GridDev& g)
 {
     return make_float3((ha.x - hb.x) + (float)(ca.x - cb.x) * g.cs.x, (ha.y - hb.y) + (float)(ca.y - cb.y) * g.cs.y,

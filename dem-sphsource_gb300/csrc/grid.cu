@@ -46,6 +46,7 @@ __device__ __forceinline__ void fluidHashOne(const DeviceState& d, int i, const 
         d.fcell[i] = c;
         d.fph[0][i] = h;
         d.fpl[0][i] = l;
+        if (d.cellPack) d.fcp[i] = make_float4(h.x, h.y, h.z, packCell(c));
         return;
     }
     // copy the whole particle into the gather sources
@@ -101,8 +102,11 @@ __device__ __forceinline__ void fluidGatherOne(const DeviceState& d, int p)
 {
     int e;
     const int q = stableRank(p, d.fsortTmp, d.fkey, d.fcellStart, d.tid, e);
-    d.fcell[q] = d.tcell[e];
-    d.fph[0][q] = d.fph[1][e];
+    const int4 c = d.tcell[e];
+    const float4 h = d.fph[1][e];
+    d.fcell[q] = c;
+    d.fph[0][q] = h;
+    if (d.cellPack) d.fcp[q] = make_float4(h.x, h.y, h.z, packCell(c));
     d.fpl[0][q] = d.fpl[1][e];
     d.fvh[0][q] = d.fvh[1][e];
     d.fvl[0][q] = d.fvl[1][e];

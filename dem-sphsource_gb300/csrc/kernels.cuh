@@ -182,6 +182,11 @@ struct DeviceState {
     float4 fparU;            // speed, viscosity, mass) and the same smoothing length
     float4 fconstU;          // with them: 4 h^2, 0.5 / h, KG / h^5, 1 / sound speed
     int4* fcell;
+    // filter records of uniform fluids on grids of at most 2048 x 2048 x 1024
+    // cells (cellPack): the position offset of fph[0] and the cell packed in w
+    // (packCell), as each fluid step's hash or reorder leaves them
+    float4* fcp;
+    int cellPack;
     float4* fph[2];
     float4* fpl[2];
     float4* fvh[2];

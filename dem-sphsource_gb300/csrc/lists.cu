@@ -327,12 +327,18 @@ __device__ __forceinline__ int walkPosition(int4 ci, int4 cj)
 // around the particle's current cell (all particles are inside the domain
 // here, so those are the cells the reference walks).  The rebuild flag is
 // cleared: the last position update of the step raises it again.
-template <int L>
-__global__ void __launch_bounds__(T) kFluidFilter(DeviceState d)
+//
+// P (cellPack): a candidate's cell and position offset come from its filter
+// record (one 16-byte read); the smoothing length is every particle's.
+#ifndef DEMSPH_FILTER_UNROLL
+#define DEMSPH_FILTER_UNROLL 4  // rounds of candidate reads in flight with one lane per particle
+#endif
+template <int L, bool P>
+__device__ __forceinline__ void fluidFilter(const DeviceState& d)
 {
     // one lane per particle walks a long candidate list: 4 rounds of reads in
     // flight; with 4 or 8 lanes a round already covers many candidates
-    constexpr int FILTER_UNROLL = L == 1 ? 4 : (L == 2 ? 2 : 1);
+    constexpr int FILTER_UNROLL = L == 1 ? DEMSPH_FILTER_UNROLL : (L == 2 ? 2 : 1);
     stepKernelBegin();
     const int th = blockIdx.x * blockDim.x + threadIdx.x;
     if ((th & ~31) >= d.nf * L || *d.status || *d.fslowMode || *d.slowMode) return;
@@ -360,20 +366,35 @@ __global__ void __launch_bounds__(T) kFluidFilter(DeviceState d)
     // reads are issued together, their results compacted round by round (the
     // list order of one round per iteration)
     int nff = 0;
+    // the next rounds' candidate ids are read while this round's partners are
+    // gathered and tested
+    int jn[FILTER_UNROLL];
+#pragma unroll
+    for (int u = 0; u < FILTER_UNROLL; ++u) {
+        const int k = u * L + lane;
+        jn[u] = k < nc ? (int)d.fvc[(size_t)k * n + i] : -1;
+    }
     for (int base = 0; __any_sync(0xffffffffu, base < nc); base += FILTER_UNROLL * L) {
         int j[FILTER_UNROLL];
         int4 cj[FILTER_UNROLL];
         float4 hj[FILTER_UNROLL];
 #pragma unroll
         for (int u = 0; u < FILTER_UNROLL; ++u) {
-            const int k = base + u * L + lane;
-            j[u] = k < nc ? (int)d.fvc[(size_t)k * n + i] : -1;
+            j[u] = jn[u];
+            const int k = base + (FILTER_UNROLL + u) * L + lane;
+            jn[u] = k < nc ? (int)d.fvc[(size_t)k * n + i] : -1;
         }
 #pragma unroll
         for (int u = 0; u < FILTER_UNROLL; ++u) {
             if (j[u] >= 0) {
-                cj[u] = d.fcell[j[u]];
-                hj[u] = d.fph[0][j[u]];
+                if constexpr (P) {
+                    const float4 r = __ldg(d.fcp + j[u]);
+                    cj[u] = unpackCell(r.w);
+                    hj[u] = make_float4(r.x, r.y, r.z, hi.w);
+                } else {
+                    cj[u] = d.fcell[j[u]];
+                    hj[u] = d.fph[0][j[u]];
+                }
             }
         }
 #pragma unroll
@@ -389,7 +410,7 @@ __global__ void __launch_bounds__(T) kFluidFilter(DeviceState d)
                     if (d2 < c2 * (1.f - 1.e-5f)) {
                         take = true;
                     } else if (d2 <= c2 * (1.f + 1.e-5f)) {
-                        const dfl hJ = df_make(hj[u].w, d.fpl[0][j[u]].w);
+                        const dfl hJ = P ? hI : df_make(hj[u].w, d.fpl[0][j[u]].w);
                         const dfl rad = dfMax(hI, hJ);
                         take = withinCut(ci, hi, li, cj[u], hj[u], d.fpl[0], j[u], df_add(rad, rad), d.grid);
                     }
@@ -432,6 +453,16 @@ __global__ void __launch_bounds__(T) kFluidFilter(DeviceState d)
     d.fsc[i] = nfs;
     if (nff > d.kff) atomicOr(d.status, ST_FF_OVERFLOW);
     if (nfs > d.kfs) atomicOr(d.status, ST_FS_OVERFLOW);
+}
+template <int L>
+__global__ void __launch_bounds__(T) kFluidFilter(DeviceState d)
+{
+    fluidFilter<L, false>(d);
+}
+template <int L>
+__global__ void __launch_bounds__(T) kFluidFilterPacked(DeviceState d)
+{
+    fluidFilter<L, true>(d);
 }
 
 // ---- fluid partners of each massive solid (coupling force) ----
@@ -826,7 +857,8 @@ void launchFluidWalk(const DeviceState& d, bool walk, cudaStream_t s)
 void launchFluidFilter(const DeviceState& d, cudaStream_t s)
 {
     if (d.nf <= 0) return;
-    LAUNCH_LANES(kFluidFilter, d.lanes, d.nf, T, s, d);
+    if (d.cellPack) LAUNCH_LANES(kFluidFilterPacked, d.lanes, d.nf, T, s, d);
+    else LAUNCH_LANES(kFluidFilter, d.lanes, d.nf, T, s, d);
 }
 
 void launchCouplingLists(const DeviceState& d, cudaStream_t s)
