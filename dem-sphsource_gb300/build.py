@@ -65,8 +65,16 @@ def _run(cmd, verbose):
 # stated tolerance against the FP64 oracle) replace the IEEE-rounded ones.
 # The double-float helpers call the correctly rounded intrinsics explicitly
 # and are unaffected.
+#
+# The DEM kernels (dem.cu) run the same arithmetic (a pair's contact law, a
+# solid's force sum and integration) inside several kernels whose results must
+# agree bit for bit (one-launch and two-launch contact forces, the per-solid
+# sums with and without the integration pass, staged calls and graphs); no
+# product is contracted into an FMA there (-fmad=false), so every kernel rounds
+# each operation as the source writes it, whatever code surrounds it.
 FILE_FLAGS = {"sph.cu": ["-prec-div=false", "-prec-sqrt=false"],
-              "sph_tiles.cu": ["-prec-div=false", "-prec-sqrt=false"]}
+              "sph_tiles.cu": ["-prec-div=false", "-prec-sqrt=false"],
+              "dem.cu": ["-fmad=false"]}
 
 
 def nvcc_flags(cuda):

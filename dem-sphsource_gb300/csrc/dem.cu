@@ -481,12 +481,9 @@ __global__ void __launch_bounds__(T, 6) kPairForces(DeviceState d, int par, floa
 // GATHER_BATCH at a time before their sums (the slots [k * nrow + row] of
 // neighbouring rows are neighbouring words).
 constexpr int GATHER_BATCH = 4;
-__global__ void __launch_bounds__(T) kSolidForces(DeviceState d, int par, float dt, int withCoupling)
+// Row `row`'s sums and tail; returns its solid.
+__device__ __forceinline__ int solidForcesRow(const DeviceState& d, int par, float dt, int withCoupling, int row)
 {
-    stepKernelBegin();
-    if (*d.status) return;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= d.nrow) return;
     const int a = solidOf(d, row);
     const size_t nr = (size_t)d.nrow;
     const int n = min(d.fcnt[par][row], d.scap), m = min(d.rcnt[row], d.scap);
@@ -545,6 +542,15 @@ __global__ void __launch_bounds__(T) kSolidForces(DeviceState d, int par, float 
             }
     }
     solidRowTail(d, par, a, F, Tq, withCoupling, dt);
+    return a;
+}
+
+__global__ void __launch_bounds__(T) kSolidForces(DeviceState d, int par, float dt, int withCoupling)
+{
+    stepKernelBegin();
+    if (*d.status) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row < d.nrow) solidForcesRow(d, par, dt, withCoupling, row);
 }
 
 // The contact list of a plain DEM step opened by a fused integration pass
@@ -1002,6 +1008,24 @@ __global__ void kIntegrate(DeviceState d, dfl half, int width, int clumpBlocks, 
     }
 }
 
+// The per-solid sums of kSolidForces and, in the same thread, the solid's
+// integration pass (MODE after or fused, kIntegrate's work for one solid),
+// for scenes whose integrated solids are exactly the contact rows (no clumps,
+// no moving dummy particles): no other thread of the launch reads the state
+// a row's integration writes.  countStep as kIntegrate's.
+template <int MODE>
+__global__ void __launch_bounds__(T) kSolidForcesIntegrate(DeviceState d, int par, float dt, int withCoupling,
+                                                           dfl half, int countStep)
+{
+    stepKernelBegin();
+    if (countStep && blockIdx.x == 0 && threadIdx.x == 0 && *d.status == 0) atomicAdd(d.stepsDone, 1);
+    if (*d.status) return;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= d.nrow) return;
+    const int a = solidForcesRow(d, par, dt, withCoupling, row);
+    solidIntegrateOne<MODE>(d, a, half, d.rebuild + (par ^ 1));
+}
+
 
 
 }  // namespace
@@ -1013,10 +1037,17 @@ void launchPairForces(const DeviceState& d, int par, float dt, cudaStream_t s)
     if (cb + bb == 0) return;
     launchStep(kPairForces, cb + bb, T, s, d, par, dt, d.forceRows, cb);
 }
-void launchSolidForces(const DeviceState& d, int par, float dt, cudaStream_t s)
+void launchSolidForces(const DeviceState& d, int par, double dt, cudaStream_t s, int integrate, bool countStep)
 {
     if (d.nrow <= 0) return;
-    launchStep(kSolidForces, blocksFor(d.nrow, T), T, s, d, par, dt, d.nf > 0 ? 1 : 0);
+    const int blocks = blocksFor(d.nrow, T), cpl = d.nf > 0 ? 1 : 0, cs = countStep ? 1 : 0;
+    const dfl h = df_from_double(0.5 * dt);
+    if (integrate == INTEGRATE_FUSED)
+        launchStep(kSolidForcesIntegrate<INTEGRATE_FUSED>, blocks, T, s, d, par, (float)dt, cpl, h, cs);
+    else if (integrate == INTEGRATE_AFTER)
+        launchStep(kSolidForcesIntegrate<INTEGRATE_AFTER>, blocks, T, s, d, par, (float)dt, cpl, h, cs);
+    else
+        launchStep(kSolidForces, blocks, T, s, d, par, (float)dt, cpl);
 }
 void launchContactForces(const DeviceState& d, int par, float dt, cudaStream_t s)
 {

@@ -381,8 +381,10 @@ void stageFluid(demsph_engine* e, double dt, int iStep, int gap, bool countStep 
 // beforeForces: enqueued between the pair forces (with the bonds) and the
 // per-solid sums (the join of a side-stream branch whose result only the
 // sums read).
+// integrate, countStep: the per-solid sums also run the solids' integration
+// pass of that kind (see sumsIntegrate).
 void stageContact(demsph_engine* e, double dt, bool withClumpForce = true,
-                  const std::function<void()>* beforeForces = nullptr)
+                  const std::function<void()>* beforeForces = nullptr, int integrate = -1, bool countStep = false)
 {
     DeviceState& d = e->d;
     {
@@ -392,12 +394,20 @@ void stageContact(demsph_engine* e, double dt, bool withClumpForce = true,
     if (beforeForces) (*beforeForces)();
     {
         TIMED("solid_forces");
-        launchSolidForces(d, e->par, (float)dt, e->stream);
+        launchSolidForces(d, e->par, dt, e->stream, integrate, countStep);
     }
     if (d.nc > 0 && withClumpForce) {
         TIMED("clump_force");
         launchClumpForce(d, e->stream);
     }
+}
+
+// The solids the integration moves are exactly the contact rows (no clumps,
+// no moving dummy particles): the per-solid sums can integrate them.
+bool sumsIntegrate(const demsph_engine* e)
+{
+    const DeviceState& d = e->d;
+    return e->foldIntegration && d.nc == 0 && d.nrow > 0 && d.nmove == d.nrow;
 }
 
 void stageAfter(demsph_engine* e, double dt, bool clumpForce = false, bool countStep = false)
@@ -422,6 +432,11 @@ void fullStep(demsph_engine* e, double dt, int iStep, int gap, bool opened = fal
     stageNeighborSearch(e, iStep, gap, opened);
     if (!opened) stageBefore(e, dt);
     stageFluid(e, dt, iStep, gap, countInFluid);
+    if (sumsIntegrate(e)) {
+        stageContact(e, dt, false, nullptr, INTEGRATE_AFTER, !countInFluid);
+        e->keysAdvanced = true;  // as stageAfter
+        return;
+    }
     stageContact(e, dt, false);
     stageAfter(e, dt, e->d.nc > 0, !countInFluid);
 }
@@ -463,25 +478,34 @@ void fusedSteps(demsph_engine* e, double dt, int iStep, int length, int gap)
     // the join: the per-solid sums (which read the coupling force) wait for
     // the branch; the pair forces and bonds before them do not
     const std::function<void()> join = [&] { CK(cudaStreamWaitEvent(e->stream, e->joinEv, 0)); };
+    const bool fold = sumsIntegrate(e);
     bool forked = false;
     for (int k = 0; k < length; ++k) {
         if (!forked) stageFluid(e, dt, iStep + k, gap);
+        const bool last = k == length - 1;
+        bool integrated = false;
         if (k > 0 && merge) {
             TIMED("contact_forces");  // with the contact list of the step
             launchContactForces(d, e->par, (float)dt, e->stream);
         } else {
-            stageContact(e, dt, false, forked ? &join : nullptr);
+            // the sums close the step (the last) or close it and open the next
+            integrated = fold;
+            stageContact(e, dt, false, forked ? &join : nullptr,
+                         fold ? (last ? INTEGRATE_AFTER : INTEGRATE_FUSED) : -1, true);
         }
         forked = false;
-        if (k == length - 1) break;
-        {
+        if (last) {
+            if (integrated) e->keysAdvanced = true;  // as stageAfter
+            else stageAfter(e, dt, d.nc > 0, true);
+            break;
+        }
+        if (!integrated) {
             TIMED("integrate_after");  // the closing half of this step and the opening half of the next
             launchSolidIntegrate(d, dt, INTEGRATE_FUSED, e->par, d.nc > 0, true, e->stream);
         }
         stageNeighborSearch(e, iStep + k + 1, gap, true, !merge, branch ? &fork : nullptr);
         forked = branch;
     }
-    stageAfter(e, dt, d.nc > 0, true);
 }
 
 // Grows whatever overflowed and clears the status.  e->par must be the parity
@@ -985,6 +1009,10 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
             {
                 const char* v = std::getenv("DEMSPH_MERGE_CONTACTS");
                 e->mergeContacts = !(v && v[0] == '0') && !walkOnly;
+            }
+            {
+                const char* v = std::getenv("DEMSPH_FOLD_INTEGRATION");
+                e->foldIntegration = !(v && v[0] == '0');
             }
             const int both[2] = {1, 1};
             CK(cudaMemcpyAsync(d.rebuild, both, sizeof(both), cudaMemcpyHostToDevice, e->stream));

@@ -84,6 +84,10 @@ struct demsph_engine {
     // lists come from candidates (DEMSPH_MERGE_CONTACTS=0 keeps two launches;
     // off for good once the lists come from the walk).
     bool mergeContacts = true;
+    // The per-solid sums run the solids' integration pass in the same launch
+    // when the integrated solids are exactly the contact rows
+    // (DEMSPH_FOLD_INTEGRATION=0 keeps the separate pass).
+    bool foldIntegration = true;
     // The step the next attempt starts with already had its before-contact
     // half applied (a fused pass ran before its neighbour search overflowed).
     bool resumeOpened = false;
@@ -155,6 +159,7 @@ struct demsph_engine {
         swap(nMassive, o.nMassive);
         swap(fuseIntegration, o.fuseIntegration);
         swap(mergeContacts, o.mergeContacts);
+        swap(foldIntegration, o.foldIntegration);
         swap(resumeOpened, o.resumeOpened);
         swap(keysAdvanced, o.keysAdvanced);
         swap(runStats, o.runStats);

@@ -502,8 +502,12 @@ void launchCouplingPairForces(const DeviceState& d, int src, float4* out, cudaSt
 // The step's contact forces, once per contact, and the bonds.
 void launchPairForces(const DeviceState& d, int parity, float dt, cudaStream_t s);
 // Contact, bond, wall, coupling and gravity forces of every solid, summed
-// from the pair results of launchPairForces.
-void launchSolidForces(const DeviceState& d, int parity, float dt, cudaStream_t s);
+// from the pair results of launchPairForces.  integrate (INTEGRATE_AFTER or
+// INTEGRATE_FUSED; -1 none): each row's thread then runs its solid's
+// integration pass (only when the integrated solids are exactly the rows);
+// countStep as launchSolidIntegrate's.
+void launchSolidForces(const DeviceState& d, int parity, double dt, cudaStream_t s, int integrate = -1,
+                       bool countStep = false);
 // The contact list of a plain DEM step opened by a fused integration pass and
 // its contact forces in one launch (no bonds; candidates, not the walk):
 // each row filters its candidates on the end-of-step offsets (sphE/splE) and

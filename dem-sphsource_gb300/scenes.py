@@ -551,9 +551,10 @@ def tiny_escape(seed=5, with_probe_fluid=True):
     return r
 
 
-def tiny_coupled(seed=4, gap=3):
+def tiny_coupled(seed=4, gap=3, with_clump=True):
     """Dam break of 600 fluid particles onto two bonded 3x3x3 clusters and a
-    4-pebble clump, with walls; the fluid is integrated every ``gap`` steps."""
+    4-pebble clump (left out when ``with_clump`` is false), with walls; the
+    fluid is integrated every ``gap`` steps."""
     rng = np.random.default_rng(seed)
     dx = 0.01
     tank = (0.2, 0.08, 0.12)
@@ -578,7 +579,8 @@ def tiny_coupled(seed=4, gap=3):
     peb = c + tet
     pr = np.full(4, 1.5e-3)
     mass = 2500.0 * 4.0 / 3.0 * math.pi * 1.5e-3 ** 3 * 3.2
-    r.addClump(peb, pr, c, (0, 0, 0), (0, 0, 0), mass, clump_inertia(peb, pr, c, mass), 2)
+    if with_clump:
+        r.addClump(peb, pr, c, (0, 0, 0), (0, 0, 0), mass, clump_inertia(peb, pr, c, mass), 2)
     r.addInfiniteWall((0, 0, 0), (0, 0, 1), 0)
     mass1 = 2500.0 * 4.0 / 3.0 * math.pi * sr ** 3
     dt = 0.2 * math.sqrt(mass1 / 1.0e4)

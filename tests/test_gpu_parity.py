@@ -358,6 +358,36 @@ def test_profiled_update_runs_the_graph_bodies(ds, scenes, name):
     _same_state_and_lists(timed, plain)
 
 
+@pytest.mark.parametrize("name", ("coupled_without_clump", "tiny_converging", "tiny_escape"))
+def test_folded_integration_equals_the_separate_pass(ds, scenes, name, monkeypatch):
+    """Where the integrated solids are exactly the contact rows (no clumps,
+    no moving dummy particles) the per-solid force sums run the solids'
+    integration pass in the same launch: forty steps from graphs give the bits
+    and lists of the separate pass (DEMSPH_FOLD_INTEGRATION=0, read when an
+    engine is created) and of the staged calls, with fewer launches."""
+    recipe = scenes.tiny_coupled(with_clump=False) if name == "coupled_without_clump" else getattr(scenes, name)()
+    b, sc = ds.build_scene(recipe)
+    engines = []
+    for fold in ("1", "0"):
+        monkeypatch.setenv("DEMSPH_FOLD_INTEGRATION", fold)
+        engines.append(ds.Engine(sc))
+    monkeypatch.delenv("DEMSPH_FOLD_INTEGRATION")
+    staged = ds.Engine(sc)
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    for e in engines + [staged]:
+        e.initialize()
+    launches = []
+    for e in engines:
+        before = e.kernel_launches()
+        e.update(dt, 1, 40, gap, use_graph=True)
+        launches.append(e.kernel_launches() - before)
+    for s in range(1, 41):
+        staged.step(dt, s, gap)
+    assert launches[0] < launches[1], launches
+    _same_state_and_lists(engines[0], engines[1])
+    _same_state_and_lists(engines[0], staged)
+
+
 def test_walk_mode_splits_the_merged_contact_launch(ds, scenes):
     """Two solids start above the domain, so the lists come from the walk:
     the first step a fused pass opens finds the one-launch contact list
