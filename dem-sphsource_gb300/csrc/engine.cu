@@ -285,7 +285,7 @@ void stageNeighborSearch(demsph_engine* e, int iStep, int gap, bool endView = fa
     const bool fluidStep = d.nf > 0 && (iStep % gap == 0);
     // solids that never move (walls of dummy particles, fixed spheres) are
     // hashed and sorted once, and again only after their positions are uploaded
-    const bool solidsMove = e->nMassive > 0 || e->solidSortStale;
+    const bool solidsMove = e->nMassive > 0 || e->movingDummies > 0 || e->solidSortStale;
     const bool forceSort = e->forceWalk || e->solidSortStale;
     // Work needed only on some steps (sorting by cell, rebuilding candidates,
     // the walk) is launched every step and decided on the device from the
@@ -957,6 +957,17 @@ int demsph_create(const demsph_scene* sc, const demsph_options* opt, demsph_engi
                 d.nmove = (int)move.size();
                 d.moveList = dalloc<int>(move.size(), e->owned, e->stream);
                 d.moveFirst = consecutiveFirst(move.data(), move.size());
+                d.ndummy = (int)e->dummyIdx.size();
+                e->movingDummies = (int)std::count(e->dummyMoving.begin(), e->dummyMoving.end(), (unsigned char)1);
+                d.dummyIdx = dalloc<int>(std::max(1, d.ndummy), e->owned, e->stream);
+                d.dummyMoving = dalloc<unsigned char>(std::max(1, d.ndummy), e->owned, e->stream);
+                d.moveChanged = dalloc<int>(1, e->owned, e->stream);
+                if (d.ndummy > 0) {
+                    CK(cudaMemcpyAsync(d.dummyIdx, e->dummyIdx.data(), sizeof(int) * d.ndummy, cudaMemcpyHostToDevice,
+                                       e->stream));
+                    CK(cudaMemcpyAsync(d.dummyMoving, e->dummyMoving.data(), d.ndummy, cudaMemcpyHostToDevice,
+                                       e->stream));
+                }
                 if (!move.empty())
                     CK(cudaMemcpyAsync(d.moveList, move.data(), sizeof(int) * move.size(), cudaMemcpyHostToDevice,
                                        e->stream));

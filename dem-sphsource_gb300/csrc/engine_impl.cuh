@@ -68,6 +68,7 @@ struct demsph_engine {
     int debug = 0;
     double hmax = 0;              // largest fluid smoothing length
     int nMassive = 0;
+    int movingDummies = 0;  // dummy particles given a velocity (in the move list)
     // CUDA graphs of step runs, keyed by the kind of step, the contact-list
     // parity they start from and their length (all for one dt and gap)
     struct CachedGraph {
@@ -157,6 +158,7 @@ struct demsph_engine {
         swap(debug, o.debug);
         swap(hmax, o.hmax);
         swap(nMassive, o.nMassive);
+        swap(movingDummies, o.movingDummies);
         swap(fuseIntegration, o.fuseIntegration);
         swap(mergeContacts, o.mergeContacts);
         swap(foldIntegration, o.foldIntegration);

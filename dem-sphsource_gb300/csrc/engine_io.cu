@@ -331,22 +331,21 @@ void enqueueUploadFluids(demsph_engine* e, const double* pos, const double* vel,
     ++t_kernelLaunches, kFluidIn<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, dp, dv, dr);
 }
 
-void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel, const double* angvel)
+// The move list after an upload of solid velocities `vel` in which a dummy
+// particle started or stopped moving (the device found it); the moving flags
+// go back to the device.
+void rebuildMoves(demsph_engine* e, const double* vel)
 {
     DeviceState& d = e->d;
-    if (d.ns == 0) return;
-    // dummy particles given a velocity join the integration: the move list
-    // changes only when a dummy particle starts or stops moving
     bool moveChanged = false;
-    if (vel)
-        for (size_t q = 0; q < e->dummyIdx.size(); ++q) {
-            const size_t i = (size_t)e->dummyIdx[q];
-            const unsigned char m = (vel[3 * i] != 0.0 || vel[3 * i + 1] != 0.0 || vel[3 * i + 2] != 0.0) ? 1 : 0;
-            if (m != e->dummyMoving[q]) {
-                e->dummyMoving[q] = m;
-                moveChanged = true;
-            }
+    for (size_t q = 0; q < e->dummyIdx.size(); ++q) {
+        const size_t i = (size_t)e->dummyIdx[q];
+        const unsigned char m = (vel[3 * i] != 0.0 || vel[3 * i + 1] != 0.0 || vel[3 * i + 2] != 0.0) ? 1 : 0;
+        if (m != e->dummyMoving[q]) {
+            e->dummyMoving[q] = m;
+            moveChanged = true;
         }
+    }
     if (moveChanged) {
         std::vector<int> move;
         move.reserve(e->moveHost.size());
@@ -378,6 +377,26 @@ void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel,
             }
         }
     }
+    e->movingDummies = (int)std::count(e->dummyMoving.begin(), e->dummyMoving.end(), (unsigned char)1);
+    if (d.ndummy > 0)
+        CK(cudaMemcpyAsync(d.dummyMoving, e->dummyMoving.data(), d.ndummy, cudaMemcpyHostToDevice, e->stream));
+}
+
+// Raises moveChanged when an uploaded velocity starts or stops a dummy
+// particle's motion.
+__global__ void kDummyMoves(DeviceState d, const double* __restrict__ vel)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= d.ndummy) return;
+    const size_t i = (size_t)d.dummyIdx[q];
+    const unsigned char m = (vel[3 * i] != 0.0 || vel[3 * i + 1] != 0.0 || vel[3 * i + 2] != 0.0) ? 1 : 0;
+    if (m != d.dummyMoving[q]) *(volatile int*)d.moveChanged = 1;
+}
+
+void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel, const double* angvel)
+{
+    DeviceState& d = e->d;
+    if (d.ns == 0) return;
     double* buf = scratchDoubles(e, 9 * (size_t)d.ns);
     double* dp = pos ? buf : nullptr;
     double* dv = vel ? buf + 3 * (size_t)d.ns : nullptr;
@@ -385,6 +404,17 @@ void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel,
     if (dp) CK(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
     if (dw) CK(cudaMemcpyAsync(dw, angvel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
+    // dummy particles given a velocity join the integration: the move list
+    // changes only when one starts or stops moving, which the device finds
+    // (one word read back); the host then rebuilds the list
+    if (dv && d.ndummy > 0) {
+        CK(cudaMemsetAsync(d.moveChanged, 0, sizeof(int), e->stream));
+        ++t_kernelLaunches, kDummyMoves<<<blocksFor(d.ndummy, 256), 256, 0, e->stream>>>(d, dv);
+        int changed = 0;
+        CK(cudaMemcpyAsync(&changed, d.moveChanged, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        if (changed) rebuildMoves(e, vel);
+    }
     // the flag of the step that follows (its list takes the other parity)
     ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw, d.rebuild + (e->par ^ 1));
     // solids that never move are otherwise sorted only once

@@ -221,7 +221,7 @@ struct DeviceState {
     int* fvsc;               // [k * nf + i] solid indices
     int* fvsn;
     float4* fvref;           // per fluid slot: position (from the grid origin) at the rebuild
-    float4* svref;           // per solid (those with a contact row): the same
+    float4* svref;           // per solid (those with a contact row or moved): the same
     float fskin;
     float fhmax;             // largest fluid smoothing length
     int* frebuild;           // 1: fluid candidates are stale (a fluid or solid moved fskin / 2)
@@ -323,6 +323,13 @@ struct DeviceState {
     int* rebuild;            // [p] 1: the candidates are stale for the step whose list has parity p;
                              // set by the drift that ends the step before, cleared after the step
     int* slowMode;           // 1: lists come from the 27-cell walk every step (grid too small, or a solid left the domain)
+    // dummy particles (index order) and whether each is in the move list
+    // (given a velocity): an upload of the solids' velocities compares them on
+    // the device and raises moveChanged when one starts or stops moving
+    int ndummy;
+    int* dummyIdx;
+    unsigned char* dummyMoving;
+    int* moveChanged;
     int* need;               // [0] most contacts of a row, [1] most candidates of a row,
                              // [2] / [3] most fluid / solid candidates of a fluid particle,
                              // [4] most walk candidates of a fluid particle in tile mode (for growing)
@@ -546,17 +553,19 @@ __device__ __forceinline__ int solidOf(const DeviceState& d, int r) { return d.r
 
 // After the last drift of a step: once a solid that can touch others (row >=
 // 0) has moved half the candidate margin since the candidates were built, the
-// next step rebuilds them (stale: that step's flag, d.rebuild[next parity]).
-// c, h: its cell and offset after the drift; p0, q0: vref and svref of the
-// solid.
+// next step rebuilds them (stale: that step's flag, d.rebuild[next parity]);
+// once any moved solid (a dummy particle given a velocity too) has moved half
+// the fluid candidates' margin, the fluid candidates are rebuilt.  c, h: its
+// cell and offset after the drift; p0, q0: vref and svref of the solid.
 __device__ __forceinline__ void checkDisplacementOf(const DeviceState& d, int* stale, int row, int4 c, float4 h,
                                                     float4 p0, float4 q0)
 {
-    if (row < 0) return;
-    const float dx = (float)c.x * d.grid.cs.x + h.x - p0.x, dy = (float)c.y * d.grid.cs.y + h.y - p0.y,
-                dz = (float)c.z * d.grid.cs.z + h.z - p0.z;
-    const float half = 0.5f * d.skin;
-    if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)stale = 1;
+    if (row >= 0) {
+        const float dx = (float)c.x * d.grid.cs.x + h.x - p0.x, dy = (float)c.y * d.grid.cs.y + h.y - p0.y,
+                    dz = (float)c.z * d.grid.cs.z + h.z - p0.z;
+        const float half = 0.5f * d.skin;
+        if (!(dx * dx + dy * dy + dz * dz <= half * half)) *(volatile int*)stale = 1;
+    }
     if (d.nf > 0) {  // the fluid candidates' solid partners
         const float ex = (float)c.x * d.grid.cs.x + h.x - q0.x, ey = (float)c.y * d.grid.cs.y + h.y - q0.y,
                     ez = (float)c.z * d.grid.cs.z + h.z - q0.z;

@@ -830,13 +830,19 @@ __global__ void __launch_bounds__(T) kFluidWalk(DeviceState d, RunIf lists, RunI
     if (!cands.active()) return;
     fluidWalk<L, BUILD_CANDIDATES>(d, cands);
     if (*d.status) return;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < d.nrow; r += gridDim.x * blockDim.x) {
-        const int a = solidOf(d, r);
+    const auto ref = [&](int a) {
         const int4 c = d.scell[a];
         const float4 h = d.sph[a];
         d.svref[a] = make_float4((float)c.x * d.grid.cs.x + h.x, (float)c.y * d.grid.cs.y + h.y,
                                  (float)c.z * d.grid.cs.z + h.z, 0.f);
-    }
+    };
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < d.nrow; r += gridDim.x * blockDim.x) ref(solidOf(d, r));
+    // dummy particles given a velocity move too
+    if (d.ndummy > 0)
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.nmove; k += gridDim.x * blockDim.x) {
+            const int a = d.moveFirst >= 0 ? d.moveFirst + k : d.moveList[k];
+            if (rowOf(d, a) < 0) ref(a);
+        }
 }
 
 void launchFluidWalk(const DeviceState& d, bool walk, cudaStream_t s)

@@ -249,8 +249,10 @@ DEMSPH_API int demsph_update(demsph_engine* e, double dt, int first_step, int n_
    layouts of demsph_upload_fluids / demsph_upload_solids; NULL = keep),
    advances the steps, downloads into the given host arrays (the layouts of
    demsph_download_fluids / demsph_download_solids; NULL = skip), and
-   synchronises once.  A list overflow is handled as in demsph_update (the
-   transfer out follows the completed steps).  No counterpart in the
+   synchronises once at the end (and once after the upload when solid
+   velocities are given in a scene with dummy particles: see
+   demsph_upload_solids).  A list overflow is handled as in demsph_update
+   (the transfer out follows the completed steps).  No counterpart in the
    reference. */
 DEMSPH_API int demsph_update_io(demsph_engine* e, double dt, int first_step, int n_steps, int gap, int use_graph,
                                 const double* fluid_pos_in, const double* fluid_vel_in, const double* fluid_drho_in,
@@ -314,7 +316,11 @@ DEMSPH_API int demsph_download_solids(demsph_engine* e, double* position, double
                            double* normal, double* torque, double* angular_velocity);
 DEMSPH_API int demsph_download_clumps(demsph_engine* e, double* centroid, double* velocity, double* acceleration,
                            double* angular_velocity, double* torque, double* orientation);
-/* Overwrite the dynamic state (inverse of the downloads); NULL skips a field. */
+/* Overwrite the dynamic state (inverse of the downloads); NULL skips a field.
+   A dummy particle given a non-zero velocity is integrated from then on (and
+   no longer once its velocity is zero again): the device compares the
+   uploaded velocities with the dummy particles' current motion and the call
+   waits for that one word before it returns. */
 DEMSPH_API int demsph_upload_fluids(demsph_engine* e, const double* position, const double* velocity, const double* drho);
 DEMSPH_API int demsph_upload_solids(demsph_engine* e, const double* position, const double* velocity,
                          const double* angular_velocity);

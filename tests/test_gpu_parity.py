@@ -547,3 +547,61 @@ def test_tile_and_list_pair_loops_agree(ds, scenes, name, monkeypatch):
     assert np.max(np.linalg.norm(a0 - a1, axis=1) / np.maximum(np.linalg.norm(a1, axis=1), 9.81)) <= FORCE_TOL
     assert np.max(np.abs(r0 - r1)) <= 1e-6 * 1000.0
     assert np.max(np.abs(p0 - p1)) <= 1e-9
+
+
+def test_dummies_given_a_velocity_move_and_stop(ds, scenes):
+    """An upload that gives dummy particles a velocity puts them in the
+    integration (the device finds that their motion changed): they drift by
+    v t while the other dummy particles stay put; an upload that sets the
+    velocity back to zero stops them, through graphs and staged calls alike."""
+    b, sc = ds.build_scene(scenes.tiny_dam_break())
+    moving = np.array([i for i in range(sc.n_solid) if sc.solid_is_dummy[i]][:10])
+    assert len(moving) == 10
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    e = ds.Engine(sc)
+    e.initialize()
+    e.update(dt, 1, 2, gap)
+    s0 = e.download_solids()
+    pos, vel, w = s0["pos"].copy(), s0["vel"].copy(), s0["angvel"].copy()
+    vel[moving] = (0.01, -0.02, 0.0)
+    e.upload_solids(pos, vel, w)
+    e.update(dt, 3, 5, gap, use_graph=True)
+    for s in range(8, 10):
+        e.step(dt, s, gap)
+    s1 = e.download_solids()
+    t = 7 * dt
+    assert np.allclose(s1["pos"][moving], pos[moving] + t * vel[moving], rtol=0, atol=1e-12)
+    others = np.setdiff1d(np.arange(sc.n_solid), moving)
+    assert np.array_equal(s1["pos"][others], pos[others])
+    assert np.allclose(s1["vel"][moving], vel[moving], rtol=1e-14, atol=0)  # kept as double-float
+    vel[moving] = 0.0
+    e.upload_solids(s1["pos"], vel, s1["angvel"])
+    e.update(dt, 10, 4, gap, use_graph=True)
+    s2 = e.download_solids()
+    assert np.array_equal(s2["pos"], s1["pos"])
+
+
+def test_moving_dummies_keep_the_fluid_candidates_fresh(ds, scenes):
+    """The tank's dummy particles given a velocity that carries them past half
+    the fluid candidates' margin within a few steps: the candidates are rebuilt
+    as the walls move, so the fluid forces follow those of the reference's
+    walk every fluid step (fluid_verlet_skin < 0) within a rounding-level
+    bound."""
+    b, sc = ds.build_scene(scenes.tiny_dam_break())
+    dummies = np.array([i for i in range(sc.n_solid) if sc.solid_is_dummy[i]])
+    dt, gap = sc.time_step, sc.fluid_integrate_gap
+    cand, walk = ds.Engine(sc), ds.Engine(sc, fluid_verlet_skin=-1.0)
+    for e in (cand, walk):
+        e.initialize()
+        e.update(dt, 1, 2, gap)
+        s = e.download_solids()
+        vel = s["vel"].copy()
+        vel[dummies] = (2.0, 0.0, 0.0)
+        e.upload_solids(s["pos"], vel, s["angvel"])
+        e.update(dt, 3, 14, gap, use_graph=True)
+    fc, fw = cand.download_fluids(), walk.download_fluids()
+    moved = cand.download_solids()["pos"][dummies, 0] - walk.download_solids()["pos"][dummies, 0]
+    assert np.abs(moved).max() == 0.0
+    scale = max(np.abs(fw[2]).max(), 9.81)
+    assert np.abs(fc[2] - fw[2]).max() <= 1e-4 * scale
+    assert np.abs(fc[0] - fw[0]).max() <= 1e-9
