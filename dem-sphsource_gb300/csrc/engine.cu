@@ -60,15 +60,15 @@ void dropGraph(demsph_engine* e)
     e->rounds.clear();
 }
 
-double* scratchDoubles(demsph_engine* e, size_t n)
+double* scratchDoubles(demsph_engine* e, size_t n, int slot)
 {
-    if (n > e->dscratchN) {
-        void* p = e->dscratch;
+    if (n > e->dscratchN[slot]) {
+        void* p = e->dscratch[slot];
         freeOne(e, p);
-        e->dscratch = dalloc<double>(n, e->owned, e->stream, false);
-        e->dscratchN = n;
+        e->dscratch[slot] = dalloc<double>(n, e->owned, e->stream, false);
+        e->dscratchN[slot] = n;
     }
-    return e->dscratch;
+    return e->dscratch[slot];
 }
 
 // Cell and double-float offset of an absolute FP64 position.  The cell is the
@@ -1502,14 +1502,40 @@ int demsph_update_io(demsph_engine* e, double dt, int first_step, int n_steps, i
     if (gap < 1 || n_steps < 0) return DEMSPH_ERR_ARGUMENT;
     ENGINE_GUARD(e)
     REQUIRE_INIT(e);
-    if (fluid_pos_in || fluid_vel_in || fluid_drho_in) enqueueUploadFluids(e, fluid_pos_in, fluid_vel_in, fluid_drho_in);
-    if (solid_pos_in || solid_vel_in || solid_angvel_in)
-        enqueueUploadSolids(e, solid_pos_in, solid_vel_in, solid_angvel_in);
+    const DeviceState& d = e->d;
+    const bool fIn = fluid_pos_in || fluid_vel_in || fluid_drho_in, sIn = solid_pos_in || solid_vel_in || solid_angvel_in;
+    const bool fOut = fluid_pos_out || fluid_vel_out || fluid_drho_out,
+               sOut = solid_pos_out || solid_vel_out || solid_angvel_out;
+    // the solids' transfers and conversions on the second stream beside the
+    // fluids' (their own staging slot; the conversions touch disjoint arrays),
+    // forked from and joined back into the engine's stream
+    const bool split = d.nf > 0 && d.ns > 0 && ((fIn && sIn) || (fOut && sOut));
+    cudaStream_t ss = split ? e->side : e->stream;
+    const int sslot = split ? 1 : 0;
+    if (split) {  // both slots exist before the fork (they are allocated on the engine's stream)
+        scratchDoubles(e, 10 * (size_t)d.nf, 0);
+        scratchDoubles(e, 18 * (size_t)d.ns, 1);
+    }
+    const auto fork = [&] {
+        if (!split) return;
+        CK(cudaEventRecord(e->forkEv, e->stream));
+        CK(cudaStreamWaitEvent(e->side, e->forkEv, 0));
+    };
+    const auto join = [&] {
+        if (!split) return;
+        CK(cudaEventRecord(e->joinEv, e->side));
+        CK(cudaStreamWaitEvent(e->stream, e->joinEv, 0));
+    };
+    fork();
+    if (fIn) enqueueUploadFluids(e, fluid_pos_in, fluid_vel_in, fluid_drho_in);
+    if (sIn) enqueueUploadSolids(e, solid_pos_in, solid_vel_in, solid_angvel_in, ss, sslot);
+    join();
     const std::function<void()> download = [&] {
-        if (fluid_pos_out || fluid_vel_out || fluid_drho_out)
-            enqueueDownloadFluids(e, fluid_pos_out, fluid_vel_out, nullptr, fluid_drho_out);
-        if (solid_pos_out || solid_vel_out || solid_angvel_out)
-            enqueueDownloadSolids(e, solid_pos_out, solid_vel_out, nullptr, nullptr, nullptr, solid_angvel_out);
+        fork();
+        if (sOut) enqueueDownloadSolids(e, solid_pos_out, solid_vel_out, nullptr, nullptr, nullptr, solid_angvel_out, ss,
+                                        sslot);
+        if (fOut) enqueueDownloadFluids(e, fluid_pos_out, fluid_vel_out, nullptr, fluid_drho_out);
+        join();
     };
     return runUpdate(e, dt, first_step, n_steps, gap, use_graph, &download);
     ENGINE_END(e)

@@ -125,9 +125,11 @@ struct demsph_engine {
         cudaEvent_t a, b;
     };
     std::vector<Timed> timed;
-    // scratch for downloads (device, grown on demand)
-    double* dscratch = nullptr;
-    size_t dscratchN = 0;
+    // staging of FP64 transfers (device, grown on demand): [0] the fluids'
+    // (and every transfer on the engine's stream), [1] the solids' when
+    // demsph_update_io moves them on the second stream
+    double* dscratch[2] = {nullptr, nullptr};
+    size_t dscratchN[2] = {0, 0};
 
     // Exchanges everything two engines hold (device memory, stream, graphs,
     // state), field by field: demsph_append hands the caller's handle the
@@ -178,8 +180,10 @@ struct demsph_engine {
         swap(replayedKernels, o.replayedKernels);
         swap(profiling, o.profiling);
         swap(timed, o.timed);
-        swap(dscratch, o.dscratch);
-        swap(dscratchN, o.dscratchN);
+        swap(dscratch[0], o.dscratch[0]);
+        swap(dscratch[1], o.dscratch[1]);
+        swap(dscratchN[0], o.dscratchN[0]);
+        swap(dscratchN[1], o.dscratchN[1]);
     }
 
     ~demsph_engine()
@@ -223,12 +227,18 @@ void dropGraph(demsph_engine* e);
 int readStatus(demsph_engine* e, int* stepsDone = nullptr);
 // Host transfers of the state enqueued on the engine's stream, without
 // synchronising (engine_io.cu).
-void enqueueDownloadFluids(demsph_engine* e, double* pos, double* vel, double* acc, double* drho);
+// The transfers run on stream s (the engine's stream when null) with staging
+// slot `slot` of scratchDoubles.
+void enqueueDownloadFluids(demsph_engine* e, double* pos, double* vel, double* acc, double* drho,
+                           cudaStream_t s = nullptr, int slot = 0);
 void enqueueDownloadSolids(demsph_engine* e, double* pos, double* vel, double* acc, double* normal, double* torque,
-                           double* angvel);
-void enqueueUploadFluids(demsph_engine* e, const double* pos, const double* vel, const double* drho);
-void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel, const double* angvel);
-double* scratchDoubles(demsph_engine* e, size_t n);
+                           double* angvel, cudaStream_t s = nullptr, int slot = 0);
+void enqueueUploadFluids(demsph_engine* e, const double* pos, const double* vel, const double* drho,
+                         cudaStream_t s = nullptr, int slot = 0);
+void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel, const double* angvel,
+                         cudaStream_t s = nullptr, int slot = 0);
+// Staging slot `slot` with room for n doubles (allocated on the engine's stream).
+double* scratchDoubles(demsph_engine* e, size_t n, int slot = 0);
 void splitPosition(const DeviceState& d, double3 p, int4& c, float4& h, float4& l);
 
 }  // namespace demsph

@@ -288,47 +288,52 @@ namespace demsph {
 // The host transfers of the state, enqueued on the engine's stream (the
 // public calls below add the synchronisation; demsph_update_io enqueues them
 // around its steps and synchronises once).
-void enqueueDownloadFluids(demsph_engine* e, double* pos, double* vel, double* acc, double* drho)
+void enqueueDownloadFluids(demsph_engine* e, double* pos, double* vel, double* acc, double* drho, cudaStream_t s,
+                           int slot)
 {
     DeviceState& d = e->d;
     if (d.nf == 0) return;
+    if (!s) s = e->stream;
     const size_t n = d.nf;
-    double* buf = scratchDoubles(e, 10 * n);
-    ++t_kernelLaunches, kFluidOut<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, buf);
+    double* buf = scratchDoubles(e, 10 * n, slot);
+    ++t_kernelLaunches, kFluidOut<<<blocksFor(d.nf, 256), 256, 0, s>>>(d, buf);
     double* outs[3] = {pos, vel, acc};
     for (int k = 0; k < 3; ++k)
-        if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + 3 * n * k, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
-    if (drho) CK(cudaMemcpyAsync(drho, buf + 9 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+        if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + 3 * n * k, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+    if (drho) CK(cudaMemcpyAsync(drho, buf + 9 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
 }
 
 void enqueueDownloadSolids(demsph_engine* e, double* pos, double* vel, double* acc, double* normal, double* torque,
-                           double* angvel)
+                           double* angvel, cudaStream_t s, int slot)
 {
     DeviceState& d = e->d;
     if (d.ns == 0) return;
+    if (!s) s = e->stream;
     const size_t n3 = 3 * (size_t)d.ns;
-    double* buf = scratchDoubles(e, 6 * n3);
+    double* buf = scratchDoubles(e, 6 * n3, slot);
     double* outs[6] = {pos, vel, acc, normal, torque, angvel};
     unsigned want = 0;
     for (int k = 0; k < 6; ++k)
         if (outs[k]) want |= 1u << k;
-    ++t_kernelLaunches, kSolidOut<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, buf, want);
+    ++t_kernelLaunches, kSolidOut<<<blocksFor(d.ns, 256), 256, 0, s>>>(d, buf, want);
     for (int k = 0; k < 6; ++k)
-        if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + n3 * k, sizeof(double) * n3, cudaMemcpyDeviceToHost, e->stream));
+        if (outs[k]) CK(cudaMemcpyAsync(outs[k], buf + n3 * k, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
 }
 
-void enqueueUploadFluids(demsph_engine* e, const double* pos, const double* vel, const double* drho)
+void enqueueUploadFluids(demsph_engine* e, const double* pos, const double* vel, const double* drho, cudaStream_t s,
+                         int slot)
 {
     DeviceState& d = e->d;
     if (d.nf == 0) return;
-    double* buf = scratchDoubles(e, 7 * (size_t)d.nf);
+    if (!s) s = e->stream;
+    double* buf = scratchDoubles(e, 7 * (size_t)d.nf, slot);
     double* dp = pos ? buf : nullptr;
     double* dv = vel ? buf + 3 * (size_t)d.nf : nullptr;
     double* dr = drho ? buf + 6 * (size_t)d.nf : nullptr;
-    if (dp) CK(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, e->stream));
-    if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, e->stream));
-    if (dr) CK(cudaMemcpyAsync(dr, drho, sizeof(double) * d.nf, cudaMemcpyHostToDevice, e->stream));
-    ++t_kernelLaunches, kFluidIn<<<blocksFor(d.nf, 256), 256, 0, e->stream>>>(d, dp, dv, dr);
+    if (dp) CK(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, s));
+    if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.nf, cudaMemcpyHostToDevice, s));
+    if (dr) CK(cudaMemcpyAsync(dr, drho, sizeof(double) * d.nf, cudaMemcpyHostToDevice, s));
+    ++t_kernelLaunches, kFluidIn<<<blocksFor(d.nf, 256), 256, 0, s>>>(d, dp, dv, dr);
 }
 
 // The move list after an upload of solid velocities `vel` in which a dummy
@@ -393,30 +398,35 @@ __global__ void kDummyMoves(DeviceState d, const double* __restrict__ vel)
     if (m != d.dummyMoving[q]) *(volatile int*)d.moveChanged = 1;
 }
 
-void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel, const double* angvel)
+void enqueueUploadSolids(demsph_engine* e, const double* pos, const double* vel, const double* angvel, cudaStream_t s,
+                         int slot)
 {
     DeviceState& d = e->d;
     if (d.ns == 0) return;
-    double* buf = scratchDoubles(e, 9 * (size_t)d.ns);
+    if (!s) s = e->stream;
+    double* buf = scratchDoubles(e, 9 * (size_t)d.ns, slot);
     double* dp = pos ? buf : nullptr;
     double* dv = vel ? buf + 3 * (size_t)d.ns : nullptr;
     double* dw = angvel ? buf + 6 * (size_t)d.ns : nullptr;
-    if (dp) CK(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
-    if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
-    if (dw) CK(cudaMemcpyAsync(dw, angvel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, e->stream));
+    if (dp) CK(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, s));
+    if (dv) CK(cudaMemcpyAsync(dv, vel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, s));
+    if (dw) CK(cudaMemcpyAsync(dw, angvel, sizeof(double) * 3 * d.ns, cudaMemcpyHostToDevice, s));
     // dummy particles given a velocity join the integration: the move list
     // changes only when one starts or stops moving, which the device finds
     // (one word read back); the host then rebuilds the list
     if (dv && d.ndummy > 0) {
-        CK(cudaMemsetAsync(d.moveChanged, 0, sizeof(int), e->stream));
-        ++t_kernelLaunches, kDummyMoves<<<blocksFor(d.ndummy, 256), 256, 0, e->stream>>>(d, dv);
+        CK(cudaMemsetAsync(d.moveChanged, 0, sizeof(int), s));
+        ++t_kernelLaunches, kDummyMoves<<<blocksFor(d.ndummy, 256), 256, 0, s>>>(d, dv);
         int changed = 0;
-        CK(cudaMemcpyAsync(&changed, d.moveChanged, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
-        CK(cudaStreamSynchronize(e->stream));
-        if (changed) rebuildMoves(e, vel);
+        CK(cudaMemcpyAsync(&changed, d.moveChanged, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (changed) {
+            // the move list goes up on the engine's stream: the solids' stream joins it before the steps
+            rebuildMoves(e, vel);
+        }
     }
     // the flag of the step that follows (its list takes the other parity)
-    ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, e->stream>>>(d, dp, dv, dw, d.rebuild + (e->par ^ 1));
+    ++t_kernelLaunches, kSolidIn<<<blocksFor(d.ns, 256), 256, 0, s>>>(d, dp, dv, dw, d.rebuild + (e->par ^ 1));
     // solids that never move are otherwise sorted only once
     if (dp && e->nMassive == 0) e->solidSortStale = true;
 }
