@@ -413,7 +413,10 @@ __device__ __forceinline__ void solidRowTail(const DeviceState& d, int par, int 
 //
 // Rows hold few contacts and their counts vary: a warp shares its rows'
 // forward contacts out through warpItems, one lane per contact.
-__global__ void __launch_bounds__(T, 6) kPairForces(DeviceState d, int par, float dt, int rowsPerWarp,
+#ifndef DEMSPH_PAIR_FORCE_BLOCKS
+#define DEMSPH_PAIR_FORCE_BLOCKS 6  // resident blocks of T per SM the registers allow
+#endif
+__global__ void __launch_bounds__(T, DEMSPH_PAIR_FORCE_BLOCKS) kPairForces(DeviceState d, int par, float dt, int rowsPerWarp,
                                                     int contactBlocks)
 {
     stepKernelBegin();
