@@ -66,3 +66,21 @@ def test_reference_arm_does_not_load_the_product_library(tmp_path):
     assert r.returncode == 0, r.stderr
     assert "PRODUCT_NOT_LOADED" in r.stdout and "ORACLE_LOADED" in r.stdout, r.stdout
     assert '"impl": "reference"' in r.stdout
+
+
+def test_every_timed_stage_has_algorithmic_bytes():
+    """Each stage the engine times (its TIMED tags) has an algorithmic-bytes
+    formula in bench.py, so the roofline of whichever stage dominates a line
+    is defined (the clump force only where clumps exist is included too)."""
+    import re
+    src = ""
+    for name in ("engine.cu",):
+        with open(os.path.join(ROOT, "dem-sphsource_gb300", "csrc", name)) as f:
+            src += f.read()
+    stages = sorted(set(re.findall(r'TIMED\("([a-z_]+)"\)', src)))
+    assert "continuity" in stages and "pair_forces" in stages and "contact_forces" in stages
+    counts = {"solid_pairs": 10, "n_solid_active": 5, "n_fluid": 7, "bonds": 3, "n_solid": 9, "fluid_partners": 60.0,
+              "fluid_solid_partners": 2.0, "coupling_pairs": 4, "n_pebbles": 2}
+    b = _bench()
+    missing = [s for s in stages if not b.stage_bytes(s, counts)]
+    assert missing == []
